@@ -1,0 +1,157 @@
+/*
+ * basefold_gpu.h — C ABI of the GB300 Basefold prover (libbasefold_gpu.so).
+ *
+ * Drop-in boundary for the Basefold polynomial commitment of han0110/learn-zkp
+ * instantiated as
+ *   Basefold<Polyval, Polyval, BinaryReedSolomonCode<Polyval>,
+ *            Keccak256MerkleTreeMmcs<Polyval>>
+ * behind its `PolyCommitScheme` trait (poly-commit/src/lib.rs:20-51) and the
+ * standalone sumcheck prover (sumcheck/src/lib.rs:56-103).  The reference
+ * exposes Rust traits, not an FFI; each entry point below names the trait
+ * method or function it replaces.  A Rust binding over these symbols is shown
+ * in INTEGRATION.md.
+ *
+ * Conventions
+ *  - Field element: 16 bytes, the raw little-endian u128 that `Polyval`
+ *    stores (Montgomery form, p3/src/polyval.rs:30-34), exactly the bytes
+ *    bincode writes for it.
+ *  - Digest / commitment: 32 bytes (Plonky3 `Hash<Polyval, u8, 32>`).
+ *  - Evaluations: row-major, `width` columns (one multilinear polynomial per
+ *    column, 2^num_vars rows) — the reference's `RowMajorMatrix<F>` Data
+ *    (poly-commit/src/basefold.rs:96-97).  Only width 1 is accepted by this
+ *    build's GPU path.
+ *  - Proofs: the bincode 1.3 bytes of `BasefoldProof` (basefold.rs:49-66).
+ *  - Every call returns 0 on success or a negative BF_ERR_* code; the text of
+ *    the last error on the calling thread is available from bf_last_error.
+ *    bf_verify additionally returns the BF_VERIFY_* results.
+ *  - A bf_pcs and everything made from it belong to one host thread at a
+ *    time; all GPU work runs on the pcs's stream.
+ */
+#ifndef BASEFOLD_GPU_H
+#define BASEFOLD_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BF_OK 0
+#define BF_ERR_ARG (-1)          /* bad argument or size */
+#define BF_ERR_CUDA (-2)         /* CUDA runtime failure */
+#define BF_ERR_OOM (-3)          /* device or pinned allocation failed */
+#define BF_ERR_BUFFER (-4)       /* caller buffer too small; required size returned */
+#define BF_ERR_UNSUPPORTED (-5)  /* configuration this build does not run on the GPU */
+#define BF_ERR_NOT_INVERTIBLE (-6) /* a point coordinate r with r = 0 or r = 1 */
+
+#define BF_VERIFY_OK 0
+#define BF_VERIFY_INVALID_FINAL_POLY 1 /* BasefoldError::InvalidFinalPoly (basefold.rs:79-84) */
+#define BF_VERIFY_INVALID_QUERY 2      /* BasefoldError::InvalidQuery */
+#define BF_VERIFY_MMCS 3               /* BasefoldError::Mmcs */
+#define BF_VERIFY_MALFORMED 4          /* proof bytes do not parse */
+
+typedef struct bf_pcs bf_pcs;
+typedef struct bf_commitment bf_commitment;
+typedef struct bf_challenger bf_challenger;
+
+/* Text of the last error on this thread (NUL-terminated, truncated to len). */
+int bf_last_error(char* buf, size_t len);
+
+/* Library and device facts: number of SMs of the current device, build id. */
+int bf_device_info(int device, int* num_sms, int* cc_major, int* cc_minor);
+
+/* ---- PolyCommitScheme::setup (poly-commit/src/lib.rs:29; basefold.rs:104-110)
+ * with BinaryReedSolomonCode::new(lambda, log2_c, num_vars)
+ * (binary_reed_solomon.rs:20-27).  Builds the additive-NTT twiddle tables of
+ * AddtiveNtt::new(log2_c + num_vars) (p3/src/field/binary.rs:23-53) on the
+ * device.  `stream` is a cudaStream_t to run on, or NULL for a private one.
+ * device < 0 makes a verifier-only object that never touches a GPU (only
+ * bf_verify, bf_pcs_num_queries and bf_pcs_proof_size accept it). */
+int bf_pcs_setup(int device, int lambda, int log2_c, int num_vars, void* stream, bf_pcs** out);
+void bf_pcs_free(bf_pcs* pcs);
+/* RandomFoldableCode::num_queries (binary_reed_solomon.rs:56-59). */
+size_t bf_pcs_num_queries(const bf_pcs* pcs);
+/* Size in bytes of a proof for `width` columns and n_evals (0 or 1) points. */
+size_t bf_pcs_proof_size(const bf_pcs* pcs, size_t width, int n_evals);
+
+/* ---- PolyCommitScheme::commit (lib.rs:31; basefold.rs:112-120): encode
+ * (binary_reed_solomon.rs:67-82) + Merkle commit of the codeword.
+ * `evals` is host memory (2^num_vars * width elements, copied in). */
+int bf_commit(bf_pcs* pcs, const uint8_t* evals, size_t width, bf_commitment** out, uint8_t root[32]);
+/* Same, with `d_evals` already in device memory.  The commitment keeps a
+ * reference to it (no copy): the buffer must outlive the commitment. */
+int bf_commit_device(bf_pcs* pcs, const void* d_evals, size_t width, bf_commitment** out, uint8_t root[32]);
+void bf_commitment_free(bf_commitment* comm);
+/* AsRef<Commitment> of BasefoldCommitmentData (basefold.rs:37-47). */
+int bf_commitment_root(const bf_commitment* comm, uint8_t root[32]);
+/* PolyCommitScheme::data (lib.rs:33): copies the evaluations back to host. */
+int bf_commitment_data(const bf_commitment* comm, uint8_t* evals, size_t cap);
+
+/* ---- PolyCommitScheme::eval (lib.rs:35; basefold.rs:126-131): the value of
+ * every column's multilinear extension at `point` (num_vars elements), on
+ * the device-resident evaluations.  Writes `width` elements. */
+int bf_eval(bf_pcs* pcs, const bf_commitment* comm, const uint8_t* point, uint8_t* values);
+
+/* ---- PolyCommitScheme::open (lib.rs:37-42; basefold.rs:133-232).
+ * n_evals is 0 (empty proof) or 1 (one PolyEvals: `point` of num_vars
+ * elements, `values` of `width` elements).  `ch` is the caller's challenger
+ * state, advanced in place (the reference takes it by value; pass a clone
+ * to keep the original).  Writes the bincode proof; *proof_len receives its
+ * size (also when BF_ERR_BUFFER is returned). */
+int bf_open(bf_pcs* pcs, const bf_commitment* comm, const uint8_t* point, const uint8_t* values, int n_evals,
+            bf_challenger* ch, uint8_t* proof, size_t cap, size_t* proof_len);
+
+/* ---- PolyCommitScheme::verify (lib.rs:44-50; basefold.rs:234-324) on the
+ * host.  Returns BF_VERIFY_* (>= 0) or a negative BF_ERR_*. */
+int bf_verify(const bf_pcs* pcs, const uint8_t root[32], const uint8_t* point, const uint8_t* values, size_t width,
+              int n_evals, bf_challenger* ch, const uint8_t* proof, size_t proof_len);
+
+/* ---- Fiat–Shamir transcript: GenericChallenger<Polyval, Keccak256Hash>
+ * (p3/src/challenger.rs:24-83) over Plonky3's HashChallenger. */
+/* GenericChallenger::new(initial_state) (challenger.rs:36-42); keccak256()
+ * is an empty initial state (challenger.rs:45-49). */
+int bf_challenger_new(const uint8_t* initial_state, size_t len, bf_challenger** out);
+int bf_challenger_clone(const bf_challenger* ch, bf_challenger** out);
+void bf_challenger_free(bf_challenger* ch);
+/* CanObserve<T>::observe of bincode bytes (challenger.rs:51-60). */
+int bf_challenger_observe(bf_challenger* ch, const uint8_t* bytes, size_t len);
+/* CanSample<E>::sample of one field element (challenger.rs:62-74). */
+int bf_challenger_sample_ext(bf_challenger* ch, uint8_t out[16]);
+/* CanSampleBits<usize>::sample_bits (challenger.rs:76-83). */
+int bf_challenger_sample_bits(bf_challenger* ch, int bits, uint64_t* out);
+/* Serialized state: [u64 in_len][input buffer][u64 out_len][output buffer]. */
+int bf_challenger_state(const bf_challenger* ch, uint8_t* buf, size_t cap, size_t* len);
+int bf_challenger_from_state(const uint8_t* buf, size_t len, bf_challenger** out);
+
+/* ---- Standalone sumcheck prover: prove_sumcheck (sumcheck/src/lib.rs:56-79)
+ * of sum_b prod_{j<k} f_j(b).  k = 2 is Quadratic with the single pair
+ * (ONE, 0, 1) (function/quadratic.rs:84-134); k = 3 is this project's
+ * product-of-three extension (compressed round polynomial [c0, c2, c3]).
+ * `polys` holds k arrays of 2^num_vars elements back to back (host memory
+ * for bf_sumcheck_prove, device memory for bf_sumcheck_prove_device, which
+ * does not modify them).  Output: num_vars compressed round polynomials
+ * (k elements each, round num_vars-1 first), then the num_vars challenges,
+ * then the k final evaluations, then the final subclaim. */
+int bf_sumcheck_prove(int device, int k, int num_vars, const uint8_t* polys, const uint8_t* claim,
+                      bf_challenger* ch, uint8_t* out);
+int bf_sumcheck_prove_device(bf_pcs* pcs, int k, int num_vars, const void* d_polys, const uint8_t* claim,
+                             bf_challenger* ch, uint8_t* out);
+
+/* ---- Timing of the kernel classes (CUDA events on the pcs's stream).
+ * When enabled, every launch group is bracketed by events; bf_profile_read
+ * returns accumulated milliseconds and launch counts per class:
+ * 0 encode (NTT passes), 1 codeword leaves, 2 tree levels, 3 folded-codeword
+ * leaves, 4 fold, 5 fix + sumcheck reduction, 6 eq table, 7 query gather. */
+int bf_profile_enable(bf_pcs* pcs, int on);
+int bf_profile_read(bf_pcs* pcs, double* ms, uint64_t* launches, int nclasses);
+
+/* ---- Test hooks: device field products and Keccak-f[1600] permutations on
+ * host buffers (n elements / n states of 25 little-endian lanes). */
+int bf_test_gf_mul(int device, const uint8_t* a, const uint8_t* b, uint8_t* out, size_t n);
+int bf_test_keccak_f(int device, uint64_t* states, size_t n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,334 @@
+"""GB300-native Basefold prover (POLYVAL field, binary Reed–Solomon code,
+Keccak-256 Merkle trees) behind the reference's PolyCommitScheme interface.
+
+Mirrors han0110/learn-zkp:
+  * `Basefold` with setup / commit / data / eval / open / verify
+    (poly-commit/src/lib.rs:20-51, poly-commit/src/basefold.rs:86-325);
+  * `BinaryReedSolomonCode` (poly-commit/src/basefold/code/binary_reed_solomon.rs);
+  * `GenericChallenger.keccak256()` (p3/src/challenger.rs);
+  * `prove_sumcheck` for products of 2 (Quadratic) and 3 multilinear
+    polynomials (sumcheck/src/lib.rs:56-79).
+All computation runs in libbasefold_gpu.so on the GPU; field elements are
+numpy uint8 arrays of shape (n, 16) holding Polyval's raw little-endian value.
+"""
+import ctypes as C
+
+import numpy as np
+
+from ._native import BasefoldGpuError, check, lib  # noqa: F401
+from . import rand  # noqa: F401
+
+__all__ = [
+    "Basefold", "BasefoldConfig", "BinaryReedSolomonCode", "BasefoldError", "BasefoldGpuError", "CommitmentData",
+    "GenericChallenger", "PolyEvals", "prove_sumcheck", "rand",
+]
+
+_u8p = C.c_void_p
+
+
+def _elems(x, n=None) -> np.ndarray:
+    if isinstance(x, (bytes, bytearray)):
+        a = np.frombuffer(bytes(x), dtype=np.uint8)
+    else:
+        a = np.ascontiguousarray(np.asarray(x, dtype=np.uint8))
+    a = a.reshape(-1, 16)
+    if n is not None and a.shape[0] != n:
+        raise ValueError(f"expected {n} field elements, got {a.shape[0]}")
+    return np.ascontiguousarray(a)
+
+
+def _p(a: np.ndarray):
+    return C.c_void_p(a.ctypes.data)
+
+
+class GenericChallenger:
+    """GenericChallenger<Polyval, Keccak256Hash> (p3/src/challenger.rs:24-83)."""
+
+    def __init__(self, initial_state: bytes = b"", _handle=None):
+        if _handle is not None:
+            self._h = _handle
+            return
+        h = C.c_void_p()
+        buf = (C.c_uint8 * max(1, len(initial_state))).from_buffer_copy(bytes(initial_state) or b"\0")
+        check(lib().bf_challenger_new(C.cast(buf, C.c_void_p) if initial_state else None, len(initial_state),
+                                      C.byref(h)))
+        self._h = h
+
+    @classmethod
+    def keccak256(cls) -> "GenericChallenger":
+        return cls(b"")
+
+    @classmethod
+    def from_state(cls, blob: bytes) -> "GenericChallenger":
+        h = C.c_void_p()
+        b = np.frombuffer(bytes(blob), dtype=np.uint8).copy()
+        check(lib().bf_challenger_from_state(_p(b), b.size, C.byref(h)))
+        return cls(_handle=h)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and lib is not None:
+            try:
+                lib().bf_challenger_free(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def clone(self) -> "GenericChallenger":
+        h = C.c_void_p()
+        check(lib().bf_challenger_clone(self._h, C.byref(h)))
+        return GenericChallenger(_handle=h)
+
+    def observe(self, data: bytes) -> None:
+        """CanObserve::observe of already-bincoded bytes (a commitment is its 32 bytes)."""
+        b = np.frombuffer(bytes(data), dtype=np.uint8).copy()
+        check(lib().bf_challenger_observe(self._h, _p(b) if b.size else None, b.size))
+
+    def observe_ext_slice(self, elems) -> None:
+        self.observe(_elems(elems).tobytes())
+
+    def sample_ext_element(self) -> np.ndarray:
+        out = np.zeros(16, dtype=np.uint8)
+        check(lib().bf_challenger_sample_ext(self._h, _p(out)))
+        return out
+
+    def sample_bits(self, bits: int) -> int:
+        v = C.c_uint64()
+        check(lib().bf_challenger_sample_bits(self._h, bits, C.byref(v)))
+        return v.value
+
+    def state(self) -> bytes:
+        n = C.c_size_t()
+        lib().bf_challenger_state(self._h, None, 0, C.byref(n))
+        out = np.zeros(n.value, dtype=np.uint8)
+        check(lib().bf_challenger_state(self._h, _p(out), out.size, C.byref(n)))
+        return out.tobytes()
+
+
+class BinaryReedSolomonCode:
+    """BinaryReedSolomonCode::new(lambda, log2_c, d) (binary_reed_solomon.rs:20-27)."""
+
+    def __init__(self, lambda_: int, log2_c: int, d: int):
+        self.lambda_, self.log2_c, self.d = lambda_, log2_c, d
+
+    def c(self) -> int:
+        return 1 << self.log2_c
+
+    def k_d(self) -> int:
+        return 1 << self.d
+
+    def n_d(self) -> int:
+        return self.c() << self.d
+
+
+class BasefoldConfig:
+    """BasefoldConfig { code, mmcs = keccak256_merkle_tree() } (basefold.rs:31-35)."""
+
+    def __init__(self, code: BinaryReedSolomonCode):
+        self.code = code
+
+
+class PolyEvals:
+    """PolyEvals { values, point } (poly-commit/src/lib.rs:14-18)."""
+
+    def __init__(self, values, point):
+        self.values = _elems(values)
+        self.point = _elems(point) if len(point) else np.zeros((0, 16), np.uint8)
+
+
+class BasefoldError(Exception):
+    """BasefoldError::{InvalidFinalPoly, InvalidQuery, Mmcs} (basefold.rs:79-84), plus Malformed."""
+
+    KINDS = {1: "InvalidFinalPoly", 2: "InvalidQuery", 3: "Mmcs", 4: "Malformed"}
+
+    def __init__(self, code: int):
+        self.code = code
+        self.kind = self.KINDS.get(code, str(code))
+        super().__init__(self.kind)
+
+
+class CommitmentData:
+    """BasefoldCommitmentData: device-resident data, codeword and tree."""
+
+    def __init__(self, pcs, handle, root: bytes, width: int, keep=None):
+        self._pcs, self._h, self.root, self.width, self._keep = pcs, handle, root, width, keep
+
+    def as_ref(self) -> bytes:
+        return self.root
+
+    def free(self):
+        if self._h:
+            lib().bf_commitment_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class _DeviceData:
+    """What `Basefold.data` returns: the commitment's device-resident evaluations."""
+
+    def __init__(self, comm: CommitmentData):
+        self.comm = comm
+
+    def to_host(self) -> np.ndarray:
+        pcs = self.comm._pcs
+        out = np.zeros(((self.comm.width << pcs.config.code.d), 16), dtype=np.uint8)
+        check(lib().bf_commitment_data(self.comm._h, _p(out), out.nbytes))
+        return out
+
+
+class Basefold:
+    """PolyCommitScheme<Polyval, Polyval> for
+    Basefold<Polyval, Polyval, BinaryReedSolomonCode<Polyval>, Keccak256MerkleTreeMmcs<Polyval>>."""
+
+    def __init__(self, handle, config: BasefoldConfig, device: int):
+        self._h, self.config, self.device = handle, config, device
+
+    @classmethod
+    def setup(cls, config: BasefoldConfig, device: int = 0, stream=None) -> "Basefold":
+        h = C.c_void_p()
+        code = config.code
+        check(lib().bf_pcs_setup(device, code.lambda_, code.log2_c, code.d,
+                                 C.c_void_p(stream) if stream else None, C.byref(h)))
+        return cls(h, config, device)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                lib().bf_pcs_free(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def num_queries(self) -> int:
+        return int(lib().bf_pcs_num_queries(self._h))
+
+    def proof_size(self, width: int = 1, n_evals: int = 1) -> int:
+        return int(lib().bf_pcs_proof_size(self._h, width, n_evals))
+
+    def commit(self, data, width: int = 1) -> CommitmentData:
+        """commit (basefold.rs:112-120) of host evaluations (2^d * width elements, row-major)."""
+        d = _elems(data, (width << self.config.code.d))
+        h = C.c_void_p()
+        root = np.zeros(32, dtype=np.uint8)
+        check(lib().bf_commit(self._h, _p(d), width, C.byref(h), _p(root)))
+        return CommitmentData(self, h, root.tobytes(), width)
+
+    def commit_device(self, dev_ptr: int, width: int = 1, keep=None) -> CommitmentData:
+        """commit of evaluations already in device memory (kept by reference, not copied)."""
+        h = C.c_void_p()
+        root = np.zeros(32, dtype=np.uint8)
+        check(lib().bf_commit_device(self._h, C.c_void_p(dev_ptr), width, C.byref(h), _p(root)))
+        return CommitmentData(self, h, root.tobytes(), width, keep=keep)
+
+    def data(self, comm: CommitmentData) -> _DeviceData:
+        return _DeviceData(comm)
+
+    def eval(self, data, point) -> np.ndarray:
+        """eval (basefold.rs:126-131) on `data(comm)` (or the commitment itself)."""
+        comm = data.comm if isinstance(data, _DeviceData) else data
+        if not isinstance(comm, CommitmentData):
+            raise TypeError("eval takes Basefold.data(commitment)")
+        p = _elems(point, self.config.code.d) if self.config.code.d else np.zeros((1, 16), np.uint8)
+        out = np.zeros((comm.width, 16), dtype=np.uint8)
+        check(lib().bf_eval(self._h, comm._h, _p(p), _p(out)))
+        return out
+
+    def open(self, comm: CommitmentData, evals, challenger: GenericChallenger) -> bytes:
+        """open (basefold.rs:133-232); `challenger` is advanced in place (pass a clone)."""
+        if len(evals) > 1:
+            raise ValueError("one evaluation point only (basefold.rs:143-144)")
+        n_evals = len(evals)
+        size = self.proof_size(comm.width, n_evals)
+        out = np.zeros(max(size, 1), dtype=np.uint8)
+        ln = C.c_size_t()
+        if n_evals:
+            pt = evals[0].point if self.config.code.d else np.zeros((1, 16), np.uint8)
+            pt, vals = _elems(pt), _elems(evals[0].values, comm.width)
+            check(lib().bf_open(self._h, comm._h, _p(pt), _p(vals), 1, challenger._h, _p(out), out.size,
+                                C.byref(ln)))
+        else:
+            check(lib().bf_open(self._h, comm._h, None, None, 0, challenger._h, _p(out), out.size, C.byref(ln)))
+        return out[: ln.value].tobytes()
+
+    def verify(self, comm: bytes, evals, proof: bytes, challenger: GenericChallenger) -> None:
+        """verify (basefold.rs:234-324); raises BasefoldError on rejection."""
+        root = np.frombuffer(bytes(comm), dtype=np.uint8).copy()
+        pf = np.frombuffer(bytes(proof), dtype=np.uint8).copy() if proof else np.zeros(1, np.uint8)
+        if evals:
+            pt = evals[0].point if self.config.code.d else np.zeros((1, 16), np.uint8)
+            pt, vals = _elems(pt), _elems(evals[0].values)
+            rc = lib().bf_verify(self._h, _p(root), _p(pt), _p(vals), vals.shape[0], 1, challenger._h, _p(pf),
+                                 len(proof))
+        else:
+            rc = lib().bf_verify(self._h, _p(root), None, None, 1, 0, challenger._h, _p(pf), len(proof))
+        check(rc)
+        if rc != 0:
+            raise BasefoldError(rc)
+
+    # -- standalone sumcheck on device-resident polynomials -------------------
+    def prove_sumcheck_device(self, k: int, num_vars: int, dev_ptr: int, claim, challenger: GenericChallenger):
+        out = np.zeros((num_vars * k + num_vars + k + 1, 16), dtype=np.uint8)
+        c = _elems(claim, 1)
+        check(lib().bf_sumcheck_prove_device(self._h, k, num_vars, C.c_void_p(dev_ptr), _p(c), challenger._h,
+                                             _p(out)))
+        return _split_sumcheck(out, k, num_vars)
+
+    # -- timing of kernel classes -----------------------------------------------
+    PROFILE_CLASSES = ["encode", "leaves", "tree", "pi_leaves", "fold", "fix", "eq", "gather"]
+
+    def profile(self, on: bool = True) -> None:
+        check(lib().bf_profile_enable(self._h, 1 if on else 0))
+
+    def profile_read(self) -> dict:
+        n = len(self.PROFILE_CLASSES)
+        ms = (C.c_double * n)()
+        cnt = (C.c_uint64 * n)()
+        check(lib().bf_profile_read(self._h, ms, cnt, n))
+        return {name: (ms[i], cnt[i]) for i, name in enumerate(self.PROFILE_CLASSES)}
+
+
+def _split_sumcheck(out, k, n):
+    rp = out[: n * k].reshape(n, k, 16)
+    r = out[n * k: n * k + n]
+    fe = out[n * k + n: n * k + n + k]
+    return rp, r, fe, out[-1]
+
+
+def prove_sumcheck(k: int, polys, claim, challenger: GenericChallenger, device: int = 0):
+    """prove_sumcheck (sumcheck/src/lib.rs:56-79) of sum_b prod_{j<k} f_j(b), host input.
+
+    Returns (compressed round polys [n, k, 16], challenges [n, 16],
+    final evaluations [k, 16], final subclaim [16])."""
+    ps = _elems(polys)
+    n = int(ps.shape[0] // k).bit_length() - 1
+    if (k << n) != ps.shape[0]:
+        raise ValueError("polys must hold k arrays of 2^n elements")
+    out = np.zeros((n * k + n + k + 1, 16), dtype=np.uint8)
+    c = _elems(claim, 1)
+    check(lib().bf_sumcheck_prove(device, k, n, _p(ps), _p(c), challenger._h, _p(out)))
+    return _split_sumcheck(out, k, n)
+
+
+def device_info(device: int = 0):
+    sms, ma, mi = C.c_int(), C.c_int(), C.c_int()
+    check(lib().bf_device_info(device, C.byref(sms), C.byref(ma), C.byref(mi)))
+    return {"num_sms": sms.value, "cc": (ma.value, mi.value)}
+
+
+def test_gf_mul(a, b, device: int = 0) -> np.ndarray:
+    a, b = _elems(a), _elems(b)
+    out = np.zeros_like(a)
+    check(lib().bf_test_gf_mul(device, _p(a), _p(b), _p(out), a.shape[0]))
+    return out
+
+
+def test_keccak_f(states, device: int = 0) -> np.ndarray:
+    st = np.ascontiguousarray(states, dtype=np.uint64).copy()
+    check(lib().bf_test_keccak_f(device, st.ctypes.data_as(C.POINTER(C.c_uint64)), st.size // 25))
+    return st

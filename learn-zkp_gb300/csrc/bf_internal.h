@@ -1,0 +1,69 @@
+// Internal interface between the host orchestration (api.cu) and the
+// kernels (kernels.cu).  Not part of the public C ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+
+namespace bf {
+
+constexpr int kMaxStages = 32;
+constexpr int kTwLoBits = 12;  // twiddle(s, K) = lo_s[K & 4095] ^ hi_s[K >> 12]
+
+// Per-stage views of the additive-NTT twiddle tables.  Stage s of
+// AddtiveNtt::new(L) (p3/src/field/binary.rs:23-53) has 2^(L-1-s) entries,
+// entry K being the XOR of the stage's basis values selected by the bits of K.
+// That map is GF(2)-linear in K, so a twiddle is the XOR of one entry of a
+// table over the low 12 bits and one of a table over the remaining bits.
+struct TwiddleView {
+  const uint4* lo[kMaxStages];
+  const uint4* hi[kMaxStages];
+};
+
+// Launchers (all asynchronous on `st`).
+// `tw` points to a TwiddleView in device memory.
+cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t width, const TwiddleView* tw,
+                          cudaStream_t st);
+cudaError_t launch_leaves_elem(const uint4* cw, uint4* leaves, size_t n, size_t width, cudaStream_t st);
+cudaError_t launch_leaves_pair(const uint4* pi, uint4* leaves, size_t n, cudaStream_t st);
+// Build every level above `leaves` (n leaves, power of two); levels are stored
+// one after another right after the leaves.  Root = last digest.
+cudaError_t launch_tree(uint4* leaves, size_t n, cudaStream_t st);
+
+cudaError_t launch_eq_table(const uint4* r, int nvars, uint4* out, uint4* tmp_lo, uint4* tmp_hi, cudaStream_t st);
+cudaError_t launch_dot_xor(const uint4* x, const uint4* y, size_t n, uint32_t* acc, cudaStream_t st);
+cudaError_t launch_fold(const uint4* pi, uint4* out, size_t n_out, const uint4* tw_lo, const uint4* tw_hi, uint4 r,
+                        cudaStream_t st);
+cudaError_t launch_fix(const uint4* in, uint4* out, size_t half, uint4 r, const uint4* heq, size_t next_half,
+                       uint32_t* acc, cudaStream_t st);
+cudaError_t launch_combine_rows(const uint4* rows, size_t nrows, size_t width, const uint4* scalars, uint4* out,
+                                cudaStream_t st);
+
+// Gather of the query openings, written in the proof's bincode layout.
+struct GatherParams {
+  const uint4* cw;         // codeword, NTT order, rows of `width`
+  const uint4* cw_tree;    // codeword tree, reversed storage per level
+  const uint4* pi_first;   // folded codeword of the first round (= cw when width is 1)
+  const uint4* pi_fold;    // folded codewords of rounds d-1 .. 0, one after another
+  const uint4* pi_trees;   // their trees, one after another
+  const uint64_t* idx;     // query positions
+  uint8_t* out;            // Q blocks of `block_bytes`
+  size_t width;
+  size_t block_bytes;
+  int L;        // log2 n_d
+  int d;        // rounds
+  int log2_c;
+  int nq;
+};
+cudaError_t launch_gather(const GatherParams& p, cudaStream_t st);
+
+// Standalone product sumcheck.
+cudaError_t launch_prod_round_sums(const uint4* const* polys, int k, size_t half, uint32_t* acc, cudaStream_t st);
+cudaError_t launch_prod_fix(uint4* const* out, const uint4* const* in, int k, size_t half, uint4 r,
+                            size_t next_half, uint32_t* acc, cudaStream_t st);
+
+// Test hooks.
+cudaError_t launch_test_mul(const uint4* a, const uint4* b, uint4* out, size_t n, cudaStream_t st);
+cudaError_t launch_test_keccak(uint2* states, size_t n, cudaStream_t st);
+
+}  // namespace bf

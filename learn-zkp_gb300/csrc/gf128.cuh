@@ -1,0 +1,110 @@
+// Device arithmetic in the POLYVAL field GF(2^128).
+//
+// An element is the raw 128-bit value that the reference's `Polyval` stores
+// (p3/src/polyval.rs:30-34): bit i is the coefficient of x^i, words are
+// little-endian (x = bits 0-31 ... w = bits 96-127).  Addition is XOR
+// (polyval.rs:183-191).  Multiplication is the Montgomery product
+// a*b*x^-128 mod P with P = x^128 + x^127 + x^126 + x^121 + 1
+// (polyval/portable.rs:20-28), so values stay in the reference's
+// representation with no conversion.
+//
+// The GPU has no carry-less multiply.  The 32x32 carry-less product is taken
+// from ordinary integer products of operands whose bits are spread four
+// apart ("holes"): a product of two such operands has at most 8 terms at any
+// bit position, so its sums never carry into the next position of the same
+// residue class, and masking keeps exactly the XOR of the terms.  The
+// 128x128 product is two levels of Karatsuba over those 32-bit products
+// (9 multiplies of 32 bits), then a two-step reduction that cancels the low
+// 128 bits with multiples of P (x^128 = x^127 + x^126 + x^121 + 1).
+#pragma once
+#include <cstdint>
+
+namespace bf {
+
+__device__ __forceinline__ uint4 gf_add(uint4 a, uint4 b) {
+  return make_uint4(a.x ^ b.x, a.y ^ b.y, a.z ^ b.z, a.w ^ b.w);
+}
+
+__device__ __forceinline__ bool gf_is_zero(uint4 a) { return (a.x | a.y | a.z | a.w) == 0; }
+
+// Carry-less 32 x 32 -> 64.
+__device__ __forceinline__ uint64_t clmul32(uint32_t a, uint32_t b) {
+  const uint32_t m0 = 0x11111111u, m1 = 0x22222222u, m2 = 0x44444444u, m3 = 0x88888888u;
+  const uint32_t a0 = a & m0, a1 = a & m1, a2 = a & m2, a3 = a & m3;
+  const uint32_t b0 = b & m0, b1 = b & m1, b2 = b & m2, b3 = b & m3;
+  const uint64_t z0 = ((uint64_t)a0 * b0) ^ ((uint64_t)a1 * b3) ^ ((uint64_t)a2 * b2) ^ ((uint64_t)a3 * b1);
+  const uint64_t z1 = ((uint64_t)a0 * b1) ^ ((uint64_t)a1 * b0) ^ ((uint64_t)a2 * b3) ^ ((uint64_t)a3 * b2);
+  const uint64_t z2 = ((uint64_t)a0 * b2) ^ ((uint64_t)a1 * b1) ^ ((uint64_t)a2 * b0) ^ ((uint64_t)a3 * b3);
+  const uint64_t z3 = ((uint64_t)a0 * b3) ^ ((uint64_t)a1 * b2) ^ ((uint64_t)a2 * b1) ^ ((uint64_t)a3 * b0);
+  return (z0 & 0x1111111111111111ull) | (z1 & 0x2222222222222222ull) | (z2 & 0x4444444444444444ull) |
+         (z3 & 0x8888888888888888ull);
+}
+
+// Carry-less 64 x 64 -> 128 by one Karatsuba level.
+__device__ __forceinline__ void clmul64(uint64_t a, uint64_t b, uint64_t& lo, uint64_t& hi) {
+  const uint32_t a0 = (uint32_t)a, a1 = (uint32_t)(a >> 32);
+  const uint32_t b0 = (uint32_t)b, b1 = (uint32_t)(b >> 32);
+  const uint64_t p0 = clmul32(a0, b0);
+  const uint64_t p2 = clmul32(a1, b1);
+  const uint64_t p1 = clmul32(a0 ^ a1, b0 ^ b1) ^ p0 ^ p2;
+  lo = p0 ^ (p1 << 32);
+  hi = p2 ^ (p1 >> 32);
+}
+
+// Montgomery product a*b*x^-128 mod P.
+__device__ __forceinline__ uint4 gf_mul(uint4 a, uint4 b) {
+  const uint64_t a0 = ((uint64_t)a.y << 32) | a.x, a1 = ((uint64_t)a.w << 32) | a.z;
+  const uint64_t b0 = ((uint64_t)b.y << 32) | b.x, b1 = ((uint64_t)b.w << 32) | b.z;
+  uint64_t l0, l1, h0, h1, m0, m1;
+  clmul64(a0, b0, l0, l1);
+  clmul64(a1, b1, h0, h1);
+  clmul64(a0 ^ a1, b0 ^ b1, m0, m1);
+  m0 ^= l0 ^ h0;
+  m1 ^= l1 ^ h1;
+  const uint64_t c0 = l0;
+  uint64_t c1 = l1 ^ m0;
+  uint64_t c2 = h0 ^ m1;
+  uint64_t c3 = h1;
+  // cancel bits 0..63:   + c0 * P
+  c1 ^= (c0 << 63) ^ (c0 << 62) ^ (c0 << 57);
+  c2 ^= c0 ^ (c0 >> 1) ^ (c0 >> 2) ^ (c0 >> 7);
+  // cancel bits 64..127: + c1 * x^64 * P
+  c2 ^= (c1 << 63) ^ (c1 << 62) ^ (c1 << 57);
+  c3 ^= c1 ^ (c1 >> 1) ^ (c1 >> 2) ^ (c1 >> 7);
+  return make_uint4((uint32_t)c2, (uint32_t)(c2 >> 32), (uint32_t)c3, (uint32_t)(c3 >> 32));
+}
+
+// XOR-reduce four words across a warp.
+__device__ __forceinline__ uint4 warp_xor(uint4 v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    v.x ^= __shfl_xor_sync(0xffffffffu, v.x, o);
+    v.y ^= __shfl_xor_sync(0xffffffffu, v.y, o);
+    v.z ^= __shfl_xor_sync(0xffffffffu, v.z, o);
+    v.w ^= __shfl_xor_sync(0xffffffffu, v.w, o);
+  }
+  return v;
+}
+
+// XOR-reduce over a block whose size is a multiple of 32 and at most 1024;
+// the result is valid in thread 0.  `scratch` holds 32 elements.
+__device__ __forceinline__ uint4 block_xor(uint4 v, uint4* scratch) {
+  v = warp_xor(v);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) scratch[warp] = v;
+  __syncthreads();
+  const int nw = blockDim.x >> 5;
+  v = (threadIdx.x < nw) ? scratch[threadIdx.x] : make_uint4(0, 0, 0, 0);
+  if (warp == 0) v = warp_xor(v);
+  return v;
+}
+
+// Exact XOR accumulation into a 4-word global accumulator.
+__device__ __forceinline__ void atomic_xor4(uint32_t* acc, uint4 v) {
+  if (v.x) atomicXor(acc + 0, v.x);
+  if (v.y) atomicXor(acc + 1, v.y);
+  if (v.z) atomicXor(acc + 2, v.z);
+  if (v.w) atomicXor(acc + 3, v.w);
+}
+
+}  // namespace bf

@@ -1,0 +1,213 @@
+// Host-side scalar arithmetic of the prover: the POLYVAL field for the
+// per-round sumcheck scalars, Keccak-256 for the Fiat–Shamir transcript and
+// the transcript itself.  Only O(num_vars) scalars and a few hundred bytes
+// per round are handled here; every array of the path stays on the GPU.
+#pragma once
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#include <string>
+
+namespace bfh {
+
+typedef unsigned __int128 u128;
+
+static inline u128 mk(uint64_t lo, uint64_t hi) { return ((u128)hi << 64) | lo; }
+
+// Carry-less 32x32 -> 64 with integer products of operands whose bits are
+// four apart (the same construction as the device multiply).
+static inline uint64_t clmul32(uint32_t a, uint32_t b) {
+  const uint32_t m[4] = {0x11111111u, 0x22222222u, 0x44444444u, 0x88888888u};
+  const uint64_t M[4] = {0x1111111111111111ull, 0x2222222222222222ull, 0x4444444444444444ull,
+                         0x8888888888888888ull};
+  uint64_t a_[4], b_[4], z[4] = {0, 0, 0, 0};
+  for (int i = 0; i < 4; ++i) {
+    a_[i] = a & m[i];
+    b_[i] = b & m[i];
+  }
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) z[(i + j) & 3] ^= a_[i] * b_[j];
+  return (z[0] & M[0]) | (z[1] & M[1]) | (z[2] & M[2]) | (z[3] & M[3]);
+}
+
+static inline void clmul64(uint64_t a, uint64_t b, uint64_t& lo, uint64_t& hi) {
+  uint32_t a0 = (uint32_t)a, a1 = (uint32_t)(a >> 32), b0 = (uint32_t)b, b1 = (uint32_t)(b >> 32);
+  uint64_t p0 = clmul32(a0, b0), p2 = clmul32(a1, b1), p1 = clmul32(a0 ^ a1, b0 ^ b1) ^ p0 ^ p2;
+  lo = p0 ^ (p1 << 32);
+  hi = p2 ^ (p1 >> 32);
+}
+
+// a*b*x^-128 mod x^128 + x^127 + x^126 + x^121 + 1
+static inline u128 mul(u128 a, u128 b) {
+  uint64_t a0 = (uint64_t)a, a1 = (uint64_t)(a >> 64), b0 = (uint64_t)b, b1 = (uint64_t)(b >> 64);
+  uint64_t l0, l1, h0, h1, m0, m1;
+  clmul64(a0, b0, l0, l1);
+  clmul64(a1, b1, h0, h1);
+  clmul64(a0 ^ a1, b0 ^ b1, m0, m1);
+  m0 ^= l0 ^ h0;
+  m1 ^= l1 ^ h1;
+  uint64_t c0 = l0, c1 = l1 ^ m0, c2 = h0 ^ m1, c3 = h1;
+  c1 ^= (c0 << 63) ^ (c0 << 62) ^ (c0 << 57);
+  c2 ^= c0 ^ (c0 >> 1) ^ (c0 >> 2) ^ (c0 >> 7);
+  c2 ^= (c1 << 63) ^ (c1 << 62) ^ (c1 << 57);
+  c3 ^= c1 ^ (c1 >> 1) ^ (c1 >> 2) ^ (c1 >> 7);
+  return mk(c2, c3);
+}
+
+// Montgomery form of 1: x^128 mod P (the reference's Polyval::ONE).
+static inline u128 one() { return mk(1, 0xc200000000000000ull); }
+static inline u128 sq(u128 a) { return mul(a, a); }
+
+// x^(2^128 - 2) = prod_{k=1..127} x^(2^k); zero maps to zero.
+static inline u128 inv(u128 a) {
+  u128 r = one(), p = a;
+  for (int k = 1; k < 128; ++k) {
+    p = sq(p);
+    r = mul(r, p);
+  }
+  return r;
+}
+
+// Inverses of all entries with one field inversion (prefix products).
+// Returns false when an entry is zero.
+static inline bool batch_inverse(const std::vector<u128>& v, std::vector<u128>& out) {
+  size_t n = v.size();
+  out.assign(n, 0);
+  if (n == 0) return true;
+  std::vector<u128> pre(n);
+  u128 acc = one();
+  for (size_t i = 0; i < n; ++i) {
+    if (v[i] == 0) return false;
+    pre[i] = acc;
+    acc = mul(acc, v[i]);
+  }
+  u128 ia = inv(acc);
+  for (size_t i = n; i-- > 0;) {
+    out[i] = mul(ia, pre[i]);
+    ia = mul(ia, v[i]);
+  }
+  return true;
+}
+
+static inline u128 load(const uint8_t* p) {
+  u128 v;
+  std::memcpy(&v, p, 16);
+  return v;
+}
+static inline void store(uint8_t* p, u128 v) { std::memcpy(p, &v, 16); }
+
+// ---- Keccak-256 (FIPS 202 permutation, original Keccak padding 0x01) ----
+static const uint64_t kRC[24] = {
+    0x0000000000000001ull, 0x0000000000008082ull, 0x800000000000808aull, 0x8000000080008000ull,
+    0x000000000000808bull, 0x0000000080000001ull, 0x8000000080008081ull, 0x8000000000008009ull,
+    0x000000000000008aull, 0x0000000000000088ull, 0x0000000080008009ull, 0x000000008000000aull,
+    0x000000008000808bull, 0x800000000000008bull, 0x8000000000008089ull, 0x8000000000008003ull,
+    0x8000000000008002ull, 0x8000000000000080ull, 0x000000000000800aull, 0x800000008000000aull,
+    0x8000000080008081ull, 0x8000000000008080ull, 0x0000000080000001ull, 0x8000000080008008ull};
+static const int kRho[25] = {0, 1, 62, 28, 27, 36, 44, 6, 55, 20, 3, 10, 43, 25, 39, 41, 45, 15, 21, 8, 18, 2, 61, 56, 14};
+
+static inline uint64_t rotl(uint64_t v, int r) { return r ? (v << r) | (v >> (64 - r)) : v; }
+
+static inline void keccak_f(uint64_t A[25]) {
+  for (int ir = 0; ir < 24; ++ir) {
+    uint64_t C[5], B[25];
+    for (int x = 0; x < 5; ++x) C[x] = A[x] ^ A[x + 5] ^ A[x + 10] ^ A[x + 15] ^ A[x + 20];
+    for (int i = 0; i < 25; ++i) A[i] ^= C[(i + 4) % 5] ^ rotl(C[(i + 1) % 5], 1);
+    for (int x = 0; x < 5; ++x)
+      for (int y = 0; y < 5; ++y) B[y + 5 * ((2 * x + 3 * y) % 5)] = rotl(A[x + 5 * y], kRho[x + 5 * y]);
+    for (int y = 0; y < 25; y += 5)
+      for (int x = 0; x < 5; ++x) A[y + x] = B[y + x] ^ (~B[y + (x + 1) % 5] & B[y + (x + 2) % 5]);
+    A[0] ^= kRC[ir];
+  }
+}
+
+static inline void keccak256(const uint8_t* msg, size_t len, uint8_t out[32]) {
+  uint64_t A[25] = {0};
+  const size_t rate = 136;
+  while (len >= rate) {
+    for (int i = 0; i < 17; ++i) {
+      uint64_t v;
+      std::memcpy(&v, msg + 8 * i, 8);
+      A[i] ^= v;
+    }
+    keccak_f(A);
+    msg += rate;
+    len -= rate;
+  }
+  uint8_t block[136] = {0};
+  if (len) std::memcpy(block, msg, len);
+  block[len] ^= 0x01;
+  block[rate - 1] ^= 0x80;
+  for (int i = 0; i < 17; ++i) {
+    uint64_t v;
+    std::memcpy(&v, block + 8 * i, 8);
+    A[i] ^= v;
+  }
+  keccak_f(A);
+  std::memcpy(out, A, 32);
+}
+
+// ---- Fiat–Shamir transcript -----------------------------------------------
+// The reference's GenericChallenger<Polyval, Keccak256Hash>
+// (p3/src/challenger.rs) over Plonky3's HashChallenger<u8, _, 32>:
+// observing appends bytes to the input buffer and empties the output buffer;
+// sampling a byte first (if the output buffer is empty) hashes the input
+// buffer and makes the 32-byte digest both the output and the new input
+// buffer, then pops the LAST output byte.  A field element is 16 popped bytes
+// read little-endian; sample_bits pops 8 bytes as a little-endian usize.
+struct Challenger {
+  std::vector<uint8_t> in, out;
+  void observe(const uint8_t* p, size_t n) {
+    out.clear();
+    in.insert(in.end(), p, p + n);
+  }
+  void observe_elem(u128 v) {
+    uint8_t b[16];
+    store(b, v);
+    observe(b, 16);
+  }
+  uint8_t sample_byte() {
+    if (out.empty()) {
+      uint8_t d[32];
+      keccak256(in.data(), in.size(), d);
+      out.assign(d, d + 32);
+      in.assign(d, d + 32);
+    }
+    uint8_t b = out.back();
+    out.pop_back();
+    return b;
+  }
+  u128 sample_elem() {
+    uint8_t b[16];
+    for (int i = 0; i < 16; ++i) b[i] = sample_byte();
+    return load(b);
+  }
+  uint64_t sample_bits(int bits) {
+    uint64_t v = 0;
+    for (int i = 0; i < 8; ++i) v |= (uint64_t)sample_byte() << (8 * i);
+    return bits >= 64 ? v : (v & (((uint64_t)1 << bits) - 1));
+  }
+  // [u64 in_len][in][u64 out_len][out]
+  std::vector<uint8_t> blob() const {
+    std::vector<uint8_t> b(16 + in.size() + out.size());
+    uint64_t li = in.size(), lo = out.size();
+    std::memcpy(b.data(), &li, 8);
+    if (li) std::memcpy(b.data() + 8, in.data(), li);
+    std::memcpy(b.data() + 8 + li, &lo, 8);
+    if (lo) std::memcpy(b.data() + 16 + li, out.data(), lo);
+    return b;
+  }
+  bool from_blob(const uint8_t* p, size_t n) {
+    if (n < 16) return false;
+    uint64_t li, lo;
+    std::memcpy(&li, p, 8);
+    if (li > n - 16) return false;
+    std::memcpy(&lo, p + 8 + li, 8);
+    if (n != 16 + li + lo) return false;
+    in.assign(p + 8, p + 8 + li);
+    out.assign(p + 16 + li, p + 16 + li + lo);
+    return true;
+  }
+};
+
+}  // namespace bfh

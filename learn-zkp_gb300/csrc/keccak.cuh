@@ -1,0 +1,173 @@
+// Device Keccak-f[1600] and the fixed-length Keccak-256 digests of the
+// Basefold Merkle trees.
+//
+// The reference hashes with Plonky3's Keccak256Hash over tiny-keccak 2.0.2
+// `Keccak::v256` (original Keccak padding: 0x01 after the message, 0x80 in
+// the last byte of the 136-byte rate).  Every message on the hot path fits
+// one block: a codeword leaf is one 16-byte field element, a folded-codeword
+// leaf is two elements (32 bytes), an inner node is left || right (64 bytes)
+// (p3/src/symmetric.rs:11-26, p3/src/merkle_tree.rs:8-21).
+//
+// Lanes are 64-bit words kept as uint2 (x = low 32 bits); every rotation is
+// two funnel shifts.  Constants are FIPS 202's round constants and rho
+// offsets (checked against the spec's LFSR and lane walk by the tests).
+#pragma once
+#include <cstdint>
+
+namespace bf {
+
+__constant__ uint2 c_keccak_rc[24] = {
+    {0x00000001u, 0x00000000u}, {0x00008082u, 0x00000000u}, {0x0000808au, 0x80000000u},
+    {0x80008000u, 0x80000000u}, {0x0000808bu, 0x00000000u}, {0x80000001u, 0x00000000u},
+    {0x80008081u, 0x80000000u}, {0x00008009u, 0x80000000u}, {0x0000008au, 0x00000000u},
+    {0x00000088u, 0x00000000u}, {0x80008009u, 0x00000000u}, {0x8000000au, 0x00000000u},
+    {0x8000808bu, 0x00000000u}, {0x0000008bu, 0x80000000u}, {0x00008089u, 0x80000000u},
+    {0x00008003u, 0x80000000u}, {0x00008002u, 0x80000000u}, {0x00000080u, 0x80000000u},
+    {0x0000800au, 0x00000000u}, {0x8000000au, 0x80000000u}, {0x80008081u, 0x80000000u},
+    {0x00008080u, 0x80000000u}, {0x80000001u, 0x00000000u}, {0x80008008u, 0x80000000u},
+};
+
+__device__ __forceinline__ uint2 kx2(uint2 a, uint2 b) { return make_uint2(a.x ^ b.x, a.y ^ b.y); }
+__device__ __forceinline__ uint2 kx3(uint2 a, uint2 b, uint2 c) {
+  return make_uint2(a.x ^ b.x ^ c.x, a.y ^ b.y ^ c.y);
+}
+__device__ __forceinline__ uint2 kx5(uint2 a, uint2 b, uint2 c, uint2 d, uint2 e) {
+  return make_uint2(a.x ^ b.x ^ c.x ^ d.x ^ e.x, a.y ^ b.y ^ c.y ^ d.y ^ e.y);
+}
+// a ^ (~b & c)
+__device__ __forceinline__ uint2 kchi(uint2 a, uint2 b, uint2 c) {
+  return make_uint2(a.x ^ (~b.x & c.x), a.y ^ (~b.y & c.y));
+}
+template <int R>
+__device__ __forceinline__ uint2 krol(uint2 v) {
+  if constexpr (R == 0) {
+    return v;
+  } else if constexpr (R < 32) {
+    return make_uint2(__funnelshift_l(v.y, v.x, R), __funnelshift_l(v.x, v.y, R));
+  } else if constexpr (R == 32) {
+    return make_uint2(v.y, v.x);
+  } else {
+    return make_uint2(__funnelshift_l(v.x, v.y, R - 32), __funnelshift_l(v.y, v.x, R - 32));
+  }
+}
+
+// One round: theta, rho and pi into b[], chi back into s[], iota.
+__device__ __forceinline__ void keccak_round(uint2 s[25], uint2 rc) {
+  uint2 C[5], D[5], b[25];
+#pragma unroll
+  for (int x = 0; x < 5; ++x) C[x] = kx5(s[x], s[x + 5], s[x + 10], s[x + 15], s[x + 20]);
+#pragma unroll
+  for (int x = 0; x < 5; ++x) D[x] = krol<1>(C[(x + 1) % 5]);
+#pragma unroll
+  for (int i = 0; i < 25; ++i) s[i] = kx3(s[i], C[(i + 4) % 5], D[i % 5]);
+  // b[y + 5 ((2x + 3y) mod 5)] = rot(s[x + 5y], r[x, y])
+  b[0] = s[0];
+  b[10] = krol<1>(s[1]);
+  b[20] = krol<62>(s[2]);
+  b[5] = krol<28>(s[3]);
+  b[15] = krol<27>(s[4]);
+  b[16] = krol<36>(s[5]);
+  b[1] = krol<44>(s[6]);
+  b[11] = krol<6>(s[7]);
+  b[21] = krol<55>(s[8]);
+  b[6] = krol<20>(s[9]);
+  b[7] = krol<3>(s[10]);
+  b[17] = krol<10>(s[11]);
+  b[2] = krol<43>(s[12]);
+  b[12] = krol<25>(s[13]);
+  b[22] = krol<39>(s[14]);
+  b[23] = krol<41>(s[15]);
+  b[8] = krol<45>(s[16]);
+  b[18] = krol<15>(s[17]);
+  b[3] = krol<21>(s[18]);
+  b[13] = krol<8>(s[19]);
+  b[14] = krol<18>(s[20]);
+  b[24] = krol<2>(s[21]);
+  b[9] = krol<61>(s[22]);
+  b[19] = krol<56>(s[23]);
+  b[4] = krol<14>(s[24]);
+#pragma unroll
+  for (int y = 0; y < 25; y += 5) {
+#pragma unroll
+    for (int x = 0; x < 5; ++x) s[y + x] = kchi(b[y + x], b[y + (x + 1) % 5], b[y + (x + 2) % 5]);
+  }
+  s[0] = kx2(s[0], rc);
+}
+
+__device__ __forceinline__ void keccak_f1600(uint2 s[25]) {
+#pragma unroll 2
+  for (int r = 0; r < 24; ++r) keccak_round(s, c_keccak_rc[r]);
+}
+
+// Absorb `nlanes` message lanes (already in s[0..nlanes)), pad and permute.
+// The digest is lanes 0..3 (32 bytes, little-endian).
+__device__ __forceinline__ void keccak256_lanes(uint2 s[25], int nlanes) {
+#pragma unroll
+  for (int i = 0; i < 25; ++i)
+    if (i >= nlanes) s[i] = make_uint2(0, 0);
+  // nlanes <= 16 here, so the 0x01 byte and the final 0x80 byte never share a lane.
+#pragma unroll
+  for (int i = 0; i < 17; ++i)
+    if (i == nlanes) s[i].x ^= 0x01u;
+  s[16].y ^= 0x80000000u;
+  keccak_f1600(s);
+}
+
+struct Digest {
+  uint4 lo, hi;  // bytes 0..15, 16..31
+};
+
+__device__ __forceinline__ Digest digest_from_state(const uint2 s[25]) {
+  Digest d;
+  d.lo = make_uint4(s[0].x, s[0].y, s[1].x, s[1].y);
+  d.hi = make_uint4(s[2].x, s[2].y, s[3].x, s[3].y);
+  return d;
+}
+
+// keccak256 of one 16-byte field element.
+__device__ __forceinline__ Digest hash_elem(uint4 e) {
+  uint2 s[25];
+  s[0] = make_uint2(e.x, e.y);
+  s[1] = make_uint2(e.z, e.w);
+  keccak256_lanes(s, 2);
+  return digest_from_state(s);
+}
+
+// keccak256 of two field elements (32 bytes).
+__device__ __forceinline__ Digest hash_pair(uint4 a, uint4 b) {
+  uint2 s[25];
+  s[0] = make_uint2(a.x, a.y);
+  s[1] = make_uint2(a.z, a.w);
+  s[2] = make_uint2(b.x, b.y);
+  s[3] = make_uint2(b.z, b.w);
+  keccak256_lanes(s, 4);
+  return digest_from_state(s);
+}
+
+// keccak256(left || right), 64 bytes.
+__device__ __forceinline__ Digest hash_node(const Digest& l, const Digest& r) {
+  uint2 s[25];
+  s[0] = make_uint2(l.lo.x, l.lo.y);
+  s[1] = make_uint2(l.lo.z, l.lo.w);
+  s[2] = make_uint2(l.hi.x, l.hi.y);
+  s[3] = make_uint2(l.hi.z, l.hi.w);
+  s[4] = make_uint2(r.lo.x, r.lo.y);
+  s[5] = make_uint2(r.lo.z, r.lo.w);
+  s[6] = make_uint2(r.hi.x, r.hi.y);
+  s[7] = make_uint2(r.hi.z, r.hi.w);
+  keccak256_lanes(s, 8);
+  return digest_from_state(s);
+}
+
+__device__ __forceinline__ Digest load_digest(const uint4* p, size_t i) {
+  Digest d;
+  d.lo = p[2 * i];
+  d.hi = p[2 * i + 1];
+  return d;
+}
+__device__ __forceinline__ void store_digest(uint4* p, size_t i, const Digest& d) {
+  p[2 * i] = d.lo;
+  p[2 * i + 1] = d.hi;
+}
+
+}  // namespace bf

@@ -1,0 +1,568 @@
+// CUDA kernels of the Basefold prover path (sm_103a).
+//
+// Layout conventions shared by every kernel:
+//  * a field element is a uint4 (raw little-endian Montgomery-form u128);
+//  * a digest is two uint4 (32 bytes);
+//  * the codeword of a commitment and every folded codeword of `open` are
+//    kept in additive-NTT output order ("NTT order"): position q holds the
+//    codeword entry at bitrev(q).  The reference materialises the bit
+//    reversal (binary_reed_solomon.rs:80-81); here it is absorbed into
+//    indexing.  In NTT order the folding pair (j, j + n_i) of
+//    binary_reed_solomon.rs:88-96 is the adjacent pair (2t, 2t+1) and its
+//    twiddle is entry t of the stage table with no bit reversal;
+//  * every Merkle level is stored "reversed": node m of a level with 2^h
+//    nodes sits at bitrev_h(m).  Then node s of the next level is
+//    H(prev[s] || prev[s + half]) — both children in the two contiguous
+//    halves of the level below — so every level is one coalesced pass.
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "bf_internal.h"
+#include "gf128.cuh"
+#include "keccak.cuh"
+
+namespace bf {
+
+__device__ __forceinline__ uint32_t brev_bits(uint32_t x, int bits) { return bits ? (__brev(x) >> (32 - bits)) : 0u; }
+__device__ __forceinline__ uint64_t brev_bits64(uint64_t x, int bits) {
+  return bits ? (__brevll(x) >> (64 - bits)) : 0ull;
+}
+
+__device__ __forceinline__ uint4 gf_one() { return make_uint4(1u, 0u, 0u, 0xc2000000u); }
+
+static int g_num_sms = 0;
+static int num_sms() {
+  if (g_num_sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (g_num_sms <= 0) g_num_sms = 1;
+  }
+  return g_num_sms;
+}
+
+static unsigned grid_for(size_t n, int threads, int per_sm = 8) {
+  size_t want = (n + threads - 1) / threads;
+  size_t cap = (size_t)num_sms() * per_sm;
+  if (want > cap) want = cap;
+  if (want == 0) want = 1;
+  return (unsigned)want;
+}
+
+// ---------------------------------------------------------------------------
+// Reed–Solomon encoding (binary_reed_solomon.rs:67-82 with the coset NTTs of
+// binary.rs:55-105).  Codeword = additive NTT of pad(bitrev(m)) over
+// L = n + log2_c bits; its top log2_c layers only replicate m (the padding is
+// zero and every stage table starts with 0), so coset j is a size-2^n NTT of
+// bitrev(m) with stage-s twiddles K = (j << (n-1-s)) | k.
+//
+// One launch runs T consecutive layers [s_lo, s_lo+T) on tiles of 2^T
+// elements held in shared memory: element x = (hi << (s_lo+T)) | (a << s_lo) | u.
+// The first launch reads m directly (bit reversal and replication folded
+// into the load: for fixed u the tile's m-indices are one contiguous run).
+// ---------------------------------------------------------------------------
+struct PassParams {
+  int n, s_lo, T, first;
+};
+
+__global__ void __launch_bounds__(256) ntt_pass_kernel(const uint4* __restrict__ m, uint4* __restrict__ cw,
+                                                      PassParams p, const TwiddleView* __restrict__ tw) {
+  extern __shared__ uint4 sm[];
+  const int n = p.n, T = p.T, s_lo = p.s_lo;
+  const uint32_t tiles_per_coset = 1u << (n - T);
+  const uint32_t j = blockIdx.x >> (n - T);
+  const uint32_t rem = blockIdx.x & (tiles_per_coset - 1);
+  const uint32_t u = rem & ((1u << s_lo) - 1u);
+  const uint32_t hi = rem >> s_lo;
+  const uint32_t tsize = 1u << T;
+  const size_t coset_base = (size_t)j << n;
+
+  if (p.first) {
+    const size_t base = (size_t)brev_bits(u, s_lo) << T;
+    for (uint32_t i = threadIdx.x; i < tsize; i += blockDim.x) sm[brev_bits(i, T)] = m[base + i];
+  } else {
+    for (uint32_t i = threadIdx.x; i < tsize; i += blockDim.x) {
+      const size_t x = ((size_t)hi << (s_lo + T)) | ((size_t)i << s_lo) | u;
+      sm[i] = cw[coset_base + x];
+    }
+  }
+  __syncthreads();
+
+  for (int l = T - 1; l >= 0; --l) {
+    const int s = s_lo + l;
+    const uint4* __restrict__ lo_tab = tw->lo[s];
+    const uint4* __restrict__ hi_tab = tw->hi[s];
+    const uint32_t kbase = (j << (n - 1 - s)) | (hi << (T - 1 - l));
+    const uint32_t lmask = (1u << l) - 1u;
+    for (uint32_t bi = threadIdx.x; bi < (tsize >> 1); bi += blockDim.x) {
+      const uint32_t a = ((bi >> l) << (l + 1)) | (bi & lmask);
+      const uint32_t K = kbase | (bi >> l);
+      const uint4 t = gf_add(lo_tab[K & 4095u], hi_tab[K >> 12]);
+      uint4 x0 = sm[a], x1 = sm[a + (1u << l)];
+      x0 = gf_add(x0, gf_mul(x1, t));  // lo += hi * t
+      x1 = gf_add(x1, x0);             // hi += lo
+      sm[a] = x0;
+      sm[a + (1u << l)] = x1;
+    }
+    __syncthreads();
+  }
+
+  for (uint32_t i = threadIdx.x; i < tsize; i += blockDim.x) {
+    const size_t x = ((size_t)hi << (s_lo + T)) | ((size_t)i << s_lo) | u;
+    cw[coset_base + x] = sm[i];
+  }
+}
+
+// n = 0: every coset is m[0].
+__global__ void replicate_kernel(const uint4* __restrict__ m, uint4* __restrict__ cw, size_t c) {
+  for (size_t i = threadIdx.x; i < c; i += blockDim.x) cw[i] = m[0];
+}
+
+constexpr int kNttMaxT = 12;
+
+cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t width, const TwiddleView* tw,
+                          cudaStream_t st) {
+  if (width != 1) return cudaErrorInvalidValue;
+  const size_t c = (size_t)1 << log2_c;
+  if (n == 0) {
+    replicate_kernel<<<1, 32, 0, st>>>(m, cw, c);
+    return cudaGetLastError();
+  }
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(ntt_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(sizeof(uint4) << kNttMaxT));
+    attr_set = true;
+  }
+  const int passes = (n + kNttMaxT - 1) / kNttMaxT;
+  int top = n;
+  for (int pidx = 0; pidx < passes; ++pidx) {
+    const int remaining = passes - pidx;
+    const int T = (top + remaining - 1) / remaining;  // balanced split, largest first
+    PassParams p;
+    p.n = n;
+    p.T = T;
+    p.s_lo = top - T;
+    p.first = (pidx == 0);
+    const size_t blocks = c << (n - T);
+    ntt_pass_kernel<<<(unsigned)blocks, 256, sizeof(uint4) << T, st>>>(m, cw, p, tw);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    top -= T;
+  }
+  return cudaSuccess;
+}
+
+// ---------------------------------------------------------------------------
+// Merkle trees (Keccak256MerkleTreeMmcs, p3/src/merkle_tree.rs:8-21).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) leaves_elem_kernel(const uint4* __restrict__ cw, uint4* __restrict__ leaves,
+                                                          size_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    store_digest(leaves, i, hash_elem(cw[i]));
+}
+
+// Folded-codeword leaf s = H(pi[2s] || pi[2s+1]): the row (pi[j], pi[j+n_i])
+// of the width-2 matrix committed at basefold.rs:350-355, in NTT order.
+__global__ void __launch_bounds__(128) leaves_pair_kernel(const uint4* __restrict__ pi, uint4* __restrict__ leaves,
+                                                          size_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    store_digest(leaves, i, hash_pair(pi[2 * i], pi[2 * i + 1]));
+}
+
+__global__ void __launch_bounds__(128) level_kernel(const uint4* __restrict__ prev, uint4* __restrict__ next,
+                                                    size_t n_next) {
+  for (size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x; s < n_next; s += (size_t)gridDim.x * blockDim.x)
+    store_digest(next, s, hash_node(load_digest(prev, s), load_digest(prev, s + n_next)));
+}
+
+// The remaining levels of a small tree, in one block.
+__global__ void __launch_bounds__(256) tree_top_kernel(uint4* level, size_t n) {
+  uint4* cur = level;
+  while (n > 1) {
+    const size_t h = n >> 1;
+    uint4* nxt = cur + 2 * n;
+    for (size_t s = threadIdx.x; s < h; s += blockDim.x)
+      store_digest(nxt, s, hash_node(load_digest(cur, s), load_digest(cur, s + h)));
+    __syncthreads();
+    cur = nxt;
+    n = h;
+  }
+}
+
+cudaError_t launch_leaves_elem(const uint4* cw, uint4* leaves, size_t n, size_t width, cudaStream_t st) {
+  if (width != 1) return cudaErrorInvalidValue;
+  leaves_elem_kernel<<<grid_for(n, 128, 16), 128, 0, st>>>(cw, leaves, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_leaves_pair(const uint4* pi, uint4* leaves, size_t n, cudaStream_t st) {
+  leaves_pair_kernel<<<grid_for(n, 128, 16), 128, 0, st>>>(pi, leaves, n);
+  return cudaGetLastError();
+}
+
+constexpr size_t kTopNodes = 512;
+
+cudaError_t launch_tree(uint4* leaves, size_t n, cudaStream_t st) {
+  uint4* cur = leaves;
+  while (n > kTopNodes) {
+    const size_t h = n >> 1;
+    uint4* nxt = cur + 2 * n;
+    level_kernel<<<grid_for(h, 128, 16), 128, 0, st>>>(cur, nxt, h);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    cur = nxt;
+    n = h;
+  }
+  if (n > 1) tree_top_kernel<<<1, 256, 0, st>>>(cur, n);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Sumcheck side of `open` (sumcheck/src/function/eval_impr.rs,
+// p3/src/poly/multilinear.rs).
+// ---------------------------------------------------------------------------
+
+// eq table over nv <= 16 variables in one block (MultiPoly::eq via
+// eq_expand, multilinear.rs:41-64,216-222): bit i of the index <-> r[i].
+__global__ void __launch_bounds__(256) eq_small_kernel(const uint4* __restrict__ r, int nv, uint4* out) {
+  if (threadIdx.x == 0) out[0] = gf_one();
+  __syncthreads();
+  for (int i = 0; i < nv; ++i) {
+    const uint32_t h = 1u << i;
+    const uint4 ri = r[i];
+    for (uint32_t k = threadIdx.x; k < h; k += blockDim.x) {
+      const uint4 lo = out[k];
+      const uint4 hv = gf_mul(lo, ri);
+      out[h + k] = hv;
+      out[k] = gf_add(lo, hv);
+    }
+    __syncthreads();
+  }
+}
+
+// eq(r)[b] = eq(r_lo)[b & mask] * eq(r_hi)[b >> a]
+__global__ void eq_combine_kernel(const uint4* __restrict__ lo, int a, const uint4* __restrict__ hi,
+                                  uint4* __restrict__ out, size_t n) {
+  const size_t mask = ((size_t)1 << a) - 1;
+  for (size_t b = (size_t)blockIdx.x * blockDim.x + threadIdx.x; b < n; b += (size_t)gridDim.x * blockDim.x)
+    out[b] = gf_mul(lo[b & mask], hi[b >> a]);
+}
+
+constexpr int kEqSmall = 12;
+
+cudaError_t launch_eq_table(const uint4* r, int nvars, uint4* out, uint4* tmp_lo, uint4* tmp_hi, cudaStream_t st) {
+  if (nvars <= kEqSmall) {
+    eq_small_kernel<<<1, 256, 0, st>>>(r, nvars, out);
+    return cudaGetLastError();
+  }
+  if (nvars - kEqSmall > 16) return cudaErrorInvalidValue;
+  eq_small_kernel<<<1, 256, 0, st>>>(r, kEqSmall, tmp_lo);
+  eq_small_kernel<<<1, 256, 0, st>>>(r + kEqSmall, nvars - kEqSmall, tmp_hi);
+  const size_t n = (size_t)1 << nvars;
+  eq_combine_kernel<<<grid_for(n, 256), 256, 0, st>>>(tmp_lo, kEqSmall, tmp_hi, out, n);
+  return cudaGetLastError();
+}
+
+// acc ^= sum_i x[i] * y[i]
+__global__ void __launch_bounds__(256) dot_xor_kernel(const uint4* __restrict__ x, const uint4* __restrict__ y,
+                                                      size_t n, uint32_t* acc) {
+  __shared__ uint4 scratch[32];
+  uint4 s = make_uint4(0, 0, 0, 0);
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    s = gf_add(s, gf_mul(x[i], y[i]));
+  s = block_xor(s, scratch);
+  if (threadIdx.x == 0) atomic_xor4(acc, s);
+}
+
+cudaError_t launch_dot_xor(const uint4* x, const uint4* y, size_t n, uint32_t* acc, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  dot_xor_kernel<<<grid_for(n, 256), 256, 0, st>>>(x, y, n, acc);
+  return cudaGetLastError();
+}
+
+// fold + interpolate (binary_reed_solomon.rs:88-109) in NTT order:
+// out[t] = lo' + (hi' - lo') r with hi' = hi + lo, lo' = lo + hi' tw[t].
+__global__ void __launch_bounds__(256) fold_kernel(const uint4* __restrict__ pi, uint4* __restrict__ out,
+                                                   size_t n_out, const uint4* __restrict__ tlo,
+                                                   const uint4* __restrict__ thi, uint4 r) {
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n_out; t += (size_t)gridDim.x * blockDim.x) {
+    const uint4 tw = gf_add(tlo[t & 4095], thi[t >> 12]);
+    uint4 lo = pi[2 * t], hi = pi[2 * t + 1];
+    hi = gf_add(hi, lo);
+    lo = gf_add(lo, gf_mul(hi, tw));
+    out[t] = gf_add(lo, gf_mul(gf_add(hi, lo), r));
+  }
+}
+
+cudaError_t launch_fold(const uint4* pi, uint4* out, size_t n_out, const uint4* tw_lo, const uint4* tw_hi, uint4 r,
+                        cudaStream_t st) {
+  fold_kernel<<<grid_for(n_out, 256), 256, 0, st>>>(pi, out, n_out, tw_lo, tw_hi, r);
+  return cudaGetLastError();
+}
+
+// fix_last_var (multilinear.rs:183-198) fused with the next round's
+// sum_b half_eq[b] * poly_lo[b] (eval_impr.rs:187-197).  In-place safe.
+__global__ void __launch_bounds__(256) fix_kernel(const uint4* in, uint4* out, size_t half, uint4 r,
+                                                  const uint4* __restrict__ heq, size_t next_half, uint32_t* acc) {
+  __shared__ uint4 scratch[32];
+  uint4 s = make_uint4(0, 0, 0, 0);
+  for (size_t b = (size_t)blockIdx.x * blockDim.x + threadIdx.x; b < half; b += (size_t)gridDim.x * blockDim.x) {
+    const uint4 lo = in[b], hi = in[b + half];
+    const uint4 v = gf_add(lo, gf_mul(r, gf_add(hi, lo)));
+    out[b] = v;
+    if (b < next_half) s = gf_add(s, gf_mul(heq[b], v));
+  }
+  if (acc) {
+    s = block_xor(s, scratch);
+    if (threadIdx.x == 0) atomic_xor4(acc, s);
+  }
+}
+
+cudaError_t launch_fix(const uint4* in, uint4* out, size_t half, uint4 r, const uint4* heq, size_t next_half,
+                       uint32_t* acc, cudaStream_t st) {
+  fix_kernel<<<grid_for(half, 256), 256, 0, st>>>(in, out, half, r, heq, next_half, acc);
+  return cudaGetLastError();
+}
+
+// out[row] = sum_c scalars[c] * rows[row * width + c]   (basefold.rs:166-183)
+__global__ void combine_rows_kernel(const uint4* __restrict__ rows, size_t nrows, size_t width,
+                                    const uint4* __restrict__ scalars, uint4* __restrict__ out) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < nrows; i += (size_t)gridDim.x * blockDim.x) {
+    uint4 acc = make_uint4(0, 0, 0, 0);
+    for (size_t c = 0; c < width; ++c) acc = gf_add(acc, gf_mul(scalars[c], rows[i * width + c]));
+    out[i] = acc;
+  }
+}
+
+cudaError_t launch_combine_rows(const uint4* rows, size_t nrows, size_t width, const uint4* scalars, uint4* out,
+                                cudaStream_t st) {
+  combine_rows_kernel<<<grid_for(nrows, 256), 256, 0, st>>>(rows, nrows, width, scalars, out);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Query openings (basefold.rs:200-222 over MerkleTreeMmcs::open_batch),
+// written straight into the proof's bincode layout.  One block per query.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void put_u64(uint8_t* out, size_t off, uint64_t v) {
+  *reinterpret_cast<uint64_t*>(out + off) = v;
+}
+__device__ __forceinline__ void put_elem(uint8_t* out, size_t off, uint4 v) {
+  uint2* p = reinterpret_cast<uint2*>(out + off);
+  p[0] = make_uint2(v.x, v.y);
+  p[1] = make_uint2(v.z, v.w);
+}
+__device__ __forceinline__ void put_digest(uint8_t* out, size_t off, const uint4* tree, size_t i) {
+  put_elem(out, off, tree[2 * i]);
+  put_elem(out, off + 16, tree[2 * i + 1]);
+}
+
+__global__ void gather_kernel(GatherParams p) {
+  const int q = blockIdx.x;
+  const uint64_t idx = p.idx[q];
+  uint8_t* out = p.out + (size_t)q * p.block_bytes;
+  const int L = p.L, d = p.d;
+  const size_t w = p.width;
+  // codeword row + path
+  const uint64_t qpos = brev_bits64(idx, L);
+  if (threadIdx.x == 0) {
+    put_u64(out, 0, w);
+    put_u64(out, 8 + 16 * w, (uint64_t)L);
+  }
+  for (size_t c = threadIdx.x; c < w; c += blockDim.x) put_elem(out, 8 + 16 * c, p.cw[qpos * w + c]);
+  for (int k = threadIdx.x; k < L; k += blockDim.x) {
+    const uint64_t m = (idx >> k) ^ 1ull;
+    const size_t off_k = ((size_t)2 << L) - ((size_t)2 << (L - k));
+    put_digest(out, 16 + 16 * w + 32 * (size_t)k, p.cw_tree, off_k + brev_bits64(m, L - k));
+  }
+  size_t off = 16 + 16 * w + 32 * (size_t)L;
+  if (threadIdx.x == 0) put_u64(out, off, (uint64_t)d);
+  off += 8;
+  const size_t c = (size_t)1 << p.log2_c;
+  for (int k = 0; k < d; ++k) {
+    const int i = d - 1 - k;
+    const int Li = p.log2_c + i + 1;  // log2 of the folded codeword size 2 n_i
+    const uint64_t ni = (uint64_t)1 << (Li - 1);
+    const uint64_t ii = idx & (ni - 1);
+    const uint64_t sib = ((idx >> (Li - 1)) & 1) ^ 1;
+    const uint4* pi;
+    if (k == 0) {
+      pi = p.pi_first;
+    } else {
+      // output of round i+1 sits after the outputs of rounds d-1 .. i+2
+      pi = p.pi_fold + c * (((size_t)1 << d) - ((size_t)1 << (i + 2)));
+    }
+    const size_t tree_off = (c << 1) * (((size_t)1 << d) - ((size_t)1 << (i + 1))) - (size_t)(d - 1 - i);
+    const uint4* tree = p.pi_trees + 2 * tree_off;
+    if (threadIdx.x == 0) {
+      put_elem(out, off, pi[2 * brev_bits64(ii, Li - 1) + sib]);
+      put_u64(out, off + 16, (uint64_t)(Li - 1));
+    }
+    for (int kk = threadIdx.x; kk < Li - 1; kk += blockDim.x) {
+      const uint64_t m = (ii >> kk) ^ 1ull;
+      const size_t loff = ((size_t)1 << Li) - ((size_t)1 << (Li - kk));
+      put_digest(out, off + 24 + 32 * (size_t)kk, tree, loff + brev_bits64(m, Li - 1 - kk));
+    }
+    off += 24 + 32 * (size_t)(Li - 1);
+  }
+}
+
+cudaError_t launch_gather(const GatherParams& p, cudaStream_t st) {
+  if (p.nq == 0) return cudaSuccess;
+  gather_kernel<<<p.nq, 64, 0, st>>>(p);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Standalone product sumcheck (sumcheck/src/function/quadratic.rs:100-128 for
+// two polynomials; the project's product-of-three extension for k = 3).
+// acc[0..3] = c0, acc[4..7] = c2, acc[8..11] = c3.
+// ---------------------------------------------------------------------------
+struct PolyPtrs {
+  const uint4* in[3];
+  uint4* out[3];
+};
+
+template <int K>
+__device__ __forceinline__ void prod_terms(const uint4 lo[K], const uint4 hi[K], uint4& s0, uint4& s2, uint4& s3) {
+  if (K == 2) {
+    s0 = gf_add(s0, gf_mul(lo[0], lo[1]));
+    s2 = gf_add(s2, gf_mul(gf_add(hi[0], lo[0]), gf_add(hi[1], lo[1])));
+  } else {
+    const uint4 b0 = gf_add(hi[0], lo[0]), b1 = gf_add(hi[1], lo[1]), b2 = gf_add(hi[2], lo[2]);
+    const uint4 b12 = gf_mul(b1, b2);
+    s0 = gf_add(s0, gf_mul(lo[0], gf_mul(lo[1], lo[2])));
+    s2 = gf_add(s2, gf_add(gf_mul(b0, gf_add(gf_mul(b1, lo[2]), gf_mul(lo[1], b2))), gf_mul(lo[0], b12)));
+    s3 = gf_add(s3, gf_mul(b0, b12));
+  }
+}
+
+template <int K>
+__global__ void __launch_bounds__(256) prod_sums_kernel(PolyPtrs p, size_t half, uint32_t* acc) {
+  __shared__ uint4 scratch[32];
+  uint4 s0 = make_uint4(0, 0, 0, 0), s2 = s0, s3 = s0;
+  for (size_t b = (size_t)blockIdx.x * blockDim.x + threadIdx.x; b < half; b += (size_t)gridDim.x * blockDim.x) {
+    uint4 lo[K], hi[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      lo[k] = p.in[k][b];
+      hi[k] = p.in[k][b + half];
+    }
+    prod_terms<K>(lo, hi, s0, s2, s3);
+  }
+  s0 = block_xor(s0, scratch);
+  __syncthreads();
+  s2 = block_xor(s2, scratch);
+  __syncthreads();
+  if (K == 3) s3 = block_xor(s3, scratch);
+  if (threadIdx.x == 0) {
+    atomic_xor4(acc, s0);
+    atomic_xor4(acc + 4, s2);
+    if (K == 3) atomic_xor4(acc + 8, s3);
+  }
+}
+
+// Fix the top variable of every polynomial at r and accumulate the next
+// round's sums.  Each thread produces the pair (b, b + half/2) of the fixed
+// polynomials, which is exactly what the next round's sums need.
+template <int K>
+__global__ void __launch_bounds__(256) prod_fix_kernel(PolyPtrs p, size_t half, uint4 r, uint32_t* acc) {
+  __shared__ uint4 scratch[32];
+  uint4 s0 = make_uint4(0, 0, 0, 0), s2 = s0, s3 = s0;
+  const size_t nh = half >> 1;
+  if (nh == 0) {  // last round: one output per polynomial
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        const uint4 lo = p.in[k][0], hi = p.in[k][1];
+        p.out[k][0] = gf_add(lo, gf_mul(r, gf_add(hi, lo)));
+      }
+    }
+    return;
+  }
+  for (size_t b = (size_t)blockIdx.x * blockDim.x + threadIdx.x; b < nh; b += (size_t)gridDim.x * blockDim.x) {
+    uint4 lo[K], hi[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const uint4 a0 = p.in[k][b], a1 = p.in[k][b + half];
+      const uint4 c0 = p.in[k][b + nh], c1 = p.in[k][b + nh + half];
+      lo[k] = gf_add(a0, gf_mul(r, gf_add(a1, a0)));
+      hi[k] = gf_add(c0, gf_mul(r, gf_add(c1, c0)));
+      p.out[k][b] = lo[k];
+      p.out[k][b + nh] = hi[k];
+    }
+    prod_terms<K>(lo, hi, s0, s2, s3);
+  }
+  s0 = block_xor(s0, scratch);
+  __syncthreads();
+  s2 = block_xor(s2, scratch);
+  __syncthreads();
+  if (K == 3) s3 = block_xor(s3, scratch);
+  if (threadIdx.x == 0) {
+    atomic_xor4(acc, s0);
+    atomic_xor4(acc + 4, s2);
+    if (K == 3) atomic_xor4(acc + 8, s3);
+  }
+}
+
+cudaError_t launch_prod_round_sums(const uint4* const* polys, int k, size_t half, uint32_t* acc, cudaStream_t st) {
+  PolyPtrs p{};
+  for (int i = 0; i < k; ++i) p.in[i] = polys[i];
+  if (k == 2)
+    prod_sums_kernel<2><<<grid_for(half, 256), 256, 0, st>>>(p, half, acc);
+  else if (k == 3)
+    prod_sums_kernel<3><<<grid_for(half, 256), 256, 0, st>>>(p, half, acc);
+  else
+    return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_prod_fix(uint4* const* out, const uint4* const* in, int k, size_t half, uint4 r, size_t next_half,
+                            uint32_t* acc, cudaStream_t st) {
+  (void)next_half;
+  PolyPtrs p{};
+  for (int i = 0; i < k; ++i) {
+    p.in[i] = in[i];
+    p.out[i] = out[i];
+  }
+  const size_t work = half > 1 ? half / 2 : 1;
+  if (k == 2)
+    prod_fix_kernel<2><<<grid_for(work, 256), 256, 0, st>>>(p, half, r, acc);
+  else if (k == 3)
+    prod_fix_kernel<3><<<grid_for(work, 256), 256, 0, st>>>(p, half, r, acc);
+  else
+    return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Test hooks: raw field products and Keccak-f permutations.
+// ---------------------------------------------------------------------------
+__global__ void test_mul_kernel(const uint4* a, const uint4* b, uint4* out, size_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = gf_mul(a[i], b[i]);
+}
+
+__global__ void test_keccak_kernel(uint2* states, size_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    uint2 s[25];
+#pragma unroll
+    for (int k = 0; k < 25; ++k) s[k] = states[25 * i + k];
+    keccak_f1600(s);
+#pragma unroll
+    for (int k = 0; k < 25; ++k) states[25 * i + k] = s[k];
+  }
+}
+
+cudaError_t launch_test_mul(const uint4* a, const uint4* b, uint4* out, size_t n, cudaStream_t st) {
+  test_mul_kernel<<<grid_for(n, 256), 256, 0, st>>>(a, b, out, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_test_keccak(uint2* states, size_t n, cudaStream_t st) {
+  test_keccak_kernel<<<grid_for(n, 128), 128, 0, st>>>(states, n);
+  return cudaGetLastError();
+}
+
+}  // namespace bf

@@ -1,0 +1,34 @@
+"""Build recipe for the oracle (test infrastructure only).
+
+Compiles oracle.cpp with the host C++ compiler into oracle/_build/liboracle.so.
+On aarch64 the carry-less multiply uses the PMULL instruction (the analogue of
+the reference's NEON backend, p3/src/polyval/aarch64_neon.rs); elsewhere the
+portable 4-bit-window multiply is used.  Both give identical results.
+"""
+import os
+import platform
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT_DIR = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT_DIR, "liboracle.so")
+
+
+def build(force: bool = False) -> str:
+    src = os.path.join(HERE, "oracle.cpp")
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(src):
+        return LIB
+    os.makedirs(OUT_DIR, exist_ok=True)
+    cxx = os.environ.get("CXX", "g++")
+    flags = ["-O3", "-std=c++17", "-shared", "-fPIC", "-pthread", "-Wall"]
+    if platform.machine() in ("aarch64", "arm64"):
+        flags += ["-march=armv8-a+crypto", "-DORACLE_PMULL"]
+    tmp = LIB + ".tmp"
+    subprocess.check_call([cxx, *flags, src, "-o", tmp])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv))

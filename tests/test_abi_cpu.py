@@ -1,0 +1,98 @@
+"""The C ABI without a GPU: the library loads, exports every declared symbol,
+and its host-side logic (transcript, verifier) matches the oracle."""
+import os
+import re
+
+import numpy as np
+
+from oracle import oracle as O
+from basefold_gpu import rand
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    text = open(os.path.join(ROOT, "include", "basefold_gpu.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(bf_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    from basefold_gpu import _native
+
+    L = _native.lib()
+    decl = declared_symbols()
+    assert len(decl) >= 25
+    for name in decl:
+        assert hasattr(L, name), name
+    assert sorted(_native.EXPORTS) == decl
+
+
+def test_challenger_matches_oracle(built_lib):
+    bg = built_lib
+    ch = bg.GenericChallenger(b"init")
+    blob = O.challenger_blob(b"init")
+    ch.observe(b"\x01" * 32)
+    blob = O.challenger_blob(b"init" + b"\x01" * 32)
+    got = [ch.sample_ext_element() for _ in range(3)]
+    want, blob2 = O.challenger_sample(blob, 3)
+    assert all(np.array_equal(g, w) for g, w in zip(got, want))
+    assert ch.state() == blob2
+    bits = [ch.sample_bits(21) for _ in range(9)]
+    wb, _ = O.challenger_sample(blob2, 9, bits=21)
+    assert bits == [int(x) for x in wb]
+    c2 = bg.GenericChallenger.from_state(ch.state())
+    assert np.array_equal(c2.sample_ext_element(), ch.clone().sample_ext_element())
+
+
+def _setup_verifier(bg, n, log2_c):
+    import ctypes as C
+
+    from basefold_gpu import _native
+
+    h = C.c_void_p()
+    _native.check(_native.lib().bf_pcs_setup(-1, 128, log2_c, n, None, C.byref(h)))
+    return bg.Basefold(h, bg.BasefoldConfig(bg.BinaryReedSolomonCode(128, log2_c, n)), -1)
+
+
+def test_host_verifier_agrees_with_oracle(built_lib):
+    bg = built_lib
+    for log2_c in (0, 1, 2):
+        for n in (0, 1, 3, 7):
+            data = rand.random_elems((1 << n) + n, 77 + n + 13 * log2_c)
+            evals, point = data[: 1 << n], data[1 << n:]
+            root, values, blob = O.harness_prepare(n, log2_c, evals, point)
+            proof = O.open_proof(n, log2_c, evals, point, values, blob)
+            pcs = _setup_verifier(bg, n, log2_c)
+            assert pcs.num_queries() == O.num_queries(log2_c)
+            assert pcs.proof_size(1, 1) == len(proof)
+            pcs.verify(root, [bg.PolyEvals(values, point)], proof, bg.GenericChallenger.from_state(blob))
+            if O.num_queries(log2_c) == 0:
+                continue
+            for pos in (-3, -40, len(proof) // 2, 20):
+                bad = bytearray(proof)
+                bad[pos] ^= 1
+                want = O.verify(n, log2_c, root, point, values, blob, bytes(bad))
+                assert want != 0
+                try:
+                    pcs.verify(root, [bg.PolyEvals(values, point)], bytes(bad), bg.GenericChallenger.from_state(blob))
+                    raise AssertionError("tampered proof accepted")
+                except bg.BasefoldError as e:
+                    assert e.code == want, (n, log2_c, pos, e.kind, want)
+            wrong = values.copy()
+            wrong[0, 0] ^= 1
+            try:
+                pcs.verify(root, [bg.PolyEvals(wrong, point)], proof, bg.GenericChallenger.from_state(blob))
+                raise AssertionError("wrong claim accepted")
+            except bg.BasefoldError as e:
+                assert e.kind in ("InvalidFinalPoly", "Mmcs", "InvalidQuery")
+
+
+def test_gpu_entry_points_refuse_verifier_only_object(built_lib):
+    bg = built_lib
+    pcs = _setup_verifier(bg, 4, 1)
+    try:
+        pcs.commit(rand.random_elems(16, 1))
+        raise AssertionError("commit ran without a device")
+    except bg.BasefoldGpuError as e:
+        assert e.code == -1

@@ -1,0 +1,163 @@
+"""GPU path against the oracle, byte for byte (bit-exact: all arithmetic is
+exact GF(2^128) and Keccak, so the tolerance is zero).  Everything goes
+through the C ABI of libbasefold_gpu.so."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from basefold_gpu import rand
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+ONE = 0xC2000000000000000000000000000001
+
+
+@pytest.fixture(scope="module")
+def bg(built_lib):
+    return built_lib
+
+
+def setup_pcs(bg, n, log2_c):
+    return bg.Basefold.setup(bg.BasefoldConfig(bg.BinaryReedSolomonCode(128, log2_c, n)), device=0)
+
+
+def test_device_is_blackwell(bg):
+    info = bg.device_info(0)
+    assert info["cc"][0] >= 10 and info["num_sms"] > 0
+
+
+def test_gf_mul_matches_oracle(bg):
+    n = 1 << 17
+    a, b = rand.random_elems(n, 1), rand.random_elems(n, 2)
+    edge = O.from_ints([0, 1, ONE, (1 << 128) - 1, 1 << 127, 1 << 64, (1 << 64) - 1, 0x1E563DF92EA7081B4563DF92EA7081B5]
+                       + [1 << i for i in range(0, 128, 7)])
+    ea = np.repeat(edge, len(edge), axis=0)
+    eb = np.tile(edge, (len(edge), 1))
+    a, b = np.concatenate([a, ea]), np.concatenate([b, eb])
+    assert np.array_equal(bg.test_gf_mul(a, b), O.gf_mul(a, b))
+
+
+def test_keccak_f_matches_oracle(bg):
+    st = rand.splitmix64(25 * 1000, seed=9).reshape(1000, 25)
+    got = bg.test_keccak_f(st)
+    for i in range(0, 1000, 97):
+        assert np.array_equal(got[i], O.keccak_f(st[i])), i
+
+
+@pytest.mark.parametrize("log2_c", [0, 1, 2])
+def test_commit_root_matches_oracle(bg, log2_c):
+    for n in list(range(0, 15)) + [17]:
+        evals = rand.random_elems(1 << n, 300 + n + 31 * log2_c)
+        pcs = setup_pcs(bg, n, log2_c)
+        comm = pcs.commit(evals)
+        assert comm.root == O.commit(n, log2_c, evals), (n, log2_c)
+        assert np.array_equal(pcs.data(comm).to_host(), evals)
+
+
+def test_commit_root_large(bg):
+    """2^20 evaluations at blowup 2 and 4: root identical to the oracle's."""
+    for n, log2_c in ((20, 1), (19, 2)):
+        evals = rand.random_elems(1 << n, 4000 + n)
+        pcs = setup_pcs(bg, n, log2_c)
+        assert pcs.commit(evals).root == O.commit(n, log2_c, evals)
+
+
+def harness(bg, n, log2_c, seed):
+    data = rand.random_elems((1 << n) + n, seed)
+    evals, point = data[: 1 << n], data[1 << n:]
+    pcs = setup_pcs(bg, n, log2_c)
+    comm = pcs.commit(evals)
+    ch = bg.GenericChallenger.keccak256()
+    ch.observe(comm.root)
+    values = pcs.eval(pcs.data(comm), point)
+    ch.observe_ext_slice(values)
+    proof = pcs.open(comm, [bg.PolyEvals(values, point)], ch.clone())
+    return pcs, comm, evals, point, values, ch, proof
+
+
+@pytest.mark.parametrize("log2_c", [0, 1, 2])
+def test_open_proof_matches_oracle(bg, log2_c):
+    for n in list(range(0, 12)) + [13]:
+        pcs, comm, evals, point, values, ch, proof = harness(bg, n, log2_c, 500 + n + 17 * log2_c)
+        root_o, values_o, blob = O.harness_prepare(n, log2_c, evals, point)
+        assert comm.root == root_o
+        assert np.array_equal(values, values_o), ("eval", n, log2_c)
+        assert ch.state() == blob
+        proof_o = O.open_proof(n, log2_c, evals, point, values_o, blob)
+        assert len(proof) == len(proof_o), (n, log2_c)
+        assert proof == proof_o, ("proof", n, log2_c)
+        pcs.verify(comm.root, [bg.PolyEvals(values, point)], proof, ch.clone())
+
+
+def test_open_matches_committed_vectors(bg):
+    vec = json.load(open(os.path.join(GOLDEN, "oracle_vectors.json")))
+    for case in vec["basefold"]:
+        n, log2_c, w, seed = case["n"], case["log2_c"], case["width"], case["seed"]
+        if w != 1:
+            continue
+        data = rand.random_elems((w << n) + n, seed)
+        evals, point = data[: w << n], data[w << n:]
+        pcs = setup_pcs(bg, n, log2_c)
+        comm = pcs.commit(evals)
+        assert comm.root.hex() == case["root"]
+        values = pcs.eval(pcs.data(comm), point)
+        assert [bytes(v).hex() for v in values] == case["values"]
+        ch = bg.GenericChallenger.keccak256()
+        ch.observe(comm.root)
+        ch.observe_ext_slice(values)
+        proof = pcs.open(comm, [bg.PolyEvals(values, point)], ch)
+        assert len(proof) == case["proof_len"]
+        assert hashlib.sha256(proof).hexdigest() == case["proof_sha256"]
+
+
+def test_open_large_matches_oracle(bg):
+    n, log2_c = 18, 1
+    pcs, comm, evals, point, values, ch, proof = harness(bg, n, log2_c, 77)
+    root_o, values_o, blob = O.harness_prepare(n, log2_c, evals, point)
+    assert comm.root == root_o and np.array_equal(values, values_o)
+    assert proof == O.open_proof(n, log2_c, evals, point, values_o, blob)
+
+
+def test_open_empty_evals(bg):
+    pcs = setup_pcs(bg, 4, 1)
+    comm = pcs.commit(rand.random_elems(16, 3))
+    assert pcs.open(comm, [], bg.GenericChallenger.keccak256()) == bytes(32)
+
+
+def test_repeated_opens_are_identical(bg):
+    """Workspace reuse across calls leaves no state behind."""
+    pcs, comm, evals, point, values, ch, proof = harness(bg, 9, 1, 21)
+    for _ in range(3):
+        again = pcs.open(comm, [bg.PolyEvals(values, point)], ch.clone())
+        assert again == proof
+
+
+@pytest.mark.parametrize("k", [2, 3])
+def test_sumcheck_matches_oracle(bg, k):
+    for n in list(range(0, 11)) + [14]:
+        polys = rand.random_elems(k << n, 900 + 10 * k + n)
+        claim = rand.random_elems(1, 1900 + n)
+        init = bytes(range(32))
+        got = bg.prove_sumcheck(k, polys, claim, bg.GenericChallenger(init))
+        want = O.sumcheck_prove(k, n, polys, claim, O.challenger_blob(init))
+        for g, w in zip(got, want):
+            assert np.array_equal(g, w), (k, n)
+
+
+@pytest.mark.parametrize("k", [2, 3])
+def test_sumcheck_prover_verifies(bg, k):
+    n = 12
+    polys = rand.random_elems(k << n, 41 + k)
+    P = polys.reshape(k, 1 << n, 16)
+    prod = P[0]
+    for j in range(1, k):
+        prod = O.gf_mul(prod, P[j])
+    claim = np.bitwise_xor.reduce(prod, axis=0)[None]
+    if k == 2:
+        claim = O.gf_mul(claim, O.from_ints([ONE]))
+    rp, r, fe, fc = bg.prove_sumcheck(k, polys, claim, bg.GenericChallenger(b"x"))
+    assert O.sumcheck_verify(k, n, claim, rp, fe, O.challenger_blob(b"x")) == 0
