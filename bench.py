@@ -1,0 +1,341 @@
+#!/usr/bin/env python
+"""Basefold commit+open throughput on GB300.
+
+Workload: the plain single-polynomial prover step of han0110/learn-zkp's
+Basefold over POLYVAL with the binary Reed–Solomon code — commit (encode +
+Keccak-256 Merkle tree), eval at a random point, open (interleaved sumcheck /
+fold rounds + 309 query openings) — for 2^24 evaluations at blowup 2, one
+column, lambda = 128.  Inputs are synthetic (SplitMix64, seed 0).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+One JSON line on stdout (rank 0).  `value` is commit+open per second with the
+evaluations already resident in HBM; `e2e` is the same through the C ABI with
+host buffers (H2D of the evaluations and D2H of the proof inside the timed
+region).  Multi-GPU runs are independent replicas (the path does not shard).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "learn-zkp_gb300"))
+sys.path.insert(0, ROOT)
+
+METRIC = "Basefold commit+open/sec at 2^20-2^24, batched vs plain on GB300; p99 latency"
+UNIT = "commit+open/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--n", type=int, default=24, help="log2 of the number of evaluations")
+    ap.add_argument("--log2-c", type=int, default=1, help="log2 of the blowup")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-only", action="store_true", help="warmup + steps, no JSON extras (for ncu)")
+    return ap.parse_args()
+
+
+def dist_init(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if args.impl == "gb300" else "gloo"
+        if backend == "nccl":
+            import torch
+
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(ws, v, device=None):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device, self.proc = device, None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            time.sleep(0.3)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc:
+            time.sleep(0.1)
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in getattr(self, "lines", []):
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower() in ("active", "1", "yes"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def algorithmic_bytes(n, log2_c):
+    """Minimal compulsory DRAM bytes of one commit+open (width 1): commit
+    (16 + 80c) N, open (112c + 72) N."""
+    N, c = 1 << n, 1 << log2_c
+    return (16 + 80 * c) * N + (112 * c + 72) * N
+
+
+def tree_nodes(n, log2_c):
+    """Inner Merkle nodes hashed per commit+open: codeword tree + folded-codeword trees."""
+    nd = 1 << (n + log2_c)
+    return (nd - 1) + sum(((1 << log2_c) << i) - 1 for i in range(n))
+
+
+def load_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0}, "fallback"
+
+
+def load_traffic():
+    try:
+        return json.load(open(os.path.join(ROOT, "profiles", "level_kernel_traffic.json")))
+    except OSError:
+        return None
+
+
+def cpu_step_oracle(n, log2_c):
+    """One full commit+eval+open of the oracle (C++ restatement of the
+    reference's CPU path) on all host cores; returns seconds."""
+    from oracle import oracle as O
+    from basefold_gpu import rand
+
+    data = rand.random_elems((1 << n) + n, 0)
+    O.set_threads(os.cpu_count() or 1)
+    t = time.perf_counter()
+    O.commit_eval_open(n, log2_c, data[: 1 << n], data[1 << n:])
+    return time.perf_counter() - t
+
+
+def run_reference(args, ws, rank):
+    """The reference arm: the reference's CPU path (Rust) cannot be built here,
+    so its C++ restatement (oracle) is timed on the host cores."""
+    if rank != 0:
+        return
+    from oracle import oracle as O
+
+    O.lib()
+    W, K = min(args.warmup, 1), min(args.steps, 3)  # full-size CPU steps take tens of seconds
+    for _ in range(W):
+        cpu_step_oracle(args.n, args.log2_c)
+    ts = [cpu_step_oracle(args.n, args.log2_c) for _ in range(K)]
+    total = sum(ts)
+    value = K / total
+    cores = os.cpu_count() or 1
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": K,
+        "warmup": W, "ms_per_step": 1e3 * total / K, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "gf2^128+keccak-u64", "data": "synthetic (SplitMix64 seed 0)",
+        "config": workload_config(args),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"full commit+eval+open at 2^{args.n}, {K} steps (warmup {W}); C++ restatement "
+                                   "of the reference CPU path (Rust toolchain absent)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(args):
+    return {"workload": f"plain Basefold commit+eval+open, 2^{args.n} evaluations, blowup {1 << args.log2_c}, "
+                        "width 1, lambda 128, Keccak-256 Merkle",
+            "num_vars": args.n, "log2_c": args.log2_c, "width": 1,
+            "l2": "inputs larger than L2 (evaluations 16*2^n B, codeword+trees several GB)"}
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_init(args)
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        barrier(ws)
+        return
+    import numpy as np
+    import torch
+
+    import basefold_gpu as bg
+
+    torch.cuda.set_device(local)
+    stream = torch.cuda.current_stream()
+    n, log2_c = args.n, args.log2_c
+    pcs = bg.Basefold.setup(bg.BasefoldConfig(bg.BinaryReedSolomonCode(128, log2_c, n)), device=local,
+                            stream=stream.cuda_stream)
+    data = bg.rand.random_elems((1 << n) + n, seed=rank)
+    evals, point = data[: 1 << n], data[1 << n:]
+    dev = torch.from_numpy(evals).to(f"cuda:{local}")
+    host = torch.from_numpy(evals).pin_memory()
+
+    def step_device():
+        comm = pcs.commit_device(dev.data_ptr(), keep=dev)
+        ch = bg.GenericChallenger.keccak256()
+        ch.observe(comm.root)
+        vals = pcs.eval(pcs.data(comm), point)
+        ch.observe_ext_slice(vals)
+        proof = pcs.open(comm, [bg.PolyEvals(vals, point)], ch)
+        comm.free()
+        return proof
+
+    def step_host():
+        comm = pcs.commit(host.numpy())  # H2D of the pinned evaluations inside bf_commit
+        ch = bg.GenericChallenger.keccak256()
+        ch.observe(comm.root)
+        vals = pcs.eval(pcs.data(comm), point)
+        ch.observe_ext_slice(vals)
+        proof = pcs.open(comm, [bg.PolyEvals(vals, point)], ch)  # D2H of the proof inside bf_open
+        comm.free()
+        return proof
+
+    for _ in range(args.warmup):
+        proof = step_device()
+    if args.profile_only:
+        for _ in range(args.steps):
+            step_device()
+        torch.cuda.synchronize()
+        return
+
+    # ---- timed region: device-resident inputs ----------------------------
+    pcs.profile(True)
+    l0 = bg.kernel_launches()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        barrier(ws)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step_device()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        barrier(ws)
+    launches = bg.kernel_launches() - l0
+    prof = pcs.profile_read()
+    pcs.profile(False)
+    ms = max_over_ranks(ws, ev0.elapsed_time(ev1), device=f"cuda:{local}")
+    value = ws * args.steps / (ms / 1e3)
+
+    # ---- timed region: host buffers through the C ABI ----------------------
+    for _ in range(2):
+        step_host()
+    torch.cuda.synchronize()
+    barrier(ws)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        proof = step_host()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(ws)
+    ms_e2e = max_over_ranks(ws, ev0.elapsed_time(ev1), device=f"cuda:{local}")
+    e2e = ws * args.steps / (ms_e2e / 1e3)
+
+    if rank != 0:
+        return
+    Q = pcs.num_queries()
+    d2h = len(proof) + 48 * n + 16
+    h2d = 16 * (1 << n) + 16 * n + 8 * Q
+
+    # roofline of the dominant kernel class (tree levels: Keccak of 64-byte nodes)
+    peaks, peak_kind = load_peaks()
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    tree_ms, tree_launches = prof["tree"]
+    nodes = tree_nodes(n, log2_c) * args.steps
+    alg_bytes_per_launch = 96.0 * nodes / max(tree_launches, 1)
+    avg_launch_s = tree_ms / 1e3 / max(tree_launches, 1)
+    achieved = alg_bytes_per_launch / avg_launch_s / 1e9 if avg_launch_s > 0 else None
+    traffic = None
+    tr = load_traffic()
+    if tr and tr.get("bytes_per_node"):
+        traffic = tr["bytes_per_node"] * nodes / max(tree_launches, 1)
+    total_ms_classes = sum(v[0] for v in prof.values())
+    cpu = None
+    if not args.no_cpu_baseline and ws == 1:
+        t = cpu_step_oracle(n, log2_c)
+        cpu = {"value": 1.0 / t, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": f"one full commit+eval+open at 2^{n} (C++ restatement of the reference CPU path, "
+                         "all host threads; the Rust reference cannot be built here)"}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "gf2^128+keccak-u64", "data": "synthetic (SplitMix64 seed = rank)",
+        "config": workload_config(args),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                     "kernel": "level_kernel+tree_top_kernel (Merkle levels, keccak256 of 64-byte nodes)",
+                     "peak_source": f"{peak_kind} hbm_gbs",
+                     "note": "Keccak-bound (integer pipes), not HBM-bound; see int_pipe"},
+        "int_pipe": {"keccak_perms_per_s": (nodes / (tree_ms / 1e3)) if tree_ms else None,
+                     "kernel_share_of_step": tree_ms / total_ms_classes if total_ms_classes else None},
+        "kernel_ms_per_step": {k: v[0] / args.steps for k, v in prof.items()},
+        "algorithmic_bytes_per_step": algorithmic_bytes(n, log2_c),
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": ms_e2e / args.steps},
+        "clocks": clk.summary(),
+        "gpu_launches": launches,
+        "proof_bytes": len(proof),
+    }
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -58,8 +58,10 @@ typedef struct bf_challenger bf_challenger;
 /* Text of the last error on this thread (NUL-terminated, truncated to len). */
 int bf_last_error(char* buf, size_t len);
 
-/* Library and device facts: number of SMs of the current device, build id. */
+/* Device facts: number of SMs and compute capability. */
 int bf_device_info(int device, int* num_sms, int* cc_major, int* cc_minor);
+/* Number of CUDA kernels this library has launched since it was loaded. */
+int bf_kernel_launches(uint64_t* count);
 
 /* ---- PolyCommitScheme::setup (poly-commit/src/lib.rs:29; basefold.rs:104-110)
  * with BinaryReedSolomonCode::new(lambda, log2_c, num_vars)

@@ -321,6 +321,13 @@ def device_info(device: int = 0):
     return {"num_sms": sms.value, "cc": (ma.value, mi.value)}
 
 
+def kernel_launches() -> int:
+    """Kernels launched by libbasefold_gpu.so since it was loaded."""
+    v = C.c_uint64()
+    check(lib().bf_kernel_launches(C.byref(v)))
+    return v.value
+
+
 def test_gf_mul(a, b, device: int = 0) -> np.ndarray:
     a, b = _elems(a), _elems(b)
     out = np.zeros_like(a)

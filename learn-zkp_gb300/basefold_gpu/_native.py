@@ -11,7 +11,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libbasefold_gpu.so")
 
 # Every symbol declared in include/basefold_gpu.h.
 EXPORTS = [
-    "bf_last_error", "bf_device_info", "bf_pcs_setup", "bf_pcs_free", "bf_pcs_num_queries", "bf_pcs_proof_size",
+    "bf_last_error", "bf_device_info", "bf_kernel_launches", "bf_pcs_setup", "bf_pcs_free", "bf_pcs_num_queries", "bf_pcs_proof_size",
     "bf_commit", "bf_commit_device", "bf_commitment_free", "bf_commitment_root", "bf_commitment_data", "bf_eval",
     "bf_open", "bf_verify", "bf_challenger_new", "bf_challenger_clone", "bf_challenger_free",
     "bf_challenger_observe", "bf_challenger_sample_ext", "bf_challenger_sample_bits", "bf_challenger_state",
@@ -52,6 +52,7 @@ def lib():
     decl = {
         "bf_last_error": ([C.c_char_p, sz], i),
         "bf_device_info": ([i, C.POINTER(i), C.POINTER(i), C.POINTER(i)], i),
+        "bf_kernel_launches": ([C.POINTER(C.c_uint64)], i),
         "bf_pcs_setup": ([i, i, i, i, vp, C.POINTER(vp)], i),
         "bf_pcs_free": ([vp], None),
         "bf_pcs_num_queries": ([vp], sz),

@@ -428,6 +428,12 @@ int bf_last_error(char* buf, size_t len) {
   return BF_OK;
 }
 
+int bf_kernel_launches(uint64_t* count) {
+  if (!count) return fail(BF_ERR_ARG, "null argument");
+  *count = bf::launches_total();
+  return BF_OK;
+}
+
 int bf_device_info(int device, int* num_sms, int* cc_major, int* cc_minor) {
   int n = 0;
   CU(cudaGetDeviceCount(&n));

@@ -62,6 +62,8 @@ cudaError_t launch_prod_round_sums(const uint4* const* polys, int k, size_t half
 cudaError_t launch_prod_fix(uint4* const* out, const uint4* const* in, int k, size_t half, uint4 r,
                             size_t next_half, uint32_t* acc, cudaStream_t st);
 
+unsigned long long launches_total();
+
 // Test hooks.
 cudaError_t launch_test_mul(const uint4* a, const uint4* b, uint4* out, size_t n, cudaStream_t st);
 cudaError_t launch_test_keccak(uint2* states, size_t n, cudaStream_t st);

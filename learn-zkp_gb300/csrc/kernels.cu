@@ -15,6 +15,7 @@
 //    H(prev[s] || prev[s + half]) — both children in the two contiguous
 //    halves of the level below — so every level is one coalesced pass.
 #include <cuda_runtime.h>
+#include <atomic>
 #include <cstdint>
 
 #include "bf_internal.h"
@@ -29,6 +30,11 @@ __device__ __forceinline__ uint64_t brev_bits64(uint64_t x, int bits) {
 }
 
 __device__ __forceinline__ uint4 gf_one() { return make_uint4(1u, 0u, 0u, 0xc2000000u); }
+
+// Number of kernels this library has launched (all devices, all streams).
+static std::atomic<unsigned long long> g_launches{0};
+unsigned long long launches_total() { return g_launches.load(); }
+#define COUNT_LAUNCH() g_launches.fetch_add(1, std::memory_order_relaxed)
 
 static int g_num_sms = 0;
 static int num_sms() {
@@ -126,6 +132,7 @@ cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t w
   const size_t c = (size_t)1 << log2_c;
   if (n == 0) {
     replicate_kernel<<<1, 32, 0, st>>>(m, cw, c);
+    COUNT_LAUNCH();
     return cudaGetLastError();
   }
   static bool attr_set = false;
@@ -146,6 +153,7 @@ cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t w
     p.first = (pidx == 0);
     const size_t blocks = c << (n - T);
     ntt_pass_kernel<<<(unsigned)blocks, 256, sizeof(uint4) << T, st>>>(m, cw, p, tw);
+    COUNT_LAUNCH();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     top -= T;
@@ -193,11 +201,13 @@ __global__ void __launch_bounds__(256) tree_top_kernel(uint4* level, size_t n) {
 cudaError_t launch_leaves_elem(const uint4* cw, uint4* leaves, size_t n, size_t width, cudaStream_t st) {
   if (width != 1) return cudaErrorInvalidValue;
   leaves_elem_kernel<<<grid_for(n, 128, 16), 128, 0, st>>>(cw, leaves, n);
+  COUNT_LAUNCH();
   return cudaGetLastError();
 }
 
 cudaError_t launch_leaves_pair(const uint4* pi, uint4* leaves, size_t n, cudaStream_t st) {
   leaves_pair_kernel<<<grid_for(n, 128, 16), 128, 0, st>>>(pi, leaves, n);
+  COUNT_LAUNCH();
   return cudaGetLastError();
 }
 
@@ -209,12 +219,16 @@ cudaError_t launch_tree(uint4* leaves, size_t n, cudaStream_t st) {
     const size_t h = n >> 1;
     uint4* nxt = cur + 2 * n;
     level_kernel<<<grid_for(h, 128, 16), 128, 0, st>>>(cur, nxt, h);
+    COUNT_LAUNCH();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     cur = nxt;
     n = h;
   }
-  if (n > 1) tree_top_kernel<<<1, 256, 0, st>>>(cur, n);
+  if (n > 1) {
+    tree_top_kernel<<<1, 256, 0, st>>>(cur, n);
+    COUNT_LAUNCH();
+  }
   return cudaGetLastError();
 }
 
@@ -254,13 +268,17 @@ constexpr int kEqSmall = 12;
 cudaError_t launch_eq_table(const uint4* r, int nvars, uint4* out, uint4* tmp_lo, uint4* tmp_hi, cudaStream_t st) {
   if (nvars <= kEqSmall) {
     eq_small_kernel<<<1, 256, 0, st>>>(r, nvars, out);
+    COUNT_LAUNCH();
     return cudaGetLastError();
   }
   if (nvars - kEqSmall > 16) return cudaErrorInvalidValue;
   eq_small_kernel<<<1, 256, 0, st>>>(r, kEqSmall, tmp_lo);
+  COUNT_LAUNCH();
   eq_small_kernel<<<1, 256, 0, st>>>(r + kEqSmall, nvars - kEqSmall, tmp_hi);
+  COUNT_LAUNCH();
   const size_t n = (size_t)1 << nvars;
   eq_combine_kernel<<<grid_for(n, 256), 256, 0, st>>>(tmp_lo, kEqSmall, tmp_hi, out, n);
+  COUNT_LAUNCH();
   return cudaGetLastError();
 }
 
@@ -278,6 +296,7 @@ __global__ void __launch_bounds__(256) dot_xor_kernel(const uint4* __restrict__ 
 cudaError_t launch_dot_xor(const uint4* x, const uint4* y, size_t n, uint32_t* acc, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   dot_xor_kernel<<<grid_for(n, 256), 256, 0, st>>>(x, y, n, acc);
+  COUNT_LAUNCH();
   return cudaGetLastError();
 }
 
@@ -298,6 +317,7 @@ __global__ void __launch_bounds__(256) fold_kernel(const uint4* __restrict__ pi,
 cudaError_t launch_fold(const uint4* pi, uint4* out, size_t n_out, const uint4* tw_lo, const uint4* tw_hi, uint4 r,
                         cudaStream_t st) {
   fold_kernel<<<grid_for(n_out, 256), 256, 0, st>>>(pi, out, n_out, tw_lo, tw_hi, r);
+  COUNT_LAUNCH();
   return cudaGetLastError();
 }
 
@@ -322,6 +342,7 @@ __global__ void __launch_bounds__(256) fix_kernel(const uint4* in, uint4* out, s
 cudaError_t launch_fix(const uint4* in, uint4* out, size_t half, uint4 r, const uint4* heq, size_t next_half,
                        uint32_t* acc, cudaStream_t st) {
   fix_kernel<<<grid_for(half, 256), 256, 0, st>>>(in, out, half, r, heq, next_half, acc);
+  COUNT_LAUNCH();
   return cudaGetLastError();
 }
 
@@ -338,6 +359,7 @@ __global__ void combine_rows_kernel(const uint4* __restrict__ rows, size_t nrows
 cudaError_t launch_combine_rows(const uint4* rows, size_t nrows, size_t width, const uint4* scalars, uint4* out,
                                 cudaStream_t st) {
   combine_rows_kernel<<<grid_for(nrows, 256), 256, 0, st>>>(rows, nrows, width, scalars, out);
+  COUNT_LAUNCH();
   return cudaGetLastError();
 }
 
@@ -411,6 +433,7 @@ __global__ void gather_kernel(GatherParams p) {
 cudaError_t launch_gather(const GatherParams& p, cudaStream_t st) {
   if (p.nq == 0) return cudaSuccess;
   gather_kernel<<<p.nq, 64, 0, st>>>(p);
+  COUNT_LAUNCH();
   return cudaGetLastError();
 }
 
@@ -515,6 +538,7 @@ cudaError_t launch_prod_round_sums(const uint4* const* polys, int k, size_t half
     prod_sums_kernel<3><<<grid_for(half, 256), 256, 0, st>>>(p, half, acc);
   else
     return cudaErrorInvalidValue;
+  COUNT_LAUNCH();
   return cudaGetLastError();
 }
 
@@ -533,6 +557,7 @@ cudaError_t launch_prod_fix(uint4* const* out, const uint4* const* in, int k, si
     prod_fix_kernel<3><<<grid_for(work, 256), 256, 0, st>>>(p, half, r, acc);
   else
     return cudaErrorInvalidValue;
+  COUNT_LAUNCH();
   return cudaGetLastError();
 }
 
@@ -557,11 +582,13 @@ __global__ void test_keccak_kernel(uint2* states, size_t n) {
 
 cudaError_t launch_test_mul(const uint4* a, const uint4* b, uint4* out, size_t n, cudaStream_t st) {
   test_mul_kernel<<<grid_for(n, 256), 256, 0, st>>>(a, b, out, n);
+  COUNT_LAUNCH();
   return cudaGetLastError();
 }
 
 cudaError_t launch_test_keccak(uint2* states, size_t n, cudaStream_t st) {
   test_keccak_kernel<<<grid_for(n, 128), 128, 0, st>>>(states, n);
+  COUNT_LAUNCH();
   return cudaGetLastError();
 }
 

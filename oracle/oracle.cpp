@@ -205,56 +205,62 @@ static inline void store(uint8_t* p, u128 v) { std::memcpy(p, &v, 16); }
 // used by tiny-keccak 2.0.2 `Keccak::v256`, reached through Plonky3's
 // Keccak256Hash).
 // ---------------------------------------------------------------------------
-static uint64_t g_rc[24];
-static int g_rho[25];
-static bool g_keccak_init = false;
+struct KeccakTables {
+  uint64_t rc[24];
+  int rho[25];
+};
 
-static int lfsr_rc(int t) {
-  if (t % 255 == 0) return 1;
-  unsigned R = 0x01;  // R[0] = 1 (bit i of R is R[i])
-  for (int i = 1; i <= t % 255; ++i) {
-    unsigned r8 = (R >> 7) & 1;  // R[8] after the shift is the old R[7]
-    R = (R << 1) & 0xff;
-    if (r8) R ^= 0x71;  // R[0], R[4], R[5], R[6] ^= R[8]
-  }
-  return R & 1;
-}
-
-static void keccak_init() {
-  if (g_keccak_init) return;
+// Round constants from the rc(t) LFSR of FIPS 202 section 3.2.5 and rho
+// offsets from the (x, y) walk of section 3.2.2, evaluated at compile time.
+static constexpr KeccakTables make_keccak_tables() {
+  KeccakTables t{};
   for (int ir = 0; ir < 24; ++ir) {
     uint64_t rc = 0;
-    for (int j = 0; j <= 6; ++j)
-      if (lfsr_rc(j + 7 * ir)) rc |= (uint64_t)1 << ((1u << j) - 1);
-    g_rc[ir] = rc;
+    for (int j = 0; j <= 6; ++j) {
+      int tt = (j + 7 * ir) % 255;
+      unsigned R = 0x01;
+      for (int i = 1; i <= tt; ++i) {
+        unsigned r8 = (R >> 7) & 1;
+        R = (R << 1) & 0xff;
+        if (r8) R ^= 0x71;  // R[0], R[4], R[5], R[6] ^= R[8]
+      }
+      if (R & 1) rc |= (uint64_t)1 << ((1u << j) - 1);
+    }
+    t.rc[ir] = rc;
   }
-  g_rho[0] = 0;
+  t.rho[0] = 0;
   int x = 1, y = 0;
-  for (int t = 0; t < 24; ++t) {
-    g_rho[x + 5 * y] = ((t + 1) * (t + 2) / 2) % 64;
+  for (int s = 0; s < 24; ++s) {
+    t.rho[x + 5 * y] = ((s + 1) * (s + 2) / 2) % 64;
     int nx = y, ny = (2 * x + 3 * y) % 5;
     x = nx;
     y = ny;
   }
-  g_keccak_init = true;
+  return t;
 }
+static constexpr KeccakTables KT = make_keccak_tables();
 
 static inline uint64_t rotl(uint64_t v, int r) { return r ? (v << r) | (v >> (64 - r)) : v; }
 
 static void keccak_f(uint64_t A[25]) {
-  keccak_init();
   for (int ir = 0; ir < 24; ++ir) {
-    uint64_t C[5], D[5], B[25];
+    uint64_t C[5], B[25];
+#pragma GCC unroll 5
     for (int x = 0; x < 5; ++x) C[x] = A[x] ^ A[x + 5] ^ A[x + 10] ^ A[x + 15] ^ A[x + 20];
-    for (int x = 0; x < 5; ++x) D[x] = C[(x + 4) % 5] ^ rotl(C[(x + 1) % 5], 1);
-    for (int i = 0; i < 25; ++i) A[i] ^= D[i % 5];
+#pragma GCC unroll 25
+    for (int i = 0; i < 25; ++i) A[i] ^= C[(i + 4) % 5] ^ rotl(C[(i + 1) % 5], 1);
     // rho and pi: B[y, 2x+3y] = rot(A[x, y], r[x, y])
-    for (int x = 0; x < 5; ++x)
-      for (int y = 0; y < 5; ++y) B[y + 5 * ((2 * x + 3 * y) % 5)] = rotl(A[x + 5 * y], g_rho[x + 5 * y]);
-    for (int x = 0; x < 5; ++x)
-      for (int y = 0; y < 5; ++y)
-        A[x + 5 * y] = B[x + 5 * y] ^ ((~B[(x + 1) % 5 + 5 * y]) & B[(x + 2) % 5 + 5 * y]);
-    A[0] ^= g_rc[ir];
+#pragma GCC unroll 25
+    for (int i = 0; i < 25; ++i) {
+      const int x = i % 5, y = i / 5;
+      B[y + 5 * ((2 * x + 3 * y) % 5)] = rotl(A[i], KT.rho[i]);
+    }
+#pragma GCC unroll 25
+    for (int i = 0; i < 25; ++i) {
+      const int x = i % 5, y5 = i - x;
+      A[i] = B[i] ^ ((~B[y5 + (x + 1) % 5]) & B[y5 + (x + 2) % 5]);
+    }
+    A[0] ^= KT.rc[ir];
   }
 }
 
@@ -299,9 +305,15 @@ struct Digest {
 // Additive NTT (p3/src/field/binary.rs).
 // ---------------------------------------------------------------------------
 static size_t reverse_bits_len(size_t x, int bits) {
-  size_t r = 0;
-  for (int i = 0; i < bits; ++i) r |= ((x >> i) & 1) << (bits - 1 - i);
-  return r;
+  if (bits == 0) return 0;
+  uint64_t v = x;
+  v = ((v >> 1) & 0x5555555555555555ull) | ((v & 0x5555555555555555ull) << 1);
+  v = ((v >> 2) & 0x3333333333333333ull) | ((v & 0x3333333333333333ull) << 2);
+  v = ((v >> 4) & 0x0f0f0f0f0f0f0f0full) | ((v & 0x0f0f0f0f0f0f0f0full) << 4);
+  v = ((v >> 8) & 0x00ff00ff00ff00ffull) | ((v & 0x00ff00ff00ff00ffull) << 8);
+  v = ((v >> 16) & 0x0000ffff0000ffffull) | ((v & 0x0000ffff0000ffffull) << 16);
+  v = (v >> 32) | (v << 32);
+  return (size_t)(v >> (64 - bits));
 }
 
 // AddtiveNtt::new (binary.rs:23-53).  Returns `twiddles` in the reference's
@@ -1252,9 +1264,8 @@ void orc_polyval_rfc(const uint8_t* h, const uint8_t* xs, size_t n, uint8_t* out
 
 void orc_keccak_f(uint64_t* st) { keccak_f(st); }
 void orc_keccak_consts(uint64_t* rc24, int* rho25) {
-  keccak_init();
-  std::memcpy(rc24, g_rc, sizeof(g_rc));
-  std::memcpy(rho25, g_rho, sizeof(g_rho));
+  std::memcpy(rc24, KT.rc, sizeof(KT.rc));
+  std::memcpy(rho25, KT.rho, sizeof(KT.rho));
 }
 void orc_keccak256(const uint8_t* msg, size_t len, uint8_t* out) { keccak256(msg, len, out); }
 void orc_sha3_256(const uint8_t* msg, size_t len, uint8_t* out) { sponge256(msg, len, 0x06, out); }
@@ -1396,6 +1407,30 @@ int orc_open(int n, int log2_c, size_t width, const uint8_t* data, const uint8_t
   bool ok;
   Proof pf = open(code, cd, n_evals == 1, load_vec(point, n_evals ? n : 0), load_vec(values, n_evals ? width : 0),
                   ch, ok);
+  if (!ok) return -3;
+  std::vector<uint8_t> b = serialize(pf);
+  *proof_len = b.size();
+  if (cap < b.size()) return -2;
+  std::memcpy(proof_out, b.data(), b.size());
+  return 0;
+}
+
+// One full prover step of the reference's harness, timed as the CPU
+// baseline: commit, observe the root, evaluate, observe the values, open.
+int orc_commit_eval_open(int n, int log2_c, const uint8_t* data, const uint8_t* point, uint8_t* root,
+                         uint8_t* proof_out, size_t cap, size_t* proof_len) {
+  if (n < 0 || log2_c < 0 || n + log2_c > 28) return -1;
+  Code code(128, log2_c, n);
+  std::vector<u128> d = load_vec(data, (size_t)1 << n);
+  std::vector<u128> pt = load_vec(point, n);
+  CommitmentData cd = commit(code, d, 1);
+  std::memcpy(root, cd.codewords.root().b, 32);
+  Challenger ch;
+  ch.observe_digest(cd.codewords.root());
+  std::vector<u128> vals = eval(d, 1, pt);
+  for (u128 v : vals) ch.observe_elem(v);
+  bool ok;
+  Proof pf = open(code, cd, true, pt, vals, ch, ok);
   if (!ok) return -3;
   std::vector<uint8_t> b = serialize(pf);
   *proof_len = b.size();

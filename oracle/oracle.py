@@ -49,6 +49,7 @@ def lib():
         L.orc_harness_prepare.argtypes = [C.c_int, C.c_int, sz, u8p, u8p, u8p, u8p, u8p, C.POINTER(sz)]
         L.orc_open.argtypes = [C.c_int, C.c_int, sz, u8p, u8p, u8p, C.c_int, u8p, sz, u8p, sz, C.POINTER(sz)]
         L.orc_verify.argtypes = [C.c_int, C.c_int, sz, u8p, u8p, u8p, C.c_int, u8p, sz, u8p, sz]
+        L.orc_commit_eval_open.argtypes = [C.c_int, C.c_int, u8p, u8p, u8p, u8p, sz, C.POINTER(sz)]
         L.orc_sumcheck_prove.argtypes = [C.c_int, C.c_int, u8p, u8p, u8p, sz, u8p]
         L.orc_sumcheck_verify.argtypes = [C.c_int, C.c_int, u8p, u8p, u8p, u8p, sz, u8p]
         _lib = L
@@ -259,6 +260,19 @@ def open_proof(n: int, log2_c: int, data, point, values, blob: bytes, width: int
             continue
         assert rc == 0, rc
         return out[: ln.value].tobytes()
+
+
+def commit_eval_open(n: int, log2_c: int, data, point):
+    """One full prover step (commit, eval, open with the harness transcript); returns (root, proof)."""
+    d = _elems(data)
+    p = _elems(point) if n else np.zeros((1, 16), np.uint8)
+    root = np.zeros(32, dtype=np.uint8)
+    cap = 1 << 23
+    out = np.zeros(cap, dtype=np.uint8)
+    ln = C.c_size_t(0)
+    rc = lib().orc_commit_eval_open(n, log2_c, _p(d), _p(p), _p(root), _p(out), cap, C.byref(ln))
+    assert rc == 0, rc
+    return root.tobytes(), out[: ln.value].tobytes()
 
 
 def verify(n: int, log2_c: int, root: bytes, point, values, blob: bytes, proof: bytes, width: int = 1,
