@@ -54,6 +54,7 @@ extern "C" {
 typedef struct bf_pcs bf_pcs;
 typedef struct bf_commitment bf_commitment;
 typedef struct bf_challenger bf_challenger;
+typedef struct bf_open_session bf_open_session;
 
 /* Text of the last error on this thread (NUL-terminated, truncated to len). */
 int bf_last_error(char* buf, size_t len);
@@ -103,6 +104,32 @@ int bf_eval(bf_pcs* pcs, const bf_commitment* comm, const uint8_t* point, uint8_
  * size (also when BF_ERR_BUFFER is returned). */
 int bf_open(bf_pcs* pcs, const bf_commitment* comm, const uint8_t* point, const uint8_t* values, int n_evals,
             bf_challenger* ch, uint8_t* proof, size_t cap, size_t* proof_len);
+
+/* ---- PolyCommitScheme::open driven round by round by the caller's own
+ * transcript (any FieldChallenger): the device computes each round's
+ * folded-codeword Merkle root and compressed round polynomial [c0, c2]; the
+ * caller observes both (basefold.rs:356, sumcheck/src/lib.rs:97), samples the
+ * challenge and passes it back.  After the last round the caller observes the
+ * final polynomial (basefold.rs:196), samples the query indices
+ * (basefold.rs:200-203) and finishes.  `stream` (cudaStream_t or NULL for the
+ * pcs's stream) lets several sessions overlap on the GPU.
+ * bf_open_start: begins open (basefold.rs:133-193) for one point.
+ * bf_open_round: waits for the device and writes the current round index
+ *   (d-1 .. 0, or -1 once every round is done), its root and round poly.
+ * bf_open_challenge: applies the round's challenge; returns without waiting.
+ * bf_open_poll: 1 when the session's enqueued work has finished, else 0.
+ * bf_open_final: the final polynomial (one element) after the last round.
+ * bf_open_finish: gathers the openings at the caller's indices (exactly
+ *   num_queries of them) and writes the bincode proof. */
+int bf_open_start(bf_pcs* pcs, const bf_commitment* comm, const uint8_t* point, const uint8_t* values, void* stream,
+                  bf_open_session** out);
+int bf_open_round(bf_open_session* s, int* round, uint8_t pi_root[32], uint8_t round_poly[32]);
+int bf_open_challenge(bf_open_session* s, const uint8_t r[16]);
+int bf_open_poll(bf_open_session* s);
+int bf_open_final(bf_open_session* s, uint8_t final_poly[16]);
+int bf_open_finish(bf_open_session* s, const uint64_t* indices, size_t nq, uint8_t* proof, size_t cap,
+                   size_t* proof_len);
+void bf_open_session_free(bf_open_session* s);
 
 /* ---- PolyCommitScheme::verify (lib.rs:44-50; basefold.rs:234-324) on the
  * host.  Returns BF_VERIFY_* (>= 0) or a negative BF_ERR_*. */

@@ -256,6 +256,10 @@ class Basefold:
             check(lib().bf_open(self._h, comm._h, None, None, 0, challenger._h, _p(out), out.size, C.byref(ln)))
         return out[: ln.value].tobytes()
 
+    def open_session(self, comm: CommitmentData, evals: "PolyEvals", stream=None) -> "OpenSession":
+        """Round-level open driven by the caller's transcript (see OpenSession)."""
+        return OpenSession(self, comm, evals, stream)
+
     def verify(self, comm: bytes, evals, proof: bytes, challenger: GenericChallenger) -> None:
         """verify (basefold.rs:234-324); raises BasefoldError on rejection."""
         root = np.frombuffer(bytes(comm), dtype=np.uint8).copy()
@@ -291,6 +295,77 @@ class Basefold:
         cnt = (C.c_uint64 * n)()
         check(lib().bf_profile_read(self._h, ms, cnt, n))
         return {name: (ms[i], cnt[i]) for i, name in enumerate(self.PROFILE_CLASSES)}
+
+
+class OpenSession:
+    """Basefold::open (basefold.rs:133-232) one round at a time.
+
+    Loop: `round()` gives (i, pi_root, compressed round poly) for rounds
+    i = d-1 .. 0; the caller observes the root and the poly, samples r and calls
+    `challenge(r)`.  When `round()` returns i = -1, `final_poly()` is observed,
+    `num_queries` indices are sampled and `finish(indices)` returns the proof."""
+
+    def __init__(self, pcs: "Basefold", comm: CommitmentData, evals: "PolyEvals", stream=None):
+        self._pcs, self._comm = pcs, comm
+        d = pcs.config.code.d
+        pt = _elems(evals.point) if d else np.zeros((1, 16), np.uint8)
+        vals = _elems(evals.values, 1)
+        h = C.c_void_p()
+        check(lib().bf_open_start(pcs._h, comm._h, _p(pt), _p(vals), C.c_void_p(stream) if stream else None,
+                                  C.byref(h)))
+        self._h = h
+
+    def round(self):
+        rnd = C.c_int()
+        root = np.zeros(32, dtype=np.uint8)
+        poly = np.zeros((2, 16), dtype=np.uint8)
+        check(lib().bf_open_round(self._h, C.byref(rnd), _p(root), _p(poly)))
+        return rnd.value, root.tobytes(), poly
+
+    def challenge(self, r) -> None:
+        check(lib().bf_open_challenge(self._h, _p(_elems(r, 1))))
+
+    def poll(self) -> bool:
+        return check(lib().bf_open_poll(self._h)) == 1
+
+    def final_poly(self) -> np.ndarray:
+        out = np.zeros((1, 16), dtype=np.uint8)
+        check(lib().bf_open_final(self._h, _p(out)))
+        return out
+
+    def finish(self, indices) -> bytes:
+        idx = np.ascontiguousarray(np.asarray(indices, dtype=np.uint64))
+        size = self._pcs.proof_size(1, 1)
+        out = np.zeros(size, dtype=np.uint8)
+        ln = C.c_size_t()
+        check(lib().bf_open_finish(self._h, idx.ctypes.data_as(C.POINTER(C.c_uint64)), idx.size, _p(out), out.size,
+                                   C.byref(ln)))
+        return out[: ln.value].tobytes()
+
+    def free(self):
+        if getattr(self, "_h", None):
+            lib().bf_open_session_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def prove(self, challenger: GenericChallenger) -> bytes:
+        """Drive every round with `challenger` (the same transcript as Basefold.open)."""
+        while True:
+            i, root, poly = self.round()
+            if i < 0:
+                break
+            challenger.observe(root)
+            challenger.observe_ext_slice(poly)
+            self.challenge(challenger.sample_ext_element())
+        challenger.observe_ext_slice(self.final_poly())
+        L = self._pcs.config.code.log2_c + self._pcs.config.code.d
+        idx = [challenger.sample_bits(L) for _ in range(self._pcs.num_queries())]
+        return self.finish(idx)
 
 
 def _split_sumcheck(out, k, n):

@@ -13,7 +13,8 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libbasefold_gpu.so")
 EXPORTS = [
     "bf_last_error", "bf_device_info", "bf_kernel_launches", "bf_pcs_setup", "bf_pcs_free", "bf_pcs_num_queries", "bf_pcs_proof_size",
     "bf_commit", "bf_commit_device", "bf_commitment_free", "bf_commitment_root", "bf_commitment_data", "bf_eval",
-    "bf_open", "bf_verify", "bf_challenger_new", "bf_challenger_clone", "bf_challenger_free",
+    "bf_open", "bf_open_start", "bf_open_round", "bf_open_challenge", "bf_open_poll", "bf_open_final",
+    "bf_open_finish", "bf_open_session_free", "bf_verify", "bf_challenger_new", "bf_challenger_clone", "bf_challenger_free",
     "bf_challenger_observe", "bf_challenger_sample_ext", "bf_challenger_sample_bits", "bf_challenger_state",
     "bf_challenger_from_state", "bf_sumcheck_prove", "bf_sumcheck_prove_device", "bf_profile_enable",
     "bf_profile_read", "bf_test_gf_mul", "bf_test_keccak_f",
@@ -64,6 +65,13 @@ def lib():
         "bf_commitment_data": ([vp, u8p, sz], i),
         "bf_eval": ([vp, vp, u8p, u8p], i),
         "bf_open": ([vp, vp, u8p, u8p, i, vp, u8p, sz, C.POINTER(sz)], i),
+        "bf_open_start": ([vp, vp, u8p, u8p, vp, C.POINTER(vp)], i),
+        "bf_open_round": ([vp, C.POINTER(i), u8p, u8p], i),
+        "bf_open_challenge": ([vp, u8p], i),
+        "bf_open_poll": ([vp], i),
+        "bf_open_final": ([vp, u8p], i),
+        "bf_open_finish": ([vp, C.POINTER(C.c_uint64), sz, u8p, sz, C.POINTER(sz)], i),
+        "bf_open_session_free": ([vp], None),
         "bf_verify": ([vp, u8p, u8p, u8p, sz, i, vp, u8p, sz], i),
         "bf_challenger_new": ([u8p, sz, C.POINTER(vp)], i),
         "bf_challenger_clone": ([vp, C.POINTER(vp)], i),

@@ -1,0 +1,196 @@
+// Shared host-side definitions of libbasefold_gpu.so: error reporting,
+// device/pinned buffers, kernel-class timing and the ABI objects.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <array>
+#include <cstdint>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/basefold_gpu.h"
+#include "bf_internal.h"
+#include "host_math.h"
+
+namespace bfapi {
+
+using bfh::u128;
+
+// Records the message as the calling thread's last error and returns `code`.
+int fail(int code, const char* fmt, ...);
+const std::string& last_error();
+
+#define CU(expr)                                                                                      \
+  do {                                                                                                \
+    cudaError_t e__ = (expr);                                                                         \
+    if (e__ != cudaSuccess)                                                                           \
+      return ::bfapi::fail(e__ == cudaErrorMemoryAllocation ? BF_ERR_OOM : BF_ERR_CUDA, "%s: %s (%s:%d)", \
+                           #expr, cudaGetErrorString(e__), __FILE__, __LINE__);                       \
+  } while (0)
+
+#define TRY(expr)              \
+  do {                         \
+    int rc__ = (expr);         \
+    if (rc__ < 0) return rc__; \
+  } while (0)
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  bool owned = true;
+  cudaStream_t pool_stream = nullptr;  // set when allocated from a stream-ordered pool
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p && owned) {
+      if (pool_stream)
+        cudaFreeAsync(p, pool_stream);
+      else
+        cudaFree(p);
+    }
+    p = nullptr;
+    bytes = 0;
+    pool_stream = nullptr;
+  }
+  cudaError_t alloc(size_t n) {
+    release();
+    owned = true;
+    if (n == 0) n = 16;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e == cudaSuccess) bytes = n;
+    return e;
+  }
+  // Stream-ordered allocation from `pool`, released in stream order on `st`.
+  cudaError_t alloc_async(size_t n, cudaMemPool_t pool, cudaStream_t st) {
+    release();
+    owned = true;
+    if (n == 0) n = 16;
+    cudaError_t e = cudaMallocFromPoolAsync(&p, n, pool, st);
+    if (e == cudaSuccess) {
+      bytes = n;
+      pool_stream = st;
+    }
+    return e;
+  }
+  template <class T>
+  T* as() const {
+    return reinterpret_cast<T*>(p);
+  }
+};
+
+struct PinnedBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  PinnedBuf() = default;
+  PinnedBuf(const PinnedBuf&) = delete;
+  PinnedBuf& operator=(const PinnedBuf&) = delete;
+  ~PinnedBuf() {
+    if (p) cudaFreeHost(p);
+  }
+  cudaError_t ensure(size_t n) {
+    if (n <= bytes) return cudaSuccess;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMallocHost(&p, n);
+    if (e == cudaSuccess) bytes = n;
+    return e;
+  }
+  uint8_t* b() const { return reinterpret_cast<uint8_t*>(p); }
+};
+
+inline uint4 to_uint4(u128 v) {
+  uint4 r;
+  std::memcpy(&r, &v, 16);
+  return r;
+}
+
+// Kernel classes timed with CUDA events when profiling is on.
+constexpr int kProfClasses = 8;
+enum ProfClass { P_ENCODE = 0, P_LEAVES = 1, P_TREE = 2, P_PI_LEAVES = 3, P_FOLD = 4, P_FIX = 5, P_EQ = 6, P_GATHER = 7 };
+
+struct Profiler {
+  bool on = false;
+  struct Pending {
+    int cls;
+    cudaEvent_t a, b;
+  };
+  std::vector<Pending> pending;
+  std::vector<cudaEvent_t> pool;
+  double ms[kProfClasses] = {0};
+  uint64_t count[kProfClasses] = {0};
+  cudaEvent_t get();
+  ~Profiler();
+  void drain();  // resolve recorded pairs; the stream must have been synchronised
+};
+
+struct ProfScope {
+  Profiler& pr;
+  cudaStream_t st;
+  int cls;
+  cudaEvent_t a = nullptr;
+  ProfScope(Profiler& p, cudaStream_t s, int c);
+  ~ProfScope();
+};
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev);
+  ~DeviceGuard();
+};
+
+size_t num_queries(int lambda, int log2_c);
+u128 horner(const u128* c, int n, u128 x);
+void put_u64(std::vector<uint8_t>& b, uint64_t v);
+void put_elem(std::vector<uint8_t>& b, u128 v);
+
+}  // namespace bfapi
+
+struct bf_challenger {
+  bfh::Challenger c;
+};
+
+struct bf_pcs {
+  int device = 0;
+  int lambda = 128, log2_c = 1, d = 0, L = 0;
+  size_t Q = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  // Commitments and open sessions draw their buffers from this pool; it keeps
+  // freed memory for reuse instead of returning it to the driver.
+  cudaMemPool_t pool = nullptr;
+  bfapi::DevBuf tw_tables, tw_view;
+  bf::TwiddleView tw_host{};
+  std::vector<std::vector<bfh::u128>> bases;  // stage bases (host copy, for the verifier)
+  bfapi::DevBuf sc_ws;                        // standalone-sumcheck scratch
+  bfapi::DevBuf eval_ws;                      // bf_eval scratch
+  bfapi::PinnedBuf pinned;
+  std::vector<std::unique_ptr<bfapi::PinnedBuf>> pinned_cache;  // staging kept between open sessions
+  bfapi::Profiler prof;
+
+  size_t n_d() const { return (size_t)1 << L; }
+  size_t c() const { return (size_t)1 << log2_c; }
+  size_t n_i(int i) const { return c() << i; }
+  // Bytes of one query opening in the proof (basefold.rs:56-65).
+  size_t block_bytes(size_t width) const {
+    size_t b = 8 + 16 * width + 8 + 32 * (size_t)L + 8;
+    for (int i = 0; i < d; ++i) b += 24 + 32 * (size_t)(log2_c + i);
+    return b;
+  }
+  ~bf_pcs();
+};
+
+struct bf_commitment {
+  bf_pcs* pcs = nullptr;
+  size_t width = 1;
+  bfapi::DevBuf data, cw, tree;
+  // Tree of the first open round's folded codeword (for width 1 it is the
+  // codeword itself, paired (2s, 2s+1) in NTT order), built at commit time.
+  bfapi::DevBuf pi_tree;
+  uint8_t root[32];
+  uint8_t pi_root[32];
+};

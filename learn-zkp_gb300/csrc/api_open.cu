@@ -1,0 +1,416 @@
+// libbasefold_gpu.so: Basefold::open (poly-commit/src/basefold.rs:133-232) as a
+// round-level session.
+//
+// Each round the device returns the folded-codeword Merkle root and the
+// compressed sumcheck round polynomial; the caller's transcript observes them
+// and samples the challenge; the device then folds, fixes the variable, and
+// builds the next round's tree.  Sessions own their device workspace, so
+// several can be in flight on different streams.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "api_common.h"
+
+using bfh::u128;
+using namespace bfapi;
+
+struct bf_open_session {
+  bf_pcs* p = nullptr;
+  const bf_commitment* cm = nullptr;
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev = nullptr;
+  int d = 0;
+  int i = 0;               // current round (d-1 .. 0); -1 once every round is done
+  bool msg_ready = false;  // host message of the current round computed
+  bool pending = false;    // device work enqueued, its result not read yet
+  bool final_ready = false;
+  std::vector<u128> r, r_inv, corr;
+  u128 outer_val = 0, inner_val = 0, delta_prod = 0;
+  uint8_t root[32] = {0};
+  u128 rp[3] = {0, 0, 0};
+  u128 c01[2] = {0, 0};
+  u128 final_val = 0;
+  std::vector<uint8_t> rounds, roots;
+  DevBuf ws;
+  uint4* w_point = nullptr;
+  uint4* w_pi_fold = nullptr;
+  uint4* w_pi_trees = nullptr;
+  uint4* w_poly = nullptr;
+  uint4* w_heq = nullptr;
+  uint4* w_eq_lo = nullptr;
+  uint4* w_eq_hi = nullptr;
+  uint8_t* w_stage = nullptr;  // per round: root (32 B) + sumcheck reduction (16 B)
+  uint64_t* w_idx = nullptr;
+  uint8_t* w_open = nullptr;
+  std::unique_ptr<PinnedBuf> pin;  // [0,64) staging, [64,64+16d) point, indices, openings
+  uint64_t* idx_pin = nullptr;
+  uint8_t* open_pin = nullptr;
+
+  size_t c() const { return p->c(); }
+  uint4* pi_fold_out(int k) const { return w_pi_fold + c() * (((size_t)1 << d) - ((size_t)1 << (k + 1))); }
+  // tree of round k <= d-2 (round d-1's tree is the commitment's)
+  uint4* pi_tree(int k) const {
+    return w_pi_trees + 2 * ((c() << 1) * (((size_t)1 << (d - 1)) - ((size_t)1 << (k + 1))) - (size_t)(d - 2 - k));
+  }
+  uint8_t* stage(int k) const { return w_stage + 48 * (size_t)k; }
+  ~bf_open_session() {
+    if (st) cudaStreamSynchronize(st);
+    if (ev) cudaEventDestroy(ev);
+    ws.release();
+    if (pin) {
+      // keep the pinned staging for the next session of this pcs
+      p->pinned_cache.push_back(std::move(pin));
+    }
+  }
+};
+
+namespace {
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+int session_alloc(bf_open_session* s) {
+  bf_pcs* p = s->p;
+  const int d = s->d;
+  const size_t c = p->c();
+  const size_t half = d >= 1 ? ((size_t)1 << (d - 1)) : 1;
+  const size_t n_point = d > 0 ? d : 1;
+  const size_t n_fold = c * (((size_t)1 << d) - 1) + 1;
+  const size_t n_tree = d >= 2 ? (c << 1) * (((size_t)1 << (d - 1)) - 1) - (size_t)(d - 1) + 1 : 1;
+  const int hi_vars = d - 1 > 12 ? d - 1 - 12 : 0;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    size_t o = off;
+    off += align256(bytes);
+    return o;
+  };
+  const size_t o_point = take(16 * n_point), o_fold = take(16 * n_fold), o_tree = take(32 * n_tree);
+  const size_t o_poly = take(16 * half), o_heq = take(16 * half), o_lo = take(16 * 4096);
+  const size_t o_hi = take(16 * ((size_t)1 << hi_vars)), o_stage = take(48 * n_point);
+  const size_t o_idx = take(8 * (p->Q + 1)), o_open = take(p->block_bytes(1) * (p->Q + 1));
+  CU(s->ws.alloc_async(off, p->pool, s->st));
+  uint8_t* b = s->ws.as<uint8_t>();
+  s->w_point = reinterpret_cast<uint4*>(b + o_point);
+  s->w_pi_fold = reinterpret_cast<uint4*>(b + o_fold);
+  s->w_pi_trees = reinterpret_cast<uint4*>(b + o_tree);
+  s->w_poly = reinterpret_cast<uint4*>(b + o_poly);
+  s->w_heq = reinterpret_cast<uint4*>(b + o_heq);
+  s->w_eq_lo = reinterpret_cast<uint4*>(b + o_lo);
+  s->w_eq_hi = reinterpret_cast<uint4*>(b + o_hi);
+  s->w_stage = b + o_stage;
+  s->w_idx = reinterpret_cast<uint64_t*>(b + o_idx);
+  s->w_open = b + o_open;
+  const size_t pin_bytes = 64 + 16 * n_point + 8 * (p->Q + 1) + p->block_bytes(1) * (p->Q + 1);
+  if (!p->pinned_cache.empty()) {
+    s->pin = std::move(p->pinned_cache.back());
+    p->pinned_cache.pop_back();
+  } else {
+    s->pin.reset(new PinnedBuf());
+  }
+  CU(s->pin->ensure(pin_bytes));
+  s->idx_pin = reinterpret_cast<uint64_t*>(s->pin->b() + 64 + 16 * n_point);
+  s->open_pin = reinterpret_cast<uint8_t*>(s->idx_pin + (p->Q + 1));
+  return BF_OK;
+}
+
+// Reads the result of the enqueued work and computes the host-side message of
+// the current round: EvalImprProver::compute_round_poly + decompress
+// (eval_impr.rs:116-127,187-197) lifted by EvalProver (eval.rs:89-106).
+int ensure_message(bf_open_session* s) {
+  if (s->pending) {
+    CU(cudaStreamSynchronize(s->st));
+    s->p->prof.drain();
+    s->pending = false;
+  }
+  if (s->i < 0) {
+    if (!s->final_ready) {
+      s->final_val = bfh::load(s->pin->b());
+      s->final_ready = true;
+    }
+    return BF_OK;
+  }
+  if (s->msg_ready) return BF_OK;
+  const int i = s->i, d = s->d;
+  const u128 ONE = bfh::one();
+  if (i == d - 1)
+    std::memcpy(s->root, s->cm->pi_root, 32);
+  else
+    std::memcpy(s->root, s->pin->b(), 32);
+  const u128 S = bfh::load(s->pin->b() + 32);
+  const u128 sc_val = (i == d - 1) ? s->outer_val : s->inner_val;
+  const u128 c0 = bfh::mul(s->corr[i], S);
+  const u128 c1 = bfh::mul(sc_val ^ bfh::mul(ONE ^ s->r[i], c0), s->r_inv[i]) ^ c0;
+  const u128 scalar = (i == d - 1) ? ONE : s->delta_prod;  // delta_scalar (eval_impr.rs:45-51)
+  const u128 d0 = bfh::mul(scalar, ONE ^ s->r[i]);
+  const u128 d1 = bfh::mul(scalar, s->r[i] ^ (ONE ^ s->r[i]));
+  s->c01[0] = c0;
+  s->c01[1] = c1;
+  s->rp[0] = bfh::mul(c0, d0);
+  s->rp[1] = bfh::mul(c0, d1) ^ bfh::mul(c1, d0);
+  s->rp[2] = bfh::mul(c1, d1);
+  s->msg_ready = true;
+  return BF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bf_open_start(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, const uint8_t* values, void* stream,
+                  bf_open_session** out) {
+  if (!p || !cm || !out || !values || (p->d > 0 && !point)) return fail(BF_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (p->device < 0) return fail(BF_ERR_ARG, "verifier-only pcs (device < 0)");
+  if (cm->pcs != p) return fail(BF_ERR_ARG, "commitment belongs to another pcs");
+  if (cm->width != 1) return fail(BF_ERR_UNSUPPORTED, "width != 1");
+  DeviceGuard g(p->device);
+  std::unique_ptr<bf_open_session> s(new bf_open_session());
+  s->p = p;
+  s->cm = cm;
+  s->st = stream ? reinterpret_cast<cudaStream_t>(stream) : p->stream;
+  CU(cudaEventCreateWithFlags(&s->ev, cudaEventDisableTiming));
+  const int d = p->d;
+  s->d = d;
+  s->i = d - 1;
+  const u128 ONE = bfh::one();
+  s->r.resize(d);
+  for (int k = 0; k < d; ++k) s->r[k] = bfh::load(point + 16 * k);
+  s->outer_val = bfh::load(values);
+  s->delta_prod = ONE;
+  // EvalImpr::new / HalfEq::new (eval_impr.rs:20-27, 69-79)
+  if (!bfh::batch_inverse(s->r, s->r_inv)) return fail(BF_ERR_NOT_INVERTIBLE, "point has a zero coordinate");
+  std::vector<u128> omr, omr_inv;
+  for (int k = 0; k + 1 < d; ++k) omr.push_back(ONE ^ s->r[k]);
+  if (!bfh::batch_inverse(omr, omr_inv)) return fail(BF_ERR_NOT_INVERTIBLE, "point has a coordinate equal to one");
+  // correcting_factor(i) = prod_{i <= k < d-1} (1 - r_k)^-1 (eval_impr.rs:83-90)
+  s->corr.assign(d > 0 ? d : 1, ONE);
+  for (int i = d - 2; i >= 0; --i) s->corr[i] = bfh::mul(s->corr[i + 1], omr_inv[i]);
+  put_u64(s->rounds, (uint64_t)d);
+  put_u64(s->roots, (uint64_t)d);
+  TRY(session_alloc(s.get()));
+  uint8_t* pin = s->pin->b();
+  const uint4* data = cm->data.as<uint4>();
+  cudaStream_t st = s->st;
+  if (d == 0) {
+    CU(cudaMemcpyAsync(pin, data, 16, cudaMemcpyDeviceToHost, st));
+  } else {
+    std::memcpy(pin + 64, point, 16 * (size_t)d);
+    CU(cudaMemcpyAsync(s->w_point, pin + 64, 16 * (size_t)d, cudaMemcpyHostToDevice, st));
+    CU(cudaMemsetAsync(s->w_stage, 0, 48 * (size_t)d, st));
+    {
+      ProfScope ps(p->prof, st, P_EQ);
+      CU(bf::launch_eq_table(s->w_point, d - 1, s->w_heq, s->w_eq_lo, s->w_eq_hi, st));
+    }
+    {
+      ProfScope ps(p->prof, st, P_FIX);
+      CU(bf::launch_dot_xor(s->w_heq, data, (size_t)1 << (d - 1),
+                            reinterpret_cast<uint32_t*>(s->stage(d - 1) + 32), st));
+    }
+    CU(cudaMemcpyAsync(pin, s->stage(d - 1), 48, cudaMemcpyDeviceToHost, st));
+  }
+  CU(cudaEventRecord(s->ev, st));
+  s->pending = true;
+  *out = s.release();
+  return BF_OK;
+}
+
+int bf_open_poll(bf_open_session* s) {
+  if (!s) return fail(BF_ERR_ARG, "null argument");
+  if (!s->pending) return 1;
+  cudaError_t e = cudaEventQuery(s->ev);
+  if (e == cudaSuccess) return 1;
+  if (e == cudaErrorNotReady) return 0;
+  CU(e);
+  return 0;
+}
+
+int bf_open_round(bf_open_session* s, int* round, uint8_t pi_root[32], uint8_t round_poly[32]) {
+  if (!s || !round) return fail(BF_ERR_ARG, "null argument");
+  DeviceGuard g(s->p->device);
+  TRY(ensure_message(s));
+  *round = s->i;
+  if (s->i < 0) return BF_OK;
+  if (pi_root) std::memcpy(pi_root, s->root, 32);
+  if (round_poly) {  // compressed [c0, c2] (eval.rs:64-66)
+    bfh::store(round_poly, s->rp[0]);
+    bfh::store(round_poly + 16, s->rp[2]);
+  }
+  return BF_OK;
+}
+
+int bf_open_challenge(bf_open_session* s, const uint8_t r_i[16]) {
+  if (!s || !r_i) return fail(BF_ERR_ARG, "null argument");
+  DeviceGuard g(s->p->device);
+  TRY(ensure_message(s));
+  if (s->i < 0) return fail(BF_ERR_ARG, "every round is done");
+  bf_pcs* p = s->p;
+  const int i = s->i, d = s->d;
+  const u128 ONE = bfh::one();
+  s->roots.insert(s->roots.end(), s->root, s->root + 32);
+  put_u64(s->rounds, 2);
+  put_elem(s->rounds, s->rp[0]);
+  put_elem(s->rounds, s->rp[2]);
+  const u128 x = bfh::load(r_i);
+  s->inner_val = horner(s->c01, 2, x);  // EvalProver::fix_last_var (eval.rs:108-111)
+  s->outer_val = horner(s->rp, 3, x);   // SumcheckSubclaim::reduce (sumcheck/src/lib.rs:41-47)
+  s->delta_prod = bfh::mul(s->delta_prod, ONE ^ s->r[i] ^ x);
+  const uint4 xr = to_uint4(x);
+  cudaStream_t st = s->st;
+  // fold (binary_reed_solomon.rs:88-96) with the stage d-1-i twiddles,
+  // fused with the leaves of the next round's tree
+  const size_t ni = p->n_i(i);
+  const uint4* cw = s->cm->cw.as<uint4>();
+  const uint4* pi_in = (i == d - 1) ? cw : s->pi_fold_out(i + 1);
+  const uint4* tlo = p->tw_host.lo[d - 1 - i];
+  const uint4* thi = p->tw_host.hi[d - 1 - i];
+  {
+    ProfScope ps(p->prof, st, P_FOLD);
+    if (i > 0)
+      CU(bf::launch_fold_leaves(pi_in, s->pi_fold_out(i), s->pi_tree(i - 1), ni / 2, tlo, thi, xr, st));
+    else
+      CU(bf::launch_fold(pi_in, s->pi_fold_out(i), ni, tlo, thi, xr, st));
+  }
+  // fix_last_var (multilinear.rs:183-198) + next round's reduction
+  const uint4* poly_in = (i == d - 1) ? s->cm->data.as<uint4>() : s->w_poly;
+  {
+    ProfScope ps(p->prof, st, P_FIX);
+    CU(bf::launch_fix(poly_in, s->w_poly, (size_t)1 << i, xr, s->w_heq, i > 0 ? ((size_t)1 << (i - 1)) : 0,
+                      i > 0 ? reinterpret_cast<uint32_t*>(s->stage(i - 1) + 32) : nullptr, st));
+  }
+  uint8_t* pin = s->pin->b();
+  if (i > 0) {
+    {
+      ProfScope ps(p->prof, st, P_TREE);
+      CU(bf::launch_tree(s->pi_tree(i - 1), p->n_i(i - 1), st, reinterpret_cast<uint4*>(s->stage(i - 1))));
+    }
+    CU(cudaMemcpyAsync(pin, s->stage(i - 1), 48, cudaMemcpyDeviceToHost, st));
+  } else {
+    CU(cudaMemcpyAsync(pin, s->w_poly, 16, cudaMemcpyDeviceToHost, st));
+  }
+  CU(cudaEventRecord(s->ev, st));
+  s->pending = true;
+  s->msg_ready = false;
+  s->i -= 1;
+  return BF_OK;
+}
+
+int bf_open_final(bf_open_session* s, uint8_t final_poly[16]) {
+  if (!s || !final_poly) return fail(BF_ERR_ARG, "null argument");
+  if (s->i >= 0) return fail(BF_ERR_ARG, "rounds remain");
+  DeviceGuard g(s->p->device);
+  TRY(ensure_message(s));
+  bfh::store(final_poly, s->final_val);
+  return BF_OK;
+}
+
+int bf_open_finish(bf_open_session* s, const uint64_t* indices, size_t nq, uint8_t* proof, size_t cap,
+                   size_t* proof_len) {
+  if (!s || !proof_len || (nq && !indices)) return fail(BF_ERR_ARG, "null argument");
+  bf_pcs* p = s->p;
+  if (s->i >= 0) return fail(BF_ERR_ARG, "rounds remain");
+  if (nq != p->Q) return fail(BF_ERR_ARG, "expected %zu query indices, got %zu", p->Q, nq);
+  const size_t need = bf_pcs_proof_size(p, 1, 1);
+  *proof_len = need;
+  if (!proof || cap < need) return fail(BF_ERR_BUFFER, "proof buffer needs %zu bytes", need);
+  DeviceGuard g(p->device);
+  TRY(ensure_message(s));
+  const size_t bb = p->block_bytes(1);
+  for (size_t q = 0; q < nq; ++q) {
+    if (indices[q] >= p->n_d()) return fail(BF_ERR_ARG, "query index %llu out of range", (unsigned long long)indices[q]);
+    s->idx_pin[q] = indices[q];
+  }
+  cudaStream_t st = s->st;
+  if (nq) {
+    CU(cudaMemcpyAsync(s->w_idx, s->idx_pin, 8 * nq, cudaMemcpyHostToDevice, st));
+    bf::GatherParams gp{};
+    gp.cw = s->cm->cw.as<uint4>();
+    gp.cw_tree = s->cm->tree.as<uint4>();
+    gp.pi_first = gp.cw;
+    gp.pi_first_tree = s->cm->pi_tree.as<uint4>();
+    gp.pi_fold = s->w_pi_fold;
+    gp.pi_trees = s->w_pi_trees;
+    gp.idx = s->w_idx;
+    gp.out = s->w_open;
+    gp.width = 1;
+    gp.block_bytes = bb;
+    gp.L = p->L;
+    gp.d = s->d;
+    gp.log2_c = p->log2_c;
+    gp.nq = (int)nq;
+    {
+      ProfScope ps(p->prof, st, P_GATHER);
+      CU(bf::launch_gather(gp, st));
+    }
+    CU(cudaMemcpyAsync(s->open_pin, s->w_open, bb * nq, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    p->prof.drain();
+  }
+  // BasefoldProof bincode (basefold.rs:49-66): round polys, final poly,
+  // pi_comms, openings
+  uint8_t* o = proof;
+  std::memcpy(o, s->rounds.data(), s->rounds.size());
+  o += s->rounds.size();
+  std::vector<uint8_t> fin;
+  put_u64(fin, 1);
+  put_elem(fin, s->final_val);
+  std::memcpy(o, fin.data(), fin.size());
+  o += fin.size();
+  std::memcpy(o, s->roots.data(), s->roots.size());
+  o += s->roots.size();
+  std::vector<uint8_t> qn;
+  put_u64(qn, nq);
+  std::memcpy(o, qn.data(), 8);
+  o += 8;
+  if (nq) std::memcpy(o, s->open_pin, bb * nq);
+  o += bb * nq;
+  if ((size_t)(o - proof) != need) return fail(BF_ERR_CUDA, "internal: proof size mismatch");
+  return BF_OK;
+}
+
+void bf_open_session_free(bf_open_session* s) {
+  if (!s) return;
+  DeviceGuard g(s->p->device);
+  delete s;
+}
+
+// Whole open with this library's transcript (basefold.rs:133-232).
+int bf_open(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, const uint8_t* values, int n_evals,
+            bf_challenger* chp, uint8_t* proof, size_t cap, size_t* proof_len) {
+  if (!p || !cm || !chp || !proof_len) return fail(BF_ERR_ARG, "null argument");
+  if (n_evals < 0 || n_evals > 1) return fail(BF_ERR_ARG, "n_evals must be 0 or 1");
+  const size_t need = bf_pcs_proof_size(p, cm->width, n_evals);
+  *proof_len = need;
+  if (!proof || cap < need) return fail(BF_ERR_BUFFER, "proof buffer needs %zu bytes", need);
+  if (n_evals == 0) {  // basefold.rs:139-141: Default proof
+    std::memset(proof, 0, 32);
+    return BF_OK;
+  }
+  bf_open_session* s = nullptr;
+  TRY(bf_open_start(p, cm, point, values, nullptr, &s));
+  std::unique_ptr<bf_open_session, void (*)(bf_open_session*)> guard(s, bf_open_session_free);
+  bfh::Challenger& ch = chp->c;
+  while (true) {
+    int round;
+    uint8_t root[32], poly[32];
+    TRY(bf_open_round(s, &round, root, poly));
+    if (round < 0) break;
+    ch.observe(root, 32);  // basefold.rs:356
+    ch.observe(poly, 32);  // sumcheck/src/lib.rs:97
+    uint8_t r[16];
+    bfh::store(r, ch.sample_elem());
+    TRY(bf_open_challenge(s, r));
+  }
+  uint8_t fin[16];
+  TRY(bf_open_final(s, fin));
+  ch.observe(fin, 16);  // basefold.rs:196
+  std::vector<uint64_t> idx(p->Q);
+  for (size_t q = 0; q < p->Q; ++q) idx[q] = ch.sample_bits(p->L);  // basefold.rs:200-203
+  size_t len = 0;
+  TRY(bf_open_finish(s, idx.data(), idx.size(), proof, cap, &len));
+  *proof_len = len;
+  return BF_OK;
+}
+
+}  // extern "C"

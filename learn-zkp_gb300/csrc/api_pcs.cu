@@ -1,0 +1,524 @@
+// libbasefold_gpu.so: setup, commit, eval, transcript objects, timing and
+// test hooks.
+//
+// The prover keeps every array of the path in device memory: evaluations,
+// codeword, Merkle trees, folded codewords and their trees, the sumcheck
+// polynomial and its eq table.  Only the Fiat–Shamir transcript crosses to
+// the host.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <memory>
+
+#include "api_common.h"
+
+using bfh::u128;
+
+namespace bfapi {
+
+namespace {
+thread_local std::string g_err;
+}
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+const std::string& last_error() { return g_err; }
+
+cudaEvent_t Profiler::get() {
+  if (!pool.empty()) {
+    cudaEvent_t e = pool.back();
+    pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  return e;
+}
+
+Profiler::~Profiler() {
+  for (auto& p : pending) {
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  for (auto e : pool) cudaEventDestroy(e);
+}
+
+void Profiler::drain() {
+  for (auto& p : pending) {
+    float t = 0.f;
+    if (cudaEventElapsedTime(&t, p.a, p.b) == cudaSuccess) {
+      ms[p.cls] += t;
+      count[p.cls] += 1;
+    }
+    pool.push_back(p.a);
+    pool.push_back(p.b);
+  }
+  pending.clear();
+}
+
+ProfScope::ProfScope(Profiler& p, cudaStream_t s, int c) : pr(p), st(s), cls(c) {
+  if (pr.on) {
+    a = pr.get();
+    cudaEventRecord(a, st);
+  }
+}
+
+ProfScope::~ProfScope() {
+  if (pr.on) {
+    cudaEvent_t b = pr.get();
+    cudaEventRecord(b, st);
+    pr.pending.push_back({cls, a, b});
+  }
+}
+
+DeviceGuard::DeviceGuard(int dev) {
+  cudaGetDevice(&prev);
+  if (dev >= 0 && prev != dev) cudaSetDevice(dev);
+}
+
+DeviceGuard::~DeviceGuard() {
+  int cur = -1;
+  cudaGetDevice(&cur);
+  if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+}
+
+// Formula 8 of 2024/504 (binary_reed_solomon.rs:56-59); a non-finite or
+// non-positive quotient saturates to 0 like Rust's float-to-usize cast.
+size_t num_queries(int lambda, int log2_c) {
+  double c = (double)((size_t)1 << log2_c);
+  double delta = (1.0 + 1.0 / c) / 2.0;
+  double q = std::ceil((double)lambda / -std::log2(delta));
+  if (!(q > 0) || !std::isfinite(q)) return 0;
+  return (size_t)q;
+}
+
+// univariate horner (p3/src/poly/univariate.rs:5-12)
+u128 horner(const u128* c, int n, u128 x) {
+  u128 acc = 0;
+  for (int k = n - 1; k >= 0; --k) acc = bfh::mul(acc, x) ^ c[k];
+  return acc;
+}
+
+void put_u64(std::vector<uint8_t>& b, uint64_t v) {
+  for (int i = 0; i < 8; ++i) b.push_back((uint8_t)(v >> (8 * i)));
+}
+
+void put_elem(std::vector<uint8_t>& b, u128 v) {
+  uint8_t t[16];
+  bfh::store(t, v);
+  b.insert(b.end(), t, t + 16);
+}
+
+}  // namespace bfapi
+
+using namespace bfapi;
+
+bf_pcs::~bf_pcs() {
+  if (stream) cudaStreamSynchronize(stream);
+  sc_ws.release();
+  eval_ws.release();
+  if (stream) cudaStreamSynchronize(stream);
+  if (pool) cudaMemPoolDestroy(pool);
+  if (stream && own_stream) cudaStreamDestroy(stream);
+}
+
+// ---------------------------------------------------------------------------
+// Setup: additive-NTT twiddle bases (p3/src/field/binary.rs:23-53).
+// W_0(x) = x, W_{i+1}(x) = W_i(x)^2 + W_i(x) W_i(beta_i); stage s has basis
+// W_s(beta_{s+1+b}) / W_s(beta_s), beta_i = basis(i) = from_canonical(1<<i)
+// (p3/src/polyval.rs:167-172).
+// ---------------------------------------------------------------------------
+namespace {
+
+u128 mul_x(u128 v) {
+  bool carry = (v >> 127) & 1;
+  v <<= 1;
+  if (carry) v ^= (u128)1 ^ ((u128)1 << 121) ^ ((u128)1 << 126) ^ ((u128)1 << 127);
+  return v;
+}
+
+// x^256 mod P: from_canonical(v) = v * x^256 * x^-128.
+u128 r2_const() {
+  static u128 r2 = 0;
+  if (!r2) {
+    u128 v = 1;
+    for (int i = 0; i < 256; ++i) v = mul_x(v);
+    r2 = v;
+  }
+  return r2;
+}
+
+std::vector<std::vector<u128>> stage_bases(int L) {
+  std::vector<std::vector<u128>> out(L);
+  if (L == 0) return out;
+  auto beta = [](int i) { return bfh::mul((u128)1 << i, r2_const()); };
+  u128 wbi = beta(0);
+  std::vector<u128> wb;
+  for (int i = 1; i < L; ++i) wb.push_back(beta(i));
+  for (int s = 0; s < L; ++s) {
+    u128 inv_i = bfh::inv(wbi);
+    for (u128 w : wb) out[s].push_back(bfh::mul(w, inv_i));
+    if (wb.empty()) break;
+    auto q = [wbi](u128 w) { return bfh::sq(w) ^ bfh::mul(w, wbi); };
+    u128 first = q(wb[0]);
+    std::vector<u128> rest;
+    for (size_t b = 1; b < wb.size(); ++b) rest.push_back(q(wb[b]));
+    wbi = first;
+    wb = rest;
+  }
+  return out;
+}
+
+int build_twiddles(bf_pcs* p) {
+  const int L = p->L;
+  p->bases = stage_bases(L);
+  const auto& bases = p->bases;
+  // stage s table has 2^(L-1-s) entries: lo covers the low 12 bits of K, hi the rest.
+  std::vector<u128> host;
+  std::vector<size_t> lo_off(L), hi_off(L);
+  for (int s = 0; s < L; ++s) {
+    const int bits = L - 1 - s;
+    const int lo_bits = bits < bf::kTwLoBits ? bits : bf::kTwLoBits;
+    const int hi_bits = bits - lo_bits;
+    lo_off[s] = host.size();
+    size_t base = host.size();
+    host.resize(base + ((size_t)1 << lo_bits), 0);
+    for (int b = 0; b < lo_bits; ++b) {
+      size_t h = (size_t)1 << b;
+      for (size_t k = 0; k < h; ++k) host[base + h + k] = host[base + k] ^ bases[s][b];
+    }
+    hi_off[s] = host.size();
+    base = host.size();
+    host.resize(base + ((size_t)1 << hi_bits), 0);
+    for (int b = 0; b < hi_bits; ++b) {
+      size_t h = (size_t)1 << b;
+      for (size_t k = 0; k < h; ++k) host[base + h + k] = host[base + k] ^ bases[s][lo_bits + b];
+    }
+  }
+  CU(p->tw_tables.alloc(host.size() * 16 + 16));
+  CU(cudaMemcpy(p->tw_tables.p, host.data(), host.size() * 16, cudaMemcpyHostToDevice));
+  const uint4* t = p->tw_tables.as<uint4>();
+  for (int s = 0; s < L; ++s) {
+    p->tw_host.lo[s] = t + lo_off[s];
+    p->tw_host.hi[s] = t + hi_off[s];
+  }
+  CU(p->tw_view.alloc(sizeof(bf::TwiddleView)));
+  CU(cudaMemcpy(p->tw_view.p, &p->tw_host, sizeof(bf::TwiddleView), cudaMemcpyHostToDevice));
+  return BF_OK;
+}
+
+int commit_device(bf_pcs* p, bf_commitment* cm, const uint4* data) {
+  const size_t nd = p->n_d();
+  CU(cm->cw.alloc_async(16 * nd, p->pool, p->stream));
+  CU(cm->tree.alloc_async(32 * (2 * nd - 1), p->pool, p->stream));
+  if (p->d > 0) CU(cm->pi_tree.alloc_async(32 * (nd - 1), p->pool, p->stream));
+  uint4* cw = cm->cw.as<uint4>();
+  uint4* tree = cm->tree.as<uint4>();
+  uint4* pit = cm->pi_tree.as<uint4>();
+  {
+    ProfScope ps(p->prof, p->stream, P_ENCODE);
+    CU(bf::launch_encode(data, cw, p->d, p->log2_c, 1, p->tw_view.as<bf::TwiddleView>(), p->stream));
+  }
+  {
+    ProfScope ps(p->prof, p->stream, P_LEAVES);
+    if (p->d > 0)
+      CU(bf::launch_leaves_cw_pairs(cw, tree, pit, nd / 2, p->stream));
+    else
+      CU(bf::launch_leaves_elem(cw, tree, nd, 1, p->stream));
+  }
+  {
+    ProfScope ps(p->prof, p->stream, P_TREE);
+    CU(bf::launch_tree(tree, nd, p->stream));
+    if (p->d > 0) CU(bf::launch_tree(pit, nd / 2, p->stream));
+  }
+  CU(cudaMemcpyAsync(p->pinned.b(), tree + 2 * (2 * nd - 2), 32, cudaMemcpyDeviceToHost, p->stream));
+  if (p->d > 0) CU(cudaMemcpyAsync(p->pinned.b() + 32, pit + 2 * (nd - 2), 32, cudaMemcpyDeviceToHost, p->stream));
+  CU(cudaStreamSynchronize(p->stream));
+  p->prof.drain();
+  std::memcpy(cm->root, p->pinned.b(), 32);
+  std::memcpy(cm->pi_root, p->pinned.b() + 32, 32);
+  return BF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bf_last_error(char* buf, size_t len) {
+  if (!buf || len == 0) return BF_ERR_ARG;
+  const std::string& e = last_error();
+  size_t n = e.size() < len - 1 ? e.size() : len - 1;
+  std::memcpy(buf, e.data(), n);
+  buf[n] = 0;
+  return BF_OK;
+}
+
+int bf_kernel_launches(uint64_t* count) {
+  if (!count) return fail(BF_ERR_ARG, "null argument");
+  *count = bf::launches_total();
+  return BF_OK;
+}
+
+int bf_device_info(int device, int* num_sms, int* cc_major, int* cc_minor) {
+  int n = 0;
+  CU(cudaGetDeviceCount(&n));
+  if (device < 0 || device >= n) return fail(BF_ERR_ARG, "device %d out of range (%d devices)", device, n);
+  if (num_sms) CU(cudaDeviceGetAttribute(num_sms, cudaDevAttrMultiProcessorCount, device));
+  if (cc_major) CU(cudaDeviceGetAttribute(cc_major, cudaDevAttrComputeCapabilityMajor, device));
+  if (cc_minor) CU(cudaDeviceGetAttribute(cc_minor, cudaDevAttrComputeCapabilityMinor, device));
+  return BF_OK;
+}
+
+int bf_pcs_setup(int device, int lambda, int log2_c, int num_vars, void* stream, bf_pcs** out) {
+  if (!out) return fail(BF_ERR_ARG, "out is null");
+  *out = nullptr;
+  if (lambda < 0 || log2_c < 0 || log2_c > 4 || num_vars < 0 || num_vars + log2_c > 30)
+    return fail(BF_ERR_ARG, "unsupported code parameters lambda=%d log2_c=%d num_vars=%d", lambda, log2_c, num_vars);
+  std::unique_ptr<bf_pcs> p(new bf_pcs());
+  p->device = device;
+  p->lambda = lambda;
+  p->log2_c = log2_c;
+  p->d = num_vars;
+  p->L = num_vars + log2_c;
+  p->Q = num_queries(lambda, log2_c);
+  if (device < 0) {  // verifier-only object: no GPU is touched
+    p->bases = stage_bases(p->L);
+    *out = p.release();
+    return BF_OK;
+  }
+  CU(cudaSetDevice(device));
+  if (stream) {
+    p->stream = reinterpret_cast<cudaStream_t>(stream);
+  } else {
+    CU(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
+    p->own_stream = true;
+  }
+  TRY(build_twiddles(p.get()));
+  CU(p->pinned.ensure(4096));
+  {
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    CU(cudaMemPoolCreate(&p->pool, &props));
+    uint64_t keep = ~(uint64_t)0;
+    CU(cudaMemPoolSetAttribute(p->pool, cudaMemPoolAttrReleaseThreshold, &keep));
+  }
+  *out = p.release();
+  return BF_OK;
+}
+
+void bf_pcs_free(bf_pcs* pcs) {
+  if (!pcs) return;
+  if (pcs->device < 0) {
+    delete pcs;
+    return;
+  }
+  DeviceGuard g(pcs->device);
+  delete pcs;
+}
+
+size_t bf_pcs_num_queries(const bf_pcs* pcs) { return pcs ? pcs->Q : 0; }
+
+size_t bf_pcs_proof_size(const bf_pcs* p, size_t width, int n_evals) {
+  if (!p) return 0;
+  if (n_evals == 0) return 32;
+  return 8 + (size_t)p->d * 40 + 24 + 8 + 32 * (size_t)p->d + 8 + p->Q * p->block_bytes(width);
+}
+
+int bf_commit(bf_pcs* p, const uint8_t* evals, size_t width, bf_commitment** out, uint8_t root[32]) {
+  if (!p || !evals || !out) return fail(BF_ERR_ARG, "null argument");
+  if (p->device < 0) return fail(BF_ERR_ARG, "verifier-only pcs (device < 0)");
+  *out = nullptr;
+  if (width != 1) return fail(BF_ERR_UNSUPPORTED, "width %zu: only width 1 runs on the GPU in this build", width);
+  DeviceGuard g(p->device);
+  std::unique_ptr<bf_commitment> cm(new bf_commitment());
+  cm->pcs = p;
+  cm->width = width;
+  const size_t n = (size_t)1 << p->d;
+  CU(cm->data.alloc_async(16 * n * width, p->pool, p->stream));
+  CU(cudaMemcpyAsync(cm->data.p, evals, 16 * n * width, cudaMemcpyHostToDevice, p->stream));
+  TRY(commit_device(p, cm.get(), cm->data.as<uint4>()));
+  if (root) std::memcpy(root, cm->root, 32);
+  *out = cm.release();
+  return BF_OK;
+}
+
+int bf_commit_device(bf_pcs* p, const void* d_evals, size_t width, bf_commitment** out, uint8_t root[32]) {
+  if (!p || !d_evals || !out) return fail(BF_ERR_ARG, "null argument");
+  if (p->device < 0) return fail(BF_ERR_ARG, "verifier-only pcs (device < 0)");
+  *out = nullptr;
+  if (width != 1) return fail(BF_ERR_UNSUPPORTED, "width %zu: only width 1 runs on the GPU in this build", width);
+  if (reinterpret_cast<uintptr_t>(d_evals) & 15) return fail(BF_ERR_ARG, "device evaluations must be 16-byte aligned");
+  DeviceGuard g(p->device);
+  std::unique_ptr<bf_commitment> cm(new bf_commitment());
+  cm->pcs = p;
+  cm->width = width;
+  cm->data.p = const_cast<void*>(d_evals);
+  cm->data.owned = false;
+  cm->data.bytes = 16 * ((size_t)1 << p->d) * width;
+  TRY(commit_device(p, cm.get(), reinterpret_cast<const uint4*>(d_evals)));
+  if (root) std::memcpy(root, cm->root, 32);
+  *out = cm.release();
+  return BF_OK;
+}
+
+void bf_commitment_free(bf_commitment* cm) {
+  if (!cm) return;
+  DeviceGuard g(cm->pcs->device);
+  delete cm;  // buffers return to the pcs's pool in stream order
+}
+
+int bf_commitment_root(const bf_commitment* cm, uint8_t root[32]) {
+  if (!cm || !root) return fail(BF_ERR_ARG, "null argument");
+  std::memcpy(root, cm->root, 32);
+  return BF_OK;
+}
+
+int bf_commitment_data(const bf_commitment* cm, uint8_t* evals, size_t cap) {
+  if (!cm || !evals) return fail(BF_ERR_ARG, "null argument");
+  if (cap < cm->data.bytes) return fail(BF_ERR_BUFFER, "need %zu bytes", cm->data.bytes);
+  DeviceGuard g(cm->pcs->device);
+  CU(cudaMemcpyAsync(evals, cm->data.p, cm->data.bytes, cudaMemcpyDeviceToHost, cm->pcs->stream));
+  CU(cudaStreamSynchronize(cm->pcs->stream));
+  return BF_OK;
+}
+
+int bf_eval(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, uint8_t* values) {
+  if (!p || !cm || !values || (p->d > 0 && !point)) return fail(BF_ERR_ARG, "null argument");
+  if (cm->width != 1) return fail(BF_ERR_UNSUPPORTED, "width != 1");
+  DeviceGuard g(p->device);
+  const int d = p->d;
+  const uint4* data = cm->data.as<uint4>();
+  if (d == 0) {
+    CU(cudaMemcpyAsync(p->pinned.b(), data, 16, cudaMemcpyDeviceToHost, p->stream));
+  } else {
+    const size_t half = (size_t)1 << (d - 1);
+    if (p->eval_ws.bytes < 16 * half) CU(p->eval_ws.alloc(16 * half));
+    uint4* w = p->eval_ws.as<uint4>();
+    // MultiPoly::evaluate (multilinear.rs:124-141): fix the top variable with
+    // the last coordinate, repeatedly.
+    const uint4* in = data;
+    for (int k = d - 1; k >= 0; --k) {
+      uint4 r;
+      std::memcpy(&r, point + 16 * k, 16);
+      ProfScope ps(p->prof, p->stream, P_FIX);
+      CU(bf::launch_fix(in, w, (size_t)1 << k, r, nullptr, 0, nullptr, p->stream));
+      in = w;
+    }
+    CU(cudaMemcpyAsync(p->pinned.b(), w, 16, cudaMemcpyDeviceToHost, p->stream));
+  }
+  CU(cudaStreamSynchronize(p->stream));
+  p->prof.drain();
+  std::memcpy(values, p->pinned.b(), 16);
+  return BF_OK;
+}
+
+// ---- challenger -----------------------------------------------------------
+int bf_challenger_new(const uint8_t* initial_state, size_t len, bf_challenger** out) {
+  if (!out || (len && !initial_state)) return fail(BF_ERR_ARG, "null argument");
+  bf_challenger* c = new bf_challenger();
+  if (len) c->c.in.assign(initial_state, initial_state + len);
+  *out = c;
+  return BF_OK;
+}
+int bf_challenger_clone(const bf_challenger* ch, bf_challenger** out) {
+  if (!ch || !out) return fail(BF_ERR_ARG, "null argument");
+  *out = new bf_challenger(*ch);
+  return BF_OK;
+}
+void bf_challenger_free(bf_challenger* ch) { delete ch; }
+int bf_challenger_observe(bf_challenger* ch, const uint8_t* bytes, size_t len) {
+  if (!ch || (len && !bytes)) return fail(BF_ERR_ARG, "null argument");
+  ch->c.observe(bytes, len);
+  return BF_OK;
+}
+int bf_challenger_sample_ext(bf_challenger* ch, uint8_t out[16]) {
+  if (!ch || !out) return fail(BF_ERR_ARG, "null argument");
+  bfh::store(out, ch->c.sample_elem());
+  return BF_OK;
+}
+int bf_challenger_sample_bits(bf_challenger* ch, int bits, uint64_t* out) {
+  if (!ch || !out || bits < 0 || bits > 64) return fail(BF_ERR_ARG, "bad argument");
+  *out = ch->c.sample_bits(bits);
+  return BF_OK;
+}
+int bf_challenger_state(const bf_challenger* ch, uint8_t* buf, size_t cap, size_t* len) {
+  if (!ch || !len) return fail(BF_ERR_ARG, "null argument");
+  std::vector<uint8_t> b = ch->c.blob();
+  *len = b.size();
+  if (!buf || cap < b.size()) return fail(BF_ERR_BUFFER, "need %zu bytes", b.size());
+  std::memcpy(buf, b.data(), b.size());
+  return BF_OK;
+}
+int bf_challenger_from_state(const uint8_t* buf, size_t len, bf_challenger** out) {
+  if (!buf || !out) return fail(BF_ERR_ARG, "null argument");
+  bf_challenger* c = new bf_challenger();
+  if (!c->c.from_blob(buf, len)) {
+    delete c;
+    return fail(BF_ERR_ARG, "malformed challenger state");
+  }
+  *out = c;
+  return BF_OK;
+}
+
+// ---- profiling ---------------------------------------------------------------
+int bf_profile_enable(bf_pcs* p, int on) {
+  if (!p) return fail(BF_ERR_ARG, "null argument");
+  p->prof.on = on != 0;
+  for (int k = 0; k < kProfClasses; ++k) {
+    p->prof.ms[k] = 0;
+    p->prof.count[k] = 0;
+  }
+  return BF_OK;
+}
+int bf_profile_read(bf_pcs* p, double* ms, uint64_t* launches, int nclasses) {
+  if (!p || p->device < 0) return fail(BF_ERR_ARG, "null argument or verifier-only pcs");
+  DeviceGuard g(p->device);
+  CU(cudaStreamSynchronize(p->stream));
+  p->prof.drain();
+  for (int k = 0; k < nclasses && k < kProfClasses; ++k) {
+    if (ms) ms[k] = p->prof.ms[k];
+    if (launches) launches[k] = p->prof.count[k];
+  }
+  return BF_OK;
+}
+
+// ---- test hooks --------------------------------------------------------------
+int bf_test_gf_mul(int device, const uint8_t* a, const uint8_t* b, uint8_t* out, size_t n) {
+  if (!a || !b || !out) return fail(BF_ERR_ARG, "null argument");
+  CU(cudaSetDevice(device));
+  DevBuf da, db, dc;
+  CU(da.alloc(16 * n));
+  CU(db.alloc(16 * n));
+  CU(dc.alloc(16 * n));
+  CU(cudaMemcpy(da.p, a, 16 * n, cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(db.p, b, 16 * n, cudaMemcpyHostToDevice));
+  CU(bf::launch_test_mul(da.as<uint4>(), db.as<uint4>(), dc.as<uint4>(), n, 0));
+  CU(cudaMemcpy(out, dc.p, 16 * n, cudaMemcpyDeviceToHost));
+  return BF_OK;
+}
+
+int bf_test_keccak_f(int device, uint64_t* states, size_t n) {
+  if (!states) return fail(BF_ERR_ARG, "null argument");
+  CU(cudaSetDevice(device));
+  DevBuf ds;
+  CU(ds.alloc(200 * n));
+  CU(cudaMemcpy(ds.p, states, 200 * n, cudaMemcpyHostToDevice));
+  CU(bf::launch_test_keccak(ds.as<uint2>(), n, 0));
+  CU(cudaMemcpy(states, ds.p, 200 * n, cudaMemcpyDeviceToHost));
+  return BF_OK;
+}
+
+}  // extern "C"

@@ -26,14 +26,19 @@ cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t w
                           cudaStream_t st);
 cudaError_t launch_leaves_elem(const uint4* cw, uint4* leaves, size_t n, size_t width, cudaStream_t st);
 cudaError_t launch_leaves_pair(const uint4* pi, uint4* leaves, size_t n, cudaStream_t st);
+cudaError_t launch_leaves_cw_pairs(const uint4* cw, uint4* leaves, uint4* pair_leaves, size_t n_pairs,
+                                   cudaStream_t st);
 // Build every level above `leaves` (n leaves, power of two); levels are stored
-// one after another right after the leaves.  Root = last digest.
-cudaError_t launch_tree(uint4* leaves, size_t n, cudaStream_t st);
+// one after another right after the leaves.  Root = last digest, also copied
+// to `root_out` (32 bytes) when it is not null.
+cudaError_t launch_tree(uint4* leaves, size_t n, cudaStream_t st, uint4* root_out = nullptr);
 
 cudaError_t launch_eq_table(const uint4* r, int nvars, uint4* out, uint4* tmp_lo, uint4* tmp_hi, cudaStream_t st);
 cudaError_t launch_dot_xor(const uint4* x, const uint4* y, size_t n, uint32_t* acc, cudaStream_t st);
 cudaError_t launch_fold(const uint4* pi, uint4* out, size_t n_out, const uint4* tw_lo, const uint4* tw_hi, uint4 r,
                         cudaStream_t st);
+cudaError_t launch_fold_leaves(const uint4* pi, uint4* out, uint4* leaves, size_t n_leaves, const uint4* tw_lo,
+                               const uint4* tw_hi, uint4 r, cudaStream_t st);
 cudaError_t launch_fix(const uint4* in, uint4* out, size_t half, uint4 r, const uint4* heq, size_t next_half,
                        uint32_t* acc, cudaStream_t st);
 cudaError_t launch_combine_rows(const uint4* rows, size_t nrows, size_t width, const uint4* scalars, uint4* out,
@@ -43,9 +48,10 @@ cudaError_t launch_combine_rows(const uint4* rows, size_t nrows, size_t width, c
 struct GatherParams {
   const uint4* cw;         // codeword, NTT order, rows of `width`
   const uint4* cw_tree;    // codeword tree, reversed storage per level
-  const uint4* pi_first;   // folded codeword of the first round (= cw when width is 1)
-  const uint4* pi_fold;    // folded codewords of rounds d-1 .. 0, one after another
-  const uint4* pi_trees;   // their trees, one after another
+  const uint4* pi_first;       // folded codeword of the first round (= cw when width is 1)
+  const uint4* pi_first_tree;  // its tree
+  const uint4* pi_fold;        // outputs of the folds of rounds d-1 .. 0, one after another
+  const uint4* pi_trees;       // trees of rounds d-2 .. 0, one after another
   const uint64_t* idx;     // query positions
   uint8_t* out;            // Q blocks of `block_bytes`
   size_t width;

@@ -27,15 +27,24 @@ __device__ __forceinline__ uint4 gf_add(uint4 a, uint4 b) {
 
 __device__ __forceinline__ bool gf_is_zero(uint4 a) { return (a.x | a.y | a.z | a.w) == 0; }
 
-// Carry-less 32 x 32 -> 64.
+__device__ __forceinline__ uint64_t mulw(uint32_t a, uint32_t b) { return (uint64_t)a * b; }
+__device__ __forceinline__ uint64_t madw(uint32_t a, uint32_t b, uint64_t c) { return (uint64_t)a * b + c; }
+
+// Carry-less 32 x 32 -> 64.  a_i / b_i keep the bits of residue i mod 4; the
+// product a_i * b_j only has terms at positions of residue i + j, at most 8
+// per position.  Two products of the same residue may be ADDED (one integer
+// multiply-add, no XOR) whenever their combined count stays <= 15 at every
+// position, which holds for the pairs grouped below (checked exhaustively
+// over positions with all-ones operands, the worst case); the remaining
+// terms are XORed.
 __device__ __forceinline__ uint64_t clmul32(uint32_t a, uint32_t b) {
   const uint32_t m0 = 0x11111111u, m1 = 0x22222222u, m2 = 0x44444444u, m3 = 0x88888888u;
   const uint32_t a0 = a & m0, a1 = a & m1, a2 = a & m2, a3 = a & m3;
   const uint32_t b0 = b & m0, b1 = b & m1, b2 = b & m2, b3 = b & m3;
-  const uint64_t z0 = ((uint64_t)a0 * b0) ^ ((uint64_t)a1 * b3) ^ ((uint64_t)a2 * b2) ^ ((uint64_t)a3 * b1);
-  const uint64_t z1 = ((uint64_t)a0 * b1) ^ ((uint64_t)a1 * b0) ^ ((uint64_t)a2 * b3) ^ ((uint64_t)a3 * b2);
-  const uint64_t z2 = ((uint64_t)a0 * b2) ^ ((uint64_t)a1 * b1) ^ ((uint64_t)a2 * b0) ^ ((uint64_t)a3 * b3);
-  const uint64_t z3 = ((uint64_t)a0 * b3) ^ ((uint64_t)a1 * b2) ^ ((uint64_t)a2 * b1) ^ ((uint64_t)a3 * b0);
+  const uint64_t z0 = madw(a1, b3, mulw(a0, b0)) ^ mulw(a2, b2) ^ mulw(a3, b1);
+  const uint64_t z1 = madw(a2, b3, mulw(a0, b1)) ^ madw(a3, b2, mulw(a1, b0));
+  const uint64_t z2 = madw(a3, b3, mulw(a0, b2)) ^ mulw(a1, b1) ^ mulw(a2, b0);
+  const uint64_t z3 = mulw(a0, b3) ^ mulw(a1, b2) ^ mulw(a2, b1) ^ mulw(a3, b0);
   return (z0 & 0x1111111111111111ull) | (z1 & 0x2222222222222222ull) | (z2 & 0x4444444444444444ull) |
          (z3 & 0x8888888888888888ull);
 }

@@ -38,6 +38,10 @@ __device__ __forceinline__ uint2 kx5(uint2 a, uint2 b, uint2 c, uint2 d, uint2 e
 __device__ __forceinline__ uint2 kchi(uint2 a, uint2 b, uint2 c) {
   return make_uint2(a.x ^ (~b.x & c.x), a.y ^ (~b.y & c.y));
 }
+// 64-bit rotation by R in two funnel shifts.  (Measured on GB300: funnel
+// shifts, LOP3 and IADD3 all issue at half rate on the ALU pipe; a rotation
+// rebuilt from integer multiplies needs the quarter-rate IMAD.HI/IMAD.WIDE
+// forms and was slower, so rotations stay on the ALU pipe.)
 template <int R>
 __device__ __forceinline__ uint2 krol(uint2 v) {
   if constexpr (R == 0) {
@@ -94,9 +98,41 @@ __device__ __forceinline__ void keccak_round(uint2 s[25], uint2 rc) {
   s[0] = kx2(s[0], rc);
 }
 
+// Last round when only the 32-byte digest (lanes 0..3) is wanted: theta is
+// still needed in full, but rho/pi/chi only for the five lanes of row y = 0.
+__device__ __forceinline__ void keccak_round_digest(uint2 s[25], uint2 rc) {
+  uint2 C[5], D[5];
+#pragma unroll
+  for (int x = 0; x < 5; ++x) C[x] = kx5(s[x], s[x + 5], s[x + 10], s[x + 15], s[x + 20]);
+#pragma unroll
+  for (int x = 0; x < 5; ++x) D[x] = krol<1>(C[(x + 1) % 5]);
+  // row y = 0 of b takes lanes 0, 6, 12, 18, 24
+  const uint2 b0 = kx3(s[0], C[4], D[0]);
+  const uint2 b1 = krol<44>(kx3(s[6], C[0], D[1]));
+  const uint2 b2 = krol<43>(kx3(s[12], C[1], D[2]));
+  const uint2 b3 = krol<21>(kx3(s[18], C[2], D[3]));
+  const uint2 b4 = krol<14>(kx3(s[24], C[3], D[4]));
+  s[0] = kx2(kchi(b0, b1, b2), rc);
+  s[1] = kchi(b1, b2, b3);
+  s[2] = kchi(b2, b3, b4);
+  s[3] = kchi(b3, b4, b0);
+}
+
+// Full permutation.  The first round is peeled so that the compiler folds
+// the lanes a fixed-length message leaves constant (zero or padding).
 __device__ __forceinline__ void keccak_f1600(uint2 s[25]) {
+  keccak_round(s, c_keccak_rc[0]);
 #pragma unroll 2
-  for (int r = 0; r < 24; ++r) keccak_round(s, c_keccak_rc[r]);
+  for (int r = 1; r < 23; ++r) keccak_round(s, c_keccak_rc[r]);
+  keccak_round(s, c_keccak_rc[23]);
+}
+
+// Permutation whose output is only read in lanes 0..3.
+__device__ __forceinline__ void keccak_f1600_digest(uint2 s[25]) {
+  keccak_round(s, c_keccak_rc[0]);
+#pragma unroll 2
+  for (int r = 1; r < 23; ++r) keccak_round(s, c_keccak_rc[r]);
+  keccak_round_digest(s, c_keccak_rc[23]);
 }
 
 // Absorb `nlanes` message lanes (already in s[0..nlanes)), pad and permute.
@@ -110,7 +146,7 @@ __device__ __forceinline__ void keccak256_lanes(uint2 s[25], int nlanes) {
   for (int i = 0; i < 17; ++i)
     if (i == nlanes) s[i].x ^= 0x01u;
   s[16].y ^= 0x80000000u;
-  keccak_f1600(s);
+  keccak_f1600_digest(s);
 }
 
 struct Digest {

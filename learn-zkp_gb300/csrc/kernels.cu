@@ -170,6 +170,21 @@ __global__ void __launch_bounds__(128) leaves_elem_kernel(const uint4* __restric
     store_digest(leaves, i, hash_elem(cw[i]));
 }
 
+// Codeword leaves H(cw[q]) together with the leaves of the first round's
+// folded-codeword tree H(cw[2s] || cw[2s+1]) (for width 1 the first round
+// commits the codeword itself as pairs, basefold.rs:159-165,350-355): both
+// read the same 32 bytes.
+__global__ void __launch_bounds__(128) leaves_cw_pairs_kernel(const uint4* __restrict__ cw,
+                                                              uint4* __restrict__ leaves,
+                                                              uint4* __restrict__ pair_leaves, size_t n_pairs) {
+  for (size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x; s < n_pairs; s += (size_t)gridDim.x * blockDim.x) {
+    const uint4 e0 = cw[2 * s], e1 = cw[2 * s + 1];
+    store_digest(leaves, 2 * s, hash_elem(e0));
+    store_digest(leaves, 2 * s + 1, hash_elem(e1));
+    store_digest(pair_leaves, s, hash_pair(e0, e1));
+  }
+}
+
 // Folded-codeword leaf s = H(pi[2s] || pi[2s+1]): the row (pi[j], pi[j+n_i])
 // of the width-2 matrix committed at basefold.rs:350-355, in NTT order.
 __global__ void __launch_bounds__(128) leaves_pair_kernel(const uint4* __restrict__ pi, uint4* __restrict__ leaves,
@@ -184,8 +199,9 @@ __global__ void __launch_bounds__(128) level_kernel(const uint4* __restrict__ pr
     store_digest(next, s, hash_node(load_digest(prev, s), load_digest(prev, s + n_next)));
 }
 
-// The remaining levels of a small tree, in one block.
-__global__ void __launch_bounds__(256) tree_top_kernel(uint4* level, size_t n) {
+// The remaining levels of a small tree, in one block; the root is also
+// copied to `root_out` when given.
+__global__ void __launch_bounds__(256) tree_top_kernel(uint4* level, size_t n, uint4* root_out) {
   uint4* cur = level;
   while (n > 1) {
     const size_t h = n >> 1;
@@ -196,11 +212,19 @@ __global__ void __launch_bounds__(256) tree_top_kernel(uint4* level, size_t n) {
     cur = nxt;
     n = h;
   }
+  if (root_out && threadIdx.x == 0) store_digest(root_out, 0, load_digest(cur, 0));
 }
 
 cudaError_t launch_leaves_elem(const uint4* cw, uint4* leaves, size_t n, size_t width, cudaStream_t st) {
   if (width != 1) return cudaErrorInvalidValue;
   leaves_elem_kernel<<<grid_for(n, 128, 16), 128, 0, st>>>(cw, leaves, n);
+  COUNT_LAUNCH();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_leaves_cw_pairs(const uint4* cw, uint4* leaves, uint4* pair_leaves, size_t n_pairs,
+                                   cudaStream_t st) {
+  leaves_cw_pairs_kernel<<<grid_for(n_pairs, 128, 16), 128, 0, st>>>(cw, leaves, pair_leaves, n_pairs);
   COUNT_LAUNCH();
   return cudaGetLastError();
 }
@@ -213,7 +237,7 @@ cudaError_t launch_leaves_pair(const uint4* pi, uint4* leaves, size_t n, cudaStr
 
 constexpr size_t kTopNodes = 512;
 
-cudaError_t launch_tree(uint4* leaves, size_t n, cudaStream_t st) {
+cudaError_t launch_tree(uint4* leaves, size_t n, cudaStream_t st, uint4* root_out) {
   uint4* cur = leaves;
   while (n > kTopNodes) {
     const size_t h = n >> 1;
@@ -225,8 +249,8 @@ cudaError_t launch_tree(uint4* leaves, size_t n, cudaStream_t st) {
     cur = nxt;
     n = h;
   }
-  if (n > 1) {
-    tree_top_kernel<<<1, 256, 0, st>>>(cur, n);
+  if (n > 1 || root_out) {
+    tree_top_kernel<<<1, 256, 0, st>>>(cur, n, root_out);
     COUNT_LAUNCH();
   }
   return cudaGetLastError();
@@ -312,6 +336,36 @@ __global__ void __launch_bounds__(256) fold_kernel(const uint4* __restrict__ pi,
     lo = gf_add(lo, gf_mul(hi, tw));
     out[t] = gf_add(lo, gf_mul(gf_add(hi, lo), r));
   }
+}
+
+// Fold fused with the next round's leaf hashing: thread s folds the four
+// entries pi[4s..4s+3] into out[2s], out[2s+1] and hashes that pair, which is
+// leaf s of the next round's folded-codeword tree.
+__global__ void __launch_bounds__(128) fold_leaves_kernel(const uint4* __restrict__ pi, uint4* __restrict__ out,
+                                                          uint4* __restrict__ leaves, size_t n_leaves,
+                                                          const uint4* __restrict__ tlo,
+                                                          const uint4* __restrict__ thi, uint4 r) {
+  for (size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x; s < n_leaves; s += (size_t)gridDim.x * blockDim.x) {
+    uint4 f[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const size_t t = 2 * s + k;
+      const uint4 tw = gf_add(tlo[t & 4095], thi[t >> 12]);
+      uint4 lo = pi[2 * t], hi = pi[2 * t + 1];
+      hi = gf_add(hi, lo);
+      lo = gf_add(lo, gf_mul(hi, tw));
+      f[k] = gf_add(lo, gf_mul(gf_add(hi, lo), r));
+      out[t] = f[k];
+    }
+    store_digest(leaves, s, hash_pair(f[0], f[1]));
+  }
+}
+
+cudaError_t launch_fold_leaves(const uint4* pi, uint4* out, uint4* leaves, size_t n_leaves, const uint4* tw_lo,
+                               const uint4* tw_hi, uint4 r, cudaStream_t st) {
+  fold_leaves_kernel<<<grid_for(n_leaves, 128, 16), 128, 0, st>>>(pi, out, leaves, n_leaves, tw_lo, tw_hi, r);
+  COUNT_LAUNCH();
+  return cudaGetLastError();
 }
 
 cudaError_t launch_fold(const uint4* pi, uint4* out, size_t n_out, const uint4* tw_lo, const uint4* tw_hi, uint4 r,
@@ -409,14 +463,17 @@ __global__ void gather_kernel(GatherParams p) {
     const uint64_t ii = idx & (ni - 1);
     const uint64_t sib = ((idx >> (Li - 1)) & 1) ^ 1;
     const uint4* pi;
+    const uint4* tree;
     if (k == 0) {
       pi = p.pi_first;
+      tree = p.pi_first_tree;
     } else {
-      // output of round i+1 sits after the outputs of rounds d-1 .. i+2
+      // input of round i = output of round i+1, after the outputs of rounds d-1 .. i+2
       pi = p.pi_fold + c * (((size_t)1 << d) - ((size_t)1 << (i + 2)));
+      // trees of rounds d-2 .. i+1 come first
+      tree = p.pi_trees +
+             2 * ((c << 1) * (((size_t)1 << (d - 1)) - ((size_t)1 << (i + 1))) - (size_t)(d - 2 - i));
     }
-    const size_t tree_off = (c << 1) * (((size_t)1 << d) - ((size_t)1 << (i + 1))) - (size_t)(d - 1 - i);
-    const uint4* tree = p.pi_trees + 2 * tree_off;
     if (threadIdx.x == 0) {
       put_elem(out, off, pi[2 * brev_bits64(ii, Li - 1) + sib]);
       put_u64(out, off + 16, (uint64_t)(Li - 1));
