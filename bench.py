@@ -39,6 +39,7 @@ def parse():
     ap.add_argument("--n", type=int, default=24, help="log2 of the number of evaluations")
     ap.add_argument("--log2-c", type=int, default=1, help="log2 of the blowup")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the batched and served workloads")
     ap.add_argument("--profile-only", action="store_true", help="warmup + steps, no JSON extras (for ncu)")
     return ap.parse_args()
 
@@ -198,6 +199,110 @@ def run_reference(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+def gen_inputs(sizes, seed):
+    """One synthetic input per distinct size (reused by jobs of that size)."""
+    from basefold_gpu import rand
+
+    inputs = {}
+    for n in sorted(set(sizes)):
+        data = rand.random_elems((1 << n) + n, seed + n)
+        inputs[n] = (data[: 1 << n], data[1 << n:])
+    return inputs
+
+
+def run_batched(bg, torch, device, log2_c, count=256, lo=10, hi=22, seed=4):
+    """Config 4: `count` polynomials with sizes log-uniform in 2^lo..2^hi.
+    Plain = commit/eval/open one at a time through the public API; batched =
+    the engine with all jobs in flight.  Inputs device-resident in both."""
+    import hashlib
+
+    import numpy as np
+
+    sizes = [int(x) for x in np.random.default_rng(seed).integers(lo, hi + 1, count)]
+    inputs = gen_inputs(sizes, 1000)
+    dev = {n: torch.from_numpy(ev).to(f"cuda:{device}") for n, (ev, _) in inputs.items()}
+    pcs = {n: bg.Basefold.setup(bg.BasefoldConfig(bg.BinaryReedSolomonCode(128, log2_c, n)), device=device)
+           for n in inputs}
+
+    def plain_one(n):
+        comm = pcs[n].commit_device(dev[n].data_ptr(), keep=dev[n])
+        ch = bg.GenericChallenger.keccak256()
+        ch.observe(comm.root)
+        vals = pcs[n].eval(pcs[n].data(comm), inputs[n][1])
+        ch.observe_ext_slice(vals)
+        proof = pcs[n].open(comm, [bg.PolyEvals(vals, inputs[n][1])], ch)
+        comm.free()
+        return proof
+
+    for n in inputs:  # warm every size
+        plain_one(n)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    plain = [plain_one(n) for n in sizes]
+    torch.cuda.synchronize()
+    t_plain = time.perf_counter() - t
+    eng = bg.Engine(device=device, log2_c=log2_c, max_inflight=32)
+    jobs = [(n, dev[n].data_ptr(), inputs[n][1]) for n in sizes]
+    eng.prove(jobs[:32], device_input=True)  # warm
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    res = eng.prove(jobs, device_input=True)
+    torch.cuda.synchronize()
+    t_batch = time.perf_counter() - t
+    identical = all(r["proof"] == p for r, p in zip(res, plain))
+    digest = hashlib.sha256(b"".join(hashlib.sha256(p).digest() for p in plain)).hexdigest()
+    return {"workload": f"{count} polys, sizes log-uniform 2^{lo}..2^{hi} (seed {seed}), blowup {1 << log2_c}",
+            "plain_proofs_per_s": count / t_plain, "batched_proofs_per_s": count / t_batch,
+            "speedup": t_plain / t_batch, "proofs_identical": identical, "proofs_sha256": digest,
+            "plain_s": t_plain, "batched_s": t_batch, "max_inflight": 32,
+            "note": "batched = engine with per-stream job state machines (continuous batching), not one fused launch"}
+
+
+def run_served(bg, device, log2_c, lo=12, hi=24, per_level=48, loads=(0.25, 0.5, 0.9), seed=5):
+    """Config 5: open-loop Poisson arrivals, sizes log-uniform 2^lo..2^hi, host
+    inputs (H2D inside), at fractions of the measured capacity."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    inputs = gen_inputs(list(range(lo, hi + 1)), 2000)
+    eng = bg.Engine(device=device, log2_c=log2_c, max_inflight=16)
+    # capacity: saturated batch of the same size distribution
+    cap_sizes = [int(x) for x in rng.integers(lo, hi + 1, per_level)]
+    eng.prove([(n, inputs[n][0], inputs[n][1]) for n in cap_sizes[:8]])
+    t = time.perf_counter()
+    eng.prove([(n, inputs[n][0], inputs[n][1]) for n in cap_sizes])
+    capacity = per_level / (time.perf_counter() - t)
+    out = {"workload": f"Poisson arrivals, sizes log-uniform 2^{lo}..2^{hi}, blowup {1 << log2_c}, "
+                       f"{per_level} requests per load, host inputs", "capacity_proofs_per_s": capacity,
+           "levels": []}
+    eng.start()
+    for load in loads:
+        rate = load * capacity
+        sizes = [int(x) for x in rng.integers(lo, hi + 1, per_level)]
+        gaps = rng.exponential(1.0 / rate, per_level)
+        lat, done = [], 0
+        t0 = time.perf_counter()
+        t_next = t0
+        for k, n in enumerate(sizes):
+            t_next += gaps[k]
+            while time.perf_counter() < t_next:
+                for _, r in eng.poll():
+                    lat.append(r["latency_ms"])
+                time.sleep(0.0002)
+            eng.submit(n, inputs[n][0], inputs[n][1], tag=k)
+        while len(lat) < per_level:
+            for _, r in eng.poll():
+                lat.append(r["latency_ms"])
+            time.sleep(0.0005)
+        elapsed = time.perf_counter() - t0
+        lat.sort()
+        out["levels"].append({"offered_load": load, "offered_rate_per_s": rate, "achieved_proofs_per_s":
+                              per_level / elapsed, "p50_ms": lat[len(lat) // 2],
+                              "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))], "max_ms": lat[-1]})
+    eng.stop()
+    return out
+
+
 def workload_config(args):
     return {"workload": f"plain Basefold commit+eval+open, 2^{args.n} evaluations, blowup {1 << args.log2_c}, "
                         "width 1, lambda 128, Keccak-256 Merkle",
@@ -307,6 +412,10 @@ def main():
     if tr and tr.get("bytes_per_node"):
         traffic = tr["bytes_per_node"] * nodes / max(tree_launches, 1)
     total_ms_classes = sum(v[0] for v in prof.values())
+    batched = served = None
+    if ws == 1 and not args.no_extras:
+        batched = run_batched(bg, torch, local, log2_c)
+        served = run_served(bg, local, log2_c)
     cpu = None
     if not args.no_cpu_baseline and ws == 1:
         t = cpu_step_oracle(n, log2_c)
@@ -333,6 +442,8 @@ def main():
         "clocks": clk.summary(),
         "gpu_launches": launches,
         "proof_bytes": len(proof),
+        "batched": batched,
+        "served": served,
     }
     print(json.dumps(line), flush=True)
 

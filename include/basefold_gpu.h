@@ -55,6 +55,22 @@ typedef struct bf_pcs bf_pcs;
 typedef struct bf_commitment bf_commitment;
 typedef struct bf_challenger bf_challenger;
 typedef struct bf_open_session bf_open_session;
+typedef struct bf_engine bf_engine;
+
+/* One commit + eval + open job of the engine (the reference harness,
+ * poly-commit/src/lib.rs:80-100, with GenericChallenger::keccak256()). */
+typedef struct {
+  int32_t num_vars;      /* in: log2 of the number of evaluations */
+  int32_t status;        /* out: 0 done, 1 pending, < 0 BF_ERR_* */
+  const void* evals;     /* in: 2^num_vars elements (host or device memory) */
+  const uint8_t* point;  /* in: num_vars elements, host memory */
+  uint8_t* proof;        /* in: caller buffer for the bincode proof */
+  size_t proof_cap;      /* in: its size (bf_engine_proof_size) */
+  size_t proof_len;      /* out */
+  double latency_ms;     /* out: submission to completion */
+  uint8_t root[32];      /* out: commitment */
+  uint8_t value[16];     /* out: evaluation at the point */
+} bf_job;
 
 /* Text of the last error on this thread (NUL-terminated, truncated to len). */
 int bf_last_error(char* buf, size_t len);
@@ -130,6 +146,25 @@ int bf_open_final(bf_open_session* s, uint8_t final_poly[16]);
 int bf_open_finish(bf_open_session* s, const uint64_t* indices, size_t nq, uint8_t* proof, size_t cap,
                    size_t* proof_len);
 void bf_open_session_free(bf_open_session* s);
+
+/* ---- Prover engine: many jobs of different sizes in flight at once.
+ * Jobs run as per-stream state machines; the engine admits them while
+ * streams (max_inflight) and the HBM budget (mem_budget bytes, 0 = 80% of
+ * free memory) allow, and advances whichever job's GPU step has finished, so
+ * requests also join between the rounds of running ones.  Proofs are
+ * identical to bf_commit/bf_eval/bf_open one at a time.  (No counterpart in
+ * the reference, which proves one polynomial at a time on the CPU.)
+ * bf_engine_prove: runs `count` jobs to completion on the calling thread.
+ * bf_engine_start/stop + submit/poll: serving from a background thread;
+ *   submitted bf_job structs must stay valid until returned by poll. */
+int bf_engine_create(int device, int lambda, int log2_c, int max_inflight, size_t mem_budget, bf_engine** out);
+void bf_engine_free(bf_engine* e);
+size_t bf_engine_proof_size(bf_engine* e, int num_vars);
+int bf_engine_prove(bf_engine* e, bf_job* jobs, size_t count, int device_input);
+int bf_engine_start(bf_engine* e);
+int bf_engine_stop(bf_engine* e);
+int bf_engine_submit(bf_engine* e, bf_job* job, int device_input);
+int bf_engine_poll(bf_engine* e, bf_job** done, size_t cap, size_t* n);
 
 /* ---- PolyCommitScheme::verify (lib.rs:44-50; basefold.rs:234-324) on the
  * host.  Returns BF_VERIFY_* (>= 0) or a negative BF_ERR_*. */

@@ -15,12 +15,12 @@ import ctypes as C
 
 import numpy as np
 
-from ._native import BasefoldGpuError, check, lib  # noqa: F401
+from ._native import BasefoldGpuError, BfJob, check, lib  # noqa: F401
 from . import rand  # noqa: F401
 
 __all__ = [
     "Basefold", "BasefoldConfig", "BinaryReedSolomonCode", "BasefoldError", "BasefoldGpuError", "CommitmentData",
-    "GenericChallenger", "PolyEvals", "prove_sumcheck", "rand",
+    "Engine", "GenericChallenger", "PolyEvals", "prove_sumcheck", "rand",
 ]
 
 _u8p = C.c_void_p
@@ -366,6 +366,95 @@ class OpenSession:
         L = self._pcs.config.code.log2_c + self._pcs.config.code.d
         idx = [challenger.sample_bits(L) for _ in range(self._pcs.num_queries())]
         return self.finish(idx)
+
+
+class Engine:
+    """Many commit+eval+open jobs of different sizes in flight on one GPU.
+
+    Each job is the reference's harness (commit, observe root, eval at the
+    point, observe the value, open with GenericChallenger::keccak256());
+    results are identical to Basefold.commit/eval/open one at a time.
+    `prove` runs a batch to completion; `start`/`submit`/`poll`/`stop` serve
+    requests from a background thread (continuous batching)."""
+
+    def __init__(self, device: int = 0, lambda_: int = 128, log2_c: int = 1, max_inflight: int = 16,
+                 mem_budget: int = 0):
+        h = C.c_void_p()
+        check(lib().bf_engine_create(device, lambda_, log2_c, max_inflight, mem_budget, C.byref(h)))
+        self._h, self.log2_c = h, log2_c
+        self._keep = {}
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                lib().bf_engine_free(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def proof_size(self, num_vars: int) -> int:
+        return int(lib().bf_engine_proof_size(self._h, num_vars))
+
+    def _job(self, num_vars, evals, point, device_input):
+        job = BfJob()
+        job.num_vars = num_vars
+        if device_input:
+            job.evals = int(evals)
+            ev = None
+        else:
+            ev = _elems(evals, 1 << num_vars)
+            job.evals = ev.ctypes.data
+        pt = _elems(point, num_vars) if num_vars else np.zeros((1, 16), np.uint8)
+        job.point = pt.ctypes.data
+        buf = np.zeros(self.proof_size(num_vars), dtype=np.uint8)
+        job.proof = buf.ctypes.data
+        job.proof_cap = buf.size
+        return job, (ev, pt, buf)
+
+    @staticmethod
+    def _result(job, keep):
+        buf = keep[2]
+        return {"status": job.status, "root": bytes(job.root), "value": np.frombuffer(bytes(job.value), np.uint8)
+                .reshape(1, 16), "proof": buf[: job.proof_len].tobytes(), "latency_ms": job.latency_ms}
+
+    def prove(self, jobs, device_input: bool = False):
+        """jobs: list of (num_vars, evals, point); evals are host arrays or device pointers."""
+        arr = (BfJob * len(jobs))()
+        keeps = []
+        for i, (n, ev, pt) in enumerate(jobs):
+            job, keep = self._job(n, ev, pt, device_input)
+            arr[i] = job
+            keeps.append(keep)
+        check(lib().bf_engine_prove(self._h, arr, len(jobs), 1 if device_input else 0))
+        return [self._result(arr[i], keeps[i]) for i in range(len(jobs))]
+
+    def start(self) -> None:
+        check(lib().bf_engine_start(self._h))
+
+    def stop(self) -> None:
+        check(lib().bf_engine_stop(self._h))
+
+    def submit(self, num_vars: int, evals, point, device_input: bool = False, tag=None) -> int:
+        job, keep = self._job(num_vars, evals, point, device_input)
+        key = C.addressof(job)
+        self._keep[key] = (job, keep, tag)
+        check(lib().bf_engine_submit(self._h, C.byref(job), 1 if device_input else 0))
+        return key
+
+    def poll(self):
+        """Finished jobs since the last poll: list of (tag, result)."""
+        out = (C.POINTER(BfJob) * 64)()
+        n = C.c_size_t()
+        res = []
+        while True:
+            check(lib().bf_engine_poll(self._h, out, 64, C.byref(n)))
+            for i in range(n.value):
+                key = C.addressof(out[i].contents)
+                job, keep, tag = self._keep.pop(key)
+                res.append((tag, self._result(job, keep)))
+            if n.value < 64:
+                return res
 
 
 def _split_sumcheck(out, k, n):

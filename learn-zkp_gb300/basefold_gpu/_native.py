@@ -17,7 +17,9 @@ EXPORTS = [
     "bf_open_finish", "bf_open_session_free", "bf_verify", "bf_challenger_new", "bf_challenger_clone", "bf_challenger_free",
     "bf_challenger_observe", "bf_challenger_sample_ext", "bf_challenger_sample_bits", "bf_challenger_state",
     "bf_challenger_from_state", "bf_sumcheck_prove", "bf_sumcheck_prove_device", "bf_profile_enable",
-    "bf_profile_read", "bf_test_gf_mul", "bf_test_keccak_f",
+    "bf_profile_read", "bf_test_gf_mul", "bf_test_keccak_f", "bf_engine_create", "bf_engine_free",
+    "bf_engine_proof_size", "bf_engine_prove", "bf_engine_start", "bf_engine_stop", "bf_engine_submit",
+    "bf_engine_poll",
 ]
 
 BF_OK = 0
@@ -27,6 +29,15 @@ BF_ERR_OOM = -3
 BF_ERR_BUFFER = -4
 BF_ERR_UNSUPPORTED = -5
 BF_ERR_NOT_INVERTIBLE = -6
+
+
+class BfJob(C.Structure):
+    """bf_job of include/basefold_gpu.h."""
+    _fields_ = [
+        ("num_vars", C.c_int32), ("status", C.c_int32), ("evals", C.c_void_p), ("point", C.c_void_p),
+        ("proof", C.c_void_p), ("proof_cap", C.c_size_t), ("proof_len", C.c_size_t), ("latency_ms", C.c_double),
+        ("root", C.c_uint8 * 32), ("value", C.c_uint8 * 16),
+    ]
 
 
 class BasefoldGpuError(RuntimeError):
@@ -87,6 +98,14 @@ def lib():
         "bf_profile_read": ([vp, C.POINTER(C.c_double), C.POINTER(C.c_uint64), i], i),
         "bf_test_gf_mul": ([i, u8p, u8p, u8p, sz], i),
         "bf_test_keccak_f": ([i, C.POINTER(C.c_uint64), sz], i),
+        "bf_engine_create": ([i, i, i, i, sz, C.POINTER(vp)], i),
+        "bf_engine_free": ([vp], None),
+        "bf_engine_proof_size": ([vp, i], sz),
+        "bf_engine_prove": ([vp, C.POINTER(BfJob), sz, i], i),
+        "bf_engine_start": ([vp], i),
+        "bf_engine_stop": ([vp], i),
+        "bf_engine_submit": ([vp, C.POINTER(BfJob), i], i),
+        "bf_engine_poll": ([vp, C.POINTER(C.POINTER(BfJob)), sz, C.POINTER(sz)], i),
     }
     for name, (args, res) in decl.items():
         f = getattr(L, name)

@@ -150,6 +150,14 @@ void put_elem(std::vector<uint8_t>& b, u128 v);
 
 }  // namespace bfapi
 
+struct bf_pcs;
+struct bf_commitment;
+namespace bfapi {
+int commit_enqueue(bf_pcs* p, bf_commitment* cm, const uint4* data, cudaStream_t st, uint8_t* roots_pin);
+int eval_enqueue(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, uint4* scratch, cudaStream_t st,
+                 uint8_t* value_pin);
+}  // namespace bfapi
+
 struct bf_challenger {
   bfh::Challenger c;
 };

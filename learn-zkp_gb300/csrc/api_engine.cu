@@ -1,0 +1,401 @@
+// libbasefold_gpu.so: the prover engine — many commit+eval+open jobs of
+// different sizes in flight at once (batched and served forms).
+//
+// Each job follows the reference's harness (poly-commit/src/lib.rs:80-100):
+// commit, observe the root, evaluate at the point, observe the value, open
+// with a fresh keccak256 transcript.  A job is a state machine whose GPU work
+// runs on one stream of a pool; the engine admits jobs while streams and the
+// HBM budget allow, and advances whichever job's last GPU step has finished,
+// so small latency-bound proofs overlap with large ones and new requests join
+// between the rounds of running ones (continuous batching).  Proof bytes are
+// identical to the one-at-a-time path.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "api_common.h"
+
+using bfh::u128;
+using namespace bfapi;
+
+namespace {
+
+double now_ms() {
+  using namespace std::chrono;
+  return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+enum JobState { J_COMMIT = 0, J_EVAL = 1, J_ROUNDS = 2, J_DONE = 3 };
+
+struct Job {
+  bf_job* pub = nullptr;
+  bool device_input = false;
+  double t_submit = 0;
+  bf_pcs* pcs = nullptr;
+  int slot = -1;
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev = nullptr;
+  std::unique_ptr<bf_commitment> cm;
+  bf_open_session* sess = nullptr;
+  bfh::Challenger ch;
+  DevBuf eval_ws;
+  int state = J_COMMIT;
+  size_t footprint = 0;
+  uint8_t value[16];
+};
+
+}  // namespace
+
+struct bf_engine {
+  int device = 0, lambda = 128, log2_c = 1, max_inflight = 8;
+  size_t mem_budget = 0, mem_used = 0;
+  std::map<int, bf_pcs*> pcs_by_n;
+  std::vector<cudaStream_t> streams;
+  std::vector<int> free_slots;
+  PinnedBuf pin;  // 128 bytes per slot: roots (64) + value (16)
+  std::deque<Job*> queue;
+  std::vector<Job*> inflight;
+  std::vector<bf_job*> finished;  // completed, not yet collected by bf_engine_poll
+  std::mutex mu;
+  std::condition_variable cv;
+  std::thread worker;
+  bool running = false;
+  bool stop = false;
+  size_t outstanding = 0;  // submitted and not finished
+  ~bf_engine();
+};
+
+namespace {
+
+size_t job_footprint(int n, int log2_c, bool device_input, size_t Q, size_t block_bytes) {
+  const size_t N = (size_t)1 << n, c = (size_t)1 << log2_c;
+  size_t b = (40 + 160 * c) * N + Q * block_bytes + (2u << 20);
+  if (!device_input) b += 16 * N;
+  return b;
+}
+
+int get_pcs(bf_engine* e, int n, bf_pcs** out) {
+  auto it = e->pcs_by_n.find(n);
+  if (it != e->pcs_by_n.end()) {
+    *out = it->second;
+    return BF_OK;
+  }
+  bf_pcs* p = nullptr;
+  TRY(bf_pcs_setup(e->device, e->lambda, e->log2_c, n, e->streams[0], &p));
+  e->pcs_by_n[n] = p;
+  *out = p;
+  return BF_OK;
+}
+
+void finish_job(bf_engine* e, Job* j, int status) {
+  j->pub->status = status;
+  j->pub->latency_ms = now_ms() - j->t_submit;
+  if (j->sess) {
+    bf_open_session_free(j->sess);
+    j->sess = nullptr;
+  }
+  j->eval_ws.release();
+  j->cm.reset();
+  if (j->ev) cudaEventDestroy(j->ev);
+  j->ev = nullptr;
+  if (j->slot >= 0) e->free_slots.push_back(j->slot);
+  e->mem_used -= j->footprint;
+  j->state = J_DONE;
+}
+
+uint8_t* slot_pin(bf_engine* e, int slot) { return e->pin.b() + 128 * (size_t)slot; }
+
+// Starts a job on a free slot: allocate, copy the evaluations in, enqueue the commit.
+int admit(bf_engine* e, Job* j) {
+  bf_job* pj = j->pub;
+  TRY(get_pcs(e, pj->num_vars, &j->pcs));
+  bf_pcs* p = j->pcs;
+  const size_t need = bf_pcs_proof_size(p, 1, 1);
+  if (pj->proof_cap < need) return fail(BF_ERR_BUFFER, "job proof buffer needs %zu bytes", need);
+  j->st = e->streams[j->slot];
+  CU(cudaEventCreateWithFlags(&j->ev, cudaEventDisableTiming));
+  j->cm.reset(new bf_commitment());
+  j->cm->pcs = p;
+  j->cm->width = 1;
+  const size_t bytes = 16 * ((size_t)1 << p->d);
+  if (j->device_input) {
+    if (reinterpret_cast<uintptr_t>(pj->evals) & 15) return fail(BF_ERR_ARG, "device evaluations must be 16-byte aligned");
+    j->cm->data.p = const_cast<void*>(pj->evals);
+    j->cm->data.owned = false;
+    j->cm->data.bytes = bytes;
+  } else {
+    CU(j->cm->data.alloc_async(bytes, p->pool, j->st));
+    CU(cudaMemcpyAsync(j->cm->data.p, pj->evals, bytes, cudaMemcpyHostToDevice, j->st));
+  }
+  TRY(commit_enqueue(p, j->cm.get(), j->cm->data.as<uint4>(), j->st, slot_pin(e, j->slot)));
+  CU(cudaEventRecord(j->ev, j->st));
+  j->state = J_COMMIT;
+  return BF_OK;
+}
+
+// Advances a job whose last GPU step has completed.  Returns 1 if it moved.
+int step(bf_engine* e, Job* j) {
+  bf_pcs* p = j->pcs;
+  bf_job* pj = j->pub;
+  if (j->state == J_COMMIT || j->state == J_EVAL) {
+    cudaError_t q = cudaEventQuery(j->ev);
+    if (q == cudaErrorNotReady) return 0;
+    CU(q);
+  }
+  if (j->state == J_COMMIT) {
+    std::memcpy(j->cm->root, slot_pin(e, j->slot), 32);
+    std::memcpy(j->cm->pi_root, slot_pin(e, j->slot) + 32, 32);
+    std::memcpy(pj->root, j->cm->root, 32);
+    j->ch = bfh::Challenger();  // GenericChallenger::keccak256()
+    j->ch.observe(j->cm->root, 32);
+    const size_t half = p->d > 0 ? ((size_t)1 << (p->d - 1)) : 1;
+    CU(j->eval_ws.alloc_async(16 * half, p->pool, j->st));
+    TRY(eval_enqueue(p, j->cm.get(), pj->point, j->eval_ws.as<uint4>(), j->st, slot_pin(e, j->slot) + 64));
+    CU(cudaEventRecord(j->ev, j->st));
+    j->state = J_EVAL;
+    return 1;
+  }
+  if (j->state == J_EVAL) {
+    std::memcpy(j->value, slot_pin(e, j->slot) + 64, 16);
+    std::memcpy(pj->value, j->value, 16);
+    j->ch.observe(j->value, 16);
+    j->eval_ws.release();
+    TRY(bf_open_start(p, j->cm.get(), pj->point, j->value, j->st, &j->sess));
+    j->state = J_ROUNDS;
+    return 1;
+  }
+  if (j->state == J_ROUNDS) {
+    int ready = bf_open_poll(j->sess);
+    TRY(ready);
+    if (!ready) return 0;
+    int round;
+    uint8_t root[32], poly[32];
+    TRY(bf_open_round(j->sess, &round, root, poly));
+    if (round >= 0) {
+      j->ch.observe(root, 32);
+      j->ch.observe(poly, 32);
+      uint8_t r[16];
+      bfh::store(r, j->ch.sample_elem());
+      TRY(bf_open_challenge(j->sess, r));
+      return 1;
+    }
+    uint8_t fin[16];
+    TRY(bf_open_final(j->sess, fin));
+    j->ch.observe(fin, 16);
+    std::vector<uint64_t> idx(p->Q);
+    for (size_t q = 0; q < p->Q; ++q) idx[q] = j->ch.sample_bits(p->L);
+    TRY(bf_open_finish(j->sess, idx.data(), idx.size(), pj->proof, pj->proof_cap, &pj->proof_len));
+    finish_job(e, j, BF_OK);
+    return 1;
+  }
+  return 0;
+}
+
+// One pass over the engine: admit what fits, advance what is ready, retire
+// finished jobs.  Called with e->mu held only around queue access.
+bool progress(bf_engine* e) {
+  bool moved = false;
+  while (true) {
+    Job* j = nullptr;
+    {
+      std::lock_guard<std::mutex> lk(e->mu);
+      if (e->queue.empty() || e->free_slots.empty()) break;
+      Job* cand = e->queue.front();
+      // admission by HBM footprint: always admit when idle so oversized jobs still run
+      if (!e->inflight.empty() && e->mem_used + cand->footprint > e->mem_budget) break;
+      e->queue.pop_front();
+      j = cand;
+    }
+    j->slot = e->free_slots.back();
+    e->free_slots.pop_back();
+    e->mem_used += j->footprint;
+    e->inflight.push_back(j);
+    int rc = admit(e, j);
+    if (rc < 0) finish_job(e, j, rc);
+    moved = true;
+  }
+  for (Job* j : e->inflight) {
+    if (j->state == J_DONE) continue;
+    int rc = step(e, j);
+    if (rc < 0) finish_job(e, j, rc);
+    if (rc != 0) moved = true;
+  }
+  std::vector<Job*> keep;
+  for (Job* j : e->inflight) {
+    if (j->state == J_DONE) {
+      std::lock_guard<std::mutex> lk(e->mu);
+      e->finished.push_back(j->pub);
+      e->outstanding -= 1;
+      delete j;
+      e->cv.notify_all();
+    } else {
+      keep.push_back(j);
+    }
+  }
+  e->inflight.swap(keep);
+  return moved;
+}
+
+void worker_loop(bf_engine* e) {
+  cudaSetDevice(e->device);
+  while (true) {
+    {
+      std::unique_lock<std::mutex> lk(e->mu);
+      if (e->stop && e->outstanding == 0) break;
+      if (e->outstanding == 0) {
+        e->cv.wait_for(lk, std::chrono::milliseconds(5));
+        continue;
+      }
+    }
+    if (!progress(e)) std::this_thread::sleep_for(std::chrono::microseconds(20));
+  }
+}
+
+}  // namespace
+
+bf_engine::~bf_engine() {
+  for (auto& kv : pcs_by_n) bf_pcs_free(kv.second);
+  for (cudaStream_t s : streams) {
+    cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+  }
+}
+
+extern "C" {
+
+int bf_engine_create(int device, int lambda, int log2_c, int max_inflight, size_t mem_budget, bf_engine** out) {
+  if (!out || max_inflight <= 0 || max_inflight > 256 || log2_c < 0 || log2_c > 4)
+    return fail(BF_ERR_ARG, "bad engine parameters");
+  *out = nullptr;
+  CU(cudaSetDevice(device));
+  std::unique_ptr<bf_engine> e(new bf_engine());
+  e->device = device;
+  e->lambda = lambda;
+  e->log2_c = log2_c;
+  e->max_inflight = max_inflight;
+  if (mem_budget == 0) {
+    size_t free_b = 0, total_b = 0;
+    CU(cudaMemGetInfo(&free_b, &total_b));
+    mem_budget = free_b / 10 * 8;
+  }
+  e->mem_budget = mem_budget;
+  for (int i = 0; i < max_inflight; ++i) {
+    cudaStream_t s;
+    CU(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    e->streams.push_back(s);
+    e->free_slots.push_back(max_inflight - 1 - i);
+  }
+  CU(e->pin.ensure(128 * (size_t)max_inflight));
+  *out = e.release();
+  return BF_OK;
+}
+
+void bf_engine_free(bf_engine* e) {
+  if (!e) return;
+  if (e->running) {
+    {
+      std::lock_guard<std::mutex> lk(e->mu);
+      e->stop = true;
+      e->cv.notify_all();
+    }
+    e->worker.join();
+  }
+  for (Job* j : e->inflight) {
+    finish_job(e, j, BF_ERR_ARG);
+    delete j;
+  }
+  for (Job* j : e->queue) delete j;
+  DeviceGuard g(e->device);
+  delete e;
+}
+
+size_t bf_engine_proof_size(bf_engine* e, int num_vars) {
+  if (!e || num_vars < 0) return 0;
+  bf_pcs* p = nullptr;
+  if (get_pcs(e, num_vars, &p) < 0) return 0;
+  return bf_pcs_proof_size(p, 1, 1);
+}
+
+int bf_engine_submit(bf_engine* e, bf_job* job, int device_input) {
+  if (!e || !job || !job->evals || (job->num_vars > 0 && !job->point) || !job->proof)
+    return fail(BF_ERR_ARG, "null argument");
+  if (job->num_vars < 0 || job->num_vars + e->log2_c > 30) return fail(BF_ERR_ARG, "bad num_vars");
+  Job* j = new Job();
+  j->pub = job;
+  j->device_input = device_input != 0;
+  j->t_submit = now_ms();
+  job->status = 1;  // pending
+  job->proof_len = 0;
+  const size_t Q = num_queries(e->lambda, e->log2_c);
+  size_t bb = 8 + 16 + 8 + 32 * (size_t)(job->num_vars + e->log2_c) + 8;
+  for (int i = 0; i < job->num_vars; ++i) bb += 24 + 32 * (size_t)(e->log2_c + i);
+  j->footprint = job_footprint(job->num_vars, e->log2_c, j->device_input, Q, bb);
+  std::lock_guard<std::mutex> lk(e->mu);
+  e->queue.push_back(j);
+  e->outstanding += 1;
+  e->cv.notify_all();
+  return BF_OK;
+}
+
+int bf_engine_start(bf_engine* e) {
+  if (!e) return fail(BF_ERR_ARG, "null argument");
+  if (e->running) return BF_OK;
+  e->stop = false;
+  e->running = true;
+  e->worker = std::thread(worker_loop, e);
+  return BF_OK;
+}
+
+int bf_engine_stop(bf_engine* e) {
+  if (!e) return fail(BF_ERR_ARG, "null argument");
+  if (!e->running) return BF_OK;
+  {
+    std::lock_guard<std::mutex> lk(e->mu);
+    e->stop = true;
+    e->cv.notify_all();
+  }
+  e->worker.join();
+  e->running = false;
+  return BF_OK;
+}
+
+int bf_engine_poll(bf_engine* e, bf_job** done, size_t cap, size_t* n) {
+  if (!e || !n) return fail(BF_ERR_ARG, "null argument");
+  std::lock_guard<std::mutex> lk(e->mu);
+  size_t k = 0;
+  while (k < cap && !e->finished.empty()) {
+    if (done) done[k] = e->finished.front();
+    e->finished.erase(e->finished.begin());
+    ++k;
+  }
+  *n = k;
+  return BF_OK;
+}
+
+int bf_engine_prove(bf_engine* e, bf_job* jobs, size_t count, int device_input) {
+  if (!e || (count && !jobs)) return fail(BF_ERR_ARG, "null argument");
+  if (e->running) return fail(BF_ERR_ARG, "engine is serving; use bf_engine_submit");
+  DeviceGuard g(e->device);
+  for (size_t i = 0; i < count; ++i) TRY(bf_engine_submit(e, &jobs[i], device_input));
+  while (true) {
+    {
+      std::lock_guard<std::mutex> lk(e->mu);
+      if (e->outstanding == 0) break;
+    }
+    if (!progress(e)) std::this_thread::yield();
+  }
+  std::lock_guard<std::mutex> lk(e->mu);
+  e->finished.clear();
+  for (size_t i = 0; i < count; ++i)
+    if (jobs[i].status < 0) return jobs[i].status;
+  return BF_OK;
+}
+
+}  // extern "C"

@@ -217,32 +217,72 @@ int build_twiddles(bf_pcs* p) {
   return BF_OK;
 }
 
-int commit_device(bf_pcs* p, bf_commitment* cm, const uint4* data) {
+}  // namespace
+
+namespace bfapi {
+
+// Encode + Merkle commit of `data` (width 1) on stream `st`; the codeword
+// root and the first folded-codeword root are copied to roots_pin[0..64)
+// (pinned) when the stream reaches that point.
+int commit_enqueue(bf_pcs* p, bf_commitment* cm, const uint4* data, cudaStream_t st, uint8_t* roots_pin) {
   const size_t nd = p->n_d();
-  CU(cm->cw.alloc_async(16 * nd, p->pool, p->stream));
-  CU(cm->tree.alloc_async(32 * (2 * nd - 1), p->pool, p->stream));
-  if (p->d > 0) CU(cm->pi_tree.alloc_async(32 * (nd - 1), p->pool, p->stream));
+  CU(cm->cw.alloc_async(16 * nd, p->pool, st));
+  CU(cm->tree.alloc_async(32 * (2 * nd - 1), p->pool, st));
+  if (p->d > 0) CU(cm->pi_tree.alloc_async(32 * (nd - 1), p->pool, st));
   uint4* cw = cm->cw.as<uint4>();
   uint4* tree = cm->tree.as<uint4>();
   uint4* pit = cm->pi_tree.as<uint4>();
   {
-    ProfScope ps(p->prof, p->stream, P_ENCODE);
-    CU(bf::launch_encode(data, cw, p->d, p->log2_c, 1, p->tw_view.as<bf::TwiddleView>(), p->stream));
+    ProfScope ps(p->prof, st, P_ENCODE);
+    CU(bf::launch_encode(data, cw, p->d, p->log2_c, 1, p->tw_view.as<bf::TwiddleView>(), st));
   }
   {
-    ProfScope ps(p->prof, p->stream, P_LEAVES);
+    ProfScope ps(p->prof, st, P_LEAVES);
     if (p->d > 0)
-      CU(bf::launch_leaves_cw_pairs(cw, tree, pit, nd / 2, p->stream));
+      CU(bf::launch_leaves_cw_pairs(cw, tree, pit, nd / 2, st));
     else
-      CU(bf::launch_leaves_elem(cw, tree, nd, 1, p->stream));
+      CU(bf::launch_leaves_elem(cw, tree, nd, 1, st));
   }
   {
-    ProfScope ps(p->prof, p->stream, P_TREE);
-    CU(bf::launch_tree(tree, nd, p->stream));
-    if (p->d > 0) CU(bf::launch_tree(pit, nd / 2, p->stream));
+    ProfScope ps(p->prof, st, P_TREE);
+    CU(bf::launch_tree(tree, nd, st));
+    if (p->d > 0) CU(bf::launch_tree(pit, nd / 2, st));
   }
-  CU(cudaMemcpyAsync(p->pinned.b(), tree + 2 * (2 * nd - 2), 32, cudaMemcpyDeviceToHost, p->stream));
-  if (p->d > 0) CU(cudaMemcpyAsync(p->pinned.b() + 32, pit + 2 * (nd - 2), 32, cudaMemcpyDeviceToHost, p->stream));
+  CU(cudaMemcpyAsync(roots_pin, tree + 2 * (2 * nd - 2), 32, cudaMemcpyDeviceToHost, st));
+  if (p->d > 0) CU(cudaMemcpyAsync(roots_pin + 32, pit + 2 * (nd - 2), 32, cudaMemcpyDeviceToHost, st));
+  return BF_OK;
+}
+
+// MultiPoly::evaluate (multilinear.rs:124-141) of the commitment's data at
+// `point` (host, d elements) on stream `st`: fix the top variable with the
+// last coordinate, repeatedly, in `scratch` (2^(d-1) elements).  The value
+// lands in value_pin[0..16).
+int eval_enqueue(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, uint4* scratch, cudaStream_t st,
+                 uint8_t* value_pin) {
+  const int d = p->d;
+  const uint4* data = cm->data.as<uint4>();
+  if (d == 0) {
+    CU(cudaMemcpyAsync(value_pin, data, 16, cudaMemcpyDeviceToHost, st));
+    return BF_OK;
+  }
+  const uint4* in = data;
+  for (int k = d - 1; k >= 0; --k) {
+    uint4 r;
+    std::memcpy(&r, point + 16 * k, 16);
+    ProfScope ps(p->prof, st, P_FIX);
+    CU(bf::launch_fix(in, scratch, (size_t)1 << k, r, nullptr, 0, nullptr, st));
+    in = scratch;
+  }
+  CU(cudaMemcpyAsync(value_pin, scratch, 16, cudaMemcpyDeviceToHost, st));
+  return BF_OK;
+}
+
+}  // namespace bfapi
+
+namespace {
+
+int commit_device(bf_pcs* p, bf_commitment* cm, const uint4* data) {
+  TRY(commit_enqueue(p, cm, data, p->stream, p->pinned.b()));
   CU(cudaStreamSynchronize(p->stream));
   p->prof.drain();
   std::memcpy(cm->root, p->pinned.b(), 32);
@@ -399,26 +439,9 @@ int bf_eval(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, uint8_t* v
   if (!p || !cm || !values || (p->d > 0 && !point)) return fail(BF_ERR_ARG, "null argument");
   if (cm->width != 1) return fail(BF_ERR_UNSUPPORTED, "width != 1");
   DeviceGuard g(p->device);
-  const int d = p->d;
-  const uint4* data = cm->data.as<uint4>();
-  if (d == 0) {
-    CU(cudaMemcpyAsync(p->pinned.b(), data, 16, cudaMemcpyDeviceToHost, p->stream));
-  } else {
-    const size_t half = (size_t)1 << (d - 1);
-    if (p->eval_ws.bytes < 16 * half) CU(p->eval_ws.alloc(16 * half));
-    uint4* w = p->eval_ws.as<uint4>();
-    // MultiPoly::evaluate (multilinear.rs:124-141): fix the top variable with
-    // the last coordinate, repeatedly.
-    const uint4* in = data;
-    for (int k = d - 1; k >= 0; --k) {
-      uint4 r;
-      std::memcpy(&r, point + 16 * k, 16);
-      ProfScope ps(p->prof, p->stream, P_FIX);
-      CU(bf::launch_fix(in, w, (size_t)1 << k, r, nullptr, 0, nullptr, p->stream));
-      in = w;
-    }
-    CU(cudaMemcpyAsync(p->pinned.b(), w, 16, cudaMemcpyDeviceToHost, p->stream));
-  }
+  const size_t half = p->d > 0 ? ((size_t)1 << (p->d - 1)) : 1;
+  if (p->eval_ws.bytes < 16 * half) CU(p->eval_ws.alloc(16 * half));
+  TRY(eval_enqueue(p, cm, point, p->eval_ws.as<uint4>(), p->stream, p->pinned.b()));
   CU(cudaStreamSynchronize(p->stream));
   p->prof.drain();
   std::memcpy(values, p->pinned.b(), 16);

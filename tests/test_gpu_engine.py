@@ -1,0 +1,93 @@
+"""The prover engine (batched and served forms): every proof is identical to
+the one produced by commit/eval/open one at a time (tolerance: bit-exact),
+alone or in the mix."""
+import time
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from basefold_gpu import rand
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def bg(built_lib):
+    return built_lib
+
+
+def alone(bg, n, evals, point, log2_c=1):
+    pcs = bg.Basefold.setup(bg.BasefoldConfig(bg.BinaryReedSolomonCode(128, log2_c, n)), device=0)
+    comm = pcs.commit(evals)
+    ch = bg.GenericChallenger.keccak256()
+    ch.observe(comm.root)
+    values = pcs.eval(pcs.data(comm), point)
+    ch.observe_ext_slice(values)
+    return comm.root, values, pcs.open(comm, [bg.PolyEvals(values, point)], ch)
+
+
+def make_jobs(sizes, seed0):
+    jobs = []
+    for k, n in enumerate(sizes):
+        data = rand.random_elems((1 << n) + n, seed0 + k)
+        jobs.append((n, data[: 1 << n], data[1 << n:]))
+    return jobs
+
+
+def test_engine_batch_matches_alone(bg):
+    sizes = [0, 1, 3, 12, 7, 10, 5, 14, 9, 11, 6, 13, 8, 2, 4, 10]
+    jobs = make_jobs(sizes, 8000)
+    eng = bg.Engine(max_inflight=6)
+    res = eng.prove(jobs)
+    for (n, ev, pt), r in zip(jobs, res):
+        root, values, proof = alone(bg, n, ev, pt)
+        assert r["status"] == 0
+        assert r["root"] == root and np.array_equal(r["value"], values) and r["proof"] == proof, n
+    n, ev, pt = jobs[3]
+    root_o, values_o, blob = O.harness_prepare(n, 1, ev, pt)
+    assert res[3]["proof"] == O.open_proof(n, 1, ev, pt, values_o, blob)
+
+
+def test_engine_device_input(bg):
+    torch = pytest.importorskip("torch")
+    jobs = make_jobs([9, 11, 6], 8100)
+    devs = [torch.from_numpy(ev).cuda() for _, ev, _ in jobs]
+    eng = bg.Engine(max_inflight=3)
+    res = eng.prove([(n, d.data_ptr(), pt) for (n, _, pt), d in zip(jobs, devs)], device_input=True)
+    for (n, ev, pt), r in zip(jobs, res):
+        assert r["proof"] == alone(bg, n, ev, pt)[2]
+
+
+def test_engine_serving_continuous_batching(bg):
+    """Requests submitted while others run are admitted between rounds; each
+    result equals the alone result."""
+    sizes = [13, 8, 11, 6, 12, 9, 10, 7, 14, 5]
+    jobs = make_jobs(sizes, 8200)
+    eng = bg.Engine(max_inflight=4)
+    eng.start()
+    got = {}
+    for k, (n, ev, pt) in enumerate(jobs):
+        eng.submit(n, ev, pt, tag=k)
+        time.sleep(0.002)
+        for tag, r in eng.poll():
+            got[tag] = r
+    deadline = time.time() + 60
+    while len(got) < len(jobs) and time.time() < deadline:
+        for tag, r in eng.poll():
+            got[tag] = r
+        time.sleep(0.001)
+    eng.stop()
+    assert len(got) == len(jobs)
+    for k, (n, ev, pt) in enumerate(jobs):
+        assert got[k]["status"] == 0 and got[k]["latency_ms"] > 0
+        assert got[k]["proof"] == alone(bg, n, ev, pt)[2], k
+
+
+def test_engine_admission_by_memory_budget(bg):
+    """A budget smaller than one job still completes (one job at a time)."""
+    jobs = make_jobs([10, 11, 9], 8300)
+    eng = bg.Engine(max_inflight=4, mem_budget=1 << 20)
+    res = eng.prove(jobs)
+    for (n, ev, pt), r in zip(jobs, res):
+        assert r["proof"] == alone(bg, n, ev, pt)[2]
