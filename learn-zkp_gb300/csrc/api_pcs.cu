@@ -233,15 +233,14 @@ int commit_enqueue(bf_pcs* p, bf_commitment* cm, const uint4* data, cudaStream_t
   uint4* tree = cm->tree.as<uint4>();
   uint4* pit = cm->pi_tree.as<uint4>();
   {
+    // encode; for d >= 1 the last NTT pass also hashes the leaves
     ProfScope ps(p->prof, st, P_ENCODE);
-    CU(bf::launch_encode(data, cw, p->d, p->log2_c, 1, p->tw_view.as<bf::TwiddleView>(), st));
+    CU(bf::launch_encode(data, cw, p->d, p->log2_c, 1, p->tw_view.as<bf::TwiddleView>(), st,
+                         p->d > 0 ? tree : nullptr, p->d > 0 ? pit : nullptr));
   }
-  {
+  if (p->d == 0) {
     ProfScope ps(p->prof, st, P_LEAVES);
-    if (p->d > 0)
-      CU(bf::launch_leaves_cw_pairs(cw, tree, pit, nd / 2, st));
-    else
-      CU(bf::launch_leaves_elem(cw, tree, nd, 1, st));
+    CU(bf::launch_leaves_elem(cw, tree, nd, 1, st));
   }
   {
     ProfScope ps(p->prof, st, P_TREE);

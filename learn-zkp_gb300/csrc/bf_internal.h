@@ -21,9 +21,11 @@ struct TwiddleView {
 };
 
 // Launchers (all asynchronous on `st`).
-// `tw` points to a TwiddleView in device memory.
+// `tw` points to a TwiddleView in device memory.  When `leaves` and
+// `pair_leaves` are given (n >= 1), the last pass also writes the codeword
+// leaves and the first folded-codeword leaves.
 cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t width, const TwiddleView* tw,
-                          cudaStream_t st);
+                          cudaStream_t st, uint4* leaves = nullptr, uint4* pair_leaves = nullptr);
 cudaError_t launch_leaves_elem(const uint4* cw, uint4* leaves, size_t n, size_t width, cudaStream_t st);
 cudaError_t launch_leaves_pair(const uint4* pi, uint4* leaves, size_t n, cudaStream_t st);
 cudaError_t launch_leaves_cw_pairs(const uint4* cw, uint4* leaves, uint4* pair_leaves, size_t n_pairs,

@@ -69,8 +69,16 @@ static unsigned grid_for(size_t n, int threads, int per_sm = 8) {
 // ---------------------------------------------------------------------------
 struct PassParams {
   int n, s_lo, T, first;
+  // Last pass only: also hash the codeword leaves H(cw[q]) and the first
+  // folded-codeword leaves H(cw[2s] || cw[2s+1]) from the tile in shared
+  // memory (null: no hashing).  The hashing is integer-ALU work and the
+  // butterflies are multiplier work, so co-resident blocks in the two phases
+  // keep both pipes busy.
+  uint4* leaves;
+  uint4* pair_leaves;
 };
 
+template <bool HASH>
 __global__ void __launch_bounds__(256) ntt_pass_kernel(const uint4* __restrict__ m, uint4* __restrict__ cw,
                                                       PassParams p, const TwiddleView* __restrict__ tw) {
   extern __shared__ uint4 sm[];
@@ -117,6 +125,17 @@ __global__ void __launch_bounds__(256) ntt_pass_kernel(const uint4* __restrict__
     const size_t x = ((size_t)hi << (s_lo + T)) | ((size_t)i << s_lo) | u;
     cw[coset_base + x] = sm[i];
   }
+  if (HASH) {
+    // last pass: s_lo = 0, the tile is the contiguous run [coset_base + hi 2^T, +2^T)
+    const size_t q0 = coset_base + ((size_t)hi << T);
+    for (uint32_t k = threadIdx.x; k < (tsize >> 1); k += blockDim.x) {
+      const uint4 e0 = sm[2 * k], e1 = sm[2 * k + 1];
+      const size_t q = q0 + 2 * k;
+      store_digest(p.leaves, q, hash_elem(e0));
+      store_digest(p.leaves, q + 1, hash_elem(e1));
+      store_digest(p.pair_leaves, q >> 1, hash_pair(e0, e1));
+    }
+  }
 }
 
 // n = 0: every coset is m[0].
@@ -127,7 +146,7 @@ __global__ void replicate_kernel(const uint4* __restrict__ m, uint4* __restrict_
 constexpr int kNttMaxT = 12;
 
 cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t width, const TwiddleView* tw,
-                          cudaStream_t st) {
+                          cudaStream_t st, uint4* leaves, uint4* pair_leaves) {
   if (width != 1) return cudaErrorInvalidValue;
   const size_t c = (size_t)1 << log2_c;
   if (n == 0) {
@@ -137,7 +156,9 @@ cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t w
   }
   static bool attr_set = false;
   if (!attr_set) {
-    cudaFuncSetAttribute(ntt_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(ntt_pass_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(sizeof(uint4) << kNttMaxT));
+    cudaFuncSetAttribute(ntt_pass_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)(sizeof(uint4) << kNttMaxT));
     attr_set = true;
   }
@@ -151,8 +172,14 @@ cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t w
     p.T = T;
     p.s_lo = top - T;
     p.first = (pidx == 0);
+    const bool last = (pidx == passes - 1);
+    p.leaves = last ? leaves : nullptr;
+    p.pair_leaves = last ? pair_leaves : nullptr;
     const size_t blocks = c << (n - T);
-    ntt_pass_kernel<<<(unsigned)blocks, 256, sizeof(uint4) << T, st>>>(m, cw, p, tw);
+    if (p.leaves)
+      ntt_pass_kernel<true><<<(unsigned)blocks, 256, sizeof(uint4) << T, st>>>(m, cw, p, tw);
+    else
+      ntt_pass_kernel<false><<<(unsigned)blocks, 256, sizeof(uint4) << T, st>>>(m, cw, p, tw);
     COUNT_LAUNCH();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
