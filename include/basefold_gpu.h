@@ -166,6 +166,22 @@ int bf_engine_stop(bf_engine* e);
 int bf_engine_submit(bf_engine* e, bf_job* job, int device_input);
 int bf_engine_poll(bf_engine* e, bf_job** done, size_t cap, size_t* n);
 
+/* ---- Evaluation that allocates nothing.  No counterpart in the reference.
+ * Same value as bf_eval (MultiPoly::evaluate of 2^num_vars evaluations at
+ * `point`), for callers that cannot allocate device memory at this point —
+ * e.g. a service whose device memory is all carved into fixed per-request
+ * slots, or a latency-critical loop where cudaMalloc/cudaFree would
+ * synchronise the device.  Inputs and output are the caller's: `d_evals` and
+ * `d_value` (16 bytes) in device memory, `point` in host memory; the work is
+ * queued on `stream` (cudaStream_t, NULL = default stream) and the call does
+ * not wait for it.  Scratch is a fixed 1 MiB array in the library's device
+ * image, so num_vars <= 17 (larger sizes return BF_ERR_ARG; use bf_eval).
+ * Every call on a device shares that array and it keeps the last call's
+ * contents: calls whose GPU work overlaps (other streams or threads) race.
+ * The first call on each device looks up the array's device address; make
+ * that first call before any stream capture. */
+int bf_eval_noalloc(const void* d_evals, int num_vars, const uint8_t* point, void* d_value, void* stream);
+
 /* ---- PolyCommitScheme::verify (lib.rs:44-50; basefold.rs:234-324) on the
  * host.  Returns BF_VERIFY_* (>= 0) or a negative BF_ERR_*. */
 int bf_verify(const bf_pcs* pcs, const uint8_t root[32], const uint8_t* point, const uint8_t* values, size_t width,
