@@ -18,8 +18,8 @@
  *  - Digest / commitment: 32 bytes (Plonky3 `Hash<Polyval, u8, 32>`).
  *  - Evaluations: row-major, `width` columns (one multilinear polynomial per
  *    column, 2^num_vars rows) — the reference's `RowMajorMatrix<F>` Data
- *    (poly-commit/src/basefold.rs:96-97).  Only width 1 is accepted by this
- *    build's GPU path.
+ *    (poly-commit/src/basefold.rs:96-97).  The engine (bf_engine_*) runs
+ *    width 1 only.
  *  - Proofs: the bincode 1.3 bytes of `BasefoldProof` (basefold.rs:49-66).
  *  - Every call returns 0 on success or a negative BF_ERR_* code; the text of
  *    the last error on the calling thread is available from bf_last_error.
@@ -129,7 +129,10 @@ int bf_open(bf_pcs* pcs, const bf_commitment* comm, const uint8_t* point, const 
  * final polynomial (basefold.rs:196), samples the query indices
  * (basefold.rs:200-203) and finishes.  `stream` (cudaStream_t or NULL for the
  * pcs's stream) lets several sessions overlap on the GPU.
- * bf_open_start: begins open (basefold.rs:133-193) for one point.
+ * bf_open_start: begins open (basefold.rs:133-193) for one point; for a
+ *   commitment of width > 1, `scalars` holds the caller's eq scalars
+ *   (sample_random_scalars_by_eq, basefold.rs:398-408; width elements), which
+ *   combine the rows (basefold.rs:166-183); NULL for width 1.
  * bf_open_round: waits for the device and writes the current round index
  *   (d-1 .. 0, or -1 once every round is done), its root and round poly.
  * bf_open_challenge: applies the round's challenge; returns without waiting.
@@ -137,8 +140,8 @@ int bf_open(bf_pcs* pcs, const bf_commitment* comm, const uint8_t* point, const 
  * bf_open_final: the final polynomial (one element) after the last round.
  * bf_open_finish: gathers the openings at the caller's indices (exactly
  *   num_queries of them) and writes the bincode proof. */
-int bf_open_start(bf_pcs* pcs, const bf_commitment* comm, const uint8_t* point, const uint8_t* values, void* stream,
-                  bf_open_session** out);
+int bf_open_start(bf_pcs* pcs, const bf_commitment* comm, const uint8_t* point, const uint8_t* values,
+                  const uint8_t* scalars, void* stream, bf_open_session** out);
 int bf_open_round(bf_open_session* s, int* round, uint8_t pi_root[32], uint8_t round_poly[32]);
 int bf_open_challenge(bf_open_session* s, const uint8_t r[16]);
 int bf_open_poll(bf_open_session* s);

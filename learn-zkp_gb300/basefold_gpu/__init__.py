@@ -256,9 +256,10 @@ class Basefold:
             check(lib().bf_open(self._h, comm._h, None, None, 0, challenger._h, _p(out), out.size, C.byref(ln)))
         return out[: ln.value].tobytes()
 
-    def open_session(self, comm: CommitmentData, evals: "PolyEvals", stream=None) -> "OpenSession":
-        """Round-level open driven by the caller's transcript (see OpenSession)."""
-        return OpenSession(self, comm, evals, stream)
+    def open_session(self, comm: CommitmentData, evals: "PolyEvals", stream=None, scalars=None) -> "OpenSession":
+        """Round-level open driven by the caller's transcript (see OpenSession);
+        width > 1 needs the caller's eq scalars (basefold.rs:398-408)."""
+        return OpenSession(self, comm, evals, stream, scalars)
 
     def verify(self, comm: bytes, evals, proof: bytes, challenger: GenericChallenger) -> None:
         """verify (basefold.rs:234-324); raises BasefoldError on rejection."""
@@ -305,14 +306,15 @@ class OpenSession:
     `challenge(r)`.  When `round()` returns i = -1, `final_poly()` is observed,
     `num_queries` indices are sampled and `finish(indices)` returns the proof."""
 
-    def __init__(self, pcs: "Basefold", comm: CommitmentData, evals: "PolyEvals", stream=None):
+    def __init__(self, pcs: "Basefold", comm: CommitmentData, evals: "PolyEvals", stream=None, scalars=None):
         self._pcs, self._comm = pcs, comm
         d = pcs.config.code.d
         pt = _elems(evals.point) if d else np.zeros((1, 16), np.uint8)
-        vals = _elems(evals.values, 1)
+        vals = _elems(evals.values, comm.width)
+        sc = _elems(scalars, comm.width) if scalars is not None else None
         h = C.c_void_p()
-        check(lib().bf_open_start(pcs._h, comm._h, _p(pt), _p(vals), C.c_void_p(stream) if stream else None,
-                                  C.byref(h)))
+        check(lib().bf_open_start(pcs._h, comm._h, _p(pt), _p(vals), _p(sc) if sc is not None else None,
+                                  C.c_void_p(stream) if stream else None, C.byref(h)))
         self._h = h
 
     def round(self):
@@ -335,7 +337,7 @@ class OpenSession:
 
     def finish(self, indices) -> bytes:
         idx = np.ascontiguousarray(np.asarray(indices, dtype=np.uint64))
-        size = self._pcs.proof_size(1, 1)
+        size = self._pcs.proof_size(self._comm.width, 1)
         out = np.zeros(size, dtype=np.uint8)
         ln = C.c_size_t()
         check(lib().bf_open_finish(self._h, idx.ctypes.data_as(C.POINTER(C.c_uint64)), idx.size, _p(out), out.size,

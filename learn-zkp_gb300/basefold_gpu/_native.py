@@ -76,7 +76,7 @@ def lib():
         "bf_commitment_data": ([vp, u8p, sz], i),
         "bf_eval": ([vp, vp, u8p, u8p], i),
         "bf_open": ([vp, vp, u8p, u8p, i, vp, u8p, sz, C.POINTER(sz)], i),
-        "bf_open_start": ([vp, vp, u8p, u8p, vp, C.POINTER(vp)], i),
+        "bf_open_start": ([vp, vp, u8p, u8p, u8p, vp, C.POINTER(vp)], i),
         "bf_open_round": ([vp, C.POINTER(i), u8p, u8p], i),
         "bf_open_challenge": ([vp, u8p], i),
         "bf_open_poll": ([vp], i),

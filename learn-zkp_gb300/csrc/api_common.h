@@ -147,6 +147,10 @@ size_t num_queries(int lambda, int log2_c);
 u128 horner(const u128* c, int n, u128 x);
 void put_u64(std::vector<uint8_t>& b, uint64_t v);
 void put_elem(std::vector<uint8_t>& b, u128 v);
+// MultiPoly::eq(x, ONE) on the host (p3/src/poly/multilinear.rs:41-64).
+std::vector<u128> eq_table_host(const std::vector<u128>& x);
+// sample_random_scalars_by_eq (poly-commit/src/basefold.rs:398-408).
+std::vector<u128> sample_scalars_by_eq(size_t n, bfh::Challenger& ch);
 
 }  // namespace bfapi
 

@@ -167,7 +167,7 @@ int step(bf_engine* e, Job* j) {
     std::memcpy(pj->value, j->value, 16);
     j->ch.observe(j->value, 16);
     j->eval_ws.release();
-    TRY(bf_open_start(p, j->cm.get(), pj->point, j->value, j->st, &j->sess));
+    TRY(bf_open_start(p, j->cm.get(), pj->point, j->value, nullptr, j->st, &j->sess));
     j->state = J_ROUNDS;
     return 1;
   }

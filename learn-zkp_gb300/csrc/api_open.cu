@@ -23,6 +23,7 @@ struct bf_open_session {
   cudaStream_t st = nullptr;
   cudaEvent_t ev = nullptr;
   int d = 0;
+  size_t w = 1;            // columns of the commitment
   int i = 0;               // current round (d-1 .. 0); -1 once every round is done
   bool msg_ready = false;  // host message of the current round computed
   bool pending = false;    // device work enqueued, its result not read yet
@@ -45,6 +46,13 @@ struct bf_open_session {
   uint8_t* w_stage = nullptr;  // per round: root (32 B) + sumcheck reduction (16 B)
   uint64_t* w_idx = nullptr;
   uint8_t* w_open = nullptr;
+  // width > 1: the eq-scalar combinations of the codeword rows (the first
+  // round's folded codeword) and of the data rows (the sumcheck polynomial),
+  // basefold.rs:166-183, and the first round's tree
+  uint4* w_scalars = nullptr;
+  uint4* w_pi_first = nullptr;
+  uint4* w_pi_first_tree = nullptr;
+  uint4* w_poly_first = nullptr;
   std::unique_ptr<PinnedBuf> pin;  // [0,64) staging, [64,64+16d) point, indices, openings
   uint64_t* idx_pin = nullptr;
   uint8_t* open_pin = nullptr;
@@ -56,6 +64,9 @@ struct bf_open_session {
     return w_pi_trees + 2 * ((c() << 1) * (((size_t)1 << (d - 1)) - ((size_t)1 << (k + 1))) - (size_t)(d - 2 - k));
   }
   uint8_t* stage(int k) const { return w_stage + 48 * (size_t)k; }
+  const uint4* first_pi() const { return w == 1 ? cm->cw.as<uint4>() : w_pi_first; }
+  const uint4* first_poly() const { return w == 1 ? cm->data.as<uint4>() : w_poly_first; }
+  const uint4* first_tree() const { return w == 1 ? cm->pi_tree.as<uint4>() : w_pi_first_tree; }
   ~bf_open_session() {
     if (st) cudaStreamSynchronize(st);
     if (ev) cudaEventDestroy(ev);
@@ -89,9 +100,23 @@ int session_alloc(bf_open_session* s) {
   const size_t o_point = take(16 * n_point), o_fold = take(16 * n_fold), o_tree = take(32 * n_tree);
   const size_t o_poly = take(16 * half), o_heq = take(16 * half), o_lo = take(16 * 4096);
   const size_t o_hi = take(16 * ((size_t)1 << hi_vars)), o_stage = take(48 * n_point);
-  const size_t o_idx = take(8 * (p->Q + 1)), o_open = take(p->block_bytes(1) * (p->Q + 1));
+  const size_t bb = p->block_bytes(s->w);
+  const size_t o_idx = take(8 * (p->Q + 1)), o_open = take(bb * (p->Q + 1));
+  size_t o_sc = 0, o_pif = 0, o_pift = 0, o_polyf = 0;
+  if (s->w > 1) {
+    o_sc = take(16 * s->w);
+    o_pif = take(16 * p->n_d());
+    o_pift = take(32 * p->n_d());
+    o_polyf = take(16 * ((size_t)1 << d));
+  }
   CU(s->ws.alloc_async(off, p->pool, s->st));
   uint8_t* b = s->ws.as<uint8_t>();
+  if (s->w > 1) {
+    s->w_scalars = reinterpret_cast<uint4*>(b + o_sc);
+    s->w_pi_first = reinterpret_cast<uint4*>(b + o_pif);
+    s->w_pi_first_tree = reinterpret_cast<uint4*>(b + o_pift);
+    s->w_poly_first = reinterpret_cast<uint4*>(b + o_polyf);
+  }
   s->w_point = reinterpret_cast<uint4*>(b + o_point);
   s->w_pi_fold = reinterpret_cast<uint4*>(b + o_fold);
   s->w_pi_trees = reinterpret_cast<uint4*>(b + o_tree);
@@ -102,7 +127,7 @@ int session_alloc(bf_open_session* s) {
   s->w_stage = b + o_stage;
   s->w_idx = reinterpret_cast<uint64_t*>(b + o_idx);
   s->w_open = b + o_open;
-  const size_t pin_bytes = 64 + 16 * n_point + 8 * (p->Q + 1) + p->block_bytes(1) * (p->Q + 1);
+  const size_t pin_bytes = 64 + 16 * (n_point + s->w) + 8 * (p->Q + 1) + bb * (p->Q + 1);
   if (!p->pinned_cache.empty()) {
     s->pin = std::move(p->pinned_cache.back());
     p->pinned_cache.pop_back();
@@ -110,7 +135,7 @@ int session_alloc(bf_open_session* s) {
     s->pin.reset(new PinnedBuf());
   }
   CU(s->pin->ensure(pin_bytes));
-  s->idx_pin = reinterpret_cast<uint64_t*>(s->pin->b() + 64 + 16 * n_point);
+  s->idx_pin = reinterpret_cast<uint64_t*>(s->pin->b() + 64 + 16 * (n_point + s->w));
   s->open_pin = reinterpret_cast<uint8_t*>(s->idx_pin + (p->Q + 1));
   return BF_OK;
 }
@@ -134,7 +159,7 @@ int ensure_message(bf_open_session* s) {
   if (s->msg_ready) return BF_OK;
   const int i = s->i, d = s->d;
   const u128 ONE = bfh::one();
-  if (i == d - 1)
+  if (i == d - 1 && s->w == 1)
     std::memcpy(s->root, s->cm->pi_root, 32);
   else
     std::memcpy(s->root, s->pin->b(), 32);
@@ -158,26 +183,34 @@ int ensure_message(bf_open_session* s) {
 
 extern "C" {
 
-int bf_open_start(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, const uint8_t* values, void* stream,
-                  bf_open_session** out) {
+int bf_open_start(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, const uint8_t* values,
+                  const uint8_t* scalars, void* stream, bf_open_session** out) {
   if (!p || !cm || !out || !values || (p->d > 0 && !point)) return fail(BF_ERR_ARG, "null argument");
   *out = nullptr;
   if (p->device < 0) return fail(BF_ERR_ARG, "verifier-only pcs (device < 0)");
   if (cm->pcs != p) return fail(BF_ERR_ARG, "commitment belongs to another pcs");
-  if (cm->width != 1) return fail(BF_ERR_UNSUPPORTED, "width != 1");
+  if (cm->width > 1 && !scalars) return fail(BF_ERR_ARG, "width > 1 needs the eq scalars");
   DeviceGuard g(p->device);
   std::unique_ptr<bf_open_session> s(new bf_open_session());
   s->p = p;
   s->cm = cm;
+  s->w = cm->width;
   s->st = stream ? reinterpret_cast<cudaStream_t>(stream) : p->stream;
   CU(cudaEventCreateWithFlags(&s->ev, cudaEventDisableTiming));
   const int d = p->d;
+  const size_t w = s->w;
   s->d = d;
   s->i = d - 1;
   const u128 ONE = bfh::one();
   s->r.resize(d);
   for (int k = 0; k < d; ++k) s->r[k] = bfh::load(point + 16 * k);
-  s->outer_val = bfh::load(values);
+  if (w == 1) {
+    s->outer_val = bfh::load(values);
+  } else {  // claim = <scalars, values> (basefold.rs:176)
+    u128 claim = 0;
+    for (size_t c = 0; c < w; ++c) claim ^= bfh::mul(bfh::load(scalars + 16 * c), bfh::load(values + 16 * c));
+    s->outer_val = claim;
+  }
   s->delta_prod = ONE;
   // EvalImpr::new / HalfEq::new (eval_impr.rs:20-27, 69-79)
   if (!bfh::batch_inverse(s->r, s->r_inv)) return fail(BF_ERR_NOT_INVERTIBLE, "point has a zero coordinate");
@@ -191,21 +224,34 @@ int bf_open_start(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, cons
   put_u64(s->roots, (uint64_t)d);
   TRY(session_alloc(s.get()));
   uint8_t* pin = s->pin->b();
-  const uint4* data = cm->data.as<uint4>();
   cudaStream_t st = s->st;
+  if (w > 1) {  // combine rows with the eq scalars (basefold.rs:166-183)
+    std::memcpy(pin + 64, scalars, 16 * w);
+    CU(cudaMemcpyAsync(s->w_scalars, pin + 64, 16 * w, cudaMemcpyHostToDevice, st));
+    ProfScope ps(p->prof, st, P_FIX);
+    CU(bf::launch_combine_rows(cm->cw.as<uint4>(), p->n_d(), w, s->w_scalars, s->w_pi_first, st));
+    CU(bf::launch_combine_rows(cm->data.as<uint4>(), (size_t)1 << d, w, s->w_scalars, s->w_poly_first, st));
+  }
   if (d == 0) {
-    CU(cudaMemcpyAsync(pin, data, 16, cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(pin, s->first_poly(), 16, cudaMemcpyDeviceToHost, st));
   } else {
-    std::memcpy(pin + 64, point, 16 * (size_t)d);
-    CU(cudaMemcpyAsync(s->w_point, pin + 64, 16 * (size_t)d, cudaMemcpyHostToDevice, st));
-    CU(cudaMemsetAsync(s->w_stage, 0, 48 * (size_t)d, st));
+    if (w > 1) {  // the first round's tree over the combined codeword pairs
+      ProfScope ps(p->prof, st, P_TREE);
+      const size_t n1 = p->n_i(d - 1);
+      CU(bf::launch_leaves_pair(s->w_pi_first, s->w_pi_first_tree, n1, st));
+      CU(bf::launch_tree(s->w_pi_first_tree, n1, st, reinterpret_cast<uint4*>(s->stage(d - 1))));
+    }
+    std::memcpy(pin + 64 + 16 * w, point, 16 * (size_t)d);
+    CU(cudaMemcpyAsync(s->w_point, pin + 64 + 16 * w, 16 * (size_t)d, cudaMemcpyHostToDevice, st));
+    CU(cudaMemsetAsync(s->stage(d - 1) + 32, 0, 16, st));
+    if (d >= 2) CU(cudaMemsetAsync(s->w_stage, 0, 48 * (size_t)(d - 1), st));
     {
       ProfScope ps(p->prof, st, P_EQ);
       CU(bf::launch_eq_table(s->w_point, d - 1, s->w_heq, s->w_eq_lo, s->w_eq_hi, st));
     }
     {
       ProfScope ps(p->prof, st, P_FIX);
-      CU(bf::launch_dot_xor(s->w_heq, data, (size_t)1 << (d - 1),
+      CU(bf::launch_dot_xor(s->w_heq, s->first_poly(), (size_t)1 << (d - 1),
                             reinterpret_cast<uint32_t*>(s->stage(d - 1) + 32), st));
     }
     CU(cudaMemcpyAsync(pin, s->stage(d - 1), 48, cudaMemcpyDeviceToHost, st));
@@ -261,8 +307,7 @@ int bf_open_challenge(bf_open_session* s, const uint8_t r_i[16]) {
   // fold (binary_reed_solomon.rs:88-96) with the stage d-1-i twiddles,
   // fused with the leaves of the next round's tree
   const size_t ni = p->n_i(i);
-  const uint4* cw = s->cm->cw.as<uint4>();
-  const uint4* pi_in = (i == d - 1) ? cw : s->pi_fold_out(i + 1);
+  const uint4* pi_in = (i == d - 1) ? s->first_pi() : s->pi_fold_out(i + 1);
   const uint4* tlo = p->tw_host.lo[d - 1 - i];
   const uint4* thi = p->tw_host.hi[d - 1 - i];
   {
@@ -273,7 +318,7 @@ int bf_open_challenge(bf_open_session* s, const uint8_t r_i[16]) {
       CU(bf::launch_fold(pi_in, s->pi_fold_out(i), ni, tlo, thi, xr, st));
   }
   // fix_last_var (multilinear.rs:183-198) + next round's reduction
-  const uint4* poly_in = (i == d - 1) ? s->cm->data.as<uint4>() : s->w_poly;
+  const uint4* poly_in = (i == d - 1) ? s->first_poly() : s->w_poly;
   {
     ProfScope ps(p->prof, st, P_FIX);
     CU(bf::launch_fix(poly_in, s->w_poly, (size_t)1 << i, xr, s->w_heq, i > 0 ? ((size_t)1 << (i - 1)) : 0,
@@ -311,12 +356,12 @@ int bf_open_finish(bf_open_session* s, const uint64_t* indices, size_t nq, uint8
   bf_pcs* p = s->p;
   if (s->i >= 0) return fail(BF_ERR_ARG, "rounds remain");
   if (nq != p->Q) return fail(BF_ERR_ARG, "expected %zu query indices, got %zu", p->Q, nq);
-  const size_t need = bf_pcs_proof_size(p, 1, 1);
+  const size_t need = bf_pcs_proof_size(p, s->w, 1);
   *proof_len = need;
   if (!proof || cap < need) return fail(BF_ERR_BUFFER, "proof buffer needs %zu bytes", need);
   DeviceGuard g(p->device);
   TRY(ensure_message(s));
-  const size_t bb = p->block_bytes(1);
+  const size_t bb = p->block_bytes(s->w);
   for (size_t q = 0; q < nq; ++q) {
     if (indices[q] >= p->n_d()) return fail(BF_ERR_ARG, "query index %llu out of range", (unsigned long long)indices[q]);
     s->idx_pin[q] = indices[q];
@@ -327,13 +372,13 @@ int bf_open_finish(bf_open_session* s, const uint64_t* indices, size_t nq, uint8
     bf::GatherParams gp{};
     gp.cw = s->cm->cw.as<uint4>();
     gp.cw_tree = s->cm->tree.as<uint4>();
-    gp.pi_first = gp.cw;
-    gp.pi_first_tree = s->cm->pi_tree.as<uint4>();
+    gp.pi_first = s->first_pi();
+    gp.pi_first_tree = s->first_tree();
     gp.pi_fold = s->w_pi_fold;
     gp.pi_trees = s->w_pi_trees;
     gp.idx = s->w_idx;
     gp.out = s->w_open;
-    gp.width = 1;
+    gp.width = s->w;
     gp.block_bytes = bb;
     gp.L = p->L;
     gp.d = s->d;
@@ -387,10 +432,16 @@ int bf_open(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, const uint
     std::memset(proof, 0, 32);
     return BF_OK;
   }
-  bf_open_session* s = nullptr;
-  TRY(bf_open_start(p, cm, point, values, nullptr, &s));
-  std::unique_ptr<bf_open_session, void (*)(bf_open_session*)> guard(s, bf_open_session_free);
   bfh::Challenger& ch = chp->c;
+  std::vector<uint8_t> scal;
+  if (cm->width > 1) {  // sample_random_scalars_by_eq (basefold.rs:166-167,398-408)
+    std::vector<u128> sc = sample_scalars_by_eq(cm->width, ch);
+    scal.resize(16 * sc.size());
+    for (size_t c = 0; c < sc.size(); ++c) bfh::store(scal.data() + 16 * c, sc[c]);
+  }
+  bf_open_session* s = nullptr;
+  TRY(bf_open_start(p, cm, point, values, scal.empty() ? nullptr : scal.data(), nullptr, &s));
+  std::unique_ptr<bf_open_session, void (*)(bf_open_session*)> guard(s, bf_open_session_free);
   while (true) {
     int round;
     uint8_t root[32], poly[32];

@@ -119,6 +119,30 @@ void put_elem(std::vector<uint8_t>& b, u128 v) {
   b.insert(b.end(), t, t + 16);
 }
 
+std::vector<u128> eq_table_host(const std::vector<u128>& x) {
+  std::vector<u128> e((size_t)1 << x.size(), 0);
+  e[0] = bfh::one();
+  for (size_t i = 0; i < x.size(); ++i) {  // eq_expand (multilinear.rs:216-222)
+    const size_t h = (size_t)1 << i;
+    for (size_t k = 0; k < h; ++k) {
+      const u128 hv = bfh::mul(e[k], x[i]);
+      e[h + k] = hv;
+      e[k] ^= hv;
+    }
+  }
+  return e;
+}
+
+std::vector<u128> sample_scalars_by_eq(size_t n, bfh::Challenger& ch) {
+  int log_n = 0;
+  while (((size_t)1 << log_n) < n) ++log_n;
+  std::vector<u128> r;
+  for (int i = 0; i < log_n; ++i) r.push_back(ch.sample_elem());
+  std::vector<u128> eq = eq_table_host(r);
+  eq.resize(n);
+  return eq;
+}
+
 }  // namespace bfapi
 
 using namespace bfapi;
@@ -225,30 +249,33 @@ namespace bfapi {
 // root and the first folded-codeword root are copied to roots_pin[0..64)
 // (pinned) when the stream reaches that point.
 int commit_enqueue(bf_pcs* p, bf_commitment* cm, const uint4* data, cudaStream_t st, uint8_t* roots_pin) {
-  const size_t nd = p->n_d();
-  CU(cm->cw.alloc_async(16 * nd, p->pool, st));
+  const size_t nd = p->n_d(), w = cm->width;
+  // For width 1 the first open round commits the codeword itself (as pairs),
+  // so that tree is built here; wider data is first combined in open.
+  const bool pairs = p->d > 0 && w == 1;
+  CU(cm->cw.alloc_async(16 * nd * w, p->pool, st));
   CU(cm->tree.alloc_async(32 * (2 * nd - 1), p->pool, st));
-  if (p->d > 0) CU(cm->pi_tree.alloc_async(32 * (nd - 1), p->pool, st));
+  if (pairs) CU(cm->pi_tree.alloc_async(32 * (nd - 1), p->pool, st));
   uint4* cw = cm->cw.as<uint4>();
   uint4* tree = cm->tree.as<uint4>();
   uint4* pit = cm->pi_tree.as<uint4>();
   {
-    // encode; for d >= 1 the last NTT pass also hashes the leaves
+    // encode; for width 1 and d >= 1 the last NTT pass also hashes the leaves
     ProfScope ps(p->prof, st, P_ENCODE);
-    CU(bf::launch_encode(data, cw, p->d, p->log2_c, 1, p->tw_view.as<bf::TwiddleView>(), st,
-                         p->d > 0 ? tree : nullptr, p->d > 0 ? pit : nullptr));
+    CU(bf::launch_encode(data, cw, p->d, p->log2_c, w, p->tw_view.as<bf::TwiddleView>(), st,
+                         pairs ? tree : nullptr, pairs ? pit : nullptr));
   }
-  if (p->d == 0) {
+  if (!pairs) {
     ProfScope ps(p->prof, st, P_LEAVES);
-    CU(bf::launch_leaves_elem(cw, tree, nd, 1, st));
+    CU(bf::launch_leaves_elem(cw, tree, nd, w, st));
   }
   {
     ProfScope ps(p->prof, st, P_TREE);
     CU(bf::launch_tree(tree, nd, st));
-    if (p->d > 0) CU(bf::launch_tree(pit, nd / 2, st));
+    if (pairs) CU(bf::launch_tree(pit, nd / 2, st));
   }
   CU(cudaMemcpyAsync(roots_pin, tree + 2 * (2 * nd - 2), 32, cudaMemcpyDeviceToHost, st));
-  if (p->d > 0) CU(cudaMemcpyAsync(roots_pin + 32, pit + 2 * (nd - 2), 32, cudaMemcpyDeviceToHost, st));
+  if (pairs) CU(cudaMemcpyAsync(roots_pin + 32, pit + 2 * (nd - 2), 32, cudaMemcpyDeviceToHost, st));
   return BF_OK;
 }
 
@@ -259,20 +286,29 @@ int commit_enqueue(bf_pcs* p, bf_commitment* cm, const uint4* data, cudaStream_t
 int eval_enqueue(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, uint4* scratch, cudaStream_t st,
                  uint8_t* value_pin) {
   const int d = p->d;
+  const size_t w = cm->width;
   const uint4* data = cm->data.as<uint4>();
   if (d == 0) {
-    CU(cudaMemcpyAsync(value_pin, data, 16, cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(value_pin, data, 16 * w, cudaMemcpyDeviceToHost, st));
     return BF_OK;
   }
-  const uint4* in = data;
-  for (int k = d - 1; k >= 0; --k) {
+  for (size_t col = 0; col < w; ++col) {  // one value per column (basefold.rs:126-131)
     uint4 r;
-    std::memcpy(&r, point + 16 * k, 16);
-    ProfScope ps(p->prof, st, P_FIX);
-    CU(bf::launch_fix(in, scratch, (size_t)1 << k, r, nullptr, 0, nullptr, st));
-    in = scratch;
+    std::memcpy(&r, point + 16 * (d - 1), 16);
+    {
+      ProfScope ps(p->prof, st, P_FIX);
+      if (w == 1)
+        CU(bf::launch_fix(data, scratch, (size_t)1 << (d - 1), r, nullptr, 0, nullptr, st));
+      else
+        CU(bf::launch_fix_column(data, w, col, scratch, (size_t)1 << (d - 1), r, st));
+    }
+    for (int k = d - 2; k >= 0; --k) {
+      std::memcpy(&r, point + 16 * k, 16);
+      ProfScope ps(p->prof, st, P_FIX);
+      CU(bf::launch_fix(scratch, scratch, (size_t)1 << k, r, nullptr, 0, nullptr, st));
+    }
+    CU(cudaMemcpyAsync(value_pin + 16 * col, scratch, 16, cudaMemcpyDeviceToHost, st));
   }
-  CU(cudaMemcpyAsync(value_pin, scratch, 16, cudaMemcpyDeviceToHost, st));
   return BF_OK;
 }
 
@@ -380,7 +416,7 @@ int bf_commit(bf_pcs* p, const uint8_t* evals, size_t width, bf_commitment** out
   if (!p || !evals || !out) return fail(BF_ERR_ARG, "null argument");
   if (p->device < 0) return fail(BF_ERR_ARG, "verifier-only pcs (device < 0)");
   *out = nullptr;
-  if (width != 1) return fail(BF_ERR_UNSUPPORTED, "width %zu: only width 1 runs on the GPU in this build", width);
+  if (width == 0 || width > 4096) return fail(BF_ERR_ARG, "width %zu out of range (1..4096)", width);
   DeviceGuard g(p->device);
   std::unique_ptr<bf_commitment> cm(new bf_commitment());
   cm->pcs = p;
@@ -398,7 +434,7 @@ int bf_commit_device(bf_pcs* p, const void* d_evals, size_t width, bf_commitment
   if (!p || !d_evals || !out) return fail(BF_ERR_ARG, "null argument");
   if (p->device < 0) return fail(BF_ERR_ARG, "verifier-only pcs (device < 0)");
   *out = nullptr;
-  if (width != 1) return fail(BF_ERR_UNSUPPORTED, "width %zu: only width 1 runs on the GPU in this build", width);
+  if (width == 0 || width > 4096) return fail(BF_ERR_ARG, "width %zu out of range (1..4096)", width);
   if (reinterpret_cast<uintptr_t>(d_evals) & 15) return fail(BF_ERR_ARG, "device evaluations must be 16-byte aligned");
   DeviceGuard g(p->device);
   std::unique_ptr<bf_commitment> cm(new bf_commitment());
@@ -436,14 +472,14 @@ int bf_commitment_data(const bf_commitment* cm, uint8_t* evals, size_t cap) {
 
 int bf_eval(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, uint8_t* values) {
   if (!p || !cm || !values || (p->d > 0 && !point)) return fail(BF_ERR_ARG, "null argument");
-  if (cm->width != 1) return fail(BF_ERR_UNSUPPORTED, "width != 1");
   DeviceGuard g(p->device);
   const size_t half = p->d > 0 ? ((size_t)1 << (p->d - 1)) : 1;
   if (p->eval_ws.bytes < 16 * half) CU(p->eval_ws.alloc(16 * half));
+  CU(p->pinned.ensure(16 * cm->width + 64));
   TRY(eval_enqueue(p, cm, point, p->eval_ws.as<uint4>(), p->stream, p->pinned.b()));
   CU(cudaStreamSynchronize(p->stream));
   p->prof.drain();
-  std::memcpy(values, p->pinned.b(), 16);
+  std::memcpy(values, p->pinned.b(), 16 * cm->width);
   return BF_OK;
 }
 

@@ -112,20 +112,6 @@ bool merkle_verify_host(const uint8_t root[32], int log_h, uint64_t index, const
   return std::memcmp(cur, root, 32) == 0;
 }
 
-std::vector<u128> eq_host(const std::vector<u128>& x) {
-  std::vector<u128> e((size_t)1 << x.size(), 0);
-  e[0] = bfh::one();
-  for (size_t i = 0; i < x.size(); ++i) {
-    size_t h = (size_t)1 << i;
-    for (size_t k = 0; k < h; ++k) {
-      u128 hv = bfh::mul(e[k], x[i]);
-      e[h + k] = hv;
-      e[k] ^= hv;
-    }
-  }
-  return e;
-}
-
 uint64_t rev_bits(uint64_t x, int bits) {
   uint64_t r = 0;
   for (int i = 0; i < bits; ++i) r |= ((x >> i) & 1) << (bits - 1 - i);
@@ -150,13 +136,8 @@ extern "C" int bf_verify(const bf_pcs* p, const uint8_t root[32], const uint8_t*
   if (width == 1) {
     scalars = {ONE};
     claim = vals[0];
-  } else {  // sample_random_scalars_by_eq (basefold.rs:398-408)
-    int lw = 0;
-    while (((size_t)1 << lw) < width) ++lw;
-    std::vector<u128> rr;
-    for (int i = 0; i < lw; ++i) rr.push_back(ch.sample_elem());
-    scalars = eq_host(rr);
-    scalars.resize(width);
+  } else {
+    scalars = sample_scalars_by_eq(width, ch);
     for (size_t i = 0; i < width; ++i) claim ^= bfh::mul(scalars[i], vals[i]);
   }
   if ((int)pf.round_polys.size() != d || (int)pf.pi_comms.size() != d) return BF_VERIFY_MALFORMED;

@@ -43,6 +43,8 @@ cudaError_t launch_fold_leaves(const uint4* pi, uint4* out, uint4* leaves, size_
                                const uint4* tw_hi, uint4 r, cudaStream_t st);
 cudaError_t launch_fix(const uint4* in, uint4* out, size_t half, uint4 r, const uint4* heq, size_t next_half,
                        uint32_t* acc, cudaStream_t st);
+cudaError_t launch_fix_column(const uint4* in, size_t width, size_t col, uint4* out, size_t half, uint4 r,
+                              cudaStream_t st);
 cudaError_t launch_combine_rows(const uint4* rows, size_t nrows, size_t width, const uint4* scalars, uint4* out,
                                 cudaStream_t st);
 

@@ -69,6 +69,7 @@ static unsigned grid_for(size_t n, int threads, int per_sm = 8) {
 // ---------------------------------------------------------------------------
 struct PassParams {
   int n, s_lo, T, first;
+  int width;  // row width of m and cw; blockIdx.y is the column
   // Last pass only: also hash the codeword leaves H(cw[q]) and the first
   // folded-codeword leaves H(cw[2s] || cw[2s+1]) from the tile in shared
   // memory (null: no hashing).  The hashing is integer-ALU work and the
@@ -90,14 +91,15 @@ __global__ void __launch_bounds__(256) ntt_pass_kernel(const uint4* __restrict__
   const uint32_t hi = rem >> s_lo;
   const uint32_t tsize = 1u << T;
   const size_t coset_base = (size_t)j << n;
+  const size_t w = (size_t)p.width, col = blockIdx.y;
 
   if (p.first) {
     const size_t base = (size_t)brev_bits(u, s_lo) << T;
-    for (uint32_t i = threadIdx.x; i < tsize; i += blockDim.x) sm[brev_bits(i, T)] = m[base + i];
+    for (uint32_t i = threadIdx.x; i < tsize; i += blockDim.x) sm[brev_bits(i, T)] = m[(base + i) * w + col];
   } else {
     for (uint32_t i = threadIdx.x; i < tsize; i += blockDim.x) {
       const size_t x = ((size_t)hi << (s_lo + T)) | ((size_t)i << s_lo) | u;
-      sm[i] = cw[coset_base + x];
+      sm[i] = cw[(coset_base + x) * w + col];
     }
   }
   __syncthreads();
@@ -123,7 +125,7 @@ __global__ void __launch_bounds__(256) ntt_pass_kernel(const uint4* __restrict__
 
   for (uint32_t i = threadIdx.x; i < tsize; i += blockDim.x) {
     const size_t x = ((size_t)hi << (s_lo + T)) | ((size_t)i << s_lo) | u;
-    cw[coset_base + x] = sm[i];
+    cw[(coset_base + x) * w + col] = sm[i];
   }
   if (HASH) {
     // last pass: s_lo = 0, the tile is the contiguous run [coset_base + hi 2^T, +2^T)
@@ -138,19 +140,19 @@ __global__ void __launch_bounds__(256) ntt_pass_kernel(const uint4* __restrict__
   }
 }
 
-// n = 0: every coset is m[0].
-__global__ void replicate_kernel(const uint4* __restrict__ m, uint4* __restrict__ cw, size_t c) {
-  for (size_t i = threadIdx.x; i < c; i += blockDim.x) cw[i] = m[0];
+// n = 0: every coset is the single row of m.
+__global__ void replicate_kernel(const uint4* __restrict__ m, uint4* __restrict__ cw, size_t c, size_t w) {
+  for (size_t i = threadIdx.x; i < c * w; i += blockDim.x) cw[i] = m[i % w];
 }
 
 constexpr int kNttMaxT = 12;
 
 cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t width, const TwiddleView* tw,
                           cudaStream_t st, uint4* leaves, uint4* pair_leaves) {
-  if (width != 1) return cudaErrorInvalidValue;
+  if (width == 0 || width > 65535 || (width != 1 && (leaves || pair_leaves))) return cudaErrorInvalidValue;
   const size_t c = (size_t)1 << log2_c;
   if (n == 0) {
-    replicate_kernel<<<1, 32, 0, st>>>(m, cw, c);
+    replicate_kernel<<<1, 128, 0, st>>>(m, cw, c, width);
     COUNT_LAUNCH();
     return cudaGetLastError();
   }
@@ -172,14 +174,15 @@ cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t w
     p.T = T;
     p.s_lo = top - T;
     p.first = (pidx == 0);
+    p.width = (int)width;
     const bool last = (pidx == passes - 1);
     p.leaves = last ? leaves : nullptr;
     p.pair_leaves = last ? pair_leaves : nullptr;
-    const size_t blocks = c << (n - T);
+    const dim3 grid((unsigned)(c << (n - T)), (unsigned)width);
     if (p.leaves)
-      ntt_pass_kernel<true><<<(unsigned)blocks, 256, sizeof(uint4) << T, st>>>(m, cw, p, tw);
+      ntt_pass_kernel<true><<<grid, 256, sizeof(uint4) << T, st>>>(m, cw, p, tw);
     else
-      ntt_pass_kernel<false><<<(unsigned)blocks, 256, sizeof(uint4) << T, st>>>(m, cw, p, tw);
+      ntt_pass_kernel<false><<<grid, 256, sizeof(uint4) << T, st>>>(m, cw, p, tw);
     COUNT_LAUNCH();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -242,9 +245,38 @@ __global__ void __launch_bounds__(256) tree_top_kernel(uint4* level, size_t n, u
   if (root_out && threadIdx.x == 0) store_digest(root_out, 0, load_digest(cur, 0));
 }
 
+// Leaf of a row of `width` elements: keccak256 of its 16*width bytes
+// (GenericHasher over the row's bincode, p3/src/symmetric.rs:16-25), any
+// number of 136-byte blocks.
+__global__ void __launch_bounds__(128) leaves_rows_kernel(const uint4* __restrict__ cw, uint4* __restrict__ leaves,
+                                                          size_t n, size_t width) {
+  const size_t lanes = 2 * width;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    uint2 s[25];
+#pragma unroll
+    for (int k = 0; k < 25; ++k) s[k] = make_uint2(0, 0);
+    const uint2* row = reinterpret_cast<const uint2*>(cw + i * width);
+    size_t k = 0;
+    for (; k + 17 <= lanes; k += 17) {  // full blocks
+      for (int q = 0; q < 17; ++q) s[q] = kx2(s[q], row[k + q]);
+      keccak_f1600(s);
+    }
+    const int rem = (int)(lanes - k);  // 0..16 lanes left
+    for (int q = 0; q < rem; ++q) s[q] = kx2(s[q], row[k + q]);
+    // pad10*1: 0x01 after the message, 0x80 in the last byte of the block
+    for (int q = 0; q < 17; ++q)
+      if (q == rem) s[q].x ^= 0x01u;
+    s[16].y ^= 0x80000000u;
+    keccak_f1600(s);
+    store_digest(leaves, i, digest_from_state(s));
+  }
+}
+
 cudaError_t launch_leaves_elem(const uint4* cw, uint4* leaves, size_t n, size_t width, cudaStream_t st) {
-  if (width != 1) return cudaErrorInvalidValue;
-  leaves_elem_kernel<<<grid_for(n, 128, 16), 128, 0, st>>>(cw, leaves, n);
+  if (width == 1)
+    leaves_elem_kernel<<<grid_for(n, 128, 16), 128, 0, st>>>(cw, leaves, n);
+  else
+    leaves_rows_kernel<<<grid_for(n, 128, 16), 128, 0, st>>>(cw, leaves, n, width);
   COUNT_LAUNCH();
   return cudaGetLastError();
 }
@@ -423,6 +455,23 @@ __global__ void __launch_bounds__(256) fix_kernel(const uint4* in, uint4* out, s
 cudaError_t launch_fix(const uint4* in, uint4* out, size_t half, uint4 r, const uint4* heq, size_t next_half,
                        uint32_t* acc, cudaStream_t st) {
   fix_kernel<<<grid_for(half, 256), 256, 0, st>>>(in, out, half, r, heq, next_half, acc);
+  COUNT_LAUNCH();
+  return cudaGetLastError();
+}
+
+// First fix_last_var of column `col` of a row-major matrix with `width`
+// columns: out[b] = in[b] + r (in[b + half] - in[b]) on that column.
+__global__ void __launch_bounds__(256) fix_column_kernel(const uint4* __restrict__ in, size_t width, size_t col,
+                                                         uint4* __restrict__ out, size_t half, uint4 r) {
+  for (size_t b = (size_t)blockIdx.x * blockDim.x + threadIdx.x; b < half; b += (size_t)gridDim.x * blockDim.x) {
+    const uint4 lo = in[b * width + col], hi = in[(b + half) * width + col];
+    out[b] = gf_add(lo, gf_mul(r, gf_add(hi, lo)));
+  }
+}
+
+cudaError_t launch_fix_column(const uint4* in, size_t width, size_t col, uint4* out, size_t half, uint4 r,
+                              cudaStream_t st) {
+  fix_column_kernel<<<grid_for(half, 256), 256, 0, st>>>(in, width, col, out, half, r);
   COUNT_LAUNCH();
   return cudaGetLastError();
 }

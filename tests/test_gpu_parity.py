@@ -97,12 +97,10 @@ def test_open_matches_committed_vectors(bg):
     vec = json.load(open(os.path.join(GOLDEN, "oracle_vectors.json")))
     for case in vec["basefold"]:
         n, log2_c, w, seed = case["n"], case["log2_c"], case["width"], case["seed"]
-        if w != 1:
-            continue
         data = rand.random_elems((w << n) + n, seed)
         evals, point = data[: w << n], data[w << n:]
         pcs = setup_pcs(bg, n, log2_c)
-        comm = pcs.commit(evals)
+        comm = pcs.commit(evals, width=w)
         assert comm.root.hex() == case["root"]
         values = pcs.eval(pcs.data(comm), point)
         assert [bytes(v).hex() for v in values] == case["values"]
@@ -161,3 +159,39 @@ def test_sumcheck_prover_verifies(bg, k):
         claim = O.gf_mul(claim, O.from_ints([ONE]))
     rp, r, fe, fc = bg.prove_sumcheck(k, polys, claim, bg.GenericChallenger(b"x"))
     assert O.sumcheck_verify(k, n, claim, rp, fe, O.challenger_blob(b"x")) == 0
+
+
+def harness_w(bg, n, log2_c, width, seed):
+    data = rand.random_elems((width << n) + n, seed)
+    evals, point = data[: width << n], data[width << n:]
+    pcs = setup_pcs(bg, n, log2_c)
+    comm = pcs.commit(evals, width=width)
+    ch = bg.GenericChallenger.keccak256()
+    ch.observe(comm.root)
+    values = pcs.eval(pcs.data(comm), point)
+    ch.observe_ext_slice(values)
+    proof = pcs.open(comm, [bg.PolyEvals(values, point)], ch.clone())
+    return pcs, comm, evals, point, values, ch, proof
+
+
+@pytest.mark.parametrize("log2_c", [0, 1, 2])
+def test_reference_harness_matrix_matches_oracle(bg, log2_c):
+    """The reference's own test matrix for the binary code (basefold.rs:480-490
+    over poly-commit/src/lib.rs:64-105): num_vars 0..9, num_polys 1..9."""
+    for n in range(0, 10):
+        for width in range(1, 10):
+            pcs, comm, evals, point, values, ch, proof = harness_w(bg, n, log2_c, width, 10000 + 100 * n + width)
+            root_o, values_o, blob = O.harness_prepare(n, log2_c, evals, point, width)
+            assert comm.root == root_o, (n, width, log2_c)
+            assert np.array_equal(values, values_o), (n, width, log2_c)
+            assert ch.state() == blob
+            assert proof == O.open_proof(n, log2_c, evals, point, values_o, blob, width), (n, width, log2_c)
+            pcs.verify(comm.root, [bg.PolyEvals(values, point)], proof, ch.clone())
+
+
+def test_wide_commit_large(bg):
+    n, log2_c, width = 15, 1, 3
+    pcs, comm, evals, point, values, ch, proof = harness_w(bg, n, log2_c, width, 77)
+    root_o, values_o, blob = O.harness_prepare(n, log2_c, evals, point, width)
+    assert comm.root == root_o and np.array_equal(values, values_o)
+    assert proof == O.open_proof(n, log2_c, evals, point, values_o, blob, width)
