@@ -67,6 +67,11 @@ def barrier(ws):
         dist.barrier()
 
 
+def throughput(ws, steps, ms):
+    """Whole-job rate: every rank ran `steps` steps; `ms` is the slowest rank's time."""
+    return ws * steps / (ms / 1e3)
+
+
 def max_over_ranks(ws, v, device=None):
     if ws == 1:
         return v
@@ -377,7 +382,7 @@ def main():
     prof = pcs.profile_read()
     pcs.profile(False)
     ms = max_over_ranks(ws, ev0.elapsed_time(ev1), device=f"cuda:{local}")
-    value = ws * args.steps / (ms / 1e3)
+    value = throughput(ws, args.steps, ms)
 
     # ---- timed region: host buffers through the C ABI ----------------------
     for _ in range(2):
@@ -391,7 +396,7 @@ def main():
     torch.cuda.synchronize()
     barrier(ws)
     ms_e2e = max_over_ranks(ws, ev0.elapsed_time(ev1), device=f"cuda:{local}")
-    e2e = ws * args.steps / (ms_e2e / 1e3)
+    e2e = throughput(ws, args.steps, ms_e2e)
 
     if rank != 0:
         return
