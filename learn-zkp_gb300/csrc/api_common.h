@@ -160,6 +160,14 @@ namespace bfapi {
 int commit_enqueue(bf_pcs* p, bf_commitment* cm, const uint4* data, cudaStream_t st, uint8_t* roots_pin);
 int eval_enqueue(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, uint4* scratch, cudaStream_t st,
                  uint8_t* value_pin);
+struct OpenSessionFwd;
+}  // namespace bfapi
+
+struct bf_open_session;
+namespace bfapi {
+bool open_tail_eligible(const bf_open_session* s, const bfh::Challenger& ch);
+int open_tail_enqueue(bf_open_session* s, const bfh::Challenger& ch);
+int open_tail_complete(bf_open_session* s, bfh::Challenger& ch);
 }  // namespace bfapi
 
 struct bf_challenger {

@@ -47,6 +47,7 @@ struct Job {
   bfh::Challenger ch;
   DevBuf eval_ws;
   int state = J_COMMIT;
+  bool tail_running = false;  // the remaining rounds run on the device
   size_t footprint = 0;
   uint8_t value[16];
 };
@@ -177,7 +178,17 @@ int step(bf_engine* e, Job* j) {
     if (!ready) return 0;
     int round;
     uint8_t root[32], poly[32];
-    TRY(bf_open_round(j->sess, &round, root, poly));
+    if (j->tail_running) {
+      TRY(open_tail_complete(j->sess, j->ch));
+      j->tail_running = false;
+      round = -1;
+    } else if (open_tail_eligible(j->sess, j->ch)) {
+      TRY(open_tail_enqueue(j->sess, j->ch));
+      j->tail_running = true;
+      return 1;
+    } else {
+      TRY(bf_open_round(j->sess, &round, root, poly));
+    }
     if (round >= 0) {
       j->ch.observe(root, 32);
       j->ch.observe(poly, 32);

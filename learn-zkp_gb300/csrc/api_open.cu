@@ -8,6 +8,7 @@
 // several can be in flight on different streams.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <memory>
 #include <vector>
@@ -53,7 +54,10 @@ struct bf_open_session {
   uint4* w_pi_first = nullptr;
   uint4* w_pi_first_tree = nullptr;
   uint4* w_poly_first = nullptr;
-  std::unique_ptr<PinnedBuf> pin;  // [0,64) staging, [64,64+16d) point, indices, openings
+  uint8_t* w_tail = nullptr;       // tail kernel: inputs (scalars, transcript) and result
+  bool tail_pending = false;       // the tail kernel's result is in flight
+  std::unique_ptr<PinnedBuf> pin;  // [0,64) staging, [64,64+16(w+d)) scalars and point, indices, openings;
+                                   // tail kernel inputs at tail_in_off()
   uint64_t* idx_pin = nullptr;
   uint8_t* open_pin = nullptr;
 
@@ -67,6 +71,10 @@ struct bf_open_session {
   const uint4* first_pi() const { return w == 1 ? cm->cw.as<uint4>() : w_pi_first; }
   const uint4* first_poly() const { return w == 1 ? cm->data.as<uint4>() : w_poly_first; }
   const uint4* first_tree() const { return w == 1 ? cm->pi_tree.as<uint4>() : w_pi_first_tree; }
+  // Pinned offset of the tail kernel's inputs: past the staging, the eq
+  // scalars and the point, whose host-to-device copies may still be queued
+  // when the tail is enqueued.
+  size_t tail_in_off() const { return 64 + 16 * ((size_t)(d > 0 ? d : 1) + w); }
   ~bf_open_session() {
     if (st) cudaStreamSynchronize(st);
     if (ev) cudaEventDestroy(ev);
@@ -81,6 +89,13 @@ struct bf_open_session {
 namespace {
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Tail kernel I/O: per round 3 scalars in, 64 bytes out; final poly and the
+// transcript state; the transcript input.
+constexpr size_t kTailScalOff = 0;
+size_t tail_result_off(int d) { return align256(48 * (size_t)(d > 0 ? d : 1)); }
+size_t tail_tr_off(int d) { return tail_result_off(d) + align256(64 * (size_t)(d + 1) + 16 + 4 + 2 * bf::kTailTranscriptMax); }
+size_t tail_bytes(int d) { return tail_tr_off(d) + 2 * bf::kTailTranscriptMax; }
 
 int session_alloc(bf_open_session* s) {
   bf_pcs* p = s->p;
@@ -102,6 +117,7 @@ int session_alloc(bf_open_session* s) {
   const size_t o_hi = take(16 * ((size_t)1 << hi_vars)), o_stage = take(48 * n_point);
   const size_t bb = p->block_bytes(s->w);
   const size_t o_idx = take(8 * (p->Q + 1)), o_open = take(bb * (p->Q + 1));
+  const size_t o_tail = take(tail_bytes(d));
   size_t o_sc = 0, o_pif = 0, o_pift = 0, o_polyf = 0;
   if (s->w > 1) {
     o_sc = take(16 * s->w);
@@ -117,6 +133,7 @@ int session_alloc(bf_open_session* s) {
     s->w_pi_first_tree = reinterpret_cast<uint4*>(b + o_pift);
     s->w_poly_first = reinterpret_cast<uint4*>(b + o_polyf);
   }
+  s->w_tail = b + o_tail;
   s->w_point = reinterpret_cast<uint4*>(b + o_point);
   s->w_pi_fold = reinterpret_cast<uint4*>(b + o_fold);
   s->w_pi_trees = reinterpret_cast<uint4*>(b + o_tree);
@@ -127,7 +144,9 @@ int session_alloc(bf_open_session* s) {
   s->w_stage = b + o_stage;
   s->w_idx = reinterpret_cast<uint64_t*>(b + o_idx);
   s->w_open = b + o_open;
-  const size_t pin_bytes = 64 + 16 * (n_point + s->w) + 8 * (p->Q + 1) + bb * (p->Q + 1);
+  const size_t pin_bytes =
+      std::max(64 + 16 * (n_point + s->w) + 8 * (p->Q + 1) + bb * (p->Q + 1),
+               std::max(tail_bytes(d), s->tail_in_off() + 48 * (size_t)(d + 1) + 2 * (size_t)bf::kTailTranscriptMax));
   if (!p->pinned_cache.empty()) {
     s->pin = std::move(p->pinned_cache.back());
     p->pinned_cache.pop_back();
@@ -180,6 +199,105 @@ int ensure_message(bf_open_session* s) {
 }
 
 }  // namespace
+
+namespace bfapi {
+
+// The current round and every later one fit the single-block kernel, and the
+// transcript input fits its buffer.
+bool open_tail_eligible(const bf_open_session* s, const bfh::Challenger& ch) {
+  if (s->i < 0) return false;
+  if ((s->p->n_i(s->i) >> 1) > ((size_t)1 << bf::kTailMaxLeavesLog)) return false;
+  return ch.in.size() + 64 <= (size_t)bf::kTailTranscriptMax && ch.out.size() <= 32;
+}
+
+// Runs every remaining round on the device with transcript `ch`: enqueues
+// the tail kernel and the copy of its result; open_tail_complete reads it.
+int open_tail_enqueue(bf_open_session* s, const bfh::Challenger& ch) {
+  bf_pcs* p = s->p;
+  const int i0 = s->i, d = s->d;
+  uint8_t* pin = s->pin->b();
+  // Inputs go where no copy still in flight reads or writes (the previous
+  // round's staging copy, bf_open_start's scalar and point copies): scalars
+  // r_i, r_i^-1, correcting factor for rounds 0..i0, then the transcript.
+  uint8_t* in = pin + s->tail_in_off();
+  for (int i = 0; i <= i0; ++i) {
+    bfh::store(in + 48 * i, s->r[i]);
+    bfh::store(in + 48 * i + 16, s->r_inv[i]);
+    bfh::store(in + 48 * i + 32, s->corr[i]);
+  }
+  uint8_t* tr = in + 48 * (size_t)(d + 1);
+  std::memcpy(tr, ch.in.data(), ch.in.size());
+  std::memcpy(tr + bf::kTailTranscriptMax, ch.out.data(), ch.out.size());
+  cudaStream_t st = s->st;
+  CU(cudaMemcpyAsync(s->w_tail, in, 48 * (size_t)(i0 + 1), cudaMemcpyHostToDevice, st));
+  CU(cudaMemcpyAsync(s->w_tail + tail_tr_off(d), tr, 2 * bf::kTailTranscriptMax, cudaMemcpyHostToDevice, st));
+  bf::TailParams tp{};
+  tp.i0 = i0;
+  tp.d = d;
+  tp.log2_c = p->log2_c;
+  tp.pi_first = s->first_pi();
+  tp.pi_fold = s->w_pi_fold;
+  tp.pi_trees = s->w_pi_trees;
+  tp.poly_first = s->first_poly();
+  tp.poly = s->w_poly;
+  tp.heq = s->w_heq;
+  tp.stage_i0 = s->stage(i0);
+  tp.root_in_params = (i0 == d - 1 && s->w == 1);
+  if (tp.root_in_params) {
+    std::memcpy(&tp.root_lo, s->cm->pi_root, 16);
+    std::memcpy(&tp.root_hi, s->cm->pi_root + 16, 16);
+  }
+  tp.scal = reinterpret_cast<const uint4*>(s->w_tail + kTailScalOff);
+  tp.outer = to_uint4(s->outer_val);
+  tp.inner = to_uint4(s->inner_val);
+  tp.delta = to_uint4(s->delta_prod);
+  tp.tw = p->tw_view.as<bf::TwiddleView>();
+  tp.tr_in = s->w_tail + tail_tr_off(d);
+  tp.tr_in_len = (int)ch.in.size();
+  tp.tr_out = s->w_tail + tail_tr_off(d) + bf::kTailTranscriptMax;
+  tp.tr_out_len = (int)ch.out.size();
+  tp.result = s->w_tail + tail_result_off(d);
+  {
+    ProfScope ps(p->prof, st, P_TREE);
+    CU(bf::launch_open_tail(tp, st));
+  }
+  const size_t res_bytes = 64 * (size_t)(i0 + 1) + 16 + 4 + 2 * bf::kTailTranscriptMax;
+  CU(cudaMemcpyAsync(pin, tp.result, res_bytes, cudaMemcpyDeviceToHost, st));
+  CU(cudaEventRecord(s->ev, st));
+  s->pending = true;
+  s->tail_pending = true;
+  s->msg_ready = false;
+  return BF_OK;
+}
+
+// Reads the tail kernel's result: the rounds' roots and compressed round
+// polynomials, the final polynomial, and the transcript state (into `ch`).
+int open_tail_complete(bf_open_session* s, bfh::Challenger& ch) {
+  if (!s->tail_pending) return fail(BF_ERR_ARG, "no tail in flight");
+  CU(cudaStreamSynchronize(s->st));
+  s->p->prof.drain();
+  s->pending = false;
+  s->tail_pending = false;
+  const uint8_t* res = s->pin->b();
+  const int rounds = s->i + 1;
+  for (int k = 0; k < rounds; ++k) {
+    const uint8_t* rec = res + 64 * (size_t)k;
+    s->roots.insert(s->roots.end(), rec, rec + 32);
+    put_u64(s->rounds, 2);
+    s->rounds.insert(s->rounds.end(), rec + 32, rec + 64);
+  }
+  const uint8_t* fin = res + 64 * (size_t)rounds;
+  s->final_val = bfh::load(fin);
+  const uint8_t* stt = fin + 16;
+  const int in_len = stt[0] | (stt[1] << 8), out_len = stt[2];
+  ch.in.assign(stt + 4, stt + 4 + in_len);
+  ch.out.assign(stt + 4 + in_len, stt + 4 + in_len + out_len);
+  s->i = -1;
+  s->final_ready = true;
+  return BF_OK;
+}
+
+}  // namespace bfapi
 
 extern "C" {
 
@@ -443,6 +561,11 @@ int bf_open(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, const uint
   TRY(bf_open_start(p, cm, point, values, scal.empty() ? nullptr : scal.data(), nullptr, &s));
   std::unique_ptr<bf_open_session, void (*)(bf_open_session*)> guard(s, bf_open_session_free);
   while (true) {
+    if (open_tail_eligible(s, ch)) {  // the remaining rounds, transcript on the device
+      TRY(open_tail_enqueue(s, ch));
+      TRY(open_tail_complete(s, ch));
+      break;
+    }
     int round;
     uint8_t root[32], poly[32];
     TRY(bf_open_round(s, &round, root, poly));

@@ -73,6 +73,33 @@ cudaError_t launch_prod_fix(uint4* const* out, const uint4* const* in, int k, si
                             size_t next_half, uint32_t* acc, cudaStream_t st);
 
 unsigned long long launches_total();
+void count_launch();
+
+// ---- the last rounds of open in one block with the transcript on the device
+constexpr int kTailThreads = 512;
+constexpr int kTailTranscriptMax = 512;  // bytes of transcript input buffer the kernel can hold
+constexpr int kTailMaxLeavesLog = 11;    // rounds whose next tree has <= 2^11 leaves
+struct TailParams {
+  int i0, d, log2_c;
+  const uint4* pi_first;    // folded codeword input of round d-1
+  uint4* pi_fold;           // fold outputs of rounds d-1 .. 0
+  uint4* pi_trees;          // trees of rounds d-2 .. 0
+  const uint4* poly_first;  // sumcheck polynomial of round d-1
+  uint4* poly;              // sumcheck polynomial after each fix (in place)
+  const uint4* heq;         // half eq table
+  const uint8_t* stage_i0;  // root (32 B) + reduction S (16 B) of round i0
+  int root_in_params;       // round i0's root is root_lo/root_hi instead of stage_i0
+  uint4 root_lo, root_hi;
+  const uint4* scal;        // per round i: r_i, r_i^-1, correcting factor
+  uint4 outer, inner, delta;
+  const TwiddleView* tw;
+  const uint8_t* tr_in;     // transcript input buffer
+  int tr_in_len;
+  const uint8_t* tr_out;    // transcript output buffer
+  int tr_out_len;
+  uint8_t* result;          // per round: root, c0, c2 (64 B); final poly (16 B); transcript state
+};
+cudaError_t launch_open_tail(const TailParams& p, cudaStream_t st);
 
 // Test hooks.
 cudaError_t launch_test_mul(const uint4* a, const uint4* b, uint4* out, size_t n, cudaStream_t st);

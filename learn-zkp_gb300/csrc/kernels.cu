@@ -34,6 +34,7 @@ __device__ __forceinline__ uint4 gf_one() { return make_uint4(1u, 0u, 0u, 0xc200
 // Number of kernels this library has launched (all devices, all streams).
 static std::atomic<unsigned long long> g_launches{0};
 unsigned long long launches_total() { return g_launches.load(); }
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 #define COUNT_LAUNCH() g_launches.fetch_add(1, std::memory_order_relaxed)
 
 static int g_num_sms = 0;
