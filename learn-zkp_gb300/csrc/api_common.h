@@ -158,16 +158,21 @@ struct bf_pcs;
 struct bf_commitment;
 namespace bfapi {
 int commit_enqueue(bf_pcs* p, bf_commitment* cm, const uint4* data, cudaStream_t st, uint8_t* roots_pin);
+// The value lands in value_pin; *value_dev (when given) receives where it
+// lives on the device.
 int eval_enqueue(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, uint4* scratch, cudaStream_t st,
-                 uint8_t* value_pin);
-struct OpenSessionFwd;
+                 uint8_t* value_pin, const uint4** value_dev = nullptr);
 }  // namespace bfapi
 
 struct bf_open_session;
 namespace bfapi {
-bool open_tail_eligible(const bf_open_session* s, const bfh::Challenger& ch);
-int open_tail_enqueue(bf_open_session* s, const bfh::Challenger& ch);
-int open_tail_complete(bf_open_session* s, bfh::Challenger& ch);
+int open_start_impl(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, const uint8_t* values,
+                    const uint8_t* scalars, void* stream, bf_open_session** out);
+int open_resident_enqueue(bf_open_session* s, const bfh::Challenger& ch, const uint4* root_dev,
+                          const uint4* value_dev);
+int open_resident_complete(bf_open_session* s, bfh::Challenger& ch);
+int open_finish_enqueue(bf_open_session* s, const uint64_t* indices, size_t nq);
+int open_finish_complete(bf_open_session* s, uint8_t* proof, size_t cap, size_t* proof_len);
 }  // namespace bfapi
 
 struct bf_challenger {

@@ -3,12 +3,15 @@
 //
 // Each job follows the reference's harness (poly-commit/src/lib.rs:80-100):
 // commit, observe the root, evaluate at the point, observe the value, open
-// with a fresh keccak256 transcript.  A job is a state machine whose GPU work
-// runs on one stream of a pool; the engine admits jobs while streams and the
-// HBM budget allow, and advances whichever job's last GPU step has finished,
-// so small latency-bound proofs overlap with large ones and new requests join
-// between the rounds of running ones (continuous batching).  Proof bytes are
-// identical to the one-at-a-time path.
+// with a fresh keccak256 transcript.  A job runs on one stream of a pool.  At
+// admission the whole commit, evaluation and open up to the final polynomial
+// are enqueued at once, with the transcript on the device, so the GPU never
+// waits for the host inside a proof; the host then samples the query
+// positions from the returned transcript and reads the openings.  The engine
+// admits jobs while streams and the HBM budget allow and advances whichever
+// job's GPU work has finished, so small latency-bound proofs overlap with
+// large ones and new requests join while others run (continuous batching).
+// Proof bytes are identical to the one-at-a-time path.
 #include <cuda_runtime.h>
 
 #include <chrono>
@@ -32,7 +35,7 @@ double now_ms() {
   return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
 }
 
-enum JobState { J_COMMIT = 0, J_EVAL = 1, J_ROUNDS = 2, J_DONE = 3 };
+enum JobState { J_OPEN = 0, J_GATHER = 1, J_DONE = 2 };
 
 struct Job {
   bf_job* pub = nullptr;
@@ -41,15 +44,12 @@ struct Job {
   bf_pcs* pcs = nullptr;
   int slot = -1;
   cudaStream_t st = nullptr;
-  cudaEvent_t ev = nullptr;
   std::unique_ptr<bf_commitment> cm;
   bf_open_session* sess = nullptr;
   bfh::Challenger ch;
   DevBuf eval_ws;
-  int state = J_COMMIT;
-  bool tail_running = false;  // the remaining rounds run on the device
+  int state = J_OPEN;
   size_t footprint = 0;
-  uint8_t value[16];
 };
 
 }  // namespace
@@ -104,8 +104,6 @@ void finish_job(bf_engine* e, Job* j, int status) {
   }
   j->eval_ws.release();
   j->cm.reset();
-  if (j->ev) cudaEventDestroy(j->ev);
-  j->ev = nullptr;
   if (j->slot >= 0) e->free_slots.push_back(j->slot);
   e->mem_used -= j->footprint;
   j->state = J_DONE;
@@ -113,7 +111,8 @@ void finish_job(bf_engine* e, Job* j, int status) {
 
 uint8_t* slot_pin(bf_engine* e, int slot) { return e->pin.b() + 128 * (size_t)slot; }
 
-// Starts a job on a free slot: allocate, copy the evaluations in, enqueue the commit.
+// Starts a job on a free slot: allocate, copy the evaluations in, enqueue
+// the commit, the evaluation and the device-transcript open.
 int admit(bf_engine* e, Job* j) {
   bf_job* pj = j->pub;
   TRY(get_pcs(e, pj->num_vars, &j->pcs));
@@ -121,7 +120,6 @@ int admit(bf_engine* e, Job* j) {
   const size_t need = bf_pcs_proof_size(p, 1, 1);
   if (pj->proof_cap < need) return fail(BF_ERR_BUFFER, "job proof buffer needs %zu bytes", need);
   j->st = e->streams[j->slot];
-  CU(cudaEventCreateWithFlags(&j->ev, cudaEventDisableTiming));
   j->cm.reset(new bf_commitment());
   j->cm->pcs = p;
   j->cm->width = 1;
@@ -135,74 +133,40 @@ int admit(bf_engine* e, Job* j) {
     CU(j->cm->data.alloc_async(bytes, p->pool, j->st));
     CU(cudaMemcpyAsync(j->cm->data.p, pj->evals, bytes, cudaMemcpyHostToDevice, j->st));
   }
-  TRY(commit_enqueue(p, j->cm.get(), j->cm->data.as<uint4>(), j->st, slot_pin(e, j->slot)));
-  CU(cudaEventRecord(j->ev, j->st));
-  j->state = J_COMMIT;
+  uint8_t* pin = slot_pin(e, j->slot);
+  TRY(commit_enqueue(p, j->cm.get(), j->cm->data.as<uint4>(), j->st, pin));
+  const size_t half = p->d > 0 ? ((size_t)1 << (p->d - 1)) : 1;
+  CU(j->eval_ws.alloc_async(16 * half, p->pool, j->st));
+  const uint4* value_dev = nullptr;
+  TRY(eval_enqueue(p, j->cm.get(), pj->point, j->eval_ws.as<uint4>(), j->st, pin + 64, &value_dev));
+  TRY(open_start_impl(p, j->cm.get(), pj->point, nullptr, nullptr, j->st, &j->sess));
+  const size_t nd = p->n_d();
+  const uint4* root_dev = j->cm->tree.as<uint4>() + 2 * (2 * nd - 2);
+  j->ch = bfh::Challenger();  // GenericChallenger::keccak256()
+  TRY(open_resident_enqueue(j->sess, j->ch, root_dev, value_dev));
+  j->state = J_OPEN;
   return BF_OK;
 }
 
-// Advances a job whose last GPU step has completed.  Returns 1 if it moved.
+// Advances a job whose GPU work has completed.  Returns 1 if it moved.
 int step(bf_engine* e, Job* j) {
   bf_pcs* p = j->pcs;
   bf_job* pj = j->pub;
-  if (j->state == J_COMMIT || j->state == J_EVAL) {
-    cudaError_t q = cudaEventQuery(j->ev);
-    if (q == cudaErrorNotReady) return 0;
-    CU(q);
-  }
-  if (j->state == J_COMMIT) {
-    std::memcpy(j->cm->root, slot_pin(e, j->slot), 32);
-    std::memcpy(j->cm->pi_root, slot_pin(e, j->slot) + 32, 32);
-    std::memcpy(pj->root, j->cm->root, 32);
-    j->ch = bfh::Challenger();  // GenericChallenger::keccak256()
-    j->ch.observe(j->cm->root, 32);
-    const size_t half = p->d > 0 ? ((size_t)1 << (p->d - 1)) : 1;
-    CU(j->eval_ws.alloc_async(16 * half, p->pool, j->st));
-    TRY(eval_enqueue(p, j->cm.get(), pj->point, j->eval_ws.as<uint4>(), j->st, slot_pin(e, j->slot) + 64));
-    CU(cudaEventRecord(j->ev, j->st));
-    j->state = J_EVAL;
-    return 1;
-  }
-  if (j->state == J_EVAL) {
-    std::memcpy(j->value, slot_pin(e, j->slot) + 64, 16);
-    std::memcpy(pj->value, j->value, 16);
-    j->ch.observe(j->value, 16);
-    j->eval_ws.release();
-    TRY(bf_open_start(p, j->cm.get(), pj->point, j->value, nullptr, j->st, &j->sess));
-    j->state = J_ROUNDS;
-    return 1;
-  }
-  if (j->state == J_ROUNDS) {
-    int ready = bf_open_poll(j->sess);
-    TRY(ready);
-    if (!ready) return 0;
-    int round;
-    uint8_t root[32], poly[32];
-    if (j->tail_running) {
-      TRY(open_tail_complete(j->sess, j->ch));
-      j->tail_running = false;
-      round = -1;
-    } else if (open_tail_eligible(j->sess, j->ch)) {
-      TRY(open_tail_enqueue(j->sess, j->ch));
-      j->tail_running = true;
-      return 1;
-    } else {
-      TRY(bf_open_round(j->sess, &round, root, poly));
-    }
-    if (round >= 0) {
-      j->ch.observe(root, 32);
-      j->ch.observe(poly, 32);
-      uint8_t r[16];
-      bfh::store(r, j->ch.sample_elem());
-      TRY(bf_open_challenge(j->sess, r));
-      return 1;
-    }
-    uint8_t fin[16];
-    TRY(bf_open_final(j->sess, fin));
-    j->ch.observe(fin, 16);
+  int ready = bf_open_poll(j->sess);
+  TRY(ready);
+  if (!ready) return 0;
+  if (j->state == J_OPEN) {
+    TRY(open_resident_complete(j->sess, j->ch));
     std::vector<uint64_t> idx(p->Q);
-    for (size_t q = 0; q < p->Q; ++q) idx[q] = j->ch.sample_bits(p->L);
-    TRY(bf_open_finish(j->sess, idx.data(), idx.size(), pj->proof, pj->proof_cap, &pj->proof_len));
+    for (size_t q = 0; q < p->Q; ++q) idx[q] = j->ch.sample_bits(p->L);  // basefold.rs:200-203
+    TRY(open_finish_enqueue(j->sess, idx.data(), idx.size()));
+    j->state = J_GATHER;
+    return 1;
+  }
+  if (j->state == J_GATHER) {
+    TRY(open_finish_complete(j->sess, pj->proof, pj->proof_cap, &pj->proof_len));
+    std::memcpy(pj->root, slot_pin(e, j->slot), 32);
+    std::memcpy(pj->value, slot_pin(e, j->slot) + 64, 16);
     finish_job(e, j, BF_OK);
     return 1;
   }

@@ -54,12 +54,17 @@ struct bf_open_session {
   uint4* w_pi_first = nullptr;
   uint4* w_pi_first_tree = nullptr;
   uint4* w_poly_first = nullptr;
-  uint8_t* w_tail = nullptr;       // tail kernel: inputs (scalars, transcript) and result
-  bool tail_pending = false;       // the tail kernel's result is in flight
-  std::unique_ptr<PinnedBuf> pin;  // [0,64) staging, [64,64+16(w+d)) scalars and point, indices, openings;
-                                   // tail kernel inputs at tail_in_off()
+  // device transcript: per-round scalars, the OpenState, the round records
+  uint8_t* w_tail = nullptr;
+  bf::OpenState* w_state = nullptr;
+  uint8_t* w_rec = nullptr;
+  bool resident_pending = false;   // a device-transcript open is in flight
+  bool gather_pending = false;     // query openings in flight
+  std::unique_ptr<PinnedBuf> pin;  // [0,64) staging, [64,64+16(w+d)) scalars and point, indices,
+                                   // openings, device-transcript results; inputs at tail_in_off()
   uint64_t* idx_pin = nullptr;
   uint8_t* open_pin = nullptr;
+  uint8_t* res_pin = nullptr;
 
   size_t c() const { return p->c(); }
   uint4* pi_fold_out(int k) const { return w_pi_fold + c() * (((size_t)1 << d) - ((size_t)1 << (k + 1))); }
@@ -71,10 +76,15 @@ struct bf_open_session {
   const uint4* first_pi() const { return w == 1 ? cm->cw.as<uint4>() : w_pi_first; }
   const uint4* first_poly() const { return w == 1 ? cm->data.as<uint4>() : w_poly_first; }
   const uint4* first_tree() const { return w == 1 ? cm->pi_tree.as<uint4>() : w_pi_first_tree; }
-  // Pinned offset of the tail kernel's inputs: past the staging, the eq
+  // Pinned offset of the device-transcript inputs: past the staging, the eq
   // scalars and the point, whose host-to-device copies may still be queued
-  // when the tail is enqueued.
+  // when the resident open is enqueued.
   size_t tail_in_off() const { return 64 + 16 * ((size_t)(d > 0 ? d : 1) + w); }
+  // Root of round d-1's tree on the device: the commitment's pair tree for
+  // width 1, the combined rows' tree otherwise.
+  const uint4* first_root_dev() const {
+    return w == 1 ? cm->pi_tree.as<uint4>() + 2 * (p->n_d() - 2) : reinterpret_cast<const uint4*>(stage(d - 1));
+  }
   ~bf_open_session() {
     if (st) cudaStreamSynchronize(st);
     if (ev) cudaEventDestroy(ev);
@@ -90,12 +100,15 @@ namespace {
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-// Tail kernel I/O: per round 3 scalars in, 64 bytes out; final poly and the
-// transcript state; the transcript input.
-constexpr size_t kTailScalOff = 0;
-size_t tail_result_off(int d) { return align256(48 * (size_t)(d > 0 ? d : 1)); }
-size_t tail_tr_off(int d) { return tail_result_off(d) + align256(64 * (size_t)(d + 1) + 16 + 4 + 2 * bf::kTailTranscriptMax); }
-size_t tail_bytes(int d) { return tail_tr_off(d) + 2 * bf::kTailTranscriptMax; }
+size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+// Device-transcript workspace: per round 3 scalars (r_i, r_i^-1, correcting
+// factor), the OpenState, then 64 bytes per round (root, c0, c2) and the
+// final polynomial.
+size_t state_off(int d) { return align256(48 * (size_t)(d > 0 ? d : 1)); }
+size_t rec_off(int d) { return state_off(d) + align256(sizeof(bf::OpenState)); }
+size_t rec_bytes(int d) { return 64 * (size_t)d + 16; }
+size_t tail_bytes(int d) { return rec_off(d) + rec_bytes(d); }
 
 int session_alloc(bf_open_session* s) {
   bf_pcs* p = s->p;
@@ -134,6 +147,8 @@ int session_alloc(bf_open_session* s) {
     s->w_poly_first = reinterpret_cast<uint4*>(b + o_polyf);
   }
   s->w_tail = b + o_tail;
+  s->w_state = reinterpret_cast<bf::OpenState*>(b + o_tail + state_off(d));
+  s->w_rec = b + o_tail + rec_off(d);
   s->w_point = reinterpret_cast<uint4*>(b + o_point);
   s->w_pi_fold = reinterpret_cast<uint4*>(b + o_fold);
   s->w_pi_trees = reinterpret_cast<uint4*>(b + o_tree);
@@ -144,9 +159,10 @@ int session_alloc(bf_open_session* s) {
   s->w_stage = b + o_stage;
   s->w_idx = reinterpret_cast<uint64_t*>(b + o_idx);
   s->w_open = b + o_open;
+  const size_t res_off = align16(64 + 16 * (n_point + s->w) + 8 * (p->Q + 1) + bb * (p->Q + 1));
   const size_t pin_bytes =
-      std::max(64 + 16 * (n_point + s->w) + 8 * (p->Q + 1) + bb * (p->Q + 1),
-               std::max(tail_bytes(d), s->tail_in_off() + 48 * (size_t)(d + 1) + 2 * (size_t)bf::kTailTranscriptMax));
+      std::max(res_off + align16(rec_bytes(d)) + sizeof(bf::OpenState),
+               s->tail_in_off() + 48 * n_point + sizeof(bf::OpenState));
   if (!p->pinned_cache.empty()) {
     s->pin = std::move(p->pinned_cache.back());
     p->pinned_cache.pop_back();
@@ -156,6 +172,7 @@ int session_alloc(bf_open_session* s) {
   CU(s->pin->ensure(pin_bytes));
   s->idx_pin = reinterpret_cast<uint64_t*>(s->pin->b() + 64 + 16 * (n_point + s->w));
   s->open_pin = reinterpret_cast<uint8_t*>(s->idx_pin + (p->Q + 1));
+  s->res_pin = s->pin->b() + res_off;
   return BF_OK;
 }
 
@@ -202,37 +219,74 @@ int ensure_message(bf_open_session* s) {
 
 namespace bfapi {
 
-// The current round and every later one fit the single-block kernel, and the
-// transcript input fits its buffer.
-bool open_tail_eligible(const bf_open_session* s, const bfh::Challenger& ch) {
-  if (s->i < 0) return false;
-  if ((s->p->n_i(s->i) >> 1) > ((size_t)1 << bf::kTailMaxLeavesLog)) return false;
-  return ch.in.size() + 64 <= (size_t)bf::kTailTranscriptMax && ch.out.size() <= 32;
+// First round run by the single-block kernel: the largest i <= d-1 whose
+// folded codeword has at most 2^(kTailMaxLeavesLog+1) entries.
+int tail_first_round(const bf_pcs* p, int d) {
+  const int lim = bf::kTailMaxLeavesLog + 1 - p->log2_c;
+  return std::min(d - 1, lim);
 }
 
-// Runs every remaining round on the device with transcript `ch`: enqueues
-// the tail kernel and the copy of its result; open_tail_complete reads it.
-int open_tail_enqueue(bf_open_session* s, const bfh::Challenger& ch) {
+// Enqueues every round of `s`, and the final polynomial, with the transcript
+// on the device, starting from `ch`; root_dev / value_dev, when given, are
+// observed first (the commitment root and the evaluation on the device, the
+// value becoming the claim).  Nothing is read back until
+// open_resident_complete.
+int open_resident_enqueue(bf_open_session* s, const bfh::Challenger& ch, const uint4* root_dev,
+                          const uint4* value_dev) {
   bf_pcs* p = s->p;
-  const int i0 = s->i, d = s->d;
-  uint8_t* pin = s->pin->b();
-  // Inputs go where no copy still in flight reads or writes (the previous
-  // round's staging copy, bf_open_start's scalar and point copies): scalars
-  // r_i, r_i^-1, correcting factor for rounds 0..i0, then the transcript.
-  uint8_t* in = pin + s->tail_in_off();
-  for (int i = 0; i <= i0; ++i) {
+  const int d = s->d;
+  if (s->i != d - 1 || s->msg_ready || s->resident_pending)
+    return fail(BF_ERR_ARG, "a device-transcript open starts before the first round");
+  if (ch.in.size() > (size_t)bf::kTrMax || ch.out.size() > 32)
+    return fail(BF_ERR_ARG, "transcript state too large for the device (%zu input bytes)", ch.in.size());
+  const size_t n_point = d > 0 ? d : 1;
+  // Inputs go where no copy still in flight reads (bf_open_start's scalar
+  // and point copies): scalars per round, then the OpenState image.
+  uint8_t* in = s->pin->b() + s->tail_in_off();
+  for (int i = 0; i < d; ++i) {
     bfh::store(in + 48 * i, s->r[i]);
     bfh::store(in + 48 * i + 16, s->r_inv[i]);
     bfh::store(in + 48 * i + 32, s->corr[i]);
   }
-  uint8_t* tr = in + 48 * (size_t)(d + 1);
-  std::memcpy(tr, ch.in.data(), ch.in.size());
-  std::memcpy(tr + bf::kTailTranscriptMax, ch.out.data(), ch.out.size());
+  bf::OpenState img;
+  std::memset(&img, 0, sizeof(img));
+  if (!ch.in.empty()) std::memcpy(img.tr.in, ch.in.data(), ch.in.size());
+  if (!ch.out.empty()) std::memcpy(img.tr.out, ch.out.data(), ch.out.size());
+  img.tr.in_len = (int)ch.in.size();
+  img.tr.out_len = (int)ch.out.size();
+  img.outer = to_uint4(s->outer_val);
+  img.delta = to_uint4(bfh::one());
+  std::memcpy(in + 48 * n_point, &img, sizeof(img));
   cudaStream_t st = s->st;
-  CU(cudaMemcpyAsync(s->w_tail, in, 48 * (size_t)(i0 + 1), cudaMemcpyHostToDevice, st));
-  CU(cudaMemcpyAsync(s->w_tail + tail_tr_off(d), tr, 2 * bf::kTailTranscriptMax, cudaMemcpyHostToDevice, st));
+  if (d > 0) CU(cudaMemcpyAsync(s->w_tail, in, 48 * (size_t)d, cudaMemcpyHostToDevice, st));
+  CU(cudaMemcpyAsync(s->w_state, in + 48 * n_point, sizeof(img), cudaMemcpyHostToDevice, st));
+  if (root_dev || value_dev) CU(bf::launch_open_observe(s->w_state, root_dev, value_dev, st));
+  const uint4* scal = reinterpret_cast<const uint4*>(s->w_tail);
+  const uint4* xp = &s->w_state->x;
+  const int i_tail = d > 0 ? tail_first_round(p, d) : -1;
+  for (int i = d - 1; i > i_tail; --i) {  // large rounds: one kernel per step
+    const uint4* root_i = (i == d - 1) ? s->first_root_dev() : reinterpret_cast<const uint4*>(s->stage(i));
+    CU(bf::launch_open_round(s->w_state, i, d, scal, root_i, reinterpret_cast<const uint4*>(s->stage(i) + 32),
+                             s->w_rec + 64 * (size_t)(d - 1 - i), st));
+    const size_t ni = p->n_i(i);
+    const uint4* pi_in = (i == d - 1) ? s->first_pi() : s->pi_fold_out(i + 1);
+    {
+      ProfScope ps(p->prof, st, P_FOLD);
+      CU(bf::launch_fold_leaves(pi_in, s->pi_fold_out(i), s->pi_tree(i - 1), ni / 2, p->tw_host.lo[d - 1 - i],
+                                p->tw_host.hi[d - 1 - i], uint4{}, st, xp));
+    }
+    {
+      ProfScope ps(p->prof, st, P_FIX);
+      CU(bf::launch_fix((i == d - 1) ? s->first_poly() : s->w_poly, s->w_poly, (size_t)1 << i, uint4{}, s->w_heq,
+                        (size_t)1 << (i - 1), reinterpret_cast<uint32_t*>(s->stage(i - 1) + 32), st, xp));
+    }
+    {
+      ProfScope ps(p->prof, st, P_TREE);
+      CU(bf::launch_tree(s->pi_tree(i - 1), p->n_i(i - 1), st, reinterpret_cast<uint4*>(s->stage(i - 1))));
+    }
+  }
   bf::TailParams tp{};
-  tp.i0 = i0;
+  tp.i0 = i_tail;
   tp.d = d;
   tp.log2_c = p->log2_c;
   tp.pi_first = s->first_pi();
@@ -241,59 +295,128 @@ int open_tail_enqueue(bf_open_session* s, const bfh::Challenger& ch) {
   tp.poly_first = s->first_poly();
   tp.poly = s->w_poly;
   tp.heq = s->w_heq;
-  tp.stage_i0 = s->stage(i0);
-  tp.root_in_params = (i0 == d - 1 && s->w == 1);
-  if (tp.root_in_params) {
-    std::memcpy(&tp.root_lo, s->cm->pi_root, 16);
-    std::memcpy(&tp.root_hi, s->cm->pi_root + 16, 16);
+  if (i_tail >= 0) {
+    tp.root_i0 = (i_tail == d - 1) ? s->first_root_dev() : reinterpret_cast<const uint4*>(s->stage(i_tail));
+    tp.S_i0 = reinterpret_cast<const uint4*>(s->stage(i_tail) + 32);
   }
-  tp.scal = reinterpret_cast<const uint4*>(s->w_tail + kTailScalOff);
-  tp.outer = to_uint4(s->outer_val);
-  tp.inner = to_uint4(s->inner_val);
-  tp.delta = to_uint4(s->delta_prod);
+  tp.scal = scal;
   tp.tw = p->tw_view.as<bf::TwiddleView>();
-  tp.tr_in = s->w_tail + tail_tr_off(d);
-  tp.tr_in_len = (int)ch.in.size();
-  tp.tr_out = s->w_tail + tail_tr_off(d) + bf::kTailTranscriptMax;
-  tp.tr_out_len = (int)ch.out.size();
-  tp.result = s->w_tail + tail_result_off(d);
+  tp.state = s->w_state;
+  tp.result = s->w_rec + 64 * (size_t)(d - 1 - i_tail);
   {
     ProfScope ps(p->prof, st, P_TREE);
     CU(bf::launch_open_tail(tp, st));
   }
-  const size_t res_bytes = 64 * (size_t)(i0 + 1) + 16 + 4 + 2 * bf::kTailTranscriptMax;
-  CU(cudaMemcpyAsync(pin, tp.result, res_bytes, cudaMemcpyDeviceToHost, st));
+  CU(cudaMemcpyAsync(s->res_pin, s->w_rec, rec_bytes(d), cudaMemcpyDeviceToHost, st));
+  CU(cudaMemcpyAsync(s->res_pin + align16(rec_bytes(d)), s->w_state, sizeof(bf::OpenState), cudaMemcpyDeviceToHost,
+                     st));
   CU(cudaEventRecord(s->ev, st));
   s->pending = true;
-  s->tail_pending = true;
+  s->resident_pending = true;
   s->msg_ready = false;
   return BF_OK;
 }
 
-// Reads the tail kernel's result: the rounds' roots and compressed round
+// Reads the device-transcript open: the rounds' roots and compressed round
 // polynomials, the final polynomial, and the transcript state (into `ch`).
-int open_tail_complete(bf_open_session* s, bfh::Challenger& ch) {
-  if (!s->tail_pending) return fail(BF_ERR_ARG, "no tail in flight");
+int open_resident_complete(bf_open_session* s, bfh::Challenger& ch) {
+  if (!s->resident_pending) return fail(BF_ERR_ARG, "no device-transcript open in flight");
   CU(cudaStreamSynchronize(s->st));
   s->p->prof.drain();
   s->pending = false;
-  s->tail_pending = false;
-  const uint8_t* res = s->pin->b();
-  const int rounds = s->i + 1;
-  for (int k = 0; k < rounds; ++k) {
+  s->resident_pending = false;
+  const int d = s->d;
+  const uint8_t* res = s->res_pin;
+  bf::OpenState img;
+  std::memcpy(&img, res + align16(rec_bytes(d)), sizeof(img));
+  if (img.status != 0) return fail(BF_ERR_ARG, "transcript input outgrew the device buffer");
+  for (int k = 0; k < d; ++k) {
     const uint8_t* rec = res + 64 * (size_t)k;
     s->roots.insert(s->roots.end(), rec, rec + 32);
     put_u64(s->rounds, 2);
     s->rounds.insert(s->rounds.end(), rec + 32, rec + 64);
   }
-  const uint8_t* fin = res + 64 * (size_t)rounds;
-  s->final_val = bfh::load(fin);
-  const uint8_t* stt = fin + 16;
-  const int in_len = stt[0] | (stt[1] << 8), out_len = stt[2];
-  ch.in.assign(stt + 4, stt + 4 + in_len);
-  ch.out.assign(stt + 4 + in_len, stt + 4 + in_len + out_len);
+  s->final_val = bfh::load(res + 64 * (size_t)d);
+  ch.in.assign(img.tr.in, img.tr.in + img.tr.in_len);
+  ch.out.assign(img.tr.out, img.tr.out + img.tr.out_len);
   s->i = -1;
   s->final_ready = true;
+  return BF_OK;
+}
+
+// Gather of the openings at `indices` (basefold.rs:204-221) and their copy
+// to the host; open_finish_complete waits and writes the proof.
+int open_finish_enqueue(bf_open_session* s, const uint64_t* indices, size_t nq) {
+  bf_pcs* p = s->p;
+  if (s->i >= 0) return fail(BF_ERR_ARG, "rounds remain");
+  if (nq != p->Q) return fail(BF_ERR_ARG, "expected %zu query indices, got %zu", p->Q, nq);
+  if (nq && !indices) return fail(BF_ERR_ARG, "null argument");
+  TRY(ensure_message(s));
+  const size_t bb = p->block_bytes(s->w);
+  for (size_t q = 0; q < nq; ++q) {
+    if (indices[q] >= p->n_d()) return fail(BF_ERR_ARG, "query index %llu out of range", (unsigned long long)indices[q]);
+    s->idx_pin[q] = indices[q];
+  }
+  cudaStream_t st = s->st;
+  if (nq) {
+    CU(cudaMemcpyAsync(s->w_idx, s->idx_pin, 8 * nq, cudaMemcpyHostToDevice, st));
+    bf::GatherParams gp{};
+    gp.cw = s->cm->cw.as<uint4>();
+    gp.cw_tree = s->cm->tree.as<uint4>();
+    gp.pi_first = s->first_pi();
+    gp.pi_first_tree = s->first_tree();
+    gp.pi_fold = s->w_pi_fold;
+    gp.pi_trees = s->w_pi_trees;
+    gp.idx = s->w_idx;
+    gp.out = s->w_open;
+    gp.width = s->w;
+    gp.block_bytes = bb;
+    gp.L = p->L;
+    gp.d = s->d;
+    gp.log2_c = p->log2_c;
+    gp.nq = (int)nq;
+    {
+      ProfScope ps(p->prof, st, P_GATHER);
+      CU(bf::launch_gather(gp, st));
+    }
+    CU(cudaMemcpyAsync(s->open_pin, s->w_open, bb * nq, cudaMemcpyDeviceToHost, st));
+  }
+  CU(cudaEventRecord(s->ev, st));
+  s->pending = true;
+  s->gather_pending = true;
+  return BF_OK;
+}
+
+// BasefoldProof bincode (basefold.rs:49-66): round polys, final poly,
+// pi_comms, openings.
+int open_finish_complete(bf_open_session* s, uint8_t* proof, size_t cap, size_t* proof_len) {
+  bf_pcs* p = s->p;
+  if (!s->gather_pending) return fail(BF_ERR_ARG, "no openings in flight");
+  const size_t need = bf_pcs_proof_size(p, s->w, 1);
+  *proof_len = need;
+  if (!proof || cap < need) return fail(BF_ERR_BUFFER, "proof buffer needs %zu bytes", need);
+  CU(cudaStreamSynchronize(s->st));
+  p->prof.drain();
+  s->pending = false;
+  s->gather_pending = false;
+  const size_t nq = p->Q, bb = p->block_bytes(s->w);
+  uint8_t* o = proof;
+  std::memcpy(o, s->rounds.data(), s->rounds.size());
+  o += s->rounds.size();
+  std::vector<uint8_t> fin;
+  put_u64(fin, 1);
+  put_elem(fin, s->final_val);
+  std::memcpy(o, fin.data(), fin.size());
+  o += fin.size();
+  std::memcpy(o, s->roots.data(), s->roots.size());
+  o += s->roots.size();
+  std::vector<uint8_t> qn;
+  put_u64(qn, nq);
+  std::memcpy(o, qn.data(), 8);
+  o += 8;
+  if (nq) std::memcpy(o, s->open_pin, bb * nq);
+  o += bb * nq;
+  if ((size_t)(o - proof) != need) return fail(BF_ERR_CUDA, "internal: proof size mismatch");
   return BF_OK;
 }
 
@@ -303,7 +426,20 @@ extern "C" {
 
 int bf_open_start(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, const uint8_t* values,
                   const uint8_t* scalars, void* stream, bf_open_session** out) {
-  if (!p || !cm || !out || !values || (p->d > 0 && !point)) return fail(BF_ERR_ARG, "null argument");
+  if (!values) return fail(BF_ERR_ARG, "null argument");
+  return open_start_impl(p, cm, point, values, scalars, stream, out);
+}
+
+}  // extern "C"
+
+namespace bfapi {
+
+// bf_open_start; `values` may be null when a device-transcript open will
+// observe the evaluation on the device (width 1).
+int open_start_impl(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, const uint8_t* values,
+                    const uint8_t* scalars, void* stream, bf_open_session** out) {
+  if (!p || !cm || !out || (p->d > 0 && !point)) return fail(BF_ERR_ARG, "null argument");
+  if (!values && cm->width != 1) return fail(BF_ERR_ARG, "null argument");
   *out = nullptr;
   if (p->device < 0) return fail(BF_ERR_ARG, "verifier-only pcs (device < 0)");
   if (cm->pcs != p) return fail(BF_ERR_ARG, "commitment belongs to another pcs");
@@ -323,7 +459,7 @@ int bf_open_start(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, cons
   s->r.resize(d);
   for (int k = 0; k < d; ++k) s->r[k] = bfh::load(point + 16 * k);
   if (w == 1) {
-    s->outer_val = bfh::load(values);
+    s->outer_val = values ? bfh::load(values) : 0;
   } else {  // claim = <scalars, values> (basefold.rs:176)
     u128 claim = 0;
     for (size_t c = 0; c < w; ++c) claim ^= bfh::mul(bfh::load(scalars + 16 * c), bfh::load(values + 16 * c));
@@ -379,6 +515,10 @@ int bf_open_start(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, cons
   *out = s.release();
   return BF_OK;
 }
+
+}  // namespace bfapi
+
+extern "C" {
 
 int bf_open_poll(bf_open_session* s) {
   if (!s) return fail(BF_ERR_ARG, "null argument");
@@ -478,58 +618,8 @@ int bf_open_finish(bf_open_session* s, const uint64_t* indices, size_t nq, uint8
   *proof_len = need;
   if (!proof || cap < need) return fail(BF_ERR_BUFFER, "proof buffer needs %zu bytes", need);
   DeviceGuard g(p->device);
-  TRY(ensure_message(s));
-  const size_t bb = p->block_bytes(s->w);
-  for (size_t q = 0; q < nq; ++q) {
-    if (indices[q] >= p->n_d()) return fail(BF_ERR_ARG, "query index %llu out of range", (unsigned long long)indices[q]);
-    s->idx_pin[q] = indices[q];
-  }
-  cudaStream_t st = s->st;
-  if (nq) {
-    CU(cudaMemcpyAsync(s->w_idx, s->idx_pin, 8 * nq, cudaMemcpyHostToDevice, st));
-    bf::GatherParams gp{};
-    gp.cw = s->cm->cw.as<uint4>();
-    gp.cw_tree = s->cm->tree.as<uint4>();
-    gp.pi_first = s->first_pi();
-    gp.pi_first_tree = s->first_tree();
-    gp.pi_fold = s->w_pi_fold;
-    gp.pi_trees = s->w_pi_trees;
-    gp.idx = s->w_idx;
-    gp.out = s->w_open;
-    gp.width = s->w;
-    gp.block_bytes = bb;
-    gp.L = p->L;
-    gp.d = s->d;
-    gp.log2_c = p->log2_c;
-    gp.nq = (int)nq;
-    {
-      ProfScope ps(p->prof, st, P_GATHER);
-      CU(bf::launch_gather(gp, st));
-    }
-    CU(cudaMemcpyAsync(s->open_pin, s->w_open, bb * nq, cudaMemcpyDeviceToHost, st));
-    CU(cudaStreamSynchronize(st));
-    p->prof.drain();
-  }
-  // BasefoldProof bincode (basefold.rs:49-66): round polys, final poly,
-  // pi_comms, openings
-  uint8_t* o = proof;
-  std::memcpy(o, s->rounds.data(), s->rounds.size());
-  o += s->rounds.size();
-  std::vector<uint8_t> fin;
-  put_u64(fin, 1);
-  put_elem(fin, s->final_val);
-  std::memcpy(o, fin.data(), fin.size());
-  o += fin.size();
-  std::memcpy(o, s->roots.data(), s->roots.size());
-  o += s->roots.size();
-  std::vector<uint8_t> qn;
-  put_u64(qn, nq);
-  std::memcpy(o, qn.data(), 8);
-  o += 8;
-  if (nq) std::memcpy(o, s->open_pin, bb * nq);
-  o += bb * nq;
-  if ((size_t)(o - proof) != need) return fail(BF_ERR_CUDA, "internal: proof size mismatch");
-  return BF_OK;
+  TRY(open_finish_enqueue(s, indices, nq));
+  return open_finish_complete(s, proof, cap, proof_len);
 }
 
 void bf_open_session_free(bf_open_session* s) {
@@ -560,25 +650,10 @@ int bf_open(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, const uint
   bf_open_session* s = nullptr;
   TRY(bf_open_start(p, cm, point, values, scal.empty() ? nullptr : scal.data(), nullptr, &s));
   std::unique_ptr<bf_open_session, void (*)(bf_open_session*)> guard(s, bf_open_session_free);
-  while (true) {
-    if (open_tail_eligible(s, ch)) {  // the remaining rounds, transcript on the device
-      TRY(open_tail_enqueue(s, ch));
-      TRY(open_tail_complete(s, ch));
-      break;
-    }
-    int round;
-    uint8_t root[32], poly[32];
-    TRY(bf_open_round(s, &round, root, poly));
-    if (round < 0) break;
-    ch.observe(root, 32);  // basefold.rs:356
-    ch.observe(poly, 32);  // sumcheck/src/lib.rs:97
-    uint8_t r[16];
-    bfh::store(r, ch.sample_elem());
-    TRY(bf_open_challenge(s, r));
-  }
-  uint8_t fin[16];
-  TRY(bf_open_final(s, fin));
-  ch.observe(fin, 16);  // basefold.rs:196
+  // every round and the final polynomial with the transcript on the device
+  // (basefold.rs:185-196, 335-369), then the queries on the host
+  TRY(open_resident_enqueue(s, ch, nullptr, nullptr));
+  TRY(open_resident_complete(s, ch));
   std::vector<uint64_t> idx(p->Q);
   for (size_t q = 0; q < p->Q; ++q) idx[q] = ch.sample_bits(p->L);  // basefold.rs:200-203
   size_t len = 0;

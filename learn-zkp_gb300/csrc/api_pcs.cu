@@ -284,10 +284,11 @@ int commit_enqueue(bf_pcs* p, bf_commitment* cm, const uint4* data, cudaStream_t
 // last coordinate, repeatedly, in `scratch` (2^(d-1) elements).  The value
 // lands in value_pin[0..16).
 int eval_enqueue(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, uint4* scratch, cudaStream_t st,
-                 uint8_t* value_pin) {
+                 uint8_t* value_pin, const uint4** value_dev) {
   const int d = p->d;
   const size_t w = cm->width;
   const uint4* data = cm->data.as<uint4>();
+  if (value_dev) *value_dev = d == 0 ? data : scratch;
   if (d == 0) {
     CU(cudaMemcpyAsync(value_pin, data, 16 * w, cudaMemcpyDeviceToHost, st));
     return BF_OK;

@@ -37,12 +37,14 @@ cudaError_t launch_tree(uint4* leaves, size_t n, cudaStream_t st, uint4* root_ou
 
 cudaError_t launch_eq_table(const uint4* r, int nvars, uint4* out, uint4* tmp_lo, uint4* tmp_hi, cudaStream_t st);
 cudaError_t launch_dot_xor(const uint4* x, const uint4* y, size_t n, uint32_t* acc, cudaStream_t st);
+// The fold and fix challenge is `r`, or *xp when xp is not null (a challenge
+// sampled on the device).
 cudaError_t launch_fold(const uint4* pi, uint4* out, size_t n_out, const uint4* tw_lo, const uint4* tw_hi, uint4 r,
-                        cudaStream_t st);
+                        cudaStream_t st, const uint4* xp = nullptr);
 cudaError_t launch_fold_leaves(const uint4* pi, uint4* out, uint4* leaves, size_t n_leaves, const uint4* tw_lo,
-                               const uint4* tw_hi, uint4 r, cudaStream_t st);
+                               const uint4* tw_hi, uint4 r, cudaStream_t st, const uint4* xp = nullptr);
 cudaError_t launch_fix(const uint4* in, uint4* out, size_t half, uint4 r, const uint4* heq, size_t next_half,
-                       uint32_t* acc, cudaStream_t st);
+                       uint32_t* acc, cudaStream_t st, const uint4* xp = nullptr);
 cudaError_t launch_fix_column(const uint4* in, size_t width, size_t col, uint4* out, size_t half, uint4 r,
                               cudaStream_t st);
 cudaError_t launch_combine_rows(const uint4* rows, size_t nrows, size_t width, const uint4* scalars, uint4* out,
@@ -75,29 +77,52 @@ cudaError_t launch_prod_fix(uint4* const* out, const uint4* const* in, int k, si
 unsigned long long launches_total();
 void count_launch();
 
-// ---- the last rounds of open in one block with the transcript on the device
+// ---- Fiat-Shamir on the device
+// HashChallenger<u8, Keccak256Hash, 32> (p3/src/challenger.rs) as bytes: the
+// pending input and the unread output of the last digest.
+constexpr int kTrMax = 512;
+struct alignas(16) DevTranscript {
+  uint8_t in[kTrMax];
+  uint8_t out[32];
+  int in_len, out_len, pad_[2];
+};
+// Device-resident state of one open (basefold.rs:133-232): the transcript,
+// the claim of the current sumcheck round (`outer`), the EvalProver claim
+// (`inner`), the product of delta scalars (eval_impr.rs:45-51) and the last
+// challenge.  status != 0: the transcript input outgrew kTrMax.
+struct alignas(16) OpenState {
+  DevTranscript tr;
+  uint4 outer, inner, delta, x;
+  int status, pad_[3];
+};
+// Observes the commitment root (32 bytes at `root`) and the evaluation
+// (16 bytes at `value`, which also becomes the claim), as the caller of open
+// does (poly-commit/src/lib.rs:80-100).
+cudaError_t launch_open_observe(OpenState* s, const uint4* root, const uint4* value, cudaStream_t st);
+// The transcript step of round i: round polynomial from the reduction
+// S = sum half_eq * poly_lo (eval_impr.rs:116-127, eval.rs:89-106), observe
+// root and [c0, c2], sample the challenge into s->x.  `rec` receives root,
+// c0, c2 (64 bytes).  `scal` holds r_i, r_i^-1, correcting factor per round.
+cudaError_t launch_open_round(OpenState* s, int i, int d, const uint4* scal, const uint4* root, const uint4* S,
+                              uint8_t* rec, cudaStream_t st);
+
+// ---- the last rounds of open in one block, then the final polynomial
 constexpr int kTailThreads = 512;
-constexpr int kTailTranscriptMax = 512;  // bytes of transcript input buffer the kernel can hold
 constexpr int kTailMaxLeavesLog = 11;    // rounds whose next tree has <= 2^11 leaves
 struct TailParams {
-  int i0, d, log2_c;
+  int i0, d, log2_c;        // rounds i0 .. 0 (i0 = -1: none)
   const uint4* pi_first;    // folded codeword input of round d-1
   uint4* pi_fold;           // fold outputs of rounds d-1 .. 0
   uint4* pi_trees;          // trees of rounds d-2 .. 0
   const uint4* poly_first;  // sumcheck polynomial of round d-1
   uint4* poly;              // sumcheck polynomial after each fix (in place)
   const uint4* heq;         // half eq table
-  const uint8_t* stage_i0;  // root (32 B) + reduction S (16 B) of round i0
-  int root_in_params;       // round i0's root is root_lo/root_hi instead of stage_i0
-  uint4 root_lo, root_hi;
+  const uint4* root_i0;     // root of round i0's tree (32 B)
+  const uint4* S_i0;        // reduction of round i0 (16 B)
   const uint4* scal;        // per round i: r_i, r_i^-1, correcting factor
-  uint4 outer, inner, delta;
   const TwiddleView* tw;
-  const uint8_t* tr_in;     // transcript input buffer
-  int tr_in_len;
-  const uint8_t* tr_out;    // transcript output buffer
-  int tr_out_len;
-  uint8_t* result;          // per round: root, c0, c2 (64 B); final poly (16 B); transcript state
+  OpenState* state;
+  uint8_t* result;          // per round: root, c0, c2 (64 B); then the final polynomial (16 B)
 };
 cudaError_t launch_open_tail(const TailParams& p, cudaStream_t st);
 

@@ -388,7 +388,8 @@ cudaError_t launch_dot_xor(const uint4* x, const uint4* y, size_t n, uint32_t* a
 // out[t] = lo' + (hi' - lo') r with hi' = hi + lo, lo' = lo + hi' tw[t].
 __global__ void __launch_bounds__(256) fold_kernel(const uint4* __restrict__ pi, uint4* __restrict__ out,
                                                    size_t n_out, const uint4* __restrict__ tlo,
-                                                   const uint4* __restrict__ thi, uint4 r) {
+                                                   const uint4* __restrict__ thi, uint4 r, const uint4* xp) {
+  if (xp) r = *xp;
   for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n_out; t += (size_t)gridDim.x * blockDim.x) {
     const uint4 tw = gf_add(tlo[t & 4095], thi[t >> 12]);
     uint4 lo = pi[2 * t], hi = pi[2 * t + 1];
@@ -404,7 +405,9 @@ __global__ void __launch_bounds__(256) fold_kernel(const uint4* __restrict__ pi,
 __global__ void __launch_bounds__(128) fold_leaves_kernel(const uint4* __restrict__ pi, uint4* __restrict__ out,
                                                           uint4* __restrict__ leaves, size_t n_leaves,
                                                           const uint4* __restrict__ tlo,
-                                                          const uint4* __restrict__ thi, uint4 r) {
+                                                          const uint4* __restrict__ thi, uint4 r,
+                                                          const uint4* xp) {
+  if (xp) r = *xp;
   for (size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x; s < n_leaves; s += (size_t)gridDim.x * blockDim.x) {
     uint4 f[2];
 #pragma unroll
@@ -422,15 +425,15 @@ __global__ void __launch_bounds__(128) fold_leaves_kernel(const uint4* __restric
 }
 
 cudaError_t launch_fold_leaves(const uint4* pi, uint4* out, uint4* leaves, size_t n_leaves, const uint4* tw_lo,
-                               const uint4* tw_hi, uint4 r, cudaStream_t st) {
-  fold_leaves_kernel<<<grid_for(n_leaves, 128, 16), 128, 0, st>>>(pi, out, leaves, n_leaves, tw_lo, tw_hi, r);
+                               const uint4* tw_hi, uint4 r, cudaStream_t st, const uint4* xp) {
+  fold_leaves_kernel<<<grid_for(n_leaves, 128, 16), 128, 0, st>>>(pi, out, leaves, n_leaves, tw_lo, tw_hi, r, xp);
   COUNT_LAUNCH();
   return cudaGetLastError();
 }
 
 cudaError_t launch_fold(const uint4* pi, uint4* out, size_t n_out, const uint4* tw_lo, const uint4* tw_hi, uint4 r,
-                        cudaStream_t st) {
-  fold_kernel<<<grid_for(n_out, 256), 256, 0, st>>>(pi, out, n_out, tw_lo, tw_hi, r);
+                        cudaStream_t st, const uint4* xp) {
+  fold_kernel<<<grid_for(n_out, 256), 256, 0, st>>>(pi, out, n_out, tw_lo, tw_hi, r, xp);
   COUNT_LAUNCH();
   return cudaGetLastError();
 }
@@ -438,8 +441,10 @@ cudaError_t launch_fold(const uint4* pi, uint4* out, size_t n_out, const uint4* 
 // fix_last_var (multilinear.rs:183-198) fused with the next round's
 // sum_b half_eq[b] * poly_lo[b] (eval_impr.rs:187-197).  In-place safe.
 __global__ void __launch_bounds__(256) fix_kernel(const uint4* in, uint4* out, size_t half, uint4 r,
-                                                  const uint4* __restrict__ heq, size_t next_half, uint32_t* acc) {
+                                                  const uint4* __restrict__ heq, size_t next_half, uint32_t* acc,
+                                                  const uint4* xp) {
   __shared__ uint4 scratch[32];
+  if (xp) r = *xp;
   uint4 s = make_uint4(0, 0, 0, 0);
   for (size_t b = (size_t)blockIdx.x * blockDim.x + threadIdx.x; b < half; b += (size_t)gridDim.x * blockDim.x) {
     const uint4 lo = in[b], hi = in[b + half];
@@ -454,8 +459,8 @@ __global__ void __launch_bounds__(256) fix_kernel(const uint4* in, uint4* out, s
 }
 
 cudaError_t launch_fix(const uint4* in, uint4* out, size_t half, uint4 r, const uint4* heq, size_t next_half,
-                       uint32_t* acc, cudaStream_t st) {
-  fix_kernel<<<grid_for(half, 256), 256, 0, st>>>(in, out, half, r, heq, next_half, acc);
+                       uint32_t* acc, cudaStream_t st, const uint4* xp) {
+  fix_kernel<<<grid_for(half, 256), 256, 0, st>>>(in, out, half, r, heq, next_half, acc, xp);
   COUNT_LAUNCH();
   return cudaGetLastError();
 }
