@@ -225,7 +225,8 @@ int bf_sumcheck_prove_device(bf_pcs* pcs, int k, int num_vars, const void* d_pol
  * When enabled, every launch group is bracketed by events; bf_profile_read
  * returns accumulated milliseconds and launch counts per class:
  * 0 encode (NTT passes), 1 codeword leaves, 2 tree levels, 3 folded-codeword
- * leaves, 4 fold, 5 fix + sumcheck reduction, 6 eq table, 7 query gather. */
+ * leaves, 4 fold, 5 fix + sumcheck reduction, 6 eq table, 7 query gather,
+ * 8 single-block last rounds of open, 9 on-device transcript steps. */
 int bf_profile_enable(bf_pcs* pcs, int on);
 int bf_profile_read(bf_pcs* pcs, double* ms, uint64_t* launches, int nclasses);
 

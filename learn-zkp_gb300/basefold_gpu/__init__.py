@@ -285,7 +285,8 @@ class Basefold:
         return _split_sumcheck(out, k, num_vars)
 
     # -- timing of kernel classes -----------------------------------------------
-    PROFILE_CLASSES = ["encode", "leaves", "tree", "pi_leaves", "fold", "fix", "eq", "gather"]
+    PROFILE_CLASSES = ["encode", "leaves", "tree", "pi_leaves", "fold", "fix", "eq", "gather", "open_tail",
+                       "transcript"]
 
     def profile(self, on: bool = True) -> None:
         check(lib().bf_profile_enable(self._h, 1 if on else 0))

@@ -110,8 +110,11 @@ inline uint4 to_uint4(u128 v) {
 }
 
 // Kernel classes timed with CUDA events when profiling is on.
-constexpr int kProfClasses = 8;
-enum ProfClass { P_ENCODE = 0, P_LEAVES = 1, P_TREE = 2, P_PI_LEAVES = 3, P_FOLD = 4, P_FIX = 5, P_EQ = 6, P_GATHER = 7 };
+constexpr int kProfClasses = 10;
+enum ProfClass {
+  P_ENCODE = 0, P_LEAVES = 1, P_TREE = 2, P_PI_LEAVES = 3, P_FOLD = 4, P_FIX = 5, P_EQ = 6, P_GATHER = 7,
+  P_TAIL = 8, P_TRANSCRIPT = 9
+};
 
 struct Profiler {
   bool on = false;

@@ -266,8 +266,11 @@ int open_resident_enqueue(bf_open_session* s, const bfh::Challenger& ch, const u
   const int i_tail = d > 0 ? tail_first_round(p, d) : -1;
   for (int i = d - 1; i > i_tail; --i) {  // large rounds: one kernel per step
     const uint4* root_i = (i == d - 1) ? s->first_root_dev() : reinterpret_cast<const uint4*>(s->stage(i));
-    CU(bf::launch_open_round(s->w_state, i, d, scal, root_i, reinterpret_cast<const uint4*>(s->stage(i) + 32),
-                             s->w_rec + 64 * (size_t)(d - 1 - i), st));
+    {
+      ProfScope ps(p->prof, st, P_TRANSCRIPT);
+      CU(bf::launch_open_round(s->w_state, i, d, scal, root_i, reinterpret_cast<const uint4*>(s->stage(i) + 32),
+                               s->w_rec + 64 * (size_t)(d - 1 - i), st));
+    }
     const size_t ni = p->n_i(i);
     const uint4* pi_in = (i == d - 1) ? s->first_pi() : s->pi_fold_out(i + 1);
     {
@@ -304,7 +307,7 @@ int open_resident_enqueue(bf_open_session* s, const bfh::Challenger& ch, const u
   tp.state = s->w_state;
   tp.result = s->w_rec + 64 * (size_t)(d - 1 - i_tail);
   {
-    ProfScope ps(p->prof, st, P_TREE);
+    ProfScope ps(p->prof, st, P_TAIL);
     CU(bf::launch_open_tail(tp, st));
   }
   CU(cudaMemcpyAsync(s->res_pin, s->w_rec, rec_bytes(d), cudaMemcpyDeviceToHost, st));

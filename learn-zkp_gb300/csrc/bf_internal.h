@@ -87,9 +87,10 @@ struct alignas(16) DevTranscript {
   int in_len, out_len, pad_[2];
 };
 // Device-resident state of one open (basefold.rs:133-232): the transcript,
-// the claim of the current sumcheck round (`outer`), the EvalProver claim
-// (`inner`), the product of delta scalars (eval_impr.rs:45-51) and the last
-// challenge.  status != 0: the transcript input outgrew kTrMax.
+// the claim of the first sumcheck round (`outer`, the evaluation), the
+// EvalProver claim of the later rounds (`inner`), the product of delta
+// scalars (eval_impr.rs:45-51) and the last challenge.  status != 0: the
+// transcript input outgrew kTrMax.
 struct alignas(16) OpenState {
   DevTranscript tr;
   uint4 outer, inner, delta, x;
@@ -107,8 +108,9 @@ cudaError_t launch_open_round(OpenState* s, int i, int d, const uint4* scal, con
                               uint8_t* rec, cudaStream_t st);
 
 // ---- the last rounds of open in one block, then the final polynomial
-constexpr int kTailThreads = 512;
-constexpr int kTailMaxLeavesLog = 11;    // rounds whose next tree has <= 2^11 leaves
+constexpr int kTailThreads = 256;
+constexpr int kTailMaxLeavesLog = 9;     // rounds whose next tree has <= 2^9 leaves
+constexpr int kWarpLevelMax = 32;        // tree levels of at most this many nodes hash one node per warp
 struct TailParams {
   int i0, d, log2_c;        // rounds i0 .. 0 (i0 = -1: none)
   const uint4* pi_first;    // folded codeword input of round d-1

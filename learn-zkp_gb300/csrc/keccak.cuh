@@ -195,6 +195,86 @@ __device__ __forceinline__ Digest hash_node(const Digest& l, const Digest& r) {
   return digest_from_state(s);
 }
 
+// ---------------------------------------------------------------------------
+// Keccak-f[1600] spread over a warp, for latency-bound hashing (the top
+// levels of a Merkle tree, the transcript): lane j < 25 holds state word
+// A[x][y], j = x + 5y; lanes 25..31 only take part in the shuffles.  One
+// round is nine 64-bit shuffles (theta column sums and neighbours, pi, chi)
+// and a per-lane rotation, so a permutation's latency is a few times shorter
+// than one thread's, at several times the instructions.
+struct WarpKeccak {
+  int lane, x, y;
+  int col[4];      // theta: the other four lanes of this column
+  int xm1, xp1;    // theta: lanes of columns x-1, x+1 in this row
+  int pi_src;      // pi: B[x][y] = A[x'][y'] with x = y', y = 2x' + 3y'
+  int chi1, chi2;  // chi: lanes of columns x+1, x+2 in this row
+  int rho;         // rotation of this lane
+
+  __device__ __forceinline__ WarpKeccak() {
+    lane = threadIdx.x & 31;
+    const int j = lane < 25 ? lane : 0;
+    x = j % 5;
+    y = j / 5;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) col[k] = x + 5 * ((y + 1 + k) % 5);
+    xm1 = (x + 4) % 5 + 5 * y;
+    xp1 = (x + 1) % 5 + 5 * y;
+    // lane (X, Y) receives A[x'][y'] with y' = X, x' = 3 (Y - 3X) mod 5
+    const int xs = (3 * ((y - 3 * x) % 5 + 5)) % 5;
+    pi_src = xs + 5 * x;
+    chi1 = (x + 1) % 5 + 5 * y;
+    chi2 = (x + 2) % 5 + 5 * y;
+    // rotation of A[x][y] (FIPS 202 rho offsets), applied before pi moves it
+    constexpr int kRho[25] = {0,  1,  62, 28, 27, 36, 44, 6,  55, 20, 3,  10, 43,
+                              25, 39, 41, 45, 15, 21, 8,  18, 2,  61, 56, 14};
+    int r = 0;
+#pragma unroll
+    for (int k = 0; k < 25; ++k)
+      if (k == j) r = kRho[k];
+    rho = r;
+  }
+
+  static __device__ __forceinline__ uint2 shfl(uint2 v, int src) {
+    return make_uint2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+  }
+  static __device__ __forceinline__ uint2 rolv(uint2 v, int r) {
+    if (r & 32) v = make_uint2(v.y, v.x);
+    const int s = r & 31;
+    return make_uint2(__funnelshift_l(v.y, v.x, s), __funnelshift_l(v.x, v.y, s));
+  }
+
+  // All 32 lanes call this; `a` is this lane's word.
+  __device__ __forceinline__ uint2 permute(uint2 a) const {
+#pragma unroll 1
+    for (int r = 0; r < 24; ++r) {
+      const uint2 c1 = shfl(a, col[0]), c2 = shfl(a, col[1]), c3 = shfl(a, col[2]), c4 = shfl(a, col[3]);
+      const uint2 c = kx5(a, c1, c2, c3, c4);  // C[x]
+      const uint2 cm = shfl(c, xm1), cp = shfl(c, xp1);
+      a = kx3(a, cm, krol<1>(cp));             // theta
+      a = rolv(a, rho);                        // rho
+      const uint2 b = shfl(a, pi_src);         // pi
+      const uint2 b1 = shfl(b, chi1), b2 = shfl(b, chi2);
+      a = kchi(b, b1, b2);                     // chi
+      if (lane == 0) a = kx2(a, c_keccak_rc[r]);  // iota
+    }
+    return a;
+  }
+};
+
+// keccak256(left || right) of node `s` by one warp: lanes 0..7 read the 64
+// message bytes, lanes 0..3 write the digest.
+__device__ __forceinline__ void warp_hash_node(const WarpKeccak& wk, const uint4* cur, size_t s, size_t h, uint4* nxt) {
+  const uint2* left = reinterpret_cast<const uint2*>(cur + 2 * s);
+  const uint2* right = reinterpret_cast<const uint2*>(cur + 2 * (s + h));
+  uint2 a = make_uint2(0, 0);
+  if (wk.lane < 4) a = left[wk.lane];
+  else if (wk.lane < 8) a = right[wk.lane - 4];
+  if (wk.lane == 8) a.x ^= 0x01u;         // pad10*1 after 64 bytes
+  if (wk.lane == 16) a.y ^= 0x80000000u;  // last byte of the 136-byte rate
+  a = wk.permute(a);
+  if (wk.lane < 4) reinterpret_cast<uint2*>(nxt + 2 * s)[wk.lane] = a;
+}
+
 __device__ __forceinline__ Digest load_digest(const uint4* p, size_t i) {
   Digest d;
   d.lo = p[2 * i];

@@ -233,12 +233,18 @@ __global__ void __launch_bounds__(128) level_kernel(const uint4* __restrict__ pr
 // The remaining levels of a small tree, in one block; the root is also
 // copied to `root_out` when given.
 __global__ void __launch_bounds__(256) tree_top_kernel(uint4* level, size_t n, uint4* root_out) {
+  const WarpKeccak wk;
+  const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   uint4* cur = level;
   while (n > 1) {
     const size_t h = n >> 1;
     uint4* nxt = cur + 2 * n;
-    for (size_t s = threadIdx.x; s < h; s += blockDim.x)
-      store_digest(nxt, s, hash_node(load_digest(cur, s), load_digest(cur, s + h)));
+    if (h <= (size_t)kWarpLevelMax) {  // latency-bound: one warp per node
+      for (size_t s = warp; s < h; s += nwarps) warp_hash_node(wk, cur, s, h, nxt);
+    } else {
+      for (size_t s = threadIdx.x; s < h; s += blockDim.x)
+        store_digest(nxt, s, hash_node(load_digest(cur, s), load_digest(cur, s + h)));
+    }
     __syncthreads();
     cur = nxt;
     n = h;

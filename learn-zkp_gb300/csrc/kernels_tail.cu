@@ -31,109 +31,140 @@ namespace {
 
 __device__ __forceinline__ uint4 one_dev() { return make_uint4(1u, 0u, 0u, 0xc2000000u); }
 
-// Keccak-256 (original padding) of `len` bytes.
-__device__ void keccak256_bytes(const uint8_t* msg, int len, uint8_t digest[32]) {
-  uint2 s[25];
-#pragma unroll
-  for (int k = 0; k < 25; ++k) s[k] = make_uint2(0, 0);
-  int off = 0;
-  while (true) {
+// The transcript is kept in shared memory and driven by one warp: the
+// Keccak permutations run on all 32 lanes (WarpKeccak), the byte bookkeeping
+// and the field arithmetic on lane 0, with __syncwarp between them.
+
+// HashChallenger::flush: digest = keccak256(input); input = output = digest.
+__device__ void warp_flush(const WarpKeccak& wk, DevTranscript& t) {
+  __syncwarp();
+  const int len = t.in_len;
+  uint2 a = make_uint2(0, 0);
+  for (int off = 0;; off += 136) {
     const int take = len - off < 136 ? len - off : 136;
     const bool last = take < 136;
-#pragma unroll
-    for (int q = 0; q < 17; ++q) {
-      uint32_t w0 = 0, w1 = 0;
-#pragma unroll
-      for (int b = 0; b < 8; ++b) {
-        const int pos = 8 * q + b;
-        uint32_t v = pos < take ? msg[off + pos] : 0u;
-        if (last && pos == take) v ^= 0x01u;  // pad10*1
-        if (last && pos == 135) v ^= 0x80u;
-        if (b < 4)
-          w0 |= v << (8 * b);
-        else
-          w1 |= v << (8 * (b - 4));
+    if (wk.lane < 17) {
+      const int pos0 = 8 * wk.lane;
+      uint2 w;
+      if (pos0 + 8 <= take) {  // a whole message word (off and pos0 are multiples of 8)
+        w = *reinterpret_cast<const uint2*>(t.in + off + pos0);
+      } else {
+        uint32_t h[2] = {0, 0};
+        for (int b = 0; b < 8; ++b) {
+          const int pos = pos0 + b;
+          uint32_t v = pos < take ? t.in[off + pos] : 0u;
+          if (last && pos == take) v ^= 0x01u;  // pad10*1 (original Keccak)
+          h[b >> 2] |= v << (8 * (b & 3));
+        }
+        w = make_uint2(h[0], h[1]);
       }
-      s[q] = kx2(s[q], make_uint2(w0, w1));
+      if (last && wk.lane == 16) w.y ^= 0x80000000u;  // last byte of the rate
+      a = kx2(a, w);
     }
-    keccak_f1600(s);
-    off += take;
+    a = wk.permute(a);
     if (last) break;
   }
-#pragma unroll
-  for (int q = 0; q < 4; ++q)
-#pragma unroll
-    for (int b = 0; b < 4; ++b) {
-      digest[8 * q + b] = (uint8_t)(s[q].x >> (8 * b));
-      digest[8 * q + 4 + b] = (uint8_t)(s[q].y >> (8 * b));
-    }
-}
-
-// CanObserve<u8>: append to the input, drop unread output.
-__device__ void tr_observe(OpenState& o, const uint8_t* p, int n) {
-  DevTranscript& t = o.tr;
-  t.out_len = 0;
-  if (t.in_len + n > kTrMax) {
-    o.status = 1;
-    return;
+  __syncwarp();
+  if (wk.lane < 4) {
+    reinterpret_cast<uint2*>(t.out)[wk.lane] = a;
+    reinterpret_cast<uint2*>(t.in)[wk.lane] = a;
   }
-  for (int k = 0; k < n; ++k) t.in[t.in_len++] = p[k];
-}
-
-// CanSample<u8>: when the output is empty, hash the input; the digest becomes
-// both the new input and the output, which is read from its end.
-__device__ uint8_t tr_sample_byte(DevTranscript& t) {
-  if (t.out_len == 0) {
-    uint8_t d[32];
-    keccak256_bytes(t.in, t.in_len, d);
-    for (int k = 0; k < 32; ++k) {
-      t.out[k] = d[k];
-      t.in[k] = d[k];
-    }
+  if (wk.lane == 0) {
     t.out_len = 32;
     t.in_len = 32;
   }
-  return t.out[--t.out_len];
+  __syncwarp();
 }
 
-// A field element from 16 sampled bytes, little-endian (from_uniform_bytes.rs:20-26).
-__device__ uint4 tr_sample_elem(DevTranscript& t) {
+// CanObserve<u8> of the 16*N bytes of v (lane 0): append to the input, drop
+// unread output.
+template <int N>
+__device__ void tr_observe(OpenState& o, const uint4 (&v)[N]) {
+  DevTranscript& t = o.tr;
+  t.out_len = 0;
+  const int len = t.in_len;
+  if (len + 16 * N > kTrMax) {
+    o.status = 1;
+    return;
+  }
+  if ((len & 15) == 0) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) reinterpret_cast<uint4*>(t.in + len)[k] = v[k];
+  } else {
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      const uint32_t w[4] = {v[k].x, v[k].y, v[k].z, v[k].w};
+#pragma unroll
+      for (int b = 0; b < 16; ++b) t.in[len + 16 * k + b] = (uint8_t)(w[b >> 2] >> (8 * (b & 3)));
+    }
+  }
+  t.in_len = len + 16 * N;
+}
+
+// A field element from 16 sampled bytes, each popped from the end of the
+// output, little-endian (challenger.rs sample, from_uniform_bytes.rs:20-26).
+// Warp-collective; the element is returned on lane 0.
+__device__ uint4 warp_sample_elem(const WarpKeccak& wk, OpenState& o) {
+  __syncwarp();
+  if (o.tr.out_len == 0) warp_flush(wk, o.tr);
   uint32_t w[4] = {0, 0, 0, 0};
-  for (int k = 0; k < 16; ++k) w[k >> 2] |= (uint32_t)tr_sample_byte(t) << (8 * (k & 3));
+  if (o.tr.out_len >= 16) {
+    if (wk.lane == 0) {
+      const int top = o.tr.out_len - 1;
+#pragma unroll
+      for (int k = 0; k < 16; ++k) w[k >> 2] |= (uint32_t)o.tr.out[top - k] << (8 * (k & 3));
+      o.tr.out_len = top + 1 - 16;
+    }
+  } else {
+    for (int k = 0; k < 16; ++k) {
+      __syncwarp();
+      if (o.tr.out_len == 0) warp_flush(wk, o.tr);
+      if (wk.lane == 0) {
+        const uint32_t byte = o.tr.out[--o.tr.out_len];
+        w[k >> 2] |= byte << (8 * (k & 3));
+      }
+    }
+  }
+  __syncwarp();
   return make_uint4(w[0], w[1], w[2], w[3]);
 }
 
-__device__ void put4(uint8_t* p, uint4 v) {
-  const uint32_t w[4] = {v.x, v.y, v.z, v.w};
-  for (int k = 0; k < 4; ++k)
-    for (int b = 0; b < 4; ++b) p[4 * k + b] = (uint8_t)(w[k] >> (8 * b));
-}
-
-// Transcript step of round i (one thread).  S = sum_b half_eq[b] poly_lo[b].
-__device__ void round_step(OpenState& o, int i, int d, const uint4* scal, uint4 root_lo, uint4 root_hi, uint4 S,
-                           uint8_t* rec) {
-  const uint4 ONE = one_dev();
-  const uint4 r = scal[3 * i], r_inv = scal[3 * i + 1], corr = scal[3 * i + 2];
-  const uint4 sc_val = (i == d - 1) ? o.outer : o.inner;
-  const uint4 c0 = gf_mul(corr, S);
-  const uint4 one_r = gf_add(ONE, r);
-  const uint4 c1 = gf_add(gf_mul(gf_add(sc_val, gf_mul(one_r, c0)), r_inv), c0);
-  const uint4 scalar = (i == d - 1) ? ONE : o.delta;
-  const uint4 d0 = gf_mul(scalar, one_r);
-  const uint4 d1 = gf_mul(scalar, gf_add(r, one_r));
-  const uint4 rp0 = gf_mul(c0, d0);
-  const uint4 rp1 = gf_add(gf_mul(c0, d1), gf_mul(c1, d0));
-  const uint4 rp2 = gf_mul(c1, d1);
-  put4(rec, root_lo);
-  put4(rec + 16, root_hi);
-  put4(rec + 32, rp0);
-  put4(rec + 48, rp2);
-  tr_observe(o, rec, 64);  // root (basefold.rs:356), then [c0, c2] (sumcheck/src/lib.rs:97)
-  const uint4 x = tr_sample_elem(o.tr);
-  o.inner = gf_add(gf_mul(c1, x), c0);                            // EvalProver::fix_last_var (eval.rs:108-111)
-  o.outer = gf_add(gf_mul(gf_add(gf_mul(rp2, x), rp1), x), rp0);  // SumcheckSubclaim::reduce
-  o.delta = gf_mul(o.delta, gf_add(one_r, x));
-  o.x = x;
+// Transcript step of round i, warp-collective.  S = sum_b half_eq[b] poly_lo[b].
+// `rec` (global, 16-byte aligned) receives root, c0, c2.
+//
+// EvalImprProver::compute_round_poly gives [c0, c1] (eval_impr.rs:116-127);
+// EvalProver lifts it by delta = d * [1 - r, r - (1 - r)] = d * [1 + r, 1]
+// in characteristic 2 (eval.rs:89-106), so the round polynomial is
+// (c0 + c1 X)(d (1 + r) + d X): c0' = c0 d (1 + r), c2' = c1 d.  After the
+// challenge x the EvalProver claim is c0 + c1 x and d becomes d (1 + r + x);
+// the sumcheck claim (the round polynomial at x) is only read in the first
+// round, so it is not carried.
+__device__ void round_step(const WarpKeccak& wk, OpenState& o, int i, int d, const uint4* scal, uint4 root_lo,
+                           uint4 root_hi, uint4 S, uint4* rec) {
+  uint4 c0, c1, one_r;
+  if (wk.lane == 0) {
+    const uint4 ONE = one_dev();
+    const uint4 r = scal[3 * i], r_inv = scal[3 * i + 1], corr = scal[3 * i + 2];
+    const uint4 claim = (i == d - 1) ? o.outer : o.inner;
+    c0 = gf_mul(corr, S);
+    one_r = gf_add(ONE, r);
+    c1 = gf_add(gf_mul(gf_add(claim, gf_mul(one_r, c0)), r_inv), c0);
+    const uint4 rp0 = gf_mul(c0, gf_mul(o.delta, one_r));
+    const uint4 rp2 = gf_mul(c1, o.delta);
+    rec[0] = root_lo;
+    rec[1] = root_hi;
+    rec[2] = rp0;
+    rec[3] = rp2;
+    const uint4 m[4] = {root_lo, root_hi, rp0, rp2};
+    tr_observe(o, m);  // root (basefold.rs:356), then [c0, c2] (sumcheck/src/lib.rs:97)
+  }
+  const uint4 x = warp_sample_elem(wk, o);
+  if (wk.lane == 0) {
+    o.inner = gf_add(gf_mul(c1, x), c0);  // EvalProver::fix_last_var (eval.rs:108-111)
+    o.delta = gf_mul(o.delta, gf_add(one_r, x));
+    o.x = x;
+  }
+  __syncwarp();
 }
 
 constexpr int kStateVecs = (int)(sizeof(OpenState) / sizeof(uint4));
@@ -156,17 +187,14 @@ __global__ void __launch_bounds__(32) open_observe_kernel(OpenState* S, const ui
   state_load(sh, S);
   __syncthreads();
   if (threadIdx.x == 0) {
-    uint8_t b[32];
     if (root) {
-      put4(b, root[0]);
-      put4(b + 16, root[1]);
-      tr_observe(sh, b, 32);
+      const uint4 m[2] = {root[0], root[1]};
+      tr_observe(sh, m);
     }
     if (value) {
-      const uint4 v = value[0];
-      put4(b, v);
-      tr_observe(sh, b, 16);
-      sh.outer = v;
+      const uint4 m[1] = {value[0]};
+      tr_observe(sh, m);
+      sh.outer = m[0];
     }
   }
   __syncthreads();
@@ -176,9 +204,10 @@ __global__ void __launch_bounds__(32) open_observe_kernel(OpenState* S, const ui
 __global__ void __launch_bounds__(32) open_round_kernel(OpenState* S, int i, int d, const uint4* scal,
                                                         const uint4* root, const uint4* Sred, uint8_t* rec) {
   __shared__ OpenState sh;
+  const WarpKeccak wk;
   state_load(sh, S);
   __syncthreads();
-  if (threadIdx.x == 0) round_step(sh, i, d, scal, root[0], root[1], Sred[0], rec);
+  round_step(wk, sh, i, d, scal, root[0], root[1], Sred[0], reinterpret_cast<uint4*>(rec));
   __syncthreads();
   state_store(S, sh);
 }
@@ -189,6 +218,8 @@ __global__ void __launch_bounds__(kTailThreads, 1) open_tail_kernel(TailParams P
   __shared__ uint4 scratch[32];
   const int d = P.d;
   const size_t c = (size_t)1 << P.log2_c;
+  const WarpKeccak wk;
+  const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   state_load(sh, P.state);
   if (threadIdx.x == 0 && P.i0 >= 0) {
     sh_root_lo = P.root_i0[0];
@@ -198,8 +229,9 @@ __global__ void __launch_bounds__(kTailThreads, 1) open_tail_kernel(TailParams P
   __syncthreads();
   int k = 0;
   for (int i = P.i0; i >= 0; --i, ++k) {
-    // ---- transcript step (thread 0) ----
-    if (threadIdx.x == 0) round_step(sh, i, d, P.scal, sh_root_lo, sh_root_hi, sh_S, P.result + 64 * (size_t)k);
+    // ---- transcript step (warp 0) ----
+    if (warp == 0)
+      round_step(wk, sh, i, d, P.scal, sh_root_lo, sh_root_hi, sh_S, reinterpret_cast<uint4*>(P.result + 64 * (size_t)k));
     __syncthreads();
     const uint4 x = sh.x;
     // ---- fold (+ next leaves) and fix (+ next reduction), whole block ----
@@ -254,8 +286,12 @@ __global__ void __launch_bounds__(kTailThreads, 1) open_tail_kernel(TailParams P
       while (n > 1) {
         const size_t h = n >> 1;
         uint4* nxt = cur + 2 * n;
-        for (size_t s = threadIdx.x; s < h; s += blockDim.x)
-          store_digest(nxt, s, hash_node(load_digest(cur, s), load_digest(cur, s + h)));
+        if (h <= (size_t)kWarpLevelMax) {  // latency-bound: one warp per node
+          for (size_t s = warp; s < h; s += nwarps) warp_hash_node(wk, cur, s, h, nxt);
+        } else {
+          for (size_t s = threadIdx.x; s < h; s += blockDim.x)
+            store_digest(nxt, s, hash_node(load_digest(cur, s), load_digest(cur, s + h)));
+        }
         __syncthreads();
         cur = nxt;
         n = h;
@@ -270,9 +306,9 @@ __global__ void __launch_bounds__(kTailThreads, 1) open_tail_kernel(TailParams P
   // ---- final polynomial (basefold.rs:196) ----
   if (threadIdx.x == 0) {
     const uint4 fin = (k == 0) ? P.poly_first[0] : P.poly[0];
-    uint8_t* rec = P.result + 64 * (size_t)k;
-    put4(rec, fin);
-    tr_observe(sh, rec, 16);
+    reinterpret_cast<uint4*>(P.result + 64 * (size_t)k)[0] = fin;
+    const uint4 m[1] = {fin};
+    tr_observe(sh, m);
   }
   __syncthreads();
   state_store(P.state, sh);
