@@ -150,13 +150,32 @@ int bf_open_finish(bf_open_session* s, const uint64_t* indices, size_t nq, uint8
                    size_t* proof_len);
 void bf_open_session_free(bf_open_session* s);
 
+/* ---- Launch-shape autotuner.  No counterpart in the reference.
+ * A pcs's launch shapes are four integers: threads per NTT block (128, 256,
+ * 512), butterfly layers per NTT pass (6..12, a shared-memory tile of 2^T
+ * elements), the largest Merkle level run by the single-block top kernel
+ * (64..4096, a power of two), and the single-block open tail (rounds whose
+ * next tree has <= 2^tail_log leaves, 1..11).  They change how work is
+ * launched, never the proof bytes.  bf_pcs_autotune times `reps` whole
+ * proofs (commit + eval + open) on random device data per candidate, one
+ * parameter at a time, keeps the fastest in the pcs, and writes a JSON
+ * report (timings per candidate, ms) into `report` when given.
+ * get/set: vals = {ntt_threads, ntt_max_T, top_nodes, tail_log}. */
+int bf_pcs_autotune(bf_pcs* pcs, int reps, char* report, size_t cap);
+int bf_pcs_get_tune(const bf_pcs* pcs, int* vals, int n);
+int bf_pcs_set_tune(bf_pcs* pcs, const int* vals, int n);
+
 /* ---- Prover engine: many jobs of different sizes in flight at once.
- * Jobs run as per-stream state machines; the engine admits them while
- * streams (max_inflight) and the HBM budget (mem_budget bytes, 0 = 80% of
- * free memory) allow, and advances whichever job's GPU step has finished, so
- * requests also join between the rounds of running ones.  Proofs are
- * identical to bf_commit/bf_eval/bf_open one at a time.  (No counterpart in
- * the reference, which proves one polynomial at a time on the CPU.)
+ * Each job runs on one stream of a pool: at admission its commit,
+ * evaluation and whole open (transcript on the device) are queued at once;
+ * the host only samples the query positions and reads the proof back.  The
+ * engine admits jobs while streams (max_inflight) and the HBM budget
+ * (mem_budget bytes, 0 = 80% of free memory) allow, so requests join while
+ * others run.  Proofs are identical to bf_commit/bf_eval/bf_open one at a
+ * time.  (No counterpart in the reference, which proves one polynomial at a
+ * time on the CPU.)
+ * bf_engine_autotune: reps > 0 autotunes (bf_pcs_autotune) each size the
+ *   first time a job of that size is admitted; 0 (default) keeps defaults.
  * bf_engine_prove: runs `count` jobs to completion on the calling thread.
  * bf_engine_start/stop + submit/poll: serving from a background thread;
  *   submitted bf_job structs must stay valid until returned by poll. */
@@ -168,6 +187,7 @@ int bf_engine_start(bf_engine* e);
 int bf_engine_stop(bf_engine* e);
 int bf_engine_submit(bf_engine* e, bf_job* job, int device_input);
 int bf_engine_poll(bf_engine* e, bf_job** done, size_t cap, size_t* n);
+int bf_engine_autotune(bf_engine* e, int reps);
 
 /* ---- Evaluation that allocates nothing.  No counterpart in the reference.
  * Same value as bf_eval (MultiPoly::evaluate of 2^num_vars evaluations at

@@ -288,6 +288,30 @@ class Basefold:
     PROFILE_CLASSES = ["encode", "leaves", "tree", "pi_leaves", "fold", "fix", "eq", "gather", "open_tail",
                        "transcript"]
 
+    # -- launch shapes -----------------------------------------------------------
+    TUNE_KEYS = ["ntt_threads", "ntt_max_T", "top_nodes", "tail_log"]
+
+    def autotune(self, reps: int = 3) -> dict:
+        """Times whole proofs per candidate launch shape and keeps the fastest
+        in this pcs (bf_pcs_autotune); returns the report."""
+        buf = C.create_string_buffer(8192)
+        check(lib().bf_pcs_autotune(self._h, reps, buf, len(buf)))
+        import json
+        return json.loads(buf.value.decode())
+
+    @property
+    def tune(self) -> dict:
+        v = (C.c_int * 4)()
+        check(lib().bf_pcs_get_tune(self._h, v, 4))
+        return dict(zip(self.TUNE_KEYS, list(v)))
+
+    @tune.setter
+    def tune(self, t: dict) -> None:
+        cur = self.tune
+        cur.update(t)
+        v = (C.c_int * 4)(*[int(cur[k]) for k in self.TUNE_KEYS])
+        check(lib().bf_pcs_set_tune(self._h, v, 4))
+
     def profile(self, on: bool = True) -> None:
         check(lib().bf_profile_enable(self._h, 1 if on else 0))
 
@@ -381,11 +405,13 @@ class Engine:
     requests from a background thread (continuous batching)."""
 
     def __init__(self, device: int = 0, lambda_: int = 128, log2_c: int = 1, max_inflight: int = 16,
-                 mem_budget: int = 0):
+                 mem_budget: int = 0, autotune_reps: int = 0):
         h = C.c_void_p()
         check(lib().bf_engine_create(device, lambda_, log2_c, max_inflight, mem_budget, C.byref(h)))
         self._h, self.log2_c = h, log2_c
         self._keep = {}
+        if autotune_reps:
+            check(lib().bf_engine_autotune(h, autotune_reps))
 
     def __del__(self):
         h = getattr(self, "_h", None)

@@ -19,7 +19,8 @@ EXPORTS = [
     "bf_challenger_from_state", "bf_sumcheck_prove", "bf_sumcheck_prove_device", "bf_profile_enable",
     "bf_profile_read", "bf_test_gf_mul", "bf_test_keccak_f", "bf_engine_create", "bf_engine_free",
     "bf_engine_proof_size", "bf_engine_prove", "bf_engine_start", "bf_engine_stop", "bf_engine_submit",
-    "bf_engine_poll", "bf_eval_noalloc",
+    "bf_engine_poll", "bf_eval_noalloc", "bf_pcs_autotune", "bf_pcs_get_tune", "bf_pcs_set_tune",
+    "bf_engine_autotune",
 ]
 
 BF_OK = 0
@@ -107,6 +108,10 @@ def lib():
         "bf_engine_submit": ([vp, C.POINTER(BfJob), i], i),
         "bf_engine_poll": ([vp, C.POINTER(C.POINTER(BfJob)), sz, C.POINTER(sz)], i),
         "bf_eval_noalloc": ([vp, i, u8p, vp, vp], i),
+        "bf_pcs_autotune": ([vp, i, C.c_char_p, sz], i),
+        "bf_pcs_get_tune": ([vp, C.POINTER(C.c_int), i], i),
+        "bf_pcs_set_tune": ([vp, C.POINTER(C.c_int), i], i),
+        "bf_engine_autotune": ([vp, i], i),
     }
     for name, (args, res) in decl.items():
         f = getattr(L, name)

@@ -199,6 +199,7 @@ struct bf_pcs {
   bfapi::PinnedBuf pinned;
   std::vector<std::unique_ptr<bfapi::PinnedBuf>> pinned_cache;  // staging kept between open sessions
   bfapi::Profiler prof;
+  bf::Tune tune;  // launch shapes and thresholds (bf_pcs_autotune / bf_pcs_set_tune)
 
   size_t n_d() const { return (size_t)1 << L; }
   size_t c() const { return (size_t)1 << log2_c; }

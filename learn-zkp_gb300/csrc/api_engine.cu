@@ -56,6 +56,7 @@ struct Job {
 
 struct bf_engine {
   int device = 0, lambda = 128, log2_c = 1, max_inflight = 8;
+  int autotune_reps = 0;  // > 0: autotune each size's pcs when it is created
   size_t mem_budget = 0, mem_used = 0;
   std::map<int, bf_pcs*> pcs_by_n;
   std::vector<cudaStream_t> streams;
@@ -91,6 +92,7 @@ int get_pcs(bf_engine* e, int n, bf_pcs** out) {
   bf_pcs* p = nullptr;
   TRY(bf_pcs_setup(e->device, e->lambda, e->log2_c, n, e->streams[0], &p));
   e->pcs_by_n[n] = p;
+  if (e->autotune_reps > 0) TRY(bf_pcs_autotune(p, e->autotune_reps, nullptr, 0));
   *out = p;
   return BF_OK;
 }
@@ -316,6 +318,12 @@ int bf_engine_submit(bf_engine* e, bf_job* job, int device_input) {
   e->queue.push_back(j);
   e->outstanding += 1;
   e->cv.notify_all();
+  return BF_OK;
+}
+
+int bf_engine_autotune(bf_engine* e, int reps) {
+  if (!e || reps < 0 || reps > 100) return fail(BF_ERR_ARG, "bad argument");
+  e->autotune_reps = reps;
   return BF_OK;
 }
 

@@ -220,9 +220,9 @@ int ensure_message(bf_open_session* s) {
 namespace bfapi {
 
 // First round run by the single-block kernel: the largest i <= d-1 whose
-// folded codeword has at most 2^(kTailMaxLeavesLog+1) entries.
+// folded codeword has at most 2^(tail_log+1) entries.
 int tail_first_round(const bf_pcs* p, int d) {
-  const int lim = bf::kTailMaxLeavesLog + 1 - p->log2_c;
+  const int lim = p->tune.tail_log + 1 - p->log2_c;
   return std::min(d - 1, lim);
 }
 
@@ -285,7 +285,8 @@ int open_resident_enqueue(bf_open_session* s, const bfh::Challenger& ch, const u
     }
     {
       ProfScope ps(p->prof, st, P_TREE);
-      CU(bf::launch_tree(s->pi_tree(i - 1), p->n_i(i - 1), st, reinterpret_cast<uint4*>(s->stage(i - 1))));
+      CU(bf::launch_tree(s->pi_tree(i - 1), p->n_i(i - 1), st, reinterpret_cast<uint4*>(s->stage(i - 1)),
+                         p->tune.top_nodes));
     }
   }
   bf::TailParams tp{};
@@ -496,7 +497,7 @@ int open_start_impl(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, co
       ProfScope ps(p->prof, st, P_TREE);
       const size_t n1 = p->n_i(d - 1);
       CU(bf::launch_leaves_pair(s->w_pi_first, s->w_pi_first_tree, n1, st));
-      CU(bf::launch_tree(s->w_pi_first_tree, n1, st, reinterpret_cast<uint4*>(s->stage(d - 1))));
+      CU(bf::launch_tree(s->w_pi_first_tree, n1, st, reinterpret_cast<uint4*>(s->stage(d - 1)), p->tune.top_nodes));
     }
     std::memcpy(pin + 64 + 16 * w, point, 16 * (size_t)d);
     CU(cudaMemcpyAsync(s->w_point, pin + 64 + 16 * w, 16 * (size_t)d, cudaMemcpyHostToDevice, st));
@@ -589,7 +590,8 @@ int bf_open_challenge(bf_open_session* s, const uint8_t r_i[16]) {
   if (i > 0) {
     {
       ProfScope ps(p->prof, st, P_TREE);
-      CU(bf::launch_tree(s->pi_tree(i - 1), p->n_i(i - 1), st, reinterpret_cast<uint4*>(s->stage(i - 1))));
+      CU(bf::launch_tree(s->pi_tree(i - 1), p->n_i(i - 1), st, reinterpret_cast<uint4*>(s->stage(i - 1)),
+                         p->tune.top_nodes));
     }
     CU(cudaMemcpyAsync(pin, s->stage(i - 1), 48, cudaMemcpyDeviceToHost, st));
   } else {

@@ -263,7 +263,7 @@ int commit_enqueue(bf_pcs* p, bf_commitment* cm, const uint4* data, cudaStream_t
     // encode; for width 1 and d >= 1 the last NTT pass also hashes the leaves
     ProfScope ps(p->prof, st, P_ENCODE);
     CU(bf::launch_encode(data, cw, p->d, p->log2_c, w, p->tw_view.as<bf::TwiddleView>(), st,
-                         pairs ? tree : nullptr, pairs ? pit : nullptr));
+                         pairs ? tree : nullptr, pairs ? pit : nullptr, p->tune));
   }
   if (!pairs) {
     ProfScope ps(p->prof, st, P_LEAVES);
@@ -271,8 +271,8 @@ int commit_enqueue(bf_pcs* p, bf_commitment* cm, const uint4* data, cudaStream_t
   }
   {
     ProfScope ps(p->prof, st, P_TREE);
-    CU(bf::launch_tree(tree, nd, st));
-    if (pairs) CU(bf::launch_tree(pit, nd / 2, st));
+    CU(bf::launch_tree(tree, nd, st, nullptr, p->tune.top_nodes));
+    if (pairs) CU(bf::launch_tree(pit, nd / 2, st, nullptr, p->tune.top_nodes));
   }
   CU(cudaMemcpyAsync(roots_pin, tree + 2 * (2 * nd - 2), 32, cudaMemcpyDeviceToHost, st));
   if (pairs) CU(cudaMemcpyAsync(roots_pin + 32, pit + 2 * (nd - 2), 32, cudaMemcpyDeviceToHost, st));

@@ -20,12 +20,24 @@ struct TwiddleView {
   const uint4* hi[kMaxStages];
 };
 
+// Launch shapes and thresholds, chosen per (num_vars, blowup) by the
+// autotuner (bf_pcs_autotune) or left at these defaults.
+constexpr int kNttMaxT = 12;  // largest shared-memory tile of an NTT pass: 2^12 elements
+struct Tune {
+  int ntt_threads = 256;  // threads per NTT pass block: 128, 256 or 512
+  int ntt_max_T = 12;     // butterfly layers per NTT pass (tile 2^T), 6 .. kNttMaxT
+  int top_nodes = 512;    // Merkle levels at or below this many nodes run in one block (64 .. 4096)
+  int tail_log = 8;       // open rounds whose next tree has <= 2^tail_log leaves run in one block (1 .. 11)
+};
+bool tune_valid(const Tune& t);
+
 // Launchers (all asynchronous on `st`).
 // `tw` points to a TwiddleView in device memory.  When `leaves` and
 // `pair_leaves` are given (n >= 1), the last pass also writes the codeword
 // leaves and the first folded-codeword leaves.
 cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t width, const TwiddleView* tw,
-                          cudaStream_t st, uint4* leaves = nullptr, uint4* pair_leaves = nullptr);
+                          cudaStream_t st, uint4* leaves = nullptr, uint4* pair_leaves = nullptr,
+                          const Tune& tune = Tune());
 cudaError_t launch_leaves_elem(const uint4* cw, uint4* leaves, size_t n, size_t width, cudaStream_t st);
 cudaError_t launch_leaves_pair(const uint4* pi, uint4* leaves, size_t n, cudaStream_t st);
 cudaError_t launch_leaves_cw_pairs(const uint4* cw, uint4* leaves, uint4* pair_leaves, size_t n_pairs,
@@ -33,7 +45,10 @@ cudaError_t launch_leaves_cw_pairs(const uint4* cw, uint4* leaves, uint4* pair_l
 // Build every level above `leaves` (n leaves, power of two); levels are stored
 // one after another right after the leaves.  Root = last digest, also copied
 // to `root_out` (32 bytes) when it is not null.
-cudaError_t launch_tree(uint4* leaves, size_t n, cudaStream_t st, uint4* root_out = nullptr);
+cudaError_t launch_tree(uint4* leaves, size_t n, cudaStream_t st, uint4* root_out = nullptr,
+                        size_t top_nodes = 512);
+// SplitMix64 words as field elements (autotuner inputs).
+cudaError_t launch_fill_random(uint4* out, size_t n, uint64_t seed, cudaStream_t st);
 
 cudaError_t launch_eq_table(const uint4* r, int nvars, uint4* out, uint4* tmp_lo, uint4* tmp_hi, cudaStream_t st);
 cudaError_t launch_dot_xor(const uint4* x, const uint4* y, size_t n, uint32_t* acc, cudaStream_t st);
@@ -109,7 +124,7 @@ cudaError_t launch_open_round(OpenState* s, int i, int d, const uint4* scal, con
 
 // ---- the last rounds of open in one block, then the final polynomial
 constexpr int kTailThreads = 256;
-constexpr int kTailMaxLeavesLog = 9;     // rounds whose next tree has <= 2^9 leaves
+constexpr int kTailMaxLeavesLog = 11;    // largest Tune::tail_log
 constexpr int kWarpLevelMax = 32;        // tree levels of at most this many nodes hash one node per warp
 struct TailParams {
   int i0, d, log2_c;        // rounds i0 .. 0 (i0 = -1: none)

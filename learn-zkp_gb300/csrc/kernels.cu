@@ -16,6 +16,7 @@
 //    halves of the level below — so every level is one coalesced pass.
 #include <cuda_runtime.h>
 #include <atomic>
+#include <algorithm>
 #include <cstdint>
 
 #include "bf_internal.h"
@@ -81,7 +82,7 @@ struct PassParams {
 };
 
 template <bool HASH>
-__global__ void __launch_bounds__(256) ntt_pass_kernel(const uint4* __restrict__ m, uint4* __restrict__ cw,
+__global__ void __launch_bounds__(512) ntt_pass_kernel(const uint4* __restrict__ m, uint4* __restrict__ cw,
                                                       PassParams p, const TwiddleView* __restrict__ tw) {
   extern __shared__ uint4 sm[];
   const int n = p.n, T = p.T, s_lo = p.s_lo;
@@ -146,11 +147,17 @@ __global__ void replicate_kernel(const uint4* __restrict__ m, uint4* __restrict_
   for (size_t i = threadIdx.x; i < c * w; i += blockDim.x) cw[i] = m[i % w];
 }
 
-constexpr int kNttMaxT = 12;
+bool tune_valid(const Tune& t) {
+  const bool threads_ok = t.ntt_threads == 128 || t.ntt_threads == 256 || t.ntt_threads == 512;
+  const bool top_ok = t.top_nodes >= 64 && t.top_nodes <= 4096 && (t.top_nodes & (t.top_nodes - 1)) == 0;
+  return threads_ok && t.ntt_max_T >= 6 && t.ntt_max_T <= kNttMaxT && top_ok && t.tail_log >= 1 &&
+         t.tail_log <= kTailMaxLeavesLog;
+}
 
 cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t width, const TwiddleView* tw,
-                          cudaStream_t st, uint4* leaves, uint4* pair_leaves) {
+                          cudaStream_t st, uint4* leaves, uint4* pair_leaves, const Tune& tune) {
   if (width == 0 || width > 65535 || (width != 1 && (leaves || pair_leaves))) return cudaErrorInvalidValue;
+  if (!tune_valid(tune)) return cudaErrorInvalidValue;
   const size_t c = (size_t)1 << log2_c;
   if (n == 0) {
     replicate_kernel<<<1, 128, 0, st>>>(m, cw, c, width);
@@ -165,7 +172,15 @@ cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t w
                          (int)(sizeof(uint4) << kNttMaxT));
     attr_set = true;
   }
-  const int passes = (n + kNttMaxT - 1) / kNttMaxT;
+  // Fewest passes whose tiles fit 2^ntt_max_T, then more (smaller tiles) while
+  // a pass would have fewer blocks than SMs and tiles stay >= 2^5.
+  int passes = (n + tune.ntt_max_T - 1) / tune.ntt_max_T;
+  while (passes < n) {
+    const int T = (n + passes - 1) / passes;
+    const int T_next = (n + passes) / (passes + 1);
+    if ((c << (n - T)) >= (size_t)num_sms() || T_next < 5) break;
+    ++passes;
+  }
   int top = n;
   for (int pidx = 0; pidx < passes; ++pidx) {
     const int remaining = passes - pidx;
@@ -180,10 +195,12 @@ cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t w
     p.leaves = last ? leaves : nullptr;
     p.pair_leaves = last ? pair_leaves : nullptr;
     const dim3 grid((unsigned)(c << (n - T)), (unsigned)width);
+    // one butterfly per thread and layer at most: 2^(T-1) threads, >= one warp
+    const int threads = std::max(32, std::min(tune.ntt_threads, 1 << (T - 1)));
     if (p.leaves)
-      ntt_pass_kernel<true><<<grid, 256, sizeof(uint4) << T, st>>>(m, cw, p, tw);
+      ntt_pass_kernel<true><<<grid, threads, sizeof(uint4) << T, st>>>(m, cw, p, tw);
     else
-      ntt_pass_kernel<false><<<grid, 256, sizeof(uint4) << T, st>>>(m, cw, p, tw);
+      ntt_pass_kernel<false><<<grid, threads, sizeof(uint4) << T, st>>>(m, cw, p, tw);
     COUNT_LAUNCH();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -301,11 +318,9 @@ cudaError_t launch_leaves_pair(const uint4* pi, uint4* leaves, size_t n, cudaStr
   return cudaGetLastError();
 }
 
-constexpr size_t kTopNodes = 512;
-
-cudaError_t launch_tree(uint4* leaves, size_t n, cudaStream_t st, uint4* root_out) {
+cudaError_t launch_tree(uint4* leaves, size_t n, cudaStream_t st, uint4* root_out, size_t top_nodes) {
   uint4* cur = leaves;
-  while (n > kTopNodes) {
+  while (n > top_nodes) {
     const size_t h = n >> 1;
     uint4* nxt = cur + 2 * n;
     level_kernel<<<grid_for(h, 128, 16), 128, 0, st>>>(cur, nxt, h);
@@ -319,6 +334,27 @@ cudaError_t launch_tree(uint4* leaves, size_t n, cudaStream_t st, uint4* root_ou
     tree_top_kernel<<<1, 256, 0, st>>>(cur, n, root_out);
     COUNT_LAUNCH();
   }
+  return cudaGetLastError();
+}
+
+__device__ __forceinline__ uint64_t splitmix64(uint64_t& x) {
+  uint64_t z = (x += 0x9e3779b97f4a7c15ull);
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+__global__ void fill_random_kernel(uint4* out, size_t n, uint64_t seed) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    uint64_t x = seed ^ (i * 0xd1342543de82ef95ull);
+    const uint64_t a = splitmix64(x), b = splitmix64(x);
+    out[i] = make_uint4((uint32_t)a, (uint32_t)(a >> 32), (uint32_t)b, (uint32_t)(b >> 32));
+  }
+}
+
+cudaError_t launch_fill_random(uint4* out, size_t n, uint64_t seed, cudaStream_t st) {
+  fill_random_kernel<<<grid_for(n, 256), 256, 0, st>>>(out, n, seed);
+  COUNT_LAUNCH();
   return cudaGetLastError();
 }
 

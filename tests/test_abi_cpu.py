@@ -96,3 +96,26 @@ def test_gpu_entry_points_refuse_verifier_only_object(built_lib):
         raise AssertionError("commit ran without a device")
     except bg.BasefoldGpuError as e:
         assert e.code == -1
+
+
+def test_launch_shape_validation(built_lib):
+    """bf_pcs_set_tune accepts only the documented ranges; the autotuner
+    needs a device."""
+    bg = built_lib
+    pcs = _setup_verifier(bg, 4, 1)
+    assert pcs.tune == dict(ntt_threads=256, ntt_max_T=12, top_nodes=512, tail_log=8)
+    pcs.tune = dict(ntt_threads=512, tail_log=3)
+    assert pcs.tune == dict(ntt_threads=512, ntt_max_T=12, top_nodes=512, tail_log=3)
+    for bad in (dict(ntt_threads=96), dict(ntt_max_T=13), dict(ntt_max_T=5), dict(top_nodes=100),
+                dict(top_nodes=8192), dict(tail_log=0), dict(tail_log=12)):
+        try:
+            pcs.tune = bad
+            raise AssertionError(f"accepted {bad}")
+        except bg.BasefoldGpuError as e:
+            assert e.code == -1
+    assert pcs.tune["ntt_threads"] == 512
+    try:
+        pcs.autotune(1)
+        raise AssertionError("autotune ran without a device")
+    except bg.BasefoldGpuError as e:
+        assert e.code == -1
