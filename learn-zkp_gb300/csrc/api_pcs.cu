@@ -7,6 +7,8 @@
 // the host.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -303,10 +305,19 @@ int eval_enqueue(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, uint4
       else
         CU(bf::launch_fix_column(data, w, col, scratch, (size_t)1 << (d - 1), r, st));
     }
-    for (int k = d - 2; k >= 0; --k) {
+    // large levels one launch each; the last (<= kEvalTailMaxVars) in one block
+    const int tail = std::min(d - 1, bf::kEvalTailMaxVars);
+    for (int k = d - 2; k >= tail; --k) {
       std::memcpy(&r, point + 16 * k, 16);
       ProfScope ps(p->prof, st, P_FIX);
       CU(bf::launch_fix(scratch, scratch, (size_t)1 << k, r, nullptr, 0, nullptr, st));
+    }
+    if (tail > 0) {
+      bf::EvalTail et{};
+      et.nvars = tail;
+      for (int k = 0; k < tail; ++k) std::memcpy(&et.r[k], point + 16 * k, 16);
+      ProfScope ps(p->prof, st, P_FIX);
+      CU(bf::launch_eval_tail(scratch, et, st));
     }
     CU(cudaMemcpyAsync(value_pin + 16 * col, scratch, 16, cudaMemcpyDeviceToHost, st));
   }

@@ -64,6 +64,15 @@ cudaError_t launch_fix_column(const uint4* in, size_t width, size_t col, uint4* 
                               cudaStream_t st);
 cudaError_t launch_combine_rows(const uint4* rows, size_t nrows, size_t width, const uint4* scalars, uint4* out,
                                 cudaStream_t st);
+// The last `nvars` (<= kEvalTailMaxVars) fixes of MultiPoly::evaluate in one
+// block, in place on buf[0 .. 2^nvars): variable k is fixed with r[k], top
+// first; the value lands in buf[0].
+constexpr int kEvalTailMaxVars = 12;
+struct EvalTail {
+  uint4 r[kEvalTailMaxVars];
+  int nvars;
+};
+cudaError_t launch_eval_tail(uint4* buf, const EvalTail& p, cudaStream_t st);
 
 // Gather of the query openings, written in the proof's bincode layout.
 struct GatherParams {

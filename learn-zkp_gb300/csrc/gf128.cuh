@@ -60,14 +60,10 @@ __device__ __forceinline__ void clmul64(uint64_t a, uint64_t b, uint64_t& lo, ui
   hi = p2 ^ (p1 >> 32);
 }
 
-// Montgomery product a*b*x^-128 mod P.
-__device__ __forceinline__ uint4 gf_mul(uint4 a, uint4 b) {
-  const uint64_t a0 = ((uint64_t)a.y << 32) | a.x, a1 = ((uint64_t)a.w << 32) | a.z;
-  const uint64_t b0 = ((uint64_t)b.y << 32) | b.x, b1 = ((uint64_t)b.w << 32) | b.z;
-  uint64_t l0, l1, h0, h1, m0, m1;
-  clmul64(a0, b0, l0, l1);
-  clmul64(a1, b1, h0, h1);
-  clmul64(a0 ^ a1, b0 ^ b1, m0, m1);
+// Montgomery reduction of the 256-bit carry-less product given as three
+// 128-bit Karatsuba parts: low = a0 b0, high = a1 b1, mid = (a0+a1)(b0+b1).
+__device__ __forceinline__ uint4 gf_karatsuba_reduce(uint64_t l0, uint64_t l1, uint64_t h0, uint64_t h1,
+                                                     uint64_t m0, uint64_t m1) {
   m0 ^= l0 ^ h0;
   m1 ^= l1 ^ h1;
   const uint64_t c0 = l0;
@@ -81,6 +77,74 @@ __device__ __forceinline__ uint4 gf_mul(uint4 a, uint4 b) {
   c2 ^= (c1 << 63) ^ (c1 << 62) ^ (c1 << 57);
   c3 ^= c1 ^ (c1 >> 1) ^ (c1 >> 2) ^ (c1 >> 7);
   return make_uint4((uint32_t)c2, (uint32_t)(c2 >> 32), (uint32_t)c3, (uint32_t)(c3 >> 32));
+}
+
+// Montgomery product a*b*x^-128 mod P.
+__device__ __forceinline__ uint4 gf_mul(uint4 a, uint4 b) {
+  const uint64_t a0 = ((uint64_t)a.y << 32) | a.x, a1 = ((uint64_t)a.w << 32) | a.z;
+  const uint64_t b0 = ((uint64_t)b.y << 32) | b.x, b1 = ((uint64_t)b.w << 32) | b.z;
+  uint64_t l0, l1, h0, h1, m0, m1;
+  clmul64(a0, b0, l0, l1);
+  clmul64(a1, b1, h0, h1);
+  clmul64(a0 ^ a1, b0 ^ b1, m0, m1);
+  return gf_karatsuba_reduce(l0, l1, h0, h1, m0, m1);
+}
+
+// The 32x32 carry-less product number j (0..8) of gf_mul's Karatsuba tree:
+// 64-bit pair t = j / 3 (low, high, sum halves), 32-bit pair u = j % 3.
+__device__ __forceinline__ uint64_t gf_mul_part(uint4 a, uint4 b, int j) {
+  const int t = j / 3, u = j % 3;
+  const uint32_t ax = t == 0 ? a.x : t == 1 ? a.z : a.x ^ a.z;
+  const uint32_t ay = t == 0 ? a.y : t == 1 ? a.w : a.y ^ a.w;
+  const uint32_t bx = t == 0 ? b.x : t == 1 ? b.z : b.x ^ b.z;
+  const uint32_t by = t == 0 ? b.y : t == 1 ? b.w : b.y ^ b.w;
+  const uint32_t x = u == 0 ? ax : u == 1 ? ay : ax ^ ay;
+  const uint32_t y = u == 0 ? bx : u == 1 ? by : bx ^ by;
+  return clmul32(x, y);
+}
+
+// Combines the nine parts (as gf_mul's clmul64 calls do) and reduces.
+__device__ __forceinline__ uint4 gf_mul_combine(const uint64_t q[9]) {
+  uint64_t lo[3], hi[3];
+#pragma unroll
+  for (int t = 0; t < 3; ++t) {
+    const uint64_t p0 = q[3 * t], p2 = q[3 * t + 1], p1 = q[3 * t + 2] ^ p0 ^ p2;
+    lo[t] = p0 ^ (p1 << 32);
+    hi[t] = p2 ^ (p1 >> 32);
+  }
+  return gf_karatsuba_reduce(lo[0], hi[0], lo[1], hi[1], lo[2], hi[2]);
+}
+
+__device__ __forceinline__ uint64_t shfl64(uint64_t v, int src) {
+  const uint32_t lo = __shfl_sync(0xffffffffu, (uint32_t)v, src);
+  const uint32_t hi = __shfl_sync(0xffffffffu, (uint32_t)(v >> 32), src);
+  return ((uint64_t)hi << 32) | lo;
+}
+
+// Two products a1*b1 and a2*b2 by one warp, for latency-bound scalar work:
+// lanes 0..8 and 9..17 each take one 32x32 part, every lane gathers the
+// parts and combines them, so the results are the same in all lanes.  The
+// operands must be the same in all lanes.  All 32 lanes call this.
+__device__ __forceinline__ void gf_mul_warp2(uint4 a1, uint4 b1, uint4 a2, uint4 b2, uint4& r1, uint4& r2) {
+  const int lane = threadIdx.x & 31;
+  const bool second = lane >= 9;
+  const int j = second ? lane - 9 : lane;
+  uint64_t part = 0;
+  if (lane < 18) part = gf_mul_part(second ? a2 : a1, second ? b2 : b1, j);
+  uint64_t q1[9], q2[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    q1[k] = shfl64(part, k);
+    q2[k] = shfl64(part, 9 + k);
+  }
+  r1 = gf_mul_combine(q1);
+  r2 = gf_mul_combine(q2);
+}
+
+__device__ __forceinline__ uint4 gf_mul_warp(uint4 a, uint4 b) {
+  uint4 r, unused;
+  gf_mul_warp2(a, b, a, b, r, unused);
+  return r;
 }
 
 // XOR-reduce four words across a warp.

@@ -524,6 +524,27 @@ cudaError_t launch_fix_column(const uint4* in, size_t width, size_t col, uint4* 
   return cudaGetLastError();
 }
 
+__global__ void __launch_bounds__(512) eval_tail_kernel(uint4* buf, EvalTail p) {
+  for (int k = p.nvars - 1; k >= 0; --k) {
+    const uint32_t half = 1u << k;
+    const uint4 r = p.r[k];
+    // in place: thread b writes buf[b] (b < half) and reads buf[b], buf[b + half]
+    for (uint32_t b = threadIdx.x; b < half; b += blockDim.x) {
+      const uint4 lo = buf[b], hi = buf[b + half];
+      buf[b] = gf_add(lo, gf_mul(r, gf_add(hi, lo)));
+    }
+    __syncthreads();
+  }
+}
+
+cudaError_t launch_eval_tail(uint4* buf, const EvalTail& p, cudaStream_t st) {
+  if (p.nvars < 0 || p.nvars > kEvalTailMaxVars) return cudaErrorInvalidValue;
+  if (p.nvars == 0) return cudaSuccess;
+  eval_tail_kernel<<<1, 512, 0, st>>>(buf, p);
+  COUNT_LAUNCH();
+  return cudaGetLastError();
+}
+
 // out[row] = sum_c scalars[c] * rows[row * width + c]   (basefold.rs:166-183)
 __global__ void combine_rows_kernel(const uint4* __restrict__ rows, size_t nrows, size_t width,
                                     const uint4* __restrict__ scalars, uint4* __restrict__ out) {

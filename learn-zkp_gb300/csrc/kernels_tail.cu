@@ -141,16 +141,20 @@ __device__ uint4 warp_sample_elem(const WarpKeccak& wk, OpenState& o) {
 // round, so it is not carried.
 __device__ void round_step(const WarpKeccak& wk, OpenState& o, int i, int d, const uint4* scal, uint4 root_lo,
                            uint4 root_hi, uint4 S, uint4* rec) {
-  uint4 c0, c1, one_r;
+  // Every lane computes the same scalars; the products are spread over the
+  // warp (gf_mul_warp2), two independent ones at a time.
+  const uint4 ONE = one_dev();
+  const uint4 r = scal[3 * i], r_inv = scal[3 * i + 1], corr = scal[3 * i + 2];
+  const uint4 claim = (i == d - 1) ? o.outer : o.inner;
+  const uint4 delta = o.delta;
+  const uint4 one_r = gf_add(ONE, r);
+  uint4 c0, d0, t, rp0, c1, rp2;
+  gf_mul_warp2(corr, S, delta, one_r, c0, d0);  // c0 = corr * S; d0 = delta (1 + r)
+  gf_mul_warp2(one_r, c0, c0, d0, t, rp0);      // rp0 = c0 d0
+  c1 = gf_add(gf_mul_warp(gf_add(claim, t), r_inv), c0);
+  rp2 = gf_mul_warp(c1, delta);
+  __syncwarp();
   if (wk.lane == 0) {
-    const uint4 ONE = one_dev();
-    const uint4 r = scal[3 * i], r_inv = scal[3 * i + 1], corr = scal[3 * i + 2];
-    const uint4 claim = (i == d - 1) ? o.outer : o.inner;
-    c0 = gf_mul(corr, S);
-    one_r = gf_add(ONE, r);
-    c1 = gf_add(gf_mul(gf_add(claim, gf_mul(one_r, c0)), r_inv), c0);
-    const uint4 rp0 = gf_mul(c0, gf_mul(o.delta, one_r));
-    const uint4 rp2 = gf_mul(c1, o.delta);
     rec[0] = root_lo;
     rec[1] = root_hi;
     rec[2] = rp0;
@@ -158,10 +162,16 @@ __device__ void round_step(const WarpKeccak& wk, OpenState& o, int i, int d, con
     const uint4 m[4] = {root_lo, root_hi, rp0, rp2};
     tr_observe(o, m);  // root (basefold.rs:356), then [c0, c2] (sumcheck/src/lib.rs:97)
   }
-  const uint4 x = warp_sample_elem(wk, o);
+  uint4 x = warp_sample_elem(wk, o);  // valid on lane 0
+  x.x = __shfl_sync(0xffffffffu, x.x, 0);
+  x.y = __shfl_sync(0xffffffffu, x.y, 0);
+  x.z = __shfl_sync(0xffffffffu, x.z, 0);
+  x.w = __shfl_sync(0xffffffffu, x.w, 0);
+  uint4 c1x, delta_next;
+  gf_mul_warp2(c1, x, delta, gf_add(one_r, x), c1x, delta_next);
   if (wk.lane == 0) {
-    o.inner = gf_add(gf_mul(c1, x), c0);  // EvalProver::fix_last_var (eval.rs:108-111)
-    o.delta = gf_mul(o.delta, gf_add(one_r, x));
+    o.inner = gf_add(c1x, c0);  // EvalProver::fix_last_var (eval.rs:108-111)
+    o.delta = delta_next;
     o.x = x;
   }
   __syncwarp();
