@@ -176,6 +176,13 @@ int bf_pcs_set_tune(bf_pcs* pcs, const int* vals, int n);
  * time on the CPU.)
  * bf_engine_autotune: reps > 0 autotunes (bf_pcs_autotune) each size the
  *   first time a job of that size is admitted; 0 (default) keeps defaults.
+ * bf_engine_graphs (default on): each slot keeps, per job size, fixed
+ *   buffers and one captured CUDA graph of the commit, evaluation and
+ *   device-transcript open; a job then costs a staging write, one copy of
+ *   its evaluations and one graph launch.  Idle slots' buffers count toward
+ *   mem_budget and are dropped when a job of another size needs the room.
+ *   Off: every job enqueues its kernels one by one on pool memory.  Call
+ *   only while no job is in flight.
  * bf_engine_prove: runs `count` jobs to completion on the calling thread.
  * bf_engine_start/stop + submit/poll: serving from a background thread;
  *   submitted bf_job structs must stay valid until returned by poll. */
@@ -188,6 +195,12 @@ int bf_engine_stop(bf_engine* e);
 int bf_engine_submit(bf_engine* e, bf_job* job, int device_input);
 int bf_engine_poll(bf_engine* e, bf_job** done, size_t cap, size_t* n);
 int bf_engine_autotune(bf_engine* e, int reps);
+int bf_engine_graphs(bf_engine* e, int on);
+/* Host-side accounting since creation: out = {ms spent admitting jobs
+ * (allocation, capture, staging, enqueue), of which ms in graph launches,
+ * ms completing jobs (query sampling, proof readout), plans built, plans
+ * dropped, jobs done}. */
+int bf_engine_stats(bf_engine* e, double* out, int n);
 
 /* ---- Evaluation that allocates nothing.  No counterpart in the reference.
  * Same value as bf_eval (MultiPoly::evaluate of 2^num_vars evaluations at

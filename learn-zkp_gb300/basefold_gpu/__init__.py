@@ -405,13 +405,14 @@ class Engine:
     requests from a background thread (continuous batching)."""
 
     def __init__(self, device: int = 0, lambda_: int = 128, log2_c: int = 1, max_inflight: int = 16,
-                 mem_budget: int = 0, autotune_reps: int = 0):
+                 mem_budget: int = 0, autotune_reps: int = 0, graphs: bool = True):
         h = C.c_void_p()
         check(lib().bf_engine_create(device, lambda_, log2_c, max_inflight, mem_budget, C.byref(h)))
         self._h, self.log2_c = h, log2_c
         self._keep = {}
         if autotune_reps:
             check(lib().bf_engine_autotune(h, autotune_reps))
+        check(lib().bf_engine_graphs(h, 1 if graphs else 0))
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -424,6 +425,14 @@ class Engine:
 
     def proof_size(self, num_vars: int) -> int:
         return int(lib().bf_engine_proof_size(self._h, num_vars))
+
+    def stats(self) -> dict:
+        """Host-side accounting (bf_engine_stats)."""
+        v = (C.c_double * 6)()
+        check(lib().bf_engine_stats(self._h, v, 6))
+        keys = ["host_ms_enqueue", "host_ms_graph_launch", "host_ms_complete", "plans_built", "plans_dropped",
+                "jobs_done"]
+        return dict(zip(keys, list(v)))
 
     def _job(self, num_vars, evals, point, device_input):
         job = BfJob()

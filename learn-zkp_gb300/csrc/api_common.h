@@ -160,17 +160,30 @@ std::vector<u128> sample_scalars_by_eq(size_t n, bfh::Challenger& ch);
 struct bf_pcs;
 struct bf_commitment;
 namespace bfapi {
+int commit_alloc(bf_pcs* p, bf_commitment* cm, cudaStream_t st);
 int commit_enqueue(bf_pcs* p, bf_commitment* cm, const uint4* data, cudaStream_t st, uint8_t* roots_pin);
 // The value lands in value_pin; *value_dev (when given) receives where it
-// lives on the device.
+// lives on the device.  With point_dev the coordinates are read from device
+// memory at run time (for graph capture), else taken from the host `point`.
 int eval_enqueue(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, uint4* scratch, cudaStream_t st,
-                 uint8_t* value_pin, const uint4** value_dev = nullptr);
+                 uint8_t* value_pin, const uint4** value_dev = nullptr, const uint4* point_dev = nullptr);
 }  // namespace bfapi
 
 struct bf_open_session;
 namespace bfapi {
 int open_start_impl(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, const uint8_t* values,
                     const uint8_t* scalars, void* stream, bf_open_session** out);
+// The pieces of open_start_impl / open_resident_enqueue, for graph capture:
+// host-side preparation (pinned staging) apart from the device work.
+int open_session_create(bf_pcs* p, const bf_commitment* cm, void* stream, bf_open_session** out);
+int open_session_prepare(bf_open_session* s, const uint8_t* point, const uint8_t* values, const uint8_t* scalars);
+int open_session_enqueue_start(bf_open_session* s);
+const uint4* open_session_point_dev(const bf_open_session* s);
+void open_session_mark_launched(bf_open_session* s);  // the resident open was launched by a graph
+cudaStream_t open_session_stream(const bf_open_session* s);
+cudaEvent_t open_session_event(const bf_open_session* s);
+int open_resident_prepare(bf_open_session* s, const bfh::Challenger& ch);
+int open_resident_enqueue_device(bf_open_session* s, const uint4* root_dev, const uint4* value_dev);
 int open_resident_enqueue(bf_open_session* s, const bfh::Challenger& ch, const uint4* root_dev,
                           const uint4* value_dev);
 int open_resident_complete(bf_open_session* s, bfh::Challenger& ch);

@@ -37,8 +37,30 @@ double now_ms() {
 
 enum JobState { J_OPEN = 0, J_GATHER = 1, J_DONE = 2 };
 
+// One size's job captured on one slot: fixed buffers (evaluations,
+// codeword, trees, open workspace) and the CUDA graph that runs commit,
+// evaluation and the device-transcript open on them.  A job of that size on
+// that slot writes its point into the staging, copies its evaluations in and
+// replays the graph.
+struct Plan {
+  int n = -1;
+  bf_pcs* p = nullptr;
+  std::unique_ptr<bf_commitment> cm;
+  DevBuf eval_ws;
+  bf_open_session* sess = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  long long launches = 0;  // kernels per replay
+  size_t footprint = 0;
+  uint64_t last_use = 0;   // admission counter value of its last job (LRU eviction)
+  ~Plan() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (sess) bf_open_session_free(sess);
+  }
+};
+
 struct Job {
   bf_job* pub = nullptr;
+  Plan* plan = nullptr;  // graph replay: the session and buffers belong to the plan
   bool device_input = false;
   double t_submit = 0;
   bf_pcs* pcs = nullptr;
@@ -57,6 +79,12 @@ struct Job {
 struct bf_engine {
   int device = 0, lambda = 128, log2_c = 1, max_inflight = 8;
   int autotune_reps = 0;  // > 0: autotune each size's pcs when it is created
+  bool use_graphs = true;  // replay one captured graph per (slot, size)
+  std::vector<std::map<int, std::unique_ptr<Plan>>> plans;  // per slot, by size
+  uint64_t admissions = 0;
+  // host-side accounting (bf_engine_stats)
+  double host_ms_enqueue = 0, host_ms_launch = 0, host_ms_complete = 0;
+  uint64_t plans_built = 0, plans_dropped = 0, jobs_done = 0;
   size_t mem_budget = 0, mem_used = 0;
   std::map<int, bf_pcs*> pcs_by_n;
   std::vector<cudaStream_t> streams;
@@ -100,6 +128,18 @@ int get_pcs(bf_engine* e, int n, bf_pcs** out) {
 void finish_job(bf_engine* e, Job* j, int status) {
   j->pub->status = status;
   j->pub->latency_ms = now_ms() - j->t_submit;
+  if (j->plan) {
+    if (status == BF_ERR_CUDA && j->slot >= 0) {  // a failed replay: rebuild the plan next time
+      auto& m = e->plans[j->slot];
+      auto it = m.find(j->plan->n);
+      if (it != m.end()) {
+        e->mem_used -= it->second->footprint;
+        m.erase(it);
+      }
+    }
+    j->sess = nullptr;
+    j->plan = nullptr;
+  }
   if (j->sess) {
     bf_open_session_free(j->sess);
     j->sess = nullptr;
@@ -150,6 +190,84 @@ int admit(bf_engine* e, Job* j) {
   return BF_OK;
 }
 
+// Enqueues one job's GPU work on the plan's buffers (captured once).
+int capture_job(bf_engine* e, int slot, Plan* pl) {
+  bf_pcs* p = pl->p;
+  bf_commitment* cm = pl->cm.get();
+  cudaStream_t st = e->streams[slot];
+  uint8_t* pin = slot_pin(e, slot);
+  TRY(open_session_enqueue_start(pl->sess));  // copies the point first: the evaluation reads it
+  TRY(commit_enqueue(p, cm, cm->data.as<uint4>(), st, pin));
+  const uint4* value_dev = nullptr;
+  TRY(eval_enqueue(p, cm, nullptr, pl->eval_ws.as<uint4>(), st, pin + 64, &value_dev,
+                   open_session_point_dev(pl->sess)));
+  const uint4* root_dev = cm->tree.as<uint4>() + 2 * (2 * p->n_d() - 2);
+  TRY(open_resident_enqueue_device(pl->sess, root_dev, value_dev));
+  return BF_OK;
+}
+
+int build_plan(bf_engine* e, int slot, int n, std::unique_ptr<Plan>& out) {
+  std::unique_ptr<Plan> pl(new Plan());
+  pl->n = n;
+  TRY(get_pcs(e, n, &pl->p));
+  bf_pcs* p = pl->p;
+  cudaStream_t st = e->streams[slot];
+  pl->cm.reset(new bf_commitment());
+  pl->cm->pcs = p;
+  pl->cm->width = 1;
+  CU(pl->cm->data.alloc_async(16 * ((size_t)1 << n), p->pool, st));
+  TRY(commit_alloc(p, pl->cm.get(), st));
+  CU(pl->eval_ws.alloc_async(16 * (n > 0 ? ((size_t)1 << (n - 1)) : 1), p->pool, st));
+  TRY(open_session_create(p, pl->cm.get(), st, &pl->sess));
+  const long long before = (long long)bf::launches_total();
+  cudaGraph_t graph = nullptr;
+  CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  const int rc = capture_job(e, slot, pl.get());
+  const cudaError_t ce = cudaStreamEndCapture(st, &graph);
+  pl->launches = (long long)bf::launches_total() - before;
+  bf::add_launches(-pl->launches);  // captured, not run
+  if (rc < 0) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  CU(ce);
+  const cudaError_t ie = cudaGraphInstantiate(&pl->exec, graph, 0);
+  cudaGraphDestroy(graph);
+  CU(ie);
+  const size_t Q = p->Q;
+  pl->footprint = job_footprint(n, e->log2_c, false, Q, p->block_bytes(1));
+  out = std::move(pl);
+  return BF_OK;
+}
+
+// Graph replay of a job on its slot's plan for its size (built by progress()).
+int admit_graph(bf_engine* e, Job* j) {
+  bf_job* pj = j->pub;
+  Plan* pl = e->plans[j->slot][pj->num_vars].get();
+  pl->last_use = ++e->admissions;
+  j->plan = pl;
+  j->pcs = pl->p;
+  j->st = e->streams[j->slot];
+  j->sess = pl->sess;
+  const size_t need = bf_pcs_proof_size(pl->p, 1, 1);
+  if (pj->proof_cap < need) return fail(BF_ERR_BUFFER, "job proof buffer needs %zu bytes", need);
+  if (j->device_input && (reinterpret_cast<uintptr_t>(pj->evals) & 15))
+    return fail(BF_ERR_ARG, "device evaluations must be 16-byte aligned");
+  TRY(open_session_prepare(pl->sess, pj->point, nullptr, nullptr));
+  j->ch = bfh::Challenger();  // GenericChallenger::keccak256()
+  TRY(open_resident_prepare(pl->sess, j->ch));
+  CU(cudaMemcpyAsync(pl->cm->data.p, pj->evals, 16 * ((size_t)1 << pl->n),
+                     j->device_input ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, j->st));
+  const double t0 = now_ms();
+  CU(cudaGraphLaunch(pl->exec, j->st));
+  e->host_ms_launch += now_ms() - t0;
+  bf::add_launches(pl->launches);
+  CU(cudaEventRecord(open_session_event(pl->sess), j->st));
+  open_session_mark_launched(pl->sess);
+  j->state = J_OPEN;
+  return BF_OK;
+}
+
 // Advances a job whose GPU work has completed.  Returns 1 if it moved.
 int step(bf_engine* e, Job* j) {
   bf_pcs* p = j->pcs;
@@ -181,28 +299,89 @@ bool progress(bf_engine* e) {
   bool moved = false;
   while (true) {
     Job* j = nullptr;
+    int slot = -1;
     {
       std::lock_guard<std::mutex> lk(e->mu);
       if (e->queue.empty() || e->free_slots.empty()) break;
       Job* cand = e->queue.front();
-      // admission by HBM footprint: always admit when idle so oversized jobs still run
-      if (!e->inflight.empty() && e->mem_used + cand->footprint > e->mem_budget) break;
+      if (e->use_graphs) {
+        // a free slot that has a plan of this size, else the free slot with the
+        // least plan memory; room for a new plan comes from idle plans, least
+        // recently used first (always admit when idle so oversized jobs run)
+        const int n = cand->pub->num_vars;
+        size_t pick = e->free_slots.size();
+        for (size_t k = 0; k < e->free_slots.size() && pick == e->free_slots.size(); ++k)
+          if (e->plans[e->free_slots[k]].count(n)) pick = k;
+        if (pick == e->free_slots.size()) {
+          size_t best = ~(size_t)0;
+          for (size_t k = 0; k < e->free_slots.size(); ++k) {
+            size_t held = 0;
+            for (auto& kv : e->plans[e->free_slots[k]]) held += kv.second->footprint;
+            if (held < best) {
+              best = held;
+              pick = k;
+            }
+          }
+          while (e->mem_used + cand->footprint > e->mem_budget) {
+            Plan* victim = nullptr;
+            int vslot = -1;
+            for (int fs : e->free_slots)
+              for (auto& kv : e->plans[fs])
+                if (!victim || kv.second->last_use < victim->last_use) {
+                  victim = kv.second.get();
+                  vslot = fs;
+                }
+            if (!victim) break;
+            e->mem_used -= victim->footprint;
+            e->plans[vslot].erase(victim->n);
+            e->plans_dropped += 1;
+          }
+          if (!e->inflight.empty() && e->mem_used + cand->footprint > e->mem_budget) break;
+        }
+        slot = e->free_slots[pick];
+        e->free_slots.erase(e->free_slots.begin() + pick);
+      } else {
+        // admission by HBM footprint: always admit when idle so oversized jobs still run
+        if (!e->inflight.empty() && e->mem_used + cand->footprint > e->mem_budget) break;
+        slot = e->free_slots.back();
+        e->free_slots.pop_back();
+      }
       e->queue.pop_front();
       j = cand;
     }
-    j->slot = e->free_slots.back();
-    e->free_slots.pop_back();
-    e->mem_used += j->footprint;
+    j->slot = slot;
     e->inflight.push_back(j);
-    int rc = admit(e, j);
+    int rc = BF_OK;
+    const double t_enq = now_ms();
+    if (e->use_graphs) {
+      j->footprint = 0;  // memory is held by the slot's plan
+      const int n = j->pub->num_vars;
+      if (!e->plans[slot].count(n)) {
+        std::unique_ptr<Plan> pl;
+        rc = build_plan(e, slot, n, pl);
+        if (rc >= 0) {
+          e->mem_used += pl->footprint;
+          e->plans[slot][n] = std::move(pl);
+          e->plans_built += 1;
+        }
+      }
+      if (rc >= 0) rc = admit_graph(e, j);
+    } else {
+      e->mem_used += j->footprint;
+      rc = admit(e, j);
+    }
+    e->host_ms_enqueue += now_ms() - t_enq;
     if (rc < 0) finish_job(e, j, rc);
     moved = true;
   }
   for (Job* j : e->inflight) {
     if (j->state == J_DONE) continue;
+    const double t_step = now_ms();
     int rc = step(e, j);
+    if (rc != 0) e->host_ms_complete += now_ms() - t_step;
     if (rc < 0) finish_job(e, j, rc);
     if (rc != 0) moved = true;
+    if (j->state == J_DONE) e->jobs_done += 1;
   }
   std::vector<Job*> keep;
   for (Job* j : e->inflight) {
@@ -238,6 +417,8 @@ void worker_loop(bf_engine* e) {
 }  // namespace
 
 bf_engine::~bf_engine() {
+  for (cudaStream_t s : streams) cudaStreamSynchronize(s);
+  plans.clear();
   for (auto& kv : pcs_by_n) bf_pcs_free(kv.second);
   for (cudaStream_t s : streams) {
     cudaStreamSynchronize(s);
@@ -270,6 +451,7 @@ int bf_engine_create(int device, int lambda, int log2_c, int max_inflight, size_
     e->free_slots.push_back(max_inflight - 1 - i);
   }
   CU(e->pin.ensure(128 * (size_t)max_inflight));
+  e->plans.resize(max_inflight);
   *out = e.release();
   return BF_OK;
 }
@@ -318,6 +500,31 @@ int bf_engine_submit(bf_engine* e, bf_job* job, int device_input) {
   e->queue.push_back(j);
   e->outstanding += 1;
   e->cv.notify_all();
+  return BF_OK;
+}
+
+int bf_engine_stats(bf_engine* e, double* out, int n) {
+  if (!e || !out || n < 6) return fail(BF_ERR_ARG, "need 6 values");
+  std::lock_guard<std::mutex> lk(e->mu);
+  out[0] = e->host_ms_enqueue;
+  out[1] = e->host_ms_launch;
+  out[2] = e->host_ms_complete;
+  out[3] = (double)e->plans_built;
+  out[4] = (double)e->plans_dropped;
+  out[5] = (double)e->jobs_done;
+  return BF_OK;
+}
+
+int bf_engine_graphs(bf_engine* e, int on) {
+  if (!e) return fail(BF_ERR_ARG, "null argument");
+  if (e->running || !e->inflight.empty()) return fail(BF_ERR_ARG, "engine busy");
+  e->use_graphs = on != 0;
+  if (!e->use_graphs) {
+    for (auto& m : e->plans) {
+      for (auto& kv : m) e->mem_used -= kv.second->footprint;
+      m.clear();
+    }
+  }
   return BF_OK;
 }
 

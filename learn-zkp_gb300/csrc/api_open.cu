@@ -226,22 +226,18 @@ int tail_first_round(const bf_pcs* p, int d) {
   return std::min(d - 1, lim);
 }
 
-// Enqueues every round of `s`, and the final polynomial, with the transcript
-// on the device, starting from `ch`; root_dev / value_dev, when given, are
-// observed first (the commitment root and the evaluation on the device, the
-// value becoming the claim).  Nothing is read back until
-// open_resident_complete.
-int open_resident_enqueue(bf_open_session* s, const bfh::Challenger& ch, const uint4* root_dev,
-                          const uint4* value_dev) {
-  bf_pcs* p = s->p;
+// Host side of a device-transcript open: the per-round scalars and the
+// starting OpenState (transcript `ch`, claim, delta = 1) in the pinned
+// staging.
+int open_resident_prepare(bf_open_session* s, const bfh::Challenger& ch) {
   const int d = s->d;
   if (s->i != d - 1 || s->msg_ready || s->resident_pending)
     return fail(BF_ERR_ARG, "a device-transcript open starts before the first round");
   if (ch.in.size() > (size_t)bf::kTrMax || ch.out.size() > 32)
     return fail(BF_ERR_ARG, "transcript state too large for the device (%zu input bytes)", ch.in.size());
   const size_t n_point = d > 0 ? d : 1;
-  // Inputs go where no copy still in flight reads (bf_open_start's scalar
-  // and point copies): scalars per round, then the OpenState image.
+  // Inputs go where no copy still in flight reads (the start's scalar and
+  // point copies): scalars per round, then the OpenState image.
   uint8_t* in = s->pin->b() + s->tail_in_off();
   for (int i = 0; i < d; ++i) {
     bfh::store(in + 48 * i, s->r[i]);
@@ -257,9 +253,22 @@ int open_resident_enqueue(bf_open_session* s, const bfh::Challenger& ch, const u
   img.outer = to_uint4(s->outer_val);
   img.delta = to_uint4(bfh::one());
   std::memcpy(in + 48 * n_point, &img, sizeof(img));
+  return BF_OK;
+}
+
+// Device side: every round of `s` and the final polynomial with the
+// transcript on the device, from the staging; root_dev / value_dev, when
+// given, are observed first (the commitment root and the evaluation on the
+// device, the value becoming the claim).  Results are copied to the pinned
+// staging; no event is recorded.
+int open_resident_enqueue_device(bf_open_session* s, const uint4* root_dev, const uint4* value_dev) {
+  bf_pcs* p = s->p;
+  const int d = s->d;
+  const size_t n_point = d > 0 ? d : 1;
+  const uint8_t* in = s->pin->b() + s->tail_in_off();
   cudaStream_t st = s->st;
   if (d > 0) CU(cudaMemcpyAsync(s->w_tail, in, 48 * (size_t)d, cudaMemcpyHostToDevice, st));
-  CU(cudaMemcpyAsync(s->w_state, in + 48 * n_point, sizeof(img), cudaMemcpyHostToDevice, st));
+  CU(cudaMemcpyAsync(s->w_state, in + 48 * n_point, sizeof(bf::OpenState), cudaMemcpyHostToDevice, st));
   if (root_dev || value_dev) CU(bf::launch_open_observe(s->w_state, root_dev, value_dev, st));
   const uint4* scal = reinterpret_cast<const uint4*>(s->w_tail);
   const uint4* xp = &s->w_state->x;
@@ -314,7 +323,18 @@ int open_resident_enqueue(bf_open_session* s, const bfh::Challenger& ch, const u
   CU(cudaMemcpyAsync(s->res_pin, s->w_rec, rec_bytes(d), cudaMemcpyDeviceToHost, st));
   CU(cudaMemcpyAsync(s->res_pin + align16(rec_bytes(d)), s->w_state, sizeof(bf::OpenState), cudaMemcpyDeviceToHost,
                      st));
-  CU(cudaEventRecord(s->ev, st));
+  return BF_OK;
+}
+
+// Enqueues every round of `s`, and the final polynomial, with the transcript
+// on the device, starting from `ch` (see open_resident_prepare /
+// open_resident_enqueue_device); nothing is read back until
+// open_resident_complete.
+int open_resident_enqueue(bf_open_session* s, const bfh::Challenger& ch, const uint4* root_dev,
+                          const uint4* value_dev) {
+  TRY(open_resident_prepare(s, ch));
+  TRY(open_resident_enqueue_device(s, root_dev, value_dev));
+  CU(cudaEventRecord(s->ev, s->st));
   s->pending = true;
   s->resident_pending = true;
   s->msg_ready = false;
@@ -438,16 +458,13 @@ int bf_open_start(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, cons
 
 namespace bfapi {
 
-// bf_open_start; `values` may be null when a device-transcript open will
-// observe the evaluation on the device (width 1).
-int open_start_impl(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, const uint8_t* values,
-                    const uint8_t* scalars, void* stream, bf_open_session** out) {
-  if (!p || !cm || !out || (p->d > 0 && !point)) return fail(BF_ERR_ARG, "null argument");
-  if (!values && cm->width != 1) return fail(BF_ERR_ARG, "null argument");
+// A session for `cm` on `stream` with its device workspace and pinned
+// staging; no device work.
+int open_session_create(bf_pcs* p, const bf_commitment* cm, void* stream, bf_open_session** out) {
+  if (!p || !cm || !out) return fail(BF_ERR_ARG, "null argument");
   *out = nullptr;
   if (p->device < 0) return fail(BF_ERR_ARG, "verifier-only pcs (device < 0)");
   if (cm->pcs != p) return fail(BF_ERR_ARG, "commitment belongs to another pcs");
-  if (cm->width > 1 && !scalars) return fail(BF_ERR_ARG, "width > 1 needs the eq scalars");
   DeviceGuard g(p->device);
   std::unique_ptr<bf_open_session> s(new bf_open_session());
   s->p = p;
@@ -455,12 +472,28 @@ int open_start_impl(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, co
   s->w = cm->width;
   s->st = stream ? reinterpret_cast<cudaStream_t>(stream) : p->stream;
   CU(cudaEventCreateWithFlags(&s->ev, cudaEventDisableTiming));
-  const int d = p->d;
+  s->d = p->d;
+  s->i = s->d - 1;
+  TRY(session_alloc(s.get()));
+  *out = s.release();
+  return BF_OK;
+}
+
+// Host side of starting an open at `point`: the round scalars and the claim,
+// the point (and the eq scalars) written to the session's pinned staging,
+// the rounds reset.  `values` may be null when the evaluation will be
+// observed on the device (width 1).
+int open_session_prepare(bf_open_session* s, const uint8_t* point, const uint8_t* values, const uint8_t* scalars) {
+  const int d = s->d;
   const size_t w = s->w;
-  s->d = d;
-  s->i = d - 1;
+  if (d > 0 && !point) return fail(BF_ERR_ARG, "null argument");
+  if (!values && w != 1) return fail(BF_ERR_ARG, "null argument");
+  if (w > 1 && !scalars) return fail(BF_ERR_ARG, "width > 1 needs the eq scalars");
+  if (s->pending) return fail(BF_ERR_ARG, "session busy");
   const u128 ONE = bfh::one();
-  s->r.resize(d);
+  s->i = d - 1;
+  s->msg_ready = s->final_ready = s->resident_pending = s->gather_pending = false;
+  s->r.assign(d, 0);
   for (int k = 0; k < d; ++k) s->r[k] = bfh::load(point + 16 * k);
   if (w == 1) {
     s->outer_val = values ? bfh::load(values) : 0;
@@ -469,6 +502,7 @@ int open_start_impl(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, co
     for (size_t c = 0; c < w; ++c) claim ^= bfh::mul(bfh::load(scalars + 16 * c), bfh::load(values + 16 * c));
     s->outer_val = claim;
   }
+  s->inner_val = 0;
   s->delta_prod = ONE;
   // EvalImpr::new / HalfEq::new (eval_impr.rs:20-27, 69-79)
   if (!bfh::batch_inverse(s->r, s->r_inv)) return fail(BF_ERR_NOT_INVERTIBLE, "point has a zero coordinate");
@@ -478,13 +512,27 @@ int open_start_impl(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, co
   // correcting_factor(i) = prod_{i <= k < d-1} (1 - r_k)^-1 (eval_impr.rs:83-90)
   s->corr.assign(d > 0 ? d : 1, ONE);
   for (int i = d - 2; i >= 0; --i) s->corr[i] = bfh::mul(s->corr[i + 1], omr_inv[i]);
+  s->rounds.clear();
+  s->roots.clear();
   put_u64(s->rounds, (uint64_t)d);
   put_u64(s->roots, (uint64_t)d);
-  TRY(session_alloc(s.get()));
+  uint8_t* pin = s->pin->b();
+  if (w > 1) std::memcpy(pin + 64, scalars, 16 * w);
+  if (d > 0) std::memcpy(pin + 64 + 16 * w, point, 16 * (size_t)d);
+  return BF_OK;
+}
+
+// Device side of the start, from the staging: row combination and the first
+// round's tree (width > 1), the point, the half-eq table and the first
+// round's reduction.  No event is recorded.
+int open_session_enqueue_start(bf_open_session* s) {
+  bf_pcs* p = s->p;
+  const bf_commitment* cm = s->cm;
+  const int d = s->d;
+  const size_t w = s->w;
   uint8_t* pin = s->pin->b();
   cudaStream_t st = s->st;
   if (w > 1) {  // combine rows with the eq scalars (basefold.rs:166-183)
-    std::memcpy(pin + 64, scalars, 16 * w);
     CU(cudaMemcpyAsync(s->w_scalars, pin + 64, 16 * w, cudaMemcpyHostToDevice, st));
     ProfScope ps(p->prof, st, P_FIX);
     CU(bf::launch_combine_rows(cm->cw.as<uint4>(), p->n_d(), w, s->w_scalars, s->w_pi_first, st));
@@ -492,29 +540,55 @@ int open_start_impl(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, co
   }
   if (d == 0) {
     CU(cudaMemcpyAsync(pin, s->first_poly(), 16, cudaMemcpyDeviceToHost, st));
-  } else {
-    if (w > 1) {  // the first round's tree over the combined codeword pairs
-      ProfScope ps(p->prof, st, P_TREE);
-      const size_t n1 = p->n_i(d - 1);
-      CU(bf::launch_leaves_pair(s->w_pi_first, s->w_pi_first_tree, n1, st));
-      CU(bf::launch_tree(s->w_pi_first_tree, n1, st, reinterpret_cast<uint4*>(s->stage(d - 1)), p->tune.top_nodes));
-    }
-    std::memcpy(pin + 64 + 16 * w, point, 16 * (size_t)d);
-    CU(cudaMemcpyAsync(s->w_point, pin + 64 + 16 * w, 16 * (size_t)d, cudaMemcpyHostToDevice, st));
-    CU(cudaMemsetAsync(s->stage(d - 1) + 32, 0, 16, st));
-    if (d >= 2) CU(cudaMemsetAsync(s->w_stage, 0, 48 * (size_t)(d - 1), st));
-    {
-      ProfScope ps(p->prof, st, P_EQ);
-      CU(bf::launch_eq_table(s->w_point, d - 1, s->w_heq, s->w_eq_lo, s->w_eq_hi, st));
-    }
-    {
-      ProfScope ps(p->prof, st, P_FIX);
-      CU(bf::launch_dot_xor(s->w_heq, s->first_poly(), (size_t)1 << (d - 1),
-                            reinterpret_cast<uint32_t*>(s->stage(d - 1) + 32), st));
-    }
-    CU(cudaMemcpyAsync(pin, s->stage(d - 1), 48, cudaMemcpyDeviceToHost, st));
+    return BF_OK;
   }
-  CU(cudaEventRecord(s->ev, st));
+  if (w > 1) {  // the first round's tree over the combined codeword pairs
+    ProfScope ps(p->prof, st, P_TREE);
+    const size_t n1 = p->n_i(d - 1);
+    CU(bf::launch_leaves_pair(s->w_pi_first, s->w_pi_first_tree, n1, st));
+    CU(bf::launch_tree(s->w_pi_first_tree, n1, st, reinterpret_cast<uint4*>(s->stage(d - 1)), p->tune.top_nodes));
+  }
+  CU(cudaMemcpyAsync(s->w_point, pin + 64 + 16 * w, 16 * (size_t)d, cudaMemcpyHostToDevice, st));
+  CU(cudaMemsetAsync(s->stage(d - 1) + 32, 0, 16, st));
+  if (d >= 2) CU(cudaMemsetAsync(s->w_stage, 0, 48 * (size_t)(d - 1), st));
+  {
+    ProfScope ps(p->prof, st, P_EQ);
+    CU(bf::launch_eq_table(s->w_point, d - 1, s->w_heq, s->w_eq_lo, s->w_eq_hi, st));
+  }
+  {
+    ProfScope ps(p->prof, st, P_FIX);
+    CU(bf::launch_dot_xor(s->w_heq, s->first_poly(), (size_t)1 << (d - 1),
+                          reinterpret_cast<uint32_t*>(s->stage(d - 1) + 32), st));
+  }
+  CU(cudaMemcpyAsync(pin, s->stage(d - 1), 48, cudaMemcpyDeviceToHost, st));
+  return BF_OK;
+}
+
+const uint4* open_session_point_dev(const bf_open_session* s) { return s->w_point; }
+
+void open_session_mark_launched(bf_open_session* s) {
+  s->pending = true;
+  s->resident_pending = true;
+}
+
+cudaStream_t open_session_stream(const bf_open_session* s) { return s->st; }
+cudaEvent_t open_session_event(const bf_open_session* s) { return s->ev; }
+
+// bf_open_start; `values` may be null when a device-transcript open will
+// observe the evaluation on the device (width 1).
+int open_start_impl(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, const uint8_t* values,
+                    const uint8_t* scalars, void* stream, bf_open_session** out) {
+  if (!p || !cm || !out || (p->d > 0 && !point)) return fail(BF_ERR_ARG, "null argument");
+  if (!values && cm->width != 1) return fail(BF_ERR_ARG, "null argument");
+  if (cm->width > 1 && !scalars) return fail(BF_ERR_ARG, "width > 1 needs the eq scalars");
+  *out = nullptr;
+  bf_open_session* raw = nullptr;
+  TRY(open_session_create(p, cm, stream, &raw));
+  std::unique_ptr<bf_open_session> s(raw);
+  DeviceGuard g(p->device);
+  TRY(open_session_prepare(s.get(), point, values, scalars));
+  TRY(open_session_enqueue_start(s.get()));
+  CU(cudaEventRecord(s->ev, s->st));
   s->pending = true;
   *out = s.release();
   return BF_OK;

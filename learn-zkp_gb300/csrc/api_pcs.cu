@@ -250,14 +250,23 @@ namespace bfapi {
 // Encode + Merkle commit of `data` (width 1) on stream `st`; the codeword
 // root and the first folded-codeword root are copied to roots_pin[0..64)
 // (pinned) when the stream reaches that point.
+// The codeword and tree buffers of `cm` from the pcs's pool (kept when they
+// are already there, e.g. for a captured graph's fixed buffers).
+int commit_alloc(bf_pcs* p, bf_commitment* cm, cudaStream_t st) {
+  const size_t nd = p->n_d(), w = cm->width;
+  const bool pairs = p->d > 0 && w == 1;
+  if (!cm->cw.p) CU(cm->cw.alloc_async(16 * nd * w, p->pool, st));
+  if (!cm->tree.p) CU(cm->tree.alloc_async(32 * (2 * nd - 1), p->pool, st));
+  if (pairs && !cm->pi_tree.p) CU(cm->pi_tree.alloc_async(32 * (nd - 1), p->pool, st));
+  return BF_OK;
+}
+
 int commit_enqueue(bf_pcs* p, bf_commitment* cm, const uint4* data, cudaStream_t st, uint8_t* roots_pin) {
   const size_t nd = p->n_d(), w = cm->width;
   // For width 1 the first open round commits the codeword itself (as pairs),
   // so that tree is built here; wider data is first combined in open.
   const bool pairs = p->d > 0 && w == 1;
-  CU(cm->cw.alloc_async(16 * nd * w, p->pool, st));
-  CU(cm->tree.alloc_async(32 * (2 * nd - 1), p->pool, st));
-  if (pairs) CU(cm->pi_tree.alloc_async(32 * (nd - 1), p->pool, st));
+  TRY(commit_alloc(p, cm, st));
   uint4* cw = cm->cw.as<uint4>();
   uint4* tree = cm->tree.as<uint4>();
   uint4* pit = cm->pi_tree.as<uint4>();
@@ -286,7 +295,7 @@ int commit_enqueue(bf_pcs* p, bf_commitment* cm, const uint4* data, cudaStream_t
 // last coordinate, repeatedly, in `scratch` (2^(d-1) elements).  The value
 // lands in value_pin[0..16).
 int eval_enqueue(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, uint4* scratch, cudaStream_t st,
-                 uint8_t* value_pin, const uint4** value_dev) {
+                 uint8_t* value_pin, const uint4** value_dev, const uint4* point_dev) {
   const int d = p->d;
   const size_t w = cm->width;
   const uint4* data = cm->data.as<uint4>();
@@ -295,27 +304,32 @@ int eval_enqueue(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, uint4
     CU(cudaMemcpyAsync(value_pin, data, 16 * w, cudaMemcpyDeviceToHost, st));
     return BF_OK;
   }
+  auto coord = [&](int k) {
+    uint4 r{};
+    if (!point_dev) std::memcpy(&r, point + 16 * k, 16);
+    return r;
+  };
+  auto coord_dev = [&](int k) { return point_dev ? point_dev + k : nullptr; };
   for (size_t col = 0; col < w; ++col) {  // one value per column (basefold.rs:126-131)
-    uint4 r;
-    std::memcpy(&r, point + 16 * (d - 1), 16);
     {
       ProfScope ps(p->prof, st, P_FIX);
       if (w == 1)
-        CU(bf::launch_fix(data, scratch, (size_t)1 << (d - 1), r, nullptr, 0, nullptr, st));
+        CU(bf::launch_fix(data, scratch, (size_t)1 << (d - 1), coord(d - 1), nullptr, 0, nullptr, st,
+                          coord_dev(d - 1)));
       else
-        CU(bf::launch_fix_column(data, w, col, scratch, (size_t)1 << (d - 1), r, st));
+        CU(bf::launch_fix_column(data, w, col, scratch, (size_t)1 << (d - 1), coord(d - 1), st, coord_dev(d - 1)));
     }
     // large levels one launch each; the last (<= kEvalTailMaxVars) in one block
     const int tail = std::min(d - 1, bf::kEvalTailMaxVars);
     for (int k = d - 2; k >= tail; --k) {
-      std::memcpy(&r, point + 16 * k, 16);
       ProfScope ps(p->prof, st, P_FIX);
-      CU(bf::launch_fix(scratch, scratch, (size_t)1 << k, r, nullptr, 0, nullptr, st));
+      CU(bf::launch_fix(scratch, scratch, (size_t)1 << k, coord(k), nullptr, 0, nullptr, st, coord_dev(k)));
     }
     if (tail > 0) {
       bf::EvalTail et{};
       et.nvars = tail;
-      for (int k = 0; k < tail; ++k) std::memcpy(&et.r[k], point + 16 * k, 16);
+      et.rp = point_dev;
+      for (int k = 0; k < tail; ++k) et.r[k] = coord(k);
       ProfScope ps(p->prof, st, P_FIX);
       CU(bf::launch_eval_tail(scratch, et, st));
     }
@@ -391,6 +405,7 @@ int bf_pcs_setup(int device, int lambda, int log2_c, int num_vars, void* stream,
     p->own_stream = true;
   }
   TRY(build_twiddles(p.get()));
+  bf::init_kernel_attributes();
   CU(p->pinned.ensure(4096));
   {
     cudaMemPoolProps props{};

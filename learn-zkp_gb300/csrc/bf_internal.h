@@ -61,15 +61,17 @@ cudaError_t launch_fold_leaves(const uint4* pi, uint4* out, uint4* leaves, size_
 cudaError_t launch_fix(const uint4* in, uint4* out, size_t half, uint4 r, const uint4* heq, size_t next_half,
                        uint32_t* acc, cudaStream_t st, const uint4* xp = nullptr);
 cudaError_t launch_fix_column(const uint4* in, size_t width, size_t col, uint4* out, size_t half, uint4 r,
-                              cudaStream_t st);
+                              cudaStream_t st, const uint4* xp = nullptr);
 cudaError_t launch_combine_rows(const uint4* rows, size_t nrows, size_t width, const uint4* scalars, uint4* out,
                                 cudaStream_t st);
 // The last `nvars` (<= kEvalTailMaxVars) fixes of MultiPoly::evaluate in one
-// block, in place on buf[0 .. 2^nvars): variable k is fixed with r[k], top
-// first; the value lands in buf[0].
+// block, in place on buf[0 .. 2^nvars): variable k is fixed with r[k] (or
+// rp[k] in device memory when rp is not null), top first; the value lands in
+// buf[0].
 constexpr int kEvalTailMaxVars = 12;
 struct EvalTail {
   uint4 r[kEvalTailMaxVars];
+  const uint4* rp;
   int nvars;
 };
 cudaError_t launch_eval_tail(uint4* buf, const EvalTail& p, cudaStream_t st);
@@ -100,6 +102,10 @@ cudaError_t launch_prod_fix(uint4* const* out, const uint4* const* in, int k, si
 
 unsigned long long launches_total();
 void count_launch();
+void add_launches(long long n);  // kernels run by a replayed CUDA graph (negative: captured, not run)
+// Function attributes (dynamic shared memory) set once per device, outside
+// any stream capture.
+void init_kernel_attributes();
 
 // ---- Fiat-Shamir on the device
 // HashChallenger<u8, Keccak256Hash, 32> (p3/src/challenger.rs) as bytes: the

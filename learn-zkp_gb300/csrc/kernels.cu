@@ -36,6 +36,7 @@ __device__ __forceinline__ uint4 gf_one() { return make_uint4(1u, 0u, 0u, 0xc200
 static std::atomic<unsigned long long> g_launches{0};
 unsigned long long launches_total() { return g_launches.load(); }
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void add_launches(long long n) { g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed); }
 #define COUNT_LAUNCH() g_launches.fetch_add(1, std::memory_order_relaxed)
 
 static int g_num_sms = 0;
@@ -147,6 +148,19 @@ __global__ void replicate_kernel(const uint4* __restrict__ m, uint4* __restrict_
   for (size_t i = threadIdx.x; i < c * w; i += blockDim.x) cw[i] = m[i % w];
 }
 
+void init_kernel_attributes() {
+  static std::atomic<uint64_t> done{0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const uint64_t bit = 1ull << (dev & 63);
+  if (done.load() & bit) return;
+  cudaFuncSetAttribute(ntt_pass_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)(sizeof(uint4) << kNttMaxT));
+  cudaFuncSetAttribute(ntt_pass_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)(sizeof(uint4) << kNttMaxT));
+  done.fetch_or(bit);
+}
+
 bool tune_valid(const Tune& t) {
   const bool threads_ok = t.ntt_threads == 128 || t.ntt_threads == 256 || t.ntt_threads == 512;
   const bool top_ok = t.top_nodes >= 64 && t.top_nodes <= 4096 && (t.top_nodes & (t.top_nodes - 1)) == 0;
@@ -164,14 +178,7 @@ cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t w
     COUNT_LAUNCH();
     return cudaGetLastError();
   }
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(ntt_pass_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)(sizeof(uint4) << kNttMaxT));
-    cudaFuncSetAttribute(ntt_pass_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)(sizeof(uint4) << kNttMaxT));
-    attr_set = true;
-  }
+  init_kernel_attributes();
   // Fewest passes whose tiles fit 2^ntt_max_T, then more (smaller tiles) while
   // a pass would have fewer blocks than SMs and tiles stay >= 2^5.
   int passes = (n + tune.ntt_max_T - 1) / tune.ntt_max_T;
@@ -510,7 +517,9 @@ cudaError_t launch_fix(const uint4* in, uint4* out, size_t half, uint4 r, const 
 // First fix_last_var of column `col` of a row-major matrix with `width`
 // columns: out[b] = in[b] + r (in[b + half] - in[b]) on that column.
 __global__ void __launch_bounds__(256) fix_column_kernel(const uint4* __restrict__ in, size_t width, size_t col,
-                                                         uint4* __restrict__ out, size_t half, uint4 r) {
+                                                         uint4* __restrict__ out, size_t half, uint4 r,
+                                                         const uint4* xp) {
+  if (xp) r = *xp;
   for (size_t b = (size_t)blockIdx.x * blockDim.x + threadIdx.x; b < half; b += (size_t)gridDim.x * blockDim.x) {
     const uint4 lo = in[b * width + col], hi = in[(b + half) * width + col];
     out[b] = gf_add(lo, gf_mul(r, gf_add(hi, lo)));
@@ -518,8 +527,8 @@ __global__ void __launch_bounds__(256) fix_column_kernel(const uint4* __restrict
 }
 
 cudaError_t launch_fix_column(const uint4* in, size_t width, size_t col, uint4* out, size_t half, uint4 r,
-                              cudaStream_t st) {
-  fix_column_kernel<<<grid_for(half, 256), 256, 0, st>>>(in, width, col, out, half, r);
+                              cudaStream_t st, const uint4* xp) {
+  fix_column_kernel<<<grid_for(half, 256), 256, 0, st>>>(in, width, col, out, half, r, xp);
   COUNT_LAUNCH();
   return cudaGetLastError();
 }
@@ -527,7 +536,7 @@ cudaError_t launch_fix_column(const uint4* in, size_t width, size_t col, uint4* 
 __global__ void __launch_bounds__(512) eval_tail_kernel(uint4* buf, EvalTail p) {
   for (int k = p.nvars - 1; k >= 0; --k) {
     const uint32_t half = 1u << k;
-    const uint4 r = p.r[k];
+    const uint4 r = p.rp ? p.rp[k] : p.r[k];
     // in place: thread b writes buf[b] (b < half) and reads buf[b], buf[b + half]
     for (uint32_t b = threadIdx.x; b < half; b += blockDim.x) {
       const uint4 lo = buf[b], hi = buf[b + half];

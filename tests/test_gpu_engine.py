@@ -91,3 +91,28 @@ def test_engine_admission_by_memory_budget(bg):
     res = eng.prove(jobs)
     for (n, ev, pt), r in zip(jobs, res):
         assert r["proof"] == alone(bg, n, ev, pt)[2]
+
+
+def test_engine_graph_replay_matches_direct(bg):
+    """Captured-graph jobs (one plan per slot and size, replayed) give the
+    same bytes as the direct path and as proofs made one at a time, with
+    sizes repeating so plans are reused and other sizes evict them."""
+    sizes = [8, 8, 11, 8, 11, 5, 8, 13, 5, 11, 8, 0, 1, 8]
+    jobs = make_jobs(sizes, 8400)
+    direct = bg.Engine(max_inflight=3, graphs=False).prove(jobs)
+    for max_inflight in (1, 3):
+        replay = bg.Engine(max_inflight=max_inflight, graphs=True).prove(jobs)
+        for d, r in zip(direct, replay):
+            assert r["status"] == 0 and r["proof"] == d["proof"] and r["root"] == d["root"]
+    for k in (0, 2, 7):
+        n, ev, pt = jobs[k]
+        assert direct[k]["proof"] == alone(bg, n, ev, pt)[2]
+
+
+def test_engine_graph_eviction_under_budget(bg):
+    """A budget below one plan: every new size evicts the idle plans first,
+    jobs then run one at a time, results unchanged."""
+    jobs = make_jobs([9, 6, 9, 10, 6], 8500)
+    res = bg.Engine(max_inflight=4, mem_budget=1, graphs=True).prove(jobs)
+    for (n, ev, pt), r in zip(jobs, res):
+        assert r["status"] == 0 and r["proof"] == alone(bg, n, ev, pt)[2]
