@@ -1,0 +1,60 @@
+"""The headline sizes, checked bit for bit or through size-independent
+properties: a 2^24-evaluation proof identical to the oracle's and accepted by
+both verifiers, 2^22 commits at blowup 4 against the oracle, and the product
+sumcheck at 2^20 and 2^24 points (round identities through the verifier, the
+final evaluations against direct multilinear evaluation at the challenges).
+Tolerance: bit-exact (exact GF(2^128) and Keccak arithmetic)."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from basefold_gpu import rand
+
+pytestmark = pytest.mark.gpu
+ONE = 0xC2000000000000000000000000000001
+
+
+def test_proof_2_24_matches_oracle_and_verifies(built_lib):
+    bg = built_lib
+    n, log2_c = 24, 1
+    data = rand.random_elems((1 << n) + n, 24)
+    evals, point = data[: 1 << n], data[1 << n:]
+    pcs = bg.Basefold.setup(bg.BasefoldConfig(bg.BinaryReedSolomonCode(128, log2_c, n)))
+    comm = pcs.commit(evals)
+    ch = bg.GenericChallenger.keccak256()
+    ch.observe(comm.root)
+    values = pcs.eval(pcs.data(comm), point)
+    ch.observe_ext_slice(values)
+    blob = ch.state()
+    proof = pcs.open(comm, [bg.PolyEvals(values, point)], ch.clone())
+    root_o, values_o, blob_o = O.harness_prepare(n, log2_c, evals, point)
+    assert comm.root == root_o and np.array_equal(values, values_o) and blob == blob_o
+    assert proof == O.open_proof(n, log2_c, evals, point, values_o, blob_o)
+    pcs.verify(comm.root, [bg.PolyEvals(values, point)], proof, ch.clone())
+    assert O.verify(n, log2_c, comm.root, point, values, blob, proof) == 0
+
+
+def test_commit_2_22_blowup_4_matches_oracle(built_lib):
+    bg = built_lib
+    n, log2_c = 22, 2
+    evals = rand.random_elems(1 << n, 2222)
+    pcs = bg.Basefold.setup(bg.BasefoldConfig(bg.BinaryReedSolomonCode(128, log2_c, n)))
+    assert pcs.commit(evals).root == O.commit(n, log2_c, evals)
+
+
+@pytest.mark.parametrize("k,n", [(2, 20), (3, 20), (2, 24)])
+def test_product_sumcheck_full_size(built_lib, k, n):
+    bg = built_lib
+    polys = rand.random_elems(k << n, 7700 + 10 * k + n)
+    P = polys.reshape(k, 1 << n, 16)
+    prod = P[0]
+    for j in range(1, k):
+        prod = O.gf_mul(prod, P[j])
+    claim = np.bitwise_xor.reduce(prod, axis=0)[None]
+    init = b"full size"
+    rp, r, fe, fc = bg.prove_sumcheck(k, polys, claim, bg.GenericChallenger(init))
+    assert O.sumcheck_verify(k, n, claim, rp, fe, O.challenger_blob(init)) == 0
+    # fix_last_var takes the top variable first: the point is the challenges reversed
+    point = r[::-1].copy()
+    for j in range(k):
+        assert np.array_equal(fe[j], O.eval_poly(n, P[j].copy(), point)[0]), j
