@@ -278,8 +278,8 @@ def run_served(bg, device, log2_c, lo=12, hi=24, per_level=48, loads=(0.25, 0.5,
     eng.prove([(n, inputs[n][0], inputs[n][1]) for n in cap_sizes])
     capacity = per_level / (time.perf_counter() - t)
     out = {"workload": f"Poisson arrivals, sizes log-uniform 2^{lo}..2^{hi}, blowup {1 << log2_c}, "
-                       f"{per_level} requests per load, host inputs", "capacity_proofs_per_s": capacity,
-           "levels": []}
+                       f"{per_level} requests per load, host inputs", "size_range": [lo, hi],
+           "capacity_proofs_per_s": capacity, "levels": []}
     eng.start()
     for load in loads:
         rate = load * capacity
@@ -306,6 +306,22 @@ def run_served(bg, device, log2_c, lo=12, hi=24, per_level=48, loads=(0.25, 0.5,
                               "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))], "max_ms": lat[-1]})
     eng.stop()
     return out
+
+
+def served_cpu_reference(log2_c, size_range):
+    """The served mix on the CPU reference path (C++ restatement, all host
+    cores): one proof per size; sizes are uniform over the range, so the
+    service-time distribution of the mix is these times with equal weight.
+    Queueing is left out: the mix's CPU capacity is far below any GPU load."""
+    lo, hi = size_range
+    times = {n: 1e3 * cpu_step_oracle(n, log2_c) for n in range(lo, hi + 1)}
+    t = sorted(times.values())
+    mean = sum(t) / len(t)
+    return {"kind": "port", "cores": os.cpu_count() or 1,
+            "service_ms_by_size": {str(k): v for k, v in times.items()},
+            "service_p50_ms": t[len(t) // 2], "service_p99_ms": t[min(len(t) - 1, int(0.99 * len(t)))],
+            "capacity_proofs_per_s": 1e3 / mean,
+            "note": "service time of one proof per size on the host cores, no queueing"}
 
 
 def workload_config(args):
@@ -427,6 +443,8 @@ def main():
         cpu = {"value": 1.0 / t, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
                "sample": f"one full commit+eval+open at 2^{n} (C++ restatement of the reference CPU path, "
                          "all host threads; the Rust reference cannot be built here)"}
+        if served is not None:
+            served["cpu_baseline"] = served_cpu_reference(log2_c, served["size_range"])
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,

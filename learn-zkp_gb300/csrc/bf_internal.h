@@ -140,7 +140,6 @@ cudaError_t launch_open_round(OpenState* s, int i, int d, const uint4* scal, con
 // ---- the last rounds of open in one block, then the final polynomial
 constexpr int kTailThreads = 256;
 constexpr int kTailMaxLeavesLog = 11;    // largest Tune::tail_log
-constexpr int kWarpLevelMax = 32;        // tree levels of at most this many nodes hash one node per warp
 struct TailParams {
   int i0, d, log2_c;        // rounds i0 .. 0 (i0 = -1: none)
   const uint4* pi_first;    // folded codeword input of round d-1

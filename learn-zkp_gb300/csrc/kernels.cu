@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(256) tree_top_kernel(uint4* level, size_t n, u
   while (n > 1) {
     const size_t h = n >> 1;
     uint4* nxt = cur + 2 * n;
-    if (h <= (size_t)kWarpLevelMax) {  // latency-bound: one warp per node
+    if (h <= (size_t)nwarps) {  // latency-bound: one warp per node
       for (size_t s = warp; s < h; s += nwarps) warp_hash_node(wk, cur, s, h, nxt);
     } else {
       for (size_t s = threadIdx.x; s < h; s += blockDim.x)
