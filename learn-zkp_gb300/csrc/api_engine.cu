@@ -129,7 +129,7 @@ void finish_job(bf_engine* e, Job* j, int status) {
   j->pub->status = status;
   j->pub->latency_ms = now_ms() - j->t_submit;
   if (j->plan) {
-    if (status == BF_ERR_CUDA && j->slot >= 0) {  // a failed replay: rebuild the plan next time
+    if (status < 0 && j->slot >= 0) {  // a failed job may leave the plan mid-way: rebuild it next time
       auto& m = e->plans[j->slot];
       auto it = m.find(j->plan->n);
       if (it != m.end()) {
@@ -148,6 +148,7 @@ void finish_job(bf_engine* e, Job* j, int status) {
   j->cm.reset();
   if (j->slot >= 0) e->free_slots.push_back(j->slot);
   e->mem_used -= j->footprint;
+  e->jobs_done += 1;
   j->state = J_DONE;
 }
 
@@ -381,7 +382,6 @@ bool progress(bf_engine* e) {
     if (rc != 0) e->host_ms_complete += now_ms() - t_step;
     if (rc < 0) finish_job(e, j, rc);
     if (rc != 0) moved = true;
-    if (j->state == J_DONE) e->jobs_done += 1;
   }
   std::vector<Job*> keep;
   for (Job* j : e->inflight) {

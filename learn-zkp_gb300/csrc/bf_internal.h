@@ -40,8 +40,6 @@ cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t w
                           const Tune& tune = Tune());
 cudaError_t launch_leaves_elem(const uint4* cw, uint4* leaves, size_t n, size_t width, cudaStream_t st);
 cudaError_t launch_leaves_pair(const uint4* pi, uint4* leaves, size_t n, cudaStream_t st);
-cudaError_t launch_leaves_cw_pairs(const uint4* cw, uint4* leaves, uint4* pair_leaves, size_t n_pairs,
-                                   cudaStream_t st);
 // Build every level above `leaves` (n leaves, power of two); levels are stored
 // one after another right after the leaves.  Root = last digest, also copied
 // to `root_out` (32 bytes) when it is not null.

@@ -225,21 +225,6 @@ __global__ void __launch_bounds__(128) leaves_elem_kernel(const uint4* __restric
     store_digest(leaves, i, hash_elem(cw[i]));
 }
 
-// Codeword leaves H(cw[q]) together with the leaves of the first round's
-// folded-codeword tree H(cw[2s] || cw[2s+1]) (for width 1 the first round
-// commits the codeword itself as pairs, basefold.rs:159-165,350-355): both
-// read the same 32 bytes.
-__global__ void __launch_bounds__(128) leaves_cw_pairs_kernel(const uint4* __restrict__ cw,
-                                                              uint4* __restrict__ leaves,
-                                                              uint4* __restrict__ pair_leaves, size_t n_pairs) {
-  for (size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x; s < n_pairs; s += (size_t)gridDim.x * blockDim.x) {
-    const uint4 e0 = cw[2 * s], e1 = cw[2 * s + 1];
-    store_digest(leaves, 2 * s, hash_elem(e0));
-    store_digest(leaves, 2 * s + 1, hash_elem(e1));
-    store_digest(pair_leaves, s, hash_pair(e0, e1));
-  }
-}
-
 // Folded-codeword leaf s = H(pi[2s] || pi[2s+1]): the row (pi[j], pi[j+n_i])
 // of the width-2 matrix committed at basefold.rs:350-355, in NTT order.
 __global__ void __launch_bounds__(128) leaves_pair_kernel(const uint4* __restrict__ pi, uint4* __restrict__ leaves,
@@ -308,13 +293,6 @@ cudaError_t launch_leaves_elem(const uint4* cw, uint4* leaves, size_t n, size_t 
     leaves_elem_kernel<<<grid_for(n, 128, 16), 128, 0, st>>>(cw, leaves, n);
   else
     leaves_rows_kernel<<<grid_for(n, 128, 16), 128, 0, st>>>(cw, leaves, n, width);
-  COUNT_LAUNCH();
-  return cudaGetLastError();
-}
-
-cudaError_t launch_leaves_cw_pairs(const uint4* cw, uint4* leaves, uint4* pair_leaves, size_t n_pairs,
-                                   cudaStream_t st) {
-  leaves_cw_pairs_kernel<<<grid_for(n_pairs, 128, 16), 128, 0, st>>>(cw, leaves, pair_leaves, n_pairs);
   COUNT_LAUNCH();
   return cudaGetLastError();
 }
