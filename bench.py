@@ -308,6 +308,36 @@ def run_served(bg, device, log2_c, lo=12, hi=24, per_level=48, loads=(0.25, 0.5,
     return out
 
 
+def run_commit_sweep(bg, torch, device, sizes=(18, 20, 22, 24, 26), blowups=(1, 2), reps=3):
+    """Encode + Merkle commit alone (the standalone encode/commit sweep):
+    device-resident evaluations, commit time per size and blowup, its
+    algorithmic bytes (16 + 80c) N as GB/s and its Keccak-f rate (2cN
+    permutations: cN leaves, cN - 1 nodes of the codeword tree, plus the
+    first folded-codeword tree of cN/2 leaves for width 1)."""
+    out = []
+    peaks, _ = load_peaks()
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    for log2_c in blowups:
+        for n in sizes:
+            N, c = 1 << n, 1 << log2_c
+            ev = torch.from_numpy(bg.rand.random_elems(N, 4000 + n)).to(f"cuda:{device}")
+            pcs = bg.Basefold.setup(bg.BasefoldConfig(bg.BinaryReedSolomonCode(128, log2_c, n)), device=device)
+            pcs.commit_device(ev.data_ptr(), keep=ev).free()
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            for _ in range(reps):
+                pcs.commit_device(ev.data_ptr(), keep=ev).free()
+            torch.cuda.synchronize()
+            ms = (time.perf_counter() - t) / reps * 1e3
+            gbs = (16 + 80 * c) * N / (ms * 1e-3) / 1e9
+            perms = (c * N) + (c * N - 1) + (c * N // 2 + c * N // 2 - 1)
+            out.append({"num_vars": n, "blowup": c, "ms": ms, "algorithmic_gbs": gbs, "hbm_frac": gbs / hbm,
+                        "keccak_perms_per_s": perms / (ms * 1e-3)})
+            del ev, pcs
+            torch.cuda.empty_cache()
+    return out
+
+
 def served_cpu_reference(log2_c, size_range):
     """The served mix on the CPU reference path (C++ restatement, all host
     cores): one proof per size; sizes are uniform over the range, so the
@@ -433,10 +463,11 @@ def main():
     if tr and tr.get("bytes_per_node"):
         traffic = tr["bytes_per_node"] * nodes / max(tree_launches, 1)
     total_ms_classes = sum(v[0] for v in prof.values())
-    batched = served = None
+    batched = served = sweep = None
     if ws == 1 and not args.no_extras:
         batched = run_batched(bg, torch, local, log2_c)
         served = run_served(bg, local, log2_c)
+        sweep = run_commit_sweep(bg, torch, local)
     cpu = None
     if not args.no_cpu_baseline and ws == 1:
         t = cpu_step_oracle(n, log2_c)
@@ -467,6 +498,7 @@ def main():
         "proof_bytes": len(proof),
         "batched": batched,
         "served": served,
+        "commit_sweep": sweep,
     }
     print(json.dumps(line), flush=True)
 

@@ -245,7 +245,7 @@ class Basefold:
             raise ValueError("one evaluation point only (basefold.rs:143-144)")
         n_evals = len(evals)
         size = self.proof_size(comm.width, n_evals)
-        out = np.zeros(max(size, 1), dtype=np.uint8)
+        out = np.empty(max(size, 1), dtype=np.uint8)
         ln = C.c_size_t()
         if n_evals:
             pt = evals[0].point if self.config.code.d else np.zeros((1, 16), np.uint8)

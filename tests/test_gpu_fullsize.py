@@ -58,3 +58,32 @@ def test_product_sumcheck_full_size(built_lib, k, n):
     point = r[::-1].copy()
     for j in range(k):
         assert np.array_equal(fe[j], O.eval_poly(n, P[j].copy(), point)[0]), j
+
+
+def test_proof_2_26_blowup_4_verifies(built_lib):
+    """The largest commit of the encode/commit sweep (2^26 evaluations,
+    blowup 4: a 2^28-entry codeword): same root twice, and a full proof whose
+    189 query paths through every tree the host verifier accepts."""
+    bg = built_lib
+    torch = pytest.importorskip("torch")
+    n, log2_c = 26, 2
+    data = rand.random_elems((1 << n) + n, 2626)
+    evals, point = data[: 1 << n], data[1 << n:]
+    dev = torch.from_numpy(evals).cuda()
+    pcs = bg.Basefold.setup(bg.BasefoldConfig(bg.BinaryReedSolomonCode(128, log2_c, n)))
+    first = pcs.commit_device(dev.data_ptr(), keep=dev)
+    root0 = first.root
+    first.free()
+    comm = pcs.commit_device(dev.data_ptr(), keep=dev)
+    assert comm.root == root0
+    ch = bg.GenericChallenger.keccak256()
+    ch.observe(comm.root)
+    values = pcs.eval(pcs.data(comm), point)
+    ch.observe_ext_slice(values)
+    proof = pcs.open(comm, [bg.PolyEvals(values, point)], ch.clone())
+    pcs.verify(comm.root, [bg.PolyEvals(values, point)], proof, ch.clone())
+    bad = bytearray(proof)
+    bad[-5] ^= 1
+    with pytest.raises(bg.BasefoldError):
+        pcs.verify(comm.root, [bg.PolyEvals(values, point)], bytes(bad), ch.clone())
+    comm.free()
