@@ -176,13 +176,16 @@ int bf_pcs_set_tune(bf_pcs* pcs, const int* vals, int n);
  * time on the CPU.)
  * bf_engine_autotune: reps > 0 autotunes (bf_pcs_autotune) each size the
  *   first time a job of that size is admitted; 0 (default) keeps defaults.
- * bf_engine_graphs (default on): each slot keeps, per job size, fixed
+ * bf_engine_graphs (default off): on, each slot keeps, per job size, fixed
  *   buffers and one captured CUDA graph of the commit, evaluation and
  *   device-transcript open; a job then costs a staging write, one copy of
- *   its evaluations and one graph launch.  Idle slots' buffers count toward
- *   mem_budget and are dropped when a job of another size needs the room.
- *   Off: every job enqueues its kernels one by one on pool memory.  Call
- *   only while no job is in flight.
+ *   its evaluations and one graph launch (lower latency for a job alone).
+ *   Idle slots' buffers count toward mem_budget and are dropped when a job
+ *   of another size needs the room.  Off: every job enqueues its kernels one
+ *   by one on pool memory (as fast or faster with many jobs in flight).
+ *   Call only while no job is in flight.
+ * Completed jobs (query sampling, openings, proof) are finished on a few
+ *   host threads of the engine, apart from the scheduling thread.
  * bf_engine_prove: runs `count` jobs to completion on the calling thread.
  * bf_engine_start/stop + submit/poll: serving from a background thread;
  *   submitted bf_job structs must stay valid until returned by poll. */

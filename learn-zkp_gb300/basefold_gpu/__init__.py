@@ -405,7 +405,7 @@ class Engine:
     requests from a background thread (continuous batching)."""
 
     def __init__(self, device: int = 0, lambda_: int = 128, log2_c: int = 1, max_inflight: int = 16,
-                 mem_budget: int = 0, autotune_reps: int = 0, graphs: bool = True):
+                 mem_budget: int = 0, autotune_reps: int = 0, graphs: bool = False):
         h = C.c_void_p()
         check(lib().bf_engine_create(device, lambda_, log2_c, max_inflight, mem_budget, C.byref(h)))
         self._h, self.log2_c = h, log2_c

@@ -14,6 +14,8 @@
 // Proof bytes are identical to the one-at-a-time path.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -35,7 +37,10 @@ double now_ms() {
   return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
 }
 
-enum JobState { J_OPEN = 0, J_GATHER = 1, J_DONE = 2 };
+// J_OPEN: GPU work up to the final polynomial in flight; J_COMPLETING: a
+// completion thread samples the queries, gathers the openings and writes the
+// proof; J_DONE: retired.
+enum JobState { J_OPEN = 0, J_COMPLETING = 1, J_DONE = 2 };
 
 // One size's job captured on one slot: fixed buffers (evaluations,
 // codeword, trees, open workspace) and the CUDA graph that runs commit,
@@ -72,6 +77,8 @@ struct Job {
   DevBuf eval_ws;
   int state = J_OPEN;
   size_t footprint = 0;
+  std::atomic<bool> completed{false};  // set by the completion thread
+  int complete_rc = 0;
 };
 
 }  // namespace
@@ -79,12 +86,19 @@ struct Job {
 struct bf_engine {
   int device = 0, lambda = 128, log2_c = 1, max_inflight = 8;
   int autotune_reps = 0;  // > 0: autotune each size's pcs when it is created
-  bool use_graphs = true;  // replay one captured graph per (slot, size)
+  bool use_graphs = false;  // replay one captured graph per (slot, size)
   std::vector<std::map<int, std::unique_ptr<Plan>>> plans;  // per slot, by size
   uint64_t admissions = 0;
   // host-side accounting (bf_engine_stats)
   double host_ms_enqueue = 0, host_ms_launch = 0, host_ms_complete = 0;
   uint64_t plans_built = 0, plans_dropped = 0, jobs_done = 0;
+  // Completion threads: query sampling, gather and proof readout of jobs
+  // whose GPU work is done, off the scheduling thread.
+  std::vector<std::thread> completers;
+  std::deque<Job*> complete_q;
+  std::mutex complete_mu;
+  std::condition_variable complete_cv;
+  bool complete_stop = false;
   size_t mem_budget = 0, mem_used = 0;
   std::map<int, bf_pcs*> pcs_by_n;
   std::vector<cudaStream_t> streams;
@@ -269,25 +283,61 @@ int admit_graph(bf_engine* e, Job* j) {
   return BF_OK;
 }
 
-// Advances a job whose GPU work has completed.  Returns 1 if it moved.
-int step(bf_engine* e, Job* j) {
+// The completion of one job (on a completion thread): read the rounds and
+// the transcript, sample the query positions (basefold.rs:200-203), gather
+// the openings and write the proof, root and value.
+int complete_job(bf_engine* e, Job* j) {
   bf_pcs* p = j->pcs;
   bf_job* pj = j->pub;
-  int ready = bf_open_poll(j->sess);
-  TRY(ready);
-  if (!ready) return 0;
+  TRY(open_resident_complete(j->sess, j->ch));
+  std::vector<uint64_t> idx(p->Q);
+  for (size_t q = 0; q < p->Q; ++q) idx[q] = j->ch.sample_bits(p->L);
+  TRY(open_finish_enqueue(j->sess, idx.data(), idx.size()));
+  TRY(open_finish_complete(j->sess, pj->proof, pj->proof_cap, &pj->proof_len));
+  std::memcpy(pj->root, slot_pin(e, j->slot), 32);
+  std::memcpy(pj->value, slot_pin(e, j->slot) + 64, 16);
+  return BF_OK;
+}
+
+void completer_loop(bf_engine* e) {
+  cudaSetDevice(e->device);
+  while (true) {
+    Job* j = nullptr;
+    {
+      std::unique_lock<std::mutex> lk(e->complete_mu);
+      e->complete_cv.wait(lk, [e] { return e->complete_stop || !e->complete_q.empty(); });
+      if (e->complete_q.empty()) return;  // stopping and drained
+      j = e->complete_q.front();
+      e->complete_q.pop_front();
+    }
+    const double t0 = now_ms();
+    j->complete_rc = complete_job(e, j);
+    const double dt = now_ms() - t0;
+    {
+      std::lock_guard<std::mutex> lk(e->complete_mu);
+      e->host_ms_complete += dt;
+    }
+    j->completed.store(true, std::memory_order_release);
+  }
+}
+
+// Advances a job whose GPU work has completed.  Returns 1 if it moved.
+int step(bf_engine* e, Job* j) {
   if (j->state == J_OPEN) {
-    TRY(open_resident_complete(j->sess, j->ch));
-    std::vector<uint64_t> idx(p->Q);
-    for (size_t q = 0; q < p->Q; ++q) idx[q] = j->ch.sample_bits(p->L);  // basefold.rs:200-203
-    TRY(open_finish_enqueue(j->sess, idx.data(), idx.size()));
-    j->state = J_GATHER;
+    int ready = bf_open_poll(j->sess);
+    TRY(ready);
+    if (!ready) return 0;
+    j->state = J_COMPLETING;
+    {
+      std::lock_guard<std::mutex> lk(e->complete_mu);
+      e->complete_q.push_back(j);
+    }
+    e->complete_cv.notify_one();
     return 1;
   }
-  if (j->state == J_GATHER) {
-    TRY(open_finish_complete(j->sess, pj->proof, pj->proof_cap, &pj->proof_len));
-    std::memcpy(pj->root, slot_pin(e, j->slot), 32);
-    std::memcpy(pj->value, slot_pin(e, j->slot) + 64, 16);
+  if (j->state == J_COMPLETING) {
+    if (!j->completed.load(std::memory_order_acquire)) return 0;
+    TRY(j->complete_rc);
     finish_job(e, j, BF_OK);
     return 1;
   }
@@ -377,9 +427,7 @@ bool progress(bf_engine* e) {
   }
   for (Job* j : e->inflight) {
     if (j->state == J_DONE) continue;
-    const double t_step = now_ms();
     int rc = step(e, j);
-    if (rc != 0) e->host_ms_complete += now_ms() - t_step;
     if (rc < 0) finish_job(e, j, rc);
     if (rc != 0) moved = true;
   }
@@ -452,6 +500,9 @@ int bf_engine_create(int device, int lambda, int log2_c, int max_inflight, size_
   }
   CU(e->pin.ensure(128 * (size_t)max_inflight));
   e->plans.resize(max_inflight);
+  const unsigned hw = std::thread::hardware_concurrency();
+  const int n_completers = std::max(1, std::min(4, (int)(hw > 2 ? hw / 2 : 1)));
+  for (int i = 0; i < n_completers; ++i) e->completers.emplace_back(completer_loop, e.get());
   *out = e.release();
   return BF_OK;
 }
@@ -466,6 +517,16 @@ void bf_engine_free(bf_engine* e) {
     }
     e->worker.join();
   }
+  // jobs with a completion thread are left to finish it first
+  for (Job* j : e->inflight)
+    while (j->state == J_COMPLETING && !j->completed.load(std::memory_order_acquire))
+      std::this_thread::sleep_for(std::chrono::microseconds(50));
+  {
+    std::lock_guard<std::mutex> lk(e->complete_mu);
+    e->complete_stop = true;
+  }
+  e->complete_cv.notify_all();
+  for (auto& t : e->completers) t.join();
   for (Job* j : e->inflight) {
     finish_job(e, j, BF_ERR_ARG);
     delete j;
@@ -508,7 +569,10 @@ int bf_engine_stats(bf_engine* e, double* out, int n) {
   std::lock_guard<std::mutex> lk(e->mu);
   out[0] = e->host_ms_enqueue;
   out[1] = e->host_ms_launch;
-  out[2] = e->host_ms_complete;
+  {
+    std::lock_guard<std::mutex> lk2(e->complete_mu);
+    out[2] = e->host_ms_complete;
+  }
   out[3] = (double)e->plans_built;
   out[4] = (double)e->plans_dropped;
   out[5] = (double)e->jobs_done;
