@@ -161,7 +161,10 @@ struct bf_pcs;
 struct bf_commitment;
 namespace bfapi {
 int commit_alloc(bf_pcs* p, bf_commitment* cm, cudaStream_t st);
-int commit_enqueue(bf_pcs* p, bf_commitment* cm, const uint4* data, cudaStream_t st, uint8_t* roots_pin);
+// With fork_trees (and st the pcs's own stream) the codeword tree and the
+// first folded-codeword tree are built concurrently on the pcs's second stream.
+int commit_enqueue(bf_pcs* p, bf_commitment* cm, const uint4* data, cudaStream_t st, uint8_t* roots_pin,
+                   bool fork_trees = false);
 // The value lands in value_pin; *value_dev (when given) receives where it
 // lives on the device.  With point_dev the coordinates are read from device
 // memory at run time (for graph capture), else taken from the host `point`.
@@ -201,6 +204,8 @@ struct bf_pcs {
   size_t Q = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
+  cudaStream_t aux = nullptr;  // second stream for independent work of one commit
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   // Commitments and open sessions draw their buffers from this pool; it keeps
   // freed memory for reuse instead of returning it to the driver.
   cudaMemPool_t pool = nullptr;

@@ -150,12 +150,16 @@ std::vector<u128> sample_scalars_by_eq(size_t n, bfh::Challenger& ch) {
 using namespace bfapi;
 
 bf_pcs::~bf_pcs() {
+  if (aux) cudaStreamSynchronize(aux);
   if (stream) cudaStreamSynchronize(stream);
   sc_ws.release();
   eval_ws.release();
   if (stream) cudaStreamSynchronize(stream);
   if (pool) cudaMemPoolDestroy(pool);
   if (stream && own_stream) cudaStreamDestroy(stream);
+  if (aux) cudaStreamDestroy(aux);
+  if (ev_fork) cudaEventDestroy(ev_fork);
+  if (ev_join) cudaEventDestroy(ev_join);
 }
 
 // ---------------------------------------------------------------------------
@@ -247,9 +251,6 @@ int build_twiddles(bf_pcs* p) {
 
 namespace bfapi {
 
-// Encode + Merkle commit of `data` (width 1) on stream `st`; the codeword
-// root and the first folded-codeword root are copied to roots_pin[0..64)
-// (pinned) when the stream reaches that point.
 // The codeword and tree buffers of `cm` from the pcs's pool (kept when they
 // are already there, e.g. for a captured graph's fixed buffers).
 int commit_alloc(bf_pcs* p, bf_commitment* cm, cudaStream_t st) {
@@ -261,7 +262,11 @@ int commit_alloc(bf_pcs* p, bf_commitment* cm, cudaStream_t st) {
   return BF_OK;
 }
 
-int commit_enqueue(bf_pcs* p, bf_commitment* cm, const uint4* data, cudaStream_t st, uint8_t* roots_pin) {
+// Encode + Merkle commit of `data` on stream `st`; the codeword root and
+// (width 1) the first folded-codeword root are copied to roots_pin[0..64)
+// (pinned) when the stream reaches that point.
+int commit_enqueue(bf_pcs* p, bf_commitment* cm, const uint4* data, cudaStream_t st, uint8_t* roots_pin,
+                   bool fork_trees) {
   const size_t nd = p->n_d(), w = cm->width;
   // For width 1 the first open round commits the codeword itself (as pairs),
   // so that tree is built here; wider data is first combined in open.
@@ -280,7 +285,17 @@ int commit_enqueue(bf_pcs* p, bf_commitment* cm, const uint4* data, cudaStream_t
     ProfScope ps(p->prof, st, P_LEAVES);
     CU(bf::launch_leaves_elem(cw, tree, nd, w, st));
   }
-  {
+  if (pairs && fork_trees && st == p->stream && p->aux) {
+    // the two trees are independent: the folded-codeword tree on the second
+    // stream, joined before the roots are read
+    ProfScope ps(p->prof, st, P_TREE);  // one scope from the fork to the join
+    CU(cudaEventRecord(p->ev_fork, st));
+    CU(cudaStreamWaitEvent(p->aux, p->ev_fork, 0));
+    CU(bf::launch_tree(pit, nd / 2, p->aux, nullptr, p->tune.top_nodes));
+    CU(bf::launch_tree(tree, nd, st, nullptr, p->tune.top_nodes));
+    CU(cudaEventRecord(p->ev_join, p->aux));
+    CU(cudaStreamWaitEvent(st, p->ev_join, 0));
+  } else {
     ProfScope ps(p->prof, st, P_TREE);
     CU(bf::launch_tree(tree, nd, st, nullptr, p->tune.top_nodes));
     if (pairs) CU(bf::launch_tree(pit, nd / 2, st, nullptr, p->tune.top_nodes));
@@ -343,7 +358,7 @@ int eval_enqueue(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, uint4
 namespace {
 
 int commit_device(bf_pcs* p, bf_commitment* cm, const uint4* data) {
-  TRY(commit_enqueue(p, cm, data, p->stream, p->pinned.b()));
+  TRY(commit_enqueue(p, cm, data, p->stream, p->pinned.b(), true));
   CU(cudaStreamSynchronize(p->stream));
   p->prof.drain();
   std::memcpy(cm->root, p->pinned.b(), 32);
@@ -404,6 +419,9 @@ int bf_pcs_setup(int device, int lambda, int log2_c, int num_vars, void* stream,
     CU(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
     p->own_stream = true;
   }
+  CU(cudaStreamCreateWithFlags(&p->aux, cudaStreamNonBlocking));
+  CU(cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming));
+  CU(cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming));
   TRY(build_twiddles(p.get()));
   bf::init_kernel_attributes();
   CU(p->pinned.ensure(4096));
