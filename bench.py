@@ -41,6 +41,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the batched and served workloads")
     ap.add_argument("--profile-only", action="store_true", help="warmup + steps, no JSON extras (for ncu)")
+    ap.add_argument("--profile-sumcheck", type=int, nargs=2, metavar=("K", "N"),
+                    help="one product sumcheck of K polys over 2^N points, nothing else (for ncu)")
     return ap.parse_args()
 
 
@@ -215,6 +217,22 @@ def gen_inputs(sizes, seed):
     return inputs
 
 
+def release(*objs):
+    """Frees engines, pcs objects (and their memory pools) and device inputs
+    of one phase before the next is timed."""
+    import gc
+
+    import torch
+
+    for o in objs:
+        if isinstance(o, dict):
+            o.clear()
+    del objs
+    gc.collect()
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+
+
 def run_batched(bg, torch, device, log2_c, count=256, lo=10, hi=22, seed=4):
     """Config 4: `count` polynomials with sizes log-uniform in 2^lo..2^hi.
     Plain = commit/eval/open one at a time through the public API; batched =
@@ -256,6 +274,7 @@ def run_batched(bg, torch, device, log2_c, count=256, lo=10, hi=22, seed=4):
     t_batch = time.perf_counter() - t
     identical = all(r["proof"] == p for r, p in zip(res, plain))
     digest = hashlib.sha256(b"".join(hashlib.sha256(p).digest() for p in plain)).hexdigest()
+    release(eng, pcs, dev)
     return {"workload": f"{count} polys, sizes log-uniform 2^{lo}..2^{hi} (seed {seed}), blowup {1 << log2_c}",
             "plain_proofs_per_s": count / t_plain, "batched_proofs_per_s": count / t_batch,
             "speedup": t_plain / t_batch, "proofs_identical": identical, "proofs_sha256": digest,
@@ -305,6 +324,7 @@ def run_served(bg, device, log2_c, lo=12, hi=24, per_level=48, loads=(0.25, 0.5,
                               per_level / elapsed, "p50_ms": lat[len(lat) // 2],
                               "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))], "max_ms": lat[-1]})
     eng.stop()
+    release(eng)
     return out
 
 
@@ -335,6 +355,27 @@ def run_commit_sweep(bg, torch, device, sizes=(18, 20, 22, 24, 26), blowups=(1, 
                         "keccak_perms_per_s": perms / (ms * 1e-3)})
             del ev, pcs
             torch.cuda.empty_cache()
+    return out
+
+
+def run_sumcheck(bg, torch, device, cases=((2, 20), (3, 20), (2, 24), (3, 24)), reps=3):
+    """The product sumcheck prover alone (sum over the hypercube of the
+    product of k multilinear polynomials), device-resident polynomials."""
+    out = []
+    for k, n in cases:
+        polys = torch.from_numpy(bg.rand.random_elems(k << n, 5000 + 10 * k + n)).to(f"cuda:{device}")
+        pcs = bg.Basefold.setup(bg.BasefoldConfig(bg.BinaryReedSolomonCode(128, 1, 0)), device=device)
+        claim = bg.rand.random_elems(1, 77)
+        pcs.prove_sumcheck_device(k, n, polys.data_ptr(), claim, bg.GenericChallenger(b"sumcheck"))
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(reps):
+            pcs.prove_sumcheck_device(k, n, polys.data_ptr(), claim, bg.GenericChallenger(b"sumcheck"))
+        torch.cuda.synchronize()
+        ms = (time.perf_counter() - t) / reps * 1e3
+        out.append({"k": k, "num_vars": n, "ms": ms, "points_per_s": (1 << n) / (ms * 1e-3),
+                    "input_gbs": 16 * k * (1 << n) / (ms * 1e-3) / 1e9})
+        del polys, pcs
     return out
 
 
@@ -374,6 +415,14 @@ def main():
     import basefold_gpu as bg
 
     torch.cuda.set_device(local)
+    if args.profile_sumcheck:
+        k, ns = args.profile_sumcheck
+        polys = torch.from_numpy(bg.rand.random_elems(k << ns, 5000 + 10 * k + ns)).to(f"cuda:{local}")
+        sc_pcs = bg.Basefold.setup(bg.BasefoldConfig(bg.BinaryReedSolomonCode(128, 1, 0)), device=local)
+        sc_pcs.prove_sumcheck_device(k, ns, polys.data_ptr(), bg.rand.random_elems(1, 77),
+                                     bg.GenericChallenger(b"sumcheck"))
+        torch.cuda.synchronize()
+        return
     stream = torch.cuda.current_stream()
     n, log2_c = args.n, args.log2_c
     pcs = bg.Basefold.setup(bg.BasefoldConfig(bg.BinaryReedSolomonCode(128, log2_c, n)), device=local,
@@ -463,11 +512,12 @@ def main():
     if tr and tr.get("bytes_per_node"):
         traffic = tr["bytes_per_node"] * nodes / max(tree_launches, 1)
     total_ms_classes = sum(v[0] for v in prof.values())
-    batched = served = sweep = None
+    batched = served = sweep = sumcheck = None
     if ws == 1 and not args.no_extras:
         batched = run_batched(bg, torch, local, log2_c)
         served = run_served(bg, local, log2_c)
         sweep = run_commit_sweep(bg, torch, local)
+        sumcheck = run_sumcheck(bg, torch, local)
     cpu = None
     if not args.no_cpu_baseline and ws == 1:
         t = cpu_step_oracle(n, log2_c)
@@ -499,6 +549,7 @@ def main():
         "batched": batched,
         "served": served,
         "commit_sweep": sweep,
+        "sumcheck": sumcheck,
     }
     print(json.dumps(line), flush=True)
 
