@@ -730,9 +730,29 @@ int bf_open(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, const uint
   TRY(bf_open_start(p, cm, point, values, scal.empty() ? nullptr : scal.data(), nullptr, &s));
   std::unique_ptr<bf_open_session, void (*)(bf_open_session*)> guard(s, bf_open_session_free);
   // every round and the final polynomial with the transcript on the device
-  // (basefold.rs:185-196, 335-369), then the queries on the host
-  TRY(open_resident_enqueue(s, ch, nullptr, nullptr));
-  TRY(open_resident_complete(s, ch));
+  // (basefold.rs:185-196, 335-369), then the queries on the host; a pending
+  // transcript input too long for the device buffer drives the rounds from
+  // the host instead (same kernels)
+  const bool fits = ch.in.size() + 64 <= (size_t)bf::kTrMax && ch.out.size() <= 32;
+  if (fits) {
+    TRY(open_resident_enqueue(s, ch, nullptr, nullptr));
+    TRY(open_resident_complete(s, ch));
+  } else {
+    while (true) {
+      int round;
+      uint8_t root[32], poly[32];
+      TRY(bf_open_round(s, &round, root, poly));
+      if (round < 0) break;
+      ch.observe(root, 32);  // basefold.rs:356
+      ch.observe(poly, 32);  // sumcheck/src/lib.rs:97
+      uint8_t r[16];
+      bfh::store(r, ch.sample_elem());
+      TRY(bf_open_challenge(s, r));
+    }
+    uint8_t fin[16];
+    TRY(bf_open_final(s, fin));
+    ch.observe(fin, 16);  // basefold.rs:196
+  }
   std::vector<uint64_t> idx(p->Q);
   for (size_t q = 0; q < p->Q; ++q) idx[q] = ch.sample_bits(p->L);  // basefold.rs:200-203
   size_t len = 0;

@@ -195,3 +195,23 @@ def test_wide_commit_large(bg):
     root_o, values_o, blob = O.harness_prepare(n, log2_c, evals, point, width)
     assert comm.root == root_o and np.array_equal(values, values_o)
     assert proof == O.open_proof(n, log2_c, evals, point, values_o, blob, width)
+
+
+@pytest.mark.parametrize("pending", [0, 100, 400, 401, 600, 5000])
+def test_open_with_long_pending_transcript(bg, pending):
+    """Whatever the caller observed before open (here `pending` extra bytes,
+    across the device transcript buffer's limit) the proof is the oracle's."""
+    n, log2_c = 9, 1
+    data = rand.random_elems((1 << n) + n, 4242 + pending)
+    evals, point = data[: 1 << n], data[1 << n:]
+    pcs = setup_pcs(bg, n, log2_c)
+    comm = pcs.commit(evals)
+    extra = bytes((7 * k + pending) & 0xFF for k in range(pending))
+    ch = bg.GenericChallenger.keccak256()
+    ch.observe(extra)
+    ch.observe(comm.root)
+    values = pcs.eval(pcs.data(comm), point)
+    ch.observe_ext_slice(values)
+    blob = ch.state()
+    proof = pcs.open(comm, [bg.PolyEvals(values, point)], ch.clone())
+    assert proof == O.open_proof(n, log2_c, evals, point, values, blob)
