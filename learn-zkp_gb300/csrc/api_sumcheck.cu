@@ -1,4 +1,5 @@
 // libbasefold_gpu.so: the standalone product sumcheck prover.
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -28,8 +29,13 @@ int sumcheck_run(cudaStream_t st, DevBuf& scratch, PinnedBuf& pinned, int k, int
     return BF_OK;
   }
   const size_t half0 = N / 2;
-  if (scratch.bytes < 16 * (size_t)k * half0 + 256) CU(scratch.alloc(16 * (size_t)k * half0 + 256));
-  uint32_t* acc = reinterpret_cast<uint32_t*>(scratch.as<uint8_t>() + 16 * (size_t)k * half0);
+  // scratch: k folded polynomials, the round sums (256 B), the transcript
+  // state and the per-round records (compressed polynomial + challenge)
+  const size_t rec_sz = 16 * (size_t)(k + 1);
+  const size_t o_acc = 16 * (size_t)k * half0, o_state = o_acc + 256, o_rec = o_state + sizeof(bf::OpenState);
+  const size_t need = o_rec + rec_sz * (size_t)n + 16 * (size_t)k;
+  if (scratch.bytes < need) CU(scratch.alloc(need));
+  uint32_t* acc = reinterpret_cast<uint32_t*>(scratch.as<uint8_t>() + o_acc);
   uint4* work[3];
   const uint4* in[3];
   for (int j = 0; j < k; ++j) {
@@ -37,6 +43,53 @@ int sumcheck_run(cudaStream_t st, DevBuf& scratch, PinnedBuf& pinned, int k, int
     in[j] = polys + j * N;
   }
   ch.observe_elem(sc);  // lib.rs:67
+  const size_t pin_need = std::max(sizeof(bf::OpenState), rec_sz * (size_t)n + 16 * (size_t)k) + 64;
+  if (ch.in.size() + 16 * (size_t)k <= (size_t)bf::kTrMax && ch.out.size() <= 32 && pinned.ensure(pin_need) == cudaSuccess) {
+    // every round with the transcript on the device: sums, transcript step,
+    // fix + next sums; one copy back at the end
+    bf::OpenState img;
+    std::memset(&img, 0, sizeof(img));
+    if (!ch.in.empty()) std::memcpy(img.tr.in, ch.in.data(), ch.in.size());
+    if (!ch.out.empty()) std::memcpy(img.tr.out, ch.out.data(), ch.out.size());
+    img.tr.in_len = (int)ch.in.size();
+    img.tr.out_len = (int)ch.out.size();
+    img.outer = to_uint4(sc);
+    std::memcpy(pinned.b(), &img, sizeof(img));
+    bf::OpenState* S = reinterpret_cast<bf::OpenState*>(scratch.as<uint8_t>() + o_state);
+    uint8_t* rec = scratch.as<uint8_t>() + o_rec;
+    CU(cudaMemcpyAsync(S, pinned.b(), sizeof(img), cudaMemcpyHostToDevice, st));
+    CU(cudaMemsetAsync(acc, 0, 48, st));
+    CU(bf::launch_prod_round_sums(in, k, half0, acc, st));
+    int ri = 0;
+    for (int round = n - 1; round >= 0; --round, ++ri) {
+      CU(bf::launch_sumcheck_round(S, k, acc, rec + rec_sz * (size_t)ri, st));
+      const size_t half = (size_t)1 << round;
+      if (round > 0) CU(cudaMemsetAsync(acc, 0, 48, st));
+      const uint4* const* src = (round == n - 1) ? in : const_cast<const uint4* const*>(work);
+      CU(bf::launch_prod_fix(work, src, k, half, uint4{}, half / 2, acc, st, &S->x));
+    }
+    uint8_t* fin = rec + rec_sz * (size_t)n;
+    for (int j = 0; j < k; ++j) CU(cudaMemcpyAsync(fin + 16 * j, work[j], 16, cudaMemcpyDeviceToDevice, st));
+    // pinned: records and final evaluations, then the state
+    const size_t rec_bytes = rec_sz * (size_t)n + 16 * (size_t)k;
+    CU(cudaMemcpyAsync(pinned.b(), rec, rec_bytes, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    const uint8_t* r = pinned.b();
+    for (int i = 0; i < n; ++i) {
+      std::memcpy(out + 16 * (size_t)i * k, r + rec_sz * (size_t)i, 16 * (size_t)k);
+      std::memcpy(out + off_r + 16 * (size_t)i, r + rec_sz * (size_t)i + 16 * (size_t)k, 16);
+    }
+    std::memcpy(out + off_f, r + rec_sz * (size_t)n, 16 * (size_t)k);
+    CU(cudaMemcpyAsync(pinned.b(), S, sizeof(img), cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    std::memcpy(&img, pinned.b(), sizeof(img));
+    if (img.status != 0) return fail(BF_ERR_ARG, "transcript input outgrew the device buffer");
+    ch.in.assign(img.tr.in, img.tr.in + img.tr.in_len);
+    ch.out.assign(img.tr.out, img.tr.out + img.tr.out_len);
+    std::memcpy(out + off_c, &img.outer, 16);
+    return BF_OK;
+  }
+  // a long pending transcript: the rounds' transcript on the host
   CU(cudaMemsetAsync(acc, 0, 48, st));
   CU(bf::launch_prod_round_sums(in, k, half0, acc, st));
   CU(cudaMemcpyAsync(pinned.b(), acc, 48, cudaMemcpyDeviceToHost, st));

@@ -96,7 +96,7 @@ cudaError_t launch_gather(const GatherParams& p, cudaStream_t st);
 // Standalone product sumcheck.
 cudaError_t launch_prod_round_sums(const uint4* const* polys, int k, size_t half, uint32_t* acc, cudaStream_t st);
 cudaError_t launch_prod_fix(uint4* const* out, const uint4* const* in, int k, size_t half, uint4 r,
-                            size_t next_half, uint32_t* acc, cudaStream_t st);
+                            size_t next_half, uint32_t* acc, cudaStream_t st, const uint4* xp = nullptr);
 
 unsigned long long launches_total();
 void count_launch();
@@ -134,6 +134,13 @@ cudaError_t launch_open_observe(OpenState* s, const uint4* root, const uint4* va
 // c0, c2 (64 bytes).  `scal` holds r_i, r_i^-1, correcting factor per round.
 cudaError_t launch_open_round(OpenState* s, int i, int d, const uint4* scal, const uint4* root, const uint4* S,
                               uint8_t* rec, cudaStream_t st);
+// One round of the product sumcheck's transcript on the device (warp):
+// from the sums acc = [c0, c2, c3] (sumcheck/src/function/quadratic.rs
+// 116-127 for k = 2; its k = 3 extension), observe the compressed round
+// polynomial, sample the challenge into s->x, and advance the claim
+// s->outer to the round polynomial at x (lib.rs:95-103).  `rec` receives
+// the compressed polynomial (16 k bytes) and the challenge (16 bytes).
+cudaError_t launch_sumcheck_round(OpenState* s, int k, const uint32_t* acc, uint8_t* rec, cudaStream_t st);
 
 // ---- the last rounds of open in one block, then the final polynomial
 constexpr int kTailThreads = 256;

@@ -679,8 +679,10 @@ __global__ void __launch_bounds__(256) prod_sums_kernel(PolyPtrs p, size_t half,
 // round's sums.  Each thread produces the pair (b, b + half/2) of the fixed
 // polynomials, which is exactly what the next round's sums need.
 template <int K>
-__global__ void __launch_bounds__(256) prod_fix_kernel(PolyPtrs p, size_t half, uint4 r, uint32_t* acc) {
+__global__ void __launch_bounds__(256) prod_fix_kernel(PolyPtrs p, size_t half, uint4 r, uint32_t* acc,
+                                                       const uint4* xp) {
   __shared__ uint4 scratch[32];
+  if (xp) r = *xp;
   uint4 s0 = make_uint4(0, 0, 0, 0), s2 = s0, s3 = s0;
   const size_t nh = half >> 1;
   if (nh == 0) {  // last round: one output per polynomial
@@ -732,7 +734,7 @@ cudaError_t launch_prod_round_sums(const uint4* const* polys, int k, size_t half
 }
 
 cudaError_t launch_prod_fix(uint4* const* out, const uint4* const* in, int k, size_t half, uint4 r, size_t next_half,
-                            uint32_t* acc, cudaStream_t st) {
+                            uint32_t* acc, cudaStream_t st, const uint4* xp) {
   (void)next_half;
   PolyPtrs p{};
   for (int i = 0; i < k; ++i) {
@@ -741,9 +743,9 @@ cudaError_t launch_prod_fix(uint4* const* out, const uint4* const* in, int k, si
   }
   const size_t work = half > 1 ? half / 2 : 1;
   if (k == 2)
-    prod_fix_kernel<2><<<grid_for(work, 256), 256, 0, st>>>(p, half, r, acc);
+    prod_fix_kernel<2><<<grid_for(work, 256), 256, 0, st>>>(p, half, r, acc, xp);
   else if (k == 3)
-    prod_fix_kernel<3><<<grid_for(work, 256), 256, 0, st>>>(p, half, r, acc);
+    prod_fix_kernel<3><<<grid_for(work, 256), 256, 0, st>>>(p, half, r, acc, xp);
   else
     return cudaErrorInvalidValue;
   COUNT_LAUNCH();

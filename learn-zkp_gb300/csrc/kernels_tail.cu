@@ -324,6 +324,58 @@ __global__ void __launch_bounds__(kTailThreads, 1) open_tail_kernel(TailParams P
   state_store(P.state, sh);
 }
 
+// Product sumcheck round (warp): c = [c0, c2, c3] from the device sums.
+__global__ void __launch_bounds__(32) sumcheck_round_kernel(OpenState* S, int k, const uint32_t* acc, uint8_t* rec) {
+  __shared__ OpenState sh;
+  const WarpKeccak wk;
+  state_load(sh, S);
+  __syncthreads();
+  const uint4* a = reinterpret_cast<const uint4*>(acc);
+  const uint4 c0 = a[0], c2 = a[1], c3 = a[2];
+  const uint4 sc = sh.outer;
+  // k = 2: compressed [c0, c2] (the pair scalar is ONE, quadratic.rs:118),
+  // round polynomial [c0, sc - 2 c0 - c2 = sc + c2, c2]; k = 3: compressed
+  // [c0, c2, c3], round polynomial [c0, sc + c2 + c3, c2, c3]
+  if (wk.lane == 0) {
+    uint4* r = reinterpret_cast<uint4*>(rec);
+    r[0] = c0;
+    r[1] = c2;
+    if (k == 3) {
+      r[2] = c3;
+      const uint4 m[3] = {c0, c2, c3};
+      tr_observe(sh, m);
+    } else {
+      const uint4 m[2] = {c0, c2};
+      tr_observe(sh, m);
+    }
+  }
+  uint4 x = warp_sample_elem(wk, sh);  // valid on lane 0
+  x.x = __shfl_sync(0xffffffffu, x.x, 0);
+  x.y = __shfl_sync(0xffffffffu, x.y, 0);
+  x.z = __shfl_sync(0xffffffffu, x.z, 0);
+  x.w = __shfl_sync(0xffffffffu, x.w, 0);
+  // horner over the round polynomial at x
+  const uint4 c1 = (k == 3) ? gf_add(sc, gf_add(c2, c3)) : gf_add(sc, c2);
+  uint4 acc_h = (k == 3) ? c3 : c2;
+  if (k == 3) acc_h = gf_add(gf_mul_warp(acc_h, x), c2);
+  acc_h = gf_add(gf_mul_warp(acc_h, x), c1);
+  acc_h = gf_add(gf_mul_warp(acc_h, x), c0);
+  if (wk.lane == 0) {
+    reinterpret_cast<uint4*>(rec)[k] = x;
+    sh.outer = acc_h;
+    sh.x = x;
+  }
+  __syncthreads();
+  state_store(S, sh);
+}
+
+cudaError_t launch_sumcheck_round(OpenState* s, int k, const uint32_t* acc, uint8_t* rec, cudaStream_t st) {
+  if (k != 2 && k != 3) return cudaErrorInvalidValue;
+  sumcheck_round_kernel<<<1, 32, 0, st>>>(s, k, acc, rec);
+  count_launch();
+  return cudaGetLastError();
+}
+
 cudaError_t launch_open_observe(OpenState* s, const uint4* root, const uint4* value, cudaStream_t st) {
   open_observe_kernel<<<1, 32, 0, st>>>(s, root, value);
   count_launch();

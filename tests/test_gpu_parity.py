@@ -215,3 +215,27 @@ def test_open_with_long_pending_transcript(bg, pending):
     blob = ch.state()
     proof = pcs.open(comm, [bg.PolyEvals(values, point)], ch.clone())
     assert proof == O.open_proof(n, log2_c, evals, point, values, blob)
+
+
+@pytest.mark.parametrize("init_len", [0, 400, 470, 3000])
+def test_sumcheck_any_initial_transcript(bg, init_len):
+    """The product sumcheck runs its rounds' transcript on the device when the
+    initial state fits the device buffer and on the host otherwise; both give
+    the oracle's rounds and leave the challenger in the oracle's state."""
+    for k in (2, 3):
+        n = 9
+        polys = rand.random_elems(k << n, 300 + init_len + k)
+        claim = rand.random_elems(1, 31 + k)
+        init = bytes((5 * i + k) & 0xFF for i in range(init_len))
+        ch = bg.GenericChallenger(init)
+        got = bg.prove_sumcheck(k, polys, claim, ch)
+        want = O.sumcheck_prove(k, n, polys, claim, O.challenger_blob(init))
+        for g, w in zip(got, want):
+            assert np.array_equal(g, w), (k, init_len)
+        # the challenger continues like the oracle's after the proof
+        ref = bg.GenericChallenger(init)
+        ref.observe_ext_slice(claim)
+        for i in range(n):
+            ref.observe_ext_slice(want[0][i])
+            ref.sample_ext_element()
+        assert ch.sample_ext_element().tobytes() == ref.sample_ext_element().tobytes()
