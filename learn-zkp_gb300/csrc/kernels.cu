@@ -467,7 +467,7 @@ cudaError_t launch_fold(const uint4* pi, uint4* out, size_t n_out, const uint4* 
 
 // fix_last_var (multilinear.rs:183-198) fused with the next round's
 // sum_b half_eq[b] * poly_lo[b] (eval_impr.rs:187-197).  In-place safe.
-__global__ void __launch_bounds__(256) fix_kernel(const uint4* in, uint4* out, size_t half, uint4 r,
+__global__ void __launch_bounds__(256, 3) fix_kernel(const uint4* in, uint4* out, size_t half, uint4 r,
                                                   const uint4* __restrict__ heq, size_t next_half, uint32_t* acc,
                                                   const uint4* xp) {
   __shared__ uint4 scratch[32];
