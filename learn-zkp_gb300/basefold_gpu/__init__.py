@@ -456,15 +456,18 @@ class Engine:
         return {"status": job.status, "root": bytes(job.root), "value": np.frombuffer(bytes(job.value), np.uint8)
                 .reshape(1, 16), "proof": buf[: job.proof_len].tobytes(), "latency_ms": job.latency_ms}
 
-    def prove(self, jobs, device_input: bool = False):
-        """jobs: list of (num_vars, evals, point); evals are host arrays or device pointers."""
+    def prove(self, jobs, device_input: bool = False, raise_on_error: bool = True):
+        """jobs: list of (num_vars, evals, point); evals are host arrays or device pointers.
+        With raise_on_error False, failed jobs come back with a negative `status`."""
         arr = (BfJob * len(jobs))()
         keeps = []
         for i, (n, ev, pt) in enumerate(jobs):
             job, keep = self._job(n, ev, pt, device_input)
             arr[i] = job
             keeps.append(keep)
-        check(lib().bf_engine_prove(self._h, arr, len(jobs), 1 if device_input else 0))
+        rc = lib().bf_engine_prove(self._h, arr, len(jobs), 1 if device_input else 0)
+        if raise_on_error:
+            check(rc)
         return [self._result(arr[i], keeps[i]) for i in range(len(jobs))]
 
     def start(self) -> None:

@@ -119,3 +119,12 @@ def test_launch_shape_validation(built_lib):
         raise AssertionError("autotune ran without a device")
     except bg.BasefoldGpuError as e:
         assert e.code == -1
+
+
+def test_engine_rejects_bad_parameters(built_lib):
+    """Engine parameters are checked before any device is touched."""
+    import ctypes as C
+    bg = built_lib
+    h = C.c_void_p()
+    for args in ((0, 128, 1, 0, 0), (0, 128, 1, 300, 0), (0, 128, -1, 4, 0), (0, 128, 5, 4, 0)):
+        assert bg.lib().bf_engine_create(*args, C.byref(h)) == -1

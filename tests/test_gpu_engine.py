@@ -116,3 +116,23 @@ def test_engine_graph_eviction_under_budget(bg):
     res = bg.Engine(max_inflight=4, mem_budget=1, graphs=True).prove(jobs)
     for (n, ev, pt), r in zip(jobs, res):
         assert r["status"] == 0 and r["proof"] == alone(bg, n, ev, pt)[2]
+
+
+@pytest.mark.parametrize("graphs", [False, True])
+def test_engine_bad_job_fails_alone(bg, graphs):
+    """A job whose point has a zero coordinate (EvalImpr::new would divide by
+    zero, eval_impr.rs:24) fails with BF_ERR_NOT_INVERTIBLE; the jobs around
+    it, before and after, and later batches are unaffected."""
+    jobs = make_jobs([9, 9, 7, 9], 8600)
+    n, ev, pt = jobs[1]
+    bad_pt = pt.copy()
+    bad_pt[3] = 0
+    jobs[1] = (n, ev, bad_pt)
+    eng = bg.Engine(max_inflight=2, graphs=graphs)
+    res = eng.prove(jobs, raise_on_error=False)
+    assert res[1]["status"] == -6  # BF_ERR_NOT_INVERTIBLE
+    for k in (0, 2, 3):
+        n, ev, pt = jobs[k]
+        assert res[k]["status"] == 0 and res[k]["proof"] == alone(bg, n, ev, pt)[2]
+    again = eng.prove([jobs[0], jobs[3]])
+    assert again[0]["proof"] == res[0]["proof"] and again[1]["proof"] == res[3]["proof"]

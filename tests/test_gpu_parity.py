@@ -239,3 +239,19 @@ def test_sumcheck_any_initial_transcript(bg, init_len):
             ref.observe_ext_slice(want[0][i])
             ref.sample_ext_element()
         assert ch.sample_ext_element().tobytes() == ref.sample_ext_element().tobytes()
+
+
+def test_open_zero_coordinate_then_valid_open(bg):
+    """open at a point with a zero coordinate is refused (the reference would
+    divide by zero in EvalImpr::new, eval_impr.rs:24) and leaves the pcs and
+    the commitment usable for a valid open."""
+    n, log2_c = 8, 1
+    pcs, comm, evals, point, values, ch, proof = harness(bg, n, log2_c, 99)
+    bad = point.copy()
+    bad[2] = 0
+    try:
+        pcs.open(comm, [bg.PolyEvals(values, bad)], ch.clone())
+        raise AssertionError("zero coordinate accepted")
+    except bg.BasefoldGpuError as e:
+        assert e.code == -6
+    assert pcs.open(comm, [bg.PolyEvals(values, point)], ch.clone()) == proof
