@@ -294,7 +294,7 @@ int complete_job(bf_engine* e, Job* j) {
   for (size_t q = 0; q < p->Q; ++q) idx[q] = j->ch.sample_bits(p->L);
   TRY(open_finish_enqueue(j->sess, idx.data(), idx.size()));
   TRY(open_finish_complete(j->sess, pj->proof, pj->proof_cap, &pj->proof_len));
-  std::memcpy(pj->root, slot_pin(e, j->slot), 32);
+  bfh::digest_from_interleaved(slot_pin(e, j->slot), pj->root);  // the tree root, stored interleaved
   std::memcpy(pj->value, slot_pin(e, j->slot) + 64, 16);
   return BF_OK;
 }

@@ -198,7 +198,7 @@ int ensure_message(bf_open_session* s) {
   if (i == d - 1 && s->w == 1)
     std::memcpy(s->root, s->cm->pi_root, 32);
   else
-    std::memcpy(s->root, s->pin->b(), 32);
+    bfh::digest_from_interleaved(s->pin->b(), s->root);  // a tree root, stored interleaved
   const u128 S = bfh::load(s->pin->b() + 32);
   const u128 sc_val = (i == d - 1) ? s->outer_val : s->inner_val;
   const u128 c0 = bfh::mul(s->corr[i], S);

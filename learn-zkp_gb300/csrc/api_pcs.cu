@@ -361,8 +361,8 @@ int commit_device(bf_pcs* p, bf_commitment* cm, const uint4* data) {
   TRY(commit_enqueue(p, cm, data, p->stream, p->pinned.b(), true));
   CU(cudaStreamSynchronize(p->stream));
   p->prof.drain();
-  std::memcpy(cm->root, p->pinned.b(), 32);
-  std::memcpy(cm->pi_root, p->pinned.b() + 32, 32);
+  bfh::digest_from_interleaved(p->pinned.b(), cm->root);  // tree roots are stored interleaved
+  bfh::digest_from_interleaved(p->pinned.b() + 32, cm->pi_root);
   return BF_OK;
 }
 

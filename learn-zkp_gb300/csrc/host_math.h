@@ -96,6 +96,33 @@ static inline u128 load(const uint8_t* p) {
 }
 static inline void store(uint8_t* p, u128 v) { std::memcpy(p, &v, 16); }
 
+// ---- Merkle digests as the device trees store them ----
+// The device keeps tree digests with every 64-bit lane bit-interleaved (even
+// bits, odd bits); this turns such a digest back into its 32 bytes.
+inline uint32_t bi_shuffle32_host(uint32_t x) {
+  uint32_t t;
+  t = (x ^ (x >> 8)) & 0x0000FF00u;
+  x ^= t ^ (t << 8);
+  t = (x ^ (x >> 4)) & 0x00F000F0u;
+  x ^= t ^ (t << 4);
+  t = (x ^ (x >> 2)) & 0x0C0C0C0Cu;
+  x ^= t ^ (t << 2);
+  t = (x ^ (x >> 1)) & 0x22222222u;
+  x ^= t ^ (t << 1);
+  return x;
+}
+inline void digest_from_interleaved(const uint8_t in[32], uint8_t out[32]) {
+  for (int l = 0; l < 4; ++l) {
+    uint32_t e, o;
+    std::memcpy(&e, in + 8 * l, 4);
+    std::memcpy(&o, in + 8 * l + 4, 4);
+    const uint32_t lo = bi_shuffle32_host((e & 0xFFFFu) | (o << 16));
+    const uint32_t hi = bi_shuffle32_host((e >> 16) | (o & 0xFFFF0000u));
+    std::memcpy(out + 8 * l, &lo, 4);
+    std::memcpy(out + 8 * l + 4, &hi, 4);
+  }
+}
+
 // ---- Keccak-256 (FIPS 202 permutation, original Keccak padding 0x01) ----
 static const uint64_t kRC[24] = {
     0x0000000000000001ull, 0x0000000000008082ull, 0x800000000000808aull, 0x8000000080008000ull,

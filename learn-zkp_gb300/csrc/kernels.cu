@@ -2,7 +2,9 @@
 //
 // Layout conventions shared by every kernel:
 //  * a field element is a uint4 (raw little-endian Montgomery-form u128);
-//  * a digest is two uint4 (32 bytes);
+//  * a digest is two uint4 (32 bytes); inside the Merkle trees its four
+//    64-bit lanes are stored bit-interleaved (keccak.cuh), converted to
+//    bytes wherever a digest leaves a tree (openings, roots);
 //  * the codeword of a commitment and every folded codeword of `open` are
 //    kept in additive-NTT output order ("NTT order"): position q holds the
 //    codeword entry at bitrev(q).  The reference materialises the bit
@@ -284,7 +286,7 @@ __global__ void __launch_bounds__(128) leaves_rows_kernel(const uint4* __restric
       if (q == rem) s[q].x ^= 0x01u;
     s[16].y ^= 0x80000000u;
     keccak_f1600(s);
-    store_digest(leaves, i, digest_from_state(s));
+    store_digest(leaves, i, digest_interleaved(digest_from_state(s)));  // trees hold interleaved digests
   }
 }
 
@@ -561,9 +563,11 @@ __device__ __forceinline__ void put_elem(uint8_t* out, size_t off, uint4 v) {
   p[0] = make_uint2(v.x, v.y);
   p[1] = make_uint2(v.z, v.w);
 }
+// Digest i of a tree (stored interleaved) as its 32 bytes.
 __device__ __forceinline__ void put_digest(uint8_t* out, size_t off, const uint4* tree, size_t i) {
-  put_elem(out, off, tree[2 * i]);
-  put_elem(out, off + 16, tree[2 * i + 1]);
+  const Digest d = digest_bytes(load_digest(tree, i));
+  put_elem(out, off, d.lo);
+  put_elem(out, off + 16, d.hi);
 }
 
 __global__ void gather_kernel(GatherParams p) {

@@ -61,7 +61,7 @@ __device__ void warp_flush(const WarpKeccak& wk, DevTranscript& t) {
       if (last && wk.lane == 16) w.y ^= 0x80000000u;  // last byte of the rate
       a = kx2(a, w);
     }
-    a = wk.permute(a);
+    a = wk.permute<false>(a);
     if (last) break;
   }
   __syncwarp();
@@ -139,8 +139,13 @@ __device__ uint4 warp_sample_elem(const WarpKeccak& wk, OpenState& o) {
 // challenge x the EvalProver claim is c0 + c1 x and d becomes d (1 + r + x);
 // the sumcheck claim (the round polynomial at x) is only read in the first
 // round, so it is not carried.
-__device__ void round_step(const WarpKeccak& wk, OpenState& o, int i, int d, const uint4* scal, uint4 root_lo,
-                           uint4 root_hi, uint4 S, uint4* rec) {
+__device__ void round_step(const WarpKeccak& wk, OpenState& o, int i, int d, const uint4* scal, uint4 root_lo_bi,
+                           uint4 root_hi_bi, uint4 S, uint4* rec) {
+  Digest rt;  // the round's root is a tree digest (interleaved): its bytes
+  rt.lo = root_lo_bi;
+  rt.hi = root_hi_bi;
+  rt = digest_bytes(rt);
+  const uint4 root_lo = rt.lo, root_hi = rt.hi;
   // Every lane computes the same scalars; the products are spread over the
   // warp (gf_mul_warp2), two independent ones at a time.
   const uint4 ONE = one_dev();
@@ -197,8 +202,9 @@ __global__ void __launch_bounds__(32) open_observe_kernel(OpenState* S, const ui
   state_load(sh, S);
   __syncthreads();
   if (threadIdx.x == 0) {
-    if (root) {
-      const uint4 m[2] = {root[0], root[1]};
+    if (root) {  // a tree root, stored interleaved
+      const Digest rb = digest_bytes(load_digest(root, 0));
+      const uint4 m[2] = {rb.lo, rb.hi};
       tr_observe(sh, m);
     }
     if (value) {
