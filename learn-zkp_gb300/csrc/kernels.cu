@@ -305,9 +305,54 @@ cudaError_t launch_leaves_pair(const uint4* pi, uint4* leaves, size_t n, cudaStr
   return cudaGetLastError();
 }
 
+// Levels 1..k above `level` (n nodes), stored one after another after it, in
+// one launch.  Block b owns the top nodes [b M, (b+1) M) of level k
+// (n >> k nodes), M = 2^(9-k), and at level k - j the runs s + m (n >> k),
+// m < 2^j, of their subtrees: node i of a level has children i and
+// i + (its level's size) below, so a block only reads what it wrote and
+// __syncthreads separates the levels.  Level 1 has one node per thread.
+constexpr int kSubtreeThreads = 256;
+constexpr size_t kSubtreeMaxNodes = (size_t)1 << 16;  // larger levels: one launch each
+__global__ void __launch_bounds__(kSubtreeThreads) subtree_kernel(uint4* level, size_t n, int k) {
+  const size_t nk = n >> k;
+  const int log_m = 9 - k;  // M = 2^log_m top nodes per block
+  const size_t a = (size_t)blockIdx.x << log_m;
+  uint4* cur = level;
+  size_t ncur = n;
+  for (int j = 1; j <= k; ++j) {
+    const size_t h = ncur >> 1;
+    uint4* nxt = cur + 2 * ncur;
+    const int per = 1 << (log_m + k - j);  // this block's nodes at level j
+    for (int t = threadIdx.x; t < per; t += blockDim.x) {
+      const size_t s = a + (size_t)(t & ((1 << log_m) - 1)) + (size_t)(t >> log_m) * nk;
+      store_digest(nxt, s, hash_node(load_digest(cur, s), load_digest(cur, s + h)));
+    }
+    __syncthreads();
+    cur = nxt;
+    ncur = h;
+  }
+}
+
 cudaError_t launch_tree(uint4* leaves, size_t n, cudaStream_t st, uint4* root_out, size_t top_nodes) {
   uint4* cur = leaves;
   while (n > top_nodes) {
+    if (n <= kSubtreeMaxNodes && n >= 1024) {  // the latency-bound middle levels in one launch
+      int k = 0;
+      size_t m = n;
+      while (m > top_nodes && k < 9) {
+        m >>= 1;
+        ++k;
+      }
+      subtree_kernel<<<(unsigned)(n >> 9), kSubtreeThreads, 0, st>>>(cur, n, k);
+      COUNT_LAUNCH();
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+      for (int j = 0; j < k; ++j) {
+        cur += 2 * n;
+        n >>= 1;
+      }
+      continue;
+    }
     const size_t h = n >> 1;
     uint4* nxt = cur + 2 * n;
     level_kernel<<<grid_for(h, 128, 16), 128, 0, st>>>(cur, nxt, h);
