@@ -280,17 +280,25 @@ int open_resident_enqueue_device(bf_open_session* s, const uint4* root_dev, cons
       CU(bf::launch_open_round(s->w_state, i, d, scal, root_i, reinterpret_cast<const uint4*>(s->stage(i) + 32),
                                s->w_rec + 64 * (size_t)(d - 1 - i), st));
     }
-    const size_t ni = p->n_i(i);
-    const uint4* pi_in = (i == d - 1) ? s->first_pi() : s->pi_fold_out(i + 1);
     {
+      // fold (binary_reed_solomon.rs:88-96) + next leaves, and fix_last_var
+      // (multilinear.rs:183-198) + next reduction, in one launch
       ProfScope ps(p->prof, st, P_FOLD);
-      CU(bf::launch_fold_leaves(pi_in, s->pi_fold_out(i), s->pi_tree(i - 1), ni / 2, p->tw_host.lo[d - 1 - i],
-                                p->tw_host.hi[d - 1 - i], uint4{}, st, xp));
-    }
-    {
-      ProfScope ps(p->prof, st, P_FIX);
-      CU(bf::launch_fix((i == d - 1) ? s->first_poly() : s->w_poly, s->w_poly, (size_t)1 << i, uint4{}, s->w_heq,
-                        (size_t)1 << (i - 1), reinterpret_cast<uint32_t*>(s->stage(i - 1) + 32), st, xp));
+      bf::FoldFixParams fp{};
+      fp.pi = (i == d - 1) ? s->first_pi() : s->pi_fold_out(i + 1);
+      fp.pi_out = s->pi_fold_out(i);
+      fp.leaves = s->pi_tree(i - 1);
+      fp.n_leaves = p->n_i(i) / 2;
+      fp.tlo = p->tw_host.lo[d - 1 - i];
+      fp.thi = p->tw_host.hi[d - 1 - i];
+      fp.poly_in = (i == d - 1) ? s->first_poly() : s->w_poly;
+      fp.poly_out = s->w_poly;
+      fp.half = (size_t)1 << i;
+      fp.heq = s->w_heq;
+      fp.next_half = (size_t)1 << (i - 1);
+      fp.acc = reinterpret_cast<uint32_t*>(s->stage(i - 1) + 32);
+      fp.xp = xp;
+      CU(bf::launch_fold_fix(fp, uint4{}, st));
     }
     {
       ProfScope ps(p->prof, st, P_TREE);

@@ -60,6 +60,27 @@ cudaError_t launch_fix(const uint4* in, uint4* out, size_t half, uint4 r, const 
                        uint32_t* acc, cudaStream_t st, const uint4* xp = nullptr);
 cudaError_t launch_fix_column(const uint4* in, size_t width, size_t col, uint4* out, size_t half, uint4 r,
                               cudaStream_t st, const uint4* xp = nullptr);
+// A round of open (i >= 1) in one launch: the fold of `pi` into `pi_out`
+// with the next round's leaves (launch_fold_leaves) and the fix of
+// `poly_in` into `poly_out` with the next round's reduction into `acc`
+// (launch_fix).  The challenge is *xp when xp is set, else r.
+struct FoldFixParams {
+  const uint4* pi;
+  uint4* pi_out;
+  uint4* leaves;
+  size_t n_leaves;
+  const uint4* tlo;
+  const uint4* thi;
+  const uint4* poly_in;
+  uint4* poly_out;
+  size_t half;
+  const uint4* heq;
+  size_t next_half;
+  uint32_t* acc;
+  const uint4* xp;
+  unsigned fold_blocks;  // set by the launcher
+};
+cudaError_t launch_fold_fix(const FoldFixParams& p, uint4 r, cudaStream_t st);
 cudaError_t launch_combine_rows(const uint4* rows, size_t nrows, size_t width, const uint4* scalars, uint4* out,
                                 cudaStream_t st);
 // The last `nvars` (<= kEvalTailMaxVars) fixes of MultiPoly::evaluate in one

@@ -532,6 +532,53 @@ __global__ void __launch_bounds__(256, 3) fix_kernel(const uint4* in, uint4* out
   }
 }
 
+// One round of open in one launch: blocks [0, fold_blocks) fold the
+// codeword and hash the next round's leaves (as fold_leaves_kernel), the
+// other blocks fix the sumcheck polynomial and reduce for the next round (as
+// fix_kernel).  Both read the round's challenge.
+__global__ void __launch_bounds__(128) fold_fix_kernel(FoldFixParams p, uint4 r) {
+  __shared__ uint4 scratch[32];
+  if (p.xp) r = *p.xp;
+  if (blockIdx.x < p.fold_blocks) {
+    const size_t stride = (size_t)p.fold_blocks * blockDim.x;
+    for (size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x; s < p.n_leaves; s += stride) {
+      uint4 f[2];
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const size_t t = 2 * s + k;
+        const uint4 tw = gf_add(p.tlo[t & 4095], p.thi[t >> 12]);
+        uint4 lo = p.pi[2 * t], hi = p.pi[2 * t + 1];
+        hi = gf_add(hi, lo);
+        lo = gf_add(lo, gf_mul(hi, tw));
+        f[k] = gf_add(lo, gf_mul(gf_add(hi, lo), r));
+        p.pi_out[t] = f[k];
+      }
+      store_digest(p.leaves, s, hash_pair(f[0], f[1]));
+    }
+    return;
+  }
+  const size_t b0 = (size_t)(blockIdx.x - p.fold_blocks) * blockDim.x + threadIdx.x;
+  const size_t stride = (size_t)(gridDim.x - p.fold_blocks) * blockDim.x;
+  uint4 acc = make_uint4(0, 0, 0, 0);
+  for (size_t b = b0; b < p.half; b += stride) {
+    const uint4 lo = p.poly_in[b], hi = p.poly_in[b + p.half];
+    const uint4 v = gf_add(lo, gf_mul(r, gf_add(hi, lo)));
+    p.poly_out[b] = v;
+    if (b < p.next_half) acc = gf_add(acc, gf_mul(p.heq[b], v));
+  }
+  acc = block_xor(acc, scratch);
+  if (threadIdx.x == 0) atomic_xor4(p.acc, acc);
+}
+
+cudaError_t launch_fold_fix(const FoldFixParams& p0, uint4 r, cudaStream_t st) {
+  FoldFixParams p = p0;
+  p.fold_blocks = grid_for(p.n_leaves, 128, 16);
+  const unsigned fix_blocks = grid_for(p.half, 128, 8);
+  fold_fix_kernel<<<p.fold_blocks + fix_blocks, 128, 0, st>>>(p, r);
+  COUNT_LAUNCH();
+  return cudaGetLastError();
+}
+
 cudaError_t launch_fix(const uint4* in, uint4* out, size_t half, uint4 r, const uint4* heq, size_t next_half,
                        uint32_t* acc, cudaStream_t st, const uint4* xp) {
   fix_kernel<<<grid_for(half, 256), 256, 0, st>>>(in, out, half, r, heq, next_half, acc, xp);
