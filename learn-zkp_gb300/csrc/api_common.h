@@ -7,6 +7,7 @@
 #include <cstdint>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -216,6 +217,7 @@ struct bf_pcs {
   bfapi::DevBuf eval_ws;                      // bf_eval scratch
   bfapi::PinnedBuf pinned;
   std::vector<std::unique_ptr<bfapi::PinnedBuf>> pinned_cache;  // staging kept between open sessions
+  std::mutex pinned_mu;                                          // guards pinned_cache (sessions on several threads)
   bfapi::Profiler prof;
   bf::Tune tune;  // launch shapes and thresholds (bf_pcs_autotune / bf_pcs_set_tune)
 

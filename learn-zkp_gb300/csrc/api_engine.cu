@@ -101,6 +101,7 @@ struct bf_engine {
   bool complete_stop = false;
   size_t mem_budget = 0, mem_used = 0;
   std::map<int, bf_pcs*> pcs_by_n;
+  std::mutex pcs_mu;  // pcs_by_n: bf_engine_proof_size may set a size up while the engine runs
   std::vector<cudaStream_t> streams;
   std::vector<int> free_slots;
   PinnedBuf pin;  // 128 bytes per slot: roots (64) + value (16)
@@ -126,13 +127,15 @@ size_t job_footprint(int n, int log2_c, bool device_input, size_t Q, size_t bloc
 }
 
 int get_pcs(bf_engine* e, int n, bf_pcs** out) {
+  std::lock_guard<std::mutex> lk(e->pcs_mu);
   auto it = e->pcs_by_n.find(n);
   if (it != e->pcs_by_n.end()) {
     *out = it->second;
     return BF_OK;
   }
   bf_pcs* p = nullptr;
-  TRY(bf_pcs_setup(e->device, e->lambda, e->log2_c, n, e->streams[0], &p));
+  // its own stream: a slot's stream may be in graph capture meanwhile
+  TRY(bf_pcs_setup(e->device, e->lambda, e->log2_c, n, nullptr, &p));
   e->pcs_by_n[n] = p;
   if (e->autotune_reps > 0) TRY(bf_pcs_autotune(p, e->autotune_reps, nullptr, 0));
   *out = p;
@@ -234,12 +237,12 @@ int build_plan(bf_engine* e, int slot, int n, std::unique_ptr<Plan>& out) {
   TRY(commit_alloc(p, pl->cm.get(), st));
   CU(pl->eval_ws.alloc_async(16 * (n > 0 ? ((size_t)1 << (n - 1)) : 1), p->pool, st));
   TRY(open_session_create(p, pl->cm.get(), st, &pl->sess));
-  const long long before = (long long)bf::launches_total();
+  const long long before = (long long)bf::launches_this_thread();  // completions launch meanwhile
   cudaGraph_t graph = nullptr;
   CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
   const int rc = capture_job(e, slot, pl.get());
   const cudaError_t ce = cudaStreamEndCapture(st, &graph);
-  pl->launches = (long long)bf::launches_total() - before;
+  pl->launches = (long long)bf::launches_this_thread() - before;
   bf::add_launches(-pl->launches);  // captured, not run
   if (rc < 0) {
     if (graph) cudaGraphDestroy(graph);

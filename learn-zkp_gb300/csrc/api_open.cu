@@ -91,6 +91,7 @@ struct bf_open_session {
     ws.release();
     if (pin) {
       // keep the pinned staging for the next session of this pcs
+      std::lock_guard<std::mutex> lk(p->pinned_mu);
       p->pinned_cache.push_back(std::move(pin));
     }
   }
@@ -163,12 +164,14 @@ int session_alloc(bf_open_session* s) {
   const size_t pin_bytes =
       std::max(res_off + align16(rec_bytes(d)) + sizeof(bf::OpenState),
                s->tail_in_off() + 48 * n_point + sizeof(bf::OpenState));
-  if (!p->pinned_cache.empty()) {
-    s->pin = std::move(p->pinned_cache.back());
-    p->pinned_cache.pop_back();
-  } else {
-    s->pin.reset(new PinnedBuf());
+  {
+    std::lock_guard<std::mutex> lk(p->pinned_mu);
+    if (!p->pinned_cache.empty()) {
+      s->pin = std::move(p->pinned_cache.back());
+      p->pinned_cache.pop_back();
+    }
   }
+  if (!s->pin) s->pin.reset(new PinnedBuf());
   CU(s->pin->ensure(pin_bytes));
   s->idx_pin = reinterpret_cast<uint64_t*>(s->pin->b() + 64 + 16 * (n_point + s->w));
   s->open_pin = reinterpret_cast<uint8_t*>(s->idx_pin + (p->Q + 1));

@@ -120,6 +120,7 @@ cudaError_t launch_prod_fix(uint4* const* out, const uint4* const* in, int k, si
                             size_t next_half, uint32_t* acc, cudaStream_t st, const uint4* xp = nullptr);
 
 unsigned long long launches_total();
+unsigned long long launches_this_thread();  // launched by the calling thread
 void count_launch();
 void add_launches(long long n);  // kernels run by a replayed CUDA graph (negative: captured, not run)
 // Function attributes (dynamic shared memory) set once per device, outside

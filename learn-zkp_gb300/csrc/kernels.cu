@@ -35,11 +35,18 @@ __device__ __forceinline__ uint64_t brev_bits64(uint64_t x, int bits) {
 __device__ __forceinline__ uint4 gf_one() { return make_uint4(1u, 0u, 0u, 0xc2000000u); }
 
 // Number of kernels this library has launched (all devices, all streams).
+// The per-thread count lets a graph capture learn how many kernels it holds
+// while other threads launch.
 static std::atomic<unsigned long long> g_launches{0};
+static thread_local unsigned long long t_launches = 0;
 unsigned long long launches_total() { return g_launches.load(); }
-void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+unsigned long long launches_this_thread() { return t_launches; }
+void count_launch() {
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  ++t_launches;
+}
 void add_launches(long long n) { g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed); }
-#define COUNT_LAUNCH() g_launches.fetch_add(1, std::memory_order_relaxed)
+#define COUNT_LAUNCH() count_launch()
 
 static int g_num_sms = 0;
 static int num_sms() {
