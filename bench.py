@@ -379,6 +379,57 @@ def run_sumcheck(bg, torch, device, cases=((2, 20), (3, 20), (2, 24), (3, 24)), 
     return out
 
 
+def run_verify(bg, device, log2_c, n=20, count=64, distinct=8, reps=5):
+    """Batched verify: `count` proofs of 2^n evaluations (`distinct` different
+    proofs, repeated) checked in one bf_verify_batch call, from host bytes to
+    result codes; beside it the oracle's verifier (C++ restatement of the
+    reference's CPU verify) over the same proofs on all host cores."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import oracle as O
+
+    pcs = bg.Basefold.setup(bg.BasefoldConfig(bg.BinaryReedSolomonCode(128, log2_c, n)), device=device)
+    items = []
+    for j in range(distinct):
+        data = bg.rand.random_elems((1 << n) + n, 6000 + j)
+        evals, point = data[: 1 << n], data[1 << n:]
+        comm = pcs.commit(evals)
+        ch = bg.GenericChallenger.keccak256()
+        ch.observe(comm.root)
+        values = pcs.eval(pcs.data(comm), point)
+        ch.observe_ext_slice(values)
+        proof = pcs.open(comm, [bg.PolyEvals(values, point)], ch.clone())
+        items.append((comm.root, values, point, ch.state(), proof))
+        comm.free()
+    items = [items[j % distinct] for j in range(count)]
+
+    def jobs():
+        return [(r, [bg.PolyEvals(v, p)], pf, bg.GenericChallenger.from_state(b)) for r, v, p, b, pf in items]
+
+    assert pcs.verify_batch(jobs()) == [0] * count
+    ts = []
+    for _ in range(reps):
+        js = jobs()
+        t = time.perf_counter()
+        res = pcs.verify_batch(js)
+        ts.append(time.perf_counter() - t)
+        assert res == [0] * count
+    t_gpu = sorted(ts)[len(ts) // 2]
+    O.lib()
+    cores = os.cpu_count() or 1
+    with ThreadPoolExecutor(cores) as ex:
+        t = time.perf_counter()
+        codes = list(ex.map(lambda it: O.verify(n, log2_c, it[0], it[2], it[1], it[3], it[4]), items))
+        t_cpu = time.perf_counter() - t
+    assert codes == [0] * count
+    return {"workload": f"{count} proofs of 2^{n} evaluations, blowup {1 << log2_c}, host proof bytes in, "
+                        "result codes out", "proof_bytes": len(items[0][4]),
+            "gpu_proofs_per_s": count / t_gpu, "gpu_ms": t_gpu * 1e3,
+            "cpu_baseline": {"proofs_per_s": count / t_cpu, "cores": cores, "kind": "port",
+                             "sample": f"the same {count} proofs, one per host thread at a time"},
+            "speedup": t_cpu / t_gpu}
+
+
 def served_cpu_reference(log2_c, size_range):
     """The served mix on the CPU reference path (C++ restatement, all host
     cores): one proof per size; sizes are uniform over the range, so the
@@ -512,12 +563,13 @@ def main():
     if tr and tr.get("bytes_per_node"):
         traffic = tr["bytes_per_node"] * nodes / max(tree_launches, 1)
     total_ms_classes = sum(v[0] for v in prof.values())
-    batched = served = sweep = sumcheck = None
+    batched = served = sweep = sumcheck = verify = None
     if ws == 1 and not args.no_extras:
         batched = run_batched(bg, torch, local, log2_c)
         served = run_served(bg, local, log2_c)
         sweep = run_commit_sweep(bg, torch, local)
         sumcheck = run_sumcheck(bg, torch, local)
+        verify = run_verify(bg, local, log2_c)
     cpu = None
     if not args.no_cpu_baseline and ws == 1:
         t = cpu_step_oracle(n, log2_c)
@@ -550,6 +602,7 @@ def main():
         "served": served,
         "commit_sweep": sweep,
         "sumcheck": sumcheck,
+        "verify": verify,
     }
     print(json.dumps(line), flush=True)
 

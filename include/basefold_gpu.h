@@ -226,6 +226,25 @@ int bf_eval_noalloc(const void* d_evals, int num_vars, const uint8_t* point, voi
 int bf_verify(const bf_pcs* pcs, const uint8_t root[32], const uint8_t* point, const uint8_t* values, size_t width,
               int n_evals, bf_challenger* ch, const uint8_t* proof, size_t proof_len);
 
+/* ---- PolyCommitScheme::verify of many proofs of one pcs at once: each job
+ * is one bf_verify call with n_evals = 1 (basefold.rs:234-324).  The
+ * transcripts are replayed on host threads; the Merkle paths and fold chains
+ * of every query run on the GPU (the pcs must be on a device).  Each job's
+ * `result` and challenger end exactly as bf_verify's would.  Returns BF_OK or
+ * a negative BF_ERR_* (nothing is verified then).  Calls on one pcs are
+ * serialized. */
+typedef struct bf_verify_job {
+  const uint8_t* root;        /* 32-byte commitment */
+  const uint8_t* point;       /* num_vars field elements */
+  const uint8_t* values;      /* width field elements */
+  size_t width;
+  bf_challenger* challenger;  /* the caller's transcript (observed root and values) */
+  const uint8_t* proof;
+  size_t proof_len;
+  int result;                 /* out: BF_VERIFY_* */
+} bf_verify_job;
+int bf_verify_batch(bf_pcs* pcs, bf_verify_job* jobs, size_t count);
+
 /* ---- Fiat–Shamir transcript: GenericChallenger<Polyval, Keccak256Hash>
  * (p3/src/challenger.rs:24-83) over Plonky3's HashChallenger. */
 /* GenericChallenger::new(initial_state) (challenger.rs:36-42); keccak256()

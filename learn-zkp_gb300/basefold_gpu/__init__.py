@@ -276,6 +276,32 @@ class Basefold:
         if rc != 0:
             raise BasefoldError(rc)
 
+    def verify_batch(self, items) -> list:
+        """verify (basefold.rs:234-324) of many proofs at once on the GPU.
+
+        `items` holds (comm, evals, proof, challenger) tuples as verify takes
+        them, one evaluation point each.  Returns one code per item: 0 when it
+        verifies, else the BasefoldError code verify would raise.  Every
+        challenger is advanced as verify advances it."""
+        from ._native import BfVerifyJob
+        items = list(items)
+        jobs = (BfVerifyJob * max(1, len(items)))()
+        keep = []
+        for j, (comm, evals, proof, challenger) in enumerate(items):
+            if len(evals) != 1:
+                raise ValueError("verify_batch takes exactly one PolyEvals per proof")
+            root = np.frombuffer(bytes(comm), dtype=np.uint8).copy()
+            pf = bytes(proof)  # read in place: no copy when it already is bytes
+            pt = evals[0].point if self.config.code.d else np.zeros((1, 16), np.uint8)
+            pt, vals = _elems(pt), _elems(evals[0].values)
+            keep += [root, pf, pt, vals]
+            jobs[j].root, jobs[j].point, jobs[j].values = root.ctypes.data, pt.ctypes.data, vals.ctypes.data
+            jobs[j].width, jobs[j].challenger = vals.shape[0], C.cast(challenger._h, C.c_void_p).value
+            jobs[j].proof = C.cast(C.c_char_p(pf), C.c_void_p).value if pf else None
+            jobs[j].proof_len = len(pf)
+        check(lib().bf_verify_batch(self._h, jobs, len(items)))
+        return [int(jobs[j].result) for j in range(len(items))]
+
     # -- standalone sumcheck on device-resident polynomials -------------------
     def prove_sumcheck_device(self, k: int, num_vars: int, dev_ptr: int, claim, challenger: GenericChallenger):
         out = np.zeros((num_vars * k + num_vars + k + 1, 16), dtype=np.uint8)

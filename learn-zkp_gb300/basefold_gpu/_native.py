@@ -20,7 +20,7 @@ EXPORTS = [
     "bf_profile_read", "bf_test_gf_mul", "bf_test_keccak_f", "bf_engine_create", "bf_engine_free",
     "bf_engine_proof_size", "bf_engine_prove", "bf_engine_start", "bf_engine_stop", "bf_engine_submit",
     "bf_engine_poll", "bf_eval_noalloc", "bf_pcs_autotune", "bf_pcs_get_tune", "bf_pcs_set_tune",
-    "bf_engine_autotune", "bf_engine_graphs", "bf_engine_stats",
+    "bf_engine_autotune", "bf_engine_graphs", "bf_engine_stats", "bf_verify_batch",
 ]
 
 BF_OK = 0
@@ -38,6 +38,14 @@ class BfJob(C.Structure):
         ("num_vars", C.c_int32), ("status", C.c_int32), ("evals", C.c_void_p), ("point", C.c_void_p),
         ("proof", C.c_void_p), ("proof_cap", C.c_size_t), ("proof_len", C.c_size_t), ("latency_ms", C.c_double),
         ("root", C.c_uint8 * 32), ("value", C.c_uint8 * 16),
+    ]
+
+
+class BfVerifyJob(C.Structure):
+    """bf_verify_job of include/basefold_gpu.h."""
+    _fields_ = [
+        ("root", C.c_void_p), ("point", C.c_void_p), ("values", C.c_void_p), ("width", C.c_size_t),
+        ("challenger", C.c_void_p), ("proof", C.c_void_p), ("proof_len", C.c_size_t), ("result", C.c_int32),
     ]
 
 
@@ -114,6 +122,7 @@ def lib():
         "bf_engine_autotune": ([vp, i], i),
         "bf_engine_graphs": ([vp, i], i),
         "bf_engine_stats": ([vp, C.POINTER(C.c_double), i], i),
+        "bf_verify_batch": ([vp, C.POINTER(BfVerifyJob), sz], i),
     }
     for name, (args, res) in decl.items():
         f = getattr(L, name)

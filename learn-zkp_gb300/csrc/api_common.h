@@ -220,6 +220,10 @@ struct bf_pcs {
   std::mutex pinned_mu;                                          // guards pinned_cache (sessions on several threads)
   bfapi::Profiler prof;
   bf::Tune tune;  // launch shapes and thresholds (bf_pcs_autotune / bf_pcs_set_tune)
+  // bf_verify_batch staging (grow-only): proofs and query records in, flags out
+  bfapi::PinnedBuf verify_pin;
+  bfapi::DevBuf verify_dev;
+  std::mutex verify_mu;
 
   size_t n_d() const { return (size_t)1 << L; }
   size_t c() const { return (size_t)1 << log2_c; }

@@ -184,6 +184,43 @@ struct TailParams {
 };
 cudaError_t launch_open_tail(const TailParams& p, cudaStream_t st);
 
+// ---- Basefold::verify of many proofs (basefold.rs:284-320) on the device.
+// Offsets are byte offsets into `blob`, multiples of 8.  All proofs share one
+// pcs (num_vars d, blowup 2^log2_c) and are checked query by query.
+struct VerifyJob {
+  uint64_t root;        // 32-byte commitment
+  uint64_t pi_comms;    // the proof's d folded-codeword roots, 32 bytes apart
+  uint64_t final_poly;  // the proof's final polynomial (one element)
+  uint64_t challenges;  // round challenges in round order (16 bytes each)
+  uint64_t scalars;     // width > 1: the eq scalars of the columns
+  uint32_t width;
+  uint32_t pad;
+};
+struct VerifyQuery {
+  uint32_t job;
+  uint32_t pad;
+  uint64_t idx;     // sampled position in the codeword
+  uint64_t leaves;  // the opened row (16*width bytes)
+  uint64_t path;    // its L sibling digests
+};
+struct VerifyRound {
+  uint64_t sibling;  // the opened sibling element of round k
+  uint64_t path;     // its log2 n_i sibling digests
+};
+struct VerifyParams {
+  const uint8_t* blob;
+  const VerifyJob* jobs;
+  const VerifyQuery* queries;  // nq
+  const VerifyRound* rounds;   // nq * d, query-major
+  const TwiddleView* tw;
+  uint4* pairs;                // nq * d * 2 elements (scratch)
+  uint8_t* final_bad;          // nq: fold chain != final polynomial
+  uint8_t* path_bad;           // (d + 1) * nq, level-major: level 0 = codeword path, 1 + k = round k
+  uint32_t nq;
+  int d, log2_c;
+};
+cudaError_t launch_verify(const VerifyParams& p, cudaStream_t st);
+
 // Test hooks.
 cudaError_t launch_test_mul(const uint4* a, const uint4* b, uint4* out, size_t n, cudaStream_t st);
 cudaError_t launch_test_keccak(uint2* states, size_t n, cudaStream_t st);

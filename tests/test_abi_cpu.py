@@ -92,6 +92,11 @@ def test_gpu_entry_points_refuse_verifier_only_object(built_lib):
     bg = built_lib
     pcs = _setup_verifier(bg, 4, 1)
     try:
+        pcs.verify_batch([])
+        raise AssertionError("batched verify ran without a device")
+    except bg.BasefoldGpuError as e:
+        assert e.code == -1
+    try:
         pcs.commit(rand.random_elems(16, 1))
         raise AssertionError("commit ran without a device")
     except bg.BasefoldGpuError as e:
