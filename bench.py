@@ -43,6 +43,8 @@ def parse():
     ap.add_argument("--profile-only", action="store_true", help="warmup + steps, no JSON extras (for ncu)")
     ap.add_argument("--profile-sumcheck", type=int, nargs=2, metavar=("K", "N"),
                     help="one product sumcheck of K polys over 2^N points, nothing else (for ncu)")
+    ap.add_argument("--profile-verify", type=int, nargs=2, metavar=("N", "COUNT"),
+                    help="one batched verify of COUNT proofs of 2^N evaluations, nothing else (for ncu)")
     return ap.parse_args()
 
 
@@ -379,18 +381,13 @@ def run_sumcheck(bg, torch, device, cases=((2, 20), (3, 20), (2, 24), (3, 24)), 
     return out
 
 
-def run_verify(bg, device, log2_c, n=20, count=64, distinct=8, reps=5):
-    """Batched verify: `count` proofs of 2^n evaluations (`distinct` different
-    proofs, repeated) checked in one bf_verify_batch call, from host bytes to
-    result codes; beside it the oracle's verifier (C++ restatement of the
-    reference's CPU verify) over the same proofs on all host cores."""
-    from concurrent.futures import ThreadPoolExecutor
-
-    from oracle import oracle as O
-
+def verify_workload(bg, device, log2_c, n, count, distinct=8):
+    """`distinct` proofs of 2^n evaluations (the reference harness: commit,
+    observe the root, evaluate, observe the values, open), repeated to
+    `count`; jobs() gives fresh verify_batch arguments."""
     pcs = bg.Basefold.setup(bg.BasefoldConfig(bg.BinaryReedSolomonCode(128, log2_c, n)), device=device)
     items = []
-    for j in range(distinct):
+    for j in range(min(distinct, count)):
         data = bg.rand.random_elems((1 << n) + n, 6000 + j)
         evals, point = data[: 1 << n], data[1 << n:]
         comm = pcs.commit(evals)
@@ -401,10 +398,24 @@ def run_verify(bg, device, log2_c, n=20, count=64, distinct=8, reps=5):
         proof = pcs.open(comm, [bg.PolyEvals(values, point)], ch.clone())
         items.append((comm.root, values, point, ch.state(), proof))
         comm.free()
-    items = [items[j % distinct] for j in range(count)]
+    items = [items[j % len(items)] for j in range(count)]
 
     def jobs():
         return [(r, [bg.PolyEvals(v, p)], pf, bg.GenericChallenger.from_state(b)) for r, v, p, b, pf in items]
+
+    return pcs, items, jobs
+
+
+def run_verify(bg, device, log2_c, n=20, count=64, distinct=8, reps=5):
+    """Batched verify: `count` proofs of 2^n evaluations (`distinct` different
+    proofs, repeated) checked in one bf_verify_batch call, from host bytes to
+    result codes; beside it the oracle's verifier (C++ restatement of the
+    reference's CPU verify) over the same proofs on all host cores."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import oracle as O
+
+    pcs, items, jobs = verify_workload(bg, device, log2_c, n, count, distinct)
 
     assert pcs.verify_batch(jobs()) == [0] * count
     ts = []
@@ -473,6 +484,11 @@ def main():
         sc_pcs.prove_sumcheck_device(k, ns, polys.data_ptr(), bg.rand.random_elems(1, 77),
                                      bg.GenericChallenger(b"sumcheck"))
         torch.cuda.synchronize()
+        return
+    if args.profile_verify:
+        vn, vcount = args.profile_verify
+        vpcs, _, vjobs = verify_workload(bg, local, args.log2_c, vn, vcount)
+        assert vpcs.verify_batch(vjobs()) == [0] * vcount
         return
     stream = torch.cuda.current_stream()
     n, log2_c = args.n, args.log2_c

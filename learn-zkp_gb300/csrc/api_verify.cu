@@ -282,9 +282,7 @@ struct VJob {
   std::vector<uint64_t> idx;   // query positions
   size_t nq_dev = 0;
   int after = BF_VERIFY_OK;  // status of query nq_dev, decided by its structure (or OK: none left)
-  // device image offsets
-  uint64_t elems = 0, proof = 0;
-  uint32_t job_slot = 0, q0 = 0;
+  uint64_t elems = 0, proof = 0;  // device image offsets
 };
 
 // The transcript part of bf_verify for one job: the same observations,
@@ -399,78 +397,88 @@ extern "C" int bf_verify_batch(bf_pcs* p, bf_verify_job* jobs, size_t count) {
   std::lock_guard<std::mutex> lk(p->verify_mu);
   DeviceGuard g(p->device);
   const int d = p->d;
-  std::vector<VJob> v(count);
-  parallel_jobs(count, [&](size_t j) { verify_host_part(p, jobs[j], v[j]); });
-
-  // device image: [jobs | queries | rounds | elements | proofs], then the flags
-  uint64_t nj = 0, nq = 0;
-  for (auto& x : v)
-    if (x.status < 0) {
-      x.job_slot = (uint32_t)nj++;
-      x.q0 = (uint32_t)nq;
-      nq += x.nq_dev;
-    }
+  const uint64_t Q = p->Q;
+  // Device image: [jobs | queries | rounds | elements | proofs], then scratch
+  // and flags.  Every job owns Q query slots and fixed element and proof
+  // ranges, so one pass over the jobs fills it; slots a job does not use
+  // (queries decided on the host) are marked inactive.
+  const uint64_t nq = count * Q;
   if (nq > 0xffffffffull / (uint64_t)(d + 2)) return fail(BF_ERR_ARG, "too many queries in one batch");
+  std::vector<VJob> v(count);
   const uint64_t off_jobs = 0;
-  const uint64_t off_queries = align16(off_jobs + sizeof(bf::VerifyJob) * nj);
+  const uint64_t off_queries = align16(off_jobs + sizeof(bf::VerifyJob) * count);
   const uint64_t off_rounds = align16(off_queries + sizeof(bf::VerifyQuery) * nq);
   uint64_t cur = align16(off_rounds + sizeof(bf::VerifyRound) * nq * d);
-  for (size_t j = 0; j < count; ++j)
-    if (v[j].status < 0) {
-      v[j].elems = cur;
-      cur += 32 + 16 * (uint64_t)d + (jobs[j].width > 1 ? 16 * (uint64_t)jobs[j].width : 0);
-    }
-  for (size_t j = 0; j < count; ++j)
-    if (v[j].status < 0) {
-      cur = align16(cur);
-      v[j].proof = cur;
-      cur += jobs[j].proof_len;
-    }
-  const uint64_t image = align16(cur);
+  for (size_t j = 0; j < count; ++j) {
+    v[j].elems = cur;
+    cur += 32 + 16 * (uint64_t)d + (jobs[j].width > 1 ? 16 * (uint64_t)jobs[j].width : 0);
+  }
+  const uint64_t header = align16(cur);  // what the kernels read besides the proofs
+  cur = header;
+  for (size_t j = 0; j < count; ++j) {
+    v[j].proof = cur;
+    cur = align16(cur + jobs[j].proof_len);
+  }
+  const uint64_t image = cur;
   const uint64_t off_pairs = image, off_flags = off_pairs + 32 * nq * d;
   const uint64_t flag_bytes = nq * (uint64_t)(d + 2);
   const uint64_t dev_bytes = align16(off_flags + flag_bytes);
   if (nq > 0) {
     CU(p->verify_pin.ensure(image + align16(flag_bytes)));
     if (p->verify_dev.bytes < dev_bytes) CU(p->verify_dev.alloc(dev_bytes));
-    uint8_t* h = p->verify_pin.b();
-    parallel_jobs(count, [&](size_t j) {
-      const VJob& x = v[j];
-      if (x.status >= 0) return;
-      const bf_verify_job& jb = jobs[j];
-      const Layout& lay = x.lay;
-      bf::VerifyJob rec{};
-      rec.root = x.elems;
-      rec.challenges = x.elems + 32;
-      rec.scalars = x.elems + 32 + 16 * (uint64_t)d;
-      rec.pi_comms = x.proof + lay.pi_off;
-      rec.final_poly = x.proof + lay.final_off;
-      rec.width = (uint32_t)jb.width;
-      std::memcpy(h + off_jobs + sizeof(rec) * x.job_slot, &rec, sizeof(rec));
+  }
+  uint8_t* h = p->verify_pin.b();
+  uint8_t* dv = reinterpret_cast<uint8_t*>(p->verify_dev.p);
+  cudaStream_t st = p->stream;
+  std::vector<cudaError_t> copy_err(count, cudaSuccess);
+  parallel_jobs(count, [&](size_t j) {
+    VJob& x = v[j];
+    const bf_verify_job& jb = jobs[j];
+    verify_host_part(p, jb, x);
+    if (Q == 0) return;
+    const Layout& lay = x.lay;
+    const size_t active = x.status < 0 ? x.nq_dev : 0;
+    bf::VerifyJob rec{};
+    rec.root = x.elems;
+    rec.challenges = x.elems + 32;
+    rec.scalars = x.elems + 32 + 16 * (uint64_t)d;
+    rec.pi_comms = x.proof + (active ? lay.pi_off : 0);
+    rec.final_poly = x.proof + (active ? lay.final_off : 0);
+    rec.width = (uint32_t)jb.width;
+    std::memcpy(h + off_jobs + sizeof(rec) * j, &rec, sizeof(rec));
+    if (active) {
       std::memcpy(h + x.elems, jb.root, 32);
       for (int k = 0; k < d; ++k) bfh::store(h + x.elems + 32 + 16 * k, x.rounds_x[k]);
       if (jb.width > 1)
         for (size_t w = 0; w < jb.width; ++w) bfh::store(h + rec.scalars + 16 * w, x.scalars[w]);
-      if (jb.proof_len) std::memcpy(h + x.proof, jb.proof, jb.proof_len);
-      for (size_t q = 0; q < x.nq_dev; ++q) {
+    }
+    for (uint64_t q = 0; q < Q; ++q) {
+      bf::VerifyQuery vq{};
+      vq.job = q < active ? (uint32_t)j : bf::kVerifyInactive;
+      const uint64_t gq = j * Q + q;
+      if (q < active) {
         const Layout::Open& o = lay.open[q];
-        bf::VerifyQuery vq{};
-        vq.job = x.job_slot;
         vq.idx = x.idx[q];
         vq.leaves = x.proof + o.leaves;
         vq.path = x.proof + o.path;
-        const uint64_t gq = x.q0 + q;
-        std::memcpy(h + off_queries + sizeof(vq) * gq, &vq, sizeof(vq));
         for (int k = 0; k < d; ++k) {
           const Layout::Ext& e = lay.ext[o.ext0 + k];
           bf::VerifyRound vr{x.proof + e.sib, x.proof + e.path};
           std::memcpy(h + off_rounds + sizeof(vr) * (gq * d + k), &vr, sizeof(vr));
         }
       }
-    });
-    cudaStream_t st = p->stream;
-    uint8_t* dv = reinterpret_cast<uint8_t*>(p->verify_dev.p);
-    CU(cudaMemcpyAsync(dv, h, image, cudaMemcpyHostToDevice, st));
+      std::memcpy(h + off_queries + sizeof(vq) * gq, &vq, sizeof(vq));
+    }
+    if (active && jb.proof_len) {  // stage the proof and start its copy while other jobs are prepared
+      std::memcpy(h + x.proof, jb.proof, jb.proof_len);
+      copy_err[j] = cudaSetDevice(p->device);  // worker threads start on device 0
+      if (copy_err[j] == cudaSuccess)
+        copy_err[j] = cudaMemcpyAsync(dv + x.proof, h + x.proof, jb.proof_len, cudaMemcpyHostToDevice, st);
+    }
+  });
+  for (cudaError_t e : copy_err) CU(e);
+  if (nq > 0) {
+    CU(cudaMemcpyAsync(dv, h, header, cudaMemcpyHostToDevice, st));
     bf::VerifyParams vp{};
     vp.blob = dv;
     vp.jobs = reinterpret_cast<const bf::VerifyJob*>(dv + off_jobs);
@@ -489,11 +497,12 @@ extern "C" int bf_verify_batch(bf_pcs* p, bf_verify_job* jobs, size_t count) {
     CU(cudaStreamSynchronize(st));
     // per job, the first query that fails decides (basefold.rs:284-322 checks
     // them in order): a bad path is an Mmcs error, a bad chain InvalidQuery
-    for (auto& x : v) {
+    for (size_t j = 0; j < count; ++j) {
+      VJob& x = v[j];
       if (x.status >= 0) continue;
       x.status = x.after;
       for (size_t q = 0; q < x.nq_dev; ++q) {
-        const uint64_t gq = x.q0 + q;
+        const uint64_t gq = j * Q + q;
         bool path_bad = false;
         for (int l = 0; l <= d && !path_bad; ++l) path_bad = flags[nq + (uint64_t)l * nq + gq] != 0;
         if (path_bad) {

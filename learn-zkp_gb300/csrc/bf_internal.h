@@ -196,8 +196,9 @@ struct VerifyJob {
   uint32_t width;
   uint32_t pad;
 };
+constexpr uint32_t kVerifyInactive = 0xffffffffu;  // a query slot with nothing to check
 struct VerifyQuery {
-  uint32_t job;
+  uint32_t job;     // kVerifyInactive: an unused slot
   uint32_t pad;
   uint64_t idx;     // sampled position in the codeword
   uint64_t leaves;  // the opened row (16*width bytes)

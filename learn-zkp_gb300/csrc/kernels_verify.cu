@@ -54,10 +54,40 @@ __device__ __forceinline__ bool digest_eq(const Digest& a, const Digest& b) {
 
 __device__ __forceinline__ bool elem_eq(uint4 a, uint4 b) { return a.x == b.x && a.y == b.y && a.z == b.z && a.w == b.w; }
 
+// Leaf of a row of `width` > 1 elements: keccak256 of its 16*width bytes,
+// any number of 136-byte (17-lane) blocks; lanes are indexed statically so
+// the state stays in registers.
+__device__ __forceinline__ Digest hash_row(const uint8_t* blob, uint64_t off, uint32_t width) {
+  uint2 s[25];
+#pragma unroll
+  for (int k = 0; k < 25; ++k) s[k] = make_uint2(0, 0);
+  const uint2* row = reinterpret_cast<const uint2*>(blob + off);
+  const uint64_t lanes = 2ull * width;
+  for (uint64_t k = 0;; k += 17) {
+    const uint64_t left = lanes - k;  // message lanes from this block on
+#pragma unroll
+    for (int r = 0; r < 17; ++r) {
+      if ((uint64_t)r < left) s[r] = kx2(s[r], row[k + r]);
+      if ((uint64_t)r == left) s[r].x ^= 0x01u;  // pad10*1 starts in this block
+    }
+    if (left < 17) {
+      s[16].y ^= 0x80000000u;
+      keccak_f1600(s);
+      break;
+    }
+    keccak_f1600(s);
+  }
+  return digest_interleaved(digest_from_state(s));
+}
+
 __global__ void __launch_bounds__(128) verify_fold_kernel(VerifyParams P) {
   const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= P.nq) return;
   const VerifyQuery Q = P.queries[q];
+  if (Q.job == kVerifyInactive) {
+    P.final_bad[q] = 0;
+    return;
+  }
   const VerifyJob J = P.jobs[Q.job];
   const uint8_t* blob = P.blob;
   uint4 folded;
@@ -95,6 +125,10 @@ __global__ void __launch_bounds__(128) verify_path_kernel(VerifyParams P) {
   if (t >= total) return;
   const uint32_t level = (uint32_t)(t / P.nq), q = (uint32_t)(t % P.nq);
   const VerifyQuery Q = P.queries[q];
+  if (Q.job == kVerifyInactive) {
+    P.path_bad[t] = 0;
+    return;
+  }
   const VerifyJob J = P.jobs[Q.job];
   const uint8_t* blob = P.blob;
   Digest cur, root;
@@ -105,27 +139,7 @@ __global__ void __launch_bounds__(128) verify_path_kernel(VerifyParams P) {
     index = Q.idx;
     path = Q.path;
     root = load_digest_bytes(blob, J.root);
-    if (J.width == 1) {
-      cur = hash_elem(load_elem8(blob, Q.leaves));
-    } else {
-      uint2 s[25];
-#pragma unroll
-      for (int k = 0; k < 25; ++k) s[k] = make_uint2(0, 0);
-      const uint2* row = reinterpret_cast<const uint2*>(blob + Q.leaves);
-      const uint64_t lanes = 2ull * J.width;
-      uint64_t k = 0;
-      for (; k + 17 <= lanes; k += 17) {  // full 136-byte blocks
-        for (int r = 0; r < 17; ++r) s[r] = kx2(s[r], row[k + r]);
-        keccak_f1600(s);
-      }
-      const int rem = (int)(lanes - k);
-      for (int r = 0; r < rem; ++r) s[r] = kx2(s[r], row[k + r]);
-      for (int r = 0; r < 17; ++r)
-        if (r == rem) s[r].x ^= 0x01u;
-      s[16].y ^= 0x80000000u;
-      keccak_f1600(s);
-      cur = digest_interleaved(digest_from_state(s));
-    }
+    cur = J.width == 1 ? hash_elem(load_elem8(blob, Q.leaves)) : hash_row(blob, Q.leaves, J.width);
   } else {  // folded codeword of round k: leaf = keccak256(values[0] || values[1])
     const int k = (int)level - 1;
     log_h = P.log2_c + P.d - 1 - k;
@@ -137,7 +151,14 @@ __global__ void __launch_bounds__(128) verify_path_kernel(VerifyParams P) {
   }
   for (int b = 0; b < log_h; ++b) {
     const Digest sib = load_digest_bytes(blob, path + 32ull * b);
-    cur = ((index >> b) & 1) ? hash_node(sib, cur) : hash_node(cur, sib);
+    // the side is picked by selects, not a branch: threads of a warp differ in it
+    const bool right = ((index >> b) & 1) != 0;
+    Digest l, r;
+    l.lo = right ? sib.lo : cur.lo;
+    l.hi = right ? sib.hi : cur.hi;
+    r.lo = right ? cur.lo : sib.lo;
+    r.hi = right ? cur.hi : sib.hi;
+    cur = hash_node(l, r);
   }
   P.path_bad[t] = digest_eq(cur, root) ? 0 : 1;
 }
