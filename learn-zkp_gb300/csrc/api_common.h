@@ -165,7 +165,7 @@ int commit_alloc(bf_pcs* p, bf_commitment* cm, cudaStream_t st);
 // With fork_trees (and st the pcs's own stream) the codeword tree and the
 // first folded-codeword tree are built concurrently on the pcs's second stream.
 int commit_enqueue(bf_pcs* p, bf_commitment* cm, const uint4* data, cudaStream_t st, uint8_t* roots_pin,
-                   bool fork_trees = false);
+                   bool fork_trees = false, const cudaEvent_t* slice_ready = nullptr, int slices = 0);
 // The value lands in value_pin; *value_dev (when given) receives where it
 // lives on the device.  With point_dev the coordinates are read from device
 // memory at run time (for graph capture), else taken from the host `point`.
@@ -207,6 +207,10 @@ struct bf_pcs {
   bool own_stream = false;
   cudaStream_t aux = nullptr;  // second stream for independent work of one commit
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // bf_commit copies host evaluations in slices on `aux`; the first NTT pass
+  // starts on each slice when its event completes
+  static constexpr int kH2DSlices = 8;
+  cudaEvent_t slice_ev[kH2DSlices] = {};
   // Commitments and open sessions draw their buffers from this pool; it keeps
   // freed memory for reuse instead of returning it to the driver.
   cudaMemPool_t pool = nullptr;

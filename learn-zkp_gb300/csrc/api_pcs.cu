@@ -160,6 +160,8 @@ bf_pcs::~bf_pcs() {
   if (aux) cudaStreamDestroy(aux);
   if (ev_fork) cudaEventDestroy(ev_fork);
   if (ev_join) cudaEventDestroy(ev_join);
+  for (cudaEvent_t e : slice_ev)
+    if (e) cudaEventDestroy(e);
 }
 
 // ---------------------------------------------------------------------------
@@ -266,7 +268,7 @@ int commit_alloc(bf_pcs* p, bf_commitment* cm, cudaStream_t st) {
 // (width 1) the first folded-codeword root are copied to roots_pin[0..64)
 // (pinned) when the stream reaches that point.
 int commit_enqueue(bf_pcs* p, bf_commitment* cm, const uint4* data, cudaStream_t st, uint8_t* roots_pin,
-                   bool fork_trees) {
+                   bool fork_trees, const cudaEvent_t* slice_ready, int slices) {
   const size_t nd = p->n_d(), w = cm->width;
   // For width 1 the first open round commits the codeword itself (as pairs),
   // so that tree is built here; wider data is first combined in open.
@@ -279,7 +281,7 @@ int commit_enqueue(bf_pcs* p, bf_commitment* cm, const uint4* data, cudaStream_t
     // encode; for width 1 and d >= 1 the last NTT pass also hashes the leaves
     ProfScope ps(p->prof, st, P_ENCODE);
     CU(bf::launch_encode(data, cw, p->d, p->log2_c, w, p->tw_view.as<bf::TwiddleView>(), st,
-                         pairs ? tree : nullptr, pairs ? pit : nullptr, p->tune));
+                         pairs ? tree : nullptr, pairs ? pit : nullptr, p->tune, slice_ready, slices));
   }
   if (!pairs) {
     ProfScope ps(p->prof, st, P_LEAVES);
@@ -357,8 +359,9 @@ int eval_enqueue(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, uint4
 
 namespace {
 
-int commit_device(bf_pcs* p, bf_commitment* cm, const uint4* data) {
-  TRY(commit_enqueue(p, cm, data, p->stream, p->pinned.b(), true));
+int commit_device(bf_pcs* p, bf_commitment* cm, const uint4* data, const cudaEvent_t* slice_ready = nullptr,
+                  int slices = 0) {
+  TRY(commit_enqueue(p, cm, data, p->stream, p->pinned.b(), true, slice_ready, slices));
   CU(cudaStreamSynchronize(p->stream));
   p->prof.drain();
   bfh::digest_from_interleaved(p->pinned.b(), cm->root);  // tree roots are stored interleaved
@@ -422,6 +425,7 @@ int bf_pcs_setup(int device, int lambda, int log2_c, int num_vars, void* stream,
   CU(cudaStreamCreateWithFlags(&p->aux, cudaStreamNonBlocking));
   CU(cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming));
   CU(cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming));
+  for (cudaEvent_t& e : p->slice_ev) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   TRY(build_twiddles(p.get()));
   bf::init_kernel_attributes();
   CU(p->pinned.ensure(4096));
@@ -468,8 +472,23 @@ int bf_commit(bf_pcs* p, const uint8_t* evals, size_t width, bf_commitment** out
   cm->width = width;
   const size_t n = (size_t)1 << p->d;
   CU(cm->data.alloc_async(16 * n * width, p->pool, p->stream));
-  CU(cudaMemcpyAsync(cm->data.p, evals, 16 * n * width, cudaMemcpyHostToDevice, p->stream));
-  TRY(commit_device(p, cm.get(), cm->data.as<uint4>()));
+  if (p->d >= 16) {
+    // copy in slices on the second stream; the first NTT pass takes each
+    // slice as it lands (pinned `evals` overlap the copy with the pass)
+    const int S = bf_pcs::kH2DSlices;
+    const size_t slice = 16 * (n / S) * width;
+    CU(cudaEventRecord(p->ev_fork, p->stream));  // the allocation
+    CU(cudaStreamWaitEvent(p->aux, p->ev_fork, 0));
+    for (int k = 0; k < S; ++k) {
+      CU(cudaMemcpyAsync(cm->data.as<uint8_t>() + k * slice, evals + k * slice, slice, cudaMemcpyHostToDevice,
+                         p->aux));
+      CU(cudaEventRecord(p->slice_ev[k], p->aux));
+    }
+    TRY(commit_device(p, cm.get(), cm->data.as<uint4>(), p->slice_ev, S));
+  } else {
+    CU(cudaMemcpyAsync(cm->data.p, evals, 16 * n * width, cudaMemcpyHostToDevice, p->stream));
+    TRY(commit_device(p, cm.get(), cm->data.as<uint4>()));
+  }
   if (root) std::memcpy(root, cm->root, 32);
   *out = cm.release();
   return BF_OK;

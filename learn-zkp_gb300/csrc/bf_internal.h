@@ -35,9 +35,13 @@ bool tune_valid(const Tune& t);
 // `tw` points to a TwiddleView in device memory.  When `leaves` and
 // `pair_leaves` are given (n >= 1), the last pass also writes the codeword
 // leaves and the first folded-codeword leaves.
+// With `slices` > 0, slice k of the input (rows [k N/slices, (k+1) N/slices))
+// is ready once slice_ready[k] has completed: the first pass waits for each
+// slice before the blocks that read it.
 cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t width, const TwiddleView* tw,
                           cudaStream_t st, uint4* leaves = nullptr, uint4* pair_leaves = nullptr,
-                          const Tune& tune = Tune());
+                          const Tune& tune = Tune(), const cudaEvent_t* slice_ready = nullptr,
+                          int slices = 0);
 cudaError_t launch_leaves_elem(const uint4* cw, uint4* leaves, size_t n, size_t width, cudaStream_t st);
 cudaError_t launch_leaves_pair(const uint4* pi, uint4* leaves, size_t n, cudaStream_t st);
 // Build every level above `leaves` (n leaves, power of two); levels are stored

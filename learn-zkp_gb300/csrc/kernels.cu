@@ -82,6 +82,9 @@ static unsigned grid_for(size_t n, int threads, int per_sm = 8) {
 struct PassParams {
   int n, s_lo, T, first;
   int width;  // row width of m and cw; blockIdx.y is the column
+  // First pass: this launch covers the input tiles [tile0, tile0 + ntiles)
+  // (tile c = input rows [c 2^T, (c+1) 2^T)) of every coset.
+  uint32_t tile0, ntiles;
   // Last pass only: also hash the codeword leaves H(cw[q]) and the first
   // folded-codeword leaves H(cw[2s] || cw[2s+1]) from the tile in shared
   // memory (null: no hashing).  The hashing is integer-ALU work and the
@@ -97,8 +100,14 @@ __global__ void __launch_bounds__(512) ntt_pass_kernel(const uint4* __restrict__
   extern __shared__ uint4 sm[];
   const int n = p.n, T = p.T, s_lo = p.s_lo;
   const uint32_t tiles_per_coset = 1u << (n - T);
-  const uint32_t j = blockIdx.x >> (n - T);
-  const uint32_t rem = blockIdx.x & (tiles_per_coset - 1);
+  uint32_t j, rem;
+  if (p.first) {  // block -> (coset, input tile c); the tile's butterflies sit at u = bitrev(c)
+    j = blockIdx.x / p.ntiles;
+    rem = brev_bits(p.tile0 + blockIdx.x % p.ntiles, s_lo);
+  } else {
+    j = blockIdx.x >> (n - T);
+    rem = blockIdx.x & (tiles_per_coset - 1);
+  }
   const uint32_t u = rem & ((1u << s_lo) - 1u);
   const uint32_t hi = rem >> s_lo;
   const uint32_t tsize = 1u << T;
@@ -178,7 +187,8 @@ bool tune_valid(const Tune& t) {
 }
 
 cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t width, const TwiddleView* tw,
-                          cudaStream_t st, uint4* leaves, uint4* pair_leaves, const Tune& tune) {
+                          cudaStream_t st, uint4* leaves, uint4* pair_leaves, const Tune& tune,
+                          const cudaEvent_t* slice_ready, int slices) {
   if (width == 0 || width > 65535 || (width != 1 && (leaves || pair_leaves))) return cudaErrorInvalidValue;
   if (!tune_valid(tune)) return cudaErrorInvalidValue;
   const size_t c = (size_t)1 << log2_c;
@@ -210,16 +220,31 @@ cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t w
     const bool last = (pidx == passes - 1);
     p.leaves = last ? leaves : nullptr;
     p.pair_leaves = last ? pair_leaves : nullptr;
-    const dim3 grid((unsigned)(c << (n - T)), (unsigned)width);
     // one butterfly per thread and layer at most: 2^(T-1) threads, >= one warp
     const int threads = std::max(32, std::min(tune.ntt_threads, 1 << (T - 1)));
-    if (p.leaves)
-      ntt_pass_kernel<true><<<grid, threads, sizeof(uint4) << T, st>>>(m, cw, p, tw);
-    else
-      ntt_pass_kernel<false><<<grid, threads, sizeof(uint4) << T, st>>>(m, cw, p, tw);
-    COUNT_LAUNCH();
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
+    const uint32_t tiles = 1u << (n - T);
+    // the first pass may start on each slice of the input as it arrives
+    const int pieces = (p.first && slices > 0 && tiles >= (uint32_t)slices) ? slices : 1;
+    if (p.first && slices > 0 && pieces == 1) {
+      cudaError_t e = cudaStreamWaitEvent(st, slice_ready[slices - 1], 0);  // copies are in order
+      if (e != cudaSuccess) return e;
+    }
+    for (int piece = 0; piece < pieces; ++piece) {
+      if (pieces > 1) {
+        cudaError_t e = cudaStreamWaitEvent(st, slice_ready[piece], 0);
+        if (e != cudaSuccess) return e;
+      }
+      p.ntiles = p.first ? tiles / pieces : tiles;
+      p.tile0 = p.first ? p.ntiles * piece : 0;
+      const dim3 grid((unsigned)(c * p.ntiles), (unsigned)width);
+      if (p.leaves)
+        ntt_pass_kernel<true><<<grid, threads, sizeof(uint4) << T, st>>>(m, cw, p, tw);
+      else
+        ntt_pass_kernel<false><<<grid, threads, sizeof(uint4) << T, st>>>(m, cw, p, tw);
+      COUNT_LAUNCH();
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+    }
     top -= T;
   }
   return cudaSuccess;
