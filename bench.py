@@ -594,6 +594,13 @@ def main():
                          "all host threads; the Rust reference cannot be built here)"}
         if served is not None:
             served["cpu_baseline"] = served_cpu_reference(log2_c, served["size_range"])
+    clocks = clk.summary()
+    perms_per_s = (nodes / (tree_ms / 1e3)) if tree_ms else None
+    # the integer-ALU roofline of the same kernels: 60 ALU thread-ops/clk/SM
+    # (LOP3/SHF, measured on GB300) x SMs x SM clock, over 4116 instructions
+    # per Keccak-f on interleaved lanes (ncu, level_kernel)
+    num_sms = bg.device_info(local)["num_sms"]
+    alu_peak = 60.0 * num_sms * (clocks.get("sm_mhz") or 2070.0) * 1e6 / 4116.0
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -603,15 +610,20 @@ def main():
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                      "kernel": "level_kernel+tree_top_kernel (Merkle levels, keccak256 of 64-byte nodes)",
                      "peak_source": f"{peak_kind} hbm_gbs",
-                     "note": "Keccak-bound (integer pipes), not HBM-bound; see int_pipe"},
-        "int_pipe": {"keccak_perms_per_s": (nodes / (tree_ms / 1e3)) if tree_ms else None,
+                     "note": "Keccak-bound (integer ALU pipe), not HBM-bound: alu_frac is the same kernels "
+                             "against the ALU-pipe peak (int_pipe)",
+                     "alu_frac": (perms_per_s / alu_peak) if perms_per_s else None},
+        "int_pipe": {"keccak_perms_per_s": perms_per_s, "alu_peak_perms_per_s": alu_peak,
+                     "frac": (perms_per_s / alu_peak) if perms_per_s else None,
+                     "peak_source": "60 ALU thread-ops/clk/SM measured x SMs x sampled SM clock / "
+                                    "4116 instructions per Keccak-f (ncu, level_kernel)",
                      "kernel_share_of_step": tree_ms / total_ms_classes if total_ms_classes else None},
         "kernel_ms_per_step": {k: v[0] / args.steps for k, v in prof.items()},
         "algorithmic_bytes_per_step": algorithmic_bytes(n, log2_c),
         "cpu_baseline": cpu,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": ms_e2e / args.steps},
-        "clocks": clk.summary(),
+        "clocks": clocks,
         "gpu_launches": launches,
         "proof_bytes": len(proof),
         "batched": batched,
