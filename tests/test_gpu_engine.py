@@ -136,3 +136,34 @@ def test_engine_bad_job_fails_alone(bg, graphs):
         assert res[k]["status"] == 0 and res[k]["proof"] == alone(bg, n, ev, pt)[2]
     again = eng.prove([jobs[0], jobs[3]])
     assert again[0]["proof"] == res[0]["proof"] and again[1]["proof"] == res[3]["proof"]
+
+
+def test_engine_proofs_verify_in_one_batch(bg):
+    """Served flow: proofs made by the engine, checked by bf_verify_batch per
+    size, all accepted; one altered claim per size rejected as the host
+    verifier rejects it."""
+    sizes = [6, 9, 12, 9, 6, 12, 16, 16]
+    jobs = make_jobs(sizes, 8600)
+    res = bg.Engine(max_inflight=4).prove(jobs)
+    for n in sorted(set(sizes)):
+        pcs = bg.Basefold.setup(bg.BasefoldConfig(bg.BinaryReedSolomonCode(128, 1, n)), device=0)
+        items, wants = [], []
+        for (m, ev, pt), r in zip(jobs, res):
+            if m != n:
+                continue
+            for bad in (False, True):
+                vals = r["value"].copy()
+                if bad:
+                    vals[0, 0] ^= 2
+                ch = bg.GenericChallenger.keccak256()
+                ch.observe(r["root"])
+                ch.observe_ext_slice(vals)
+                items.append((r["root"], [bg.PolyEvals(vals, pt)], r["proof"], ch))
+                host = ch.clone()
+                try:
+                    pcs.verify(r["root"], [bg.PolyEvals(vals, pt)], r["proof"], host)
+                    wants.append(0)
+                except bg.BasefoldError as e:
+                    wants.append(e.code)
+        got = pcs.verify_batch(items)
+        assert got == wants and got[0::2] == [0] * (len(got) // 2) and all(w != 0 for w in wants[1::2]), n

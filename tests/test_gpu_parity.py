@@ -197,6 +197,17 @@ def test_wide_commit_large(bg):
     assert proof == O.open_proof(n, log2_c, evals, point, values_o, blob, width)
 
 
+@pytest.mark.parametrize("n,log2_c,width", [(16, 1, 1), (17, 2, 2), (18, 1, 3)])
+def test_commit_from_host_in_slices(bg, n, log2_c, width):
+    """From 2^16 rows up bf_commit copies host rows in 8 slices on a second
+    stream and the first NTT pass starts on each slice as it lands: same
+    root, values and proof as the oracle, wide rows included."""
+    pcs, comm, evals, point, values, ch, proof = harness_w(bg, n, log2_c, width, 91 + n)
+    root_o, values_o, blob = O.harness_prepare(n, log2_c, evals, point, width)
+    assert comm.root == root_o and np.array_equal(values, values_o)
+    assert proof == O.open_proof(n, log2_c, evals, point, values_o, blob, width)
+
+
 @pytest.mark.parametrize("pending", [0, 100, 400, 401, 600, 5000])
 def test_open_with_long_pending_transcript(bg, pending):
     """Whatever the caller observed before open (here `pending` extra bytes,
