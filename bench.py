@@ -292,6 +292,8 @@ def run_served(bg, device, log2_c, lo=12, hi=24, per_level=48, loads=(0.25, 0.5,
     rng = np.random.default_rng(seed)
     inputs = gen_inputs(list(range(lo, hi + 1)), 2000)
     eng = bg.Engine(device=device, log2_c=log2_c, max_inflight=16)
+    # every size set up once (twiddles, pools) before anything is timed
+    eng.prove([(n, inputs[n][0], inputs[n][1]) for n in range(lo, hi + 1)])
     # capacity: saturated batch of the same size distribution
     cap_sizes = [int(x) for x in rng.integers(lo, hi + 1, per_level)]
     eng.prove([(n, inputs[n][0], inputs[n][1]) for n in cap_sizes[:8]])
