@@ -284,9 +284,12 @@ def run_batched(bg, torch, device, log2_c, count=256, lo=10, hi=22, seed=4):
             "note": "batched = engine with per-stream job state machines (continuous batching), not one fused launch"}
 
 
-def run_served(bg, device, log2_c, lo=12, hi=24, per_level=48, loads=(0.25, 0.5, 0.9), seed=5):
+def run_served(bg, device, log2_c, lo=12, hi=24, per_size=10, loads=(0.25, 0.5, 0.9), seed=5):
     """Config 5: open-loop Poisson arrivals, sizes log-uniform 2^lo..2^hi, host
-    inputs (H2D inside), at fractions of the measured capacity."""
+    inputs (H2D inside), at fractions of the measured capacity.  Each load
+    level (and the capacity batch) is a stratified mix: every size per_size
+    times in random order, so the offered work is the distribution's and not
+    a sample's."""
     import numpy as np
 
     rng = np.random.default_rng(seed)
@@ -295,18 +298,21 @@ def run_served(bg, device, log2_c, lo=12, hi=24, per_level=48, loads=(0.25, 0.5,
     # every size set up once (twiddles, pools) before anything is timed
     eng.prove([(n, inputs[n][0], inputs[n][1]) for n in range(lo, hi + 1)])
     # capacity: saturated batch of the same size distribution
-    cap_sizes = [int(x) for x in rng.integers(lo, hi + 1, per_level)]
+    mix = list(range(lo, hi + 1)) * per_size
+    per_level = len(mix)
+    cap_sizes = [int(x) for x in rng.permutation(mix)]
     eng.prove([(n, inputs[n][0], inputs[n][1]) for n in cap_sizes[:8]])
     t = time.perf_counter()
     eng.prove([(n, inputs[n][0], inputs[n][1]) for n in cap_sizes])
     capacity = per_level / (time.perf_counter() - t)
     out = {"workload": f"Poisson arrivals, sizes log-uniform 2^{lo}..2^{hi}, blowup {1 << log2_c}, "
-                       f"{per_level} requests per load, host inputs", "size_range": [lo, hi],
+                       f"{per_level} requests per load (each size {per_size} times, random order), host inputs",
+           "size_range": [lo, hi],
            "capacity_proofs_per_s": capacity, "levels": []}
     eng.start()
     for load in loads:
         rate = load * capacity
-        sizes = [int(x) for x in rng.integers(lo, hi + 1, per_level)]
+        sizes = [int(x) for x in rng.permutation(mix)]
         gaps = rng.exponential(1.0 / rate, per_level)
         lat, done = [], 0
         t0 = time.perf_counter()
