@@ -134,10 +134,11 @@ __global__ void __launch_bounds__(512) ntt_pass_kernel(const uint4* __restrict__
     for (uint32_t bi = threadIdx.x; bi < (tsize >> 1); bi += blockDim.x) {
       const uint32_t a = ((bi >> l) << (l + 1)) | (bi & lmask);
       const uint32_t K = kbase | (bi >> l);
-      const uint4 t = gf_add(lo_tab[K & 4095u], hi_tab[K >> 12]);
       uint4 x0 = sm[a], x1 = sm[a + (1u << l)];
-      x0 = gf_add(x0, gf_mul(x1, t));  // lo += hi * t
-      x1 = gf_add(x1, x0);             // hi += lo
+      // twiddle K is the XOR of independent stage bases over K's bits: zero
+      // only for K = 0 (the whole top layer of coset 0, half the next, ...)
+      if (K != 0) x0 = gf_add(x0, gf_mul(x1, gf_add(lo_tab[K & 4095u], hi_tab[K >> 12])));  // lo += hi * t
+      x1 = gf_add(x1, x0);  // hi += lo
       sm[a] = x0;
       sm[a + (1u << l)] = x1;
     }
