@@ -176,6 +176,9 @@ int bf_pcs_set_tune(bf_pcs* pcs, const int* vals, int n);
  * time on the CPU.)
  * bf_engine_autotune: reps > 0 autotunes (bf_pcs_autotune) each size the
  *   first time a job of that size is admitted; 0 (default) keeps defaults.
+ * bf_engine_set_tune: the launch shapes of bf_pcs_set_tune (4 values) for
+ *   every size, current and future (an autotune, if on, still runs after).
+ *   Call only while no job is in flight.
  * bf_engine_graphs (default off): on, each slot keeps, per job size, fixed
  *   buffers and one captured CUDA graph of the commit, evaluation and
  *   device-transcript open; a job then costs a staging write, one copy of
@@ -198,6 +201,7 @@ int bf_engine_stop(bf_engine* e);
 int bf_engine_submit(bf_engine* e, bf_job* job, int device_input);
 int bf_engine_poll(bf_engine* e, bf_job** done, size_t cap, size_t* n);
 int bf_engine_autotune(bf_engine* e, int reps);
+int bf_engine_set_tune(bf_engine* e, const int* vals, int n);
 int bf_engine_graphs(bf_engine* e, int on);
 /* Host-side accounting since creation: out = {ms spent admitting jobs
  * (allocation, capture, staging, enqueue), of which ms in graph launches,

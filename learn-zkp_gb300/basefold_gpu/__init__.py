@@ -452,6 +452,11 @@ class Engine:
     def proof_size(self, num_vars: int) -> int:
         return int(lib().bf_engine_proof_size(self._h, num_vars))
 
+    def set_tune(self, tune: dict) -> None:
+        """Launch shapes (Basefold.TUNE_KEYS) for every size (bf_engine_set_tune)."""
+        vals = (C.c_int * 4)(*[int(tune[k]) for k in Basefold.TUNE_KEYS])
+        check(lib().bf_engine_set_tune(self._h, vals, 4))
+
     def stats(self) -> dict:
         """Host-side accounting (bf_engine_stats)."""
         v = (C.c_double * 6)()

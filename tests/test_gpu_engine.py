@@ -167,3 +167,15 @@ def test_engine_proofs_verify_in_one_batch(bg):
                     wants.append(e.code)
         got = pcs.verify_batch(items)
         assert got == wants and got[0::2] == [0] * (len(got) // 2) and all(w != 0 for w in wants[1::2]), n
+
+
+def test_engine_set_tune_keeps_proofs(bg):
+    """Engine-wide launch shapes change no proof byte; invalid shapes are refused."""
+    jobs = make_jobs([11, 13, 9], 8700)
+    base = bg.Engine(max_inflight=3).prove(jobs)
+    eng = bg.Engine(max_inflight=3)
+    eng.set_tune({"ntt_threads": 128, "ntt_max_T": 7, "top_nodes": 128, "tail_log": 11})
+    for r0, r1 in zip(base, eng.prove(jobs)):
+        assert r0["proof"] == r1["proof"] and r0["root"] == r1["root"]
+    with pytest.raises(bg.BasefoldGpuError):
+        eng.set_tune({"ntt_threads": 96, "ntt_max_T": 12, "top_nodes": 512, "tail_log": 8})
