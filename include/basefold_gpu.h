@@ -8,8 +8,8 @@
  * behind its `PolyCommitScheme` trait (poly-commit/src/lib.rs:20-51) and the
  * standalone sumcheck prover (sumcheck/src/lib.rs:56-103).  The reference
  * exposes Rust traits, not an FFI; each entry point below names the trait
- * method or function it replaces.  A Rust binding over these symbols is shown
- * in INTEGRATION.md.
+ * method or function it replaces, so a Rust crate can bind these symbols
+ * with `extern "C"` declarations and implement the trait over them.
  *
  * Conventions
  *  - Field element: 16 bytes, the raw little-endian u128 that `Polyval`
