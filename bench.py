@@ -268,7 +268,7 @@ def run_batched(bg, torch, device, log2_c, count=256, lo=10, hi=22, seed=4):
     t_plain = time.perf_counter() - t
     eng = bg.Engine(device=device, log2_c=log2_c, max_inflight=32)
     jobs = [(n, dev[n].data_ptr(), inputs[n][1]) for n in sizes]
-    eng.prove(jobs[:32], device_input=True)  # warm
+    eng.prove([(n, dev[n].data_ptr(), inputs[n][1]) for n in inputs], device_input=True)  # every size set up
     torch.cuda.synchronize()
     t = time.perf_counter()
     res = eng.prove(jobs, device_input=True)
