@@ -82,9 +82,12 @@ static unsigned grid_for(size_t n, int threads, int per_sm = 8) {
 struct PassParams {
   int n, s_lo, T, first;
   int width;  // row width of m and cw; blockIdx.y is the column
-  // First pass: this launch covers the input tiles [tile0, tile0 + ntiles)
-  // (tile c = input rows [c 2^T, (c+1) 2^T)) of every coset.
-  uint32_t tile0, ntiles;
+  // First pass split into 2^piece_log launches (input slices): launch
+  // `piece` runs the butterfly columns u = (m << piece_log) | bitrev(piece),
+  // whose input tiles bitrev(u) (rows [c 2^T, (c+1) 2^T)) are slice `piece`.
+  // Unsplit (piece_log 0) block m runs column m, so neighbouring blocks write
+  // neighbouring elements.
+  int piece_log, piece;
   // Last pass only: also hash the codeword leaves H(cw[q]) and the first
   // folded-codeword leaves H(cw[2s] || cw[2s+1]) from the tile in shared
   // memory (null: no hashing).  The hashing is integer-ALU work and the
@@ -101,9 +104,10 @@ __global__ void __launch_bounds__(512) ntt_pass_kernel(const uint4* __restrict__
   const int n = p.n, T = p.T, s_lo = p.s_lo;
   const uint32_t tiles_per_coset = 1u << (n - T);
   uint32_t j, rem;
-  if (p.first) {  // block -> (coset, input tile c); the tile's butterflies sit at u = bitrev(c)
-    j = blockIdx.x / p.ntiles;
-    rem = brev_bits(p.tile0 + blockIdx.x % p.ntiles, s_lo);
+  if (p.first) {
+    const int shift = n - T - p.piece_log;  // log2 of this launch's blocks per coset
+    j = blockIdx.x >> shift;
+    rem = ((blockIdx.x & ((1u << shift) - 1u)) << p.piece_log) | brev_bits((uint32_t)p.piece, p.piece_log);
   } else {
     j = blockIdx.x >> (n - T);
     rem = blockIdx.x & (tiles_per_coset - 1);
@@ -225,8 +229,12 @@ cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t w
     const int threads = std::max(32, std::min(tune.ntt_threads, 1 << (T - 1)));
     const uint32_t tiles = 1u << (n - T);
     // the first pass may start on each slice of the input as it arrives
-    const int pieces = (p.first && slices > 0 && tiles >= (uint32_t)slices) ? slices : 1;
-    if (p.first && slices > 0 && pieces == 1) {
+    // (slices a power of two, at most the tiles per coset)
+    const bool split = p.first && slices > 0 && (slices & (slices - 1)) == 0 && tiles >= (uint32_t)slices;
+    const int pieces = split ? slices : 1;
+    int piece_log = 0;
+    while ((1 << piece_log) < pieces) ++piece_log;
+    if (p.first && slices > 0 && !split) {
       cudaError_t e = cudaStreamWaitEvent(st, slice_ready[slices - 1], 0);  // copies are in order
       if (e != cudaSuccess) return e;
     }
@@ -235,9 +243,9 @@ cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t w
         cudaError_t e = cudaStreamWaitEvent(st, slice_ready[piece], 0);
         if (e != cudaSuccess) return e;
       }
-      p.ntiles = p.first ? tiles / pieces : tiles;
-      p.tile0 = p.first ? p.ntiles * piece : 0;
-      const dim3 grid((unsigned)(c * p.ntiles), (unsigned)width);
+      p.piece_log = piece_log;
+      p.piece = piece;
+      const dim3 grid((unsigned)(c * (tiles >> piece_log)), (unsigned)width);
       if (p.leaves)
         ntt_pass_kernel<true><<<grid, threads, sizeof(uint4) << T, st>>>(m, cw, p, tw);
       else
