@@ -26,6 +26,8 @@
  *    bf_verify additionally returns the BF_VERIFY_* results.
  *  - A bf_pcs and everything made from it belong to one host thread at a
  *    time; all GPU work runs on the pcs's stream.
+ *  - Free in any order: a freed bf_pcs lives on until its last commitment
+ *    and open session are freed.
  */
 #ifndef BASEFOLD_GPU_H
 #define BASEFOLD_GPU_H
@@ -44,6 +46,7 @@ extern "C" {
 #define BF_ERR_BUFFER (-4)       /* caller buffer too small; required size returned */
 #define BF_ERR_UNSUPPORTED (-5)  /* configuration this build does not run on the GPU */
 #define BF_ERR_NOT_INVERTIBLE (-6) /* a point coordinate r with r = 0 or r = 1 */
+#define BF_ERR_CHECK (-7)        /* a self-check of the prover failed (the reference's debug asserts) */
 
 #define BF_VERIFY_OK 0
 #define BF_VERIFY_INVALID_FINAL_POLY 1 /* BasefoldError::InvalidFinalPoly (basefold.rs:79-84) */

@@ -30,6 +30,7 @@ BF_ERR_OOM = -3
 BF_ERR_BUFFER = -4
 BF_ERR_UNSUPPORTED = -5
 BF_ERR_NOT_INVERTIBLE = -6
+BF_ERR_CHECK = -7
 
 
 class BfJob(C.Structure):

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <array>
+#include <atomic>
 #include <cstdint>
 #include <cstring>
 #include <memory>
@@ -195,11 +196,20 @@ int open_finish_enqueue(bf_open_session* s, const uint64_t* indices, size_t nq);
 int open_finish_complete(bf_open_session* s, uint8_t* proof, size_t cap, size_t* proof_len);
 }  // namespace bfapi
 
+namespace bfapi {
+void pcs_acquire(bf_pcs* p);
+void pcs_release(bf_pcs* p);
+}  // namespace bfapi
+
 struct bf_challenger {
   bfh::Challenger c;
 };
 
 struct bf_pcs {
+  // Holders: the caller (until bf_pcs_free) and every commitment and open
+  // session made from it; the last to let go destroys it, so frees in any
+  // order are safe.
+  std::atomic<int> refs{1};
   int device = 0;
   int lambda = 128, log2_c = 1, d = 0, L = 0;
   size_t Q = 0;

@@ -364,7 +364,9 @@ int open_resident_complete(bf_open_session* s, bfh::Challenger& ch) {
   const uint8_t* res = s->res_pin;
   bf::OpenState img;
   std::memcpy(&img, res + align16(rec_bytes(d)), sizeof(img));
-  if (img.status != 0) return fail(BF_ERR_ARG, "transcript input outgrew the device buffer");
+  if (img.status & 1) return fail(BF_ERR_ARG, "transcript input outgrew the device buffer");
+  if (img.status & 2)
+    return fail(BF_ERR_CHECK, "self-check failed: the last folded codeword is not encode0(final polynomial)");
   for (int k = 0; k < d; ++k) {
     const uint8_t* rec = res + 64 * (size_t)k;
     s->roots.insert(s->roots.end(), rec, rec + 32);
@@ -486,6 +488,7 @@ int open_session_create(bf_pcs* p, const bf_commitment* cm, void* stream, bf_ope
   s->d = p->d;
   s->i = s->d - 1;
   TRY(session_alloc(s.get()));
+  pcs_acquire(p);
   *out = s.release();
   return BF_OK;
 }
@@ -714,8 +717,12 @@ int bf_open_finish(bf_open_session* s, const uint64_t* indices, size_t nq, uint8
 
 void bf_open_session_free(bf_open_session* s) {
   if (!s) return;
-  DeviceGuard g(s->p->device);
-  delete s;
+  bf_pcs* p = s->p;
+  {
+    DeviceGuard g(p->device);
+    delete s;
+  }
+  pcs_release(p);
 }
 
 // Whole open with this library's transcript (basefold.rs:133-232).

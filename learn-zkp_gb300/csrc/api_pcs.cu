@@ -5,6 +5,7 @@
 // codeword, Merkle trees, folded codewords and their trees, the sumcheck
 // polynomial and its eq table.  Only the Fiat–Shamir transcript crosses to
 // the host.
+#include <nvtx3/nvToolsExt.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -19,6 +20,18 @@
 using bfh::u128;
 
 namespace bfapi {
+
+void pcs_acquire(bf_pcs* p) { p->refs.fetch_add(1, std::memory_order_relaxed); }
+
+void pcs_release(bf_pcs* p) {
+  if (p->refs.fetch_sub(1, std::memory_order_acq_rel) != 1) return;
+  if (p->device < 0) {  // a verifier-only pcs touches no device
+    delete p;
+    return;
+  }
+  DeviceGuard g(p->device);
+  delete p;
+}
 
 namespace {
 thread_local std::string g_err;
@@ -68,7 +81,13 @@ void Profiler::drain() {
   pending.clear();
 }
 
+// NVTX range names of the kernel classes (in P_* order); the ranges cost
+// nothing unless a profiler is attached.
+static const char* const kProfNames[kProfClasses] = {"encode", "leaves", "tree", "pi_leaves", "fold",
+                                                     "fix", "eq", "gather", "open_tail", "transcript"};
+
 ProfScope::ProfScope(Profiler& p, cudaStream_t s, int c) : pr(p), st(s), cls(c) {
+  nvtxRangePushA(kProfNames[cls]);
   if (pr.on) {
     a = pr.get();
     cudaEventRecord(a, st);
@@ -81,6 +100,7 @@ ProfScope::~ProfScope() {
     cudaEventRecord(b, st);
     pr.pending.push_back({cls, a, b});
   }
+  nvtxRangePop();
 }
 
 DeviceGuard::DeviceGuard(int dev) {
@@ -444,13 +464,7 @@ int bf_pcs_setup(int device, int lambda, int log2_c, int num_vars, void* stream,
 }
 
 void bf_pcs_free(bf_pcs* pcs) {
-  if (!pcs) return;
-  if (pcs->device < 0) {
-    delete pcs;
-    return;
-  }
-  DeviceGuard g(pcs->device);
-  delete pcs;
+  if (pcs) pcs_release(pcs);
 }
 
 size_t bf_pcs_num_queries(const bf_pcs* pcs) { return pcs ? pcs->Q : 0; }
@@ -490,6 +504,7 @@ int bf_commit(bf_pcs* p, const uint8_t* evals, size_t width, bf_commitment** out
     TRY(commit_device(p, cm.get(), cm->data.as<uint4>()));
   }
   if (root) std::memcpy(root, cm->root, 32);
+  pcs_acquire(p);
   *out = cm.release();
   return BF_OK;
 }
@@ -509,14 +524,19 @@ int bf_commit_device(bf_pcs* p, const void* d_evals, size_t width, bf_commitment
   cm->data.bytes = 16 * ((size_t)1 << p->d) * width;
   TRY(commit_device(p, cm.get(), reinterpret_cast<const uint4*>(d_evals)));
   if (root) std::memcpy(root, cm->root, 32);
+  pcs_acquire(p);
   *out = cm.release();
   return BF_OK;
 }
 
 void bf_commitment_free(bf_commitment* cm) {
   if (!cm) return;
-  DeviceGuard g(cm->pcs->device);
-  delete cm;  // buffers return to the pcs's pool in stream order
+  bf_pcs* p = cm->pcs;
+  {
+    DeviceGuard g(p->device);
+    delete cm;  // buffers return to the pcs's pool in stream order
+  }
+  pcs_release(p);
 }
 
 int bf_commitment_root(const bf_commitment* cm, uint8_t root[32]) {

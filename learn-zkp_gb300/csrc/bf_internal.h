@@ -143,8 +143,9 @@ struct alignas(16) DevTranscript {
 // Device-resident state of one open (basefold.rs:133-232): the transcript,
 // the claim of the first sumcheck round (`outer`, the evaluation), the
 // EvalProver claim of the later rounds (`inner`), the product of delta
-// scalars (eval_impr.rs:45-51) and the last challenge.  status != 0: the
-// transcript input outgrew kTrMax.
+// scalars (eval_impr.rs:45-51) and the last challenge.  status bit 0: the
+// transcript input outgrew kTrMax; bit 1: the last folded codeword is not
+// encode0 of the final polynomial (basefold.rs:198).
 struct alignas(16) OpenState {
   DevTranscript tr;
   uint4 outer, inner, delta, x;

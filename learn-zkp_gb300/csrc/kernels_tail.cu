@@ -325,6 +325,15 @@ __global__ void __launch_bounds__(kTailThreads, 1) open_tail_kernel(TailParams P
     reinterpret_cast<uint4*>(P.result + 64 * (size_t)k)[0] = fin;
     const uint4 m[1] = {fin};
     tr_observe(sh, m);
+    // the reference's debug self-check encode0(final_poly) == pi (basefold.rs:198):
+    // every entry of the last folded codeword is the final polynomial
+    if (P.i0 >= 0) {
+      const uint4* pi0 = P.pi_fold + c * (((size_t)1 << d) - 2);
+      for (size_t t = 0; t < c; ++t) {
+        const uint4 e = pi0[t];
+        if (e.x != fin.x || e.y != fin.y || e.z != fin.z || e.w != fin.w) sh.status |= 2;
+      }
+    }
   }
   __syncthreads();
   state_store(P.state, sh);

@@ -300,3 +300,58 @@ def test_seeded_reference_harness(bg):
             c = by_key[(log2_c, n, w)]
             assert comm.root.hex() == c["root"] and values.tobytes().hex() == c["values"], (log2_c, n, w)
             assert hashlib.sha256(proof).hexdigest() == c["proof_sha256"], (log2_c, n, w)
+
+
+def test_data_changed_after_commit_is_caught(bg):
+    """commit_device keeps a reference to the caller's buffer: if the caller
+    changes it after committing, the sumcheck and the committed codeword no
+    longer describe one polynomial.  The prover's self-check (the reference's
+    debug assert encode0(final_poly) == pi, basefold.rs:198) turns that into
+    an error instead of a proof that would not verify."""
+    torch = pytest.importorskip("torch")
+    n = 12
+    data = rand.random_elems((1 << n) + n, 4242)
+    ev = torch.from_numpy(data[: 1 << n].copy()).cuda()
+    point = data[1 << n:]
+    pcs = setup_pcs(bg, n, 1)
+    comm = pcs.commit_device(ev.data_ptr(), keep=ev)
+    ev[5, 0] ^= 1  # the committed data changes under the commitment
+    torch.cuda.synchronize()
+    ch = bg.GenericChallenger.keccak256()
+    ch.observe(comm.root)
+    values = pcs.eval(pcs.data(comm), point)
+    ch.observe_ext_slice(values)
+    with pytest.raises(bg.BasefoldGpuError) as e:
+        pcs.open(comm, [bg.PolyEvals(values, point)], ch)
+    assert e.value.code == -7
+    # the same pcs proves the unchanged data afterwards
+    ev[5, 0] ^= 1
+    torch.cuda.synchronize()
+    comm2 = pcs.commit_device(ev.data_ptr(), keep=ev)
+    ch = bg.GenericChallenger.keccak256()
+    ch.observe(comm2.root)
+    values = pcs.eval(pcs.data(comm2), point)
+    ch.observe_ext_slice(values)
+    proof = pcs.open(comm2, [bg.PolyEvals(values, point)], ch.clone())
+    pcs.verify(comm2.root, [bg.PolyEvals(values, point)], proof, ch.clone())
+
+
+def test_free_order_does_not_matter(bg):
+    """A pcs freed before its commitments and open sessions stays alive until
+    the last of them is freed (the order a garbage collector may pick)."""
+    from basefold_gpu import _native
+
+    n = 10
+    data = rand.random_elems((1 << n) + n, 515)
+    pcs = setup_pcs(bg, n, 1)
+    comm = pcs.commit(data[: 1 << n])
+    root = comm.root
+    point = data[1 << n:]
+    sess = pcs.open_session(comm, bg.PolyEvals(pcs.eval(pcs.data(comm), point), point))
+    _native.lib().bf_pcs_free(pcs._h)  # the caller's reference goes first
+    pcs._h = None
+    r = np.zeros(32, dtype=np.uint8)
+    _native.check(_native.lib().bf_commitment_root(comm._h, r.ctypes.data))
+    assert r.tobytes() == root
+    del sess
+    comm.free()
