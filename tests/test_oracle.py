@@ -5,7 +5,8 @@ The reference keeps no golden vectors, so the oracle is pinned by
   * the RFC 8452 POLYVAL known-answer vector and the Keccak-256("") KAT;
   * SHA3-256 from Python's hashlib (same Keccak-f[1600], different padding);
   * the reference's own definitional NTT test (p3/src/field/binary.rs:194-217)
-    and field-axiom test (p3/src/polyval.rs:265-295);
+    and field-axiom test (p3/src/polyval.rs:265-295), and the brute-force
+    multilinear evaluation of its multilinear tests (multilinear.rs:312-379);
   * the reference's prove->verify harness (poly-commit/src/lib.rs:64-105,
     sumcheck/src/lib.rs:160-182);
 and the committed oracle vectors guard it against regressions.
@@ -97,6 +98,25 @@ def test_ntt_round_trip():
         for width in (1, 3, 9):
             a = rand.random_elems(width << log_n, 7 * log_n + width)
             assert np.array_equal(O.ntt_backward(log_n, O.ntt_forward(log_n, a, width), width), a)
+
+
+@pytest.mark.parametrize("n", [0, 1, 3, 7])
+def test_evaluate_matches_definition(n):
+    """MultiPoly::evaluate (p3/src/poly/multilinear.rs:124-141) against the
+    definition of the multilinear extension, as the reference's brute-force
+    tests do (multilinear.rs:312-379): f(p) = sum_b f(b) prod_i w_i(b) with
+    w_i = p_i when bit i of b is set, else 1 + p_i (characteristic 2)."""
+    data = rand.random_elems((1 << n) + n, 900 + n)
+    f, point = data[: 1 << n], data[1 << n:]
+    one = O.from_ints([ONE])[0]
+    w = np.tile(one, (1 << n, 1))
+    for i in range(n):
+        bit = ((np.arange(1 << n) >> i) & 1).astype(bool)
+        factor = np.where(bit[:, None], point[i], point[i] ^ one)
+        w = O.gf_mul(w, factor)
+    terms = O.gf_mul(w, f)
+    want = np.bitwise_xor.reduce(terms, axis=0) if n else f[0]
+    assert np.array_equal(O.eval_poly(n, f, point)[0], want)
 
 
 def test_num_queries():
