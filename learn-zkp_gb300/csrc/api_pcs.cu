@@ -3,8 +3,9 @@
 //
 // The prover keeps every array of the path in device memory: evaluations,
 // codeword, Merkle trees, folded codewords and their trees, the sumcheck
-// polynomial and its eq table.  Only the Fiat–Shamir transcript crosses to
-// the host.
+// polynomial and its eq table.  What crosses to the host is what the caller
+// receives (roots, evaluations, the proof) and, at the end of an open, the
+// transcript state from which the query positions are sampled.
 #include <nvtx3/nvToolsExt.h>
 #include <cuda_runtime.h>
 
