@@ -1,11 +1,17 @@
-// libbasefold_gpu.so: Basefold::open (poly-commit/src/basefold.rs:133-232) as a
-// round-level session.
+// libbasefold_gpu.so: Basefold::open (poly-commit/src/basefold.rs:133-232).
 //
-// Each round the device returns the folded-codeword Merkle root and the
-// compressed sumcheck round polynomial; the caller's transcript observes them
-// and samples the challenge; the device then folds, fixes the variable, and
-// builds the next round's tree.  Sessions own their device workspace, so
-// several can be in flight on different streams.
+// Two drivers over one session (device workspace, pinned staging):
+//  * round-level, for a caller-held transcript: each round the device returns
+//    the folded-codeword Merkle root and the compressed sumcheck round
+//    polynomial; the caller's transcript observes them and samples the
+//    challenge; the device then folds, fixes the variable and builds the
+//    next round's tree;
+//  * device-resident (bf_open, the engine): the library's transcript lives in
+//    device memory and every round is queued at once (kernels_tail.cu); the
+//    host samples only the query positions from the returned state.
+// Both then gather the query openings and write the bincode proof.  Sessions
+// own their device workspace, so several can be in flight on different
+// streams.
 #include <cuda_runtime.h>
 
 #include <algorithm>
