@@ -773,17 +773,28 @@ struct PolyPtrs {
   uint4* out[3];
 };
 
+// One GF(2^128) product as a call: the product-sumcheck kernels need several
+// per term, and inlined the compiler interleaves them into 255 registers
+// (12% occupancy); called one at a time they need about a third of that.
+__device__ __noinline__ uint4 gf_mul_call(uint4 a, uint4 b) { return gf_mul(a, b); }
+
+// Coefficients c0, c2 (and c3) of prod_k (lo_k + b_k X), b_k = hi_k - lo_k,
+// summed into s0, s2, s3.  For K = 3 the cross term lo1 b2 + b1 lo2 is
+// hi1 hi2 + lo1 lo2 + b1 b2 (characteristic 2, lo + b = hi), which reuses two
+// products the term needs anyway: 7 products instead of 8.
 template <int K>
 __device__ __forceinline__ void prod_terms(const uint4 lo[K], const uint4 hi[K], uint4& s0, uint4& s2, uint4& s3) {
   if (K == 2) {
-    s0 = gf_add(s0, gf_mul(lo[0], lo[1]));
-    s2 = gf_add(s2, gf_mul(gf_add(hi[0], lo[0]), gf_add(hi[1], lo[1])));
+    s0 = gf_add(s0, gf_mul_call(lo[0], lo[1]));
+    s2 = gf_add(s2, gf_mul_call(gf_add(hi[0], lo[0]), gf_add(hi[1], lo[1])));
   } else {
     const uint4 b0 = gf_add(hi[0], lo[0]), b1 = gf_add(hi[1], lo[1]), b2 = gf_add(hi[2], lo[2]);
-    const uint4 b12 = gf_mul(b1, b2);
-    s0 = gf_add(s0, gf_mul(lo[0], gf_mul(lo[1], lo[2])));
-    s2 = gf_add(s2, gf_add(gf_mul(b0, gf_add(gf_mul(b1, lo[2]), gf_mul(lo[1], b2))), gf_mul(lo[0], b12)));
-    s3 = gf_add(s3, gf_mul(b0, b12));
+    const uint4 b12 = gf_mul_call(b1, b2);
+    const uint4 lo12 = gf_mul_call(lo[1], lo[2]);
+    const uint4 cross = gf_add(gf_add(gf_mul_call(hi[1], hi[2]), lo12), b12);  // lo1 b2 + b1 lo2
+    s0 = gf_add(s0, gf_mul_call(lo[0], lo12));
+    s2 = gf_add(s2, gf_add(gf_mul_call(b0, cross), gf_mul_call(lo[0], b12)));
+    s3 = gf_add(s3, gf_mul_call(b0, b12));
   }
 }
 
@@ -816,7 +827,7 @@ __global__ void __launch_bounds__(256) prod_sums_kernel(PolyPtrs p, size_t half,
 // round's sums.  Each thread produces the pair (b, b + half/2) of the fixed
 // polynomials, which is exactly what the next round's sums need.
 template <int K>
-__global__ void __launch_bounds__(256) prod_fix_kernel(PolyPtrs p, size_t half, uint4 r, uint32_t* acc,
+__global__ void __launch_bounds__(256, 2) prod_fix_kernel(PolyPtrs p, size_t half, uint4 r, uint32_t* acc,
                                                        const uint4* xp) {
   __shared__ uint4 scratch[32];
   if (xp) r = *xp;
@@ -838,8 +849,8 @@ __global__ void __launch_bounds__(256) prod_fix_kernel(PolyPtrs p, size_t half, 
     for (int k = 0; k < K; ++k) {
       const uint4 a0 = p.in[k][b], a1 = p.in[k][b + half];
       const uint4 c0 = p.in[k][b + nh], c1 = p.in[k][b + nh + half];
-      lo[k] = gf_add(a0, gf_mul(r, gf_add(a1, a0)));
-      hi[k] = gf_add(c0, gf_mul(r, gf_add(c1, c0)));
+      lo[k] = gf_add(a0, gf_mul_call(r, gf_add(a1, a0)));
+      hi[k] = gf_add(c0, gf_mul_call(r, gf_add(c1, c0)));
       p.out[k][b] = lo[k];
       p.out[k][b + nh] = hi[k];
     }
