@@ -47,6 +47,7 @@ extern "C" {
 #define BF_ERR_UNSUPPORTED (-5)  /* configuration this build does not run on the GPU */
 #define BF_ERR_NOT_INVERTIBLE (-6) /* a point coordinate r with r = 0 or r = 1 */
 #define BF_ERR_CHECK (-7)        /* a self-check of the prover failed (the reference's debug asserts) */
+#define BF_ERR_CANCELLED (-8)    /* an engine job cancelled before it started */
 
 #define BF_VERIFY_OK 0
 #define BF_VERIFY_INVALID_FINAL_POLY 1 /* BasefoldError::InvalidFinalPoly (basefold.rs:79-84) */
@@ -203,6 +204,10 @@ int bf_engine_start(bf_engine* e);
 int bf_engine_stop(bf_engine* e);
 int bf_engine_submit(bf_engine* e, bf_job* job, int device_input);
 int bf_engine_poll(bf_engine* e, bf_job** done, size_t cap, size_t* n);
+/* Cancels a submitted job that is still waiting for admission: it leaves the
+ * queue with status BF_ERR_CANCELLED and is returned by bf_engine_poll.  A job
+ * whose GPU work has been queued cannot be cancelled (BF_ERR_ARG). */
+int bf_engine_cancel(bf_engine* e, bf_job* job);
 int bf_engine_autotune(bf_engine* e, int reps);
 int bf_engine_set_tune(bf_engine* e, const int* vals, int n);
 int bf_engine_graphs(bf_engine* e, int on);

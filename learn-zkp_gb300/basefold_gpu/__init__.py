@@ -519,6 +519,14 @@ class Engine:
         check(lib().bf_engine_submit(self._h, C.byref(job), 1 if device_input else 0))
         return key
 
+    def cancel(self, key) -> bool:
+        """Cancel a submitted job (the key `submit` returned) that has not
+        started: True if it left the queue (poll then returns it with status
+        BF_ERR_CANCELLED), False if it is already running or done."""
+        if key not in self._keep:
+            return False
+        return lib().bf_engine_cancel(self._h, C.c_void_p(key)) == 0
+
     def poll(self):
         """Finished jobs since the last poll: list of (tag, result)."""
         out = (C.POINTER(BfJob) * 64)()

@@ -570,6 +570,24 @@ int bf_engine_submit(bf_engine* e, bf_job* job, int device_input) {
   return BF_OK;
 }
 
+int bf_engine_cancel(bf_engine* e, bf_job* job) {
+  if (!e || !job) return fail(BF_ERR_ARG, "null argument");
+  std::lock_guard<std::mutex> lk(e->mu);
+  for (auto it = e->queue.begin(); it != e->queue.end(); ++it) {
+    Job* j = *it;
+    if (j->pub != job) continue;
+    e->queue.erase(it);
+    job->status = BF_ERR_CANCELLED;
+    job->latency_ms = now_ms() - j->t_submit;
+    delete j;
+    e->finished.push_back(job);  // returned by bf_engine_poll like any finished job
+    e->outstanding -= 1;
+    e->cv.notify_all();
+    return BF_OK;
+  }
+  return fail(BF_ERR_ARG, "job is not waiting for admission (already running or finished)");
+}
+
 int bf_engine_stats(bf_engine* e, double* out, int n) {
   if (!e || !out || n < 6) return fail(BF_ERR_ARG, "need 6 values");
   std::lock_guard<std::mutex> lk(e->mu);

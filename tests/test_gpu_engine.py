@@ -179,3 +179,23 @@ def test_engine_set_tune_keeps_proofs(bg):
         assert r0["proof"] == r1["proof"] and r0["root"] == r1["root"]
     with pytest.raises(bg.BasefoldGpuError):
         eng.set_tune({"ntt_threads": 96, "ntt_max_T": 12, "top_nodes": 512, "tail_log": 8})
+
+
+def test_engine_cancel_queued_job(bg):
+    """A served request still waiting for a slot can be cancelled: it comes
+    back from poll with BF_ERR_CANCELLED; the others complete unchanged."""
+    jobs = make_jobs([21, 10, 11, 12, 9], 8800)
+    eng = bg.Engine(max_inflight=1)  # the 2^21 job holds the only slot for milliseconds
+    eng.start()
+    keys = [eng.submit(n, ev, pt, tag=i) for i, (n, ev, pt) in enumerate(jobs)]
+    assert eng.cancel(keys[2])
+    res, t0 = {}, time.time()
+    while len(res) < len(jobs) and time.time() - t0 < 120:
+        for tag, r in eng.poll():
+            res[tag] = r
+        time.sleep(0.001)
+    eng.stop()
+    assert res[2]["status"] == -8 and res[2]["proof"] == b""
+    for i in (0, 1, 3, 4):
+        assert res[i]["status"] == 0 and res[i]["proof"] == alone(bg, *jobs[i])[2], i
+    assert not eng.cancel(keys[0])  # finished: nothing to cancel
