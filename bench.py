@@ -474,19 +474,25 @@ def run_multi_column(bg, torch, device, log2_c, sizes, pcs, reps=3):
             pcs[n].verify(comm.root, [bg.PolyEvals(vals, pts[n])], proof, ch.clone())
         comm.free()
 
+    from concurrent.futures import ThreadPoolExecutor
+
     for n, w in groups.items():
         group(n, w, check=True)  # warm, and every proof verifies
     torch.cuda.synchronize()
+    # the matrices are independent: four host threads prove them concurrently
+    # (one pcs and stream per size), largest first
+    order = sorted(groups, key=lambda n: -(groups[n] << n))
     best = float("inf")
     for _ in range(reps):
         t = time.perf_counter()
-        for n, w in groups.items():
-            group(n, w)
+        with ThreadPoolExecutor(4) as ex:
+            list(ex.map(lambda n: group(n, groups[n]), order))
         torch.cuda.synchronize()
         best = min(best, time.perf_counter() - t)
     release(mats)
     return {"workload": f"the same {len(sizes)} polys as {len(groups)} matrices (one per size, columns = polys of "
-                        "that size), one point per matrix", "proofs": len(groups), "polys_per_s": len(sizes) / best,
+                        "that size), one point per matrix, 4 host threads", "proofs": len(groups),
+            "polys_per_s": len(sizes) / best,
             "seconds": best, "verified": True}
 
 
