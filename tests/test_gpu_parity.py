@@ -355,3 +355,24 @@ def test_free_order_does_not_matter(bg):
     assert r.tobytes() == root
     del sess
     comm.free()
+
+
+def test_concurrent_provers_on_threads(bg):
+    """Four host threads, each with its own pcs (and stream), prove at once:
+    every proof equals the one made alone.  Covers the library's shared state
+    under concurrency (launch counting, kernel attributes, error text,
+    pinned staging)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    cases = [(n, 1 + (k % 2), 7700 + k) for k, n in enumerate((9, 12, 14, 16, 11, 13, 15, 10))]
+
+    def prove(case):
+        n, log2_c, seed = case
+        pcs, comm, evals, point, values, ch, proof = harness(bg, n, log2_c, seed)
+        comm.free()
+        return proof
+
+    alone = [prove(c) for c in cases]
+    for _ in range(2):
+        with ThreadPoolExecutor(4) as ex:
+            assert list(ex.map(prove, cases)) == alone
