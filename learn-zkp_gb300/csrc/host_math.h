@@ -135,17 +135,98 @@ static const int kRho[25] = {0, 1, 62, 28, 27, 36, 44, 6, 55, 20, 3, 10, 43, 25,
 
 static inline uint64_t rotl(uint64_t v, int r) { return r ? (v << r) | (v >> (64 - r)) : v; }
 
+// Keccak-f[1600] on 25 local lanes (a<x><y> = A[x + 5y]), one round per
+// iteration written out: theta (column parities c, d = c[x-1] ^ rot(c[x+1], 1)),
+// rho and pi (b[y][2x+3y] = rot(a[x][y] ^ d[x], r[x][y])), chi, iota.
 static inline void keccak_f(uint64_t A[25]) {
+  uint64_t a00 = A[0], a10 = A[1], a20 = A[2], a30 = A[3], a40 = A[4], a01 = A[5], a11 = A[6], a21 = A[7], a31 = A[8], a41 = A[9], a02 = A[10], a12 = A[11], a22 = A[12], a32 = A[13], a42 = A[14], a03 = A[15], a13 = A[16], a23 = A[17], a33 = A[18], a43 = A[19], a04 = A[20], a14 = A[21], a24 = A[22], a34 = A[23], a44 = A[24];
   for (int ir = 0; ir < 24; ++ir) {
-    uint64_t C[5], B[25];
-    for (int x = 0; x < 5; ++x) C[x] = A[x] ^ A[x + 5] ^ A[x + 10] ^ A[x + 15] ^ A[x + 20];
-    for (int i = 0; i < 25; ++i) A[i] ^= C[(i + 4) % 5] ^ rotl(C[(i + 1) % 5], 1);
-    for (int x = 0; x < 5; ++x)
-      for (int y = 0; y < 5; ++y) B[y + 5 * ((2 * x + 3 * y) % 5)] = rotl(A[x + 5 * y], kRho[x + 5 * y]);
-    for (int y = 0; y < 25; y += 5)
-      for (int x = 0; x < 5; ++x) A[y + x] = B[y + x] ^ (~B[y + (x + 1) % 5] & B[y + (x + 2) % 5]);
-    A[0] ^= kRC[ir];
+    const uint64_t c0 = a00 ^ a01 ^ a02 ^ a03 ^ a04, c1 = a10 ^ a11 ^ a12 ^ a13 ^ a14,
+                   c2 = a20 ^ a21 ^ a22 ^ a23 ^ a24, c3 = a30 ^ a31 ^ a32 ^ a33 ^ a34,
+                   c4 = a40 ^ a41 ^ a42 ^ a43 ^ a44;
+    const uint64_t d0 = c4 ^ rotl(c1, 1);
+    const uint64_t d1 = c0 ^ rotl(c2, 1);
+    const uint64_t d2 = c1 ^ rotl(c3, 1);
+    const uint64_t d3 = c2 ^ rotl(c4, 1);
+    const uint64_t d4 = c3 ^ rotl(c0, 1);
+    const uint64_t b00 = (a00 ^ d0);
+    const uint64_t b10 = rotl(a11 ^ d1, 44);
+    const uint64_t b20 = rotl(a22 ^ d2, 43);
+    const uint64_t b30 = rotl(a33 ^ d3, 21);
+    const uint64_t b40 = rotl(a44 ^ d4, 14);
+    const uint64_t b01 = rotl(a30 ^ d3, 28);
+    const uint64_t b11 = rotl(a41 ^ d4, 20);
+    const uint64_t b21 = rotl(a02 ^ d0, 3);
+    const uint64_t b31 = rotl(a13 ^ d1, 45);
+    const uint64_t b41 = rotl(a24 ^ d2, 61);
+    const uint64_t b02 = rotl(a10 ^ d1, 1);
+    const uint64_t b12 = rotl(a21 ^ d2, 6);
+    const uint64_t b22 = rotl(a32 ^ d3, 25);
+    const uint64_t b32 = rotl(a43 ^ d4, 8);
+    const uint64_t b42 = rotl(a04 ^ d0, 18);
+    const uint64_t b03 = rotl(a40 ^ d4, 27);
+    const uint64_t b13 = rotl(a01 ^ d0, 36);
+    const uint64_t b23 = rotl(a12 ^ d1, 10);
+    const uint64_t b33 = rotl(a23 ^ d2, 15);
+    const uint64_t b43 = rotl(a34 ^ d3, 56);
+    const uint64_t b04 = rotl(a20 ^ d2, 62);
+    const uint64_t b14 = rotl(a31 ^ d3, 55);
+    const uint64_t b24 = rotl(a42 ^ d4, 39);
+    const uint64_t b34 = rotl(a03 ^ d0, 41);
+    const uint64_t b44 = rotl(a14 ^ d1, 2);
+    a00 = b00 ^ (~b10 & b20);
+    a10 = b10 ^ (~b20 & b30);
+    a20 = b20 ^ (~b30 & b40);
+    a30 = b30 ^ (~b40 & b00);
+    a40 = b40 ^ (~b00 & b10);
+    a01 = b01 ^ (~b11 & b21);
+    a11 = b11 ^ (~b21 & b31);
+    a21 = b21 ^ (~b31 & b41);
+    a31 = b31 ^ (~b41 & b01);
+    a41 = b41 ^ (~b01 & b11);
+    a02 = b02 ^ (~b12 & b22);
+    a12 = b12 ^ (~b22 & b32);
+    a22 = b22 ^ (~b32 & b42);
+    a32 = b32 ^ (~b42 & b02);
+    a42 = b42 ^ (~b02 & b12);
+    a03 = b03 ^ (~b13 & b23);
+    a13 = b13 ^ (~b23 & b33);
+    a23 = b23 ^ (~b33 & b43);
+    a33 = b33 ^ (~b43 & b03);
+    a43 = b43 ^ (~b03 & b13);
+    a04 = b04 ^ (~b14 & b24);
+    a14 = b14 ^ (~b24 & b34);
+    a24 = b24 ^ (~b34 & b44);
+    a34 = b34 ^ (~b44 & b04);
+    a44 = b44 ^ (~b04 & b14);
+    a00 ^= kRC[ir];
+
   }
+  A[0] = a00;
+  A[1] = a10;
+  A[2] = a20;
+  A[3] = a30;
+  A[4] = a40;
+  A[5] = a01;
+  A[6] = a11;
+  A[7] = a21;
+  A[8] = a31;
+  A[9] = a41;
+  A[10] = a02;
+  A[11] = a12;
+  A[12] = a22;
+  A[13] = a32;
+  A[14] = a42;
+  A[15] = a03;
+  A[16] = a13;
+  A[17] = a23;
+  A[18] = a33;
+  A[19] = a43;
+  A[20] = a04;
+  A[21] = a14;
+  A[22] = a24;
+  A[23] = a34;
+  A[24] = a44;
 }
 
 static inline void keccak256(const uint8_t* msg, size_t len, uint8_t out[32]) {
