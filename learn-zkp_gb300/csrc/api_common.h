@@ -215,7 +215,8 @@ struct bf_pcs {
   size_t Q = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
-  cudaStream_t aux = nullptr;  // second stream for independent work of one commit
+  cudaStream_t aux = nullptr;   // second stream for independent work of one commit
+  cudaStream_t aux2 = nullptr;  // third: the first NTT pass of a sliced host commit
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   // bf_commit copies host evaluations in slices on `aux`; the first NTT pass
   // starts on each slice when its event completes

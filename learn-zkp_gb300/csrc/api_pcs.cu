@@ -172,6 +172,7 @@ using namespace bfapi;
 
 bf_pcs::~bf_pcs() {
   if (aux) cudaStreamSynchronize(aux);
+  if (aux2) cudaStreamSynchronize(aux2);
   if (stream) cudaStreamSynchronize(stream);
   sc_ws.release();
   eval_ws.release();
@@ -179,6 +180,7 @@ bf_pcs::~bf_pcs() {
   if (pool) cudaMemPoolDestroy(pool);
   if (stream && own_stream) cudaStreamDestroy(stream);
   if (aux) cudaStreamDestroy(aux);
+  if (aux2) cudaStreamDestroy(aux2);
   if (ev_fork) cudaEventDestroy(ev_fork);
   if (ev_join) cudaEventDestroy(ev_join);
   for (cudaEvent_t e : slice_ev)
@@ -302,7 +304,8 @@ int commit_enqueue(bf_pcs* p, bf_commitment* cm, const uint4* data, cudaStream_t
     // encode; for width 1 and d >= 1 the last NTT pass also hashes the leaves
     ProfScope ps(p->prof, st, P_ENCODE);
     CU(bf::launch_encode(data, cw, p->d, p->log2_c, w, p->tw_view.as<bf::TwiddleView>(), st,
-                         pairs ? tree : nullptr, pairs ? pit : nullptr, p->tune, slice_ready, slices));
+                         pairs ? tree : nullptr, pairs ? pit : nullptr, p->tune, slice_ready, slices,
+                         slices > 0 ? p->aux2 : nullptr, p->ev_fork, p->ev_join));
   }
   if (!pairs) {
     ProfScope ps(p->prof, st, P_LEAVES);
@@ -444,6 +447,7 @@ int bf_pcs_setup(int device, int lambda, int log2_c, int num_vars, void* stream,
     p->own_stream = true;
   }
   CU(cudaStreamCreateWithFlags(&p->aux, cudaStreamNonBlocking));
+  CU(cudaStreamCreateWithFlags(&p->aux2, cudaStreamNonBlocking));
   CU(cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming));
   CU(cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming));
   for (cudaEvent_t& e : p->slice_ev) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));

@@ -37,11 +37,14 @@ bool tune_valid(const Tune& t);
 // leaves and the first folded-codeword leaves.
 // With `slices` > 0, slice k of the input (rows [k N/slices, (k+1) N/slices))
 // is ready once slice_ready[k] has completed: the first pass waits for each
-// slice before the blocks that read it.
+// slice before the blocks that read it, its launches alternating between st
+// and st2 (joined back to st through the events ev_a, ev_b) when those are
+// given.
 cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t width, const TwiddleView* tw,
                           cudaStream_t st, uint4* leaves = nullptr, uint4* pair_leaves = nullptr,
                           const Tune& tune = Tune(), const cudaEvent_t* slice_ready = nullptr,
-                          int slices = 0);
+                          int slices = 0, cudaStream_t st2 = nullptr, cudaEvent_t ev_a = nullptr,
+                          cudaEvent_t ev_b = nullptr);
 cudaError_t launch_leaves_elem(const uint4* cw, uint4* leaves, size_t n, size_t width, cudaStream_t st);
 cudaError_t launch_leaves_pair(const uint4* pi, uint4* leaves, size_t n, cudaStream_t st);
 // Build every level above `leaves` (n leaves, power of two); levels are stored

@@ -193,7 +193,8 @@ bool tune_valid(const Tune& t) {
 
 cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t width, const TwiddleView* tw,
                           cudaStream_t st, uint4* leaves, uint4* pair_leaves, const Tune& tune,
-                          const cudaEvent_t* slice_ready, int slices) {
+                          const cudaEvent_t* slice_ready, int slices, cudaStream_t st2, cudaEvent_t ev_a,
+                          cudaEvent_t ev_b) {
   if (width == 0 || width > 65535 || (width != 1 && (leaves || pair_leaves))) return cudaErrorInvalidValue;
   if (!tune_valid(tune)) return cudaErrorInvalidValue;
   const size_t c = (size_t)1 << log2_c;
@@ -238,20 +239,35 @@ cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t w
       cudaError_t e = cudaStreamWaitEvent(st, slice_ready[slices - 1], 0);  // copies are in order
       if (e != cudaSuccess) return e;
     }
+    // Pieces alternate between st and st2 (when given): launches on one
+    // stream run one after another, and a piece of a few hundred blocks ends
+    // in a mostly idle wave; on two streams the next piece fills it.
+    const bool two = pieces > 1 && st2 && ev_a && ev_b;
+    if (two) {
+      cudaError_t e = cudaEventRecord(ev_a, st);  // st2 after everything before the pass on st
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(st2, ev_a, 0);
+      if (e != cudaSuccess) return e;
+    }
     for (int piece = 0; piece < pieces; ++piece) {
+      cudaStream_t sp = (two && (piece & 1)) ? st2 : st;
       if (pieces > 1) {
-        cudaError_t e = cudaStreamWaitEvent(st, slice_ready[piece], 0);
+        cudaError_t e = cudaStreamWaitEvent(sp, slice_ready[piece], 0);
         if (e != cudaSuccess) return e;
       }
       p.piece_log = piece_log;
       p.piece = piece;
       const dim3 grid((unsigned)(c * (tiles >> piece_log)), (unsigned)width);
       if (p.leaves)
-        ntt_pass_kernel<true><<<grid, threads, sizeof(uint4) << T, st>>>(m, cw, p, tw);
+        ntt_pass_kernel<true><<<grid, threads, sizeof(uint4) << T, sp>>>(m, cw, p, tw);
       else
-        ntt_pass_kernel<false><<<grid, threads, sizeof(uint4) << T, st>>>(m, cw, p, tw);
+        ntt_pass_kernel<false><<<grid, threads, sizeof(uint4) << T, sp>>>(m, cw, p, tw);
       COUNT_LAUNCH();
       cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+    }
+    if (two) {  // the rest of the encode waits for the pieces on st2
+      cudaError_t e = cudaEventRecord(ev_b, st2);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev_b, 0);
       if (e != cudaSuccess) return e;
     }
     top -= T;
