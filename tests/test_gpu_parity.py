@@ -376,3 +376,17 @@ def test_concurrent_provers_on_threads(bg):
     for _ in range(2):
         with ThreadPoolExecutor(4) as ex:
             assert list(ex.map(prove, cases)) == alone
+
+
+@pytest.mark.parametrize("log2_c", [3, 4])
+def test_large_blowups_match_oracle(bg, log2_c):
+    """Blowup 8 and 16 (more cosets per NTT pass, other tail thresholds):
+    roots, claims and proofs equal the oracle's; the proofs verify on the
+    host and in the batched GPU verifier."""
+    for n, width in ((0, 1), (1, 2), (2, 1), (5, 3), (8, 1), (11, 2), (16, 1)):
+        pcs, comm, evals, point, values, ch, proof = harness_w(bg, n, log2_c, width, 600 + 10 * n + log2_c)
+        root_o, values_o, blob = O.harness_prepare(n, log2_c, evals, point, width)
+        assert comm.root == root_o and np.array_equal(values, values_o), (n, log2_c, width)
+        assert proof == O.open_proof(n, log2_c, evals, point, values_o, blob, width), (n, log2_c, width)
+        pcs.verify(comm.root, [bg.PolyEvals(values, point)], proof, ch.clone())
+        assert pcs.verify_batch([(comm.root, [bg.PolyEvals(values, point)], proof, ch.clone())]) == [0]
