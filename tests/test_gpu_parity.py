@@ -390,3 +390,17 @@ def test_large_blowups_match_oracle(bg, log2_c):
         assert proof == O.open_proof(n, log2_c, evals, point, values_o, blob, width), (n, log2_c, width)
         pcs.verify(comm.root, [bg.PolyEvals(values, point)], proof, ch.clone())
         assert pcs.verify_batch([(comm.root, [bg.PolyEvals(values, point)], proof, ch.clone())]) == [0]
+
+
+def test_random_configurations_match_oracle(bg):
+    """Sixty configurations drawn with a fixed seed (num_vars 0..13, blowup
+    1..16, 1..17 columns): every root, claim and proof equals the oracle's."""
+    rng = np.random.default_rng(20261203)
+    for k in range(60):
+        log2_c = int(rng.integers(0, 5))
+        n = int(rng.integers(0, 14 - (log2_c > 2) * 3))
+        width = int(rng.choice([1, 1, 1, 2, 3, 5, 9, 17]))
+        pcs, comm, evals, point, values, ch, proof = harness_w(bg, n, log2_c, width, 30000 + k)
+        root_o, values_o, blob = O.harness_prepare(n, log2_c, evals, point, width)
+        assert comm.root == root_o and np.array_equal(values, values_o), (k, n, log2_c, width)
+        assert proof == O.open_proof(n, log2_c, evals, point, values_o, blob, width), (k, n, log2_c, width)
