@@ -199,3 +199,15 @@ def test_engine_cancel_queued_job(bg):
     for i in (0, 1, 3, 4):
         assert res[i]["status"] == 0 and res[i]["proof"] == alone(bg, *jobs[i])[2], i
     assert not eng.cancel(keys[0])  # finished: nothing to cancel
+
+
+@pytest.mark.parametrize("log2_c", [0, 2])
+def test_engine_other_blowups(bg, log2_c):
+    """Blowup 1 (no queries, binary_reed_solomon.rs:56-59) and 4 in the engine:
+    the same proofs as one at a time."""
+    jobs = make_jobs([0, 3, 9, 12, 6, 14], 8900 + log2_c)
+    res = bg.Engine(max_inflight=4, log2_c=log2_c).prove(jobs)
+    for (n, ev, pt), r in zip(jobs, res):
+        root, values, proof = alone(bg, n, ev, pt, log2_c)
+        assert r["status"] == 0 and r["root"] == root and np.array_equal(r["value"], values), (n, log2_c)
+        assert r["proof"] == proof, (n, log2_c)
