@@ -296,7 +296,9 @@ def run_served(bg, device, log2_c, lo=12, hi=24, per_size=10, loads=(0.25, 0.5, 
 
     rng = np.random.default_rng(seed)
     inputs = gen_inputs(list(range(lo, hi + 1)), 2000)
-    eng = bg.Engine(device=device, log2_c=log2_c, max_inflight=16)
+    # serving policy: a free slot takes the smallest queued request, and
+    # requests of <= 2^18 evaluations run on high-priority streams
+    eng = bg.Engine(device=device, log2_c=log2_c, max_inflight=16, smallest_first=True, priority_max_vars=18)
     # every size set up once (twiddles, pools) before anything is timed
     eng.prove([(n, inputs[n][0], inputs[n][1]) for n in range(lo, hi + 1)])
     # capacity: saturated batch of the same size distribution
@@ -308,7 +310,8 @@ def run_served(bg, device, log2_c, lo=12, hi=24, per_size=10, loads=(0.25, 0.5, 
     eng.prove([(n, inputs[n][0], inputs[n][1]) for n in cap_sizes])
     capacity = per_level / (time.perf_counter() - t)
     out = {"workload": f"Poisson arrivals, sizes log-uniform 2^{lo}..2^{hi}, blowup {1 << log2_c}, "
-                       f"{per_level} requests per load (each size {per_size} times, random order), host inputs",
+                       f"{per_level} requests per load (each size {per_size} times, random order), host inputs, "
+                       "smallest-first admission, high-priority streams for <= 2^18",
            "size_range": [lo, hi],
            "capacity_proofs_per_s": capacity, "levels": []}
     eng.start()

@@ -211,6 +211,13 @@ int bf_engine_cancel(bf_engine* e, bf_job* job);
 int bf_engine_autotune(bf_engine* e, int reps);
 int bf_engine_set_tune(bf_engine* e, const int* vals, int n);
 int bf_engine_graphs(bf_engine* e, int on);
+/* Serving policy.  smallest_first != 0: a free slot takes the queued job with
+ * the fewest variables (default: arrival order).  prio_max_vars >= 0: jobs of
+ * at most that many variables run on high-priority CUDA streams (direct
+ * launches; graph replay keeps normal priority), whose blocks are dispatched
+ * ahead of the waiting blocks of larger jobs (default -1: off).  Call only
+ * while no job is in flight. */
+int bf_engine_schedule(bf_engine* e, int smallest_first, int prio_max_vars);
 /* Host-side accounting since creation: out = {ms spent admitting jobs
  * (allocation, capture, staging, enqueue), of which ms in graph launches,
  * ms completing jobs (query sampling, proof readout), plans built, plans

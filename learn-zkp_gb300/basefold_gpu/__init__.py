@@ -436,7 +436,9 @@ class Engine:
     requests from a background thread (continuous batching)."""
 
     def __init__(self, device: int = 0, lambda_: int = 128, log2_c: int = 1, max_inflight: int = 16,
-                 mem_budget: int = 0, autotune_reps: int = 0, graphs: bool = False):
+                 mem_budget: int = 0, autotune_reps: int = 0, graphs: bool = False,
+                 smallest_first: bool = False, priority_max_vars: int = -1):
+        """smallest_first / priority_max_vars: the serving policy (bf_engine_schedule)."""
         h = C.c_void_p()
         check(lib().bf_engine_create(device, lambda_, log2_c, max_inflight, mem_budget, C.byref(h)))
         self._h, self.log2_c = h, log2_c
@@ -444,6 +446,7 @@ class Engine:
         if autotune_reps:
             check(lib().bf_engine_autotune(h, autotune_reps))
         check(lib().bf_engine_graphs(h, 1 if graphs else 0))
+        check(lib().bf_engine_schedule(h, 1 if smallest_first else 0, priority_max_vars))
 
     def __del__(self):
         h = getattr(self, "_h", None)

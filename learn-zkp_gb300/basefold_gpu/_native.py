@@ -20,7 +20,7 @@ EXPORTS = [
     "bf_profile_read", "bf_test_gf_mul", "bf_test_keccak_f", "bf_engine_create", "bf_engine_free",
     "bf_engine_proof_size", "bf_engine_prove", "bf_engine_start", "bf_engine_stop", "bf_engine_submit",
     "bf_engine_poll", "bf_eval_noalloc", "bf_pcs_autotune", "bf_pcs_get_tune", "bf_pcs_set_tune",
-    "bf_engine_autotune", "bf_engine_graphs", "bf_engine_stats", "bf_verify_batch", "bf_engine_set_tune", "bf_engine_cancel",
+    "bf_engine_autotune", "bf_engine_graphs", "bf_engine_stats", "bf_verify_batch", "bf_engine_set_tune", "bf_engine_cancel", "bf_engine_schedule",
 ]
 
 BF_OK = 0
@@ -127,6 +127,7 @@ def lib():
         "bf_verify_batch": ([vp, C.POINTER(BfVerifyJob), sz], i),
         "bf_engine_set_tune": ([vp, C.POINTER(i), i], i),
         "bf_engine_cancel": ([vp, vp], i),
+        "bf_engine_schedule": ([vp, i, i], i),
     }
     for name, (args, res) in decl.items():
         f = getattr(L, name)

@@ -105,6 +105,13 @@ struct bf_engine {
   std::map<int, bf_pcs*> pcs_by_n;
   std::mutex pcs_mu;  // pcs_by_n: bf_engine_proof_size may set a size up while the engine runs
   std::vector<cudaStream_t> streams;
+  // Per slot, a stream of the device's highest priority: jobs of at most
+  // prio_max_vars variables run there, so their blocks are dispatched ahead
+  // of waiting blocks of larger jobs (whose long kernels retire blocks
+  // continuously).  -1: off.
+  std::vector<cudaStream_t> streams_hi;
+  int prio_max_vars = -1;
+  bool smallest_first = false;  // admit the smallest queued job first (else in arrival order)
   std::vector<int> free_slots;
   PinnedBuf pin;  // 128 bytes per slot: roots (64) + value (16)
   std::deque<Job*> queue;
@@ -182,7 +189,8 @@ int admit(bf_engine* e, Job* j) {
   bf_pcs* p = j->pcs;
   const size_t need = bf_pcs_proof_size(p, 1, 1);
   if (pj->proof_cap < need) return fail(BF_ERR_BUFFER, "job proof buffer needs %zu bytes", need);
-  j->st = e->streams[j->slot];
+  const bool hi = e->prio_max_vars >= 0 && pj->num_vars <= e->prio_max_vars && !e->streams_hi.empty();
+  j->st = hi ? e->streams_hi[j->slot] : e->streams[j->slot];
   j->cm.reset(new bf_commitment());
   j->cm->pcs = p;
   j->cm->width = 1;
@@ -360,7 +368,11 @@ bool progress(bf_engine* e) {
     {
       std::lock_guard<std::mutex> lk(e->mu);
       if (e->queue.empty() || e->free_slots.empty()) break;
-      Job* cand = e->queue.front();
+      auto qit = e->queue.begin();
+      if (e->smallest_first)
+        for (auto it = e->queue.begin(); it != e->queue.end(); ++it)
+          if ((*it)->pub->num_vars < (*qit)->pub->num_vars) qit = it;
+      Job* cand = *qit;
       if (e->use_graphs) {
         // a free slot that has a plan of this size, else the free slot with the
         // least plan memory; room for a new plan comes from idle plans, least
@@ -403,7 +415,7 @@ bool progress(bf_engine* e) {
         slot = e->free_slots.back();
         e->free_slots.pop_back();
       }
-      e->queue.pop_front();
+      e->queue.erase(qit);
       j = cand;
     }
     j->slot = slot;
@@ -472,9 +484,14 @@ void worker_loop(bf_engine* e) {
 
 bf_engine::~bf_engine() {
   for (cudaStream_t s : streams) cudaStreamSynchronize(s);
+  for (cudaStream_t s : streams_hi) cudaStreamSynchronize(s);
   plans.clear();
   for (auto& kv : pcs_by_n) bf_pcs_free(kv.second);
   for (cudaStream_t s : streams) {
+    cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+  }
+  for (cudaStream_t s : streams_hi) {
     cudaStreamSynchronize(s);
     cudaStreamDestroy(s);
   }
@@ -498,11 +515,17 @@ int bf_engine_create(int device, int lambda, int log2_c, int max_inflight, size_
     mem_budget = free_b / 10 * 8;
   }
   e->mem_budget = mem_budget;
+  int prio_least = 0, prio_greatest = 0;
+  CU(cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest));
   for (int i = 0; i < max_inflight; ++i) {
     cudaStream_t s;
     CU(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     e->streams.push_back(s);
     e->free_slots.push_back(max_inflight - 1 - i);
+    if (prio_greatest != prio_least) {
+      CU(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, prio_greatest));
+      e->streams_hi.push_back(s);
+    }
   }
   CU(e->pin.ensure(128 * (size_t)max_inflight));
   e->plans.resize(max_inflight);
@@ -630,6 +653,14 @@ int bf_engine_set_tune(bf_engine* e, const int* vals, int n) {
   }
   std::memcpy(e->tune_vals, vals, sizeof(e->tune_vals));
   e->has_tune = true;
+  return BF_OK;
+}
+
+int bf_engine_schedule(bf_engine* e, int smallest_first, int prio_max_vars) {
+  if (!e || prio_max_vars < -1 || prio_max_vars > 30) return fail(BF_ERR_ARG, "bad argument");
+  if (e->running || !e->inflight.empty()) return fail(BF_ERR_ARG, "engine busy");
+  e->smallest_first = smallest_first != 0;
+  e->prio_max_vars = prio_max_vars;
   return BF_OK;
 }
 

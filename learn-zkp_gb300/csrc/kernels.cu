@@ -67,6 +67,17 @@ static unsigned grid_for(size_t n, int threads, int per_sm = 8) {
   return (unsigned)want;
 }
 
+// One element per thread for the long grid-stride kernels (Merkle levels and
+// leaves, fold): blocks then live microseconds instead of the whole
+// launch, so work of other streams (other jobs of the engine) gets SM room as
+// blocks retire rather than only when the launch ends.
+static unsigned grid_short(size_t n, int threads) {
+  size_t want = (n + threads - 1) / threads;
+  if (want > 0x7fffffffull) want = 0x7fffffffull;
+  if (want == 0) want = 1;
+  return (unsigned)want;
+}
+
 // ---------------------------------------------------------------------------
 // Reed–Solomon encoding (binary_reed_solomon.rs:67-82 with the coset NTTs of
 // binary.rs:55-105).  Codeword = additive NTT of pad(bitrev(m)) over
@@ -349,15 +360,15 @@ __global__ void __launch_bounds__(128) leaves_rows_kernel(const uint4* __restric
 
 cudaError_t launch_leaves_elem(const uint4* cw, uint4* leaves, size_t n, size_t width, cudaStream_t st) {
   if (width == 1)
-    leaves_elem_kernel<<<grid_for(n, 128, 16), 128, 0, st>>>(cw, leaves, n);
+    leaves_elem_kernel<<<grid_short(n, 128), 128, 0, st>>>(cw, leaves, n);
   else
-    leaves_rows_kernel<<<grid_for(n, 128, 16), 128, 0, st>>>(cw, leaves, n, width);
+    leaves_rows_kernel<<<grid_short(n, 128), 128, 0, st>>>(cw, leaves, n, width);
   COUNT_LAUNCH();
   return cudaGetLastError();
 }
 
 cudaError_t launch_leaves_pair(const uint4* pi, uint4* leaves, size_t n, cudaStream_t st) {
-  leaves_pair_kernel<<<grid_for(n, 128, 16), 128, 0, st>>>(pi, leaves, n);
+  leaves_pair_kernel<<<grid_short(n, 128), 128, 0, st>>>(pi, leaves, n);
   COUNT_LAUNCH();
   return cudaGetLastError();
 }
@@ -412,7 +423,7 @@ cudaError_t launch_tree(uint4* leaves, size_t n, cudaStream_t st, uint4* root_ou
     }
     const size_t h = n >> 1;
     uint4* nxt = cur + 2 * n;
-    level_kernel<<<grid_for(h, 128, 16), 128, 0, st>>>(cur, nxt, h);
+    level_kernel<<<grid_short(h, 128), 128, 0, st>>>(cur, nxt, h);
     COUNT_LAUNCH();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -557,7 +568,7 @@ __global__ void __launch_bounds__(128) fold_leaves_kernel(const uint4* __restric
 
 cudaError_t launch_fold_leaves(const uint4* pi, uint4* out, uint4* leaves, size_t n_leaves, const uint4* tw_lo,
                                const uint4* tw_hi, uint4 r, cudaStream_t st, const uint4* xp) {
-  fold_leaves_kernel<<<grid_for(n_leaves, 128, 16), 128, 0, st>>>(pi, out, leaves, n_leaves, tw_lo, tw_hi, r, xp);
+  fold_leaves_kernel<<<grid_short(n_leaves, 128), 128, 0, st>>>(pi, out, leaves, n_leaves, tw_lo, tw_hi, r, xp);
   COUNT_LAUNCH();
   return cudaGetLastError();
 }
@@ -629,8 +640,8 @@ __global__ void __launch_bounds__(128) fold_fix_kernel(FoldFixParams p, uint4 r)
 
 cudaError_t launch_fold_fix(const FoldFixParams& p0, uint4 r, cudaStream_t st) {
   FoldFixParams p = p0;
-  p.fold_blocks = grid_for(p.n_leaves, 128, 16);
-  const unsigned fix_blocks = grid_for(p.half, 128, 8);
+  p.fold_blocks = grid_short(p.n_leaves, 128);
+  const unsigned fix_blocks = grid_for(p.half, 128, 8);  // few blocks: each ends in one atomic
   fold_fix_kernel<<<p.fold_blocks + fix_blocks, 128, 0, st>>>(p, r);
   COUNT_LAUNCH();
   return cudaGetLastError();
