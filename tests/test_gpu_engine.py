@@ -211,3 +211,23 @@ def test_engine_other_blowups(bg, log2_c):
         root, values, proof = alone(bg, n, ev, pt, log2_c)
         assert r["status"] == 0 and r["root"] == root and np.array_equal(r["value"], values), (n, log2_c)
         assert r["proof"] == proof, (n, log2_c)
+
+
+def test_engine_serving_policy_keeps_proofs(bg):
+    """Smallest-first admission and high-priority streams for small jobs change
+    the order of work, never a proof byte; bad policy values are refused."""
+    jobs = make_jobs([14, 3, 12, 9, 16, 6, 11], 9100)
+    eng = bg.Engine(max_inflight=2, smallest_first=True, priority_max_vars=11)
+    eng.start()
+    keys = {eng.submit(n, ev, pt, tag=i): i for i, (n, ev, pt) in enumerate(jobs)}
+    res, t0 = {}, time.time()
+    while len(res) < len(jobs) and time.time() - t0 < 120:
+        for tag, r in eng.poll():
+            res[tag] = r
+        time.sleep(0.001)
+    eng.stop()
+    assert len(keys) == len(jobs)
+    for i, (n, ev, pt) in enumerate(jobs):
+        assert res[i]["status"] == 0 and res[i]["proof"] == alone(bg, n, ev, pt)[2], i
+    with pytest.raises(bg.BasefoldGpuError):
+        bg.Engine(max_inflight=1, priority_max_vars=31)
