@@ -654,11 +654,12 @@ def main():
             served["cpu_baseline"] = served_cpu_reference(log2_c, served["size_range"])
     clocks = clk.summary()
     perms_per_s = (nodes / (tree_ms / 1e3)) if tree_ms else None
-    # the integer-ALU roofline of the same kernels: 60 ALU thread-ops/clk/SM
-    # (LOP3/SHF, measured on GB300) x SMs x SM clock, over 4116 instructions
-    # per Keccak-f on interleaved lanes (ncu, level_kernel)
+    # the integer-ALU roofline of the same kernels: the ALU pipe's 64 thread-ops
+    # per clock per SM (16 lanes on each of 4 sub-partitions; a LOP3/SHF
+    # microbenchmark sustains 60, the largest Merkle levels 63) x SMs x SM
+    # clock, over 4116 instructions per Keccak-f on interleaved lanes (ncu)
     num_sms = bg.device_info(local)["num_sms"]
-    alu_peak = 60.0 * num_sms * (clocks.get("sm_mhz") or 2070.0) * 1e6 / 4116.0
+    alu_peak = 64.0 * num_sms * (clocks.get("sm_mhz") or 2070.0) * 1e6 / 4116.0
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -673,7 +674,7 @@ def main():
                      "alu_frac": (perms_per_s / alu_peak) if perms_per_s else None},
         "int_pipe": {"keccak_perms_per_s": perms_per_s, "alu_peak_perms_per_s": alu_peak,
                      "frac": (perms_per_s / alu_peak) if perms_per_s else None,
-                     "peak_source": "60 ALU thread-ops/clk/SM measured x SMs x sampled SM clock / "
+                     "peak_source": "64 ALU thread-ops/clk/SM (pipe width) x SMs x sampled SM clock / "
                                     "4116 instructions per Keccak-f (ncu, level_kernel)",
                      "kernel_share_of_step": tree_ms / total_ms_classes if total_ms_classes else None},
         "kernel_ms_per_step": {k: v[0] / args.steps for k, v in prof.items()},
