@@ -28,6 +28,24 @@ def test_library_exports_every_declared_symbol(built_lib):
     assert sorted(_native.EXPORTS) == decl
 
 
+def test_status_codes_match_header(built_lib):
+    """Every BF_* status code of the header has the same value in the binding,
+    and the verifier codes are BasefoldError's (basefold.rs:79-84) plus 4."""
+    from basefold_gpu import _native
+
+    bg = built_lib
+    text = open(os.path.join(ROOT, "include", "basefold_gpu.h")).read()
+    codes = {k: int(v) for k, v in re.findall(r"#define (BF_[A-Z_]+) \(?(-?\d+)\)?", text)}
+    assert len(codes) >= 14
+    for name, value in codes.items():
+        if name.startswith("BF_VERIFY_"):
+            continue
+        assert getattr(_native, name) == value, name
+    verify = {v: k for k, v in codes.items() if k.startswith("BF_VERIFY_") and v}
+    assert {v: bg.BasefoldError.KINDS[v] for v in verify} == {
+        1: "InvalidFinalPoly", 2: "InvalidQuery", 3: "Mmcs", 4: "Malformed"}
+
+
 def test_challenger_matches_oracle(built_lib):
     bg = built_lib
     ch = bg.GenericChallenger(b"init")
