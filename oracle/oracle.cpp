@@ -461,8 +461,19 @@ struct Code {
   }
   // encode_batch (:67-82)
   std::vector<u128> encode_batch(const std::vector<u128>& m, size_t width) const {
-    size_t kd = k_d(), nd = n_d();
-    std::vector<u128> out(nd * width, 0);
+    std::vector<u128> out = encode_batch_unpermuted(m, width);
+    size_t nd = n_d();
+    std::vector<u128> res(nd * width);
+    int lb = log2_n_d();
+    for (size_t r = 0; r < nd; ++r)
+      for (size_t c0 = 0; c0 < width; ++c0) res[r * width + c0] = out[reverse_bits_len(r, lb) * width + c0];
+    return res;
+  }
+  // encode_batch before its final bit_reverse_rows (:80-81): row r of the
+  // codeword is row reverse_bits_len(r, log2_n_d) of this matrix.
+  std::vector<u128> encode_batch_unpermuted(const std::vector<u128>& m, size_t width) const {
+    size_t kd = k_d();
+    std::vector<u128> out(n_d() * width, 0);
     for (size_t r = 0; r < kd; ++r)  // bit_reverse_rows
       for (size_t c0 = 0; c0 < width; ++c0) out[r * width + c0] = m[reverse_bits_len(r, d) * width + c0];
     size_t len = width * kd;  // pad_to_height + copy_within
@@ -475,11 +486,7 @@ struct Code {
       }
       ntt_forward(out.data() + j * len, width, d, tabs);
     }
-    std::vector<u128> res(nd * width);
-    int lb = log2_n_d();
-    for (size_t r = 0; r < nd; ++r)
-      for (size_t c0 = 0; c0 < width; ++c0) res[r * width + c0] = out[reverse_bits_len(r, lb) * width + c0];
-    return res;
+    return out;
   }
   // interpolate (:103-109)
   static u128 interpolate_raw(u128 t, u128 lo, u128 hi, u128 r) {
@@ -1343,6 +1350,49 @@ int orc_commit(int n, int log2_c, size_t width, const uint8_t* data, uint8_t* ro
   Code code(128, log2_c, n);
   CommitmentData cd = commit(code, load_vec(data, width << n), width);
   std::memcpy(root, cd.codewords.root().b, 32);
+  return 0;
+}
+
+// The root of orc_commit computed in bounded memory, for the largest
+// commits (2^28-row codewords): the codeword is hashed in subtrees of at most
+// 2^14 leaves, each on one thread with its own scratch, and only the subtree
+// roots are kept; leaf r reads codeword row r through the bit reversal that
+// encode_batch applies last.  Same tree and root as merkle_commit.
+int orc_commit_root(int n, int log2_c, size_t width, const uint8_t* data, uint8_t* root) {
+  if (n < 0 || log2_c < 0 || n + log2_c > 28 || width == 0) return -1;
+  Code code(128, log2_c, n);
+  const std::vector<u128> cw = code.encode_batch_unpermuted(load_vec(data, width << n), width);
+  const size_t h = code.n_d();
+  const int lb = code.log2_n_d();
+  const size_t sub = std::min<size_t>(h, (size_t)1 << 14);
+  std::vector<Digest> tops(h / sub);
+  parallel_for(tops.size(), [&](size_t b, size_t e) {
+    std::vector<Digest> lv(sub);
+    std::vector<u128> row(width);
+    uint8_t buf[64];
+    for (size_t t = b; t < e; ++t) {
+      for (size_t i = 0; i < sub; ++i) {
+        const size_t src = reverse_bits_len(t * sub + i, lb) * width;
+        for (size_t c0 = 0; c0 < width; ++c0) row[c0] = cw[src + c0];
+        keccak256(reinterpret_cast<const uint8_t*>(row.data()), 16 * width, lv[i].b);
+      }
+      for (size_t m = sub; m > 1; m >>= 1)
+        for (size_t i = 0; i < m / 2; ++i) {
+          std::memcpy(buf, lv[2 * i].b, 32);
+          std::memcpy(buf + 32, lv[2 * i + 1].b, 32);
+          keccak256(buf, 64, lv[i].b);
+        }
+      tops[t] = lv[0];
+    }
+  }, 1);
+  uint8_t buf[64];
+  for (size_t m = tops.size(); m > 1; m >>= 1)
+    for (size_t i = 0; i < m / 2; ++i) {
+      std::memcpy(buf, tops[2 * i].b, 32);
+      std::memcpy(buf + 32, tops[2 * i + 1].b, 32);
+      keccak256(buf, 64, tops[i].b);
+    }
+  std::memcpy(root, tops[0].b, 32);
   return 0;
 }
 

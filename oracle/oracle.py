@@ -44,6 +44,7 @@ def lib():
         L.orc_encode.argtypes = [C.c_int, C.c_int, sz, u8p, u8p]
         L.orc_merkle_commit.argtypes = [u8p, sz, sz, u8p, u8p]
         L.orc_commit.argtypes = [C.c_int, C.c_int, sz, u8p, u8p]
+        L.orc_commit_root.argtypes = [C.c_int, C.c_int, sz, u8p, u8p]
         L.orc_eval.argtypes = [C.c_int, sz, u8p, u8p, u8p]
         L.orc_challenger_sample.argtypes = [u8p, sz, C.c_int, sz, C.c_int, u8p, u8p, C.POINTER(sz)]
         L.orc_harness_prepare.argtypes = [C.c_int, C.c_int, sz, u8p, u8p, u8p, u8p, u8p, C.POINTER(sz)]
@@ -206,6 +207,14 @@ def commit(n: int, log2_c: int, data, width: int = 1) -> bytes:
     d = _elems(data)
     root = np.zeros(32, dtype=np.uint8)
     assert lib().orc_commit(n, log2_c, width, _p(d), _p(root)) == 0
+    return root.tobytes()
+
+
+def commit_root(n: int, log2_c: int, data, width: int = 1) -> bytes:
+    """commit()'s root in bounded host memory (subtrees of 2^14 leaves)."""
+    d = _elems(data)
+    root = np.zeros(32, dtype=np.uint8)
+    assert lib().orc_commit_root(n, log2_c, width, _p(d), _p(root)) == 0
     return root.tobytes()
 
 

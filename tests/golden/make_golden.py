@@ -14,6 +14,8 @@
    listed beside each case.
 
 Usage:  python tests/golden/make_golden.py [--reference /path/to/learn-zkp]
+        (or LEARN_ZKP_REFERENCE=/path/to/learn-zkp); without a reference
+        checkout only oracle_vectors.json is regenerated.
 """
 import argparse
 import hashlib
@@ -89,9 +91,10 @@ def sumcheck_cases():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("LEARN_ZKP_REFERENCE"),
+                    help="learn-zkp checkout to read constants from (default: $LEARN_ZKP_REFERENCE)")
     args = ap.parse_args()
-    if os.path.isdir(args.reference):
+    if args.reference and os.path.isdir(args.reference):
         with open(os.path.join(HERE, "reference_polyval.json"), "w") as f:
             json.dump(reference_constants(args.reference), f, indent=1)
     vec = {"basefold": basefold_cases(), "sumcheck": sumcheck_cases()}

@@ -1,9 +1,18 @@
-"""The headline sizes, checked bit for bit or through size-independent
-properties: a 2^24-evaluation proof identical to the oracle's and accepted by
-both verifiers, 2^22 commits at blowup 4 against the oracle, and the product
-sumcheck at 2^20 and 2^24 points (round identities through the verifier, the
-final evaluations against direct multilinear evaluation at the challenges).
+"""The headline sizes, checked bit for bit against the oracle:
+
+* a 2^24-evaluation proof identical to the oracle's and accepted by both
+  verifiers;
+* the encode + Merkle commit sweep (2^18 .. 2^26 evaluations, blowup 2 and
+  4): every root equal to the oracle's (the 2^26 roots through the oracle's
+  bounded-memory root, which hashes the codeword in subtrees);
+* the product sumcheck of 2 and 3 polynomials at 2^20 and 2^24 points: every
+  compressed round polynomial, every challenge, the final evaluations and the
+  final claim equal to the oracle's, plus the verifier identity and the final
+  evaluations against direct multilinear evaluation at the challenges.
+
 Tolerance: bit-exact (exact GF(2^128) and Keccak arithmetic)."""
+import os
+
 import numpy as np
 import pytest
 
@@ -34,15 +43,42 @@ def test_proof_2_24_matches_oracle_and_verifies(built_lib):
     assert O.verify(n, log2_c, comm.root, point, values, blob, proof) == 0
 
 
-def test_commit_2_22_blowup_4_matches_oracle(built_lib):
+def _host_mem_available_gb():
+    try:
+        with open("/proc/meminfo") as f:
+            for line in f:
+                if line.startswith("MemAvailable:"):
+                    return int(line.split()[1]) / 2**20
+    except OSError:
+        pass
+    return None
+
+
+# (num_vars, log2 blowup): every point of the encode + Merkle commit sweep
+SWEEP = [(n, c) for c in (1, 2) for n in (18, 20, 22, 24, 26)]
+
+
+@pytest.mark.parametrize("n,log2_c", SWEEP, ids=[f"2^{n}-c{1 << c}" for n, c in SWEEP])
+def test_commit_sweep_root_matches_oracle(built_lib, n, log2_c):
     bg = built_lib
-    n, log2_c = 22, 2
-    evals = rand.random_elems(1 << n, 2222)
+    if n + log2_c >= 27:
+        # the oracle's bounded-memory root holds the codeword (16 B x 2^(n+c))
+        # and its twiddle tables (same size) on the host
+        need = 3 * (16 << (n + log2_c)) / 2**30
+        avail = _host_mem_available_gb()
+        if avail is not None and avail < need + 8:
+            pytest.skip(f"host memory: {avail:.0f} GB available, {need + 8:.0f} GB needed")
+    evals = rand.random_elems(1 << n, 1800 + 10 * n + log2_c)
     pcs = bg.Basefold.setup(bg.BasefoldConfig(bg.BinaryReedSolomonCode(128, log2_c, n)))
-    assert pcs.commit(evals).root == O.commit(n, log2_c, evals)
+    comm = pcs.commit(evals)
+    root = comm.root
+    comm.free()
+    del pcs
+    O.set_threads(os.cpu_count() or 1)
+    assert root == O.commit_root(n, log2_c, evals)
 
 
-@pytest.mark.parametrize("k,n", [(2, 20), (3, 20), (2, 24)])
+@pytest.mark.parametrize("k,n", [(2, 20), (3, 20), (2, 24), (3, 24)])
 def test_product_sumcheck_full_size(built_lib, k, n):
     bg = built_lib
     polys = rand.random_elems(k << n, 7700 + 10 * k + n)
@@ -53,6 +89,11 @@ def test_product_sumcheck_full_size(built_lib, k, n):
     claim = np.bitwise_xor.reduce(prod, axis=0)[None]
     init = b"full size"
     rp, r, fe, fc = bg.prove_sumcheck(k, polys, claim, bg.GenericChallenger(init))
+    O.set_threads(os.cpu_count() or 1)
+    rp_o, r_o, fe_o, fc_o = O.sumcheck_prove(k, n, polys, claim, O.challenger_blob(init))
+    assert np.array_equal(rp, rp_o), "round polynomials differ from the oracle"
+    assert np.array_equal(r, r_o), "challenges differ from the oracle"
+    assert np.array_equal(fe, fe_o) and np.array_equal(fc, fc_o), "final evaluations / claim differ"
     assert O.sumcheck_verify(k, n, claim, rp, fe, O.challenger_blob(init)) == 0
     # fix_last_var takes the top variable first: the point is the challenges reversed
     point = r[::-1].copy()
