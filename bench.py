@@ -153,6 +153,34 @@ def tree_nodes(n, log2_c):
     return (nd - 1) + sum(((1 << log2_c) << i) - 1 for i in range(n))
 
 
+# Integer-pipe instruction counts (ncu, this build): a Keccak-f[1600]
+# permutation on bit-interleaved lanes is 4116 ALU-pipe instructions; a
+# GF(2^128) product is 144 IMAD.WIDE (FMA pipe) plus about 276 ALU-pipe
+# instructions (masks, XORs, Karatsuba sums, reduction).  The ALU pipe
+# retires 64 thread-instructions per clock per SM, IMAD.WIDE 24.
+KECCAK_ALU, GF_ALU, GF_IMAD_WIDE = 4116, 276, 144
+
+
+def proof_work(n, log2_c):
+    """(Keccak-f permutations, GF products) of one commit+eval+open, width 1:
+    codeword leaves and tree, every folded-codeword tree (basefold.rs:350-355);
+    encode (c n N / 2), eval (N), eq table, round reductions, fixes and folds."""
+    N, c = 1 << n, 1 << log2_c
+    perms = c * N + (c * N - 1) + sum(2 * (c << i) - 1 for i in range(n))
+    gf = (c * n // 2 + 2 * c + 3) * N
+    return perms, gf
+
+
+def proof_floor_ms(n, log2_c, sm_mhz, num_sms):
+    """Instruction floor of one proof: its ALU-pipe instructions at 64 per
+    clock per SM, or its IMAD.WIDE at 24, whichever is longer."""
+    perms, gf = proof_work(n, log2_c)
+    clk = sm_mhz * 1e6 * num_sms
+    alu = (perms * KECCAK_ALU + gf * GF_ALU) / (64.0 * clk)
+    fma = gf * GF_IMAD_WIDE / (24.0 * clk)
+    return 1e3 * max(alu, fma)
+
+
 def load_peaks():
     try:
         return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))), "measured"
@@ -160,9 +188,9 @@ def load_peaks():
         return {"hbm_gbs": 6800.0}, "fallback"
 
 
-def load_traffic():
+def load_traffic(name="level_kernel_traffic.json"):
     try:
-        return json.load(open(os.path.join(ROOT, "profiles", "level_kernel_traffic.json")))
+        return json.load(open(os.path.join(ROOT, "profiles", name)))
     except OSError:
         return None
 
@@ -188,7 +216,9 @@ def run_reference(args, ws, rank):
     from oracle import oracle as O
 
     O.lib()
-    W, K = min(args.warmup, 1), min(args.steps, 3)  # full-size CPU steps take tens of seconds
+    # every requested step is a full commit+eval+open (about 5 s each on 16
+    # Grace cores at 2^24); capped at 40 steps so a run stays within minutes
+    W, K = min(args.warmup, 5), min(args.steps, 40)
     for _ in range(W):
         cpu_step_oracle(args.n, args.log2_c)
     ts = [cpu_step_oracle(args.n, args.log2_c) for _ in range(K)]
@@ -276,14 +306,77 @@ def run_batched(bg, torch, device, log2_c, count=256, lo=10, hi=22, seed=4):
     t_batch = time.perf_counter() - t
     identical = all(r["proof"] == p for r, p in zip(res, plain))
     digest = hashlib.sha256(b"".join(hashlib.sha256(p).digest() for p in plain)).hexdigest()
+    # the latency-bound share alone: the jobs of at most 2^16 evaluations
+    small = [n for n in sizes if n <= 16]
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for n in small:
+        plain_one(n)
+    torch.cuda.synchronize()
+    t_plain_small = time.perf_counter() - t
+    t = time.perf_counter()
+    eng.prove([(n, dev[n].data_ptr(), inputs[n][1]) for n in small], device_input=True)
+    torch.cuda.synchronize()
+    t_batch_small = time.perf_counter() - t
     release(eng)
     multi = run_multi_column(bg, torch, device, log2_c, sizes, pcs)
     release(pcs, dev)
+    num_sms = bg.device_info(device)["num_sms"]
+    floor_s = sum(proof_floor_ms(n, log2_c, 2070.0, num_sms) for n in sizes) / 1e3
     return {"workload": f"{count} polys, sizes log-uniform 2^{lo}..2^{hi} (seed {seed}), blowup {1 << log2_c}",
             "plain_proofs_per_s": count / t_plain, "batched_proofs_per_s": count / t_batch,
             "speedup": t_plain / t_batch, "proofs_identical": identical, "proofs_sha256": digest,
             "plain_s": t_plain, "batched_s": t_batch, "max_inflight": 32, "multi_column": multi,
-            "note": "batched = engine with per-stream job state machines (continuous batching), not one fused launch"}
+            "floor_s": floor_s, "batched_over_floor": t_batch / floor_s,
+            "small_jobs": {"count": len(small), "plain_s": t_plain_small, "batched_s": t_batch_small,
+                           "speedup": t_plain_small / t_batch_small},
+            "note": "floor = the mix's integer-pipe instructions (Keccak-f 4116 ALU, GF product 276 ALU + "
+                    "144 IMAD.WIDE) at 64 ALU / 24 IMAD.WIDE per clock per SM at 2070 MHz; batched = engine "
+                    "with per-stream job state machines (continuous batching)"}
+
+
+def run_latency(bg, torch, device, log2_c, sizes=(10, 12, 14, 16, 18, 20, 22), reps=7):
+    """Latency of one commit+eval+open per size, device-resident input:
+    through the trait-shaped calls one at a time (three host round trips:
+    root, evaluation, proof) and as one engine job (transcript on the device,
+    one round trip for the query positions), with and without its captured
+    CUDA graph.  Medians of `reps` after warm-up."""
+    inputs = gen_inputs(list(sizes), 7000)
+    rows = []
+    engines = {g: bg.Engine(device=device, log2_c=log2_c, max_inflight=1, graphs=g) for g in (False, True)}
+    for n in sizes:
+        ev, pt = inputs[n]
+        dev = torch.from_numpy(ev).to(f"cuda:{device}")
+        pcs = bg.Basefold.setup(bg.BasefoldConfig(bg.BinaryReedSolomonCode(128, log2_c, n)), device=device)
+
+        def plain():
+            comm = pcs.commit_device(dev.data_ptr(), keep=dev)
+            ch = bg.GenericChallenger.keccak256()
+            ch.observe(comm.root)
+            vals = pcs.eval(pcs.data(comm), pt)
+            ch.observe_ext_slice(vals)
+            pcs.open(comm, [bg.PolyEvals(vals, pt)], ch)
+            comm.free()
+
+        def timed(f):
+            for _ in range(3):
+                f()
+            ts = []
+            for _ in range(reps):
+                torch.cuda.synchronize()
+                t = time.perf_counter()
+                f()
+                ts.append(1e3 * (time.perf_counter() - t))
+            return sorted(ts)[len(ts) // 2]
+
+        row = [n, round(timed(plain), 3)]
+        for g in (False, True):
+            eng = engines[g]
+            row.append(round(timed(lambda: eng.prove([(n, dev.data_ptr(), pt)], device_input=True)), 3))
+        rows.append(row)
+        del pcs, dev
+    release(engines)
+    return {"cols": ["num_vars", "plain_ms", "engine_ms", "engine_graph_ms"], "rows": rows}
 
 
 def run_served(bg, device, log2_c, lo=12, hi=24, per_size=10, loads=(0.25, 0.5, 0.9), seed=5):
@@ -623,22 +716,21 @@ def main():
     Q = pcs.num_queries()
     d2h = len(proof) + 48 * n + 16
     h2d = 16 * (1 << n) + 16 * n + 8 * Q
+    total_ms_classes = sum(v[0] for k, v in prof.items() if k != "encode_last")
 
-    # roofline of the dominant kernel class (tree levels: Keccak of 64-byte nodes)
+    # The trait route: eval of host data with no commitment (bf_eval_data) and
+    # the caller-driven open session (one host round trip per round, the
+    # caller's challenger), beside the device-transcript open.
+    trait = None
+    if ws == 1 and not args.no_extras:
+        trait = run_trait_route(bg, torch, pcs, dev, evals, point)
+
     peaks, peak_kind = load_peaks()
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    tree_ms, tree_launches = prof["tree"]
-    nodes = tree_nodes(n, log2_c) * args.steps
-    alg_bytes_per_launch = 96.0 * nodes / max(tree_launches, 1)
-    avg_launch_s = tree_ms / 1e3 / max(tree_launches, 1)
-    achieved = alg_bytes_per_launch / avg_launch_s / 1e9 if avg_launch_s > 0 else None
-    traffic = None
-    tr = load_traffic()
-    if tr and tr.get("bytes_per_node"):
-        traffic = tr["bytes_per_node"] * nodes / max(tree_launches, 1)
-    total_ms_classes = sum(v[0] for v in prof.values())
-    batched = served = sweep = sumcheck = verify = None
+    num_sms = bg.device_info(local)["num_sms"]
+    batched = served = sweep = sumcheck = verify = latency = None
     if ws == 1 and not args.no_extras:
+        latency = run_latency(bg, torch, local, log2_c)
         batched = run_batched(bg, torch, local, log2_c)
         served = run_served(bg, local, log2_c)
         sweep = run_commit_sweep(bg, torch, local)
@@ -653,45 +745,133 @@ def main():
         if served is not None:
             served["cpu_baseline"] = served_cpu_reference(log2_c, served["size_range"])
     clocks = clk.summary()
+    sm_mhz = clocks.get("sm_mhz") or 2070.0
+
+    # Roofline of the dominant kernel: the last NTT pass (ntt_reg_kernel<true>),
+    # which also hashes the codeword leaves and the first folded-codeword leaves.
+    # Algorithmic bytes per codeword pair: 32 read + 32 written (the pair) + three
+    # 32-byte digests (two codeword leaves, one folded-codeword leaf) = 160 B.
+    c = 1 << log2_c
+    pairs = (c << n) // 2
+    last_ms, last_launches = prof["encode_last"]
+    last_avg_s = last_ms / 1e3 / max(last_launches, 1)
+    achieved = 160.0 * pairs / last_avg_s / 1e9 if last_avg_s > 0 else None
+    tr = load_traffic("ntt_last_pass_traffic.json")
+    traffic = tr["bytes_per_pair"] * pairs if tr and tr.get("bytes_per_pair") else None
+    alu_last = None
+    if tr and tr.get("alu_thread_inst_per_pair") and last_avg_s > 0:
+        alu_last = tr["alu_thread_inst_per_pair"] * pairs / last_avg_s / (64.0 * num_sms * sm_mhz * 1e6)
+    # second: the Merkle levels (level_kernel + subtree + top: Keccak of 64-byte nodes)
+    tree_ms, tree_scopes = prof["tree"]
+    nodes = tree_nodes(n, log2_c) * args.steps
+    tr2 = load_traffic()
     perms_per_s = (nodes / (tree_ms / 1e3)) if tree_ms else None
-    # the integer-ALU roofline of the same kernels: the ALU pipe's 64 thread-ops
-    # per clock per SM (16 lanes on each of 4 sub-partitions; a LOP3/SHF
-    # microbenchmark sustains 60, the largest Merkle levels 63) x SMs x SM
-    # clock, over 4116 instructions per Keccak-f on interleaved lanes (ncu)
-    num_sms = bg.device_info(local)["num_sms"]
-    alu_peak = 64.0 * num_sms * (clocks.get("sm_mhz") or 2070.0) * 1e6 / 4116.0
+    alu_peak = 64.0 * num_sms * sm_mhz * 1e6 / KECCAK_ALU
+    level = {"kernel": "level_kernel+subtree_kernel+tree_top_kernel (Merkle levels)",
+             "achieved_gbs": 96.0 * nodes / (tree_ms / 1e3) / 1e9 if tree_ms else None,
+             "traffic_bytes_per_node": tr2.get("bytes_per_node") if tr2 else None,
+             "keccak_perms_per_s": perms_per_s, "alu_frac": (perms_per_s / alu_peak) if perms_per_s else None}
+    step_bytes = algorithmic_bytes(n, log2_c)
+    floor_ms = proof_floor_ms(n, log2_c, sm_mhz, num_sms)
+    ms_step = ms / args.steps
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "gf2^128+keccak-u64", "data": "synthetic (SplitMix64 seed = rank)",
         "config": workload_config(args),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                     "kernel": "level_kernel+tree_top_kernel (Merkle levels, keccak256 of 64-byte nodes)",
+                     "kernel": {0: "ntt_pass_kernel<true>", 1: "ntt_reg_kernel<true>",
+                                2: "ntt_last_ws_kernel"}.get(pcs.tune["ntt_kind"], "?")
+                               + ": last NTT pass + codeword and first folded-codeword leaf hashes "
+                                 "(160 algorithmic B per codeword pair)",
+                     "launch_ms": last_avg_s * 1e3, "share_of_step": last_ms / max(total_ms_classes, 1e-9),
                      "peak_source": f"{peak_kind} hbm_gbs",
-                     "note": "Keccak-bound (integer ALU pipe), not HBM-bound: alu_frac is the same kernels "
-                             "against the ALU-pipe peak (int_pipe)",
-                     "alu_frac": (perms_per_s / alu_peak) if perms_per_s else None},
-        "int_pipe": {"keccak_perms_per_s": perms_per_s, "alu_peak_perms_per_s": alu_peak,
-                     "frac": (perms_per_s / alu_peak) if perms_per_s else None,
-                     "peak_source": "64 ALU thread-ops/clk/SM (pipe width) x SMs x sampled SM clock / "
-                                    "4116 instructions per Keccak-f (ncu, level_kernel)",
-                     "kernel_share_of_step": tree_ms / total_ms_classes if total_ms_classes else None},
-        "kernel_ms_per_step": {k: v[0] / args.steps for k, v in prof.items()},
-        "algorithmic_bytes_per_step": algorithmic_bytes(n, log2_c),
+                     "alu_frac": alu_last,
+                     "note": "integer-ALU bound (Keccak-f), not HBM bound: alu_frac = ALU-pipe instructions "
+                             "(ncu count per pair) over 64 per clock per SM at the sampled clock"},
+        "roofline_levels": level,
+        "step_roofline": {"algorithmic_bytes": step_bytes, "hbm_frac": step_bytes / (ms_step / 1e3) / 1e9 / peak,
+                          "instruction_floor_ms": floor_ms, "floor_frac": floor_ms / ms_step},
+        "kernel_ms_per_step": {k: round(v[0] / args.steps, 3) for k, v in prof.items()},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": ms_e2e / args.steps},
         "clocks": clocks,
         "gpu_launches": launches,
         "proof_bytes": len(proof),
-        "batched": batched,
-        "served": served,
-        "commit_sweep": sweep,
-        "sumcheck": sumcheck,
-        "verify": verify,
     }
+    # compact extras last: the driver keeps the end of the line
+    if trait:
+        line["trait_route"] = trait
+    if sweep:
+        line["commit_sweep"] = {"cols": ["num_vars", "blowup", "ms", "algorithmic_gbs", "keccak_gperm_s"],
+                                "rows": [[r["num_vars"], r["blowup"], round(r["ms"], 2), round(r["algorithmic_gbs"], 1),
+                                          round(r["keccak_perms_per_s"] / 1e9, 2)] for r in sweep]}
+    if latency:
+        line["latency_by_size"] = latency
+    if sumcheck:
+        line["sumcheck"] = {"cols": ["k", "num_vars", "ms"],
+                            "rows": [[r["k"], r["num_vars"], round(r["ms"], 3)] for r in sumcheck]}
+    if verify:
+        line["verify"] = {"workload": verify["workload"], "gpu_proofs_per_s": round(verify["gpu_proofs_per_s"]),
+                          "cpu_proofs_per_s": round(verify["cpu_baseline"]["proofs_per_s"]),
+                          "cpu_cores": verify["cpu_baseline"]["cores"], "speedup": round(verify["speedup"], 1)}
+    if batched:
+        mc = batched["multi_column"]
+        line["batched"] = {"workload": batched["workload"],
+                           "plain_proofs_per_s": round(batched["plain_proofs_per_s"], 1),
+                           "batched_proofs_per_s": round(batched["batched_proofs_per_s"], 1),
+                           "speedup": round(batched["speedup"], 3), "identical": batched["proofs_identical"],
+                           "floor_s": round(batched["floor_s"], 4), "batched_s": round(batched["batched_s"], 4),
+                           "batched_over_floor": round(batched["batched_over_floor"], 3),
+                           "small_jobs_le_2^16": {k: (round(v, 4) if isinstance(v, float) else v)
+                                                  for k, v in batched["small_jobs"].items()},
+                           "multi_column_polys_per_s": round(mc["polys_per_s"], 1)}
+    if served:
+        sc = served.get("cpu_baseline") or {}
+        line["served"] = {"workload": served["workload"],
+                          "capacity_proofs_per_s": round(served["capacity_proofs_per_s"], 1),
+                          "levels": [[lv["offered_load"], round(lv["achieved_proofs_per_s"], 1), round(lv["p50_ms"], 1),
+                                      round(lv["p99_ms"], 1)] for lv in served["levels"]],
+                          "levels_cols": ["offered_load", "proofs_per_s", "p50_ms", "p99_ms"],
+                          "cpu_service_p50_ms": round(sc["service_p50_ms"], 1) if sc else None,
+                          "cpu_service_p99_ms": round(sc["service_p99_ms"], 1) if sc else None,
+                          "cpu_cores": sc.get("cores")}
     print(json.dumps(line), flush=True)
+
+
+def run_trait_route(bg, torch, pcs, dev, evals, point, reps=3):
+    """The calls a Rust PolyCommitScheme binding makes (poly-commit/src/lib.rs:
+    29-50): eval of host data that has no commitment, and open driven round
+    by round by the caller's own challenger (bf_open_start/round/challenge/
+    final/finish), beside the device-transcript open on the same commitment."""
+    comm = pcs.commit_device(dev.data_ptr(), keep=dev)
+    ch = bg.GenericChallenger.keccak256()
+    ch.observe(comm.root)
+    vals = pcs.eval(evals, point)  # host rows, copied in
+    ch.observe_ext_slice(vals)
+    pe = [bg.PolyEvals(vals, point)]
+    ref = pcs.open(comm, pe, ch.clone())
+    assert pcs.open_session(comm, pe[0]).prove(ch.clone()) == ref
+
+    def timed(f):
+        ts = []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            f()
+            torch.cuda.synchronize()
+            ts.append(1e3 * (time.perf_counter() - t))
+        return sorted(ts)[len(ts) // 2]
+
+    out = {"eval_host_data_ms": timed(lambda: pcs.eval(evals, point)),
+           "eval_commitment_ms": timed(lambda: pcs.eval(pcs.data(comm), point)),
+           "open_device_transcript_ms": timed(lambda: pcs.open(comm, pe, ch.clone())),
+           "open_session_ms": timed(lambda: pcs.open_session(comm, pe[0]).prove(ch.clone())),
+           "identical": True}
+    comm.free()
+    return {k: (round(v, 3) if isinstance(v, float) else v) for k, v in out.items()}
 
 
 if __name__ == "__main__":

@@ -115,6 +115,14 @@ int bf_commitment_data(const bf_commitment* comm, uint8_t* evals, size_t cap);
  * every column's multilinear extension at `point` (num_vars elements), on
  * the device-resident evaluations.  Writes `width` elements. */
 int bf_eval(bf_pcs* pcs, const bf_commitment* comm, const uint8_t* point, uint8_t* values);
+/* ---- PolyCommitScheme::eval(&self, data: &Data, point) (lib.rs:35;
+ * basefold.rs:126-131 over MultiPoly::evaluate, p3/src/poly/multilinear.rs:
+ * 124-141) for data that has no commitment: `evals` holds 2^num_vars rows of
+ * `width` columns, in host memory (on_device 0: copied in on the pcs's
+ * stream) or device memory (on_device 1: 16-byte aligned, not modified).
+ * The evaluation runs on the GPU; writes `width` elements to `values`. */
+int bf_eval_data(bf_pcs* pcs, const void* evals, int on_device, size_t width, const uint8_t* point,
+                 uint8_t* values);
 
 /* ---- PolyCommitScheme::open (lib.rs:37-42; basefold.rs:133-232).
  * n_evals is 0 (empty proof) or 1 (one PolyEvals: `point` of num_vars
@@ -155,19 +163,35 @@ int bf_open_finish(bf_open_session* s, const uint64_t* indices, size_t nq, uint8
 void bf_open_session_free(bf_open_session* s);
 
 /* ---- Launch-shape autotuner.  No counterpart in the reference.
- * A pcs's launch shapes are four integers: threads per NTT block (128, 256,
- * 512), butterfly layers per NTT pass (6..12, a shared-memory tile of 2^T
- * elements), the largest Merkle level run by the single-block top kernel
- * (64..4096, a power of two), and the single-block open tail (rounds whose
- * next tree has <= 2^tail_log leaves, 1..11).  They change how work is
- * launched, never the proof bytes.  bf_pcs_autotune times `reps` whole
- * proofs (commit + eval + open) on random device data per candidate, one
- * parameter at a time, keeps the fastest in the pcs, and writes a JSON
- * report (timings per candidate, ms) into `report` when given.
- * get/set: vals = {ntt_threads, ntt_max_T, top_nodes, tail_log}. */
+ * A pcs's launch shapes are six integers: threads per block of the
+ * shared-memory NTT pass (128, 256, 512), butterfly layers per NTT pass
+ * (6..12, a tile of 2^T elements: the NTT radix per pass), the largest
+ * Merkle level run by the single-block top kernel (64..4096, a power of
+ * two), the single-block open tail (rounds whose next tree has
+ * <= 2^tail_log leaves, 1..11), the Merkle levels per launch (levels of
+ * 2^10 .. 2^subtree_log nodes run as one launch, 10..20), and the NTT pass
+ * kind (0: layer by layer in shared memory; 1: tiles of 2^9..2^13 elements
+ * register-blocked; 2: as 0 with the last pass and its leaf hashing
+ * warp-specialized, butterfly warps and hashing warps on two tile buffers).
+ * They change how work is launched, never the proof bytes.  bf_pcs_autotune times `reps` whole proofs (commit + eval + open)
+ * on random device data per candidate, one parameter at a time, keeps the
+ * fastest in the pcs and in the tune cache, and writes a JSON report
+ * (timings per candidate, ms) into `report` when given.
+ * get/set: vals = {ntt_threads, ntt_max_T, top_nodes, tail_log, subtree_log,
+ * ntt_kind}; n >= 4 (set leaves the values past n unchanged). */
 int bf_pcs_autotune(bf_pcs* pcs, int reps, char* report, size_t cap);
 int bf_pcs_get_tune(const bf_pcs* pcs, int* vals, int n);
 int bf_pcs_set_tune(bf_pcs* pcs, const int* vals, int n);
+/* The tune cache: launch shapes per (device name, num_vars, log2_c), filled
+ * by bf_pcs_autotune and bf_tune_cache_load; bf_pcs_setup (and so every pcs
+ * the engine makes for a size) starts from the entry for its device and size.
+ * The file is JSON: {"version": 1, "entries": [{"device": ..., "num_vars":
+ * ..., "log2_c": ..., "tune": [six values], "ms": ...}, ...]}, one entry per
+ * line.  load merges the file's entries (returns how many) and save writes
+ * every entry. */
+int bf_tune_cache_load(const char* path);
+int bf_tune_cache_save(const char* path);
+int bf_tune_cache_clear(void);
 
 /* ---- Prover engine: many jobs of different sizes in flight at once.
  * Each job runs on one stream of a pool: at admission its commit,
@@ -180,8 +204,9 @@ int bf_pcs_set_tune(bf_pcs* pcs, const int* vals, int n);
  * time on the CPU.)
  * bf_engine_autotune: reps > 0 autotunes (bf_pcs_autotune) each size the
  *   first time a job of that size is admitted; 0 (default) keeps defaults.
- * bf_engine_set_tune: the launch shapes of bf_pcs_set_tune (4 values) for
- *   every size, current and future (an autotune, if on, still runs after).
+ * bf_engine_set_tune: the launch shapes of bf_pcs_set_tune (4 to 6 values)
+ *   for every size, current and future (an autotune, if on, still runs
+ *   after).  Without it each size starts from the tune cache's entry.
  *   Call only while no job is in flight.
  * bf_engine_graphs (default off): on, each slot keeps, per job size, fixed
  *   buffers and one captured CUDA graph of the commit, evaluation and
@@ -225,19 +250,21 @@ int bf_engine_schedule(bf_engine* e, int smallest_first, int prio_max_vars);
 int bf_engine_stats(bf_engine* e, double* out, int n);
 
 /* ---- Evaluation that allocates nothing.  No counterpart in the reference.
- * Same value as bf_eval (MultiPoly::evaluate of 2^num_vars evaluations at
- * `point`), for callers that cannot allocate device memory at this point —
- * e.g. a service whose device memory is all carved into fixed per-request
- * slots, or a latency-critical loop where cudaMalloc/cudaFree would
- * synchronise the device.  Inputs and output are the caller's: `d_evals` and
- * `d_value` (16 bytes) in device memory, `point` in host memory; the work is
- * queued on `stream` (cudaStream_t, NULL = default stream) and the call does
- * not wait for it.  Scratch is a fixed 1 MiB array in the library's device
- * image, so num_vars <= 17 (larger sizes return BF_ERR_ARG; use bf_eval).
- * Every call on a device shares that array and it keeps the last call's
- * contents: calls whose GPU work overlaps (other streams or threads) race.
- * The first call on each device looks up the array's device address; make
- * that first call before any stream capture. */
+ * The multilinear extension of the 2^num_vars evaluations at `point`, the
+ * same value bf_eval returns, for callers that cannot allocate device memory
+ * at this point — e.g. a service whose device memory is all carved into
+ * fixed per-request slots, or a latency-critical loop where
+ * cudaMalloc/cudaFree would synchronise the device.  Inputs and output are
+ * the caller's: `d_evals` and `d_value` (16 bytes) in device memory, both
+ * 16-byte aligned (otherwise BF_ERR_ARG), `point` in host memory; the work
+ * is queued on `stream` (cudaStream_t, NULL = default stream) and the call
+ * does not wait for it.  Scratch is a fixed 1 MiB array in the library's
+ * device image, so num_vars <= 17 (larger sizes return BF_ERR_ARG; use
+ * bf_eval).  Every call on a device shares that array and it keeps the last
+ * call's contents: calls whose GPU work overlaps (other streams or threads)
+ * race.  The first call on each device looks up the array's device address;
+ * make that first call before any stream capture, and do not reset the
+ * device (cudaDeviceReset) after it. */
 int bf_eval_noalloc(const void* d_evals, int num_vars, const uint8_t* point, void* d_value, void* stream);
 
 /* ---- PolyCommitScheme::verify (lib.rs:44-50; basefold.rs:234-324) on the
@@ -300,7 +327,8 @@ int bf_sumcheck_prove_device(bf_pcs* pcs, int k, int num_vars, const void* d_pol
  * returns accumulated milliseconds and launch counts per class:
  * 0 encode (NTT passes), 1 codeword leaves, 2 tree levels, 3 folded-codeword
  * leaves, 4 fold, 5 fix + sumcheck reduction, 6 eq table, 7 query gather,
- * 8 single-block last rounds of open, 9 on-device transcript steps. */
+ * 8 single-block last rounds of open, 9 on-device transcript steps, 10 the
+ * last NTT pass with the leaf hashing it carries (also inside class 0). */
 int bf_profile_enable(bf_pcs* pcs, int on);
 int bf_profile_read(bf_pcs* pcs, double* ms, uint64_t* launches, int nclasses);
 

@@ -12,6 +12,7 @@ All computation runs in libbasefold_gpu.so on the GPU; field elements are
 numpy uint8 arrays of shape (n, 16) holding Polyval's raw little-endian value.
 """
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -229,14 +230,28 @@ class Basefold:
     def data(self, comm: CommitmentData) -> _DeviceData:
         return _DeviceData(comm)
 
-    def eval(self, data, point) -> np.ndarray:
-        """eval (basefold.rs:126-131) on `data(comm)` (or the commitment itself)."""
-        comm = data.comm if isinstance(data, _DeviceData) else data
-        if not isinstance(comm, CommitmentData):
-            raise TypeError("eval takes Basefold.data(commitment)")
+    def eval(self, data, point, width: int = 1) -> np.ndarray:
+        """eval (basefold.rs:126-131) on the GPU: of `data(comm)` (or the
+        commitment itself) through its device-resident evaluations, or of
+        host evaluations that have no commitment (row-major, `width`
+        columns), which are copied in."""
         p = _elems(point, self.config.code.d) if self.config.code.d else np.zeros((1, 16), np.uint8)
-        out = np.zeros((comm.width, 16), dtype=np.uint8)
-        check(lib().bf_eval(self._h, comm._h, _p(p), _p(out)))
+        comm = data.comm if isinstance(data, _DeviceData) else data
+        if isinstance(comm, CommitmentData):
+            out = np.zeros((comm.width, 16), dtype=np.uint8)
+            check(lib().bf_eval(self._h, comm._h, _p(p), _p(out)))
+            return out
+        ev = _elems(data, width << self.config.code.d)
+        out = np.zeros((width, 16), dtype=np.uint8)
+        check(lib().bf_eval_data(self._h, _p(ev), 0, width, _p(p), _p(out)))
+        return out
+
+    def eval_device(self, dev_ptr: int, point, width: int = 1) -> np.ndarray:
+        """eval of device-resident evaluations (2^num_vars rows of `width`
+        columns at dev_ptr) that have no commitment."""
+        p = _elems(point, self.config.code.d) if self.config.code.d else np.zeros((1, 16), np.uint8)
+        out = np.zeros((width, 16), dtype=np.uint8)
+        check(lib().bf_eval_data(self._h, C.c_void_p(dev_ptr), 1, width, _p(p), _p(out)))
         return out
 
     def open(self, comm: CommitmentData, evals, challenger: GenericChallenger) -> bytes:
@@ -317,10 +332,10 @@ class Basefold:
 
     # -- timing of kernel classes -----------------------------------------------
     PROFILE_CLASSES = ["encode", "leaves", "tree", "pi_leaves", "fold", "fix", "eq", "gather", "open_tail",
-                       "transcript"]
+                       "transcript", "encode_last"]
 
     # -- launch shapes -----------------------------------------------------------
-    TUNE_KEYS = ["ntt_threads", "ntt_max_T", "top_nodes", "tail_log"]
+    TUNE_KEYS = ["ntt_threads", "ntt_max_T", "top_nodes", "tail_log", "subtree_log", "ntt_kind"]
 
     def autotune(self, reps: int = 3) -> dict:
         """Times whole proofs per candidate launch shape and keeps the fastest
@@ -332,16 +347,17 @@ class Basefold:
 
     @property
     def tune(self) -> dict:
-        v = (C.c_int * 4)()
-        check(lib().bf_pcs_get_tune(self._h, v, 4))
+        n = len(self.TUNE_KEYS)
+        v = (C.c_int * n)()
+        check(lib().bf_pcs_get_tune(self._h, v, n))
         return dict(zip(self.TUNE_KEYS, list(v)))
 
     @tune.setter
     def tune(self, t: dict) -> None:
         cur = self.tune
         cur.update(t)
-        v = (C.c_int * 4)(*[int(cur[k]) for k in self.TUNE_KEYS])
-        check(lib().bf_pcs_set_tune(self._h, v, 4))
+        v = (C.c_int * len(self.TUNE_KEYS))(*[int(cur[k]) for k in self.TUNE_KEYS])
+        check(lib().bf_pcs_set_tune(self._h, v, len(self.TUNE_KEYS)))
 
     def profile(self, on: bool = True) -> None:
         check(lib().bf_profile_enable(self._h, 1 if on else 0))
@@ -462,8 +478,11 @@ class Engine:
 
     def set_tune(self, tune: dict) -> None:
         """Launch shapes (Basefold.TUNE_KEYS) for every size (bf_engine_set_tune)."""
-        vals = (C.c_int * 4)(*[int(tune[k]) for k in Basefold.TUNE_KEYS])
-        check(lib().bf_engine_set_tune(self._h, vals, 4))
+        keys = [k for k in Basefold.TUNE_KEYS if k in tune]
+        if keys != Basefold.TUNE_KEYS[: len(keys)] or len(keys) < 4:
+            raise ValueError(f"tune needs the leading keys of {Basefold.TUNE_KEYS} (at least 4)")
+        vals = (C.c_int * len(keys))(*[int(tune[k]) for k in keys])
+        check(lib().bf_engine_set_tune(self._h, vals, len(keys)))
 
     def stats(self) -> dict:
         """Host-side accounting (bf_engine_stats)."""
@@ -565,6 +584,23 @@ def prove_sumcheck(k: int, polys, claim, challenger: GenericChallenger, device: 
     c = _elems(claim, 1)
     check(lib().bf_sumcheck_prove(device, k, n, _p(ps), _p(c), challenger._h, _p(out)))
     return _split_sumcheck(out, k, n)
+
+
+def tune_cache_load(path: str) -> int:
+    """Merges the tuned launch shapes of a JSON tune file (bf_tune_cache_load);
+    every later setup of a matching (device, num_vars, blowup) starts from them."""
+    rc = lib().bf_tune_cache_load(os.fsencode(path))
+    check(rc)
+    return rc
+
+
+def tune_cache_save(path: str) -> None:
+    """Writes every cached (device, num_vars, blowup) -> launch shapes entry."""
+    check(lib().bf_tune_cache_save(os.fsencode(path)))
+
+
+def tune_cache_clear() -> None:
+    check(lib().bf_tune_cache_clear())
 
 
 def device_info(device: int = 0):

@@ -21,6 +21,7 @@ EXPORTS = [
     "bf_engine_proof_size", "bf_engine_prove", "bf_engine_start", "bf_engine_stop", "bf_engine_submit",
     "bf_engine_poll", "bf_eval_noalloc", "bf_pcs_autotune", "bf_pcs_get_tune", "bf_pcs_set_tune",
     "bf_engine_autotune", "bf_engine_graphs", "bf_engine_stats", "bf_verify_batch", "bf_engine_set_tune", "bf_engine_cancel", "bf_engine_schedule",
+    "bf_eval_data", "bf_tune_cache_load", "bf_tune_cache_save", "bf_tune_cache_clear",
 ]
 
 BF_OK = 0
@@ -86,6 +87,10 @@ def lib():
         "bf_commitment_root": ([vp, u8p], i),
         "bf_commitment_data": ([vp, u8p, sz], i),
         "bf_eval": ([vp, vp, u8p, u8p], i),
+        "bf_eval_data": ([vp, vp, i, sz, u8p, u8p], i),
+        "bf_tune_cache_load": ([C.c_char_p], i),
+        "bf_tune_cache_save": ([C.c_char_p], i),
+        "bf_tune_cache_clear": ([], i),
         "bf_open": ([vp, vp, u8p, u8p, i, vp, u8p, sz, C.POINTER(sz)], i),
         "bf_open_start": ([vp, vp, u8p, u8p, u8p, vp, C.POINTER(vp)], i),
         "bf_open_round": ([vp, C.POINTER(i), u8p, u8p], i),

@@ -112,10 +112,12 @@ inline uint4 to_uint4(u128 v) {
 }
 
 // Kernel classes timed with CUDA events when profiling is on.
-constexpr int kProfClasses = 10;
+// P_ENCODE_LAST is the last NTT pass alone (with the leaf hashing it
+// carries); it is also inside P_ENCODE.
+constexpr int kProfClasses = 11;
 enum ProfClass {
   P_ENCODE = 0, P_LEAVES = 1, P_TREE = 2, P_PI_LEAVES = 3, P_FOLD = 4, P_FIX = 5, P_EQ = 6, P_GATHER = 7,
-  P_TAIL = 8, P_TRANSCRIPT = 9
+  P_TAIL = 8, P_TRANSCRIPT = 9, P_ENCODE_LAST = 10
 };
 
 struct Profiler {
@@ -199,6 +201,8 @@ int open_finish_complete(bf_open_session* s, uint8_t* proof, size_t cap, size_t*
 namespace bfapi {
 void pcs_acquire(bf_pcs* p);
 void pcs_release(bf_pcs* p);
+// Launch shapes from the tune cache for the pcs's device and size, if any.
+void tune_cache_apply(bf_pcs* p);
 }  // namespace bfapi
 
 struct bf_challenger {

@@ -87,7 +87,8 @@ struct bf_engine {
   int device = 0, lambda = 128, log2_c = 1, max_inflight = 8;
   int autotune_reps = 0;  // > 0: autotune each size's pcs when it is created
   bool has_tune = false;  // launch shapes set for every size (bf_engine_set_tune)
-  int tune_vals[4] = {};
+  int tune_vals[bf::kTuneVals] = {};
+  int tune_n = 4;
   bool use_graphs = false;  // replay one captured graph per (slot, size)
   std::vector<std::map<int, std::unique_ptr<Plan>>> plans;  // per slot, by size
   uint64_t admissions = 0;
@@ -146,7 +147,7 @@ int get_pcs(bf_engine* e, int n, bf_pcs** out) {
   // its own stream: a slot's stream may be in graph capture meanwhile
   TRY(bf_pcs_setup(e->device, e->lambda, e->log2_c, n, nullptr, &p));
   e->pcs_by_n[n] = p;
-  if (e->has_tune) TRY(bf_pcs_set_tune(p, e->tune_vals, 4));
+  if (e->has_tune) TRY(bf_pcs_set_tune(p, e->tune_vals, e->tune_n));
   if (e->autotune_reps > 0) TRY(bf_pcs_autotune(p, e->autotune_reps, nullptr, 0));
   *out = p;
   return BF_OK;
@@ -640,7 +641,7 @@ int bf_engine_graphs(bf_engine* e, int on) {
 }
 
 int bf_engine_set_tune(bf_engine* e, const int* vals, int n) {
-  if (!e || !vals || n < 4) return fail(BF_ERR_ARG, "need 4 values");
+  if (!e || !vals || n < 4) return fail(BF_ERR_ARG, "need at least 4 values");
   if (e->running || !e->inflight.empty()) return fail(BF_ERR_ARG, "engine busy");
   std::lock_guard<std::mutex> lk(e->pcs_mu);
   for (auto& kv : e->pcs_by_n) TRY(bf_pcs_set_tune(kv.second, vals, n));
@@ -651,7 +652,8 @@ int bf_engine_set_tune(bf_engine* e, const int* vals, int n) {
     bf_pcs_free(probe);
     TRY(rc);
   }
-  std::memcpy(e->tune_vals, vals, sizeof(e->tune_vals));
+  e->tune_n = n < bf::kTuneVals ? n : bf::kTuneVals;
+  std::memcpy(e->tune_vals, vals, sizeof(int) * (size_t)e->tune_n);
   e->has_tune = true;
   return BF_OK;
 }

@@ -37,7 +37,10 @@ uint4* g_scratch_ptr[kMaxDevices] = {nullptr};
 // Device address of the scratch array on the current device (in host code
 // the array's name is only a host-side stand-in, never a device address).
 // Looked up once per device, with that device current, by the first call
-// made on it; make that first call before any stream capture.
+// made on it; make that first call before any stream capture.  The address
+// is kept for the life of the process: resetting the device
+// (cudaDeviceReset) after the first call is not supported, since the
+// reloaded module may place the array elsewhere.
 int scratch_for_current_device(uint4** out) {
   int dev = 0;
   CU(cudaGetDevice(&dev));
@@ -74,14 +77,26 @@ extern "C" int bf_eval_noalloc(const void* d_evals, int num_vars, const uint8_t*
   uint4* scratch = nullptr;
   TRY(scratch_for_current_device(&scratch));
   // MultiPoly::evaluate (multilinear.rs:124-141): fix the top variable with
-  // the last coordinate, repeatedly.  Every level writes the entries the next
-  // one reads, so nothing in the scratch needs clearing between calls.
-  const uint4* in = reinterpret_cast<const uint4*>(d_evals);
-  for (int k = num_vars - 1; k >= 0; --k) {
+  // the last coordinate, repeatedly — the large levels one launch each, the
+  // last (at most kEvalTailMaxVars) in one block, as bf_eval does.  Every
+  // level writes the entries the next one reads, so nothing in the scratch
+  // needs clearing between calls.
+  auto coord = [&](int k) {
     uint4 r;
     std::memcpy(&r, point + 16 * k, 16);
-    CU(bf::launch_fix(in, scratch, (size_t)1 << k, r, nullptr, 0, nullptr, st));
-    in = scratch;
+    return r;
+  };
+  const int tail = num_vars - 1 < bf::kEvalTailMaxVars ? num_vars - 1 : bf::kEvalTailMaxVars;
+  CU(bf::launch_fix(reinterpret_cast<const uint4*>(d_evals), scratch, (size_t)1 << (num_vars - 1),
+                    coord(num_vars - 1), nullptr, 0, nullptr, st));
+  for (int k = num_vars - 2; k >= tail; --k)
+    CU(bf::launch_fix(scratch, scratch, (size_t)1 << k, coord(k), nullptr, 0, nullptr, st));
+  if (tail > 0) {
+    bf::EvalTail et{};
+    et.nvars = tail;
+    et.rp = nullptr;
+    for (int k = 0; k < tail; ++k) et.r[k] = coord(k);
+    CU(bf::launch_eval_tail(scratch, et, st));
   }
   CU(cudaMemcpyAsync(d_value, scratch, 16, cudaMemcpyDeviceToDevice, st));
   return BF_OK;

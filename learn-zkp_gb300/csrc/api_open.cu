@@ -312,7 +312,7 @@ int open_resident_enqueue_device(bf_open_session* s, const uint4* root_dev, cons
     {
       ProfScope ps(p->prof, st, P_TREE);
       CU(bf::launch_tree(s->pi_tree(i - 1), p->n_i(i - 1), st, reinterpret_cast<uint4*>(s->stage(i - 1)),
-                         p->tune.top_nodes));
+                         p->tune));
     }
   }
   bf::TailParams tp{};
@@ -566,7 +566,7 @@ int open_session_enqueue_start(bf_open_session* s) {
     ProfScope ps(p->prof, st, P_TREE);
     const size_t n1 = p->n_i(d - 1);
     CU(bf::launch_leaves_pair(s->w_pi_first, s->w_pi_first_tree, n1, st));
-    CU(bf::launch_tree(s->w_pi_first_tree, n1, st, reinterpret_cast<uint4*>(s->stage(d - 1)), p->tune.top_nodes));
+    CU(bf::launch_tree(s->w_pi_first_tree, n1, st, reinterpret_cast<uint4*>(s->stage(d - 1)), p->tune));
   }
   CU(cudaMemcpyAsync(s->w_point, pin + 64 + 16 * w, 16 * (size_t)d, cudaMemcpyHostToDevice, st));
   CU(cudaMemsetAsync(s->stage(d - 1) + 32, 0, 16, st));
@@ -685,7 +685,7 @@ int bf_open_challenge(bf_open_session* s, const uint8_t r_i[16]) {
     {
       ProfScope ps(p->prof, st, P_TREE);
       CU(bf::launch_tree(s->pi_tree(i - 1), p->n_i(i - 1), st, reinterpret_cast<uint4*>(s->stage(i - 1)),
-                         p->tune.top_nodes));
+                         p->tune));
     }
     CU(cudaMemcpyAsync(pin, s->stage(i - 1), 48, cudaMemcpyDeviceToHost, st));
   } else {

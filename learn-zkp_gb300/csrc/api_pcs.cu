@@ -84,8 +84,8 @@ void Profiler::drain() {
 
 // NVTX range names of the kernel classes (in P_* order); the ranges cost
 // nothing unless a profiler is attached.
-static const char* const kProfNames[kProfClasses] = {"encode", "leaves", "tree", "pi_leaves", "fold",
-                                                     "fix", "eq", "gather", "open_tail", "transcript"};
+static const char* const kProfNames[kProfClasses] = {"encode", "leaves", "tree", "pi_leaves", "fold",   "fix",
+                                                     "eq",     "gather", "open_tail", "transcript", "encode_last"};
 
 ProfScope::ProfScope(Profiler& p, cudaStream_t s, int c) : pr(p), st(s), cls(c) {
   nvtxRangePushA(kProfNames[cls]);
@@ -303,9 +303,16 @@ int commit_enqueue(bf_pcs* p, bf_commitment* cm, const uint4* data, cudaStream_t
   {
     // encode; for width 1 and d >= 1 the last NTT pass also hashes the leaves
     ProfScope ps(p->prof, st, P_ENCODE);
-    CU(bf::launch_encode(data, cw, p->d, p->log2_c, w, p->tw_view.as<bf::TwiddleView>(), st,
-                         pairs ? tree : nullptr, pairs ? pit : nullptr, p->tune, slice_ready, slices,
-                         slices > 0 ? p->aux2 : nullptr, p->ev_fork, p->ev_join));
+    cudaEvent_t la = nullptr, lb = nullptr;
+    if (p->prof.on) {
+      la = p->prof.get();
+      lb = p->prof.get();
+    }
+    const cudaError_t e = bf::launch_encode(data, cw, p->d, p->log2_c, w, p->tw_view.as<bf::TwiddleView>(), st,
+                                            pairs ? tree : nullptr, pairs ? pit : nullptr, p->tune, slice_ready,
+                                            slices, slices > 0 ? p->aux2 : nullptr, p->ev_fork, p->ev_join, la, lb);
+    if (p->prof.on) p->prof.pending.push_back({P_ENCODE_LAST, la, lb});
+    CU(e);
   }
   if (!pairs) {
     ProfScope ps(p->prof, st, P_LEAVES);
@@ -317,14 +324,14 @@ int commit_enqueue(bf_pcs* p, bf_commitment* cm, const uint4* data, cudaStream_t
     ProfScope ps(p->prof, st, P_TREE);  // one scope from the fork to the join
     CU(cudaEventRecord(p->ev_fork, st));
     CU(cudaStreamWaitEvent(p->aux, p->ev_fork, 0));
-    CU(bf::launch_tree(pit, nd / 2, p->aux, nullptr, p->tune.top_nodes));
-    CU(bf::launch_tree(tree, nd, st, nullptr, p->tune.top_nodes));
+    CU(bf::launch_tree(pit, nd / 2, p->aux, nullptr, p->tune));
+    CU(bf::launch_tree(tree, nd, st, nullptr, p->tune));
     CU(cudaEventRecord(p->ev_join, p->aux));
     CU(cudaStreamWaitEvent(st, p->ev_join, 0));
   } else {
     ProfScope ps(p->prof, st, P_TREE);
-    CU(bf::launch_tree(tree, nd, st, nullptr, p->tune.top_nodes));
-    if (pairs) CU(bf::launch_tree(pit, nd / 2, st, nullptr, p->tune.top_nodes));
+    CU(bf::launch_tree(tree, nd, st, nullptr, p->tune));
+    if (pairs) CU(bf::launch_tree(pit, nd / 2, st, nullptr, p->tune));
   }
   CU(cudaMemcpyAsync(roots_pin, tree + 2 * (2 * nd - 2), 32, cudaMemcpyDeviceToHost, st));
   if (pairs) CU(cudaMemcpyAsync(roots_pin + 32, pit + 2 * (nd - 2), 32, cudaMemcpyDeviceToHost, st));
@@ -464,6 +471,7 @@ int bf_pcs_setup(int device, int lambda, int log2_c, int num_vars, void* stream,
     uint64_t keep = ~(uint64_t)0;
     CU(cudaMemPoolSetAttribute(p->pool, cudaMemPoolAttrReleaseThreshold, &keep));
   }
+  tune_cache_apply(p.get());  // shapes tuned earlier for this device and size, if any
   *out = p.release();
   return BF_OK;
 }
@@ -569,6 +577,36 @@ int bf_eval(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, uint8_t* v
   CU(cudaStreamSynchronize(p->stream));
   p->prof.drain();
   std::memcpy(values, p->pinned.b(), 16 * cm->width);
+  return BF_OK;
+}
+
+int bf_eval_data(bf_pcs* p, const void* evals, int on_device, size_t width, const uint8_t* point, uint8_t* values) {
+  if (!p || !evals || !values || (p->d > 0 && !point)) return fail(BF_ERR_ARG, "null argument");
+  if (p->device < 0) return fail(BF_ERR_ARG, "verifier-only pcs (device < 0)");
+  if (width == 0 || width > 4096) return fail(BF_ERR_ARG, "width %zu out of range (1..4096)", width);
+  if (on_device && (reinterpret_cast<uintptr_t>(evals) & 15))
+    return fail(BF_ERR_ARG, "device evaluations must be 16-byte aligned");
+  DeviceGuard g(p->device);
+  // the data of a commitment that is never made: the caller's device buffer,
+  // or a pool copy of the host rows (released in stream order)
+  bf_commitment cm;
+  cm.pcs = p;
+  cm.width = width;
+  const size_t bytes = 16 * width * ((size_t)1 << p->d);
+  if (on_device) {
+    cm.data.p = const_cast<void*>(evals);
+    cm.data.owned = false;
+  } else {
+    CU(cm.data.alloc_async(bytes, p->pool, p->stream));
+    CU(cudaMemcpyAsync(cm.data.p, evals, bytes, cudaMemcpyHostToDevice, p->stream));
+  }
+  const size_t half = p->d > 0 ? ((size_t)1 << (p->d - 1)) : 1;
+  if (p->eval_ws.bytes < 16 * half) CU(p->eval_ws.alloc(16 * half));
+  CU(p->pinned.ensure(16 * width + 64));
+  TRY(eval_enqueue(p, &cm, point, p->eval_ws.as<uint4>(), p->stream, p->pinned.b()));
+  CU(cudaStreamSynchronize(p->stream));
+  p->prof.drain();
+  std::memcpy(values, p->pinned.b(), 16 * width);
   return BF_OK;
 }
 

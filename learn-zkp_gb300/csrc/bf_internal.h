@@ -24,11 +24,17 @@ struct TwiddleView {
 // autotuner (bf_pcs_autotune) or left at these defaults.
 constexpr int kNttMaxT = 12;  // largest shared-memory tile of an NTT pass: 2^12 elements
 struct Tune {
-  int ntt_threads = 256;  // threads per NTT pass block: 128, 256 or 512
+  int ntt_threads = 256;  // threads per block of the shared-memory NTT pass: 128, 256 or 512
   int ntt_max_T = 12;     // butterfly layers per NTT pass (tile 2^T), 6 .. kNttMaxT
   int top_nodes = 512;    // Merkle levels at or below this many nodes run in one block (64 .. 4096)
   int tail_log = 8;       // open rounds whose next tree has <= 2^tail_log leaves run in one block (1 .. 11)
+  int subtree_log = 16;   // Merkle levels of 2^10 .. 2^subtree_log nodes run as one launch (10 .. 20)
+  // NTT pass kind: 0 every pass layer by layer in shared memory; 1 tiles of
+  // 2^9 .. 2^13 register-blocked; 2 as 0, with the last pass (and its leaf
+  // hashing) warp-specialized
+  int ntt_kind = 2;
 };
+constexpr int kTuneVals = 6;  // the Tune fields above, in order, as the C ABI's value vector
 bool tune_valid(const Tune& t);
 
 // Launchers (all asynchronous on `st`).
@@ -39,19 +45,20 @@ bool tune_valid(const Tune& t);
 // is ready once slice_ready[k] has completed: the first pass waits for each
 // slice before the blocks that read it, its launches alternating between st
 // and st2 (joined back to st through the events ev_a, ev_b) when those are
-// given.
+// given.  last_a / last_b (when given) are recorded on st around the last
+// pass (the kernel-class timing of the last pass with its leaf hashing).
 cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t width, const TwiddleView* tw,
                           cudaStream_t st, uint4* leaves = nullptr, uint4* pair_leaves = nullptr,
                           const Tune& tune = Tune(), const cudaEvent_t* slice_ready = nullptr,
                           int slices = 0, cudaStream_t st2 = nullptr, cudaEvent_t ev_a = nullptr,
-                          cudaEvent_t ev_b = nullptr);
+                          cudaEvent_t ev_b = nullptr, cudaEvent_t last_a = nullptr, cudaEvent_t last_b = nullptr);
 cudaError_t launch_leaves_elem(const uint4* cw, uint4* leaves, size_t n, size_t width, cudaStream_t st);
 cudaError_t launch_leaves_pair(const uint4* pi, uint4* leaves, size_t n, cudaStream_t st);
 // Build every level above `leaves` (n leaves, power of two); levels are stored
 // one after another right after the leaves.  Root = last digest, also copied
 // to `root_out` (32 bytes) when it is not null.
 cudaError_t launch_tree(uint4* leaves, size_t n, cudaStream_t st, uint4* root_out = nullptr,
-                        size_t top_nodes = 512);
+                        const Tune& tune = Tune());
 // SplitMix64 words as field elements (autotuner inputs).
 cudaError_t launch_fill_random(uint4* out, size_t n, uint64_t seed, cudaStream_t st);
 
@@ -85,7 +92,7 @@ struct FoldFixParams {
   size_t next_half;
   uint32_t* acc;
   const uint4* xp;
-  unsigned fold_blocks;  // set by the launcher
+  unsigned fold_blocks, fix_blocks, fix_stride;  // set by the launcher
 };
 cudaError_t launch_fold_fix(const FoldFixParams& p, uint4 r, cudaStream_t st);
 cudaError_t launch_combine_rows(const uint4* rows, size_t nrows, size_t width, const uint4* scalars, uint4* out,

@@ -106,6 +106,8 @@ struct PassParams {
   // keep both pipes busy.
   uint4* leaves;
   uint4* pair_leaves;
+  int log2_c;      // cosets: the persistent last pass walks c 2^(n-T) tiles
+  int ntt_warps;   // warp-specialized last pass: warps on butterflies (the rest hash)
 };
 
 template <bool HASH>
@@ -177,6 +179,236 @@ __global__ void __launch_bounds__(512) ntt_pass_kernel(const uint4* __restrict__
   }
 }
 
+// ---------------------------------------------------------------------------
+// Register-blocked NTT pass for tiles of 2^9 .. 2^13 elements.  The tile's T
+// layers run in phases of (up to) four: in a phase with base bit b, thread t
+// holds the 16 elements a(t, e) = tpart(t, b) | (e << b), e < 16, whose tile
+// indices differ only in bits [b, b+4), so the phase's layers are butterflies
+// between registers with no exchange.  Between phases the tile goes once
+// through shared memory (a transpose); a 2^12 tile takes three phases and two
+// transposes instead of twelve shared-memory layers with a barrier each.
+// Within a layer the 8 butterflies of a thread share at most 8 twiddles, and
+// by GF(2)-linearity twiddle(K | v) = twiddle(K) + lo[v] for the v < 8 low
+// bits that vary between them: one table pair lookup and block-uniform lo[v]
+// loads per layer instead of a lookup per butterfly.
+// ---------------------------------------------------------------------------
+constexpr int kNttRegMinT = 9;   // smallest tile of the register-blocked pass (32 threads)
+constexpr int kNttRegMaxT = 13;  // largest (512 threads)
+
+// Shared-memory slot of tile index a: the low three bits are XORed with bits
+// 4..6, so every phase's reads and writes (16-byte elements, 8 lanes per
+// shared-memory wavefront) fall in 8 distinct bank groups.
+__device__ __forceinline__ uint32_t ntt_slot(uint32_t a) { return a ^ ((a >> 4) & 7u); }
+
+// Tile index held by thread t as element e in the phase with base bit b.
+__device__ __forceinline__ uint32_t ntt_elem(uint32_t t, uint32_t e, int b) {
+  return (t & ((1u << b) - 1u)) | (e << b) | ((t >> b) << (b + 4));
+}
+
+// Layers b+ll_hi .. b of one phase on the thread's 16 registers.  A is the
+// thread's tile index with bits [b, b+4) clear, extended by the tile's index
+// within its coset above bit T (so that A >> (l+1) is the twiddle index's
+// position part at layer l); the stage-s twiddle index of the butterfly at
+// element e0 is K = (j << (n-1-s)) | (A >> (l+1)) | (e0 >> (ll+1)).
+__device__ __forceinline__ void ntt_phase(uint4 (&x)[16], int b, int ll_hi, uint32_t A, uint32_t j, int n, int s_lo,
+                                          const TwiddleView* __restrict__ tw) {
+#pragma unroll
+  for (int ll = 3; ll >= 0; --ll) {
+    if (ll > ll_hi) continue;
+    const int l = b + ll, s = s_lo + l;
+    const uint4* __restrict__ lo_tab = tw->lo[s];
+    const uint4* __restrict__ hi_tab = tw->hi[s];
+    const uint32_t Kb = (j << (n - 1 - s)) | (A >> (l + 1));
+    const uint4 tb = gf_add(lo_tab[Kb & 4095u], hi_tab[Kb >> 12]);
+#pragma unroll
+    for (int v = 0; v < (8 >> ll); ++v) {
+      const uint4 tv = v ? gf_add(tb, lo_tab[v]) : tb;
+      // twiddle index 0 (the top layer of coset 0, half the next, ...) has
+      // twiddle 0: the product is skipped
+      const bool mul = (Kb | (uint32_t)v) != 0u;
+#pragma unroll
+      for (int w = 0; w < (1 << ll); ++w) {
+        const int e0 = (v << (ll + 1)) | w, e1 = e0 | (1 << ll);
+        if (mul) x[e0] = gf_add(x[e0], gf_mul(x[e1], tv));  // lo += hi * t
+        x[e1] = gf_add(x[e1], x[e0]);                        // hi += lo
+      }
+    }
+  }
+}
+
+template <bool HASH>
+__global__ void __launch_bounds__(512) ntt_reg_kernel(const uint4* __restrict__ m, uint4* __restrict__ cw, PassParams p,
+                                                     const TwiddleView* __restrict__ tw) {
+  extern __shared__ uint4 sm[];
+  const int n = p.n, T = p.T, s_lo = p.s_lo;
+  const uint32_t nthr = 1u << (T - 4), t = threadIdx.x;
+  uint32_t j, rem;
+  if (p.first) {
+    const int shift = n - T - p.piece_log;
+    j = blockIdx.x >> shift;
+    rem = ((blockIdx.x & ((1u << shift) - 1u)) << p.piece_log) | brev_bits((uint32_t)p.piece, p.piece_log);
+  } else {
+    j = blockIdx.x >> (n - T);
+    rem = blockIdx.x & ((1u << (n - T)) - 1u);
+  }
+  const uint32_t u = rem & ((1u << s_lo) - 1u);
+  const uint32_t hi = rem >> s_lo;
+  const size_t coset_base = (size_t)j << n;
+  const size_t w = (size_t)p.width, col = blockIdx.y;
+  const bool last = s_lo == 0;
+  uint4 x[16];
+
+  int b = T - 4;
+  if (p.first) {
+    // coalesced rows of m, bit-reversed into the tile through shared memory
+    const size_t base = (size_t)brev_bits(u, s_lo) << T;
+#pragma unroll
+    for (int e = 0; e < 16; ++e) x[e] = m[(base + t + nthr * e) * w + col];
+#pragma unroll
+    for (int e = 0; e < 16; ++e) sm[ntt_slot(brev_bits(t + nthr * e, T))] = x[e];
+    __syncthreads();
+#pragma unroll
+    for (int e = 0; e < 16; ++e) x[e] = sm[ntt_slot(ntt_elem(t, e, b))];
+  } else {
+#pragma unroll
+    for (int e = 0; e < 16; ++e) {
+      const size_t xx = ((size_t)hi << (s_lo + T)) | ((size_t)ntt_elem(t, e, b) << s_lo) | u;
+      x[e] = cw[(coset_base + xx) * w + col];
+    }
+  }
+  int top = T - 1;
+  while (true) {
+    const uint32_t A = (hi << T) | ntt_elem(t, 0, b);
+    ntt_phase(x, b, top - b, A, j, n, s_lo, tw);
+    top = b - 1;
+    if (top < 0) break;
+    const int nb = top > 3 ? top - 3 : 0;
+    __syncthreads();  // every thread has read the previous arrangement
+#pragma unroll
+    for (int e = 0; e < 16; ++e) sm[ntt_slot(ntt_elem(t, e, b))] = x[e];
+    __syncthreads();
+#pragma unroll
+    for (int e = 0; e < 16; ++e) x[e] = sm[ntt_slot(ntt_elem(t, e, nb))];
+    b = nb;
+  }
+  if (!last) {
+#pragma unroll
+    for (int e = 0; e < 16; ++e) {
+      const size_t xx = ((size_t)hi << (s_lo + T)) | ((size_t)ntt_elem(t, e, 0) << s_lo) | u;
+      cw[(coset_base + xx) * w + col] = x[e];
+    }
+    return;
+  }
+  // last pass: the tile is the contiguous run [coset_base + hi 2^T, +2^T);
+  // stored and hashed from shared memory in coalesced order
+  __syncthreads();
+#pragma unroll
+  for (int e = 0; e < 16; ++e) sm[ntt_slot(ntt_elem(t, e, 0))] = x[e];
+  __syncthreads();
+  const size_t q0 = coset_base + ((size_t)hi << T);
+#pragma unroll 4
+  for (int e = 0; e < 16; ++e) {
+    const uint32_t i = t + nthr * e;
+    cw[(q0 + i) * w + col] = sm[ntt_slot(i)];
+  }
+  if (HASH) {
+    for (uint32_t k = t; k < (8u * nthr); k += nthr) {
+      const uint4 e0 = sm[ntt_slot(2 * k)], e1 = sm[ntt_slot(2 * k + 1)];
+      const size_t q = q0 + 2 * k;
+      store_digest(p.leaves, q, hash_elem(e0));
+      store_digest(p.leaves, q + 1, hash_elem(e1));
+      store_digest(p.pair_leaves, q >> 1, hash_pair(e0, e1));
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Warp-specialized last NTT pass with the leaf hashing.  Its butterflies are
+// multiplier work (IMAD.WIDE on the FMA pipe) and its leaf hashes ALU work;
+// in a block whose warps all run one phase and then the other, one pipe idles
+// while the other works.  Here the first ntt_warps warps of a 16-warp block
+// run the butterflies of tile k into one of two shared-memory buffers while
+// the other warps hash tile k-1 out of the other buffer, so both pipes stay
+// busy through the whole pass.  The block is persistent (tiles b, b + grid,
+// ...).  Named barriers: 1 between the butterfly warps' layers, 2 + buffer
+// "tile ready" (butterfly warps arrive, hashing warps wait), 4 + buffer
+// "buffer free" (the reverse).
+// ---------------------------------------------------------------------------
+constexpr int kNttWsThreads = 512;
+constexpr int kNttWsMaxT = 12;  // two 2^12-element buffers: 128 KB of shared memory
+
+__device__ __forceinline__ void named_sync(int id, int count) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+__device__ __forceinline__ void named_arrive(int id, int count) {
+  asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+
+__global__ void __launch_bounds__(kNttWsThreads, 1) ntt_last_ws_kernel(const uint4* __restrict__ m,
+                                                                      uint4* __restrict__ cw, PassParams p,
+                                                                      const TwiddleView* __restrict__ tw) {
+  extern __shared__ uint4 sm[];
+  const int n = p.n, T = p.T;
+  const uint32_t tsize = 1u << T;
+  const uint32_t tiles_per_coset = 1u << (n - T);
+  const uint32_t tiles = tiles_per_coset << p.log2_c;
+  const uint32_t nthr = 32u * (uint32_t)p.ntt_warps;
+  const uint32_t K = blockIdx.x < tiles ? (tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;  // this block's tiles
+  if (threadIdx.x < nthr) {
+    // butterfly warps
+    const uint32_t t = threadIdx.x;
+    for (uint32_t k = 0; k < K; ++k) {
+      const uint32_t tile = blockIdx.x + k * gridDim.x;
+      const uint32_t j = tile >> (n - T), hi = tile & (tiles_per_coset - 1);
+      const size_t q0 = ((size_t)j << n) + ((size_t)hi << T);
+      uint4* buf = sm + ((k & 1u) << T);
+      if (k >= 2) named_sync(4 + (int)(k & 1u), kNttWsThreads);  // the hashing warps are done with it
+      if (p.first) {  // a single pass (T = n): m bit-reversed into the tile
+        for (uint32_t i = t; i < tsize; i += nthr) buf[brev_bits(i, T)] = m[i];
+      } else {
+        for (uint32_t i = t; i < tsize; i += nthr) buf[i] = cw[q0 + i];
+      }
+      named_sync(1, (int)nthr);
+      for (int l = T - 1; l >= 0; --l) {
+        const uint4* __restrict__ lo_tab = tw->lo[l];
+        const uint4* __restrict__ hi_tab = tw->hi[l];
+        const uint32_t kbase = (j << (n - 1 - l)) | (hi << (T - 1 - l));
+        const uint32_t lmask = (1u << l) - 1u;
+        for (uint32_t bi = t; bi < (tsize >> 1); bi += nthr) {
+          const uint32_t a = ((bi >> l) << (l + 1)) | (bi & lmask);
+          const uint32_t Kt = kbase | (bi >> l);
+          uint4 x0 = buf[a], x1 = buf[a + (1u << l)];
+          if (Kt != 0) x0 = gf_add(x0, gf_mul(x1, gf_add(lo_tab[Kt & 4095u], hi_tab[Kt >> 12])));
+          x1 = gf_add(x1, x0);
+          buf[a] = x0;
+          buf[a + (1u << l)] = x1;
+        }
+        named_sync(1, (int)nthr);
+      }
+      for (uint32_t i = t; i < tsize; i += nthr) cw[q0 + i] = buf[i];
+      named_arrive(2 + (int)(k & 1u), kNttWsThreads);  // tile k is ready to hash
+    }
+  } else {
+    // hashing warps
+    const uint32_t t = threadIdx.x - nthr, hthr = blockDim.x - nthr;
+    for (uint32_t k = 0; k < K; ++k) {
+      const uint32_t tile = blockIdx.x + k * gridDim.x;
+      const uint32_t j = tile >> (n - T), hi = tile & (tiles_per_coset - 1);
+      const size_t q0 = ((size_t)j << n) + ((size_t)hi << T);
+      const uint4* buf = sm + ((k & 1u) << T);
+      named_sync(2 + (int)(k & 1u), kNttWsThreads);
+      for (uint32_t kk = t; kk < (tsize >> 1); kk += hthr) {
+        const uint4 e0 = buf[2 * kk], e1 = buf[2 * kk + 1];
+        const size_t q = q0 + 2 * kk;
+        store_digest(p.leaves, q, hash_elem(e0));
+        store_digest(p.leaves, q + 1, hash_elem(e1));
+        store_digest(p.pair_leaves, q >> 1, hash_pair(e0, e1));
+      }
+      if (k + 2 < K) named_arrive(4 + (int)(k & 1u), kNttWsThreads);  // the butterfly warps may refill it
+    }
+  }
+}
+
 // n = 0: every coset is the single row of m.
 __global__ void replicate_kernel(const uint4* __restrict__ m, uint4* __restrict__ cw, size_t c, size_t w) {
   for (size_t i = threadIdx.x; i < c * w; i += blockDim.x) cw[i] = m[i % w];
@@ -192,6 +424,12 @@ void init_kernel_attributes() {
                        (int)(sizeof(uint4) << kNttMaxT));
   cudaFuncSetAttribute(ntt_pass_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)(sizeof(uint4) << kNttMaxT));
+  cudaFuncSetAttribute(ntt_reg_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)(sizeof(uint4) << kNttRegMaxT));
+  cudaFuncSetAttribute(ntt_reg_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)(sizeof(uint4) << kNttRegMaxT));
+  cudaFuncSetAttribute(ntt_last_ws_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)(2 * sizeof(uint4) << kNttWsMaxT));
   done.fetch_or(bit);
 }
 
@@ -199,19 +437,22 @@ bool tune_valid(const Tune& t) {
   const bool threads_ok = t.ntt_threads == 128 || t.ntt_threads == 256 || t.ntt_threads == 512;
   const bool top_ok = t.top_nodes >= 64 && t.top_nodes <= 4096 && (t.top_nodes & (t.top_nodes - 1)) == 0;
   return threads_ok && t.ntt_max_T >= 6 && t.ntt_max_T <= kNttMaxT && top_ok && t.tail_log >= 1 &&
-         t.tail_log <= kTailMaxLeavesLog;
+         t.tail_log <= kTailMaxLeavesLog && t.subtree_log >= 10 && t.subtree_log <= 20 && t.ntt_kind >= 0 &&
+         t.ntt_kind <= 2;
 }
 
 cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t width, const TwiddleView* tw,
                           cudaStream_t st, uint4* leaves, uint4* pair_leaves, const Tune& tune,
                           const cudaEvent_t* slice_ready, int slices, cudaStream_t st2, cudaEvent_t ev_a,
-                          cudaEvent_t ev_b) {
+                          cudaEvent_t ev_b, cudaEvent_t last_a, cudaEvent_t last_b) {
   if (width == 0 || width > 65535 || (width != 1 && (leaves || pair_leaves))) return cudaErrorInvalidValue;
   if (!tune_valid(tune)) return cudaErrorInvalidValue;
   const size_t c = (size_t)1 << log2_c;
   if (n == 0) {
+    if (last_a) cudaEventRecord(last_a, st);
     replicate_kernel<<<1, 128, 0, st>>>(m, cw, c, width);
     COUNT_LAUNCH();
+    if (last_b) cudaEventRecord(last_b, st);
     return cudaGetLastError();
   }
   init_kernel_attributes();
@@ -237,6 +478,8 @@ cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t w
     const bool last = (pidx == passes - 1);
     p.leaves = last ? leaves : nullptr;
     p.pair_leaves = last ? pair_leaves : nullptr;
+    p.log2_c = log2_c;
+    p.ntt_warps = 8;
     // one butterfly per thread and layer at most: 2^(T-1) threads, >= one warp
     const int threads = std::max(32, std::min(tune.ntt_threads, 1 << (T - 1)));
     const uint32_t tiles = 1u << (n - T);
@@ -254,6 +497,10 @@ cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t w
     // stream run one after another, and a piece of a few hundred blocks ends
     // in a mostly idle wave; on two streams the next piece fills it.
     const bool two = pieces > 1 && st2 && ev_a && ev_b;
+    if (last && last_a) {  // the last pass is one launch on st (it never takes slices)
+      cudaError_t e = cudaEventRecord(last_a, st);
+      if (e != cudaSuccess) return e;
+    }
     if (two) {
       cudaError_t e = cudaEventRecord(ev_a, st);  // st2 after everything before the pass on st
       if (e == cudaSuccess) e = cudaStreamWaitEvent(st2, ev_a, 0);
@@ -268,7 +515,16 @@ cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t w
       p.piece_log = piece_log;
       p.piece = piece;
       const dim3 grid((unsigned)(c * (tiles >> piece_log)), (unsigned)width);
-      if (p.leaves)
+      const bool reg = tune.ntt_kind == 1 && T >= kNttRegMinT && T <= kNttRegMaxT;
+      const bool ws = tune.ntt_kind == 2 && p.leaves && pieces == 1 && T <= kNttWsMaxT && T >= 6;
+      if (ws)
+        ntt_last_ws_kernel<<<(unsigned)std::min<size_t>(c * tiles, (size_t)num_sms()), kNttWsThreads,
+                             2 * sizeof(uint4) << T, sp>>>(m, cw, p, tw);
+      else if (reg && p.leaves)
+        ntt_reg_kernel<true><<<grid, 1 << (T - 4), sizeof(uint4) << T, sp>>>(m, cw, p, tw);
+      else if (reg)
+        ntt_reg_kernel<false><<<grid, 1 << (T - 4), sizeof(uint4) << T, sp>>>(m, cw, p, tw);
+      else if (p.leaves)
         ntt_pass_kernel<true><<<grid, threads, sizeof(uint4) << T, sp>>>(m, cw, p, tw);
       else
         ntt_pass_kernel<false><<<grid, threads, sizeof(uint4) << T, sp>>>(m, cw, p, tw);
@@ -279,6 +535,10 @@ cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t w
     if (two) {  // the rest of the encode waits for the pieces on st2
       cudaError_t e = cudaEventRecord(ev_b, st2);
       if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev_b, 0);
+      if (e != cudaSuccess) return e;
+    }
+    if (last && last_b) {
+      cudaError_t e = cudaEventRecord(last_b, st);
       if (e != cudaSuccess) return e;
     }
     top -= T;
@@ -380,7 +640,6 @@ cudaError_t launch_leaves_pair(const uint4* pi, uint4* leaves, size_t n, cudaStr
 // i + (its level's size) below, so a block only reads what it wrote and
 // __syncthreads separates the levels.  Level 1 has one node per thread.
 constexpr int kSubtreeThreads = 256;
-constexpr size_t kSubtreeMaxNodes = (size_t)1 << 16;  // larger levels: one launch each
 __global__ void __launch_bounds__(kSubtreeThreads) subtree_kernel(uint4* level, size_t n, int k) {
   const size_t nk = n >> k;
   const int log_m = 9 - k;  // M = 2^log_m top nodes per block
@@ -401,10 +660,12 @@ __global__ void __launch_bounds__(kSubtreeThreads) subtree_kernel(uint4* level, 
   }
 }
 
-cudaError_t launch_tree(uint4* leaves, size_t n, cudaStream_t st, uint4* root_out, size_t top_nodes) {
+cudaError_t launch_tree(uint4* leaves, size_t n, cudaStream_t st, uint4* root_out, const Tune& tune) {
   uint4* cur = leaves;
+  const size_t top_nodes = (size_t)tune.top_nodes;
+  const size_t subtree_max = (size_t)1 << tune.subtree_log;  // larger levels: one launch each
   while (n > top_nodes) {
-    if (n <= kSubtreeMaxNodes && n >= 1024) {  // the latency-bound middle levels in one launch
+    if (n <= subtree_max && n >= 1024) {  // the latency-bound middle levels in one launch
       int k = 0;
       size_t m = n;
       while (m > top_nodes && k < 9) {
@@ -600,16 +861,22 @@ __global__ void __launch_bounds__(256, 3) fix_kernel(const uint4* in, uint4* out
   }
 }
 
-// One round of open in one launch: blocks [0, fold_blocks) fold the
-// codeword and hash the next round's leaves (as fold_leaves_kernel), the
-// other blocks fix the sumcheck polynomial and reduce for the next round (as
-// fix_kernel).  Both read the round's challenge.
+// One round of open in one launch: fold_blocks blocks fold the codeword and
+// hash the next round's leaves (as fold_leaves_kernel), fix_blocks blocks fix
+// the sumcheck polynomial and reduce for the next round (as fix_kernel).
+// Both read the round's challenge.  The fix blocks are spread through the
+// grid (block S q + S - 1 is fix block q, S = grid / fix_blocks), so their
+// multiplier-bound work runs beside the ALU-bound fold blocks instead of
+// alone at the end of the launch.
 __global__ void __launch_bounds__(128) fold_fix_kernel(FoldFixParams p, uint4 r) {
   __shared__ uint4 scratch[32];
   if (p.xp) r = *p.xp;
-  if (blockIdx.x < p.fold_blocks) {
+  const unsigned S = p.fix_stride, q = blockIdx.x / S;
+  const bool fix = blockIdx.x % S == S - 1 && q < p.fix_blocks;
+  if (!fix) {
+    const unsigned fb = blockIdx.x - (q < p.fix_blocks ? q : p.fix_blocks);  // fix blocks before this one
     const size_t stride = (size_t)p.fold_blocks * blockDim.x;
-    for (size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x; s < p.n_leaves; s += stride) {
+    for (size_t s = (size_t)fb * blockDim.x + threadIdx.x; s < p.n_leaves; s += stride) {
       uint4 f[2];
 #pragma unroll
       for (int k = 0; k < 2; ++k) {
@@ -625,8 +892,8 @@ __global__ void __launch_bounds__(128) fold_fix_kernel(FoldFixParams p, uint4 r)
     }
     return;
   }
-  const size_t b0 = (size_t)(blockIdx.x - p.fold_blocks) * blockDim.x + threadIdx.x;
-  const size_t stride = (size_t)(gridDim.x - p.fold_blocks) * blockDim.x;
+  const size_t b0 = (size_t)q * blockDim.x + threadIdx.x;
+  const size_t stride = (size_t)p.fix_blocks * blockDim.x;
   uint4 acc = make_uint4(0, 0, 0, 0);
   for (size_t b = b0; b < p.half; b += stride) {
     const uint4 lo = p.poly_in[b], hi = p.poly_in[b + p.half];
@@ -641,8 +908,9 @@ __global__ void __launch_bounds__(128) fold_fix_kernel(FoldFixParams p, uint4 r)
 cudaError_t launch_fold_fix(const FoldFixParams& p0, uint4 r, cudaStream_t st) {
   FoldFixParams p = p0;
   p.fold_blocks = grid_short(p.n_leaves, 128);
-  const unsigned fix_blocks = grid_for(p.half, 128, 8);  // few blocks: each ends in one atomic
-  fold_fix_kernel<<<p.fold_blocks + fix_blocks, 128, 0, st>>>(p, r);
+  p.fix_blocks = grid_for(p.half, 128, 8);  // few blocks: each ends in one atomic
+  p.fix_stride = (p.fold_blocks + p.fix_blocks) / p.fix_blocks;  // >= 2 while fold_blocks >= fix_blocks
+  fold_fix_kernel<<<p.fold_blocks + p.fix_blocks, 128, 0, st>>>(p, r);
   COUNT_LAUNCH();
   return cudaGetLastError();
 }

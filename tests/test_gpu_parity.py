@@ -404,3 +404,23 @@ def test_random_configurations_match_oracle(bg):
         root_o, values_o, blob = O.harness_prepare(n, log2_c, evals, point, width)
         assert comm.root == root_o and np.array_equal(values, values_o), (k, n, log2_c, width)
         assert proof == O.open_proof(n, log2_c, evals, point, values_o, blob, width), (k, n, log2_c, width)
+
+
+@pytest.mark.parametrize("width", list(range(1, 10)))
+def test_eval_of_uncommitted_data_matches_oracle(bg, width):
+    """PolyCommitScheme::eval(&Data, point) for data with no commitment
+    (bf_eval_data): host rows and device rows give the oracle's
+    MultiPoly::evaluate of every column, at widths 1..9 and sizes that take
+    the single-block tail only (n = 0, 5) and the per-level launches (n = 15)."""
+    torch = pytest.importorskip("torch")
+    for n in (0, 5, 15):
+        data = rand.random_elems((width << n) + n, 900 + 10 * width + n)
+        evals, point = data[: width << n], data[width << n:]
+        pcs = setup_pcs(bg, n, 1)
+        want = O.eval_poly(n, evals, point, width)
+        assert np.array_equal(pcs.eval(evals, point, width=width), want), (n, width)
+        dev = torch.from_numpy(evals).cuda()
+        assert np.array_equal(pcs.eval_device(dev.data_ptr(), point, width=width), want), (n, width)
+        if width == 1:  # the same value through a commitment
+            comm = pcs.commit(evals)
+            assert np.array_equal(pcs.eval(pcs.data(comm), point), want)

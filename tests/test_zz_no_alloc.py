@@ -21,15 +21,24 @@ def test_eval_noalloc_matches_eval_on_consecutive_calls(built_lib):
 
     L = _native.lib()
     out = torch.zeros(16, dtype=torch.uint8, device="cuda:0")
-    for call, (n, seed) in enumerate([(14, 31), (9, 32), (17, 33), (14, 34)]):
+    side = torch.cuda.Stream()
+    # consecutive calls of different sizes share the scratch: n = 0 (a copy),
+    # 1 (one fix), the single-block tail (9, 13) and the per-level launches
+    # (14, 17); the last runs on a caller-created stream
+    cases = [(14, 31), (9, 32), (0, 35), (17, 33), (1, 36), (13, 37), (14, 34)]
+    for call, (n, seed) in enumerate(cases):
         data = rand.random_elems((1 << n) + n, seed)
         evals, point = data[: 1 << n], data[1 << n:]
         pcs = bg.Basefold.setup(bg.BasefoldConfig(bg.BinaryReedSolomonCode(128, 1, n)), device=0)
         want = pcs.eval(pcs.data(pcs.commit(evals)), point)
         dev = torch.from_numpy(evals).cuda()
-        pt = np.ascontiguousarray(point)
+        pt = np.ascontiguousarray(point) if n else np.zeros((1, 16), np.uint8)
+        on_side = call == len(cases) - 1
+        if on_side:
+            side.wait_stream(torch.cuda.current_stream())
+        st = C.c_void_p(side.cuda_stream) if on_side else None
         _native.check(L.bf_eval_noalloc(C.c_void_p(dev.data_ptr()), n, C.c_void_p(pt.ctypes.data),
-                                        C.c_void_p(out.data_ptr()), None))
+                                        C.c_void_p(out.data_ptr()), st))
         torch.cuda.synchronize()
         got = out.cpu().numpy().reshape(1, 16)
         assert np.array_equal(got, want), (call, n)
