@@ -379,6 +379,47 @@ def run_latency(bg, torch, device, log2_c, sizes=(10, 12, 14, 16, 18, 20, 22), r
     return {"cols": ["num_vars", "plain_ms", "engine_ms", "engine_graph_ms"], "rows": rows}
 
 
+def run_autotune(bg, torch, device, log2_c, sizes=(20, 22, 24), reps=2):
+    """The launch-shape autotuner per size: whole-step time with the default
+    shapes and with the shapes bf_pcs_autotune picks (its own report), and
+    the proof unchanged."""
+    rows = []
+    for n in sizes:
+        data = bg.rand.random_elems((1 << n) + n, 8000 + n)
+        ev, pt = data[: 1 << n], data[1 << n:]
+        dev = torch.from_numpy(ev).to(f"cuda:{device}")
+        pcs = bg.Basefold.setup(bg.BasefoldConfig(bg.BinaryReedSolomonCode(128, log2_c, n)), device=device)
+
+        def step():
+            comm = pcs.commit_device(dev.data_ptr(), keep=dev)
+            ch = bg.GenericChallenger.keccak256()
+            ch.observe(comm.root)
+            vals = pcs.eval(pcs.data(comm), pt)
+            ch.observe_ext_slice(vals)
+            proof = pcs.open(comm, [bg.PolyEvals(vals, pt)], ch)
+            comm.free()
+            return proof
+
+        def timed():
+            step()
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            for _ in range(5):
+                step()
+            torch.cuda.synchronize()
+            return 1e3 * (time.perf_counter() - t) / 5
+
+        before = step()
+        default_ms = timed()
+        rep = pcs.autotune(reps)
+        tuned_ms = timed()
+        assert step() == before, "tuned shapes changed the proof"
+        rows.append([n, round(default_ms, 3), round(tuned_ms, 3), [rep["tune"][k] for k in bg.Basefold.TUNE_KEYS]])
+        del pcs, dev
+    bg.tune_cache_clear()
+    return {"cols": ["num_vars", "default_ms", "tuned_ms", "tune"], "tune_keys": bg.Basefold.TUNE_KEYS, "rows": rows}
+
+
 def run_served(bg, device, log2_c, lo=12, hi=24, per_size=10, loads=(0.25, 0.5, 0.9), seed=5):
     """Config 5: open-loop Poisson arrivals, sizes log-uniform 2^lo..2^hi, host
     inputs (H2D inside), at fractions of the measured capacity.  Each load
@@ -728,9 +769,10 @@ def main():
     peaks, peak_kind = load_peaks()
     peak = float(peaks.get("hbm_gbs", 6800.0))
     num_sms = bg.device_info(local)["num_sms"]
-    batched = served = sweep = sumcheck = verify = latency = None
+    batched = served = sweep = sumcheck = verify = latency = tuned = None
     if ws == 1 and not args.no_extras:
         latency = run_latency(bg, torch, local, log2_c)
+        tuned = run_autotune(bg, torch, local, log2_c)
         batched = run_batched(bg, torch, local, log2_c)
         served = run_served(bg, local, log2_c)
         sweep = run_commit_sweep(bg, torch, local)
@@ -810,6 +852,8 @@ def main():
                                           round(r["keccak_perms_per_s"] / 1e9, 2)] for r in sweep]}
     if latency:
         line["latency_by_size"] = latency
+    if tuned:
+        line["autotune"] = tuned
     if sumcheck:
         line["sumcheck"] = {"cols": ["k", "num_vars", "ms"],
                             "rows": [[r["k"], r["num_vars"], round(r["ms"], 3)] for r in sumcheck]}

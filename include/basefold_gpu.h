@@ -172,7 +172,9 @@ void bf_open_session_free(bf_open_session* s);
  * 2^10 .. 2^subtree_log nodes run as one launch, 10..20), and the NTT pass
  * kind (0: layer by layer in shared memory; 1: tiles of 2^9..2^13 elements
  * register-blocked; 2: as 0 with the last pass and its leaf hashing
- * warp-specialized, butterfly warps and hashing warps on two tile buffers).
+ * warp-specialized, butterfly warps and hashing warps on two tile buffers;
+ * 3: as 0 with the cosets of a two-pass encode pipelined, the next cosets'
+ * first pass on a high-priority stream beside a coset's last pass).
  * They change how work is launched, never the proof bytes.  bf_pcs_autotune times `reps` whole proofs (commit + eval + open)
  * on random device data per candidate, one parameter at a time, keeps the
  * fastest in the pcs and in the tune cache, and writes a JSON report

@@ -335,7 +335,8 @@ class Basefold:
                        "transcript", "encode_last"]
 
     # -- launch shapes -----------------------------------------------------------
-    TUNE_KEYS = ["ntt_threads", "ntt_max_T", "top_nodes", "tail_log", "subtree_log", "ntt_kind"]
+    TUNE_KEYS = ["ntt_threads", "ntt_max_T", "top_nodes", "tail_log", "subtree_log", "ntt_kind", "gf_mix",
+                 "ntt_ws_warps"]
 
     def autotune(self, reps: int = 3) -> dict:
         """Times whole proofs per candidate launch shape and keeps the fastest

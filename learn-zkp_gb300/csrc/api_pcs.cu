@@ -308,9 +308,13 @@ int commit_enqueue(bf_pcs* p, bf_commitment* cm, const uint4* data, cudaStream_t
       la = p->prof.get();
       lb = p->prof.get();
     }
+    // the pcs's second streams and events only serve work on its own stream
+    // (engine jobs of one size share the pcs on streams of their own)
+    const bool own = st == p->stream;
     const cudaError_t e = bf::launch_encode(data, cw, p->d, p->log2_c, w, p->tw_view.as<bf::TwiddleView>(), st,
                                             pairs ? tree : nullptr, pairs ? pit : nullptr, p->tune, slice_ready,
-                                            slices, slices > 0 ? p->aux2 : nullptr, p->ev_fork, p->ev_join, la, lb);
+                                            slices, own ? p->aux2 : nullptr, own ? p->ev_fork : nullptr,
+                                            own ? p->ev_join : nullptr, la, lb);
     if (p->prof.on) p->prof.pending.push_back({P_ENCODE_LAST, la, lb});
     CU(e);
   }
@@ -454,7 +458,13 @@ int bf_pcs_setup(int device, int lambda, int log2_c, int num_vars, void* stream,
     p->own_stream = true;
   }
   CU(cudaStreamCreateWithFlags(&p->aux, cudaStreamNonBlocking));
-  CU(cudaStreamCreateWithFlags(&p->aux2, cudaStreamNonBlocking));
+  {
+    // aux2 runs work that should be dispatched ahead of the main stream's
+    // waiting blocks (the next cosets' first NTT pass beside a last pass)
+    int lo_prio = 0, hi_prio = 0;
+    CU(cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio));
+    CU(cudaStreamCreateWithPriority(&p->aux2, cudaStreamNonBlocking, hi_prio));
+  }
   CU(cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming));
   CU(cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming));
   for (cudaEvent_t& e : p->slice_ev) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));

@@ -41,6 +41,8 @@ void to_vals(const bf::Tune& t, int* v) {
   v[3] = t.tail_log;
   v[4] = t.subtree_log;
   v[5] = t.ntt_kind;
+  v[6] = t.gf_mix;
+  v[7] = t.ntt_ws_warps;
 }
 
 // The first n (>= 4) values over `base`: callers of the four-value form keep
@@ -53,6 +55,8 @@ bf::Tune from_vals(const int* v, int n, const bf::Tune& base) {
   t.tail_log = v[3];
   if (n > 4) t.subtree_log = v[4];
   if (n > 5) t.ntt_kind = v[5];
+  if (n > 6) t.gf_mix = v[6];
+  if (n > 7) t.ntt_ws_warps = v[7];
   return t;
 }
 
@@ -138,8 +142,10 @@ int bf_pcs_set_tune(bf_pcs* p, const int* vals, int n) {
   const bf::Tune t = from_vals(vals, n, p->tune);
   if (!bf::tune_valid(t))
     return fail(BF_ERR_ARG,
-                "bad tune (ntt_threads %d, ntt_max_T %d, top_nodes %d, tail_log %d, subtree_log %d, ntt_kind %d)",
-                t.ntt_threads, t.ntt_max_T, t.top_nodes, t.tail_log, t.subtree_log, t.ntt_kind);
+                "bad tune (ntt_threads %d, ntt_max_T %d, top_nodes %d, tail_log %d, subtree_log %d, ntt_kind %d, "
+                "gf_mix %d, ntt_ws_warps %d)",
+                t.ntt_threads, t.ntt_max_T, t.top_nodes, t.tail_log, t.subtree_log, t.ntt_kind, t.gf_mix,
+                t.ntt_ws_warps);
   p->tune = t;
   return BF_OK;
 }
@@ -194,10 +200,10 @@ int bf_tune_cache_save(const char* path) {
       to_vals(kv.second.tune, v);
       char buf[384];
       std::snprintf(buf, sizeof(buf),
-                    " {\"device\": \"%s\", \"num_vars\": %d, \"log2_c\": %d, \"tune\": [%d, %d, %d, %d, %d, %d], "
-                    "\"ms\": %.4f}%s\n",
+                    " {\"device\": \"%s\", \"num_vars\": %d, \"log2_c\": %d, \"tune\": [%d, %d, %d, %d, %d, %d, %d, "
+                    "%d], \"ms\": %.4f}%s\n",
                     std::get<0>(kv.first).c_str(), std::get<1>(kv.first), std::get<2>(kv.first), v[0], v[1], v[2], v[3],
-                    v[4], v[5], kv.second.ms, ++i < g_cache.size() ? "," : "");
+                    v[4], v[5], v[6], v[7], kv.second.ms, ++i < g_cache.size() ? "," : "");
       o << buf;
     }
   }
@@ -257,12 +263,14 @@ int bf_pcs_autotune(bf_pcs* p, int reps, char* report, size_t cap) {
   std::vector<int> tails;
   for (int t = 3; t <= bf::kTailMaxLeavesLog; ++t) tails.push_back(t);
   const std::vector<Axis> axes = {
-      {"ntt_kind", 5, {2, 0, 1}},
+      {"ntt_kind", 5, {2, 0, 1, 3}},
       {"ntt_max_T", 1, {10, 11, 12}},
       {"ntt_threads", 0, {128, 256, 512}},
       {"top_nodes", 2, {128, 256, 512, 1024, 2048}},
       {"subtree_log", 4, {12, 14, 16, 18}},
       {"tail_log", 3, tails},
+      {"gf_mix", 6, {0, 2, 3, 4}},
+      {"ntt_ws_warps", 7, {8, 4, 6, 10}},
   };
   bf::Tune best = start;
   double best_ms = 0;
@@ -307,8 +315,8 @@ int bf_pcs_autotune(bf_pcs* p, int reps, char* report, size_t cap) {
   char tail[256];
   std::snprintf(tail, sizeof(tail),
                 "}, \"best_ms\": %.4f, \"tune\": {\"ntt_threads\": %d, \"ntt_max_T\": %d, \"top_nodes\": %d, "
-                "\"tail_log\": %d, \"subtree_log\": %d, \"ntt_kind\": %d}}",
-                best_ms, vals[0], vals[1], vals[2], vals[3], vals[4], vals[5]);
+                "\"tail_log\": %d, \"subtree_log\": %d, \"ntt_kind\": %d, \"gf_mix\": %d, \"ntt_ws_warps\": %d}}",
+                best_ms, vals[0], vals[1], vals[2], vals[3], vals[4], vals[5], vals[6], vals[7]);
   rep += tail;
   if (report && cap) {
     std::strncpy(report, rep.c_str(), cap - 1);

@@ -31,10 +31,13 @@ struct Tune {
   int subtree_log = 16;   // Merkle levels of 2^10 .. 2^subtree_log nodes run as one launch (10 .. 20)
   // NTT pass kind: 0 every pass layer by layer in shared memory; 1 tiles of
   // 2^9 .. 2^13 register-blocked; 2 as 0, with the last pass (and its leaf
-  // hashing) warp-specialized
+  // hashing) warp-specialized; 3 as 0, two-pass encodes with the cosets
+  // pipelined (the next cosets' first pass beside a coset's last pass)
   int ntt_kind = 2;
+  int gf_mix = 0;        // NTT passes without hashing: 32 x 32 products per field product from 16-bit pieces (0 .. 4)
+  int ntt_ws_warps = 8;  // warp-specialized last pass: butterfly warps of its 16 (2 .. 14; the rest hash)
 };
-constexpr int kTuneVals = 6;  // the Tune fields above, in order, as the C ABI's value vector
+constexpr int kTuneVals = 8;  // the Tune fields above, in order, as the C ABI's value vector
 bool tune_valid(const Tune& t);
 
 // Launchers (all asynchronous on `st`).

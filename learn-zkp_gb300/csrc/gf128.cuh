@@ -49,6 +49,51 @@ __device__ __forceinline__ uint64_t clmul32(uint32_t a, uint32_t b) {
          (z3 & 0x8888888888888888ull);
 }
 
+// The same 32 x 32 product with its work moved from the wide multiplies to
+// the ALU: one Karatsuba level over 16-bit halves, each 16 x 16 product
+// from nine 32-bit integer multiplies (IMAD, whose throughput is about 2.5
+// times IMAD.WIDE's) of operands whose bits are three apart.  A product of
+// two such operands has at most 6 terms at any position (a residue class of
+// 16 bits has 5 or 6 of them), a count that fits the three bits up to the
+// next position of its class, so masking keeps the XOR of the terms; the
+// results fit 32 bits.  The ALU carries more (operand splits and masks, Karatsuba
+// sums), so kernels bound by the multiplier take a few of these per field
+// product and the rest from clmul32.
+__device__ __forceinline__ uint32_t clmul16(uint32_t a, uint32_t b) {
+  const uint32_t a0 = a & 0x9249u, a1 = a & 0x2492u, a2 = a & 0x4924u;
+  const uint32_t b0 = b & 0x9249u, b1 = b & 0x2492u, b2 = b & 0x4924u;
+  const uint32_t z0 = (a0 * b0) ^ (a1 * b2) ^ (a2 * b1);
+  const uint32_t z1 = (a0 * b1) ^ (a1 * b0) ^ (a2 * b2);
+  const uint32_t z2 = (a0 * b2) ^ (a2 * b0) ^ (a1 * b1);
+  return (z0 & 0x49249249u) | (z1 & 0x92492492u) | (z2 & 0x24924924u);
+}
+
+__device__ __forceinline__ uint64_t clmul32_h3(uint32_t a, uint32_t b) {
+  const uint32_t al = a & 0xffffu, ah = a >> 16, bl = b & 0xffffu, bh = b >> 16;
+  const uint32_t l = clmul16(al, bl), h = clmul16(ah, bh);
+  const uint32_t m = clmul16(al ^ ah, bl ^ bh) ^ l ^ h;
+  return ((uint64_t)h << 32) ^ ((uint64_t)m << 16) ^ (uint64_t)l;
+}
+
+// Product number j of a field product: the first H of the nine from
+// clmul32_h3, the rest from clmul32.
+template <int H>
+__device__ __forceinline__ uint64_t clmul32_sel(uint32_t a, uint32_t b, int j) {
+  return j < H ? clmul32_h3(a, b) : clmul32(a, b);
+}
+
+// Carry-less 64 x 64 -> 128 by one Karatsuba level (products j0 .. j0+2).
+template <int H>
+__device__ __forceinline__ void clmul64_mix(uint64_t a, uint64_t b, uint64_t& lo, uint64_t& hi, int j0) {
+  const uint32_t a0 = (uint32_t)a, a1 = (uint32_t)(a >> 32);
+  const uint32_t b0 = (uint32_t)b, b1 = (uint32_t)(b >> 32);
+  const uint64_t p0 = clmul32_sel<H>(a0, b0, j0);
+  const uint64_t p2 = clmul32_sel<H>(a1, b1, j0 + 1);
+  const uint64_t p1 = clmul32_sel<H>(a0 ^ a1, b0 ^ b1, j0 + 2) ^ p0 ^ p2;
+  lo = p0 ^ (p1 << 32);
+  hi = p2 ^ (p1 >> 32);
+}
+
 // Carry-less 64 x 64 -> 128 by one Karatsuba level.
 __device__ __forceinline__ void clmul64(uint64_t a, uint64_t b, uint64_t& lo, uint64_t& hi) {
   const uint32_t a0 = (uint32_t)a, a1 = (uint32_t)(a >> 32);
@@ -87,6 +132,19 @@ __device__ __forceinline__ uint4 gf_mul(uint4 a, uint4 b) {
   clmul64(a0, b0, l0, l1);
   clmul64(a1, b1, h0, h1);
   clmul64(a0 ^ a1, b0 ^ b1, m0, m1);
+  return gf_karatsuba_reduce(l0, l1, h0, h1, m0, m1);
+}
+
+// gf_mul with H (0..9) of its nine 32 x 32 products from clmul32_h3: the
+// same value, with part of the multiplier work moved to the ALU pipe.
+template <int H>
+__device__ __forceinline__ uint4 gf_mul_mix(uint4 a, uint4 b) {
+  const uint64_t a0 = ((uint64_t)a.y << 32) | a.x, a1 = ((uint64_t)a.w << 32) | a.z;
+  const uint64_t b0 = ((uint64_t)b.y << 32) | b.x, b1 = ((uint64_t)b.w << 32) | b.z;
+  uint64_t l0, l1, h0, h1, m0, m1;
+  clmul64_mix<H>(a0, b0, l0, l1, 0);
+  clmul64_mix<H>(a1, b1, h0, h1, 3);
+  clmul64_mix<H>(a0 ^ a1, b0 ^ b1, m0, m1, 6);
   return gf_karatsuba_reduce(l0, l1, h0, h1, m0, m1);
 }
 

@@ -108,9 +108,13 @@ struct PassParams {
   uint4* pair_leaves;
   int log2_c;      // cosets: the persistent last pass walks c 2^(n-T) tiles
   int ntt_warps;   // warp-specialized last pass: warps on butterflies (the rest hash)
+  int coset0;      // the launch covers cosets coset0, coset0 + 1, ... (grid / tiles per coset of them)
 };
 
-template <bool HASH>
+// H: field products take H of their nine 32 x 32 products from the 16-bit
+// form (gf_mul_mix), moving multiplier work of the passes without hashing,
+// which are bound by the wide multiplies, onto the ALU pipe.
+template <bool HASH, int H = 0>
 __global__ void __launch_bounds__(512) ntt_pass_kernel(const uint4* __restrict__ m, uint4* __restrict__ cw,
                                                       PassParams p, const TwiddleView* __restrict__ tw) {
   extern __shared__ uint4 sm[];
@@ -125,6 +129,7 @@ __global__ void __launch_bounds__(512) ntt_pass_kernel(const uint4* __restrict__
     j = blockIdx.x >> (n - T);
     rem = blockIdx.x & (tiles_per_coset - 1);
   }
+  j += (uint32_t)p.coset0;
   const uint32_t u = rem & ((1u << s_lo) - 1u);
   const uint32_t hi = rem >> s_lo;
   const uint32_t tsize = 1u << T;
@@ -154,7 +159,7 @@ __global__ void __launch_bounds__(512) ntt_pass_kernel(const uint4* __restrict__
       uint4 x0 = sm[a], x1 = sm[a + (1u << l)];
       // twiddle K is the XOR of independent stage bases over K's bits: zero
       // only for K = 0 (the whole top layer of coset 0, half the next, ...)
-      if (K != 0) x0 = gf_add(x0, gf_mul(x1, gf_add(lo_tab[K & 4095u], hi_tab[K >> 12])));  // lo += hi * t
+      if (K != 0) x0 = gf_add(x0, gf_mul_mix<H>(x1, gf_add(lo_tab[K & 4095u], hi_tab[K >> 12])));  // lo += hi * t
       x1 = gf_add(x1, x0);  // hi += lo
       sm[a] = x0;
       sm[a + (1u << l)] = x1;
@@ -251,6 +256,7 @@ __global__ void __launch_bounds__(512) ntt_reg_kernel(const uint4* __restrict__ 
     j = blockIdx.x >> (n - T);
     rem = blockIdx.x & ((1u << (n - T)) - 1u);
   }
+  j += (uint32_t)p.coset0;
   const uint32_t u = rem & ((1u << s_lo) - 1u);
   const uint32_t hi = rem >> s_lo;
   const size_t coset_base = (size_t)j << n;
@@ -420,7 +426,15 @@ void init_kernel_attributes() {
   cudaGetDevice(&dev);
   const uint64_t bit = 1ull << (dev & 63);
   if (done.load() & bit) return;
-  cudaFuncSetAttribute(ntt_pass_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(ntt_pass_kernel<false, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)(sizeof(uint4) << kNttMaxT));
+  cudaFuncSetAttribute(ntt_pass_kernel<false, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)(sizeof(uint4) << kNttMaxT));
+  cudaFuncSetAttribute(ntt_pass_kernel<false, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)(sizeof(uint4) << kNttMaxT));
+  cudaFuncSetAttribute(ntt_pass_kernel<false, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)(sizeof(uint4) << kNttMaxT));
+  cudaFuncSetAttribute(ntt_pass_kernel<false, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)(sizeof(uint4) << kNttMaxT));
   cudaFuncSetAttribute(ntt_pass_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)(sizeof(uint4) << kNttMaxT));
@@ -438,7 +452,67 @@ bool tune_valid(const Tune& t) {
   const bool top_ok = t.top_nodes >= 64 && t.top_nodes <= 4096 && (t.top_nodes & (t.top_nodes - 1)) == 0;
   return threads_ok && t.ntt_max_T >= 6 && t.ntt_max_T <= kNttMaxT && top_ok && t.tail_log >= 1 &&
          t.tail_log <= kTailMaxLeavesLog && t.subtree_log >= 10 && t.subtree_log <= 20 && t.ntt_kind >= 0 &&
-         t.ntt_kind <= 2;
+         t.ntt_kind <= 3 && t.gf_mix >= 0 && t.gf_mix <= 4 && t.ntt_ws_warps >= 2 && t.ntt_ws_warps <= 14;
+}
+
+static void launch_ntt_nohash(dim3 grid, int threads, size_t smem, cudaStream_t s, const uint4* m, uint4* cw,
+                              const PassParams& p, const TwiddleView* tw, int gf_mix) {
+  switch (gf_mix) {
+    case 1: ntt_pass_kernel<false, 1><<<grid, threads, smem, s>>>(m, cw, p, tw); break;
+    case 2: ntt_pass_kernel<false, 2><<<grid, threads, smem, s>>>(m, cw, p, tw); break;
+    case 3: ntt_pass_kernel<false, 3><<<grid, threads, smem, s>>>(m, cw, p, tw); break;
+    case 4: ntt_pass_kernel<false, 4><<<grid, threads, smem, s>>>(m, cw, p, tw); break;
+    default: ntt_pass_kernel<false, 0><<<grid, threads, smem, s>>>(m, cw, p, tw); break;
+  }
+}
+
+// Two-pass encode with the cosets pipelined (NTT kind 3): the first pass of
+// coset 0 on st; then the first passes of the other cosets on st2 (a
+// high-priority stream, so their blocks are dispatched as the running blocks
+// retire) while the last pass of coset 0 — its leaf hashing ALU-bound where
+// the first pass is multiplier-bound — runs on st; then the last passes of
+// the other cosets.  Co-resident blocks of the two passes keep both pipes of
+// an SM busy.
+static cudaError_t encode_pipelined(const uint4* m, uint4* cw, int n, int log2_c, const TwiddleView* tw,
+                                    cudaStream_t st, cudaStream_t st2, cudaEvent_t ev_a, cudaEvent_t ev_b,
+                                    uint4* leaves, uint4* pair_leaves, const Tune& tune, int T0,
+                                    cudaEvent_t last_a, cudaEvent_t last_b) {
+  const size_t c = (size_t)1 << log2_c;
+  const int T1 = n - T0;
+  auto params = [&](int first, int T, int coset0) {
+    PassParams p{};
+    p.n = n;
+    p.T = T;
+    p.s_lo = first ? n - T : 0;
+    p.first = first;
+    p.width = 1;
+    p.leaves = first ? nullptr : leaves;
+    p.pair_leaves = first ? nullptr : pair_leaves;
+    p.log2_c = log2_c;
+    p.coset0 = coset0;
+    return p;
+  };
+  auto launch = [&](const PassParams& p, unsigned blocks, cudaStream_t s) {
+    const int threads = std::max(32, std::min(tune.ntt_threads, 1 << (p.T - 1)));
+    if (p.leaves)
+      ntt_pass_kernel<true><<<blocks, threads, sizeof(uint4) << p.T, s>>>(m, cw, p, tw);
+    else
+      launch_ntt_nohash(dim3(blocks), threads, sizeof(uint4) << p.T, s, m, cw, p, tw, tune.gf_mix);
+    COUNT_LAUNCH();
+    return cudaGetLastError();
+  };
+  const unsigned tiles0 = 1u << (n - T0), tiles1 = 1u << (n - T1);
+  cudaError_t e = launch(params(1, T0, 0), tiles0, st);
+  if (e == cudaSuccess) e = cudaEventRecord(ev_a, st);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(st2, ev_a, 0);
+  if (e == cudaSuccess && c > 1) e = launch(params(1, T0, 1), (unsigned)((c - 1) * tiles0), st2);
+  if (e == cudaSuccess) e = cudaEventRecord(ev_b, st2);
+  if (e == cudaSuccess && last_a) e = cudaEventRecord(last_a, st);
+  if (e == cudaSuccess) e = launch(params(0, T1, 0), tiles1, st);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev_b, 0);
+  if (e == cudaSuccess && c > 1) e = launch(params(0, T1, 1), (unsigned)((c - 1) * tiles1), st);
+  if (e == cudaSuccess && last_b) e = cudaEventRecord(last_b, st);
+  return e;
 }
 
 cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t width, const TwiddleView* tw,
@@ -465,6 +539,9 @@ cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t w
     if ((c << (n - T)) >= (size_t)num_sms() || T_next < 5) break;
     ++passes;
   }
+  if (tune.ntt_kind == 3 && passes == 2 && leaves && pair_leaves && slices == 0 && st2 && ev_a && ev_b)
+    return encode_pipelined(m, cw, n, log2_c, tw, st, st2, ev_a, ev_b, leaves, pair_leaves, tune, (n + 1) / 2,
+                            last_a, last_b);
   int top = n;
   for (int pidx = 0; pidx < passes; ++pidx) {
     const int remaining = passes - pidx;
@@ -479,7 +556,8 @@ cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t w
     p.leaves = last ? leaves : nullptr;
     p.pair_leaves = last ? pair_leaves : nullptr;
     p.log2_c = log2_c;
-    p.ntt_warps = 8;
+    p.ntt_warps = tune.ntt_ws_warps;
+    p.coset0 = 0;
     // one butterfly per thread and layer at most: 2^(T-1) threads, >= one warp
     const int threads = std::max(32, std::min(tune.ntt_threads, 1 << (T - 1)));
     const uint32_t tiles = 1u << (n - T);
@@ -527,7 +605,7 @@ cudaError_t launch_encode(const uint4* m, uint4* cw, int n, int log2_c, size_t w
       else if (p.leaves)
         ntt_pass_kernel<true><<<grid, threads, sizeof(uint4) << T, sp>>>(m, cw, p, tw);
       else
-        ntt_pass_kernel<false><<<grid, threads, sizeof(uint4) << T, sp>>>(m, cw, p, tw);
+        launch_ntt_nohash(grid, threads, sizeof(uint4) << T, sp, m, cw, p, tw, tune.gf_mix);
       COUNT_LAUNCH();
       cudaError_t e = cudaGetLastError();
       if (e != cudaSuccess) return e;

@@ -126,13 +126,15 @@ def test_launch_shape_validation(built_lib):
     needs a device."""
     bg = built_lib
     pcs = _setup_verifier(bg, 4, 1)
-    default = dict(ntt_threads=256, ntt_max_T=12, top_nodes=512, tail_log=8, subtree_log=16, ntt_kind=2)
+    default = dict(ntt_threads=256, ntt_max_T=12, top_nodes=512, tail_log=8, subtree_log=16, ntt_kind=2, gf_mix=0,
+                   ntt_ws_warps=8)
     assert pcs.tune == default
     pcs.tune = dict(ntt_threads=512, tail_log=3, subtree_log=12, ntt_kind=0)
     assert pcs.tune == dict(default, ntt_threads=512, tail_log=3, subtree_log=12, ntt_kind=0)
     for bad in (dict(ntt_threads=96), dict(ntt_max_T=13), dict(ntt_max_T=5), dict(top_nodes=100),
                 dict(top_nodes=8192), dict(tail_log=0), dict(tail_log=12), dict(subtree_log=9),
-                dict(subtree_log=21), dict(ntt_kind=3), dict(ntt_kind=-1)):
+                dict(subtree_log=21), dict(ntt_kind=4), dict(ntt_kind=-1), dict(gf_mix=5),
+                dict(ntt_ws_warps=1), dict(ntt_ws_warps=15)):
         try:
             pcs.tune = bad
             raise AssertionError(f"accepted {bad}")
@@ -163,7 +165,7 @@ def test_tune_cache_file_round_trip(built_lib, tmp_path):
     bg.tune_cache_clear()
     f = tmp_path / "tune.json"
     f.write_text('{"version": 1, "entries": [\n'
-                 ' {"device": "NVIDIA GB300", "num_vars": 20, "log2_c": 1, "tune": [256, 10, 1024, 9, 14, 2], '
+                 ' {"device": "NVIDIA GB300", "num_vars": 20, "log2_c": 1, "tune": [256, 10, 1024, 9, 14, 2, 3, 6], '
                  '"ms": 4.25},\n'
                  ' {"device": "NVIDIA GB300", "num_vars": 22, "log2_c": 2, "tune": [128, 11, 512, 8], "ms": 12.5}\n'
                  ']}\n')
@@ -171,8 +173,8 @@ def test_tune_cache_file_round_trip(built_lib, tmp_path):
     out = tmp_path / "out.json"
     bg.tune_cache_save(str(out))
     text = out.read_text()
-    assert '"num_vars": 20, "log2_c": 1, "tune": [256, 10, 1024, 9, 14, 2]' in text
-    assert '"num_vars": 22, "log2_c": 2, "tune": [128, 11, 512, 8, 16, 2]' in text  # defaults fill the rest
+    assert '"num_vars": 20, "log2_c": 1, "tune": [256, 10, 1024, 9, 14, 2, 3, 6]' in text
+    assert '"num_vars": 22, "log2_c": 2, "tune": [128, 11, 512, 8, 16, 2, 0, 8]' in text  # defaults fill the rest
     bg.tune_cache_clear()
     assert bg.tune_cache_load(str(out)) == 2
     assert _setup_verifier(bg, 20, 1).tune["ntt_max_T"] == 12  # no device: nothing applied

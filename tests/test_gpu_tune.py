@@ -19,6 +19,19 @@ SHAPES = [
     dict(ntt_threads=128, ntt_max_T=10, top_nodes=2048, tail_log=6, subtree_log=14, ntt_kind=2),
     dict(ntt_threads=256, ntt_max_T=9, top_nodes=512, tail_log=8, subtree_log=16, ntt_kind=1),
     dict(ntt_threads=256, ntt_max_T=6, top_nodes=256, tail_log=5, subtree_log=18, ntt_kind=2),
+    dict(ntt_threads=256, ntt_max_T=12, top_nodes=512, tail_log=8, subtree_log=16, ntt_kind=3),
+    dict(ntt_threads=128, ntt_max_T=8, top_nodes=1024, tail_log=4, subtree_log=16, ntt_kind=3),
+    # the field products of the passes without hashing with 1..4 of their nine
+    # 32 x 32 products from 16-bit pieces, and other splits of the
+    # warp-specialized pass
+    dict(ntt_threads=256, ntt_max_T=7, top_nodes=512, tail_log=8, subtree_log=16, ntt_kind=2, gf_mix=1,
+         ntt_ws_warps=4),
+    dict(ntt_threads=256, ntt_max_T=8, top_nodes=512, tail_log=8, subtree_log=16, ntt_kind=0, gf_mix=2,
+         ntt_ws_warps=12),
+    dict(ntt_threads=512, ntt_max_T=9, top_nodes=512, tail_log=8, subtree_log=16, ntt_kind=2, gf_mix=3,
+         ntt_ws_warps=2),
+    dict(ntt_threads=128, ntt_max_T=6, top_nodes=512, tail_log=8, subtree_log=16, ntt_kind=3, gf_mix=4,
+         ntt_ws_warps=14),
 ]
 
 
@@ -41,7 +54,7 @@ def test_every_shape_gives_the_oracle_proof(built_lib, n, log2_c):
     pcs = bg.Basefold.setup(bg.BasefoldConfig(bg.BinaryReedSolomonCode(128, log2_c, n)))
     for shape in SHAPES:
         pcs.tune = shape
-        assert pcs.tune == shape
+        assert {k: pcs.tune[k] for k in shape} == shape
         root, values, proof = prove(bg, pcs, evals, point)
         assert root == root_o and np.array_equal(values, values_o), shape
         assert proof == want, shape
@@ -56,7 +69,8 @@ def test_autotune_keeps_the_proof(built_lib):
     before = prove(bg, pcs, evals, point)
     rep = pcs.autotune(1)
     assert rep["tune"] == pcs.tune
-    assert set(rep["axes"]) == {"ntt_kind", "ntt_max_T", "ntt_threads", "top_nodes", "subtree_log", "tail_log"}
+    assert set(rep["axes"]) == {"ntt_kind", "ntt_max_T", "ntt_threads", "top_nodes", "subtree_log", "tail_log", "gf_mix",
+                                "ntt_ws_warps"}
     assert rep["best_ms"] <= rep["start_ms"]
     after = prove(bg, pcs, evals, point)
     assert after[0] == before[0] and np.array_equal(after[1], before[1]) and after[2] == before[2]
