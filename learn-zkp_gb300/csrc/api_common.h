@@ -188,6 +188,9 @@ int open_session_enqueue_start(bf_open_session* s);
 const uint4* open_session_point_dev(const bf_open_session* s);
 void open_session_mark_launched(bf_open_session* s);  // the resident open was launched by a graph
 cudaStream_t open_session_stream(const bf_open_session* s);
+// Moves the session's later work (the query gather and proof readout) to `st`;
+// its earlier work must have completed.
+void open_session_set_stream(bf_open_session* s, cudaStream_t st);
 cudaEvent_t open_session_event(const bf_open_session* s);
 int open_resident_prepare(bf_open_session* s, const bfh::Challenger& ch);
 int open_resident_enqueue_device(bf_open_session* s, const uint4* root_dev, const uint4* value_dev);

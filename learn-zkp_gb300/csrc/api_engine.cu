@@ -307,8 +307,17 @@ int complete_job(bf_engine* e, Job* j) {
   TRY(open_resident_complete(j->sess, j->ch));
   std::vector<uint64_t> idx(p->Q);
   for (size_t q = 0; q < p->Q; ++q) idx[q] = j->ch.sample_bits(p->L);
-  TRY(open_finish_enqueue(j->sess, idx.data(), idx.size()));
-  TRY(open_finish_complete(j->sess, pj->proof, pj->proof_cap, &pj->proof_len));
+  // The gather and proof readout go to the slot's high-priority stream: the
+  // job's rounds are done, and its blocks then start ahead of the waiting
+  // blocks of other jobs' long kernels instead of behind them, so the slot
+  // (and its memory) is released sooner.
+  const cudaStream_t own = open_session_stream(j->sess);
+  const cudaStream_t fast = e->streams_hi.empty() ? own : e->streams_hi[j->slot];
+  open_session_set_stream(j->sess, fast);
+  int rc = open_finish_enqueue(j->sess, idx.data(), idx.size());
+  if (rc >= 0) rc = open_finish_complete(j->sess, pj->proof, pj->proof_cap, &pj->proof_len);
+  open_session_set_stream(j->sess, own);
+  TRY(rc);
   bfh::digest_from_interleaved(slot_pin(e, j->slot), pj->root);  // the tree root, stored interleaved
   std::memcpy(pj->value, slot_pin(e, j->slot) + 64, 16);
   return BF_OK;
@@ -530,8 +539,9 @@ int bf_engine_create(int device, int lambda, int log2_c, int max_inflight, size_
   }
   CU(e->pin.ensure(128 * (size_t)max_inflight));
   e->plans.resize(max_inflight);
-  const unsigned hw = std::thread::hardware_concurrency();
-  const int n_completers = std::max(1, std::min(4, (int)(hw > 2 ? hw / 2 : 1)));
+  // Completion threads mostly wait for a job's gather and proof readout, so
+  // there is one per two slots (at least one, at most 16) rather than per core.
+  const int n_completers = std::max(1, std::min(16, max_inflight / 2));
   for (int i = 0; i < n_completers; ++i) e->completers.emplace_back(completer_loop, e.get());
   *out = e.release();
   return BF_OK;

@@ -592,6 +592,7 @@ void open_session_mark_launched(bf_open_session* s) {
 }
 
 cudaStream_t open_session_stream(const bf_open_session* s) { return s->st; }
+void open_session_set_stream(bf_open_session* s, cudaStream_t st) { s->st = st; }
 cudaEvent_t open_session_event(const bf_open_session* s) { return s->ev; }
 
 // bf_open_start; `values` may be null when a device-transcript open will
