@@ -1,6 +1,7 @@
 """Build recipe for the oracle (test infrastructure only).
 
-Compiles oracle.cpp with the host C++ compiler into oracle/_build/liboracle.so.
+Compiles oracle.cpp (the binary field POLYVAL) and oracle_bb.cpp (the prime
+field BabyBear) with the host C++ compiler into oracle/_build/liboracle.so.
 On aarch64 the carry-less multiply uses the PMULL instruction (the analogue of
 the reference's NEON backend, p3/src/polyval/aarch64_neon.rs); elsewhere the
 portable 4-bit-window multiply is used.  Both give identical results.
@@ -15,9 +16,12 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liboracle.so")
 
 
+SOURCES = ["oracle.cpp", "oracle_bb.cpp"]
+
+
 def build(force: bool = False) -> str:
-    src = os.path.join(HERE, "oracle.cpp")
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(src):
+    srcs = [os.path.join(HERE, f) for f in SOURCES]
+    if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(f) for f in srcs):
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
     cxx = os.environ.get("CXX", "g++")
@@ -25,7 +29,7 @@ def build(force: bool = False) -> str:
     if platform.machine() in ("aarch64", "arm64"):
         flags += ["-march=armv8-a+crypto", "-DORACLE_PMULL"]
     tmp = LIB + ".tmp"
-    subprocess.check_call([cxx, *flags, src, "-o", tmp])
+    subprocess.check_call([cxx, *flags, *srcs, "-o", tmp])
     os.replace(tmp, LIB)
     return LIB
 

@@ -53,6 +53,18 @@ def lib():
         L.orc_commit_eval_open.argtypes = [C.c_int, C.c_int, u8p, u8p, u8p, u8p, sz, C.POINTER(sz)]
         L.orc_sumcheck_prove.argtypes = [C.c_int, C.c_int, u8p, u8p, u8p, sz, u8p]
         L.orc_sumcheck_verify.argtypes = [C.c_int, C.c_int, u8p, u8p, u8p, u8p, sz, u8p]
+        # prime field (BabyBear, quintic extension; oracle_bb.cpp)
+        L.orc_bb_emul.argtypes = [u8p, u8p, u8p, sz]
+        L.orc_bb_einv.argtypes = [u8p, u8p, sz]
+        L.orc_bb_dft.argtypes = [C.c_int, C.POINTER(C.c_uint32), C.c_int]
+        L.orc_bb_num_queries.argtypes = [C.c_int, C.c_int]
+        L.orc_bb_num_queries.restype = sz
+        L.orc_bb_encode.argtypes = [C.c_int, C.c_int, u8p, u8p]
+        L.orc_bb_commit.argtypes = [C.c_int, C.c_int, u8p, u8p]
+        L.orc_bb_eval.argtypes = [C.c_int, u8p, u8p, u8p]
+        L.orc_bb_harness_prepare.argtypes = [C.c_int, C.c_int, u8p, u8p, u8p, u8p, u8p, C.POINTER(sz)]
+        L.orc_bb_open.argtypes = [C.c_int, C.c_int, u8p, u8p, u8p, u8p, sz, u8p, sz, C.POINTER(sz)]
+        L.orc_bb_verify.argtypes = [C.c_int, C.c_int, u8p, u8p, u8p, u8p, sz, u8p, sz]
         _lib = L
     return _lib
 
@@ -312,3 +324,95 @@ def sumcheck_verify(k: int, n: int, claim, round_polys, final_evals, blob: bytes
     fe = _elems(final_evals)
     b = _buf(blob)
     return lib().orc_sumcheck_verify(k, n, _p(c), _p(rp), _p(fe), _p(b), b.size, None)
+
+
+# ---------------------------------------------------------------------------
+# Prime field: BabyBear elements are uint32 (canonical), extension elements
+# uint32 arrays of shape (n, 5) (coefficients of 1, X, .., X^4).
+# ---------------------------------------------------------------------------
+BB_P = 2013265921
+
+
+def _u32(a):
+    return np.ascontiguousarray(np.asarray(a, dtype=np.uint32))
+
+
+def _pu(a):
+    return a.ctypes.data_as(C.POINTER(C.c_uint8))
+
+
+def bb_emul(a, b):
+    a, b = _u32(a).reshape(-1, 5), _u32(b).reshape(-1, 5)
+    out = np.zeros_like(a)
+    lib().orc_bb_emul(_pu(a), _pu(b), _pu(out), a.shape[0])
+    return out
+
+
+def bb_einv(a):
+    a = _u32(a).reshape(-1, 5)
+    out = np.zeros_like(a)
+    lib().orc_bb_einv(_pu(a), _pu(out), a.shape[0])
+    return out
+
+
+def bb_dft(log_n: int, data, definition: bool = False):
+    d = _u32(data).copy()
+    assert lib().orc_bb_dft(log_n, d.ctypes.data_as(C.POINTER(C.c_uint32)), 1 if definition else 0) == 0
+    return d
+
+
+def bb_num_queries(log2_c: int, lam: int = 128) -> int:
+    return int(lib().orc_bb_num_queries(lam, log2_c))
+
+
+def bb_encode(n: int, log2_c: int, data):
+    d = _u32(data)
+    out = np.zeros(1 << (n + log2_c), dtype=np.uint32)
+    assert lib().orc_bb_encode(n, log2_c, _pu(d), _pu(out)) == 0
+    return out
+
+
+def bb_commit(n: int, log2_c: int, data) -> bytes:
+    d = _u32(data)
+    root = np.zeros(32, dtype=np.uint8)
+    assert lib().orc_bb_commit(n, log2_c, _pu(d), _p(root)) == 0
+    return root.tobytes()
+
+
+def bb_eval(n: int, data, point):
+    d, pt = _u32(data), _u32(point).reshape(-1, 5) if n else np.zeros((1, 5), np.uint32)
+    out = np.zeros(5, dtype=np.uint32)
+    assert lib().orc_bb_eval(n, _pu(d), _pu(pt), _pu(out)) == 0
+    return out
+
+
+def bb_harness_prepare(n: int, log2_c: int, data, point):
+    d, pt = _u32(data), _u32(point).reshape(-1, 5) if n else np.zeros((1, 5), np.uint32)
+    root = np.zeros(32, dtype=np.uint8)
+    val = np.zeros(5, dtype=np.uint32)
+    blob = np.zeros(128, dtype=np.uint8)
+    bl = C.c_size_t(blob.size)
+    assert lib().orc_bb_harness_prepare(n, log2_c, _pu(d), _pu(pt), _p(root), _pu(val), _p(blob), C.byref(bl)) == 0
+    return root.tobytes(), val, blob[: bl.value].tobytes()
+
+
+def bb_open(n: int, log2_c: int, data, point, value, blob: bytes) -> bytes:
+    d, pt = _u32(data), _u32(point).reshape(-1, 5) if n else np.zeros((1, 5), np.uint32)
+    v, b = _u32(value), _buf(blob)
+    cap = 1 << 16
+    while True:
+        out = np.zeros(cap, dtype=np.uint8)
+        ln = C.c_size_t(0)
+        rc = lib().orc_bb_open(n, log2_c, _pu(d), _pu(pt), _pu(v), _p(b), b.size, _p(out), cap, C.byref(ln))
+        if rc == -2:
+            cap = ln.value
+            continue
+        assert rc == 0, rc
+        return out[: ln.value].tobytes()
+
+
+def bb_verify(n: int, log2_c: int, root: bytes, point, value, blob: bytes, proof: bytes) -> int:
+    pt = _u32(point).reshape(-1, 5) if n else np.zeros((1, 5), np.uint32)
+    v, r, b, pf = _u32(value), _buf(root), _buf(blob), _buf(proof)
+    return lib().orc_bb_verify(n, log2_c, _p(r), _pu(pt), _pu(v), _p(b), b.size,
+                               _p(pf) if pf.size else _p(np.zeros(1, np.uint8)), pf.size)

@@ -1,0 +1,71 @@
+"""The prime-field oracle (BabyBear, quintic extension, Reed–Solomon code)
+against definitions: field axioms and inverses, the DFT against its
+definition, the code's folding identity, and prove -> verify over the
+reference's harness with tampered proofs rejected (the reference's own tests
+for this path are prove/verify round trips, poly-commit/src/basefold.rs:
+470-478)."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+P = O.BB_P
+
+
+def rnd(shape, seed):
+    return np.random.default_rng(seed).integers(0, P, size=shape, dtype=np.uint64).astype(np.uint32)
+
+
+def test_field_constants():
+    assert pow(31, 15, P) == 0x1A427A41  # the two-adic generator
+    g = 0x1A427A41
+    assert pow(g, 1 << 26, P) == P - 1 and pow(g, 1 << 27, P) == 1
+    assert pow(2, (P - 1) // 5, P) != 1  # X^5 - 2 is irreducible
+
+
+def test_extension_inverse_and_product():
+    a, b, c = rnd((200, 5), 1), rnd((200, 5), 2), rnd((200, 5), 3)
+    one = np.zeros((200, 5), np.uint32)
+    one[:, 0] = 1
+    assert np.array_equal(O.bb_emul(a, O.bb_einv(a)), one)
+    assert np.array_equal(O.bb_emul(O.bb_emul(a, b), c), O.bb_emul(a, O.bb_emul(b, c)))
+    assert np.array_equal(O.bb_emul(a, b), O.bb_emul(b, a))
+    # X^5 = 2
+    x = np.zeros((1, 5), np.uint32)
+    x[0, 1] = 1
+    x5 = O.bb_emul(O.bb_emul(O.bb_emul(O.bb_emul(x, x), x), x), x)
+    assert x5.tolist() == [[2, 0, 0, 0, 0]]
+
+
+@pytest.mark.parametrize("log_n", [0, 1, 3, 6, 9])
+def test_dft_matches_definition(log_n):
+    a = rnd(1 << log_n, 10 + log_n)
+    assert np.array_equal(O.bb_dft(log_n, a), O.bb_dft(log_n, a, definition=True))
+
+
+def test_num_queries():
+    # delta = 1 - (1 - 1/c) / 3 (reed_solomon.rs:58-64)
+    import math
+    for log2_c in (1, 2, 3):
+        c = 1 << log2_c
+        assert O.bb_num_queries(log2_c) == math.ceil(128 / -math.log2(1 - (1 - 1 / c) / 3))
+
+
+@pytest.mark.parametrize("n,log2_c", [(0, 1), (1, 1), (4, 1), (6, 2), (8, 1), (9, 3)])
+def test_prove_verify_round_trip(n, log2_c):
+    data = rnd(1 << n, 100 + n)
+    point = rnd((n, 5), 200 + n)
+    root, value, blob = O.bb_harness_prepare(n, log2_c, data, point)
+    assert root == O.bb_commit(n, log2_c, data)
+    assert np.array_equal(value, O.bb_eval(n, data, point))
+    proof = O.bb_open(n, log2_c, data, point, value, blob)
+    assert O.bb_verify(n, log2_c, root, point, value, blob, proof) == 0
+    if n == 0:
+        return
+    bad_value = value.copy()
+    bad_value[0] = (int(bad_value[0]) + 1) % P
+    assert O.bb_verify(n, log2_c, root, point, bad_value, blob, proof) != 0
+    for pos in (30, len(proof) // 2, len(proof) - 3):
+        b = bytearray(proof)
+        b[pos] ^= 1
+        assert O.bb_verify(n, log2_c, root, point, value, blob, bytes(b)) != 0, pos
