@@ -339,6 +339,65 @@ int bf_profile_read(bf_pcs* pcs, double* ms, uint64_t* launches, int nclasses);
 int bf_test_gf_mul(int device, const uint8_t* a, const uint8_t* b, uint8_t* out, size_t n);
 int bf_test_keccak_f(int device, uint64_t* states, size_t n);
 
+/* ---- Prime-field Basefold: the same PolyCommitScheme instantiated as
+ *   Basefold<BabyBear, BinomialExtensionField<BabyBear, 5>,
+ *            ReedSolomonCode<BabyBear>, Keccak256MerkleTreeMmcs<BabyBear>>
+ * (poly-commit/benches/poly-commit.rs:28-43,114-123; code/reed_solomon.rs).
+ * Conventions of this section:
+ *  - A BabyBear (p = 15 * 2^27 + 1) is its canonical value as a u32
+ *    (< p), little-endian: the bytes bincode writes for it.  Evaluations are
+ *    row-major u32, 2^num_vars rows of `width` (RowMajorMatrix<BabyBear>);
+ *    a value >= p is rejected with BF_ERR_ARG.
+ *  - An extension element is its five coefficients (of 1, X, .., X^4 with
+ *    X^5 = 2), canonical u32 each: 20 bytes.  Points are num_vars of them;
+ *    values `width` of them.
+ *  - The transcript is a bf_challenger: the byte-level HashChallenger is the
+ *    same for both fields; the prime path samples field elements from it as
+ *    GenericChallenger<BabyBear, _> does (bf_challenger_sample_bb_ext).
+ *  - Same ownership and threading rules as bf_pcs. */
+typedef struct bf_bb_pcs bf_bb_pcs;
+typedef struct bf_bb_commitment bf_bb_commitment;
+
+/* PolyCommitScheme::setup with ReedSolomonCode::new(lambda, log2_c,
+ * num_vars) (reed_solomon.rs:19-39); num_vars + log2_c <= 27.  device < 0
+ * makes a verifier-only pcs (bf_bb_verify, sizes). */
+int bf_bb_pcs_setup(int device, int lambda, int log2_c, int num_vars, void* stream, bf_bb_pcs** out);
+void bf_bb_pcs_free(bf_bb_pcs* pcs);
+/* RandomFoldableCode::num_queries (reed_solomon.rs:57-64). */
+size_t bf_bb_pcs_num_queries(const bf_bb_pcs* pcs);
+/* Exact bincode size of the proof of a width-`width` open of n_evals (0 or
+ * 1) points. */
+size_t bf_bb_pcs_proof_size(const bf_bb_pcs* pcs, size_t width, int n_evals);
+/* PolyCommitScheme::commit (basefold.rs:112-120): host evaluations
+ * (bf_bb_commit, pinned memory overlaps the copy best) or device memory
+ * (bf_bb_commit_device, 4-byte aligned, read and kept by reference until
+ * the commitment is freed). */
+int bf_bb_commit(bf_bb_pcs* pcs, const uint32_t* evals, size_t width, bf_bb_commitment** out, uint8_t root[32]);
+int bf_bb_commit_device(bf_bb_pcs* pcs, const void* d_evals, size_t width, bf_bb_commitment** out,
+                        uint8_t root[32]);
+int bf_bb_commitment_root(const bf_bb_commitment* comm, uint8_t root[32]);
+void bf_bb_commitment_free(bf_bb_commitment* comm);
+/* PolyCommitScheme::eval (basefold.rs:126-131): `values` receives the
+ * width column evaluations at the point (width x 20 bytes). */
+int bf_bb_eval(bf_bb_pcs* pcs, const bf_bb_commitment* comm, const uint8_t* point, uint8_t* values);
+/* PolyCommitScheme::open (basefold.rs:133-232) of n_evals points (0: the
+ * default proof, as the reference returns for no evaluations; 1: `point`
+ * and the commitment's width `values`); the transcript advances exactly as
+ * the reference's.  Returns BF_ERR_BUFFER with *proof_len set when cap is
+ * too small, and BF_ERR_NOT_INVERTIBLE for a coordinate r = 0 (or r = 1
+ * below the last). */
+int bf_bb_open(bf_bb_pcs* pcs, const bf_bb_commitment* comm, const uint8_t* point, const uint8_t* values,
+               int n_evals, bf_challenger* ch, uint8_t* proof, size_t cap, size_t* proof_len);
+/* PolyCommitScheme::verify (basefold.rs:234-324), on the host; n_evals 0
+ * accepts anything, as the reference does.  Returns BF_VERIFY_* (>= 0) or
+ * a negative BF_ERR_*. */
+int bf_bb_verify(const bf_bb_pcs* pcs, const uint8_t root[32], const uint8_t* point, const uint8_t* values,
+                 size_t width, int n_evals, bf_challenger* ch, const uint8_t* proof, size_t proof_len);
+/* CanSample<BinomialExtensionField<BabyBear, 5>>::sample (challenger.rs:
+ * 62-74): five BabyBears, each from 4 bytes shifted right by one and
+ * rejected while >= p. */
+int bf_challenger_sample_bb_ext(bf_challenger* ch, uint8_t out[20]);
+
 #ifdef __cplusplus
 }
 #endif

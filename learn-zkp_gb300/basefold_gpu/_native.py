@@ -22,6 +22,9 @@ EXPORTS = [
     "bf_engine_poll", "bf_eval_noalloc", "bf_pcs_autotune", "bf_pcs_get_tune", "bf_pcs_set_tune",
     "bf_engine_autotune", "bf_engine_graphs", "bf_engine_stats", "bf_verify_batch", "bf_engine_set_tune", "bf_engine_cancel", "bf_engine_schedule",
     "bf_eval_data", "bf_tune_cache_load", "bf_tune_cache_save", "bf_tune_cache_clear",
+    "bf_bb_pcs_setup", "bf_bb_pcs_free", "bf_bb_pcs_num_queries", "bf_bb_pcs_proof_size", "bf_bb_commit",
+    "bf_bb_commit_device", "bf_bb_commitment_root", "bf_bb_commitment_free", "bf_bb_eval", "bf_bb_open",
+    "bf_bb_verify", "bf_challenger_sample_bb_ext",
 ]
 
 BF_OK = 0
@@ -133,6 +136,18 @@ def lib():
         "bf_engine_set_tune": ([vp, C.POINTER(i), i], i),
         "bf_engine_cancel": ([vp, vp], i),
         "bf_engine_schedule": ([vp, i, i], i),
+        "bf_bb_pcs_setup": ([i, i, i, i, vp, C.POINTER(vp)], i),
+        "bf_bb_pcs_free": ([vp], None),
+        "bf_bb_pcs_num_queries": ([vp], sz),
+        "bf_bb_pcs_proof_size": ([vp, sz, i], sz),
+        "bf_bb_commit": ([vp, vp, sz, C.POINTER(vp), u8p], i),
+        "bf_bb_commit_device": ([vp, vp, sz, C.POINTER(vp), u8p], i),
+        "bf_bb_commitment_root": ([vp, u8p], i),
+        "bf_bb_commitment_free": ([vp], None),
+        "bf_bb_eval": ([vp, vp, u8p, u8p], i),
+        "bf_bb_open": ([vp, vp, u8p, u8p, i, vp, u8p, sz, C.POINTER(sz)], i),
+        "bf_bb_verify": ([vp, u8p, u8p, u8p, sz, i, vp, u8p, sz], i),
+        "bf_challenger_sample_bb_ext": ([vp, u8p], i),
     }
     for name, (args, res) in decl.items():
         f = getattr(L, name)

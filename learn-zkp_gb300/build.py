@@ -16,8 +16,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "basefold_gpu", "_lib")
 LIB = os.path.join(OUT_DIR, "libbasefold_gpu.so")
-SOURCES = ["kernels.cu", "kernels_tail.cu", "kernels_verify.cu", "api_pcs.cu", "api_open.cu", "api_verify.cu", "api_sumcheck.cu", "api_engine.cu", "api_noalloc.cu", "api_tune.cu"]
-HEADERS = ["gf128.cuh", "keccak.cuh", "bf_internal.h", "host_math.h", "api_common.h"]
+SOURCES = ["kernels.cu", "kernels_tail.cu", "kernels_verify.cu", "kernels_bb.cu", "api_pcs.cu", "api_open.cu", "api_verify.cu", "api_sumcheck.cu", "api_engine.cu", "api_noalloc.cu", "api_tune.cu", "api_bb.cu"]
+HEADERS = ["gf128.cuh", "keccak.cuh", "bf_internal.h", "host_math.h", "api_common.h", "bb.cuh", "bb_internal.h", "bb_host.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -1,0 +1,647 @@
+// C ABI of the prime-field Basefold: Basefold<BabyBear, BinomialExtension
+// Field<BabyBear, 5>, ReedSolomonCode<BabyBear>, Keccak256MerkleTreeMmcs>
+// (poly-commit/src/basefold.rs, poly-commit/src/basefold/code/reed_solomon.rs).
+//
+// The GPU holds every array (evaluations, codeword, folded codewords, trees,
+// eq tables); the host runs the transcript and the O(num_vars) sumcheck
+// scalars, reading 96 bytes back per open round (the folded-codeword root and
+// the round's sum).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <memory>
+#include <vector>
+
+#include "api_common.h"
+#include "bb_host.h"
+#include "bb_internal.h"
+
+using namespace bfapi;
+using bbh::E;
+
+struct bf_bb_pcs {
+  std::atomic<int> refs{1};
+  int device = -1;
+  int lambda = 128, log2_c = 1, d = 0, L = 0;
+  size_t Q = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  DevBuf tw;    // DIT twiddles: layer s at 2^s - 1, g_s^k for k < 2^s (Montgomery)
+  DevBuf tinv;  // fold constants: round i at c (2^i - 1), (2 t_i^j)^-1 for j < n_i (Montgomery)
+  DevBuf small;  // 4 KB: the canonical flag, sums, roots
+  DevBuf ws;       // grow-only scratch of bf_bb_eval
+  DevBuf open_ws;  // grow-only workspace of bf_bb_open
+  PinnedBuf pin;
+
+  size_t c() const { return (size_t)1 << log2_c; }
+  size_t n_d() const { return (size_t)1 << L; }
+  size_t n_i(int i) const { return c() << i; }
+  size_t tinv_off(int i) const { return c() * (((size_t)1 << i) - 1); }
+  // One query record (basefold.rs:56-65 in bincode): the codeword row and its
+  // path, then per round the sibling and its path.
+  size_t rec_bytes(size_t w) const {
+    size_t words = 2 + w + 2 + 8 * (size_t)L + 2;
+    for (int i = 0; i < d; ++i) words += 7 + 8 * (size_t)(log2_c + i);
+    return 4 * words;
+  }
+  size_t header_bytes() const { return 52 + 80 * (size_t)d; }
+  ~bf_bb_pcs() {
+    if (device >= 0) {
+      cudaSetDevice(device);
+      if (stream) cudaStreamSynchronize(stream);
+      tw.release();
+      tinv.release();
+      small.release();
+      ws.release();
+      open_ws.release();
+      if (own_stream && stream) cudaStreamDestroy(stream);
+    }
+  }
+};
+
+struct bf_bb_commitment {
+  bf_bb_pcs* pcs = nullptr;
+  size_t w = 1;
+  DevBuf data;  // canonical evaluations (owned copy, or the caller's device buffer)
+  DevBuf cw;    // codeword, Montgomery, n_d rows of w
+  DevBuf tree;  // 2 n_d digests, reversed level storage, interleaved lanes
+  uint8_t root[32];
+};
+
+namespace {
+
+void bb_acquire(bf_bb_pcs* p) { p->refs.fetch_add(1); }
+void bb_release(bf_bb_pcs* p) {
+  if (p->refs.fetch_sub(1) == 1) delete p;
+}
+
+// RandomFoldableCode::num_queries of ReedSolomonCode (reed_solomon.rs:57-64):
+// delta = 1 - (1 - 1/c) / 3 in the unique-decoding regime.
+size_t bb_num_queries(int lambda, int log2_c) {
+  const double c = (double)((size_t)1 << log2_c);
+  const double delta = 1.0 - (1.0 - 1.0 / c) / 3.0;
+  const double q = std::ceil((double)lambda / -std::log2(delta));
+  if (!(q > 0) || !std::isfinite(q)) return 0;  // c = 1: the Rust cast of -inf is 0
+  return (size_t)q;
+}
+
+int load_points(const uint8_t* bytes, size_t n, std::vector<E>& out, const char* what) {
+  out.resize(n);
+  for (size_t k = 0; k < n; ++k) {
+    out[k] = bbh::load(bytes + 20 * k);
+    if (!bbh::canonical(out[k])) return fail(BF_ERR_ARG, "%s %zu has a coefficient >= p", what, k);
+  }
+  return BF_OK;
+}
+
+// Device eq table of x (2^|x| extension entries) in `ev`.
+int eq_table_device(bf_bb_pcs* p, const std::vector<E>& x, uint32_t* ev) {
+  const bb::E5 one = bb::e_from(bb::MONT_ONE);
+  CU(cudaMemcpyAsync(ev, &one, sizeof(one), cudaMemcpyHostToDevice, p->stream));
+  for (size_t i = 0; i < x.size(); ++i) CU(bf::bb_launch_eq_expand(ev, (size_t)1 << i, bbh::to_dev(x[i]), p->stream));
+  return BF_OK;
+}
+
+int commit_device(bf_bb_pcs* p, bf_bb_commitment* cm, const uint32_t* data) {
+  const size_t w = cm->w, n = p->n_d();
+  CU(cm->cw.alloc(4 * n * w));
+  CU(cm->tree.alloc(64 * n));
+  uint32_t* flag = p->small.as<uint32_t>();
+  CU(cudaMemsetAsync(flag, 0, 4, p->stream));
+  CU(bf::bb_launch_encode(data, cm->cw.as<uint32_t>(), p->d, p->log2_c, w, p->tw.as<uint32_t>(), flag, p->stream));
+  uint4* leaves = cm->tree.as<uint4>();
+  CU(bf::bb_launch_leaves_rows(cm->cw.as<uint32_t>(), leaves, n, w, p->L, p->stream));
+  uint4* root_dev = p->small.as<uint4>() + 2;
+  CU(bf::launch_tree(leaves, n, p->stream, root_dev, bf::Tune()));
+  CU(cudaMemcpyAsync(p->pin.b(), p->small.p, 64, cudaMemcpyDeviceToHost, p->stream));
+  CU(cudaStreamSynchronize(p->stream));
+  uint32_t bad;
+  std::memcpy(&bad, p->pin.b(), 4);
+  if (bad) return fail(BF_ERR_ARG, "an evaluation is not a canonical BabyBear (>= p)");
+  bfh::digest_from_interleaved(p->pin.b() + 32, cm->root);
+  return BF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bf_bb_pcs_setup(int device, int lambda, int log2_c, int num_vars, void* stream, bf_bb_pcs** out) {
+  if (!out) return fail(BF_ERR_ARG, "out is null");
+  *out = nullptr;
+  if (lambda < 0 || log2_c < 0 || num_vars < 0 || num_vars + log2_c > 27)
+    return fail(BF_ERR_ARG, "unsupported code parameters lambda=%d log2_c=%d num_vars=%d (num_vars + log2_c <= 27)",
+                lambda, log2_c, num_vars);
+  std::unique_ptr<bf_bb_pcs> p(new bf_bb_pcs());
+  p->lambda = lambda;
+  p->log2_c = log2_c;
+  p->d = num_vars;
+  p->L = num_vars + log2_c;
+  p->Q = bb_num_queries(lambda, log2_c);
+  if (device < 0) {  // verifier-only: no GPU is touched
+    *out = p.release();
+    return BF_OK;
+  }
+  p->device = device;
+  CU(cudaSetDevice(device));
+  if (stream) {
+    p->stream = reinterpret_cast<cudaStream_t>(stream);
+  } else {
+    CU(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
+    p->own_stream = true;
+  }
+  CU(p->pin.ensure(4096));
+  CU(p->small.alloc(4096));
+  // DIT twiddles: layer s (half-size 2^s) uses g_s = two_adic_generator(s + 1)
+  CU(p->tw.alloc(4 * p->n_d()));
+  for (int s = 0; s < p->L; ++s)
+    CU(bf::bb_launch_pow_table(p->tw.as<uint32_t>() + ((size_t)1 << s) - 1, (size_t)1 << s,
+                               bb::to_mont(bbh::two_adic_generator(s + 1)), bb::MONT_ONE, p->stream));
+  // ReedSolomonCode::new (reed_solomon.rs:20-38): t_i = two_adic_generator(
+  // log2_c + i + 1), entry j = (2 t_i^j)^-1 = 2^-1 (t_i^-1)^j
+  CU(p->tinv.alloc(4 * p->c() * (((size_t)1 << p->d) - 1) + 4));
+  for (int i = 0; i < p->d; ++i) {
+    const uint32_t t_inv = bbh::finv(bbh::two_adic_generator(p->log2_c + i + 1));
+    CU(bf::bb_launch_pow_table(p->tinv.as<uint32_t>() + p->tinv_off(i), p->n_i(i), bb::to_mont(t_inv),
+                               bb::MONT_INV2, p->stream));
+  }
+  CU(cudaStreamSynchronize(p->stream));
+  *out = p.release();
+  return BF_OK;
+}
+
+void bf_bb_pcs_free(bf_bb_pcs* pcs) {
+  if (pcs) bb_release(pcs);
+}
+
+size_t bf_bb_pcs_num_queries(const bf_bb_pcs* pcs) { return pcs ? pcs->Q : 0; }
+
+size_t bf_bb_pcs_proof_size(const bf_bb_pcs* p, size_t width, int n_evals) {
+  if (!p || width == 0) return 0;
+  if (n_evals == 0) return 32;  // BasefoldProof::default(): four empty vectors
+  return p->header_bytes() + p->Q * p->rec_bytes(width);
+}
+
+static int check_commit_args(bf_bb_pcs* p, const void* evals, size_t width, bf_bb_commitment** out) {
+  if (!p || !evals || !out) return fail(BF_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (p->device < 0) return fail(BF_ERR_ARG, "verifier-only pcs (device < 0)");
+  if (width == 0 || width > 65536) return fail(BF_ERR_ARG, "width %zu out of range (1..65536)", width);
+  return BF_OK;
+}
+
+int bf_bb_commit(bf_bb_pcs* p, const uint32_t* evals, size_t width, bf_bb_commitment** out, uint8_t root[32]) {
+  TRY(check_commit_args(p, evals, width, out));
+  DeviceGuard g(p->device);
+  std::unique_ptr<bf_bb_commitment> cm(new bf_bb_commitment());
+  cm->pcs = p;
+  cm->w = width;
+  const size_t bytes = 4 * width << p->d;
+  CU(cm->data.alloc(bytes));
+  CU(cudaMemcpyAsync(cm->data.p, evals, bytes, cudaMemcpyHostToDevice, p->stream));
+  TRY(commit_device(p, cm.get(), cm->data.as<uint32_t>()));
+  if (root) std::memcpy(root, cm->root, 32);
+  bb_acquire(p);
+  *out = cm.release();
+  return BF_OK;
+}
+
+int bf_bb_commit_device(bf_bb_pcs* p, const void* d_evals, size_t width, bf_bb_commitment** out, uint8_t root[32]) {
+  TRY(check_commit_args(p, d_evals, width, out));
+  if (reinterpret_cast<uintptr_t>(d_evals) & 3) return fail(BF_ERR_ARG, "device evaluations must be 4-byte aligned");
+  DeviceGuard g(p->device);
+  std::unique_ptr<bf_bb_commitment> cm(new bf_bb_commitment());
+  cm->pcs = p;
+  cm->w = width;
+  cm->data.p = const_cast<void*>(d_evals);
+  cm->data.owned = false;
+  cm->data.bytes = 4 * width << p->d;
+  TRY(commit_device(p, cm.get(), cm->data.as<uint32_t>()));
+  if (root) std::memcpy(root, cm->root, 32);
+  bb_acquire(p);
+  *out = cm.release();
+  return BF_OK;
+}
+
+int bf_bb_commitment_root(const bf_bb_commitment* cm, uint8_t root[32]) {
+  if (!cm || !root) return fail(BF_ERR_ARG, "null argument");
+  std::memcpy(root, cm->root, 32);
+  return BF_OK;
+}
+
+void bf_bb_commitment_free(bf_bb_commitment* cm) {
+  if (!cm) return;
+  bf_bb_pcs* p = cm->pcs;
+  {
+    DeviceGuard g(p->device);
+    cudaStreamSynchronize(p->stream);
+    delete cm;
+  }
+  bb_release(p);
+}
+
+int bf_bb_eval(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, uint8_t* values) {
+  if (!p || !cm || !values || (p->d > 0 && !point)) return fail(BF_ERR_ARG, "null argument");
+  if (cm->pcs != p) return fail(BF_ERR_ARG, "commitment made by another pcs");
+  std::vector<E> x;
+  TRY(load_points(point, (size_t)p->d, x, "point coordinate"));
+  DeviceGuard g(p->device);
+  const size_t rows = (size_t)1 << p->d, w = cm->w;
+  // the sums are 64-bit atomics: their slot starts on a 256-byte boundary
+  const size_t eq_bytes = (20 * rows + 255) & ~(size_t)255, acc_bytes = 40 * w;
+  if (p->ws.bytes < eq_bytes + acc_bytes) CU(p->ws.alloc(eq_bytes + acc_bytes));
+  CU(p->pin.ensure(acc_bytes + 64));
+  uint32_t* eq = p->ws.as<uint32_t>();
+  unsigned long long* acc = reinterpret_cast<unsigned long long*>(p->ws.as<uint8_t>() + eq_bytes);
+  TRY(eq_table_device(p, x, eq));
+  CU(cudaMemsetAsync(acc, 0, acc_bytes, p->stream));
+  // evaluate = sum over the hypercube of eq(b, point) f(b): the same field
+  // value as MultiPoly::evaluate's fix_last_var chain
+  if (w == 1)
+    CU(bf::bb_launch_dot(eq, cm->data.as<uint32_t>(), 1, rows, acc, p->stream));
+  else
+    CU(bf::bb_launch_eval_cols(eq, cm->data.as<uint32_t>(), rows, w, acc, p->stream));
+  CU(cudaMemcpyAsync(p->pin.p, acc, acc_bytes, cudaMemcpyDeviceToHost, p->stream));
+  CU(cudaStreamSynchronize(p->stream));
+  const unsigned long long* s = reinterpret_cast<const unsigned long long*>(p->pin.p);
+  for (size_t c = 0; c < w; ++c) bbh::store(values + 20 * c, bbh::from_dev_sums(s + 5 * c));
+  return BF_OK;
+}
+
+int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, const uint8_t* values,
+               int n_evals, bf_challenger* ch, uint8_t* proof, size_t cap, size_t* proof_len) {
+  if (!p || !cm || !ch || !proof_len) return fail(BF_ERR_ARG, "null argument");
+  if (cm->pcs != p) return fail(BF_ERR_ARG, "commitment made by another pcs");
+  if (n_evals < 0 || n_evals > 1) return fail(BF_ERR_ARG, "n_evals %d: one point or none (basefold.rs:143-144)", n_evals);
+  if (n_evals == 0) {  // basefold.rs:139-141
+    *proof_len = 32;
+    if (!proof || cap < 32) return fail(BF_ERR_BUFFER, "proof buffer of %zu bytes, 32 needed", cap);
+    std::memset(proof, 0, 32);
+    return BF_OK;
+  }
+  if (!values || (p->d > 0 && !point)) return fail(BF_ERR_ARG, "null argument");
+  const int d = p->d, L = p->L;
+  const size_t w = cm->w, Q = p->Q, rec = p->rec_bytes(w);
+  const size_t total = p->header_bytes() + Q * rec;
+  *proof_len = total;
+  if (!proof || cap < total) return fail(BF_ERR_BUFFER, "proof buffer of %zu bytes, %zu needed", cap, total);
+  std::vector<E> r, vals;
+  TRY(load_points(point, (size_t)d, r, "point coordinate"));
+  TRY(load_points(values, w, vals, "value"));
+  bbh::EvalScalars es;
+  if (!es.init(r)) return fail(BF_ERR_NOT_INVERTIBLE, "a point coordinate is 0, or 1 below the last");
+  DeviceGuard g(p->device);
+  bfh::Challenger& tr = ch->c;
+  cudaStream_t st = p->stream;
+
+  // Workspace: batched poly and pi (width > 1), half_eq, two fix buffers,
+  // the fold outputs of every round, the trees of every round, query indices
+  // and records.
+  const size_t rows = (size_t)1 << d, half = rows >> 1;
+  const size_t n_fold = p->c() * (rows - 1);  // sum over rounds of n_i
+  const size_t wsz[] = {w > 1 ? 20 * rows : 0,  w > 1 ? 20 * p->n_d() : 0, 20 * (half ? half : 1), 20 * half,
+                        20 * half,              20 * n_fold,             64 * n_fold,             8 * Q,
+                        Q * rec,                128};
+  size_t off[11] = {0};
+  for (int k = 0; k < 10; ++k) off[k + 1] = off[k] + ((wsz[k] + 255) & ~(size_t)255);
+  if (p->open_ws.bytes < off[10]) CU(p->open_ws.alloc(off[10]));
+  uint8_t* base = p->open_ws.as<uint8_t>();
+  uint32_t* polyE = reinterpret_cast<uint32_t*>(base + off[0]);
+  uint32_t* piE = reinterpret_cast<uint32_t*>(base + off[1]);
+  uint32_t* heq = reinterpret_cast<uint32_t*>(base + off[2]);
+  uint32_t* fixbuf[2] = {reinterpret_cast<uint32_t*>(base + off[3]), reinterpret_cast<uint32_t*>(base + off[4])};
+  uint32_t* folds = reinterpret_cast<uint32_t*>(base + off[5]);
+  uint4* trees = reinterpret_cast<uint4*>(base + off[6]);
+  uint64_t* idx_dev = reinterpret_cast<uint64_t*>(base + off[7]);
+  uint8_t* recs = base + off[8];
+  unsigned long long* acc = reinterpret_cast<unsigned long long*>(base + off[9]);
+  uint4* root_dev = reinterpret_cast<uint4*>(base + off[9] + 64);  // after the five sums
+  CU(p->pin.ensure(8 * Q + 256));
+
+  // The polynomial and codeword the folding sumcheck runs on (basefold.rs:154-177).
+  E claim;
+  const uint32_t* poly = cm->data.as<uint32_t>();
+  const uint32_t* pi = cm->cw.as<uint32_t>();
+  int base_round = 1;  // the first round's poly and pi are base-field arrays
+  if (w == 1) {
+    claim = vals[0];
+  } else {
+    const std::vector<E> s = bbh::scalars_by_eq(w, tr);
+    for (size_t c = 0; c < w; ++c) claim = bbh::eadd(claim, bbh::emul(s[c], vals[c]));
+    std::vector<bb::E5> sd(w);
+    for (size_t c = 0; c < w; ++c) sd[c] = bbh::to_dev(s[c]);
+    DevBuf sdev;
+    CU(sdev.alloc(20 * w));
+    CU(cudaMemcpyAsync(sdev.p, sd.data(), 20 * w, cudaMemcpyHostToDevice, st));
+    CU(bf::bb_launch_combine(cm->data.as<uint32_t>(), 1, rows, w, sdev.as<uint32_t>(), polyE, st));
+    CU(bf::bb_launch_combine(cm->cw.as<uint32_t>(), 0, p->n_d(), w, sdev.as<uint32_t>(), piE, st));
+    CU(cudaStreamSynchronize(st));  // sd and sdev go out of scope
+    poly = polyE;
+    pi = piE;
+    base_round = 0;
+  }
+  if (d > 0) TRY(eq_table_device(p, std::vector<E>(r.begin(), r.end() - 1), heq));
+
+  bbh::Subclaim sc;
+  sc.value = claim;
+  std::vector<std::array<E, 2>> comp;
+  std::vector<std::array<uint8_t, 32>> roots;
+  bf::BbGather gp{};
+  gp.pi0_base = w == 1;
+  size_t fold_off = 0, tree_off = 0;
+  for (int k = 0; k < d; ++k) {  // prove_interleaved_folding_sumcheck (basefold.rs:335-369)
+    const int i = d - 1 - k, li = p->log2_c + i;
+    const size_t ni = p->n_i(i);
+    uint4* tree = trees + 2 * tree_off;
+    gp.pi[k] = pi;
+    gp.trees[k] = tree;
+    const int base_k = k == 0 && base_round;
+    if (k == 0) CU(bf::bb_launch_leaves_pairs(pi, base_k, tree, ni, li, st));  // later rounds: made by the fold
+    CU(bf::launch_tree(tree, ni, st, root_dev, bf::Tune()));
+    CU(cudaMemsetAsync(acc, 0, 40, st));
+    CU(bf::bb_launch_dot(heq, poly, base_k, (size_t)1 << i, acc, st));
+    CU(cudaMemcpyAsync(p->pin.p, acc, 96, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    const unsigned long long* sums = reinterpret_cast<const unsigned long long*>(p->pin.p);
+    std::array<uint8_t, 32> root;
+    bfh::digest_from_interleaved(p->pin.b() + 64, root.data());
+    tr.observe(root.data(), 32);
+    E rp[3];
+    es.round_poly((size_t)i, sc, bbh::from_dev_sums(sums), rp);
+    bbh::observe_e(tr, rp[0]);  // Eval::compress_round_poly keeps c0 and c2
+    bbh::observe_e(tr, rp[2]);
+    const E x = bbh::sample_e(tr);
+    es.fix_last(x);
+    sc.reduce(rp, 3, x);
+    comp.push_back({rp[0], rp[2]});
+    roots.push_back(root);
+    const bb::E5 xd = bbh::to_dev(x);
+    uint32_t* fixed = fixbuf[k & 1];
+    CU(bf::bb_launch_fix(poly, base_k, fixed, (size_t)1 << i, xd, st));
+    poly = fixed;
+    bf::BbFold fp;
+    fp.w = pi;
+    fp.base = base_k;
+    fp.out = folds + 5 * fold_off;
+    fp.tinv = p->tinv.as<uint32_t>() + p->tinv_off(i);
+    fp.n = ni;
+    fp.leaves = i > 0 ? tree + 2 * (2 * ni) : nullptr;  // the next round's tree follows this one
+    fp.leaf_bits = li - 1;
+    CU(bf::bb_launch_fold(fp, xd, st));
+    pi = fp.out;
+    fold_off += ni;
+    tree_off += 2 * ni;
+  }
+  // final_poly: the fully fixed polynomial (one element), observed
+  E fin;
+  {
+    const int fin_base = d == 0 && base_round;
+    CU(cudaMemcpyAsync(p->pin.p, poly, fin_base ? 4 : 20, cudaMemcpyDeviceToHost, st));
+    size_t nchk = 0;
+    if (d > 0) {  // debug_assert_eq!(encode0(final_poly), pi): every entry of the last fold
+      nchk = p->c() < 64 ? p->c() : 64;
+      CU(cudaMemcpyAsync(p->pin.b() + 32, pi, 20 * nchk, cudaMemcpyDeviceToHost, st));
+    }
+    CU(cudaStreamSynchronize(st));
+    if (fin_base) {
+      uint32_t v;
+      std::memcpy(&v, p->pin.p, 4);
+      fin = E::from(v);
+    } else {
+      uint32_t m[5];
+      std::memcpy(m, p->pin.p, 20);
+      for (int q = 0; q < 5; ++q) fin.c[q] = bb::from_mont(m[q]);
+    }
+    for (size_t q = 0; q < nchk; ++q) {
+      uint32_t m[5];
+      std::memcpy(m, p->pin.b() + 32 + 20 * q, 20);
+      E e;
+      for (int t = 0; t < 5; ++t) e.c[t] = bb::from_mont(m[t]);
+      if (e != fin) return fail(BF_ERR_CHECK, "the last folded codeword is not the encoding of the final value");
+    }
+  }
+  bbh::observe_e(tr, fin);
+  std::vector<uint64_t> idx(Q);
+  for (uint64_t& v : idx) v = tr.sample_bits(L);
+  if (Q) {
+    std::memcpy(p->pin.p, idx.data(), 8 * Q);
+    CU(cudaMemcpyAsync(idx_dev, p->pin.p, 8 * Q, cudaMemcpyHostToDevice, st));
+    gp.cw = cm->cw.as<uint32_t>();
+    gp.cw_tree = cm->tree.as<uint4>();
+    gp.idx = idx_dev;
+    gp.out = recs;
+    gp.w = w;
+    gp.rec_bytes = rec;
+    gp.L = L;
+    gp.d = d;
+    gp.log2_c = p->log2_c;
+    gp.nq = (int)Q;
+    CU(bf::bb_launch_gather(gp, st));
+    CU(cudaMemcpyAsync(proof + p->header_bytes(), recs, Q * rec, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+  }
+  // BasefoldProof header: round polys, final poly, pi roots, query count
+  std::vector<uint8_t> h;
+  put_u64(h, (uint64_t)d);
+  for (const auto& c : comp) {
+    put_u64(h, 2);
+    uint8_t b[20];
+    for (const E& e : c) {
+      bbh::store(b, e);
+      h.insert(h.end(), b, b + 20);
+    }
+  }
+  put_u64(h, 1);
+  {
+    uint8_t b[20];
+    bbh::store(b, fin);
+    h.insert(h.end(), b, b + 20);
+  }
+  put_u64(h, (uint64_t)d);
+  for (const auto& rt : roots) h.insert(h.end(), rt.begin(), rt.end());
+  put_u64(h, (uint64_t)Q);
+  if (h.size() != p->header_bytes()) return fail(BF_ERR_CHECK, "proof header size mismatch");
+  std::memcpy(proof, h.data(), h.size());
+  return BF_OK;
+}
+
+// ---- verify (basefold.rs:234-324) on the host -------------------------------------
+namespace {
+struct Reader {
+  const uint8_t* p;
+  size_t n, off = 0;
+  bool ok = true;
+  const uint8_t* take(size_t k) {
+    if (!ok || k > n - off) {
+      ok = false;
+      return nullptr;
+    }
+    const uint8_t* r = p + off;
+    off += k;
+    return r;
+  }
+  uint64_t u64() {
+    const uint8_t* q = take(8);
+    uint64_t v = 0;
+    if (q) std::memcpy(&v, q, 8);
+    return v;
+  }
+  bool e(E& out) {
+    const uint8_t* q = take(20);
+    if (!q) return false;
+    out = bbh::load(q);
+    return bbh::canonical(out);
+  }
+};
+struct Dg {
+  uint8_t b[32];
+};
+Dg hash_bytes(const uint8_t* m, size_t n) {
+  Dg d;
+  bfh::keccak256(m, n, d.b);
+  return d;
+}
+Dg leaf_row(const uint32_t* row, size_t w) {
+  std::vector<uint8_t> b(4 * w);
+  std::memcpy(b.data(), row, 4 * w);
+  return hash_bytes(b.data(), b.size());
+}
+Dg leaf_pair(const E& a, const E& b) {
+  uint8_t m[40];
+  bbh::store(m, a);
+  bbh::store(m + 20, b);
+  return hash_bytes(m, 40);
+}
+// MerkleTreeMmcs::verify_batch for one matrix: the path from leaf `idx` of a
+// `height`-leaf tree to `root`.
+bool verify_path(const uint8_t root[32], Dg leaf, uint64_t idx, const std::vector<Dg>& path, size_t height) {
+  size_t h = 0;
+  while (((size_t)1 << h) < height) ++h;
+  if (path.size() != h) return false;
+  uint8_t buf[64];
+  for (const Dg& s : path) {
+    if (idx & 1) {
+      std::memcpy(buf, s.b, 32);
+      std::memcpy(buf + 32, leaf.b, 32);
+    } else {
+      std::memcpy(buf, leaf.b, 32);
+      std::memcpy(buf + 32, s.b, 32);
+    }
+    leaf = hash_bytes(buf, 64);
+    idx >>= 1;
+  }
+  return std::memcmp(leaf.b, root, 32) == 0;
+}
+bool read_path(Reader& rd, std::vector<Dg>& path) {
+  const uint64_t n = rd.u64();
+  if (!rd.ok || n > 64) return false;
+  path.resize(n);
+  for (Dg& g : path) {
+    const uint8_t* q = rd.take(32);
+    if (!q) return false;
+    std::memcpy(g.b, q, 32);
+  }
+  return true;
+}
+}  // namespace
+
+int bf_bb_verify(const bf_bb_pcs* p, const uint8_t root[32], const uint8_t* point, const uint8_t* values,
+                 size_t width, int n_evals, bf_challenger* ch, const uint8_t* proof, size_t proof_len) {
+  if (!p || !root || !ch || (!proof && proof_len)) return fail(BF_ERR_ARG, "null argument");
+  if (n_evals < 0 || n_evals > 1) return fail(BF_ERR_ARG, "n_evals %d: one point or none", n_evals);
+  if (n_evals == 0) return BF_VERIFY_OK;  // basefold.rs:241-243
+  if (!values || (p->d > 0 && !point)) return fail(BF_ERR_ARG, "null argument");
+  if (width == 0) return fail(BF_ERR_ARG, "width 0");
+  const int d = p->d;
+  std::vector<E> r, vals;
+  TRY(load_points(point, (size_t)d, r, "point coordinate"));
+  TRY(load_points(values, width, vals, "value"));
+  bfh::Challenger& tr = ch->c;
+  std::vector<E> scalars = {E::one()};
+  E claim = vals[0];
+  if (width > 1) {  // basefold.rs:253-259
+    scalars = bbh::scalars_by_eq(width, tr);
+    claim = E();
+    for (size_t c = 0; c < width; ++c) claim = bbh::eadd(claim, bbh::emul(scalars[c], vals[c]));
+  }
+  Reader rd{proof, proof_len};
+  if (rd.u64() != (uint64_t)d || !rd.ok) return BF_VERIFY_MALFORMED;
+  std::vector<std::array<E, 2>> comp((size_t)d);
+  for (auto& c : comp) {
+    if (rd.u64() != 2 || !rd.e(c[0]) || !rd.e(c[1])) return BF_VERIFY_MALFORMED;
+  }
+  E fin;
+  if (rd.u64() != 1 || !rd.e(fin)) return BF_VERIFY_MALFORMED;
+  if (rd.u64() != (uint64_t)d || !rd.ok) return BF_VERIFY_MALFORMED;
+  std::vector<Dg> pi_comms((size_t)d);
+  for (Dg& g : pi_comms) {
+    const uint8_t* q = rd.take(32);
+    if (!q) return BF_VERIFY_MALFORMED;
+    std::memcpy(g.b, q, 32);
+  }
+  // verify_interleaved_folding_sumcheck (basefold.rs:371-396)
+  bbh::Subclaim sc;
+  sc.value = claim;
+  for (int k = 0; k < d; ++k) {
+    tr.observe(pi_comms[k].b, 32);
+    bbh::observe_e(tr, comp[k][0]);
+    bbh::observe_e(tr, comp[k][1]);
+    // Eval::decompress_round_poly: c1 = claim - 2 c0 - c2
+    const E c1 = bbh::esub(bbh::esub(sc.value, bbh::eadd(comp[k][0], comp[k][0])), comp[k][1]);
+    const E x = bbh::sample_e(tr);
+    const E rp[3] = {comp[k][0], c1, comp[k][1]};
+    sc.reduce(rp, 3, x);
+  }
+  bbh::observe_e(tr, fin);
+  const std::vector<E> rr = sc.r();
+  // log2_k_0 = 0: evaluate(final_poly, []) = final_poly[0]
+  if (bbh::emul(fin, bbh::eq_eval(r.data(), rr.data(), r.size() < rr.size() ? r.size() : rr.size())) != sc.value)
+    return BF_VERIFY_INVALID_FINAL_POLY;
+  const size_t Q = p->Q;
+  std::vector<uint64_t> idx(Q);
+  for (uint64_t& v : idx) v = tr.sample_bits(p->L);
+  if (rd.u64() != (uint64_t)Q || !rd.ok) return BF_VERIFY_MALFORMED;
+  std::vector<uint32_t> row(width);
+  std::vector<Dg> path;
+  for (size_t qi = 0; qi < Q; ++qi) {
+    const uint64_t q = idx[qi];
+    if (rd.u64() != (uint64_t)width) return BF_VERIFY_MALFORMED;
+    const uint8_t* vp = rd.take(4 * width);
+    if (!vp) return BF_VERIFY_MALFORMED;
+    std::memcpy(row.data(), vp, 4 * width);
+    for (uint32_t v : row)
+      if (v >= bbh::P) return BF_VERIFY_MALFORMED;
+    if (!read_path(rd, path)) return BF_VERIFY_MALFORMED;
+    if (!verify_path(root, leaf_row(row.data(), width), q, path, p->n_d())) return BF_VERIFY_MMCS;
+    E folded;
+    for (size_t c = 0; c < width; ++c) folded = bbh::eadd(folded, bbh::escale(scalars[c], row[c]));
+    if (rd.u64() != (uint64_t)d) return BF_VERIFY_MALFORMED;
+    for (int k = 0; k < d; ++k) {
+      const int i = d - 1 - k;
+      const size_t ni = p->n_i(i);
+      const size_t sib = ((q / ni) & 1) ^ 1, j = q % ni;
+      E other;
+      if (!rd.e(other)) return BF_VERIFY_MALFORMED;
+      if (!read_path(rd, path)) return BF_VERIFY_MALFORMED;
+      E v[2] = {folded, folded};
+      v[sib] = other;
+      if (!verify_path(pi_comms[k].b, leaf_pair(v[0], v[1]), j, path, ni)) return BF_VERIFY_MMCS;
+      // interpolate (code.rs:79-84) with t = (2 t_i^j)^-1 and round i's challenge r[i]
+      const uint32_t tj = bbh::fpow(bbh::two_adic_generator(p->log2_c + i + 1), j);
+      const uint32_t t = bbh::finv(bbh::fadd(tj, tj));
+      const E l = bbh::escale(bbh::eadd(v[0], v[1]), (bbh::P + 1) / 2);
+      const E hh = bbh::escale(bbh::esub(v[0], v[1]), t);
+      folded = bbh::eadd(l, bbh::emul(bbh::esub(hh, l), rr[i]));
+    }
+    if (folded != fin) return BF_VERIFY_INVALID_QUERY;  // encode0(final)[q % n_0] = final
+  }
+  return rd.off == proof_len ? BF_VERIFY_OK : BF_VERIFY_MALFORMED;
+}
+
+int bf_challenger_sample_bb_ext(bf_challenger* ch, uint8_t out[20]) {
+  if (!ch || !out) return fail(BF_ERR_ARG, "null argument");
+  bbh::store(out, bbh::sample_e(ch->c));
+  return BF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,83 @@
+// Internal interface between the prime-field host code (api_bb.cu) and its
+// kernels (kernels_bb.cu).  Not part of the public C ABI.
+//
+// Arrays: evaluations as the caller gave them (canonical BabyBears,
+// row-major, `w` per row); the codeword in Montgomery form, same layout,
+// natural (DFT output) order; extension arrays as five Montgomery words per
+// element.  Merkle trees use the reversed level storage of the binary path
+// (leaf j of a 2^h-leaf tree at bitrev_h(j)), so launch_tree builds them.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+#include "bb.cuh"
+
+namespace bf {
+
+constexpr int kBbMaxRounds = 27;  // num_vars + log2_c <= 27 (the two-adicity of BabyBear)
+
+// g^k * scale for k < n (Montgomery in, Montgomery out).
+cudaError_t bb_launch_pow_table(uint32_t* out, size_t n, uint32_t g_mont, uint32_t scale_mont, cudaStream_t st);
+// encode_batch of a 2^d x w matrix into its 2^(d+log2_c) x w codeword
+// (Montgomery).  `tw` holds the DIT twiddles, tw[2^s - 1 + k] = g_s^k.  A
+// data word >= p sets *bad.
+cudaError_t bb_launch_encode(const uint32_t* m, uint32_t* cw, int d, int log2_c, size_t w, const uint32_t* tw,
+                             uint32_t* bad, cudaStream_t st);
+// Leaf of codeword row q (keccak256 of its w canonical words) at bitrev_bits(q).
+cudaError_t bb_launch_leaves_rows(const uint32_t* cw, uint4* leaves, size_t rows, size_t w, int bits,
+                                  cudaStream_t st);
+// Leaf j = keccak256(pi[j] || pi[j + half]) as extension elements (pi is
+// base-field Montgomery when `base`), at bitrev_bits(j).
+cudaError_t bb_launch_leaves_pairs(const uint32_t* pi, int base, uint4* leaves, size_t half, int bits,
+                                   cudaStream_t st);
+// out[r] = sum_c scalars[c] * src[r w + c] (extension out); `canonical`:
+// src holds canonical words (the evaluations), else Montgomery (the codeword).
+cudaError_t bb_launch_combine(const uint32_t* src, int canonical, size_t rows, size_t w, const uint32_t* scalars,
+                              uint32_t* out, cudaStream_t st);
+// acc[5 c + k] += coefficient k of sum_r eq[r] * data[r w + c] (canonical data,
+// Montgomery sums, reduced by the caller).
+cudaError_t bb_launch_eval_cols(const uint32_t* eq, const uint32_t* data, size_t rows, size_t w,
+                                unsigned long long* acc, cudaStream_t st);
+// ev[h + k] = ev[k] x; ev[k] -= ev[h + k] for k < h.
+cudaError_t bb_launch_eq_expand(uint32_t* ev, size_t h, const bb::E5& x, cudaStream_t st);
+// acc[k] += coefficient k of sum_{b < n} heq[b] * poly[b]; poly is canonical
+// base-field data when `base`, else extension.
+cudaError_t bb_launch_dot(const uint32_t* heq, const uint32_t* poly, int base, size_t n, unsigned long long* acc,
+                          cudaStream_t st);
+// out[b] = in[b] + x (in[b + half] - in[b]); `base`: in is canonical data.
+cudaError_t bb_launch_fix(const uint32_t* in, int base, uint32_t* out, size_t half, const bb::E5& x,
+                          cudaStream_t st);
+
+// Fold of round i (code.rs:66-84): out[j] = interpolate(tinv[j], w[j],
+// w[j + n], x), j < n = n_i, with the next round's leaves when `leaves` is set.
+struct BbFold {
+  const uint32_t* w;  // 2n entries: extension, or base-field Montgomery when `base`
+  int base;
+  uint32_t* out;          // n extension entries
+  const uint32_t* tinv;   // n entries (2 t_i^j)^-1, Montgomery
+  size_t n;
+  uint4* leaves;          // n/2 leaves of the next round, or null
+  int leaf_bits;          // log2(n/2)
+};
+cudaError_t bb_launch_fold(const BbFold& p, const bb::E5& x, cudaStream_t st);
+
+// Query openings in the proof's bincode layout, one record per query:
+// u64 w, w canonical words, u64 L, L digests, u64 d, then per round k:
+// the sibling (five canonical words), u64 log2 n_i, the path.
+struct BbGather {
+  const uint32_t* cw;      // codeword (Montgomery), rows of w
+  const uint4* cw_tree;
+  const uint32_t* pi[kBbMaxRounds];  // the matrix committed in round k (extension; base codeword when k = 0 and pi0_base)
+  const uint4* trees[kBbMaxRounds];
+  int pi0_base;
+  const uint64_t* idx;
+  uint8_t* out;
+  size_t w;
+  size_t rec_bytes;
+  int L, d, log2_c, nq;
+};
+cudaError_t bb_launch_gather(const BbGather& p, cudaStream_t st);
+
+}  // namespace bf

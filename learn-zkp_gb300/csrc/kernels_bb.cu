@@ -1,0 +1,578 @@
+// CUDA kernels of Basefold over BabyBear with the multiplicative Reed–Solomon
+// code (poly-commit/src/basefold/code/reed_solomon.rs) and the extension
+// E = BinomialExtensionField<BabyBear, 5> for the open (sm_103a).
+//
+// The codeword is in natural order (the order Radix2DitParallel::dft_batch
+// returns), so the folding pair of round i is (j, j + n_i) (code.rs:66-75)
+// and the rows of every folded-codeword matrix are (pi[j], pi[j + half])
+// (basefold.rs:350-355).  All of these kernels are memory- or hash-bound
+// integer work: Montgomery products on the integer multiplier, Keccak on the
+// ALU; nothing here is GEMM-shaped.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "bb.cuh"
+#include "bb_internal.h"
+#include "bf_internal.h"
+#include "keccak.cuh"
+
+namespace bf {
+
+using bb::E5;
+
+namespace {
+
+__device__ __forceinline__ uint32_t brev_bits(uint64_t x, int bits) {
+  return bits ? (uint32_t)(__brevll(x) >> (64 - bits)) : 0u;
+}
+
+__device__ __forceinline__ uint32_t mont_pow(uint32_t g, uint64_t e) {
+  uint32_t r = bb::MONT_ONE;
+  while (e) {
+    if (e & 1) r = bb::mul(r, g);
+    g = bb::mul(g, g);
+    e >>= 1;
+  }
+  return r;
+}
+
+__device__ __forceinline__ E5 ld_e5(const uint32_t* p, size_t i) {
+  E5 e;
+#pragma unroll
+  for (int k = 0; k < 5; ++k) e.c[k] = p[5 * i + k];
+  return e;
+}
+__device__ __forceinline__ void st_e5(uint32_t* p, size_t i, const E5& e) {
+#pragma unroll
+  for (int k = 0; k < 5; ++k) p[5 * i + k] = e.c[k];
+}
+
+// keccak256 of one canonical BabyBear (4 bytes): lane 0 holds the value and
+// the 0x01 padding byte, lane 16 the final 0x80 (interleaved lanes, as the
+// trees store them).
+__device__ __forceinline__ Digest hash_base(uint32_t canonical) {
+  uint2 s[25];
+#pragma unroll
+  for (int i = 0; i < 25; ++i) s[i] = make_uint2(0, 0);
+  s[0] = bi_from_lane(make_uint2(canonical, 0x01u));
+  s[16].y ^= 0x80000000u;
+  keccak_f1600_digest<true>(s);
+  return digest_from_state(s);
+}
+
+// keccak256 of two extension elements, ten canonical BabyBears (40 bytes):
+// a row of the folded-codeword matrix as ExtensionMmcs flattens it.
+__device__ __forceinline__ Digest hash_pair_e5(const E5& a, const E5& b) {
+  uint32_t w[10];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    w[k] = bb::from_mont(a.c[k]);
+    w[5 + k] = bb::from_mont(b.c[k]);
+  }
+  uint2 s[25];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) s[k] = bi_from_lane(make_uint2(w[2 * k], w[2 * k + 1]));
+  keccak256_lanes<true>(s, 5);
+  return digest_from_state(s);
+}
+
+__device__ __forceinline__ unsigned long long shfl_xor64(unsigned long long v, int o) {
+  return __shfl_xor_sync(0xffffffffu, v, o);
+}
+
+// Five Montgomery coefficient sums of a warp reduced into every lane.
+__device__ __forceinline__ void warp_sum5(unsigned long long s[5]) {
+#pragma unroll
+  for (int k = 0; k < 5; ++k)
+    for (int o = 16; o > 0; o >>= 1) s[k] += shfl_xor64(s[k], o);
+}
+
+__device__ __forceinline__ uint32_t mod_p(unsigned long long v) { return (uint32_t)(v % bb::P); }
+
+}  // namespace
+
+// ---- setup -------------------------------------------------------------------
+__global__ void bb_pow_table_kernel(uint32_t* out, size_t n, uint32_t g, uint32_t scale) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+    out[k] = bb::mul(scale, mont_pow(g, k));
+}
+
+// Single-row codeword (num_vars = log2_c = 0): the data in Montgomery form.
+__global__ void bb_copy_mont_kernel(const uint32_t* in, uint32_t* out, size_t n, uint32_t* bad) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t v = in[k];
+    if (v >= bb::P) atomicOr(bad, 1u);
+    out[k] = bb::to_mont(v);
+  }
+}
+
+// ---- encode: radix-2 DIT of the bit-reversed, zero-padded columns -------------
+// encode_batch (reed_solomon.rs:71-75) = dft_batch(pad(bit_reverse_rows(m))).
+// A DIT with natural-order output takes its input in bit-reversed order,
+// where row x holds input row bitrev_L(x): data row x >> log2_c when the low
+// log2_c bits of x are zero, else zero.  So the first pass reads the data
+// rows spread out and no permutation pass is needed.
+//
+// One launch runs layers [s_lo, s_lo + T) (half-sizes 2^s) on tiles of 2^T
+// rows x = (hi << (s_lo + T)) | (a << s_lo) | u, a < 2^T.  A block holds
+// U = 2^lu consecutive u and C = 2^lc consecutive columns of each of those
+// rows (column fastest, then u, then a), so that a warp's loads and stores
+// cover runs of C U words.  The butterfly at half-size 2^s pairs rows that
+// differ in bit s and multiplies by g_s^(x mod 2^s), g_s of order 2^(s+1).
+struct BbPass {
+  int s_lo, T, first, log2_c, lu, lc;
+  uint32_t w;
+};
+
+__global__ void __launch_bounds__(256) bb_dft_pass_kernel(const uint32_t* __restrict__ m, uint32_t* cw, BbPass p,
+                                                         const uint32_t* __restrict__ tw, uint32_t* bad) {
+  extern __shared__ uint32_t tile[];
+  const int s_lo = p.s_lo, T = p.T, lu = p.lu, lc = p.lc, ic = lu + lc;
+  const uint32_t nub_log = (uint32_t)(s_lo - lu);
+  const uint32_t u_blk = blockIdx.x & ((1u << nub_log) - 1u);
+  const uint64_t hi = blockIdx.x >> nub_log;
+  const uint32_t c0 = blockIdx.y << lc;
+  const uint32_t w = p.w;
+  const uint32_t tsize = 1u << (T + ic);
+  const uint64_t cmask = (1ull << p.log2_c) - 1ull;
+  for (uint32_t e = threadIdx.x; e < tsize; e += blockDim.x) {
+    const uint32_t col = e & ((1u << lc) - 1u), uu = (e >> lc) & ((1u << lu) - 1u), a = e >> ic;
+    const uint64_t x = (hi << (s_lo + T)) | ((uint64_t)a << s_lo) | ((u_blk << lu) | uu);
+    const uint32_t c = c0 + col;
+    uint32_t v = 0;
+    if (c < w) {
+      if (p.first) {
+        if ((x & cmask) == 0) {
+          v = m[(x >> p.log2_c) * w + c];
+          if (v >= bb::P) atomicOr(bad, 1u);
+          v = bb::to_mont(v);
+        }
+      } else {
+        v = cw[x * w + c];
+      }
+    }
+    tile[e] = v;
+  }
+  __syncthreads();
+  for (int l = 0; l < T; ++l) {
+    const int s = s_lo + l;
+    const uint32_t* __restrict__ tws = tw + ((size_t)1 << s) - 1;
+    const uint32_t lmask = (1u << l) - 1u;
+    for (uint32_t e = threadIdx.x; e < (tsize >> 1); e += blockDim.x) {
+      const uint32_t cu = e & ((1u << ic) - 1u), bi = e >> ic;
+      const uint32_t a0 = ((bi >> l) << (l + 1)) | (bi & lmask);
+      const uint32_t u = (u_blk << lu) | (cu >> lc);
+      const uint32_t k = ((a0 & lmask) << s_lo) | u;
+      const uint32_t i0 = (a0 << ic) | cu, i1 = i0 | (1u << (l + ic));
+      const uint32_t v = bb::mul(tile[i1], tws[k]), x0 = tile[i0];
+      tile[i0] = bb::add(x0, v);
+      tile[i1] = bb::sub(x0, v);
+    }
+    __syncthreads();
+  }
+  for (uint32_t e = threadIdx.x; e < tsize; e += blockDim.x) {
+    const uint32_t col = e & ((1u << lc) - 1u), uu = (e >> lc) & ((1u << lu) - 1u), a = e >> ic;
+    const uint64_t x = (hi << (s_lo + T)) | ((uint64_t)a << s_lo) | ((u_blk << lu) | uu);
+    const uint32_t c = c0 + col;
+    if (c < w) cw[x * w + c] = tile[e];
+  }
+}
+
+// ---- leaves ------------------------------------------------------------------
+// Width 1: the row is one BabyBear.
+__global__ void __launch_bounds__(128) bb_leaves_one_kernel(const uint32_t* __restrict__ cw, uint4* __restrict__ leaves,
+                                                           size_t rows, int bits) {
+  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < rows; q += (size_t)gridDim.x * blockDim.x)
+    store_digest(leaves, brev_bits(q, bits), hash_base(bb::from_mont(cw[q])));
+}
+
+// Any width: keccak256 of the row's 4w bytes (GenericHasher over the row's
+// bincode, p3/src/symmetric.rs:11-25), one lane per row.  The 136-byte rate
+// is 34 words, so the blocks of every row start on a word: a warp stages the
+// current block of its 32 rows in shared memory with coalesced loads (the
+// 0x01 padding word right after the message, 0x80 in the block's last byte),
+// then each lane absorbs its row.
+constexpr int kRateWords = 34;
+constexpr int kStagePitch = 35;  // odd pitch: lane r reads word r * 35 + i without bank conflicts
+__global__ void __launch_bounds__(128) bb_leaves_rows_kernel(const uint32_t* __restrict__ cw,
+                                                            uint4* __restrict__ leaves, size_t rows, uint32_t w,
+                                                            int bits) {
+  __shared__ uint32_t stage[4][32 * kStagePitch];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  uint32_t* st = stage[warp];
+  const uint32_t nblk = w / kRateWords + 1;
+  for (size_t r0 = ((size_t)blockIdx.x * 4 + warp) * 32; r0 < rows; r0 += (size_t)gridDim.x * 128) {
+    uint2 s[25];
+#pragma unroll
+    for (int i = 0; i < 25; ++i) s[i] = make_uint2(0, 0);
+    for (uint32_t blk = 0; blk < nblk; ++blk) {
+      for (int e = lane; e < 32 * kRateWords; e += 32) {
+        const int rr = e / kRateWords, i = e - rr * kRateWords;
+        const uint32_t col = blk * kRateWords + i;
+        uint32_t v = 0;
+        if (col < w) {
+          if (r0 + rr < rows) v = bb::from_mont(cw[(r0 + rr) * w + col]);
+        } else if (col == w) {
+          v = 0x01u;
+        }
+        if (blk == nblk - 1 && i == kRateWords - 1) v |= 0x80000000u;
+        st[rr * kStagePitch + i] = v;
+      }
+      __syncwarp();
+#pragma unroll
+      for (int k = 0; k < 17; ++k) {
+        const uint2 l = bi_from_lane(make_uint2(st[lane * kStagePitch + 2 * k], st[lane * kStagePitch + 2 * k + 1]));
+        s[k].x ^= l.x;
+        s[k].y ^= l.y;
+      }
+      __syncwarp();
+      keccak_f1600<true>(s);
+    }
+    if (r0 + lane < rows) store_digest(leaves, brev_bits(r0 + lane, bits), digest_from_state(s));
+  }
+}
+
+// Folded-codeword leaf j = keccak256(pi[j] || pi[j + half]) at bitrev(j);
+// the first round's pi of a width-1 commitment is the codeword itself, lifted
+// with E::from (basefold.rs:150-155).
+__global__ void __launch_bounds__(128) bb_leaves_pairs_kernel(const uint32_t* __restrict__ pi, int base,
+                                                             uint4* __restrict__ leaves, size_t half, int bits) {
+  for (size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < half; j += (size_t)gridDim.x * blockDim.x) {
+    const E5 a = base ? bb::e_from(pi[j]) : ld_e5(pi, j);
+    const E5 b = base ? bb::e_from(pi[j + half]) : ld_e5(pi, j + half);
+    store_digest(leaves, brev_bits(j, bits), hash_pair_e5(a, b));
+  }
+}
+
+// ---- rows combined with the batching scalars (basefold.rs:160-176) ------------
+// One warp per row, lanes over the columns; Montgomery form is linear, so the
+// integer sums of the products, reduced mod p, are the Montgomery form of the
+// dot product.
+__global__ void __launch_bounds__(256) bb_combine_kernel(const uint32_t* __restrict__ src, int canonical, size_t rows,
+                                                        uint32_t w, const uint32_t* __restrict__ scalars,
+                                                        uint32_t* __restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const size_t warps = (size_t)gridDim.x * (blockDim.x >> 5);
+  for (size_t r = (size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < rows; r += warps) {
+    unsigned long long s[5] = {0, 0, 0, 0, 0};
+    for (uint32_t c = lane; c < w; c += 32) {
+      uint32_t v = src[r * w + c];
+      if (canonical) v = bb::to_mont(v);
+#pragma unroll
+      for (int k = 0; k < 5; ++k) s[k] += bb::mul(scalars[5 * c + k], v);
+    }
+    warp_sum5(s);
+    if (lane == 0) {
+      E5 e;
+#pragma unroll
+      for (int k = 0; k < 5; ++k) e.c[k] = mod_p(s[k]);
+      st_e5(out, r, e);
+    }
+  }
+}
+
+// ---- column evaluations (basefold.rs:126-131) ---------------------------------
+// Lane = column (32 per blockIdx.y), warps and blocks over the rows.
+__global__ void __launch_bounds__(256) bb_eval_cols_kernel(const uint32_t* __restrict__ eq,
+                                                          const uint32_t* __restrict__ data, size_t rows, uint32_t w,
+                                                          unsigned long long* acc) {
+  __shared__ unsigned long long part[8][5][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t c = blockIdx.y * 32 + lane;
+  unsigned long long s[5] = {0, 0, 0, 0, 0};
+  if (c < w) {
+    for (size_t r = (size_t)blockIdx.x * 8 + warp; r < rows; r += (size_t)gridDim.x * 8) {
+      const uint32_t v = bb::to_mont(data[r * w + c]);
+#pragma unroll
+      for (int k = 0; k < 5; ++k) s[k] += bb::mul(eq[5 * r + k], v);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 5; ++k) part[warp][k][lane] = s[k];
+  __syncthreads();
+  if (warp == 0 && c < w) {
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      unsigned long long v = 0;
+      for (int q = 0; q < 8; ++q) v += part[q][k][lane];
+      if (v) atomicAdd(acc + 5 * (size_t)c + k, v);
+    }
+  }
+}
+
+// ---- multilinear evaluation and the sumcheck side -----------------------------
+// eq_expand (p3/src/poly/multilinear.rs:216-222): hi = lo x; lo -= hi.
+__global__ void bb_eq_expand_kernel(uint32_t* ev, size_t h, E5 x) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < h; k += (size_t)gridDim.x * blockDim.x) {
+    const E5 lo = ld_e5(ev, k);
+    const E5 hv = bb::e_mul(lo, x);
+    st_e5(ev, h + k, hv);
+    st_e5(ev, k, bb::e_sub(lo, hv));
+  }
+}
+
+// sum_b heq[b] poly[b] (EvalImprProver::compute_round_poly, eval_impr.rs:
+// 187-197) as five Montgomery coefficient sums.
+__global__ void __launch_bounds__(256) bb_dot_kernel(const uint32_t* __restrict__ heq, const uint32_t* __restrict__ poly,
+                                                    int base, size_t n, unsigned long long* acc) {
+  unsigned long long s[5] = {0, 0, 0, 0, 0};
+  for (size_t b = (size_t)blockIdx.x * blockDim.x + threadIdx.x; b < n; b += (size_t)gridDim.x * blockDim.x) {
+    const E5 h = ld_e5(heq, b);
+    const E5 t = base ? bb::e_scale(h, bb::to_mont(poly[b])) : bb::e_mul(h, ld_e5(poly, b));
+#pragma unroll
+    for (int k = 0; k < 5; ++k) s[k] += t.c[k];
+  }
+  __shared__ unsigned long long part[5][8];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  warp_sum5(s);
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < 5; ++k) part[k][warp] = s[k];
+  }
+  __syncthreads();
+  if (threadIdx.x < 5) {
+    unsigned long long v = 0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) v += part[threadIdx.x][q];
+    if (v) atomicAdd(acc + threadIdx.x, v);
+  }
+}
+
+// fix_last_var (multilinear.rs:183-198): out[b] = lo + x (hi - lo).
+__global__ void bb_fix_kernel(const uint32_t* in, int base, uint32_t* out, size_t half, E5 x) {
+  for (size_t b = (size_t)blockIdx.x * blockDim.x + threadIdx.x; b < half; b += (size_t)gridDim.x * blockDim.x) {
+    if (base) {
+      const uint32_t lo = bb::to_mont(in[b]), d = bb::sub(bb::to_mont(in[b + half]), lo);
+      E5 r = bb::e_scale(x, d);
+      r.c[0] = bb::add(r.c[0], lo);
+      st_e5(out, b, r);
+    } else {
+      const E5 lo = ld_e5(in, b), hi = ld_e5(in, b + half);
+      st_e5(out, b, bb::e_add(lo, bb::e_mul(x, bb::e_sub(hi, lo))));
+    }
+  }
+}
+
+// ---- fold (code.rs:66-84) with the next round's leaves ------------------------
+// interpolate(t, lo, hi, r) = l + (h - l) r with l = (lo + hi) / 2 and
+// h = (lo - hi) t, t = (2 t_i^j)^-1.  Thread s < n/2 makes out[s] and
+// out[s + n/2], the row s of the next round's matrix, and hashes it.
+__device__ __forceinline__ E5 bb_interp(const E5& lo, const E5& hi, uint32_t t, const E5& x) {
+  const E5 l = bb::e_scale(bb::e_add(lo, hi), bb::MONT_INV2);
+  const E5 h = bb::e_scale(bb::e_sub(lo, hi), t);
+  return bb::e_add(l, bb::e_mul(bb::e_sub(h, l), x));
+}
+__global__ void __launch_bounds__(128) bb_fold_kernel(BbFold p, E5 x) {
+  const size_t n = p.n, q = n >> 1;
+  const size_t work = q ? q : 1;  // n = 1: the single output, no leaves
+  for (size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x; s < work; s += (size_t)gridDim.x * blockDim.x) {
+    E5 f[2];
+    const int outs = q ? 2 : 1;
+    for (int k = 0; k < outs; ++k) {
+      const size_t j = s + k * q;
+      const E5 lo = p.base ? bb::e_from(p.w[j]) : ld_e5(p.w, j);
+      const E5 hi = p.base ? bb::e_from(p.w[j + n]) : ld_e5(p.w, j + n);
+      f[k] = bb_interp(lo, hi, p.tinv[j], x);
+      st_e5(p.out, j, f[k]);
+    }
+    if (p.leaves && q) store_digest(p.leaves, brev_bits(s, p.leaf_bits), hash_pair_e5(f[0], f[1]));
+  }
+}
+
+// ---- query openings (basefold.rs:200-222) ---------------------------------------
+// One block per query; every field of the record sits on a 4-byte boundary.
+__device__ __forceinline__ void put64w(uint32_t* o, size_t wo, uint64_t v) {
+  o[wo] = (uint32_t)v;
+  o[wo + 1] = (uint32_t)(v >> 32);
+}
+__device__ __forceinline__ void put_digest_words(uint32_t* o, size_t wo, const uint4* tree, size_t i) {
+  const Digest dg = digest_bytes(load_digest(tree, i));
+  o[wo + 0] = dg.lo.x;
+  o[wo + 1] = dg.lo.y;
+  o[wo + 2] = dg.lo.z;
+  o[wo + 3] = dg.lo.w;
+  o[wo + 4] = dg.hi.x;
+  o[wo + 5] = dg.hi.y;
+  o[wo + 6] = dg.hi.z;
+  o[wo + 7] = dg.hi.w;
+}
+__global__ void bb_gather_kernel(BbGather p) {
+  const int t = blockIdx.x;
+  const uint64_t idx = p.idx[t];
+  uint32_t* o = reinterpret_cast<uint32_t*>(p.out + (size_t)t * p.rec_bytes);
+  const int L = p.L, d = p.d;
+  const size_t w = p.w;
+  if (threadIdx.x == 0) {
+    put64w(o, 0, w);
+    put64w(o, 2 + w, (uint64_t)L);
+  }
+  for (size_t c = threadIdx.x; c < w; c += blockDim.x) o[2 + c] = bb::from_mont(p.cw[idx * w + c]);
+  size_t wo = 4 + w;
+  for (int k = threadIdx.x; k < L; k += blockDim.x) {
+    const uint64_t m = (idx >> k) ^ 1ull;
+    const size_t off = ((size_t)2 << L) - ((size_t)2 << (L - k));
+    put_digest_words(o, wo + 8 * (size_t)k, p.cw_tree, off + brev_bits(m, L - k));
+  }
+  wo += 8 * (size_t)L;
+  if (threadIdx.x == 0) put64w(o, wo, (uint64_t)d);
+  wo += 2;
+  for (int k = 0; k < d; ++k) {
+    const int i = d - 1 - k;
+    const int li = p.log2_c + i;  // the round's tree has n_i = 2^li leaves
+    const uint64_t ni = (uint64_t)1 << li;
+    const uint64_t j = idx & (ni - 1), sib = ((idx >> li) & 1) ^ 1;
+    if (threadIdx.x == 0) {
+      const size_t e = j + sib * ni;
+      if (k == 0 && p.pi0_base) {
+        o[wo] = bb::from_mont(p.pi[0][e]);
+        o[wo + 1] = o[wo + 2] = o[wo + 3] = o[wo + 4] = 0;
+      } else {
+#pragma unroll
+        for (int c = 0; c < 5; ++c) o[wo + c] = bb::from_mont(p.pi[k][5 * e + c]);
+      }
+      put64w(o, wo + 5, (uint64_t)li);
+    }
+    wo += 7;
+    const uint4* tree = p.trees[k];
+    for (int kk = threadIdx.x; kk < li; kk += blockDim.x) {
+      const uint64_t m = (j >> kk) ^ 1ull;
+      const size_t loff = ((size_t)2 << li) - ((size_t)2 << (li - kk));
+      put_digest_words(o, wo + 8 * (size_t)kk, tree, loff + brev_bits(m, li - kk));
+    }
+    wo += 8 * (size_t)li;
+  }
+}
+
+// ---- launchers -----------------------------------------------------------------
+static unsigned blocks_for(size_t n, int threads) {
+  size_t b = (n + threads - 1) / threads;
+  if (b > 152u * 64) b = 152u * 64;  // grid-stride beyond 64 blocks per SM
+  return b ? (unsigned)b : 1u;
+}
+
+cudaError_t bb_launch_pow_table(uint32_t* out, size_t n, uint32_t g_mont, uint32_t scale_mont, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  bb_pow_table_kernel<<<blocks_for(n, 256), 256, 0, st>>>(out, n, g_mont, scale_mont);
+  count_launch();
+  return cudaGetLastError();
+}
+
+static int ilog2_ceil(size_t v) {
+  int r = 0;
+  while (((size_t)1 << r) < v) ++r;
+  return r;
+}
+
+cudaError_t bb_launch_encode(const uint32_t* m, uint32_t* cw, int d, int log2_c, size_t w, const uint32_t* tw,
+                             uint32_t* bad, cudaStream_t st) {
+  const int L = d + log2_c;
+  if (L == 0) {
+    bb_copy_mont_kernel<<<blocks_for(w, 256), 256, 0, st>>>(m, cw, w, bad);
+    count_launch();
+    return cudaGetLastError();
+  }
+  const int lc = ilog2_ceil(w < 32 ? w : 32);
+  const unsigned chunks = (unsigned)((w + ((size_t)1 << lc) - 1) >> lc);
+  int lo = 0;
+  while (lo < L) {
+    int lu = 0;
+    if (lo > 0)
+      while (lu < lo && lc + lu < 5) ++lu;  // U C <= 32 consecutive words per row run
+    int T = 13 - lc - lu;                   // tile of 2^(T + lu + lc) <= 8192 words
+    if (T > 12) T = 12;
+    if (T > L - lo) T = L - lo;
+    BbPass p;
+    p.s_lo = lo;
+    p.T = T;
+    p.first = lo == 0;
+    p.log2_c = log2_c;
+    p.lu = lu;
+    p.lc = lc;
+    p.w = (uint32_t)w;
+    const size_t words = (size_t)1 << (T + lu + lc);
+    int threads = (int)(words / 2);
+    if (threads > 256) threads = 256;
+    if (threads < 32) threads = 32;
+    const dim3 grid((unsigned)((size_t)1 << (L - T - lu)), chunks);
+    bb_dft_pass_kernel<<<grid, threads, words * sizeof(uint32_t), st>>>(m, cw, p, tw, bad);
+    count_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    lo += T;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t bb_launch_leaves_rows(const uint32_t* cw, uint4* leaves, size_t rows, size_t w, int bits,
+                                  cudaStream_t st) {
+  if (w == 1)
+    bb_leaves_one_kernel<<<blocks_for(rows, 128), 128, 0, st>>>(cw, leaves, rows, bits);
+  else
+    bb_leaves_rows_kernel<<<blocks_for(rows, 128), 128, 0, st>>>(cw, leaves, rows, (uint32_t)w, bits);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t bb_launch_leaves_pairs(const uint32_t* pi, int base, uint4* leaves, size_t half, int bits,
+                                   cudaStream_t st) {
+  bb_leaves_pairs_kernel<<<blocks_for(half, 128), 128, 0, st>>>(pi, base, leaves, half, bits);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t bb_launch_combine(const uint32_t* src, int canonical, size_t rows, size_t w, const uint32_t* scalars,
+                              uint32_t* out, cudaStream_t st) {
+  bb_combine_kernel<<<blocks_for(rows * 32, 256), 256, 0, st>>>(src, canonical, rows, (uint32_t)w, scalars, out);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t bb_launch_eval_cols(const uint32_t* eq, const uint32_t* data, size_t rows, size_t w,
+                                unsigned long long* acc, cudaStream_t st) {
+  size_t bx = (rows + 63) / 64;  // at least 8 rows per warp
+  const size_t by = (w + 31) / 32;
+  size_t cap = (152u * 8 + by - 1) / by;
+  if (cap < 1) cap = 1;
+  if (bx > cap) bx = cap;
+  if (bx < 1) bx = 1;
+  bb_eval_cols_kernel<<<dim3((unsigned)bx, (unsigned)by), 256, 0, st>>>(eq, data, rows, (uint32_t)w, acc);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t bb_launch_eq_expand(uint32_t* ev, size_t h, const E5& x, cudaStream_t st) {
+  bb_eq_expand_kernel<<<blocks_for(h, 256), 256, 0, st>>>(ev, h, x);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t bb_launch_dot(const uint32_t* heq, const uint32_t* poly, int base, size_t n, unsigned long long* acc,
+                          cudaStream_t st) {
+  size_t b = (n + 255) / 256;
+  if (b > 152 * 8) b = 152 * 8;
+  bb_dot_kernel<<<b ? (unsigned)b : 1u, 256, 0, st>>>(heq, poly, base, n, acc);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t bb_launch_fix(const uint32_t* in, int base, uint32_t* out, size_t half, const E5& x, cudaStream_t st) {
+  bb_fix_kernel<<<blocks_for(half, 256), 256, 0, st>>>(in, base, out, half, x);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t bb_launch_fold(const BbFold& p, const E5& x, cudaStream_t st) {
+  const size_t q = p.n / 2;
+  bb_fold_kernel<<<blocks_for(q ? q : 1, 128), 128, 0, st>>>(p, x);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t bb_launch_gather(const BbGather& p, cudaStream_t st) {
+  if (p.nq == 0) return cudaSuccess;
+  bb_gather_kernel<<<p.nq, 64, 0, st>>>(p);
+  count_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace bf

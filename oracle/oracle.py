@@ -59,12 +59,12 @@ def lib():
         L.orc_bb_dft.argtypes = [C.c_int, C.POINTER(C.c_uint32), C.c_int]
         L.orc_bb_num_queries.argtypes = [C.c_int, C.c_int]
         L.orc_bb_num_queries.restype = sz
-        L.orc_bb_encode.argtypes = [C.c_int, C.c_int, u8p, u8p]
-        L.orc_bb_commit.argtypes = [C.c_int, C.c_int, u8p, u8p]
-        L.orc_bb_eval.argtypes = [C.c_int, u8p, u8p, u8p]
-        L.orc_bb_harness_prepare.argtypes = [C.c_int, C.c_int, u8p, u8p, u8p, u8p, u8p, C.POINTER(sz)]
-        L.orc_bb_open.argtypes = [C.c_int, C.c_int, u8p, u8p, u8p, u8p, sz, u8p, sz, C.POINTER(sz)]
-        L.orc_bb_verify.argtypes = [C.c_int, C.c_int, u8p, u8p, u8p, u8p, sz, u8p, sz]
+        L.orc_bb_encode.argtypes = [C.c_int, C.c_int, sz, u8p, u8p]
+        L.orc_bb_commit.argtypes = [C.c_int, C.c_int, sz, u8p, u8p]
+        L.orc_bb_eval.argtypes = [C.c_int, sz, u8p, u8p, u8p]
+        L.orc_bb_harness_prepare.argtypes = [C.c_int, C.c_int, sz, u8p, u8p, u8p, u8p, u8p, C.POINTER(sz)]
+        L.orc_bb_open.argtypes = [C.c_int, C.c_int, sz, u8p, u8p, u8p, u8p, sz, u8p, sz, C.POINTER(sz)]
+        L.orc_bb_verify.argtypes = [C.c_int, C.c_int, sz, u8p, u8p, u8p, u8p, sz, u8p, sz]
         _lib = L
     return _lib
 
@@ -365,45 +365,60 @@ def bb_num_queries(log2_c: int, lam: int = 128) -> int:
     return int(lib().orc_bb_num_queries(lam, log2_c))
 
 
+def _mat(data, n: int):
+    """Row-major 2^n x width data (a 1-D array is width 1) and its width."""
+    d = _u32(data).reshape(-1)
+    assert d.size % (1 << n) == 0 and d.size > 0
+    return d, d.size >> n
+
+
+def _pt(point, n: int):
+    return _u32(point).reshape(-1, 5) if n else np.zeros((1, 5), np.uint32)
+
+
 def bb_encode(n: int, log2_c: int, data):
-    d = _u32(data)
-    out = np.zeros(1 << (n + log2_c), dtype=np.uint32)
-    assert lib().orc_bb_encode(n, log2_c, _pu(d), _pu(out)) == 0
-    return out
+    """Codeword of each column; returns 2^(n+log2_c) x width (1-D for width 1)."""
+    d, w = _mat(data, n)
+    out = np.zeros(w << (n + log2_c), dtype=np.uint32)
+    assert lib().orc_bb_encode(n, log2_c, w, _pu(d), _pu(out)) == 0
+    return out if w == 1 else out.reshape(-1, w)
 
 
 def bb_commit(n: int, log2_c: int, data) -> bytes:
-    d = _u32(data)
+    d, w = _mat(data, n)
     root = np.zeros(32, dtype=np.uint8)
-    assert lib().orc_bb_commit(n, log2_c, _pu(d), _p(root)) == 0
+    assert lib().orc_bb_commit(n, log2_c, w, _pu(d), _p(root)) == 0
     return root.tobytes()
 
 
 def bb_eval(n: int, data, point):
-    d, pt = _u32(data), _u32(point).reshape(-1, 5) if n else np.zeros((1, 5), np.uint32)
-    out = np.zeros(5, dtype=np.uint32)
-    assert lib().orc_bb_eval(n, _pu(d), _pu(pt), _pu(out)) == 0
-    return out
+    """Values of the columns at the point: shape (5,) for width 1, else (width, 5)."""
+    d, w = _mat(data, n)
+    out = np.zeros((w, 5), dtype=np.uint32)
+    assert lib().orc_bb_eval(n, w, _pu(d), _pu(_pt(point, n)), _pu(out)) == 0
+    return out[0] if w == 1 else out
 
 
 def bb_harness_prepare(n: int, log2_c: int, data, point):
-    d, pt = _u32(data), _u32(point).reshape(-1, 5) if n else np.zeros((1, 5), np.uint32)
+    d, w = _mat(data, n)
     root = np.zeros(32, dtype=np.uint8)
-    val = np.zeros(5, dtype=np.uint32)
-    blob = np.zeros(128, dtype=np.uint8)
+    val = np.zeros((w, 5), dtype=np.uint32)
+    blob = np.zeros(128 + 20 * w, dtype=np.uint8)
     bl = C.c_size_t(blob.size)
-    assert lib().orc_bb_harness_prepare(n, log2_c, _pu(d), _pu(pt), _p(root), _pu(val), _p(blob), C.byref(bl)) == 0
-    return root.tobytes(), val, blob[: bl.value].tobytes()
+    assert lib().orc_bb_harness_prepare(n, log2_c, w, _pu(d), _pu(_pt(point, n)), _p(root), _pu(val), _p(blob),
+                                        C.byref(bl)) == 0
+    return root.tobytes(), (val[0] if w == 1 else val), blob[: bl.value].tobytes()
 
 
 def bb_open(n: int, log2_c: int, data, point, value, blob: bytes) -> bytes:
-    d, pt = _u32(data), _u32(point).reshape(-1, 5) if n else np.zeros((1, 5), np.uint32)
-    v, b = _u32(value), _buf(blob)
+    d, w = _mat(data, n)
+    v, b = _u32(value).reshape(w, 5), _buf(blob)
     cap = 1 << 16
     while True:
         out = np.zeros(cap, dtype=np.uint8)
         ln = C.c_size_t(0)
-        rc = lib().orc_bb_open(n, log2_c, _pu(d), _pu(pt), _pu(v), _p(b), b.size, _p(out), cap, C.byref(ln))
+        rc = lib().orc_bb_open(n, log2_c, w, _pu(d), _pu(_pt(point, n)), _pu(v), _p(b), b.size, _p(out), cap,
+                               C.byref(ln))
         if rc == -2:
             cap = ln.value
             continue
@@ -412,7 +427,8 @@ def bb_open(n: int, log2_c: int, data, point, value, blob: bytes) -> bytes:
 
 
 def bb_verify(n: int, log2_c: int, root: bytes, point, value, blob: bytes, proof: bytes) -> int:
-    pt = _u32(point).reshape(-1, 5) if n else np.zeros((1, 5), np.uint32)
-    v, r, b, pf = _u32(value), _buf(root), _buf(blob), _buf(proof)
-    return lib().orc_bb_verify(n, log2_c, _p(r), _pu(pt), _pu(v), _p(b), b.size,
+    """0 accepted; 1 final poly, 2 query, 3 Merkle path, 4 malformed."""
+    v = _u32(value).reshape(-1, 5)
+    r, b, pf = _buf(root), _buf(blob), _buf(proof)
+    return lib().orc_bb_verify(n, log2_c, v.shape[0], _p(r), _pu(_pt(point, n)), _pu(v), _p(b), b.size,
                                _p(pf) if pf.size else _p(np.zeros(1, np.uint8)), pf.size)

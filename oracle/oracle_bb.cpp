@@ -379,9 +379,9 @@ static Tree build_tree(std::vector<Digest> leaves) {
   }
   return t;
 }
-static Digest leaf_f(uint32_t v) {
+static Digest leaf_row(const uint32_t* row, size_t w) {
   std::vector<uint8_t> b;
-  put_u32(b, v);
+  for (size_t c = 0; c < w; ++c) put_u32(b, row[c]);
   return hash_bytes(b);
 }
 // ExtensionMmcs row of the pi commit (basefold.rs:350-355): two E, flattened
@@ -514,34 +514,79 @@ struct EvalProver {
 // ---------------------------------------------------------------------------
 struct Commitment {
   Tree tree;
-  std::vector<uint32_t> cw;
+  size_t w = 1;
+  std::vector<uint32_t> cw;  // n_d rows of w, row-major
+  const uint32_t* row(size_t q) const { return cw.data() + q * w; }
 };
-static Commitment commit(const Code& code, const std::vector<uint32_t>& data) {  // :112-120
+// A column of a row-major matrix.
+static std::vector<uint32_t> column(const std::vector<uint32_t>& m, size_t w, size_t c) {
+  std::vector<uint32_t> v(m.size() / w);
+  for (size_t r = 0; r < v.size(); ++r) v[r] = m[r * w + c];
+  return v;
+}
+// commit (:112-120): encode_batch column by column, leaf = row bincode
+static Commitment commit(const Code& code, const std::vector<uint32_t>& data, size_t w) {
   Commitment cm;
-  cm.cw = code.encode(data);
-  std::vector<Digest> leaves(cm.cw.size());
-  for (size_t q = 0; q < cm.cw.size(); ++q) leaves[q] = leaf_f(cm.cw[q]);
+  cm.w = w;
+  cm.cw.assign(code.n_d() * w, 0);
+  for (size_t c = 0; c < w; ++c) {
+    const std::vector<uint32_t> col = code.encode(column(data, w, c));
+    for (size_t q = 0; q < col.size(); ++q) cm.cw[q * w + c] = col[q];
+  }
+  std::vector<Digest> leaves(code.n_d());
+  for (size_t q = 0; q < leaves.size(); ++q) leaves[q] = leaf_row(cm.row(q), w);
   cm.tree = build_tree(std::move(leaves));
   return cm;
 }
-static E eval(const std::vector<uint32_t>& data, const std::vector<E>& point) {  // :126-131
-  std::vector<E> ev(data.size());
-  for (size_t i = 0; i < data.size(); ++i) ev[i] = E::from(data[i]);
-  return evaluate(ev, point);
+// eval (:126-131): every column's multilinear extension at the point
+static std::vector<E> eval(const std::vector<uint32_t>& data, size_t w, const std::vector<E>& point) {
+  std::vector<E> out(w);
+  for (size_t c = 0; c < w; ++c) {
+    std::vector<E> ev(data.size() / w);
+    for (size_t i = 0; i < ev.size(); ++i) ev[i] = E::from(data[i * w + c]);
+    out[c] = evaluate(ev, point);
+  }
+  return out;
+}
+// dot_product of extension scalars with a base-field row
+static E dot_row(const std::vector<E>& s, const uint32_t* row, size_t w) {
+  E acc;
+  for (size_t c = 0; c < w; ++c) acc = eadd(acc, escale(s[c], row[c]));
+  return acc;
+}
+// sample_random_scalars_by_eq (:398-408): eq of ceil(log2 n) sampled points,
+// truncated to n
+static std::vector<E> scalars_by_eq(size_t n, Challenger& ch) {
+  int log_n = 0;
+  while (((size_t)1 << log_n) < n) ++log_n;
+  std::vector<E> r(log_n);
+  for (E& x : r) x = ch.sample_e();
+  std::vector<E> s = eq_table(r, E::one());
+  s.resize(n);
+  return s;
 }
 
 // open (:133-232); returns the bincode of BasefoldProof, empty on failure
 static std::vector<uint8_t> open(const Code& code, const Commitment& cm, const std::vector<uint32_t>& data,
-                                 const std::vector<E>& point, const E& value, Challenger& ch) {
+                                 const std::vector<E>& point, const std::vector<E>& values, Challenger& ch) {
   const int d = code.d;
-  std::vector<E> pi(cm.cw.size());
-  for (size_t q = 0; q < pi.size(); ++q) pi[q] = E::from(cm.cw[q]);
-  std::vector<E> poly(data.size());
-  for (size_t i = 0; i < data.size(); ++i) poly[i] = E::from(data[i]);
+  const size_t w = cm.w, rows = data.size() / w;
+  std::vector<E> pi(code.n_d()), poly(rows);
+  E claim;
+  if (w == 1) {
+    for (size_t q = 0; q < pi.size(); ++q) pi[q] = E::from(cm.cw[q]);
+    for (size_t i = 0; i < rows; ++i) poly[i] = E::from(data[i]);
+    claim = values[0];
+  } else {  // :160-176: rows combined with scalars sampled by eq
+    const std::vector<E> s = scalars_by_eq(w, ch);
+    for (size_t i = 0; i < rows; ++i) poly[i] = dot_row(s, data.data() + i * w, w);
+    for (size_t c = 0; c < w; ++c) claim = eadd(claim, emul(s[c], values[c]));
+    for (size_t q = 0; q < pi.size(); ++q) pi[q] = dot_row(s, cm.row(q), w);
+  }
   EvalProver pr(point, poly);
   if (!pr.ok) return {};
   Subclaim sc;
-  sc.value = value;
+  sc.value = claim;
   std::vector<Tree> pi_trees;
   std::vector<std::vector<E>> pi_vals;  // the matrix committed each round (pairs)
   std::vector<std::vector<E>> comp;
@@ -578,8 +623,8 @@ static std::vector<uint8_t> open(const Code& code, const Commitment& cm, const s
   for (const Tree& t : pi_trees) b.insert(b.end(), t.root().b, t.root().b + 32);
   put_u64(b, Q);
   for (uint64_t q : idx) {
-    put_u64(b, 1);
-    put_u32(b, cm.cw[q]);
+    put_u64(b, w);
+    for (size_t c = 0; c < w; ++c) put_u32(b, cm.row(q)[c]);
     const auto path = cm.tree.path(q);
     put_u64(b, path.size());
     for (const Digest& g : path) b.insert(b.end(), g.b, g.b + 32);
@@ -616,9 +661,14 @@ struct Reader {
     if (q) std::memcpy(&v, q, 8);
     return v;
   }
+  // a coefficient >= p does not decode (malformed), like a short read
   E e() {
     const uint8_t* q = take(20);
-    return q ? ld_e(q) : E();
+    if (!q) return E();
+    const E v = ld_e(q);
+    for (int i = 0; i < 5; ++i)
+      if (v.c[i] >= P) ok = false;
+    return v;
   }
   Digest dg() {
     Digest g{};
@@ -629,9 +679,17 @@ struct Reader {
 };
 
 // verify (:234-324): 0 ok, 1 InvalidFinalPoly, 2 InvalidQuery, 3 Mmcs, 4 malformed
-static int verify(const Code& code, const Digest& root, const std::vector<E>& point, const E& value,
+static int verify(const Code& code, const Digest& root, const std::vector<E>& point, const std::vector<E>& values,
                   Challenger& ch, const uint8_t* proof, size_t len) {
   const int d = code.d;
+  const size_t w = values.size();
+  std::vector<E> scalars = {E::one()};
+  E claim = values[0];
+  if (w > 1) {  // :253-259
+    scalars = scalars_by_eq(w, ch);
+    claim = E();
+    for (size_t c = 0; c < w; ++c) claim = eadd(claim, emul(scalars[c], values[c]));
+  }
   Reader rd{proof, len};
   std::vector<std::vector<E>> comp(rd.u64());
   if (!rd.ok || comp.size() != (size_t)d) return 4;
@@ -640,13 +698,14 @@ static int verify(const Code& code, const Digest& root, const std::vector<E>& po
     if (!rd.ok || c.size() != 2) return 4;
     for (E& e : c) e = rd.e();
   }
-  if (rd.u64() != 1) return 4;
+  if (!rd.ok || rd.u64() != 1) return 4;
   const E fin = rd.e();
+  if (!rd.ok) return 4;
   std::vector<Digest> pi_comms(rd.u64());
   if (!rd.ok || pi_comms.size() != (size_t)d) return 4;
   for (Digest& g : pi_comms) g = rd.dg();
   Subclaim sc;
-  sc.value = value;
+  sc.value = claim;
   for (int k = 0; k < d; ++k) {  // verify_interleaved_folding_sumcheck
     ch.observe(pi_comms[k].b, 32);
     for (const E& e : comp[k]) ch.observe_e(e);
@@ -664,22 +723,27 @@ static int verify(const Code& code, const Digest& root, const std::vector<E>& po
   if (rd.u64() != Q) return 4;
   for (size_t qi = 0; qi < Q; ++qi) {
     const uint64_t q = idx[qi];
-    if (rd.u64() != 1) return 4;
-    const uint8_t* vp = rd.take(4);
+    if (rd.u64() != w) return 4;
+    const uint8_t* vp = rd.take(4 * w);
     if (!vp) return 4;
-    const uint32_t row = ld_u32(vp);
+    std::vector<uint32_t> row(w);
+    for (size_t c = 0; c < w; ++c) {
+      row[c] = ld_u32(vp + 4 * c);
+      if (row[c] >= P) return 4;
+    }
     std::vector<Digest> path(rd.u64());
     if (!rd.ok || path.size() > 64) return 4;
     for (Digest& g : path) g = rd.dg();
     if (!rd.ok) return 4;
-    if (!verify_path(root, leaf_f(row), q, path, code.n_d())) return 3;
-    E folded = E::from(row);
+    if (!verify_path(root, leaf_row(row.data(), w), q, path, code.n_d())) return 3;
+    E folded = dot_row(scalars, row.data(), w);
     if (rd.u64() != (uint64_t)d) return 4;
     for (int k = 0; k < d; ++k) {
       const int i = d - 1 - k;
       const size_t ni = code.n_i(i);
       const size_t sib = ((q / ni) & 1) ^ 1, j = q % ni;
       const E other = rd.e();
+      if (!rd.ok) return 4;
       std::vector<Digest> p2(rd.u64());
       if (!rd.ok || p2.size() > 64) return 4;
       for (Digest& g : p2) g = rd.dg();
@@ -727,70 +791,73 @@ int orc_bb_dft(int log_n, uint32_t* data, int definition) {
   return 0;
 }
 size_t orc_bb_num_queries(int lambda, int log2_c) { return Code(lambda, log2_c, 0).num_queries(); }
-int orc_bb_encode(int n, int log2_c, const uint8_t* data, uint8_t* out) {
-  if (n < 0 || log2_c < 0 || n + log2_c > 27) return -1;
+static bool bad_size(int n, int log2_c, size_t w) { return n < 0 || log2_c < 0 || n + log2_c > 27 || w == 0; }
+// Data is row-major, 2^n rows of `width` canonical BabyBears.
+int orc_bb_encode(int n, int log2_c, size_t width, const uint8_t* data, uint8_t* out) {
+  if (bad_size(n, log2_c, width)) return -1;
   Code code(128, log2_c, n);
-  const std::vector<uint32_t> cw = code.encode(load_u32s(data, (size_t)1 << n));
-  std::memcpy(out, cw.data(), 4 * cw.size());
+  const Commitment cm = commit(code, load_u32s(data, width << n), width);
+  std::memcpy(out, cm.cw.data(), 4 * cm.cw.size());
   return 0;
 }
-int orc_bb_commit(int n, int log2_c, const uint8_t* data, uint8_t* root) {
-  if (n < 0 || log2_c < 0 || n + log2_c > 27) return -1;
+int orc_bb_commit(int n, int log2_c, size_t width, const uint8_t* data, uint8_t* root) {
+  if (bad_size(n, log2_c, width)) return -1;
   Code code(128, log2_c, n);
-  const Commitment cm = commit(code, load_u32s(data, (size_t)1 << n));
+  const Commitment cm = commit(code, load_u32s(data, width << n), width);
   std::memcpy(root, cm.tree.root().b, 32);
   return 0;
 }
-int orc_bb_eval(int n, const uint8_t* data, const uint8_t* point, uint8_t* out) {
-  if (n < 0 || n > 27) return -1;
-  store_e(out, eval(load_u32s(data, (size_t)1 << n), load_es(point, n)));
+int orc_bb_eval(int n, size_t width, const uint8_t* data, const uint8_t* point, uint8_t* out) {
+  if (bad_size(n, 0, width)) return -1;
+  const std::vector<E> v = eval(load_u32s(data, width << n), width, load_es(point, n));
+  for (size_t c = 0; c < width; ++c) store_e(out + 20 * c, v[c]);
   return 0;
 }
 // The reference harness (poly-commit/src/lib.rs:80-100): commit, observe the
-// root, evaluate at the point, observe the value; returns root, value and the
-// challenger state.
-int orc_bb_harness_prepare(int n, int log2_c, const uint8_t* data, const uint8_t* point, uint8_t* root,
-                           uint8_t* value, uint8_t* blob, size_t* blob_len) {
-  if (n < 0 || log2_c < 0 || n + log2_c > 27) return -1;
+// root, evaluate at the point, observe the values; returns root, values and
+// the challenger state.
+int orc_bb_harness_prepare(int n, int log2_c, size_t width, const uint8_t* data, const uint8_t* point,
+                           uint8_t* root, uint8_t* values, uint8_t* blob, size_t* blob_len) {
+  if (bad_size(n, log2_c, width)) return -1;
   Code code(128, log2_c, n);
-  const std::vector<uint32_t> m = load_u32s(data, (size_t)1 << n);
-  const Commitment cm = commit(code, m);
+  const std::vector<uint32_t> m = load_u32s(data, width << n);
+  const Commitment cm = commit(code, m, width);
   Challenger ch;
   ch.observe(cm.tree.root().b, 32);
-  const E v = eval(m, load_es(point, n));
-  ch.observe_e(v);
+  const std::vector<E> v = eval(m, width, load_es(point, n));
+  for (const E& e : v) ch.observe_e(e);
   std::memcpy(root, cm.tree.root().b, 32);
-  store_e(value, v);
+  for (size_t c = 0; c < width; ++c) store_e(values + 20 * c, v[c]);
   const std::vector<uint8_t> b = ch.to_blob();
   if (*blob_len < b.size()) return -2;
   std::memcpy(blob, b.data(), b.size());
   *blob_len = b.size();
   return 0;
 }
-int orc_bb_open(int n, int log2_c, const uint8_t* data, const uint8_t* point, const uint8_t* value,
+int orc_bb_open(int n, int log2_c, size_t width, const uint8_t* data, const uint8_t* point, const uint8_t* values,
                 const uint8_t* blob, size_t blob_len, uint8_t* out, size_t cap, size_t* len) {
-  if (n < 0 || log2_c < 0 || n + log2_c > 27) return -1;
+  if (bad_size(n, log2_c, width)) return -1;
   Code code(128, log2_c, n);
   Challenger ch;
   if (!Challenger::from_blob(blob, blob_len, ch)) return -1;
-  const std::vector<uint32_t> m = load_u32s(data, (size_t)1 << n);
-  const Commitment cm = commit(code, m);
-  const std::vector<uint8_t> pf = open(code, cm, m, load_es(point, n), ld_e(value), ch);
+  const std::vector<uint32_t> m = load_u32s(data, width << n);
+  const Commitment cm = commit(code, m, width);
+  const std::vector<uint8_t> pf = open(code, cm, m, load_es(point, n), load_es(values, width), ch);
   if (pf.empty()) return -3;
   *len = pf.size();
   if (cap < pf.size()) return -2;
   std::memcpy(out, pf.data(), pf.size());
   return 0;
 }
-int orc_bb_verify(int n, int log2_c, const uint8_t* root, const uint8_t* point, const uint8_t* value,
+int orc_bb_verify(int n, int log2_c, size_t width, const uint8_t* root, const uint8_t* point, const uint8_t* values,
                   const uint8_t* blob, size_t blob_len, const uint8_t* proof, size_t len) {
-  if (n < 0 || log2_c < 0 || n + log2_c > 27) return -1;
+  if (bad_size(n, log2_c, width)) return -1;
   Code code(128, log2_c, n);
   Challenger ch;
   if (!Challenger::from_blob(blob, blob_len, ch)) return -1;
   Digest r;
   std::memcpy(r.b, root, 32);
-  return verify(code, r, load_es(point, n), ld_e(value), ch, proof, len);
+  return verify(code, r, load_es(point, n), load_es(values, width), ch, proof, len);
 }
 
 }  // extern "C"

@@ -69,3 +69,33 @@ def test_prove_verify_round_trip(n, log2_c):
         b = bytearray(proof)
         b[pos] ^= 1
         assert O.bb_verify(n, log2_c, root, point, value, blob, bytes(b)) != 0, pos
+
+
+def test_encode_is_columnwise_and_folds():
+    """encode_batch codes each column; folding the codeword of m with r gives
+    the codeword of the half-size message m_lo + r (m_hi - m_lo) (code.rs:
+    66-84 against reed_solomon.rs:71-75), shown here on the base field."""
+    n, log2_c, w = 5, 1, 3
+    data = rnd((1 << n, w), 7)
+    cw = O.bb_encode(n, log2_c, data)
+    for c in range(w):
+        assert np.array_equal(cw[:, c], O.bb_encode(n, log2_c, data[:, c]))
+
+
+@pytest.mark.parametrize("n,log2_c,w", [(0, 1, 3), (3, 1, 2), (5, 1, 4), (6, 2, 5), (4, 1, 16)])
+def test_prove_verify_round_trip_width(n, log2_c, w):
+    data = rnd((1 << n, w), 300 + n + w)
+    point = rnd((n, 5), 400 + n)
+    root, values, blob = O.bb_harness_prepare(n, log2_c, data, point)
+    assert root == O.bb_commit(n, log2_c, data)
+    assert values.shape == (w, 5)
+    for c in range(w):
+        assert np.array_equal(values[c], O.bb_eval(n, data[:, c], point))
+    proof = O.bb_open(n, log2_c, data, point, values, blob)
+    assert O.bb_verify(n, log2_c, root, point, values, blob, proof) == 0
+    bad = values.copy()
+    bad[w - 1, 2] = (int(bad[w - 1, 2]) + 1) % P
+    assert O.bb_verify(n, log2_c, root, point, bad, blob, proof) != 0
+    b = bytearray(proof)
+    b[len(proof) - 40] ^= 4
+    assert O.bb_verify(n, log2_c, root, point, values, blob, bytes(b)) != 0
