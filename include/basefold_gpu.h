@@ -362,8 +362,18 @@ typedef struct bf_bb_commitment bf_bb_commitment;
  * num_vars) (reed_solomon.rs:19-39); num_vars + log2_c <= 27.  device < 0
  * makes a verifier-only pcs (bf_bb_verify, sizes). */
 int bf_bb_pcs_setup(int device, int lambda, int log2_c, int num_vars, void* stream, bf_bb_pcs** out);
+/* PolyCommitScheme::setup with GenericRandomFoldableCode::
+ * reed_solomon_g_0_with_random_ts(lambda, log2_c, log2_k_0, d, rng)
+ * (code/generic.rs:43-71), d = num_vars - log2_k_0.  The random vectors the
+ * reference draws from its RNG are given: `ts` holds ts[0], .., ts[d-1]
+ * back to back (n_0 << i canonical nonzero BabyBears each, n_0 =
+ * 2^(log2_c + log2_k_0); ts_len = n_0 (2^d - 1)).  G_0 is the reference's
+ * (row i = powers of i).  Proofs carry k_0 = 2^log2_k_0 final values. */
+int bf_bb_pcs_setup_generic(int device, int lambda, int log2_c, int log2_k_0, int num_vars, const uint32_t* ts,
+                            size_t ts_len, void* stream, bf_bb_pcs** out);
 void bf_bb_pcs_free(bf_bb_pcs* pcs);
-/* RandomFoldableCode::num_queries (reed_solomon.rs:57-64). */
+/* RandomFoldableCode::num_queries (reed_solomon.rs:57-64, generic.rs:
+ * 99-103 with F::bits() = 31). */
 size_t bf_bb_pcs_num_queries(const bf_bb_pcs* pcs);
 /* Exact bincode size of the proof of a width-`width` open of n_evals (0 or
  * 1) points. */

@@ -22,7 +22,7 @@ EXPORTS = [
     "bf_engine_poll", "bf_eval_noalloc", "bf_pcs_autotune", "bf_pcs_get_tune", "bf_pcs_set_tune",
     "bf_engine_autotune", "bf_engine_graphs", "bf_engine_stats", "bf_verify_batch", "bf_engine_set_tune", "bf_engine_cancel", "bf_engine_schedule",
     "bf_eval_data", "bf_tune_cache_load", "bf_tune_cache_save", "bf_tune_cache_clear",
-    "bf_bb_pcs_setup", "bf_bb_pcs_free", "bf_bb_pcs_num_queries", "bf_bb_pcs_proof_size", "bf_bb_commit",
+    "bf_bb_pcs_setup", "bf_bb_pcs_setup_generic", "bf_bb_pcs_free", "bf_bb_pcs_num_queries", "bf_bb_pcs_proof_size", "bf_bb_commit",
     "bf_bb_commit_device", "bf_bb_commitment_root", "bf_bb_commitment_free", "bf_bb_eval", "bf_bb_open",
     "bf_bb_verify", "bf_challenger_sample_bb_ext",
 ]
@@ -137,6 +137,7 @@ def lib():
         "bf_engine_cancel": ([vp, vp], i),
         "bf_engine_schedule": ([vp, i, i], i),
         "bf_bb_pcs_setup": ([i, i, i, i, vp, C.POINTER(vp)], i),
+        "bf_bb_pcs_setup_generic": ([i, i, i, i, i, vp, sz, vp, C.POINTER(vp)], i),
         "bf_bb_pcs_free": ([vp], None),
         "bf_bb_pcs_num_queries": ([vp], sz),
         "bf_bb_pcs_proof_size": ([vp, sz, i], sz),

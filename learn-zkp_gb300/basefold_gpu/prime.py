@@ -26,7 +26,7 @@ from . import BasefoldConfig, BasefoldError, GenericChallenger
 P = 2013265921
 
 __all__ = [
-    "P", "ReedSolomonCode", "BasefoldConfig", "PrimePolyEvals", "PrimeCommitmentData", "BabyBearBasefold",
+    "P", "ReedSolomonCode", "GenericRandomFoldableCode", "BasefoldConfig", "PrimePolyEvals", "PrimeCommitmentData", "BabyBearBasefold",
     "observe_ext_slice", "sample_ext_element",
 ]
 
@@ -68,6 +68,24 @@ class ReedSolomonCode:
         return self.c() << self.d
 
 
+class GenericRandomFoldableCode:
+    """GenericRandomFoldableCode::reed_solomon_g_0_with_random_ts(lambda,
+    log2_c, log2_k_0, d, rng) (generic.rs:43-71) with the random vectors
+    given: `ts` holds ts[0], .., ts[d-1] back to back (n_0 << i nonzero
+    canonical BabyBears each, n_0 = 2^(log2_c + log2_k_0))."""
+
+    def __init__(self, lambda_: int, log2_c: int, log2_k_0: int, d: int, ts):
+        self.lambda_, self.log2_c, self.log2_k_0, self.d = lambda_, log2_c, log2_k_0, d
+        self.ts = np.ascontiguousarray(np.asarray(ts, dtype=np.uint32)).reshape(-1)
+
+    @property
+    def num_vars(self) -> int:
+        return self.log2_k_0 + self.d
+
+    def n_0(self) -> int:
+        return 1 << (self.log2_c + self.log2_k_0)
+
+
 class PrimePolyEvals:
     """PolyEvals { values, point } (poly-commit/src/lib.rs:14-18) over E."""
 
@@ -107,9 +125,19 @@ class BabyBearBasefold:
     def setup(cls, config: BasefoldConfig, device: int = 0, stream=None) -> "BabyBearBasefold":
         h = C.c_void_p()
         code = config.code
-        check(lib().bf_bb_pcs_setup(device, code.lambda_, code.log2_c, code.d,
-                                    C.c_void_p(stream) if stream else None, C.byref(h)))
+        st = C.c_void_p(stream) if stream else None
+        if isinstance(code, GenericRandomFoldableCode):
+            ts = code.ts if code.ts.size else np.zeros(1, np.uint32)
+            check(lib().bf_bb_pcs_setup_generic(device, code.lambda_, code.log2_c, code.log2_k_0, code.num_vars,
+                                                _p(ts), code.ts.size, st, C.byref(h)))
+        else:
+            check(lib().bf_bb_pcs_setup(device, code.lambda_, code.log2_c, code.d, st, C.byref(h)))
         return cls(h, config, device)
+
+    @property
+    def num_vars(self) -> int:
+        code = self.config.code
+        return code.num_vars if isinstance(code, GenericRandomFoldableCode) else code.d
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -127,14 +155,14 @@ class BabyBearBasefold:
         return int(lib().bf_bb_pcs_proof_size(self._h, width, n_evals))
 
     def _rows(self) -> int:
-        return 1 << self.config.code.d
+        return 1 << self.num_vars
 
     def commit(self, data) -> PrimeCommitmentData:
         """commit (basefold.rs:112-120) of host evaluations: 2^d rows x width."""
         d = np.ascontiguousarray(np.asarray(data, dtype=np.uint32))
         width = d.size // self._rows()
         if width == 0 or width * self._rows() != d.size:
-            raise ValueError(f"{d.size} evaluations is not a multiple of 2^{self.config.code.d} rows")
+            raise ValueError(f"{d.size} evaluations is not a multiple of 2^{self.num_vars} rows")
         h = C.c_void_p()
         root = np.zeros(32, dtype=np.uint8)
         check(lib().bf_bb_commit(self._h, _p(d), width, C.byref(h), _p(root)))
@@ -148,7 +176,7 @@ class BabyBearBasefold:
         return PrimeCommitmentData(self, h, root.tobytes(), width, keep=keep)
 
     def _point(self, point) -> np.ndarray:
-        d = self.config.code.d
+        d = self.num_vars
         return _ext(point, d) if d else np.zeros((1, 5), np.uint32)
 
     def eval(self, comm: PrimeCommitmentData, point) -> np.ndarray:

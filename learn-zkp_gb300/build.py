@@ -42,8 +42,10 @@ def build(force: bool = False, verbose: bool = False) -> str:
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
     cc = nvcc()
+    # host code: no fused multiply-add contraction, so the query-count
+    # formulas in double round as the reference's Rust does
     flags = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
-                    "-diag-suppress", "177"]
+                    "-Xcompiler", "-ffp-contract=off", "-diag-suppress", "177"]
     objs = []
 
     def compile_one(src):

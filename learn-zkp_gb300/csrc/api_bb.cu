@@ -22,29 +22,52 @@ using bbh::E;
 struct bf_bb_pcs {
   std::atomic<int> refs{1};
   int device = -1;
-  int lambda = 128, log2_c = 1, d = 0, L = 0;
+  // num_vars = log2_k0 + d; the codeword has 2^L rows, L = log2_c + num_vars
+  int lambda = 128, log2_c = 1, log2_k0 = 0, d = 0, num_vars = 0, L = 0;
+  bool generic = false;              // GenericRandomFoldableCode, else ReedSolomonCode
+  std::vector<uint32_t> ts;          // generic: ts[0], .., ts[d-1] back to back (canonical)
   size_t Q = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
-  DevBuf tw;    // DIT twiddles: layer s at 2^s - 1, g_s^k for k < 2^s (Montgomery)
-  DevBuf tinv;  // fold constants: round i at c (2^i - 1), (2 t_i^j)^-1 for j < n_i (Montgomery)
+  DevBuf tw;    // butterfly factors: layer s at 2^s - 1, 2^s of them (Montgomery)
+  DevBuf tinv;  // fold constants: round i at n_0 (2^i - 1), (2 t_i[j])^-1 for j < n_i (Montgomery)
   DevBuf small;  // 4 KB: the canonical flag, sums, roots
   DevBuf ws;       // grow-only scratch of bf_bb_eval
   DevBuf open_ws;  // grow-only workspace of bf_bb_open
   PinnedBuf pin;
 
   size_t c() const { return (size_t)1 << log2_c; }
+  size_t k0() const { return (size_t)1 << log2_k0; }
+  int log2_n0() const { return log2_c + log2_k0; }
+  size_t n0() const { return (size_t)1 << log2_n0(); }
   size_t n_d() const { return (size_t)1 << L; }
-  size_t n_i(int i) const { return c() << i; }
-  size_t tinv_off(int i) const { return c() * (((size_t)1 << i) - 1); }
+  size_t n_i(int i) const { return n0() << i; }
+  size_t tinv_off(int i) const { return n0() * (((size_t)1 << i) - 1); }
   // One query record (basefold.rs:56-65 in bincode): the codeword row and its
   // path, then per round the sibling and its path.
   size_t rec_bytes(size_t w) const {
     size_t words = 2 + w + 2 + 8 * (size_t)L + 2;
-    for (int i = 0; i < d; ++i) words += 7 + 8 * (size_t)(log2_c + i);
+    for (int i = 0; i < d; ++i) words += 7 + 8 * (size_t)(log2_n0() + i);
     return 4 * words;
   }
-  size_t header_bytes() const { return 52 + 80 * (size_t)d; }
+  // round polys (u64 + two E each), final poly (u64 + k_0 E), roots, query count
+  size_t header_bytes() const { return 8 + 48 * (size_t)d + 8 + 20 * k0() + 8 + 32 * (size_t)d + 8; }
+  // (2 t_i[j])^-1 on the host (the verifier's interpolate)
+  uint32_t t_inv_half(int i, size_t j) const {
+    const uint32_t t = generic ? ts[tinv_off(i) + j] : bbh::fpow(bbh::two_adic_generator(log2_c + i + 1), j);
+    return bbh::finv(bbh::fadd(t, t));
+  }
+  // encode0 (reed_solomon.rs:66-70, generic.rs:105-110): entry i of m G_0
+  E encode0_at(const std::vector<E>& m, size_t i) const {
+    if (!generic) return m[0];
+    E acc;
+    uint32_t pw = 1;
+    for (const E& e : m) {
+      acc = bbh::eadd(acc, bbh::escale(e, pw));
+      pw = bbh::fmul(pw, (uint32_t)i);
+    }
+    return acc;
+  }
   ~bf_bb_pcs() {
     if (device >= 0) {
       cudaSetDevice(device);
@@ -75,13 +98,25 @@ void bb_release(bf_bb_pcs* p) {
   if (p->refs.fetch_sub(1) == 1) delete p;
 }
 
-// RandomFoldableCode::num_queries of ReedSolomonCode (reed_solomon.rs:57-64):
-// delta = 1 - (1 - 1/c) / 3 in the unique-decoding regime.
-size_t bb_num_queries(int lambda, int log2_c) {
-  const double c = (double)((size_t)1 << log2_c);
-  const double delta = 1.0 - (1.0 - 1.0 / c) / 3.0;
-  const double q = std::ceil((double)lambda / -std::log2(delta));
-  if (!(q > 0) || !std::isfinite(q)) return 0;  // c = 1: the Rust cast of -inf is 0
+// Relative distance bound of the generic code: appendix C of ePrint
+// 2023/1705 as generic.rs:24-39 evaluates it, F::bits() = 31 for BabyBear.
+double generic_z_c(double lambda, double log2_f, size_t c, int i, int log2_n_i) {
+  if (i == 0) return 1.0 / (double)c;
+  return generic_z_c(lambda, log2_f, c, i - 1, log2_n_i - 1) * (log2_f / (log2_f - 1.001)) +
+         1.0 / (log2_f - 1.001) *
+             ((2.0 * (double)(log2_n_i - 1) + lambda) / (double)((uint64_t)1 << log2_n_i) + 0.6);
+}
+
+// RandomFoldableCode::num_queries (reed_solomon.rs:57-64, generic.rs:99-103):
+// delta = 1 - distance / 3 in the unique-decoding regime, the Rust cast
+// saturating (-inf, NaN and negatives give 0).
+size_t bb_num_queries(const bf_bb_pcs& p) {
+  const double rel = p.generic ? 1.0 - generic_z_c((double)p.lambda, 31.0, p.c(), p.d, p.L)
+                               : 1.0 - 1.0 / (double)p.c();
+  const double delta = 1.0 - rel / 3.0;
+  const double q = std::ceil((double)p.lambda / -std::log2(delta));
+  if (!(q > 0)) return 0;
+  if (!std::isfinite(q) || q > 1e15) return (size_t)-1;  // unreachable for lambda <= 2^20
   return (size_t)q;
 }
 
@@ -108,7 +143,8 @@ int commit_device(bf_bb_pcs* p, bf_bb_commitment* cm, const uint32_t* data) {
   CU(cm->tree.alloc(64 * n));
   uint32_t* flag = p->small.as<uint32_t>();
   CU(cudaMemsetAsync(flag, 0, 4, p->stream));
-  CU(bf::bb_launch_encode(data, cm->cw.as<uint32_t>(), p->d, p->log2_c, w, p->tw.as<uint32_t>(), flag, p->stream));
+  CU(bf::bb_launch_encode(data, cm->cw.as<uint32_t>(), p->d, p->log2_c, p->log2_k0, p->generic, w,
+                          p->tw.as<uint32_t>(), flag, p->stream));
   uint4* leaves = cm->tree.as<uint4>();
   CU(bf::bb_launch_leaves_rows(cm->cw.as<uint32_t>(), leaves, n, w, p->L, p->stream));
   uint4* root_dev = p->small.as<uint4>() + 2;
@@ -126,18 +162,32 @@ int commit_device(bf_bb_pcs* p, bf_bb_commitment* cm, const uint32_t* data) {
 
 extern "C" {
 
-int bf_bb_pcs_setup(int device, int lambda, int log2_c, int num_vars, void* stream, bf_bb_pcs** out) {
+static int bb_setup(int device, int lambda, int log2_c, int log2_k0, int num_vars, const uint32_t* ts,
+                    size_t ts_len, void* stream, bf_bb_pcs** out) {
   if (!out) return fail(BF_ERR_ARG, "out is null");
   *out = nullptr;
-  if (lambda < 0 || log2_c < 0 || num_vars < 0 || num_vars + log2_c > 27)
-    return fail(BF_ERR_ARG, "unsupported code parameters lambda=%d log2_c=%d num_vars=%d (num_vars + log2_c <= 27)",
-                lambda, log2_c, num_vars);
+  if (lambda < 0 || log2_c < 0 || num_vars < 0 || log2_k0 < 0 || log2_k0 > num_vars || num_vars + log2_c > 27)
+    return fail(BF_ERR_ARG,
+                "unsupported code parameters lambda=%d log2_c=%d log2_k_0=%d num_vars=%d (log2_k_0 <= num_vars, "
+                "num_vars + log2_c <= 27)",
+                lambda, log2_c, log2_k0, num_vars);
   std::unique_ptr<bf_bb_pcs> p(new bf_bb_pcs());
   p->lambda = lambda;
   p->log2_c = log2_c;
-  p->d = num_vars;
+  p->log2_k0 = log2_k0;
+  p->num_vars = num_vars;
+  p->d = num_vars - log2_k0;
   p->L = num_vars + log2_c;
-  p->Q = bb_num_queries(lambda, log2_c);
+  p->generic = ts != nullptr;
+  if (p->generic) {
+    const size_t need = p->n0() * (((size_t)1 << p->d) - 1);
+    if (ts_len != need)
+      return fail(BF_ERR_ARG, "ts holds %zu values; the code needs n_0 (2^d - 1) = %zu", ts_len, need);
+    for (size_t k = 0; k < need; ++k)
+      if (ts[k] == 0 || ts[k] >= bbh::P) return fail(BF_ERR_ARG, "ts[%zu] = %u is zero or not canonical", k, ts[k]);
+    p->ts.assign(ts, ts + need);
+  }
+  p->Q = bb_num_queries(*p);
   if (device < 0) {  // verifier-only: no GPU is touched
     *out = p.release();
     return BF_OK;
@@ -152,22 +202,51 @@ int bf_bb_pcs_setup(int device, int lambda, int log2_c, int num_vars, void* stre
   }
   CU(p->pin.ensure(4096));
   CU(p->small.alloc(4096));
-  // DIT twiddles: layer s (half-size 2^s) uses g_s = two_adic_generator(s + 1)
   CU(p->tw.alloc(4 * p->n_d()));
-  for (int s = 0; s < p->L; ++s)
-    CU(bf::bb_launch_pow_table(p->tw.as<uint32_t>() + ((size_t)1 << s) - 1, (size_t)1 << s,
-                               bb::to_mont(bbh::two_adic_generator(s + 1)), bb::MONT_ONE, p->stream));
-  // ReedSolomonCode::new (reed_solomon.rs:20-38): t_i = two_adic_generator(
-  // log2_c + i + 1), entry j = (2 t_i^j)^-1 = 2^-1 (t_i^-1)^j
-  CU(p->tinv.alloc(4 * p->c() * (((size_t)1 << p->d) - 1) + 4));
-  for (int i = 0; i < p->d; ++i) {
-    const uint32_t t_inv = bbh::finv(bbh::two_adic_generator(p->log2_c + i + 1));
-    CU(bf::bb_launch_pow_table(p->tinv.as<uint32_t>() + p->tinv_off(i), p->n_i(i), bb::to_mont(t_inv),
-                               bb::MONT_INV2, p->stream));
+  CU(p->tinv.alloc(4 * p->n0() * (((size_t)1 << p->d) - 1) + 4));
+  uint32_t* flag = p->small.as<uint32_t>();
+  CU(cudaMemsetAsync(flag, 0, 4, p->stream));
+  if (!p->generic) {
+    // DIT twiddles: layer s (half-size 2^s) uses g_s = two_adic_generator(s + 1)
+    for (int s = 0; s < p->L; ++s)
+      CU(bf::bb_launch_pow_table(p->tw.as<uint32_t>() + ((size_t)1 << s) - 1, (size_t)1 << s,
+                                 bb::to_mont(bbh::two_adic_generator(s + 1)), bb::MONT_ONE, p->stream));
+    // ReedSolomonCode::new (reed_solomon.rs:20-38): t_i = two_adic_generator(
+    // log2_c + i + 1), entry j = (2 t_i^j)^-1 = 2^-1 (t_i^-1)^j
+    for (int i = 0; i < p->d; ++i) {
+      const uint32_t t_inv = bbh::finv(bbh::two_adic_generator(p->log2_c + i + 1));
+      CU(bf::bb_launch_pow_table(p->tinv.as<uint32_t>() + p->tinv_off(i), p->n_i(i), bb::to_mont(t_inv),
+                                 bb::MONT_INV2, p->stream));
+    }
+  } else if (p->d > 0) {
+    // generic.rs:43-71: round i's butterflies are layer log2_n0 + i of the
+    // encode and its fold constants are (2 ts[i][j])^-1
+    DevBuf tdev;
+    const size_t total = p->ts.size();
+    CU(tdev.alloc(4 * total));
+    CU(cudaMemcpyAsync(tdev.p, p->ts.data(), 4 * total, cudaMemcpyHostToDevice, p->stream));
+    for (int i = 0; i < p->d; ++i) {
+      const int s = p->log2_n0() + i;
+      CU(bf::bb_launch_to_mont(tdev.as<uint32_t>() + p->tinv_off(i), p->tw.as<uint32_t>() + ((size_t)1 << s) - 1,
+                               p->n_i(i), flag, p->stream));
+    }
+    CU(bf::bb_launch_tinv(tdev.as<uint32_t>(), p->tinv.as<uint32_t>(), total, flag, p->stream));
+    CU(cudaStreamSynchronize(p->stream));  // tdev is released below
   }
   CU(cudaStreamSynchronize(p->stream));
   *out = p.release();
   return BF_OK;
+}
+
+int bf_bb_pcs_setup(int device, int lambda, int log2_c, int num_vars, void* stream, bf_bb_pcs** out) {
+  return bb_setup(device, lambda, log2_c, 0, num_vars, nullptr, 0, stream, out);
+}
+
+int bf_bb_pcs_setup_generic(int device, int lambda, int log2_c, int log2_k_0, int num_vars, const uint32_t* ts,
+                            size_t ts_len, void* stream, bf_bb_pcs** out) {
+  if (!ts && num_vars > log2_k_0) return fail(BF_ERR_ARG, "ts is null");
+  static const uint32_t none = 1;
+  return bb_setup(device, lambda, log2_c, log2_k_0, num_vars, ts ? ts : &none, ts_len, stream, out);
 }
 
 void bf_bb_pcs_free(bf_bb_pcs* pcs) {
@@ -196,7 +275,7 @@ int bf_bb_commit(bf_bb_pcs* p, const uint32_t* evals, size_t width, bf_bb_commit
   std::unique_ptr<bf_bb_commitment> cm(new bf_bb_commitment());
   cm->pcs = p;
   cm->w = width;
-  const size_t bytes = 4 * width << p->d;
+  const size_t bytes = 4 * width << p->num_vars;
   CU(cm->data.alloc(bytes));
   CU(cudaMemcpyAsync(cm->data.p, evals, bytes, cudaMemcpyHostToDevice, p->stream));
   TRY(commit_device(p, cm.get(), cm->data.as<uint32_t>()));
@@ -215,7 +294,7 @@ int bf_bb_commit_device(bf_bb_pcs* p, const void* d_evals, size_t width, bf_bb_c
   cm->w = width;
   cm->data.p = const_cast<void*>(d_evals);
   cm->data.owned = false;
-  cm->data.bytes = 4 * width << p->d;
+  cm->data.bytes = 4 * width << p->num_vars;
   TRY(commit_device(p, cm.get(), cm->data.as<uint32_t>()));
   if (root) std::memcpy(root, cm->root, 32);
   bb_acquire(p);
@@ -241,12 +320,12 @@ void bf_bb_commitment_free(bf_bb_commitment* cm) {
 }
 
 int bf_bb_eval(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, uint8_t* values) {
-  if (!p || !cm || !values || (p->d > 0 && !point)) return fail(BF_ERR_ARG, "null argument");
+  if (!p || !cm || !values || (p->num_vars > 0 && !point)) return fail(BF_ERR_ARG, "null argument");
   if (cm->pcs != p) return fail(BF_ERR_ARG, "commitment made by another pcs");
   std::vector<E> x;
-  TRY(load_points(point, (size_t)p->d, x, "point coordinate"));
+  TRY(load_points(point, (size_t)p->num_vars, x, "point coordinate"));
   DeviceGuard g(p->device);
-  const size_t rows = (size_t)1 << p->d, w = cm->w;
+  const size_t rows = (size_t)1 << p->num_vars, w = cm->w;
   // the sums are 64-bit atomics: their slot starts on a 256-byte boundary
   const size_t eq_bytes = (20 * rows + 255) & ~(size_t)255, acc_bytes = 40 * w;
   if (p->ws.bytes < eq_bytes + acc_bytes) CU(p->ws.alloc(eq_bytes + acc_bytes));
@@ -279,14 +358,14 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
     std::memset(proof, 0, 32);
     return BF_OK;
   }
-  if (!values || (p->d > 0 && !point)) return fail(BF_ERR_ARG, "null argument");
-  const int d = p->d, L = p->L;
-  const size_t w = cm->w, Q = p->Q, rec = p->rec_bytes(w);
+  if (!values || (p->num_vars > 0 && !point)) return fail(BF_ERR_ARG, "null argument");
+  const int d = p->d, L = p->L, nv = p->num_vars, lk = p->log2_k0;
+  const size_t w = cm->w, Q = p->Q, rec = p->rec_bytes(w), k0 = p->k0();
   const size_t total = p->header_bytes() + Q * rec;
   *proof_len = total;
   if (!proof || cap < total) return fail(BF_ERR_BUFFER, "proof buffer of %zu bytes, %zu needed", cap, total);
   std::vector<E> r, vals;
-  TRY(load_points(point, (size_t)d, r, "point coordinate"));
+  TRY(load_points(point, (size_t)nv, r, "point coordinate"));
   TRY(load_points(values, w, vals, "value"));
   bbh::EvalScalars es;
   if (!es.init(r)) return fail(BF_ERR_NOT_INVERTIBLE, "a point coordinate is 0, or 1 below the last");
@@ -297,8 +376,8 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
   // Workspace: batched poly and pi (width > 1), half_eq, two fix buffers,
   // the fold outputs of every round, the trees of every round, query indices
   // and records.
-  const size_t rows = (size_t)1 << d, half = rows >> 1;
-  const size_t n_fold = p->c() * (rows - 1);  // sum over rounds of n_i
+  const size_t rows = (size_t)1 << nv, half = rows >> 1;
+  const size_t n_fold = p->n0() * (((size_t)1 << d) - 1);  // sum over rounds of n_i
   const size_t wsz[] = {w > 1 ? 20 * rows : 0,  w > 1 ? 20 * p->n_d() : 0, 20 * (half ? half : 1), 20 * half,
                         20 * half,              20 * n_fold,             64 * n_fold,             8 * Q,
                         Q * rec,                128};
@@ -316,7 +395,7 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
   uint8_t* recs = base + off[8];
   unsigned long long* acc = reinterpret_cast<unsigned long long*>(base + off[9]);
   uint4* root_dev = reinterpret_cast<uint4*>(base + off[9] + 64);  // after the five sums
-  CU(p->pin.ensure(8 * Q + 256));
+  CU(p->pin.ensure(8 * Q + 20 * k0 + 20 * 64 + 256));
 
   // The polynomial and codeword the folding sumcheck runs on (basefold.rs:154-177).
   E claim;
@@ -340,7 +419,8 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
     pi = piE;
     base_round = 0;
   }
-  if (d > 0) TRY(eq_table_device(p, std::vector<E>(r.begin(), r.end() - 1), heq));
+  // HalfEq over the point's first num_vars - 1 coordinates (eval_impr.rs)
+  if (nv > 0) TRY(eq_table_device(p, std::vector<E>(r.begin(), r.end() - 1), heq));
 
   bbh::Subclaim sc;
   sc.value = claim;
@@ -350,7 +430,8 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
   gp.pi0_base = w == 1;
   size_t fold_off = 0, tree_off = 0;
   for (int k = 0; k < d; ++k) {  // prove_interleaved_folding_sumcheck (basefold.rs:335-369)
-    const int i = d - 1 - k, li = p->log2_c + i;
+    const int i = d - 1 - k, li = p->log2_n0() + i;
+    const int ri = i + lk;  // the sumcheck round (basefold.rs:356-361)
     const size_t ni = p->n_i(i);
     uint4* tree = trees + 2 * tree_off;
     gp.pi[k] = pi;
@@ -359,7 +440,7 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
     if (k == 0) CU(bf::bb_launch_leaves_pairs(pi, base_k, tree, ni, li, st));  // later rounds: made by the fold
     CU(bf::launch_tree(tree, ni, st, root_dev, bf::Tune()));
     CU(cudaMemsetAsync(acc, 0, 40, st));
-    CU(bf::bb_launch_dot(heq, poly, base_k, (size_t)1 << i, acc, st));
+    CU(bf::bb_launch_dot(heq, poly, base_k, (size_t)1 << ri, acc, st));
     CU(cudaMemcpyAsync(p->pin.p, acc, 96, cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));
     const unsigned long long* sums = reinterpret_cast<const unsigned long long*>(p->pin.p);
@@ -367,7 +448,7 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
     bfh::digest_from_interleaved(p->pin.b() + 64, root.data());
     tr.observe(root.data(), 32);
     E rp[3];
-    es.round_poly((size_t)i, sc, bbh::from_dev_sums(sums), rp);
+    es.round_poly((size_t)ri, sc, bbh::from_dev_sums(sums), rp);
     bbh::observe_e(tr, rp[0]);  // Eval::compress_round_poly keeps c0 and c2
     bbh::observe_e(tr, rp[2]);
     const E x = bbh::sample_e(tr);
@@ -377,7 +458,7 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
     roots.push_back(root);
     const bb::E5 xd = bbh::to_dev(x);
     uint32_t* fixed = fixbuf[k & 1];
-    CU(bf::bb_launch_fix(poly, base_k, fixed, (size_t)1 << i, xd, st));
+    CU(bf::bb_launch_fix(poly, base_k, fixed, (size_t)1 << ri, xd, st));
     poly = fixed;
     bf::BbFold fp;
     fp.w = pi;
@@ -392,35 +473,39 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
     fold_off += ni;
     tree_off += 2 * ni;
   }
-  // final_poly: the fully fixed polynomial (one element), observed
-  E fin;
+  // final_poly (into_ext_poly): the k_0 evaluations left after d fixes, observed
+  std::vector<E> fin(k0);
   {
-    const int fin_base = d == 0 && base_round;
-    CU(cudaMemcpyAsync(p->pin.p, poly, fin_base ? 4 : 20, cudaMemcpyDeviceToHost, st));
+    const int fin_base = d == 0 && base_round;  // still the caller's base-field data
+    CU(cudaMemcpyAsync(p->pin.p, poly, (fin_base ? 4 : 20) * k0, cudaMemcpyDeviceToHost, st));
+    const size_t chk_off = 20 * k0 + 64;
     size_t nchk = 0;
-    if (d > 0) {  // debug_assert_eq!(encode0(final_poly), pi): every entry of the last fold
-      nchk = p->c() < 64 ? p->c() : 64;
-      CU(cudaMemcpyAsync(p->pin.b() + 32, pi, 20 * nchk, cudaMemcpyDeviceToHost, st));
+    if (d > 0) {  // debug_assert_eq!(encode0(final_poly), pi) (basefold.rs:189), up to 64 entries
+      nchk = p->n0() < 64 ? p->n0() : 64;
+      CU(cudaMemcpyAsync(p->pin.b() + chk_off, pi, 20 * nchk, cudaMemcpyDeviceToHost, st));
     }
     CU(cudaStreamSynchronize(st));
-    if (fin_base) {
-      uint32_t v;
-      std::memcpy(&v, p->pin.p, 4);
-      fin = E::from(v);
-    } else {
-      uint32_t m[5];
-      std::memcpy(m, p->pin.p, 20);
-      for (int q = 0; q < 5; ++q) fin.c[q] = bb::from_mont(m[q]);
+    for (size_t t = 0; t < k0; ++t) {
+      if (fin_base) {
+        uint32_t v;
+        std::memcpy(&v, p->pin.b() + 4 * t, 4);
+        fin[t] = E::from(v);
+      } else {
+        uint32_t m[5];
+        std::memcpy(m, p->pin.b() + 20 * t, 20);
+        for (int q = 0; q < 5; ++q) fin[t].c[q] = bb::from_mont(m[q]);
+      }
     }
     for (size_t q = 0; q < nchk; ++q) {
       uint32_t m[5];
-      std::memcpy(m, p->pin.b() + 32 + 20 * q, 20);
+      std::memcpy(m, p->pin.b() + chk_off + 20 * q, 20);
       E e;
       for (int t = 0; t < 5; ++t) e.c[t] = bb::from_mont(m[t]);
-      if (e != fin) return fail(BF_ERR_CHECK, "the last folded codeword is not the encoding of the final value");
+      if (e != p->encode0_at(fin, q))
+        return fail(BF_ERR_CHECK, "the last folded codeword is not the encoding of the final polynomial");
     }
   }
-  bbh::observe_e(tr, fin);
+  for (const E& e : fin) bbh::observe_e(tr, e);
   std::vector<uint64_t> idx(Q);
   for (uint64_t& v : idx) v = tr.sample_bits(L);
   if (Q) {
@@ -434,7 +519,7 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
     gp.rec_bytes = rec;
     gp.L = L;
     gp.d = d;
-    gp.log2_c = p->log2_c;
+    gp.log2_n0 = p->log2_n0();
     gp.nq = (int)Q;
     CU(bf::bb_launch_gather(gp, st));
     CU(cudaMemcpyAsync(proof + p->header_bytes(), recs, Q * rec, cudaMemcpyDeviceToHost, st));
@@ -451,10 +536,10 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
       h.insert(h.end(), b, b + 20);
     }
   }
-  put_u64(h, 1);
-  {
+  put_u64(h, (uint64_t)k0);
+  for (const E& e : fin) {
     uint8_t b[20];
-    bbh::store(b, fin);
+    bbh::store(b, e);
     h.insert(h.end(), b, b + 20);
   }
   put_u64(h, (uint64_t)d);
@@ -550,11 +635,11 @@ int bf_bb_verify(const bf_bb_pcs* p, const uint8_t root[32], const uint8_t* poin
   if (!p || !root || !ch || (!proof && proof_len)) return fail(BF_ERR_ARG, "null argument");
   if (n_evals < 0 || n_evals > 1) return fail(BF_ERR_ARG, "n_evals %d: one point or none", n_evals);
   if (n_evals == 0) return BF_VERIFY_OK;  // basefold.rs:241-243
-  if (!values || (p->d > 0 && !point)) return fail(BF_ERR_ARG, "null argument");
+  if (!values || (p->num_vars > 0 && !point)) return fail(BF_ERR_ARG, "null argument");
   if (width == 0) return fail(BF_ERR_ARG, "width 0");
-  const int d = p->d;
+  const int d = p->d, lk = p->log2_k0;
   std::vector<E> r, vals;
-  TRY(load_points(point, (size_t)d, r, "point coordinate"));
+  TRY(load_points(point, (size_t)p->num_vars, r, "point coordinate"));
   TRY(load_points(values, width, vals, "value"));
   bfh::Challenger& tr = ch->c;
   std::vector<E> scalars = {E::one()};
@@ -570,8 +655,10 @@ int bf_bb_verify(const bf_bb_pcs* p, const uint8_t root[32], const uint8_t* poin
   for (auto& c : comp) {
     if (rd.u64() != 2 || !rd.e(c[0]) || !rd.e(c[1])) return BF_VERIFY_MALFORMED;
   }
-  E fin;
-  if (rd.u64() != 1 || !rd.e(fin)) return BF_VERIFY_MALFORMED;
+  std::vector<E> fin(p->k0());
+  if (rd.u64() != (uint64_t)p->k0()) return BF_VERIFY_MALFORMED;
+  for (E& e : fin)
+    if (!rd.e(e)) return BF_VERIFY_MALFORMED;
   if (rd.u64() != (uint64_t)d || !rd.ok) return BF_VERIFY_MALFORMED;
   std::vector<Dg> pi_comms((size_t)d);
   for (Dg& g : pi_comms) {
@@ -592,11 +679,22 @@ int bf_bb_verify(const bf_bb_pcs* p, const uint8_t root[32], const uint8_t* poin
     const E rp[3] = {comp[k][0], c1, comp[k][1]};
     sc.reduce(rp, 3, x);
   }
-  bbh::observe_e(tr, fin);
+  for (const E& e : fin) bbh::observe_e(tr, e);
   const std::vector<E> rr = sc.r();
-  // log2_k_0 = 0: evaluate(final_poly, []) = final_poly[0]
-  if (bbh::emul(fin, bbh::eq_eval(r.data(), rr.data(), r.size() < rr.size() ? r.size() : rr.size())) != sc.value)
+  // evaluate(final_poly, point_lo) * eq_eval(point_hi, r) (basefold.rs:271-275):
+  // fix_last_var with point_lo from its last coordinate down
+  std::vector<E> ev = fin;
+  for (int k = lk - 1; k >= 0; --k) {
+    const size_t mid = ev.size() / 2;
+    for (size_t b = 0; b < mid; ++b) ev[b] = bbh::eadd(ev[b], bbh::emul(r[k], bbh::esub(ev[b + mid], ev[b])));
+    ev.resize(mid);
+  }
+  const size_t nhi = r.size() - (size_t)lk;
+  if (bbh::emul(ev[0], bbh::eq_eval(r.data() + lk, rr.data(), nhi < rr.size() ? nhi : rr.size())) != sc.value)
     return BF_VERIFY_INVALID_FINAL_POLY;
+  // pi_0 = encode0(final_poly) (basefold.rs:277)
+  std::vector<E> pi0(p->n0());
+  for (size_t i = 0; i < pi0.size(); ++i) pi0[i] = p->encode0_at(fin, i);
   const size_t Q = p->Q;
   std::vector<uint64_t> idx(Q);
   for (uint64_t& v : idx) v = tr.sample_bits(p->L);
@@ -626,14 +724,13 @@ int bf_bb_verify(const bf_bb_pcs* p, const uint8_t root[32], const uint8_t* poin
       E v[2] = {folded, folded};
       v[sib] = other;
       if (!verify_path(pi_comms[k].b, leaf_pair(v[0], v[1]), j, path, ni)) return BF_VERIFY_MMCS;
-      // interpolate (code.rs:79-84) with t = (2 t_i^j)^-1 and round i's challenge r[i]
-      const uint32_t tj = bbh::fpow(bbh::two_adic_generator(p->log2_c + i + 1), j);
-      const uint32_t t = bbh::finv(bbh::fadd(tj, tj));
+      // interpolate (code.rs:86-91) with (2 t_i[j])^-1 and round i's challenge rr[i]
+      const uint32_t t = p->t_inv_half(i, j);
       const E l = bbh::escale(bbh::eadd(v[0], v[1]), (bbh::P + 1) / 2);
       const E hh = bbh::escale(bbh::esub(v[0], v[1]), t);
       folded = bbh::eadd(l, bbh::emul(bbh::esub(hh, l), rr[i]));
     }
-    if (folded != fin) return BF_VERIFY_INVALID_QUERY;  // encode0(final)[q % n_0] = final
+    if (folded != pi0[q % p->n0()]) return BF_VERIFY_INVALID_QUERY;  // pi_0[idx % n_0] (basefold.rs:316-318)
   }
   return rd.off == proof_len ? BF_VERIFY_OK : BF_VERIFY_MALFORMED;
 }

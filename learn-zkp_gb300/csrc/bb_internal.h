@@ -20,11 +20,17 @@ constexpr int kBbMaxRounds = 27;  // num_vars + log2_c <= 27 (the two-adicity of
 
 // g^k * scale for k < n (Montgomery in, Montgomery out).
 cudaError_t bb_launch_pow_table(uint32_t* out, size_t n, uint32_t g_mont, uint32_t scale_mont, cudaStream_t st);
-// encode_batch of a 2^d x w matrix into its 2^(d+log2_c) x w codeword
-// (Montgomery).  `tw` holds the DIT twiddles, tw[2^s - 1 + k] = g_s^k.  A
-// data word >= p sets *bad.
-cudaError_t bb_launch_encode(const uint32_t* m, uint32_t* cw, int d, int log2_c, size_t w, const uint32_t* tw,
-                             uint32_t* bad, cudaStream_t st);
+// encode_batch of a 2^(d + log2_k0) x w matrix into its 2^(d + log2_k0 +
+// log2_c) x w codeword (Montgomery).  `tw` holds the butterfly factors of
+// layer s at tw[2^s - 1 + k]: g_s^k for the Reed–Solomon code (log2_k0 = 0),
+// ts[s - log2_n0][k] for the generic code (`generic`), whose stage 0 is the
+// dense G_0.  A data word >= p sets *bad.
+cudaError_t bb_launch_encode(const uint32_t* m, uint32_t* cw, int d, int log2_c, int log2_k0, int generic, size_t w,
+                             const uint32_t* tw, uint32_t* bad, cudaStream_t st);
+// out[k] = in[k] in Montgomery form; *bad set for a word >= p.
+cudaError_t bb_launch_to_mont(const uint32_t* in, uint32_t* out, size_t n, uint32_t* bad, cudaStream_t st);
+// tinv[k] = (2 ts[k])^-1 (Montgomery); *bad set for a t that is 0 or >= p.
+cudaError_t bb_launch_tinv(const uint32_t* ts, uint32_t* tinv, size_t n, uint32_t* bad, cudaStream_t st);
 // Leaf of codeword row q (keccak256 of its w canonical words) at bitrev_bits(q).
 cudaError_t bb_launch_leaves_rows(const uint32_t* cw, uint4* leaves, size_t rows, size_t w, int bits,
                                   cudaStream_t st);
@@ -76,7 +82,7 @@ struct BbGather {
   uint8_t* out;
   size_t w;
   size_t rec_bytes;
-  int L, d, log2_c, nq;
+  int L, d, log2_n0, nq;  // round i's tree has n_0 << i leaves
 };
 cudaError_t bb_launch_gather(const BbGather& p, cudaStream_t st);
 

@@ -107,6 +107,39 @@ __global__ void bb_copy_mont_kernel(const uint32_t* in, uint32_t* out, size_t n,
   }
 }
 
+// The generic code's fold constants: (2 t)^-1 of every t (Montgomery out),
+// and a flag for a t that is zero or not canonical.
+__global__ void bb_tinv_kernel(const uint32_t* ts, uint32_t* tinv, size_t n, uint32_t* bad) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t t = ts[k];
+    if (t == 0 || t >= bb::P) atomicOr(bad, 1u);
+    const uint32_t t2 = bb::to_mont(bb::add(t % bb::P, t % bb::P));
+    tinv[k] = mont_pow(t2, bb::P - 2);  // Fermat: the inverse as a power, in Montgomery form
+  }
+}
+
+// GenericRandomFoldableCode stage 0 (generic.rs:73-86, 120-125): every
+// chunk of k_0 message rows times G_0, g_0[i][j] = i^j, into n_0 codeword
+// rows: w[b n_0 + i] = sum_j i^j m[b k_0 + j], column by column.
+__global__ void bb_stage0_kernel(const uint32_t* __restrict__ m, uint32_t* __restrict__ cw, size_t rows_out,
+                                 uint32_t w, int log2_k0, int log2_n0, uint32_t* bad) {
+  const size_t total = rows_out * w;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    const size_t x = e / w, c = e - x * w;
+    const size_t b = x >> log2_n0;
+    const uint32_t i = (uint32_t)(x & (((size_t)1 << log2_n0) - 1));
+    const uint32_t im = bb::to_mont(i);
+    uint32_t pw = bb::MONT_ONE, acc = 0;
+    for (int j = 0; j < (1 << log2_k0); ++j) {
+      const uint32_t v = m[((b << log2_k0) + j) * w + c];
+      if (v >= bb::P) atomicOr(bad, 1u);
+      acc = bb::add(acc, bb::mul(pw, bb::to_mont(v)));
+      pw = bb::mul(pw, im);
+    }
+    cw[e] = acc;
+  }
+}
+
 // ---- encode: radix-2 DIT of the bit-reversed, zero-padded columns -------------
 // encode_batch (reed_solomon.rs:71-75) = dft_batch(pad(bit_reverse_rows(m))).
 // A DIT with natural-order output takes its input in bit-reversed order,
@@ -418,7 +451,7 @@ __global__ void bb_gather_kernel(BbGather p) {
   wo += 2;
   for (int k = 0; k < d; ++k) {
     const int i = d - 1 - k;
-    const int li = p.log2_c + i;  // the round's tree has n_i = 2^li leaves
+    const int li = p.log2_n0 + i;  // the round's tree has n_i = 2^li leaves
     const uint64_t ni = (uint64_t)1 << li;
     const uint64_t j = idx & (ni - 1), sib = ((idx >> li) & 1) ^ 1;
     if (threadIdx.x == 0) {
@@ -463,17 +496,40 @@ static int ilog2_ceil(size_t v) {
   return r;
 }
 
-cudaError_t bb_launch_encode(const uint32_t* m, uint32_t* cw, int d, int log2_c, size_t w, const uint32_t* tw,
-                             uint32_t* bad, cudaStream_t st) {
-  const int L = d + log2_c;
-  if (L == 0) {
+cudaError_t bb_launch_tinv(const uint32_t* ts, uint32_t* tinv, size_t n, uint32_t* bad, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  bb_tinv_kernel<<<blocks_for(n, 256), 256, 0, st>>>(ts, tinv, n, bad);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t bb_launch_to_mont(const uint32_t* in, uint32_t* out, size_t n, uint32_t* bad, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  bb_copy_mont_kernel<<<blocks_for(n, 256), 256, 0, st>>>(in, out, n, bad);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t bb_launch_encode(const uint32_t* m, uint32_t* cw, int d, int log2_c, int log2_k0, int generic, size_t w,
+                             const uint32_t* tw, uint32_t* bad, cudaStream_t st) {
+  const int L = d + log2_c + log2_k0;
+  int lo = 0;  // the first DIT layer
+  if (generic) {
+    const int log2_n0 = log2_c + log2_k0;
+    const size_t rows = (size_t)1 << L;
+    bb_stage0_kernel<<<blocks_for(rows * w, 256), 256, 0, st>>>(m, cw, rows, (uint32_t)w, log2_k0, log2_n0, bad);
+    count_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    lo = log2_n0;  // the butterflies of ts[i-1] are layers log2_n0 + i - 1
+  } else if (L == 0) {
     bb_copy_mont_kernel<<<blocks_for(w, 256), 256, 0, st>>>(m, cw, w, bad);
     count_launch();
     return cudaGetLastError();
   }
   const int lc = ilog2_ceil(w < 32 ? w : 32);
   const unsigned chunks = (unsigned)((w + ((size_t)1 << lc) - 1) >> lc);
-  int lo = 0;
+  const int first = lo;
   while (lo < L) {
     int lu = 0;
     if (lo > 0)
@@ -484,7 +540,7 @@ cudaError_t bb_launch_encode(const uint32_t* m, uint32_t* cw, int d, int log2_c,
     BbPass p;
     p.s_lo = lo;
     p.T = T;
-    p.first = lo == 0;
+    p.first = !generic && lo == first;
     p.log2_c = log2_c;
     p.lu = lu;
     p.lc = lc;

@@ -25,7 +25,9 @@ def build(force: bool = False) -> str:
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
     cxx = os.environ.get("CXX", "g++")
-    flags = ["-O3", "-std=c++17", "-shared", "-fPIC", "-pthread", "-Wall"]
+    # no fused multiply-add contraction: the query-count formulas in double
+    # must round as the reference's Rust (which never contracts) does
+    flags = ["-O3", "-std=c++17", "-shared", "-fPIC", "-pthread", "-Wall", "-ffp-contract=off"]
     if platform.machine() in ("aarch64", "arm64"):
         flags += ["-march=armv8-a+crypto", "-DORACLE_PMULL"]
     tmp = LIB + ".tmp"

@@ -57,14 +57,17 @@ def lib():
         L.orc_bb_emul.argtypes = [u8p, u8p, u8p, sz]
         L.orc_bb_einv.argtypes = [u8p, u8p, sz]
         L.orc_bb_dft.argtypes = [C.c_int, C.POINTER(C.c_uint32), C.c_int]
-        L.orc_bb_num_queries.argtypes = [C.c_int, C.c_int]
+        L.orc_bb_num_queries.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
         L.orc_bb_num_queries.restype = sz
-        L.orc_bb_encode.argtypes = [C.c_int, C.c_int, sz, u8p, u8p]
-        L.orc_bb_commit.argtypes = [C.c_int, C.c_int, sz, u8p, u8p]
+        u32p = C.POINTER(C.c_uint32)
+        L.orc_bb_encode.argtypes = [C.c_int, C.c_int, C.c_int, u32p, sz, u8p, u8p]
+        L.orc_bb_commit.argtypes = [C.c_int, C.c_int, C.c_int, u32p, sz, u8p, u8p]
         L.orc_bb_eval.argtypes = [C.c_int, sz, u8p, u8p, u8p]
-        L.orc_bb_harness_prepare.argtypes = [C.c_int, C.c_int, sz, u8p, u8p, u8p, u8p, u8p, C.POINTER(sz)]
-        L.orc_bb_open.argtypes = [C.c_int, C.c_int, sz, u8p, u8p, u8p, u8p, sz, u8p, sz, C.POINTER(sz)]
-        L.orc_bb_verify.argtypes = [C.c_int, C.c_int, sz, u8p, u8p, u8p, u8p, sz, u8p, sz]
+        L.orc_bb_harness_prepare.argtypes = [C.c_int, C.c_int, C.c_int, u32p, sz, u8p, u8p, u8p, u8p, u8p,
+                                             C.POINTER(sz)]
+        L.orc_bb_open.argtypes = [C.c_int, C.c_int, C.c_int, u32p, sz, u8p, u8p, u8p, u8p, sz, u8p, sz,
+                                  C.POINTER(sz)]
+        L.orc_bb_verify.argtypes = [C.c_int, C.c_int, C.c_int, u32p, sz, u8p, u8p, u8p, u8p, sz, u8p, sz]
         _lib = L
     return _lib
 
@@ -361,8 +364,30 @@ def bb_dft(log_n: int, data, definition: bool = False):
     return d
 
 
-def bb_num_queries(log2_c: int, lam: int = 128) -> int:
-    return int(lib().orc_bb_num_queries(lam, log2_c))
+def bb_num_queries(log2_c: int, lam: int = 128, n: int = 0, log2_k0: int = 0, generic: bool = False) -> int:
+    """Queries of the Reed–Solomon code, or (generic) of the random foldable
+    code with num_vars n and log2_k0 (its distance bound depends on both)."""
+    return int(lib().orc_bb_num_queries(lam, n, log2_c, log2_k0, 1 if generic else 0))
+
+
+def bb_random_ts(n: int, log2_c: int, log2_k0: int, seed: int):
+    """t's of the generic code for rounds 0..d-1 back to back (n_0 << i each),
+    uniform nonzero BabyBears from a seeded generator (the reference draws
+    them from its caller's RNG)."""
+    d = n - log2_k0
+    total = (1 << (log2_c + log2_k0)) * ((1 << d) - 1)
+    rng = np.random.default_rng(seed)
+    return rng.integers(1, BB_P, size=max(total, 1), dtype=np.uint64).astype(np.uint32)[:total]
+
+
+def _code(ts):
+    """(pointer, keep-alive) of the generic code's t's, or a null pointer for Reed–Solomon."""
+    if ts is None:
+        return None, None
+    t = _u32(ts).reshape(-1)
+    if t.size == 0:
+        t = np.zeros(1, np.uint32)
+    return t.ctypes.data_as(C.POINTER(C.c_uint32)), t
 
 
 def _mat(data, n: int):
@@ -376,18 +401,20 @@ def _pt(point, n: int):
     return _u32(point).reshape(-1, 5) if n else np.zeros((1, 5), np.uint32)
 
 
-def bb_encode(n: int, log2_c: int, data):
-    """Codeword of each column; returns 2^(n+log2_c) x width (1-D for width 1)."""
+def bb_encode(n: int, log2_c: int, data, log2_k0: int = 0, ts=None):
+    """Codeword of each column; returns n_d x width (1-D for width 1)."""
     d, w = _mat(data, n)
     out = np.zeros(w << (n + log2_c), dtype=np.uint32)
-    assert lib().orc_bb_encode(n, log2_c, w, _pu(d), _pu(out)) == 0
+    tp, _keep = _code(ts)
+    assert lib().orc_bb_encode(n, log2_c, log2_k0, tp, w, _pu(d), _pu(out)) == 0
     return out if w == 1 else out.reshape(-1, w)
 
 
-def bb_commit(n: int, log2_c: int, data) -> bytes:
+def bb_commit(n: int, log2_c: int, data, log2_k0: int = 0, ts=None) -> bytes:
     d, w = _mat(data, n)
     root = np.zeros(32, dtype=np.uint8)
-    assert lib().orc_bb_commit(n, log2_c, w, _pu(d), _p(root)) == 0
+    tp, _keep = _code(ts)
+    assert lib().orc_bb_commit(n, log2_c, log2_k0, tp, w, _pu(d), _p(root)) == 0
     return root.tobytes()
 
 
@@ -399,26 +426,28 @@ def bb_eval(n: int, data, point):
     return out[0] if w == 1 else out
 
 
-def bb_harness_prepare(n: int, log2_c: int, data, point):
+def bb_harness_prepare(n: int, log2_c: int, data, point, log2_k0: int = 0, ts=None):
     d, w = _mat(data, n)
     root = np.zeros(32, dtype=np.uint8)
     val = np.zeros((w, 5), dtype=np.uint32)
     blob = np.zeros(128 + 20 * w, dtype=np.uint8)
     bl = C.c_size_t(blob.size)
-    assert lib().orc_bb_harness_prepare(n, log2_c, w, _pu(d), _pu(_pt(point, n)), _p(root), _pu(val), _p(blob),
-                                        C.byref(bl)) == 0
+    tp, _keep = _code(ts)
+    assert lib().orc_bb_harness_prepare(n, log2_c, log2_k0, tp, w, _pu(d), _pu(_pt(point, n)), _p(root), _pu(val),
+                                        _p(blob), C.byref(bl)) == 0
     return root.tobytes(), (val[0] if w == 1 else val), blob[: bl.value].tobytes()
 
 
-def bb_open(n: int, log2_c: int, data, point, value, blob: bytes) -> bytes:
+def bb_open(n: int, log2_c: int, data, point, value, blob: bytes, log2_k0: int = 0, ts=None) -> bytes:
     d, w = _mat(data, n)
     v, b = _u32(value).reshape(w, 5), _buf(blob)
+    tp, _keep = _code(ts)
     cap = 1 << 16
     while True:
         out = np.zeros(cap, dtype=np.uint8)
         ln = C.c_size_t(0)
-        rc = lib().orc_bb_open(n, log2_c, w, _pu(d), _pu(_pt(point, n)), _pu(v), _p(b), b.size, _p(out), cap,
-                               C.byref(ln))
+        rc = lib().orc_bb_open(n, log2_c, log2_k0, tp, w, _pu(d), _pu(_pt(point, n)), _pu(v), _p(b), b.size,
+                               _p(out), cap, C.byref(ln))
         if rc == -2:
             cap = ln.value
             continue
@@ -426,9 +455,11 @@ def bb_open(n: int, log2_c: int, data, point, value, blob: bytes) -> bytes:
         return out[: ln.value].tobytes()
 
 
-def bb_verify(n: int, log2_c: int, root: bytes, point, value, blob: bytes, proof: bytes) -> int:
+def bb_verify(n: int, log2_c: int, root: bytes, point, value, blob: bytes, proof: bytes, log2_k0: int = 0,
+              ts=None) -> int:
     """0 accepted; 1 final poly, 2 query, 3 Merkle path, 4 malformed."""
     v = _u32(value).reshape(-1, 5)
     r, b, pf = _buf(root), _buf(blob), _buf(proof)
-    return lib().orc_bb_verify(n, log2_c, v.shape[0], _p(r), _pu(_pt(point, n)), _pu(v), _p(b), b.size,
-                               _p(pf) if pf.size else _p(np.zeros(1, np.uint8)), pf.size)
+    tp, _keep = _code(ts)
+    return lib().orc_bb_verify(n, log2_c, log2_k0, tp, v.shape[0], _p(r), _pu(_pt(point, n)), _pu(v), _p(b),
+                               b.size, _p(pf) if pf.size else _p(np.zeros(1, np.uint8)), pf.size)

@@ -290,13 +290,20 @@ static std::vector<uint32_t> dft_definition(const std::vector<uint32_t>& a) {
 }
 
 // ---------------------------------------------------------------------------
-// ReedSolomonCode (reed_solomon.rs) with log2_k_0 = 0.
+// The two prime-field RandomFoldableCodes (code.rs:16-91): ReedSolomonCode
+// (reed_solomon.rs, log2_k_0 = 0) and GenericRandomFoldableCode with
+// reed_solomon_g_0_with_random_ts (generic.rs), whose random t's come from
+// the caller's RNG and are given here as arrays.
 // ---------------------------------------------------------------------------
 struct Code {
-  int lambda, log2_c, d;
-  std::vector<std::vector<uint32_t>> t_inv_halves;  // per i: (2 t_i^j)^-1, j < n_i
+  int lambda, log2_c, log2_k0 = 0, d;
+  bool generic = false;
+  std::vector<std::vector<uint32_t>> ts;            // generic: ts[i] has n_i entries
+  std::vector<std::vector<uint32_t>> t_inv_halves;  // per i: (2 t_i[j])^-1, j < n_i
+  // ReedSolomonCode::new (reed_solomon.rs:20-38): t_i[j] = g_i^j with
+  // g_i = two_adic_generator(log2_c + i + 1)
   Code(int lambda_, int log2_c_, int d_) : lambda(lambda_), log2_c(log2_c_), d(d_) {
-    for (int i = 0; i < d; ++i) {  // ReedSolomonCode::new (:20-38)
+    for (int i = 0; i < d; ++i) {
       const uint32_t g = two_adic_generator(log2_c + i + 1);
       std::vector<uint32_t> t((size_t)1 << (log2_c + i));
       uint32_t p = 1;
@@ -307,31 +314,95 @@ struct Code {
       t_inv_halves.push_back(std::move(t));
     }
   }
+  // reed_solomon_g_0_with_random_ts (generic.rs:43-71) with the random
+  // vectors given: ts_flat holds ts[0], ts[1], .., ts[d-1] back to back.
+  Code(int lambda_, int log2_c_, int log2_k0_, int d_, const uint32_t* ts_flat)
+      : lambda(lambda_), log2_c(log2_c_), log2_k0(log2_k0_), d(d_), generic(true) {
+    size_t off = 0;
+    for (int i = 0; i < d; ++i) {
+      std::vector<uint32_t> t(ts_flat + off, ts_flat + off + n_i(i)), inv(n_i(i));
+      off += n_i(i);
+      for (size_t j = 0; j < t.size(); ++j) inv[j] = finv(fadd(t[j], t[j]));
+      ts.push_back(std::move(t));
+      t_inv_halves.push_back(std::move(inv));
+    }
+  }
   size_t c() const { return (size_t)1 << log2_c; }
-  size_t n_d() const { return c() << d; }
-  size_t n_i(int i) const { return c() << i; }
-  int log2_n_d() const { return log2_c + d; }
-  // num_queries (:58-64)
+  size_t k0() const { return (size_t)1 << log2_k0; }
+  size_t n0() const { return c() * k0(); }
+  size_t n_d() const { return n0() << d; }
+  size_t n_i(int i) const { return n0() << i; }
+  int log2_n_d() const { return log2_c + log2_k0 + d; }
+  // Appendix C of ePrint 2023/1705 as generic.rs:24-39 computes it, with
+  // F::bits() = 31 for BabyBear.
+  static double z_c(double lambda, double log2_f, size_t c, int i, int log2_n_i) {
+    if (i == 0) return 1.0 / (double)c;
+    return z_c(lambda, log2_f, c, i - 1, log2_n_i - 1) * (log2_f / (log2_f - 1.001)) +
+           1.0 / (log2_f - 1.001) *
+               ((2.0 * (double)(log2_n_i - 1) + lambda) / (double)((uint64_t)1 << log2_n_i) + 0.6);
+  }
+  // num_queries (reed_solomon.rs:58-64, generic.rs:99-103): unique decoding,
+  // delta = 1 - distance / 3; Rust's saturating cast maps -inf, NaN and
+  // negatives to 0.
   size_t num_queries() const {
-    const double rel = 1.0 - 1.0 / (double)c();
+    const double rel = generic ? 1.0 - z_c((double)lambda, 31.0, c(), d, log2_n_d()) : 1.0 - 1.0 / (double)c();
     const double delta = 1.0 - rel / 3.0;
     const double q = std::ceil((double)lambda / -std::log2(delta));
-    if (!(q > 0) || !std::isfinite(q)) return 0;
+    if (!(q > 0)) return 0;
+    if (!std::isfinite(q) || q >= 1.8446744073709552e19) return SIZE_MAX;
     return (size_t)q;
   }
-  // encode_batch (:71-75): bit_reverse_rows, pad_to_height(n_d), dft_batch
+  // encode_batch of one column of k_0 << d entries.
   std::vector<uint32_t> encode(const std::vector<uint32_t>& m) const {
-    std::vector<uint32_t> a(n_d(), 0);
-    for (size_t r = 0; r < m.size(); ++r) a[r] = m[brev(r, d)];
-    return dft(a);
+    if (!generic) {  // reed_solomon.rs:71-75: bit_reverse_rows, pad_to_height(n_d), dft_batch
+      std::vector<uint32_t> a(n_d(), 0);
+      for (size_t r = 0; r < m.size(); ++r) a[r] = m[brev(r, d)];
+      return dft(a);
+    }
+    // generic.rs:118-140: every k_0-chunk times G_0 (g_0[i][j] = i^j), then
+    // the butterflies (l, r) -> (l + t r, l - t r) of ts[i-1] on the halves of
+    // every n_i-chunk, i = 1..d
+    std::vector<uint32_t> w(n_d(), 0);
+    for (size_t b = 0; b < ((size_t)1 << d); ++b)
+      for (size_t i = 0; i < n0(); ++i) {
+        uint32_t acc = 0, pw = 1;
+        for (size_t j = 0; j < k0(); ++j) {
+          acc = fadd(acc, fmul(pw, m[b * k0() + j]));
+          pw = fmul(pw, (uint32_t)i);
+        }
+        w[b * n0() + i] = acc;
+      }
+    for (int i = 1; i <= d; ++i) {
+      const size_t ni = n_i(i), half = ni / 2;
+      for (size_t base = 0; base < w.size(); base += ni)
+        for (size_t k = 0; k < half; ++k) {
+          const uint32_t l = w[base + k], r = fmul(w[base + half + k], ts[i - 1][k]);
+          w[base + k] = fadd(l, r);
+          w[base + half + k] = fsub(l, r);
+        }
+    }
+    return w;
   }
-  // interpolate (code.rs:79-84)
+  // encode0 (reed_solomon.rs:66-70, generic.rs:105-110): w = m G_0
+  std::vector<E> encode0(const std::vector<E>& m) const {
+    if (!generic) return std::vector<E>(c(), m[0]);
+    std::vector<E> w(n0());
+    for (size_t i = 0; i < n0(); ++i) {
+      uint32_t pw = 1;
+      for (size_t j = 0; j < m.size(); ++j) {
+        w[i] = eadd(w[i], escale(m[j], pw));
+        pw = fmul(pw, (uint32_t)i);
+      }
+    }
+    return w;
+  }
+  // interpolate (code.rs:86-91)
   E interpolate(int i, size_t j, const E& lo, const E& hi, const E& r) const {
     const E l = escale(eadd(lo, hi), INV2);
     const E h = escale(esub(lo, hi), t_inv_halves[i][j]);
     return eadd(l, emul(esub(h, l), r));
   }
-  // fold (code.rs:66-75)
+  // fold (code.rs:66-77)
   void fold(int i, std::vector<E>& w, const E& r) const {
     const size_t mid = w.size() / 2;
     for (size_t j = 0; j < mid; ++j) w[j] = interpolate(i, j, w[j], w[j + mid], r);
@@ -597,7 +668,7 @@ static std::vector<uint8_t> open(const Code& code, const Commitment& cm, const s
     pi_trees.push_back(build_tree(std::move(leaves)));
     pi_vals.push_back(pi);
     ch.observe(pi_trees.back().root().b, 32);
-    const std::vector<E> rp = pr.compute_round_poly(i, sc);
+    const std::vector<E> rp = pr.compute_round_poly(i + code.log2_k0, sc);  // round i + log2_k_0 (:356-361)
     const std::vector<E> c = {rp[0], rp[2]};  // Eval::compress_round_poly
     for (const E& e : c) ch.observe_e(e);
     const E x = ch.sample_e();
@@ -606,8 +677,9 @@ static std::vector<uint8_t> open(const Code& code, const Commitment& cm, const s
     comp.push_back(c);
     code.fold(i, pi, x);
   }
-  const E fin = pr.poly[0];
-  ch.observe_e(fin);
+  const std::vector<E> fin = pr.poly;  // into_ext_poly: the k_0 evaluations left
+  for (const E& e : fin) ch.observe_e(e);
+  if (code.encode0(fin) != pi) return {};  // debug_assert_eq!(encode0(final_poly), pi) (:189)
   const size_t Q = code.num_queries();
   std::vector<uint64_t> idx(Q);
   for (auto& v : idx) v = ch.sample_bits(code.log2_n_d());
@@ -617,8 +689,8 @@ static std::vector<uint8_t> open(const Code& code, const Commitment& cm, const s
     put_u64(b, c.size());
     for (const E& e : c) put_e(b, e);
   }
-  put_u64(b, 1);
-  put_e(b, fin);
+  put_u64(b, fin.size());
+  for (const E& e : fin) put_e(b, e);
   put_u64(b, pi_trees.size());
   for (const Tree& t : pi_trees) b.insert(b.end(), t.root().b, t.root().b + 32);
   put_u64(b, Q);
@@ -698,8 +770,9 @@ static int verify(const Code& code, const Digest& root, const std::vector<E>& po
     if (!rd.ok || c.size() != 2) return 4;
     for (E& e : c) e = rd.e();
   }
-  if (!rd.ok || rd.u64() != 1) return 4;
-  const E fin = rd.e();
+  if (!rd.ok || rd.u64() != code.k0()) return 4;
+  std::vector<E> fin(code.k0());
+  for (E& e : fin) e = rd.e();
   if (!rd.ok) return 4;
   std::vector<Digest> pi_comms(rd.u64());
   if (!rd.ok || pi_comms.size() != (size_t)d) return 4;
@@ -714,9 +787,15 @@ static int verify(const Code& code, const Digest& root, const std::vector<E>& po
     const E x = ch.sample_e();
     sc.reduce({comp[k][0], c1, comp[k][1]}, x);
   }
-  ch.observe_e(fin);
+  for (const E& e : fin) ch.observe_e(e);
   const std::vector<E> r = sc.r();
-  if (emul(fin, eq_eval(point.data(), r.data(), std::min(point.size(), r.size()))) != sc.value) return 1;
+  // evaluate(final_poly, point_lo) * eq_eval(point_hi, r) (:271-275)
+  const std::vector<E> point_lo(point.begin(), point.begin() + code.log2_k0);
+  const size_t nhi = point.size() - code.log2_k0;
+  if (emul(evaluate(fin, point_lo), eq_eval(point.data() + code.log2_k0, r.data(), std::min(nhi, r.size()))) !=
+      sc.value)
+    return 1;
+  const std::vector<E> pi0 = code.encode0(fin);
   const size_t Q = code.num_queries();
   std::vector<uint64_t> idx(Q);
   for (auto& v : idx) v = ch.sample_bits(code.log2_n_d());
@@ -753,7 +832,7 @@ static int verify(const Code& code, const Digest& root, const std::vector<E>& po
       if (!verify_path(pi_comms[k], leaf_pair(vals[0], vals[1]), j, p2, ni)) return 3;
       folded = code.interpolate(i, j, vals[0], vals[1], r[i]);  // r[i]: round i's challenge
     }
-    if (folded != fin) return 2;  // encode0(final)[q % n_0] = final
+    if (folded != pi0[q % code.n0()]) return 2;  // pi_0[idx % n_0] (:316-318)
   }
   return rd.off == len ? 0 : 4;
 }
@@ -790,25 +869,41 @@ int orc_bb_dft(int log_n, uint32_t* data, int definition) {
   std::memcpy(data, r.data(), 4 * r.size());
   return 0;
 }
-size_t orc_bb_num_queries(int lambda, int log2_c) { return Code(lambda, log2_c, 0).num_queries(); }
-static bool bad_size(int n, int log2_c, size_t w) { return n < 0 || log2_c < 0 || n + log2_c > 27 || w == 0; }
+// The code of a call: Reed–Solomon when ts is null (log2_k0 must be 0), else
+// the generic random foldable code with the given t's (d = n - log2_k0).
+static bool bad_size(int n, int log2_c, int log2_k0, size_t w) {
+  return n < 0 || log2_c < 0 || log2_k0 < 0 || log2_k0 > n || n + log2_c > 27 || w == 0;
+}
+static Code make_code(int n, int log2_c, int log2_k0, const uint32_t* ts) {
+  if (!ts) return Code(128, log2_c, n);
+  return Code(128, log2_c, log2_k0, n - log2_k0, ts);
+}
+size_t orc_bb_num_queries(int lambda, int n, int log2_c, int log2_k0, int generic) {
+  if (!generic) return Code(lambda, log2_c, 0).num_queries();
+  const int d = n - log2_k0;
+  std::vector<uint32_t> ts(((size_t)1 << (log2_c + log2_k0)) * (((size_t)1 << d) - 1) + 1, 1);
+  Code code(lambda, log2_c, log2_k0, d, ts.data());
+  return code.num_queries();
+}
 // Data is row-major, 2^n rows of `width` canonical BabyBears.
-int orc_bb_encode(int n, int log2_c, size_t width, const uint8_t* data, uint8_t* out) {
-  if (bad_size(n, log2_c, width)) return -1;
-  Code code(128, log2_c, n);
+int orc_bb_encode(int n, int log2_c, int log2_k0, const uint32_t* ts, size_t width, const uint8_t* data,
+                  uint8_t* out) {
+  if (bad_size(n, log2_c, log2_k0, width) || (!ts && log2_k0)) return -1;
+  const Code code = make_code(n, log2_c, log2_k0, ts);
   const Commitment cm = commit(code, load_u32s(data, width << n), width);
   std::memcpy(out, cm.cw.data(), 4 * cm.cw.size());
   return 0;
 }
-int orc_bb_commit(int n, int log2_c, size_t width, const uint8_t* data, uint8_t* root) {
-  if (bad_size(n, log2_c, width)) return -1;
-  Code code(128, log2_c, n);
+int orc_bb_commit(int n, int log2_c, int log2_k0, const uint32_t* ts, size_t width, const uint8_t* data,
+                  uint8_t* root) {
+  if (bad_size(n, log2_c, log2_k0, width) || (!ts && log2_k0)) return -1;
+  const Code code = make_code(n, log2_c, log2_k0, ts);
   const Commitment cm = commit(code, load_u32s(data, width << n), width);
   std::memcpy(root, cm.tree.root().b, 32);
   return 0;
 }
 int orc_bb_eval(int n, size_t width, const uint8_t* data, const uint8_t* point, uint8_t* out) {
-  if (bad_size(n, 0, width)) return -1;
+  if (bad_size(n, 0, 0, width)) return -1;
   const std::vector<E> v = eval(load_u32s(data, width << n), width, load_es(point, n));
   for (size_t c = 0; c < width; ++c) store_e(out + 20 * c, v[c]);
   return 0;
@@ -816,10 +911,10 @@ int orc_bb_eval(int n, size_t width, const uint8_t* data, const uint8_t* point, 
 // The reference harness (poly-commit/src/lib.rs:80-100): commit, observe the
 // root, evaluate at the point, observe the values; returns root, values and
 // the challenger state.
-int orc_bb_harness_prepare(int n, int log2_c, size_t width, const uint8_t* data, const uint8_t* point,
-                           uint8_t* root, uint8_t* values, uint8_t* blob, size_t* blob_len) {
-  if (bad_size(n, log2_c, width)) return -1;
-  Code code(128, log2_c, n);
+int orc_bb_harness_prepare(int n, int log2_c, int log2_k0, const uint32_t* ts, size_t width, const uint8_t* data,
+                           const uint8_t* point, uint8_t* root, uint8_t* values, uint8_t* blob, size_t* blob_len) {
+  if (bad_size(n, log2_c, log2_k0, width) || (!ts && log2_k0)) return -1;
+  const Code code = make_code(n, log2_c, log2_k0, ts);
   const std::vector<uint32_t> m = load_u32s(data, width << n);
   const Commitment cm = commit(code, m, width);
   Challenger ch;
@@ -834,10 +929,11 @@ int orc_bb_harness_prepare(int n, int log2_c, size_t width, const uint8_t* data,
   *blob_len = b.size();
   return 0;
 }
-int orc_bb_open(int n, int log2_c, size_t width, const uint8_t* data, const uint8_t* point, const uint8_t* values,
-                const uint8_t* blob, size_t blob_len, uint8_t* out, size_t cap, size_t* len) {
-  if (bad_size(n, log2_c, width)) return -1;
-  Code code(128, log2_c, n);
+int orc_bb_open(int n, int log2_c, int log2_k0, const uint32_t* ts, size_t width, const uint8_t* data,
+                const uint8_t* point, const uint8_t* values, const uint8_t* blob, size_t blob_len, uint8_t* out,
+                size_t cap, size_t* len) {
+  if (bad_size(n, log2_c, log2_k0, width) || (!ts && log2_k0)) return -1;
+  const Code code = make_code(n, log2_c, log2_k0, ts);
   Challenger ch;
   if (!Challenger::from_blob(blob, blob_len, ch)) return -1;
   const std::vector<uint32_t> m = load_u32s(data, width << n);
@@ -849,10 +945,11 @@ int orc_bb_open(int n, int log2_c, size_t width, const uint8_t* data, const uint
   std::memcpy(out, pf.data(), pf.size());
   return 0;
 }
-int orc_bb_verify(int n, int log2_c, size_t width, const uint8_t* root, const uint8_t* point, const uint8_t* values,
-                  const uint8_t* blob, size_t blob_len, const uint8_t* proof, size_t len) {
-  if (bad_size(n, log2_c, width)) return -1;
-  Code code(128, log2_c, n);
+int orc_bb_verify(int n, int log2_c, int log2_k0, const uint32_t* ts, size_t width, const uint8_t* root,
+                  const uint8_t* point, const uint8_t* values, const uint8_t* blob, size_t blob_len,
+                  const uint8_t* proof, size_t len) {
+  if (bad_size(n, log2_c, log2_k0, width) || (!ts && log2_k0)) return -1;
+  const Code code = make_code(n, log2_c, log2_k0, ts);
   Challenger ch;
   if (!Challenger::from_blob(blob, blob_len, ch)) return -1;
   Digest r;

@@ -109,3 +109,51 @@ def test_prime_entry_points_refuse_verifier_only_object(built_lib):
     assert e.value.code == -1
     with pytest.raises(bg.BasefoldGpuError):
         prime.BabyBearBasefold.setup(bg.BasefoldConfig(prime.ReedSolomonCode(128, 2, 26)), device=-1)
+
+
+@pytest.mark.parametrize("n,log2_c,log2_k0,w", [(0, 1, 0, 1), (1, 1, 1, 1), (3, 0, 1, 1), (4, 2, 2, 1), (6, 1, 2, 3),
+                                                (7, 2, 1, 9), (9, 1, 0, 1), (5, 1, 3, 2)])
+def test_host_verifier_generic_code_agrees_with_oracle(built_lib, n, log2_c, log2_k0, w):
+    """GenericRandomFoldableCode (generic.rs) with the reference test's
+    ranges (log2_c 0..3, log2_k_0 0..3 capped at num_vars, basefold.rs:
+    453-468): the library's query count and verifier against the oracle."""
+    from basefold_gpu import BasefoldConfig, prime
+
+    bg = built_lib
+    ts = O.bb_random_ts(n, log2_c, log2_k0, 31 + n)
+    kw = dict(log2_k0=log2_k0, ts=ts)
+    data = rnd((1 << n, w) if w > 1 else 1 << n, 41 + n + w)
+    point = rnd((n, 5), 51 + n)
+    root, values, blob = O.bb_harness_prepare(n, log2_c, data, point, **kw)
+    proof = O.bb_open(n, log2_c, data, point, values, blob, **kw)
+    code = prime.GenericRandomFoldableCode(128, log2_c, log2_k0, n - log2_k0, ts)
+    pcs = prime.BabyBearBasefold.setup(BasefoldConfig(code), device=-1)
+    assert pcs.num_queries() == O.bb_num_queries(log2_c, n=n, log2_k0=log2_k0, generic=True)
+    assert pcs.proof_size(w, 1) == len(proof)
+    ev = [prime.PrimePolyEvals(values, point)]
+    pcs.verify(root, ev, proof, bg.GenericChallenger.from_state(blob))
+    for pos in (len(proof) - 3, len(proof) // 2, 20, len(proof) - 30):
+        if not 0 <= pos < len(proof):
+            continue
+        bad = bytearray(proof)
+        bad[pos] ^= 0x10
+        want = O.bb_verify(n, log2_c, root, point, values, blob, bytes(bad), **kw)
+        if want == 0:
+            pcs.verify(root, ev, bytes(bad), bg.GenericChallenger.from_state(blob))
+            continue
+        with pytest.raises(bg.BasefoldError) as e:
+            pcs.verify(root, ev, bytes(bad), bg.GenericChallenger.from_state(blob))
+        assert e.value.code == want, (pos, e.value.kind, want)
+
+
+def test_generic_setup_validates_ts(built_lib):
+    from basefold_gpu import BasefoldConfig, prime
+
+    bg = built_lib
+    ts = O.bb_random_ts(4, 1, 1, 3)
+    bad = ts.copy()
+    bad[5] = 0
+    with pytest.raises(bg.BasefoldGpuError):
+        prime.BabyBearBasefold.setup(BasefoldConfig(prime.GenericRandomFoldableCode(128, 1, 1, 3, bad)), device=-1)
+    with pytest.raises(bg.BasefoldGpuError):
+        prime.BabyBearBasefold.setup(BasefoldConfig(prime.GenericRandomFoldableCode(128, 1, 1, 3, ts[:-1])), device=-1)

@@ -96,3 +96,34 @@ def test_rejects_non_canonical_and_zero_coordinate(built_lib):
         pcs.open(comm, [prime.PrimePolyEvals(values, point)], GenericChallenger.keccak256())
     assert e.value.code == -6
     assert pcs.open(comm, [], GenericChallenger.keccak256()) == bytes(32)  # basefold.rs:139-141
+
+
+def _check_generic(n, log2_c, log2_k0, w, seed):
+    from basefold_gpu import BasefoldConfig, GenericChallenger, prime
+
+    ts = O.bb_random_ts(n, log2_c, log2_k0, seed)
+    kw = dict(log2_k0=log2_k0, ts=ts)
+    data = rnd((1 << n, w) if w > 1 else 1 << n, seed + 1)
+    point = rnd((n, 5), seed + 2)
+    code = prime.GenericRandomFoldableCode(128, log2_c, log2_k0, n - log2_k0, ts)
+    pcs = prime.BabyBearBasefold.setup(BasefoldConfig(code), device=0)
+    comm = pcs.commit(data)
+    root, values, blob = O.bb_harness_prepare(n, log2_c, data, point, **kw)
+    assert comm.root == root
+    got = pcs.eval(comm, point)
+    assert np.array_equal(got, np.asarray(values).reshape(-1, 5))
+    ev = [prime.PrimePolyEvals(got, point)]
+    proof = pcs.open(comm, ev, GenericChallenger.from_state(blob))
+    assert proof == O.bb_open(n, log2_c, data, point, values, blob, **kw)
+    pcs.verify(root, ev, proof, GenericChallenger.from_state(blob))
+
+
+# (num_vars, log2_c, log2_k0, width): the reference test's log2_c 0..3 and
+# log2_k_0 0..3 (capped at num_vars), generic.rs via basefold.rs:453-468
+GENERIC = [(0, 0, 0, 1), (0, 2, 0, 2), (1, 1, 1, 1), (2, 0, 2, 1), (3, 1, 0, 1), (4, 2, 2, 1), (5, 1, 1, 3),
+           (6, 1, 2, 9), (7, 2, 0, 34), (8, 1, 2, 1), (9, 0, 1, 2), (12, 1, 2, 1), (16, 1, 1, 1), (11, 1, 1, 64)]
+
+
+@pytest.mark.parametrize("n,log2_c,log2_k0,w", GENERIC)
+def test_generic_code_matches_oracle(built_lib, n, log2_c, log2_k0, w):
+    _check_generic(n, log2_c, log2_k0, w, 3000 + 17 * n + 5 * log2_c + log2_k0 + w)
