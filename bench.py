@@ -45,6 +45,9 @@ def parse():
                     help="one product sumcheck of K polys over 2^N points, nothing else (for ncu)")
     ap.add_argument("--profile-verify", type=int, nargs=2, metavar=("N", "COUNT"),
                     help="one batched verify of COUNT proofs of 2^N evaluations, nothing else (for ncu)")
+    ap.add_argument("--profile-prime", type=int, nargs=3, metavar=("GENERIC", "LOG_N", "LOG_POLYS"),
+                    help="one prime-field commit + open (GENERIC 0: Reed-Solomon, 1: generic code with "
+                         "log2_k_0 = 3) of a 2^LOG_N x 2^LOG_POLYS BabyBear matrix, nothing else (for ncu)")
     return ap.parse_args()
 
 
@@ -633,6 +636,115 @@ def run_multi_column(bg, torch, device, log2_c, sizes, pcs, reps=3):
             "seconds": best, "verified": True}
 
 
+def prime_workload(bg, torch, device, generic, log_n, log_polys, log2_c=1, seed=7):
+    """The reference's prime-field bench setup (poly-commit/benches/poly-commit.rs:
+    27-58, 83-178): a 2^log_n x 2^log_polys matrix of uniform BabyBears, blowup
+    2^log2_c, Reed-Solomon code or the generic code with log2_k_0 = 3 (its t's
+    drawn from a seeded generator, as the bench draws them from its RNG); a
+    uniform point of the extension field."""
+    import numpy as np
+    from basefold_gpu import prime
+
+    w = 1 << log_polys
+    rng = np.random.default_rng(seed + log_n)
+    host = rng.integers(0, prime.P, size=w << log_n, dtype=np.uint64).astype(np.uint32)
+    point = rng.integers(0, prime.P, size=(log_n, 5), dtype=np.uint64).astype(np.uint32)
+    if generic:
+        lk = 3
+        d = log_n - lk
+        ts = rng.integers(1, prime.P, size=((1 << (log2_c + lk)) * ((1 << d) - 1)), dtype=np.uint64).astype(np.uint32)
+        code = prime.GenericRandomFoldableCode(128, log2_c, lk, d, ts)
+    else:
+        code = prime.ReedSolomonCode(128, log2_c, log_n)
+    pcs = prime.BabyBearBasefold.setup(bg.BasefoldConfig(code), device=device)
+    dev = torch.from_numpy(host.view(np.int32)).to(f"cuda:{device}")
+    return pcs, host, dev, point, w
+
+
+def prime_open(bg, pcs, comm, point):
+    """bench_open's measured call: open of one point with a fresh
+    GenericChallenger::keccak256() (poly-commit.rs:150-158)."""
+    from basefold_gpu import prime
+
+    vals = pcs.eval(comm, point)
+    return pcs.open(comm, [prime.PrimePolyEvals(vals, point)], bg.GenericChallenger.keccak256())
+
+
+def run_prime(bg, torch, device, sizes=(16, 17, 18, 19), log_polys=8, reps=3):
+    """Prime-field Basefold on the GPU at the reference's own prime bench
+    shapes: ms per commit (evaluations resident in HBM, and from pinned host
+    memory) and per open, both codes; every proof checked by the verifier.
+    CPU baseline: the oracle (single-threaded C++ restatement) at 2^14 rows,
+    timed beside the GPU at the same size."""
+    import numpy as np
+    from basefold_gpu import prime
+    from oracle import oracle as O
+
+    rows = []
+    for generic in (0, 1):
+        for log_n in sizes:
+            pcs, host, dev, point, w = prime_workload(bg, torch, device, generic, log_n, log_polys)
+            pin = torch.from_numpy(host.view(np.int32)).pin_memory()
+            comm = pcs.commit_device(dev.data_ptr(), w, keep=dev)
+            ch = bg.GenericChallenger.keccak256()
+            ch.observe(comm.root)
+            vals = pcs.eval(comm, point)
+            prime.observe_ext_slice(ch, vals)
+            proof = pcs.open(comm, [prime.PrimePolyEvals(vals, point)], ch.clone())
+            pcs.verify(comm.root, [prime.PrimePolyEvals(vals, point)], proof, ch.clone())
+            tc = to = th = float("inf")
+            for _ in range(reps):
+                torch.cuda.synchronize()
+                t = time.perf_counter()
+                c2 = pcs.commit_device(dev.data_ptr(), w, keep=dev)
+                tc = min(tc, time.perf_counter() - t)
+                c2.free()
+                t = time.perf_counter()
+                prime_open(bg, pcs, comm, point)
+                to = min(to, time.perf_counter() - t)
+                t = time.perf_counter()
+                c3 = pcs.commit(pin.numpy())
+                th = min(th, time.perf_counter() - t)
+                c3.free()
+            rows.append([["reed_solomon", "generic_k0_8"][generic], log_n, round(1e3 * tc, 2), round(1e3 * to, 2),
+                         round(1e3 * th, 2), len(proof)])
+            comm.free()
+            release(dev, pin)
+    # CPU: the oracle at 2^14 x 256 (Reed-Solomon), against the GPU at the same size
+    n_cpu = 14
+    pcs, host, dev, point, w = prime_workload(bg, torch, device, 0, n_cpu, log_polys)
+    data = host.reshape(-1, w)
+    t = time.perf_counter()
+    root, vals, blob = O.bb_harness_prepare(n_cpu, 1, data, point)
+    cpu_commit = time.perf_counter() - t
+    t = time.perf_counter()
+    cpu_proof = O.bb_open(n_cpu, 1, data, point, vals, blob)
+    cpu_open = time.perf_counter() - t - cpu_commit  # the oracle's open recommits first
+    comm = pcs.commit_device(dev.data_ptr(), w, keep=dev)
+    assert comm.root == root
+    gpu_proof = pcs.open(comm, [prime.PrimePolyEvals(vals, point)], bg.GenericChallenger.from_state(blob))
+    assert gpu_proof == cpu_proof
+    tc = to = float("inf")
+    for _ in range(reps):
+        t = time.perf_counter()
+        c2 = pcs.commit_device(dev.data_ptr(), w, keep=dev)
+        tc = min(tc, time.perf_counter() - t)
+        c2.free()
+        t = time.perf_counter()
+        prime_open(bg, pcs, comm, point)
+        to = min(to, time.perf_counter() - t)
+    comm.free()
+    release(dev)
+    return {"workload": f"the reference's prime benches: commit / open of a 2^log_n x {1 << log_polys} BabyBear "
+                        "matrix, blowup 2, E = BabyBear^5; Reed-Solomon and generic (log2_k_0 = 3) codes",
+            "cols": ["code", "log_n", "commit_ms", "open_ms", "commit_from_host_ms", "proof_bytes"], "rows": rows,
+            "cpu_baseline": {"kind": "port", "cores": 1,
+                             "sample": f"oracle (C++ restatement, one thread) at 2^{n_cpu} x {1 << log_polys}, "
+                                       "Reed-Solomon; proof byte-identical to the GPU's",
+                             "commit_ms": round(1e3 * cpu_commit, 1), "open_ms": round(1e3 * cpu_open, 1),
+                             "gpu_commit_ms": round(1e3 * tc, 3), "gpu_open_ms": round(1e3 * to, 3)}}
+
+
 def served_cpu_reference(log2_c, size_range):
     """The served mix on the CPU reference path (C++ restatement, all host
     cores): one proof per size; sizes are uniform over the range, so the
@@ -675,6 +787,13 @@ def main():
         sc_pcs = bg.Basefold.setup(bg.BasefoldConfig(bg.BinaryReedSolomonCode(128, 1, 0)), device=local)
         sc_pcs.prove_sumcheck_device(k, ns, polys.data_ptr(), bg.rand.random_elems(1, 77),
                                      bg.GenericChallenger(b"sumcheck"))
+        torch.cuda.synchronize()
+        return
+    if args.profile_prime:
+        generic, pn, plog = args.profile_prime
+        ppcs, _, pdev, ppoint, pw = prime_workload(bg, torch, local, generic, pn, plog)
+        pcomm = ppcs.commit_device(pdev.data_ptr(), pw, keep=pdev)
+        prime_open(bg, ppcs, pcomm, ppoint)
         torch.cuda.synchronize()
         return
     if args.profile_verify:
@@ -769,7 +888,7 @@ def main():
     peaks, peak_kind = load_peaks()
     peak = float(peaks.get("hbm_gbs", 6800.0))
     num_sms = bg.device_info(local)["num_sms"]
-    batched = served = sweep = sumcheck = verify = latency = tuned = None
+    batched = served = sweep = sumcheck = verify = latency = tuned = prime_res = None
     if ws == 1 and not args.no_extras:
         latency = run_latency(bg, torch, local, log2_c)
         tuned = run_autotune(bg, torch, local, log2_c)
@@ -778,6 +897,7 @@ def main():
         sweep = run_commit_sweep(bg, torch, local)
         sumcheck = run_sumcheck(bg, torch, local)
         verify = run_verify(bg, local, log2_c)
+        prime_res = run_prime(bg, torch, local)
     cpu = None
     if not args.no_cpu_baseline and ws == 1:
         t = cpu_step_oracle(n, log2_c)
@@ -861,6 +981,8 @@ def main():
         line["verify"] = {"workload": verify["workload"], "gpu_proofs_per_s": round(verify["gpu_proofs_per_s"]),
                           "cpu_proofs_per_s": round(verify["cpu_baseline"]["proofs_per_s"]),
                           "cpu_cores": verify["cpu_baseline"]["cores"], "speedup": round(verify["speedup"], 1)}
+    if prime_res:
+        line["prime"] = prime_res
     if batched:
         mc = batched["multi_column"]
         line["batched"] = {"workload": batched["workload"],

@@ -158,8 +158,12 @@ class BabyBearBasefold:
         return 1 << self.num_vars
 
     def commit(self, data) -> PrimeCommitmentData:
-        """commit (basefold.rs:112-120) of host evaluations: 2^d rows x width."""
-        d = np.ascontiguousarray(np.asarray(data, dtype=np.uint32))
+        """commit (basefold.rs:112-120) of host evaluations: 2^d rows x width.
+        A 4-byte integer array is passed as it lies (no copy), so pinned
+        buffers keep their fast copy path."""
+        d = np.asarray(data)
+        d = d.view(np.uint32) if d.dtype in (np.int32, np.uint32) else d.astype(np.uint32)
+        d = np.ascontiguousarray(d)
         width = d.size // self._rows()
         if width == 0 or width * self._rows() != d.size:
             raise ValueError(f"{d.size} evaluations is not a multiple of 2^{self.num_vars} rows")

@@ -343,7 +343,7 @@ int bf_bb_eval(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, u
   CU(cudaMemcpyAsync(p->pin.p, acc, acc_bytes, cudaMemcpyDeviceToHost, p->stream));
   CU(cudaStreamSynchronize(p->stream));
   const unsigned long long* s = reinterpret_cast<const unsigned long long*>(p->pin.p);
-  for (size_t c = 0; c < w; ++c) bbh::store(values + 20 * c, bbh::from_dev_sums(s + 5 * c));
+  for (size_t c = 0; c < w; ++c) bbh::store(values + 20 * c, bbh::from_canonical_sums(s + 5 * c));
   return BF_OK;
 }
 
@@ -407,13 +407,17 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
   } else {
     const std::vector<E> s = bbh::scalars_by_eq(w, tr);
     for (size_t c = 0; c < w; ++c) claim = bbh::eadd(claim, bbh::emul(s[c], vals[c]));
-    std::vector<bb::E5> sd(w);
-    for (size_t c = 0; c < w; ++c) sd[c] = bbh::to_dev(s[c]);
+    // s R^2 against the canonical evaluations, s R against the Montgomery codeword
+    std::vector<bb::E5> sd(2 * w);
+    for (size_t c = 0; c < w; ++c) {
+      sd[c] = bbh::to_dev2(s[c]);
+      sd[w + c] = bbh::to_dev(s[c]);
+    }
     DevBuf sdev;
-    CU(sdev.alloc(20 * w));
-    CU(cudaMemcpyAsync(sdev.p, sd.data(), 20 * w, cudaMemcpyHostToDevice, st));
-    CU(bf::bb_launch_combine(cm->data.as<uint32_t>(), 1, rows, w, sdev.as<uint32_t>(), polyE, st));
-    CU(bf::bb_launch_combine(cm->cw.as<uint32_t>(), 0, p->n_d(), w, sdev.as<uint32_t>(), piE, st));
+    CU(sdev.alloc(40 * w));
+    CU(cudaMemcpyAsync(sdev.p, sd.data(), 40 * w, cudaMemcpyHostToDevice, st));
+    CU(bf::bb_launch_combine(cm->data.as<uint32_t>(), rows, w, sdev.as<uint32_t>(), polyE, st));
+    CU(bf::bb_launch_combine(cm->cw.as<uint32_t>(), p->n_d(), w, sdev.as<uint32_t>() + 5 * w, piE, st));
     CU(cudaStreamSynchronize(st));  // sd and sdev go out of scope
     poly = polyE;
     pi = piE;
@@ -448,7 +452,7 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
     bfh::digest_from_interleaved(p->pin.b() + 64, root.data());
     tr.observe(root.data(), 32);
     E rp[3];
-    es.round_poly((size_t)ri, sc, bbh::from_dev_sums(sums), rp);
+    es.round_poly((size_t)ri, sc, base_k ? bbh::from_canonical_sums(sums) : bbh::from_dev_sums(sums), rp);
     bbh::observe_e(tr, rp[0]);  // Eval::compress_round_poly keeps c0 and c2
     bbh::observe_e(tr, rp[2]);
     const E x = bbh::sample_e(tr);

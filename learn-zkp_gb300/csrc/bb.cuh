@@ -16,23 +16,34 @@
 namespace bb {
 
 constexpr uint32_t P = 2013265921u;        // 0x78000001
-constexpr uint32_t P_NEG_INV = 0x77ffffffu;  // -p^-1 mod 2^32
+constexpr uint32_t P_INV = 0x88000001u;      // p^-1 mod 2^32
 constexpr uint32_t R2 = 0x45dddde3u;        // R^2 mod p (to Montgomery form)
 constexpr uint32_t MONT_ONE = 0x0ffffffeu;  // R mod p
 constexpr uint32_t MONT_INV2 = 0x07ffffffu; // 2^-1 R mod p
 constexpr uint32_t W = 2;                   // X^5 = W
 
+__host__ __device__ __forceinline__ uint32_t umin(uint32_t a, uint32_t b) { return a < b ? a : b; }
+// a + b mod p for a, b < p: with s = a + b < 2^32, s - p wraps above s
+// exactly when s < p, so the smaller of the two is the reduced sum.
 __host__ __device__ __forceinline__ uint32_t add(uint32_t a, uint32_t b) {
-  const uint32_t s = a + b;  // < 2^32 since a, b < p < 2^31
-  return s >= P ? s - P : s;
+  const uint32_t s = a + b;
+  return umin(s, s - P);
 }
-__host__ __device__ __forceinline__ uint32_t sub(uint32_t a, uint32_t b) { return a >= b ? a - b : a + P - b; }
-// Montgomery product a b R^-1 mod p of a, b < p.
+// a - b mod p: d = a - b wraps above 2^31 > p when a < b, and then d + p
+// wraps back into [0, p).
+__host__ __device__ __forceinline__ uint32_t sub(uint32_t a, uint32_t b) {
+  const uint32_t d = a - b;
+  return umin(d, d + P);
+}
+// Montgomery product a b R^-1 mod p of a, b < p (R = 2^32): with t = a b and
+// m = t p^-1 mod R, m p has the low word of t, so (t - m p) / R is
+// hi(t) - hi(m p), in (-p, p); a negative difference wraps and gets p added.
 __host__ __device__ __forceinline__ uint32_t mul(uint32_t a, uint32_t b) {
   const uint64_t t = (uint64_t)a * b;
-  const uint32_t m = (uint32_t)t * P_NEG_INV;
-  const uint32_t u = (uint32_t)((t + (uint64_t)m * P) >> 32);
-  return u >= P ? u - P : u;
+  const uint32_t m = (uint32_t)t * P_INV;
+  const uint32_t mh = (uint32_t)(((uint64_t)m * P) >> 32);
+  const uint32_t d = (uint32_t)(t >> 32) - mh;
+  return umin(d, d + P);
 }
 __host__ __device__ __forceinline__ uint32_t to_mont(uint32_t a) { return mul(a, R2); }
 __host__ __device__ __forceinline__ uint32_t from_mont(uint32_t a) { return mul(a, 1u); }

@@ -115,6 +115,16 @@ inline E from_dev_sums(const unsigned long long s[5]) {  // Montgomery coefficie
   for (int i = 0; i < 5; ++i) r.c[i] = bb::from_mont((uint32_t)(s[i] % P));
   return r;
 }
+inline E from_canonical_sums(const unsigned long long s[5]) {
+  E r;
+  for (int i = 0; i < 5; ++i) r.c[i] = (uint32_t)(s[i] % P);
+  return r;
+}
+inline bb::E5 to_dev2(const E& e) {  // e R^2 coefficient-wise: mul(e R^2, v) = e v R for canonical v
+  bb::E5 r;
+  for (int i = 0; i < 5; ++i) r.c[i] = bb::to_mont(bb::to_mont(e.c[i]));
+  return r;
+}
 
 // MultiPoly::eq (p3/src/poly/multilinear.rs:41-64, 216-222) on the host.
 inline std::vector<E> eq_table(const std::vector<E>& x, const E& scalar) {

@@ -38,18 +38,19 @@ cudaError_t bb_launch_leaves_rows(const uint32_t* cw, uint4* leaves, size_t rows
 // base-field Montgomery when `base`), at bitrev_bits(j).
 cudaError_t bb_launch_leaves_pairs(const uint32_t* pi, int base, uint4* leaves, size_t half, int bits,
                                    cudaStream_t st);
-// out[r] = sum_c scalars[c] * src[r w + c] (extension out); `canonical`:
-// src holds canonical words (the evaluations), else Montgomery (the codeword).
-cudaError_t bb_launch_combine(const uint32_t* src, int canonical, size_t rows, size_t w, const uint32_t* scalars,
-                              uint32_t* out, cudaStream_t st);
+// out[r] = sum_c mul(scalars[c], src[r w + c]) (extension out, Montgomery):
+// pass s R for a Montgomery source (the codeword), s R^2 for canonical
+// evaluations.
+cudaError_t bb_launch_combine(const uint32_t* src, size_t rows, size_t w, const uint32_t* scalars, uint32_t* out,
+                              cudaStream_t st);
 // acc[5 c + k] += coefficient k of sum_r eq[r] * data[r w + c] (canonical data,
-// Montgomery sums, reduced by the caller).
+// canonical sums, reduced by the caller).
 cudaError_t bb_launch_eval_cols(const uint32_t* eq, const uint32_t* data, size_t rows, size_t w,
                                 unsigned long long* acc, cudaStream_t st);
 // ev[h + k] = ev[k] x; ev[k] -= ev[h + k] for k < h.
 cudaError_t bb_launch_eq_expand(uint32_t* ev, size_t h, const bb::E5& x, cudaStream_t st);
 // acc[k] += coefficient k of sum_{b < n} heq[b] * poly[b]; poly is canonical
-// base-field data when `base`, else extension.
+// base-field data when `base` (canonical sums), else extension (Montgomery sums).
 cudaError_t bb_launch_dot(const uint32_t* heq, const uint32_t* poly, int base, size_t n, unsigned long long* acc,
                           cudaStream_t st);
 // out[b] = in[b] + x (in[b + half] - in[b]); `base`: in is canonical data.

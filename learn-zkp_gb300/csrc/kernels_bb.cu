@@ -10,6 +10,7 @@
 // ALU; nothing here is GEMM-shaped.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "bb.cuh"
@@ -155,38 +156,82 @@ __global__ void bb_stage0_kernel(const uint32_t* __restrict__ m, uint32_t* __res
 // differ in bit s and multiplies by g_s^(x mod 2^s), g_s of order 2^(s+1).
 struct BbPass {
   int s_lo, T, first, log2_c, lu, lc;
-  uint32_t w;
+  uint32_t w, chunks;  // row width; column chunks of 2^lc
 };
+
+// Tile coordinates of a block: the column chunk is the fastest-varying part
+// of the (flat) block index, so the chunks of the same rows run together and
+// read whole rows of the row-major matrix.
+struct BbTile {
+  uint32_t u_blk, c0;
+  uint64_t hi;
+  __device__ __forceinline__ BbTile(const BbPass& p) {
+    const uint32_t chunk = blockIdx.x % p.chunks, t = blockIdx.x / p.chunks;
+    const uint32_t nub_log = (uint32_t)(p.s_lo - p.lu);
+    u_blk = t & ((1u << nub_log) - 1u);
+    hi = t >> nub_log;
+    c0 = chunk << p.lc;
+  }
+  __device__ __forceinline__ uint64_t row(const BbPass& p, uint32_t e) const {
+    const int ic = p.lu + p.lc;
+    const uint32_t uu = (e >> p.lc) & ((1u << p.lu) - 1u), a = e >> ic;
+    return (hi << (p.s_lo + p.T)) | ((uint64_t)a << p.s_lo) | ((u_blk << p.lu) | uu);
+  }
+};
+
+// Tile load: eight independent global loads per thread in flight before any
+// is used (the loop is latency-bound otherwise).  The first pass reads the
+// spread data rows (canonical, checked and converted); later passes the
+// codeword (Montgomery).
+__device__ __forceinline__ void bb_tile_load(uint32_t* tile, const uint32_t* __restrict__ m, const uint32_t* cw,
+                                             const BbPass& p, const BbTile& tl, uint32_t* bad) {
+  const uint32_t tsize = 1u << (p.T + p.lu + p.lc);
+  const uint64_t cmask = (1ull << p.log2_c) - 1ull;
+  for (uint32_t base = 0; base < tsize; base += 8 * blockDim.x) {
+    uint32_t v[8];
+    bool ok[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const uint32_t e = base + k * blockDim.x + threadIdx.x;
+      const uint64_t x = tl.row(p, e);
+      const uint32_t c = tl.c0 + (e & ((1u << p.lc) - 1u));
+      v[k] = 0;
+      ok[k] = e < tsize && c < p.w;
+      if (p.first) {
+        ok[k] = ok[k] && (x & cmask) == 0;
+        if (ok[k]) v[k] = m[(x >> p.log2_c) * p.w + c];
+      } else if (ok[k]) {
+        v[k] = cw[x * p.w + c];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const uint32_t e = base + k * blockDim.x + threadIdx.x;
+      if (p.first && ok[k]) {
+        if (v[k] >= bb::P) atomicOr(bad, 1u);
+        v[k] = bb::to_mont(v[k]);
+      }
+      if (e < tsize) tile[e] = v[k];
+    }
+  }
+}
+
+__device__ __forceinline__ void bb_tile_store(const uint32_t* tile, uint32_t* cw, const BbPass& p, const BbTile& tl) {
+  const uint32_t tsize = 1u << (p.T + p.lu + p.lc);
+  for (uint32_t e = threadIdx.x; e < tsize; e += blockDim.x) {
+    const uint32_t c = tl.c0 + (e & ((1u << p.lc) - 1u));
+    if (c < p.w) cw[tl.row(p, e) * p.w + c] = tile[e];
+  }
+}
 
 __global__ void __launch_bounds__(256) bb_dft_pass_kernel(const uint32_t* __restrict__ m, uint32_t* cw, BbPass p,
                                                          const uint32_t* __restrict__ tw, uint32_t* bad) {
   extern __shared__ uint32_t tile[];
   const int s_lo = p.s_lo, T = p.T, lu = p.lu, lc = p.lc, ic = lu + lc;
-  const uint32_t nub_log = (uint32_t)(s_lo - lu);
-  const uint32_t u_blk = blockIdx.x & ((1u << nub_log) - 1u);
-  const uint64_t hi = blockIdx.x >> nub_log;
-  const uint32_t c0 = blockIdx.y << lc;
-  const uint32_t w = p.w;
+  const BbTile tl(p);
+  const uint32_t u_blk = tl.u_blk;
   const uint32_t tsize = 1u << (T + ic);
-  const uint64_t cmask = (1ull << p.log2_c) - 1ull;
-  for (uint32_t e = threadIdx.x; e < tsize; e += blockDim.x) {
-    const uint32_t col = e & ((1u << lc) - 1u), uu = (e >> lc) & ((1u << lu) - 1u), a = e >> ic;
-    const uint64_t x = (hi << (s_lo + T)) | ((uint64_t)a << s_lo) | ((u_blk << lu) | uu);
-    const uint32_t c = c0 + col;
-    uint32_t v = 0;
-    if (c < w) {
-      if (p.first) {
-        if ((x & cmask) == 0) {
-          v = m[(x >> p.log2_c) * w + c];
-          if (v >= bb::P) atomicOr(bad, 1u);
-          v = bb::to_mont(v);
-        }
-      } else {
-        v = cw[x * w + c];
-      }
-    }
-    tile[e] = v;
-  }
+  bb_tile_load(tile, m, cw, p, tl, bad);
   __syncthreads();
   for (int l = 0; l < T; ++l) {
     const int s = s_lo + l;
@@ -204,12 +249,63 @@ __global__ void __launch_bounds__(256) bb_dft_pass_kernel(const uint32_t* __rest
     }
     __syncthreads();
   }
-  for (uint32_t e = threadIdx.x; e < tsize; e += blockDim.x) {
-    const uint32_t col = e & ((1u << lc) - 1u), uu = (e >> lc) & ((1u << lu) - 1u), a = e >> ic;
-    const uint64_t x = (hi << (s_lo + T)) | ((uint64_t)a << s_lo) | ((u_blk << lu) | uu);
-    const uint32_t c = c0 + col;
-    if (c < w) cw[x * w + c] = tile[e];
+  bb_tile_store(tile, cw, p, tl);
+}
+
+// Register-blocked form of the same pass for tiles whose (u, column) slots
+// fill a warp (lu + lc = 5): lane = slot, and a warp takes 2^R rows of its
+// slots into registers and runs R layers there per round trip through
+// shared memory (R = 4: two round trips per 8-layer pass instead of eight).
+// Every shared-memory access of a warp is one 128-byte row run.
+template <int R>
+__device__ __forceinline__ void bb_reg_group(uint32_t* tile, uint32_t q, int l0, int s_lo, uint32_t u, uint32_t lane,
+                                             const uint32_t* __restrict__ tw) {
+  const uint32_t a_base = ((q >> l0) << (l0 + R)) | (q & ((1u << l0) - 1u));
+  uint32_t v[1 << R];
+#pragma unroll
+  for (int j = 0; j < (1 << R); ++j) v[j] = tile[((a_base | ((uint32_t)j << l0)) << 5) | lane];
+#pragma unroll
+  for (int l = 0; l < R; ++l) {
+    const int s = s_lo + l0 + l;
+    const uint32_t* __restrict__ tws = tw + ((size_t)1 << s) - 1;
+    const uint32_t lmask = (1u << (l0 + l)) - 1u;
+#pragma unroll
+    for (int j0 = 0; j0 < (1 << R); ++j0) {
+      if (j0 & (1 << l)) continue;
+      const int j1 = j0 | (1 << l);
+      const uint32_t a0 = a_base | ((uint32_t)j0 << l0);
+      const uint32_t t = tws[((a0 & lmask) << s_lo) | u];
+      const uint32_t x1 = bb::mul(v[j1], t), x0 = v[j0];
+      v[j0] = bb::add(x0, x1);
+      v[j1] = bb::sub(x0, x1);
+    }
   }
+#pragma unroll
+  for (int j = 0; j < (1 << R); ++j) tile[((a_base | ((uint32_t)j << l0)) << 5) | lane] = v[j];
+}
+
+__global__ void __launch_bounds__(256) bb_dft_reg_kernel(const uint32_t* __restrict__ m, uint32_t* cw, BbPass p,
+                                                        const uint32_t* __restrict__ tw, uint32_t* bad) {
+  extern __shared__ uint32_t tile[];
+  const int s_lo = p.s_lo, T = p.T, lu = p.lu, lc = p.lc;  // lu + lc = 5
+  const BbTile tl(p);
+  bb_tile_load(tile, m, cw, p, tl, bad);
+  __syncthreads();
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const uint32_t u = (tl.u_blk << lu) | (lane >> lc);
+  for (int l0 = 0; l0 < T; l0 += 4) {
+    const int r = T - l0 < 4 ? T - l0 : 4;
+    for (uint32_t q = warp; q < (1u << (T - r)); q += nwarps) {
+      switch (r) {
+        case 4: bb_reg_group<4>(tile, q, l0, s_lo, u, lane, tw); break;
+        case 3: bb_reg_group<3>(tile, q, l0, s_lo, u, lane, tw); break;
+        case 2: bb_reg_group<2>(tile, q, l0, s_lo, u, lane, tw); break;
+        default: bb_reg_group<1>(tile, q, l0, s_lo, u, lane, tw); break;
+      }
+    }
+    __syncthreads();
+  }
+  bb_tile_store(tile, cw, p, tl);
 }
 
 // ---- leaves ------------------------------------------------------------------
@@ -279,24 +375,54 @@ __global__ void __launch_bounds__(128) bb_leaves_pairs_kernel(const uint32_t* __
 }
 
 // ---- rows combined with the batching scalars (basefold.rs:160-176) ------------
-// One warp per row, lanes over the columns; Montgomery form is linear, so the
-// integer sums of the products, reduced mod p, are the Montgomery form of the
-// dot product.
-__global__ void __launch_bounds__(256) bb_combine_kernel(const uint32_t* __restrict__ src, int canonical, size_t rows,
-                                                        uint32_t w, const uint32_t* __restrict__ scalars,
-                                                        uint32_t* __restrict__ out) {
-  const int lane = threadIdx.x & 31;
-  const size_t warps = (size_t)gridDim.x * (blockDim.x >> 5);
-  for (size_t r = (size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < rows; r += warps) {
+// One thread per row.  A block stages 128 rows x 32 columns through shared
+// memory with coalesced loads (each warp instruction reads one 128-byte row
+// run; 32 of them in flight per warp), then every thread multiplies its
+// row's 32 words by the scalars (shared, broadcast reads).  A product
+// mul(s', v) is s' v R^-1: the caller passes s' = s R for a Montgomery source
+// (the codeword) and s' = s R^2 for canonical evaluations, so every product
+// is the Montgomery form of s v without converting the source.  Montgomery
+// form is linear, so the integer sums, reduced mod p, are the Montgomery
+// form of the dot product.
+constexpr int kCombRows = 128, kCombCols = 32;
+__global__ void __launch_bounds__(kCombRows, 6) bb_combine_kernel(const uint32_t* __restrict__ src, size_t rows,
+                                                              uint32_t w, const uint32_t* __restrict__ scalars,
+                                                              uint32_t* __restrict__ out) {
+  __shared__ uint32_t stage[kCombRows * (kCombCols + 1)];
+  __shared__ uint32_t sc[5 * kCombCols];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (size_t r0 = (size_t)blockIdx.x * kCombRows; r0 < rows; r0 += (size_t)gridDim.x * kCombRows) {
     unsigned long long s[5] = {0, 0, 0, 0, 0};
-    for (uint32_t c = lane; c < w; c += 32) {
-      uint32_t v = src[r * w + c];
-      if (canonical) v = bb::to_mont(v);
+    for (uint32_t c0 = 0; c0 < w; c0 += kCombCols) {
+      __syncthreads();  // the previous chunk's reads are done
+      for (uint32_t t = threadIdx.x; t < 5 * kCombCols; t += blockDim.x) {
+        const uint32_t c = c0 + t / 5;
+        sc[t] = c < w ? scalars[5 * c0 + t] : 0u;
+      }
 #pragma unroll
-      for (int k = 0; k < 5; ++k) s[k] += bb::mul(scalars[5 * c + k], v);
+      for (int h = 0; h < 2; ++h) {  // warp w loads rows w, w + 4, ..: 16 loads in flight per lane
+        uint32_t v[kCombRows / 8];
+#pragma unroll
+        for (int k = 0; k < kCombRows / 8; ++k) {
+          const size_t r = r0 + warp + 4 * (k + h * kCombRows / 8);
+          const uint32_t c = c0 + lane;
+          v[k] = (r < rows && c < w) ? src[r * w + c] : 0u;
+        }
+#pragma unroll
+        for (int k = 0; k < kCombRows / 8; ++k)
+          stage[(warp + 4 * (k + h * kCombRows / 8)) * (kCombCols + 1) + lane] = v[k];
+      }
+      __syncthreads();
+      const uint32_t* row = stage + threadIdx.x * (kCombCols + 1);
+#pragma unroll 8
+      for (int c = 0; c < kCombCols; ++c) {
+        const uint32_t x = row[c];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) s[k] += bb::mul(sc[5 * c + k], x);
+      }
     }
-    warp_sum5(s);
-    if (lane == 0) {
+    const size_t r = r0 + threadIdx.x;
+    if (r < rows) {
       E5 e;
 #pragma unroll
       for (int k = 0; k < 5; ++k) e.c[k] = mod_p(s[k]);
@@ -306,7 +432,9 @@ __global__ void __launch_bounds__(256) bb_combine_kernel(const uint32_t* __restr
 }
 
 // ---- column evaluations (basefold.rs:126-131) ---------------------------------
-// Lane = column (32 per blockIdx.y), warps and blocks over the rows.
+// Lane = column (32 per blockIdx.y), warps and blocks over the rows.  The
+// data stay canonical and the eq table is Montgomery, so each product and
+// the sums are canonical.
 __global__ void __launch_bounds__(256) bb_eval_cols_kernel(const uint32_t* __restrict__ eq,
                                                           const uint32_t* __restrict__ data, size_t rows, uint32_t w,
                                                           unsigned long long* acc) {
@@ -315,10 +443,18 @@ __global__ void __launch_bounds__(256) bb_eval_cols_kernel(const uint32_t* __res
   const uint32_t c = blockIdx.y * 32 + lane;
   unsigned long long s[5] = {0, 0, 0, 0, 0};
   if (c < w) {
-    for (size_t r = (size_t)blockIdx.x * 8 + warp; r < rows; r += (size_t)gridDim.x * 8) {
-      const uint32_t v = bb::to_mont(data[r * w + c]);
+    const size_t step = (size_t)gridDim.x * 8;
+    for (size_t r = (size_t)blockIdx.x * 8 + warp; r < rows; r += 4 * step) {
+      uint32_t v[4];  // four rows' loads in flight before they are used
 #pragma unroll
-      for (int k = 0; k < 5; ++k) s[k] += bb::mul(eq[5 * r + k], v);
+      for (int q = 0; q < 4; ++q) v[q] = r + q * step < rows ? data[(r + q * step) * w + c] : 0u;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        if (r + q * step >= rows) break;
+        const size_t rr = r + q * step;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) s[k] += bb::mul(eq[5 * rr + k], v[q]);  // canonical: mul(eq R, v) = eq v
+      }
     }
   }
 #pragma unroll
@@ -346,13 +482,15 @@ __global__ void bb_eq_expand_kernel(uint32_t* ev, size_t h, E5 x) {
 }
 
 // sum_b heq[b] poly[b] (EvalImprProver::compute_round_poly, eval_impr.rs:
-// 187-197) as five Montgomery coefficient sums.
+// 187-197) as five coefficient sums: Montgomery for an extension poly,
+// canonical for canonical base-field data.
 __global__ void __launch_bounds__(256) bb_dot_kernel(const uint32_t* __restrict__ heq, const uint32_t* __restrict__ poly,
                                                     int base, size_t n, unsigned long long* acc) {
   unsigned long long s[5] = {0, 0, 0, 0, 0};
   for (size_t b = (size_t)blockIdx.x * blockDim.x + threadIdx.x; b < n; b += (size_t)gridDim.x * blockDim.x) {
     const E5 h = ld_e5(heq, b);
-    const E5 t = base ? bb::e_scale(h, bb::to_mont(poly[b])) : bb::e_mul(h, ld_e5(poly, b));
+    // base: canonical data times the Montgomery table gives canonical products
+    const E5 t = base ? bb::e_scale(h, poly[b]) : bb::e_mul(h, ld_e5(poly, b));
 #pragma unroll
     for (int k = 0; k < 5; ++k) s[k] += t.c[k];
   }
@@ -530,12 +668,31 @@ cudaError_t bb_launch_encode(const uint32_t* m, uint32_t* cw, int d, int log2_c,
   const int lc = ilog2_ceil(w < 32 ? w : 32);
   const unsigned chunks = (unsigned)((w + ((size_t)1 << lc) - 1) >> lc);
   const int first = lo;
-  while (lo < L) {
+  // U C <= 32 consecutive words per row run; tiles of 2^(T + lu + lc) <= 8192 words
+  auto lu_at = [&](int s_lo) {
     int lu = 0;
-    if (lo > 0)
-      while (lu < lo && lc + lu < 5) ++lu;  // U C <= 32 consecutive words per row run
-    int T = 13 - lc - lu;                   // tile of 2^(T + lu + lc) <= 8192 words
-    if (T > 12) T = 12;
+    if (s_lo > 0)
+      while (lu < s_lo && lc + lu < 5) ++lu;
+    return lu;
+  };
+  auto tmax_at = [&](int s_lo) { return std::min(12, 13 - lc - lu_at(s_lo)); };
+  // the greedy split's pass count, then the layers spread evenly over that
+  // many passes where the tiles allow (no short last pass of idle warps)
+  int passes = 0;
+  for (int x = lo; x < L; x += tmax_at(x)) ++passes;
+  while (lo < L) {
+    const int lu = lu_at(lo);
+    int T = (L - lo + passes - 1) / passes;
+    if (T > tmax_at(lo)) T = tmax_at(lo);
+    --passes;
+    if (passes > 0) {  // keep the rest reachable in the passes left
+      int reach = 0;
+      for (int x = lo + T, k = 0; k < passes && x < L; ++k) {
+        reach += tmax_at(x);
+        x += tmax_at(x);
+      }
+      if (lo + T + reach < L) T = tmax_at(lo);
+    }
     if (T > L - lo) T = L - lo;
     BbPass p;
     p.s_lo = lo;
@@ -545,12 +702,16 @@ cudaError_t bb_launch_encode(const uint32_t* m, uint32_t* cw, int d, int log2_c,
     p.lu = lu;
     p.lc = lc;
     p.w = (uint32_t)w;
+    p.chunks = chunks;
     const size_t words = (size_t)1 << (T + lu + lc);
     int threads = (int)(words / 2);
     if (threads > 256) threads = 256;
     if (threads < 32) threads = 32;
-    const dim3 grid((unsigned)((size_t)1 << (L - T - lu)), chunks);
-    bb_dft_pass_kernel<<<grid, threads, words * sizeof(uint32_t), st>>>(m, cw, p, tw, bad);
+    const size_t blocks = ((size_t)1 << (L - T - lu)) * chunks;  // chunk fastest (BbTile)
+    if (lu + lc == 5)  // a warp's lanes are one row run: registers take 4 layers per round trip
+      bb_dft_reg_kernel<<<(unsigned)blocks, 256, words * sizeof(uint32_t), st>>>(m, cw, p, tw, bad);
+    else
+      bb_dft_pass_kernel<<<(unsigned)blocks, threads, words * sizeof(uint32_t), st>>>(m, cw, p, tw, bad);
     count_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -576,9 +737,9 @@ cudaError_t bb_launch_leaves_pairs(const uint32_t* pi, int base, uint4* leaves, 
   return cudaGetLastError();
 }
 
-cudaError_t bb_launch_combine(const uint32_t* src, int canonical, size_t rows, size_t w, const uint32_t* scalars,
-                              uint32_t* out, cudaStream_t st) {
-  bb_combine_kernel<<<blocks_for(rows * 32, 256), 256, 0, st>>>(src, canonical, rows, (uint32_t)w, scalars, out);
+cudaError_t bb_launch_combine(const uint32_t* src, size_t rows, size_t w, const uint32_t* scalars, uint32_t* out,
+                              cudaStream_t st) {
+  bb_combine_kernel<<<blocks_for(rows, kCombRows), kCombRows, 0, st>>>(src, rows, (uint32_t)w, scalars, out);
   count_launch();
   return cudaGetLastError();
 }
