@@ -266,22 +266,36 @@ __device__ __forceinline__ void bb_reg_group(uint32_t* tile, uint32_t q, int l0,
   for (int j = 0; j < (1 << R); ++j) v[j] = tile[((a_base | ((uint32_t)j << l0)) << 5) | lane];
 #pragma unroll
   for (int l = 0; l < R; ++l) {
+    // The pair (j0, j0 | 2^l) at tile row a0 = a_base | j0 << l0 takes
+    // g_s^((a0 mod 2^(l0 + l)) << s_lo | u): its low bits come from a_base and
+    // from jj = j0 mod 2^l alone, so the layer needs 2^l distinct factors,
+    // table entries base + jj 2^(l0 + s_lo).
     const int s = s_lo + l0 + l;
-    const uint32_t* __restrict__ tws = tw + ((size_t)1 << s) - 1;
     const uint32_t lmask = (1u << (l0 + l)) - 1u;
+    const uint32_t base = (1u << s) - 1u + (((a_base & lmask) << s_lo) | u);  // 2^L - 1 words in all, L <= 27
+    uint32_t tf[1 << (R - 1)];
+#pragma unroll
+    for (int jj = 0; jj < (1 << l); ++jj) tf[jj] = tw[base + ((uint32_t)jj << (l0 + s_lo))];
 #pragma unroll
     for (int j0 = 0; j0 < (1 << R); ++j0) {
       if (j0 & (1 << l)) continue;
       const int j1 = j0 | (1 << l);
-      const uint32_t a0 = a_base | ((uint32_t)j0 << l0);
-      const uint32_t t = tws[((a0 & lmask) << s_lo) | u];
-      const uint32_t x1 = bb::mul(v[j1], t), x0 = v[j0];
+      const uint32_t x1 = bb::mul(v[j1], tf[j0 & ((1 << l) - 1)]), x0 = v[j0];
       v[j0] = bb::add(x0, x1);
       v[j1] = bb::sub(x0, x1);
     }
   }
 #pragma unroll
   for (int j = 0; j < (1 << R); ++j) tile[((a_base | ((uint32_t)j << l0)) << 5) | lane] = v[j];
+}
+
+// Layers of the register group starting at l0 of a T-layer tile: up to 4,
+// but no more than T - 3, so the group has 2^(T - r) >= 8 rows of work (one
+// per warp) where the tile allows.
+__device__ __forceinline__ int bb_group_layers(int T, int l0) {
+  int r = T - l0 < 4 ? T - l0 : 4;
+  const int cap = T - 3 > 1 ? T - 3 : 1;
+  return r < cap ? r : cap;
 }
 
 __global__ void __launch_bounds__(256) bb_dft_reg_kernel(const uint32_t* __restrict__ m, uint32_t* cw, BbPass p,
@@ -293,8 +307,8 @@ __global__ void __launch_bounds__(256) bb_dft_reg_kernel(const uint32_t* __restr
   __syncthreads();
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const uint32_t u = (tl.u_blk << lu) | (lane >> lc);
-  for (int l0 = 0; l0 < T; l0 += 4) {
-    const int r = T - l0 < 4 ? T - l0 : 4;
+  for (int l0 = 0, r; l0 < T; l0 += r) {
+    r = bb_group_layers(T, l0);
     for (uint32_t q = warp; q < (1u << (T - r)); q += nwarps) {
       switch (r) {
         case 4: bb_reg_group<4>(tile, q, l0, s_lo, u, lane, tw); break;
@@ -306,6 +320,79 @@ __global__ void __launch_bounds__(256) bb_dft_reg_kernel(const uint32_t* __restr
     __syncthreads();
   }
   bb_tile_store(tile, cw, p, tl);
+}
+
+// The same pass for matrices wider than 16 columns (lc = 5, lu = 0): a tile is
+// 2^T rows x 32 columns, row a of the tile at matrix row x0 + a 2^s_lo, and
+// each thread walks its rows with one pointer increment per element instead
+// of recomputing the row index and a 64-bit product (the general loader's
+// per-element address arithmetic dominated the pass's instruction count).
+__global__ void __launch_bounds__(256) bb_dft_wide_kernel(const uint32_t* __restrict__ m, uint32_t* cw, BbPass p,
+                                                         const uint32_t* __restrict__ tw, uint32_t* bad) {
+  extern __shared__ uint32_t tile[];
+  const int s_lo = p.s_lo, T = p.T;
+  const uint32_t chunk = blockIdx.x % p.chunks, t = blockIdx.x / p.chunks;
+  const uint32_t u = t & ((1u << s_lo) - 1u);
+  const uint64_t x0 = ((uint64_t)(t >> s_lo) << (s_lo + T)) | u;
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const uint32_t c = (chunk << 5) + lane;
+  const bool col_ok = c < p.w;
+  const uint32_t rows = 1u << T;
+  const size_t w = p.w;
+  if (p.first) {  // spread rows: tile row a holds data row (x0 + a) >> log2_c when its low log2_c bits are 0
+    const uint32_t cmask = (1u << p.log2_c) - 1u;
+    for (uint32_t a0 = warp; a0 < rows; a0 += 8 * nwarps) {
+      uint32_t v[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const uint32_t a = a0 + k * nwarps;
+        const uint64_t x = x0 + a;
+        v[k] = 0;
+        if (a < rows && col_ok && ((uint32_t)x & cmask) == 0) v[k] = m[(x >> p.log2_c) * w + c];
+      }
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const uint32_t a = a0 + k * nwarps;
+        if (v[k] >= bb::P) atomicOr(bad, 1u);
+        if (a < rows) tile[(a << 5) | lane] = bb::to_mont(v[k]);
+      }
+    }
+  } else {
+    const size_t stride = (size_t)nwarps << s_lo;  // rows between a thread's consecutive tile rows
+    const uint32_t* src = cw + (x0 + ((size_t)warp << s_lo)) * w + c;
+    for (uint32_t a0 = warp; a0 < rows; a0 += 8 * nwarps) {
+      uint32_t v[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        v[k] = (a0 + k * nwarps < rows && col_ok) ? src[0] : 0u;
+        src += stride * w;
+      }
+#pragma unroll
+      for (int k = 0; k < 8; ++k)
+        if (a0 + k * nwarps < rows) tile[((a0 + k * nwarps) << 5) | lane] = v[k];
+    }
+  }
+  __syncthreads();
+  for (int l0 = 0, r; l0 < T; l0 += r) {
+    r = bb_group_layers(T, l0);
+    for (uint32_t q = warp; q < (1u << (T - r)); q += nwarps) {
+      switch (r) {
+        case 4: bb_reg_group<4>(tile, q, l0, s_lo, u, lane, tw); break;
+        case 3: bb_reg_group<3>(tile, q, l0, s_lo, u, lane, tw); break;
+        case 2: bb_reg_group<2>(tile, q, l0, s_lo, u, lane, tw); break;
+        default: bb_reg_group<1>(tile, q, l0, s_lo, u, lane, tw); break;
+      }
+    }
+    __syncthreads();
+  }
+  if (col_ok) {
+    const size_t stride = ((size_t)nwarps << s_lo) * w;
+    uint32_t* dst = cw + (x0 + ((size_t)warp << s_lo)) * w + c;
+    for (uint32_t a = warp; a < rows; a += nwarps) {
+      *dst = tile[(a << 5) | lane];
+      dst += stride;
+    }
+  }
 }
 
 // ---- leaves ------------------------------------------------------------------
@@ -336,17 +423,30 @@ __global__ void __launch_bounds__(128) bb_leaves_rows_kernel(const uint32_t* __r
 #pragma unroll
     for (int i = 0; i < 25; ++i) s[i] = make_uint2(0, 0);
     for (uint32_t blk = 0; blk < nblk; ++blk) {
-      for (int e = lane; e < 32 * kRateWords; e += 32) {
-        const int rr = e / kRateWords, i = e - rr * kRateWords;
+      // word i of the block for row rr: the message word, the 0x01 pad
+      // word right after the message, and 0x80 in the block's last byte
+      auto word = [&](uint32_t rr, uint32_t i, uint32_t raw) {
         const uint32_t col = blk * kRateWords + i;
-        uint32_t v = 0;
-        if (col < w) {
-          if (r0 + rr < rows) v = bb::from_mont(cw[(r0 + rr) * w + col]);
-        } else if (col == w) {
-          v = 0x01u;
-        }
+        uint32_t v = col < w ? bb::from_mont(raw) : (col == w ? 0x01u : 0u);
         if (blk == nblk - 1 && i == kRateWords - 1) v |= 0x80000000u;
-        st[rr * kStagePitch + i] = v;
+        return v;
+      };
+      // words 0..31 of the 32 rows: a 128-byte run per row, 8 loads in flight
+      const uint32_t col = blk * kRateWords + lane;
+#pragma unroll 1
+      for (int h = 0; h < 32; h += 8) {
+        uint32_t raw[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) raw[k] = (col < w && r0 + h + k < rows) ? cw[(r0 + h + k) * w + col] : 0u;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) st[(h + k) * kStagePitch + lane] = word(h + k, lane, raw[k]);
+      }
+      // words 32 and 33: lane = row
+#pragma unroll
+      for (int i = 32; i < kRateWords; ++i) {
+        const uint32_t c2 = blk * kRateWords + i;
+        const uint32_t v = (c2 < w && r0 + lane < rows) ? cw[(r0 + lane) * w + c2] : 0u;
+        st[lane * kStagePitch + i] = word(lane, i, v);
       }
       __syncwarp();
 #pragma unroll
@@ -708,7 +808,9 @@ cudaError_t bb_launch_encode(const uint32_t* m, uint32_t* cw, int d, int log2_c,
     if (threads > 256) threads = 256;
     if (threads < 32) threads = 32;
     const size_t blocks = ((size_t)1 << (L - T - lu)) * chunks;  // chunk fastest (BbTile)
-    if (lu + lc == 5)  // a warp's lanes are one row run: registers take 4 layers per round trip
+    if (lc == 5)  // wider than 16 columns: tiles of whole 32-column runs
+      bb_dft_wide_kernel<<<(unsigned)blocks, 256, words * sizeof(uint32_t), st>>>(m, cw, p, tw, bad);
+    else if (lu + lc == 5)  // a warp's lanes are one row run: registers take 4 layers per round trip
       bb_dft_reg_kernel<<<(unsigned)blocks, 256, words * sizeof(uint32_t), st>>>(m, cw, p, tw, bad);
     else
       bb_dft_pass_kernel<<<(unsigned)blocks, threads, words * sizeof(uint32_t), st>>>(m, cw, p, tw, bad);
