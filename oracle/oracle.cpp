@@ -1234,6 +1234,9 @@ static void store_vec(uint8_t* p, const std::vector<u128>& v) {
 
 extern "C" {
 
+// The oracle's thread count, shared with the prime-field oracle.
+int orc_num_threads() { return num_threads(); }
+
 int orc_set_threads(int n) {
   g_threads = n > 0 ? n : 0;
   return num_threads();

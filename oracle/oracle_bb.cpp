@@ -23,11 +23,31 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 extern "C" void orc_keccak256(const uint8_t* msg, size_t len, uint8_t* out);
+extern "C" int orc_num_threads();
 
 namespace orb {
+
+// f(begin, end) over [0, n) in contiguous chunks on the oracle's threads.
+template <class F>
+static void parallel_for(size_t n, const F& f, size_t grain = 256) {
+  const int nt = orc_num_threads();
+  if (nt <= 1 || n <= grain) {
+    f((size_t)0, n);
+    return;
+  }
+  const size_t chunks = std::min<size_t>((size_t)nt, (n + grain - 1) / grain);
+  const size_t per = (n + chunks - 1) / chunks;
+  std::vector<std::thread> ts;
+  for (size_t c = 0; c < chunks; ++c) {
+    const size_t b = c * per, e = std::min(n, b + per);
+    if (b < e) ts.emplace_back([&f, b, e]() { f(b, e); });
+  }
+  for (auto& t : ts) t.join();
+}
 
 // ---------------------------------------------------------------------------
 // BabyBear (canonical u32 in [0, p)).
@@ -405,7 +425,9 @@ struct Code {
   // fold (code.rs:66-77)
   void fold(int i, std::vector<E>& w, const E& r) const {
     const size_t mid = w.size() / 2;
-    for (size_t j = 0; j < mid; ++j) w[j] = interpolate(i, j, w[j], w[j + mid], r);
+    parallel_for(mid, [&](size_t b, size_t e) {
+      for (size_t j = b; j < e; ++j) w[j] = interpolate(i, j, w[j], w[j + mid], r);
+    });
     w.resize(mid);
   }
 };
@@ -445,7 +467,9 @@ static Tree build_tree(std::vector<Digest> leaves) {
   while (t.layers.back().size() > 1) {
     const auto& prev = t.layers.back();
     std::vector<Digest> next(prev.size() / 2);
-    for (size_t i = 0; i < next.size(); ++i) next[i] = hash_node(prev[2 * i], prev[2 * i + 1]);
+    parallel_for(next.size(), [&](size_t b, size_t e) {
+      for (size_t i = b; i < e; ++i) next[i] = hash_node(prev[2 * i], prev[2 * i + 1]);
+    });
     t.layers.push_back(std::move(next));
   }
   return t;
@@ -600,23 +624,29 @@ static Commitment commit(const Code& code, const std::vector<uint32_t>& data, si
   Commitment cm;
   cm.w = w;
   cm.cw.assign(code.n_d() * w, 0);
-  for (size_t c = 0; c < w; ++c) {
-    const std::vector<uint32_t> col = code.encode(column(data, w, c));
-    for (size_t q = 0; q < col.size(); ++q) cm.cw[q * w + c] = col[q];
-  }
+  parallel_for(w, [&](size_t b, size_t e) {  // columns are independent
+    for (size_t c = b; c < e; ++c) {
+      const std::vector<uint32_t> col = code.encode(column(data, w, c));
+      for (size_t q = 0; q < col.size(); ++q) cm.cw[q * w + c] = col[q];
+    }
+  }, 1);
   std::vector<Digest> leaves(code.n_d());
-  for (size_t q = 0; q < leaves.size(); ++q) leaves[q] = leaf_row(cm.row(q), w);
+  parallel_for(leaves.size(), [&](size_t b, size_t e) {
+    for (size_t q = b; q < e; ++q) leaves[q] = leaf_row(cm.row(q), w);
+  });
   cm.tree = build_tree(std::move(leaves));
   return cm;
 }
 // eval (:126-131): every column's multilinear extension at the point
 static std::vector<E> eval(const std::vector<uint32_t>& data, size_t w, const std::vector<E>& point) {
   std::vector<E> out(w);
-  for (size_t c = 0; c < w; ++c) {
-    std::vector<E> ev(data.size() / w);
-    for (size_t i = 0; i < ev.size(); ++i) ev[i] = E::from(data[i * w + c]);
-    out[c] = evaluate(ev, point);
-  }
+  parallel_for(w, [&](size_t b, size_t e) {
+    for (size_t c = b; c < e; ++c) {
+      std::vector<E> ev(data.size() / w);
+      for (size_t i = 0; i < ev.size(); ++i) ev[i] = E::from(data[i * w + c]);
+      out[c] = evaluate(ev, point);
+    }
+  }, 1);
   return out;
 }
 // dot_product of extension scalars with a base-field row
@@ -650,9 +680,13 @@ static std::vector<uint8_t> open(const Code& code, const Commitment& cm, const s
     claim = values[0];
   } else {  // :160-176: rows combined with scalars sampled by eq
     const std::vector<E> s = scalars_by_eq(w, ch);
-    for (size_t i = 0; i < rows; ++i) poly[i] = dot_row(s, data.data() + i * w, w);
+    parallel_for(rows, [&](size_t b, size_t e) {
+      for (size_t i = b; i < e; ++i) poly[i] = dot_row(s, data.data() + i * w, w);
+    });
     for (size_t c = 0; c < w; ++c) claim = eadd(claim, emul(s[c], values[c]));
-    for (size_t q = 0; q < pi.size(); ++q) pi[q] = dot_row(s, cm.row(q), w);
+    parallel_for(pi.size(), [&](size_t b, size_t e) {
+      for (size_t q = b; q < e; ++q) pi[q] = dot_row(s, cm.row(q), w);
+    });
   }
   EvalProver pr(point, poly);
   if (!pr.ok) return {};
@@ -664,7 +698,9 @@ static std::vector<uint8_t> open(const Code& code, const Commitment& cm, const s
   for (int i = d - 1; i >= 0; --i) {  // prove_interleaved_folding_sumcheck (:335-369)
     const size_t mid = pi.size() / 2;
     std::vector<Digest> leaves(mid);
-    for (size_t j = 0; j < mid; ++j) leaves[j] = leaf_pair(pi[j], pi[j + mid]);
+    parallel_for(mid, [&](size_t b, size_t e) {
+      for (size_t j = b; j < e; ++j) leaves[j] = leaf_pair(pi[j], pi[j + mid]);
+    });
     pi_trees.push_back(build_tree(std::move(leaves)));
     pi_vals.push_back(pi);
     ch.observe(pi_trees.back().root().b, 32);

@@ -9,6 +9,9 @@
   compressed round polynomial, every challenge, the final evaluations and the
   final claim equal to the oracle's, plus the verifier identity and the final
   evaluations against direct multilinear evaluation at the challenges.
+* the prime-field scheme at the reference's largest prime bench shape (2^19
+  rows x 256 BabyBear columns, blowup 2), both prime codes: root, column values
+  and proof bytes equal to the oracle's.
 
 Tolerance: bit-exact (exact GF(2^128) and Keccak arithmetic)."""
 import os
@@ -128,3 +131,38 @@ def test_proof_2_26_blowup_4_verifies(built_lib):
     with pytest.raises(bg.BasefoldError):
         pcs.verify(comm.root, [bg.PolyEvals(values, point)], bytes(bad), ch.clone())
     comm.free()
+
+
+@pytest.mark.parametrize("generic", [0, 1])
+def test_prime_bench_shape_2_19_x_256_matches_oracle(built_lib, generic):
+    """The reference's largest prime bench shape (poly-commit/benches/poly-commit.rs:83-178:
+    log_n 19, 2^8 columns, C = 1): Reed–Solomon and the generic code with log2_k_0 = 3.
+    Root, the 256 column values and the whole proof byte-for-byte against the oracle (on all
+    host threads), and the proof accepted by the library's verifier."""
+    import torch
+    from basefold_gpu import BasefoldConfig, GenericChallenger, prime
+
+    n, log2_c, w = 19, 1, 256
+    O.set_threads(os.cpu_count() or 1)
+    rng = np.random.default_rng(1900 + generic)
+    data = rng.integers(0, O.BB_P, size=(1 << n, w), dtype=np.uint64).astype(np.uint32)
+    point = rng.integers(0, O.BB_P, size=(n, 5), dtype=np.uint64).astype(np.uint32)
+    kw = {}
+    if generic:
+        lk = 3
+        ts = O.bb_random_ts(n, log2_c, lk, 77)
+        kw = dict(log2_k0=lk, ts=ts)
+        code = prime.GenericRandomFoldableCode(128, log2_c, lk, n - lk, ts)
+    else:
+        code = prime.ReedSolomonCode(128, log2_c, n)
+    pcs = prime.BabyBearBasefold.setup(BasefoldConfig(code), device=0)
+    dev = torch.from_numpy(data.view(np.int32)).cuda()
+    comm = pcs.commit_device(dev.data_ptr(), w, keep=dev)
+    root, values, blob = O.bb_harness_prepare(n, log2_c, data, point, **kw)
+    assert comm.root == root
+    got = pcs.eval(comm, point)
+    assert np.array_equal(got, values)
+    ev = [prime.PrimePolyEvals(got, point)]
+    proof = pcs.open(comm, ev, GenericChallenger.from_state(blob))
+    assert proof == O.bb_open(n, log2_c, data, point, values, blob, **kw)
+    pcs.verify(root, ev, proof, GenericChallenger.from_state(blob))
