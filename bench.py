@@ -966,7 +966,7 @@ def main():
         "gpu_launches": launches,
         "proof_bytes": len(proof),
     }
-    # compact extras last: the driver keeps the end of the line
+    # compact extras last: a log that keeps only the end of a long line still holds them
     if trait:
         line["trait_route"] = trait
     if sweep:
