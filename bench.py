@@ -748,6 +748,45 @@ def run_prime(bg, torch, device, sizes=(16, 17, 18, 19), log_polys=8, reps=3):
                              "gpu_commit_ms": round(1e3 * tc, 3), "gpu_open_ms": round(1e3 * to, 3)}}
 
 
+def run_binary_wide(bg, torch, device, sizes=(16, 17, 18, 19), log_polys=8, reps=3):
+    """The reference's binary benches at their own shape (poly-commit/benches/
+    poly-commit.rs:60-74, 83-178: basefold_binary_reed_solomon_polyval, a
+    2^log_n x 2^log_polys matrix, C = 1): ms per commit (evaluations in HBM)
+    and per open with a fresh keccak256 challenger, every proof verified."""
+    w = 1 << log_polys
+    rows = []
+    for n in sizes:
+        pcs = bg.Basefold.setup(bg.BasefoldConfig(bg.BinaryReedSolomonCode(128, 1, n)), device=device)
+        data = bg.rand.random_elems((w << n) + n, 40 + n)
+        evals, point = data[: w << n], data[w << n:]
+        dev = torch.from_numpy(evals).to(f"cuda:{device}")
+        comm = pcs.commit_device(dev.data_ptr(), width=w, keep=dev)
+        vals = pcs.eval(pcs.data(comm), point)
+        ch = bg.GenericChallenger.keccak256()
+        ch.observe(comm.root)
+        ch.observe_ext_slice(vals)
+        proof = pcs.open(comm, [bg.PolyEvals(vals, point)], ch.clone())
+        pcs.verify(comm.root, [bg.PolyEvals(vals, point)], proof, ch.clone())
+        tc = to = te = float("inf")
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            c2 = pcs.commit_device(dev.data_ptr(), width=w, keep=dev)
+            tc = min(tc, time.perf_counter() - t)
+            c2.free()
+            t = time.perf_counter()
+            pcs.eval(pcs.data(comm), point)
+            te = min(te, time.perf_counter() - t)
+            t = time.perf_counter()
+            pcs.open(comm, [bg.PolyEvals(vals, point)], bg.GenericChallenger.keccak256())
+            to = min(to, time.perf_counter() - t)
+        rows.append([n, round(1e3 * tc, 2), round(1e3 * te, 2), round(1e3 * to, 2)])
+        comm.free()
+        release(pcs, dev)
+    return {"workload": f"the reference's binary benches: a 2^log_n x {w} Polyval matrix, blowup 2",
+            "cols": ["log_n", "commit_ms", "eval_ms", "open_ms"], "rows": rows}
+
+
 def served_cpu_reference(log2_c, size_range):
     """The served mix on the CPU reference path (C++ restatement, all host
     cores): one proof per size; sizes are uniform over the range, so the
@@ -891,7 +930,7 @@ def main():
     peaks, peak_kind = load_peaks()
     peak = float(peaks.get("hbm_gbs", 6800.0))
     num_sms = bg.device_info(local)["num_sms"]
-    batched = served = sweep = sumcheck = verify = latency = tuned = prime_res = None
+    batched = served = sweep = sumcheck = verify = latency = tuned = prime_res = wide = None
     if ws == 1 and not args.no_extras:
         latency = run_latency(bg, torch, local, log2_c)
         tuned = run_autotune(bg, torch, local, log2_c)
@@ -901,6 +940,7 @@ def main():
         sumcheck = run_sumcheck(bg, torch, local)
         verify = run_verify(bg, local, log2_c)
         prime_res = run_prime(bg, torch, local)
+        wide = run_binary_wide(bg, torch, local)
     cpu = None
     if not args.no_cpu_baseline and ws == 1:
         t = cpu_step_oracle(n, log2_c)
@@ -984,6 +1024,8 @@ def main():
         line["verify"] = {"workload": verify["workload"], "gpu_proofs_per_s": round(verify["gpu_proofs_per_s"]),
                           "cpu_proofs_per_s": round(verify["cpu_baseline"]["proofs_per_s"]),
                           "cpu_cores": verify["cpu_baseline"]["cores"], "speedup": round(verify["speedup"], 1)}
+    if wide:
+        line["binary_wide"] = wide
     if prime_res:
         line["prime"] = prime_res
     if batched:

@@ -237,6 +237,7 @@ struct bf_pcs {
   std::vector<std::vector<bfh::u128>> bases;  // stage bases (host copy, for the verifier)
   bfapi::DevBuf sc_ws;                        // standalone-sumcheck scratch
   bfapi::DevBuf eval_ws;                      // bf_eval scratch
+  bfapi::DevBuf evalc_ws;                     // bf_eval of w > 1 columns: point, eq table, sums
   bfapi::PinnedBuf pinned;
   std::vector<std::unique_ptr<bfapi::PinnedBuf>> pinned_cache;  // staging kept between open sessions
   std::mutex pinned_mu;                                          // guards pinned_cache (sessions on several threads)

@@ -176,6 +176,7 @@ bf_pcs::~bf_pcs() {
   if (stream) cudaStreamSynchronize(stream);
   sc_ws.release();
   eval_ws.release();
+  evalc_ws.release();
   if (stream) cudaStreamSynchronize(stream);
   if (pool) cudaMemPoolDestroy(pool);
   if (stream && own_stream) cudaStreamDestroy(stream);
@@ -577,12 +578,52 @@ int bf_commitment_data(const bf_commitment* cm, uint8_t* evals, size_t cap) {
   return BF_OK;
 }
 
+namespace {
+// Values of every column of a w > 1 matrix at a host point in one pass over
+// the matrix: the point's eq table against all columns (the columns'
+// MultiPoly::evaluate values, basefold.rs:126-131), into value_pin.
+int eval_cols_enqueue(bf_pcs* p, const uint4* data, size_t w, const uint8_t* point, uint8_t* value_pin) {
+  const int d = p->d;
+  const size_t n = (size_t)1 << d;
+  auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const size_t o_lo = up(16 * (size_t)(d > 0 ? d : 1)), o_hi = o_lo + up(16 * 4096), o_eq = o_hi + up(16 * 65536);
+  const size_t o_acc = o_eq + up(16 * n), total = o_acc + up(16 * w);
+  if (p->evalc_ws.bytes < total) CU(p->evalc_ws.alloc(total));
+  uint8_t* ws = p->evalc_ws.as<uint8_t>();
+  if (d > 0) {
+    std::memcpy(value_pin + 16 * w, point, 16 * (size_t)d);
+    CU(cudaMemcpyAsync(ws, value_pin + 16 * w, 16 * (size_t)d, cudaMemcpyHostToDevice, p->stream));
+  }
+  uint4* eq = reinterpret_cast<uint4*>(ws + o_eq);
+  uint32_t* acc = reinterpret_cast<uint32_t*>(ws + o_acc);
+  {
+    ProfScope ps(p->prof, p->stream, P_EQ);
+    CU(bf::launch_eq_table(reinterpret_cast<const uint4*>(ws), d, eq, reinterpret_cast<uint4*>(ws + o_lo),
+                           reinterpret_cast<uint4*>(ws + o_hi), p->stream));
+  }
+  CU(cudaMemsetAsync(acc, 0, 16 * w, p->stream));
+  {
+    ProfScope ps(p->prof, p->stream, P_FIX);
+    CU(bf::launch_eval_cols(eq, data, n, w, acc, p->stream));
+  }
+  CU(cudaMemcpyAsync(value_pin, acc, 16 * w, cudaMemcpyDeviceToHost, p->stream));
+  return BF_OK;
+}
+}  // namespace
+
 int bf_eval(bf_pcs* p, const bf_commitment* cm, const uint8_t* point, uint8_t* values) {
   if (!p || !cm || !values || (p->d > 0 && !point)) return fail(BF_ERR_ARG, "null argument");
   DeviceGuard g(p->device);
   const size_t half = p->d > 0 ? ((size_t)1 << (p->d - 1)) : 1;
+  CU(p->pinned.ensure(16 * cm->width + 16 * (size_t)p->d + 64));
+  if (cm->width > 1 && p->d <= bf::kEqTableMaxVars) {
+    TRY(eval_cols_enqueue(p, cm->data.as<uint4>(), cm->width, point, p->pinned.b()));
+    CU(cudaStreamSynchronize(p->stream));
+    p->prof.drain();
+    std::memcpy(values, p->pinned.b(), 16 * cm->width);
+    return BF_OK;
+  }
   if (p->eval_ws.bytes < 16 * half) CU(p->eval_ws.alloc(16 * half));
-  CU(p->pinned.ensure(16 * cm->width + 64));
   TRY(eval_enqueue(p, cm, point, p->eval_ws.as<uint4>(), p->stream, p->pinned.b()));
   CU(cudaStreamSynchronize(p->stream));
   p->prof.drain();
@@ -611,9 +652,13 @@ int bf_eval_data(bf_pcs* p, const void* evals, int on_device, size_t width, cons
     CU(cudaMemcpyAsync(cm.data.p, evals, bytes, cudaMemcpyHostToDevice, p->stream));
   }
   const size_t half = p->d > 0 ? ((size_t)1 << (p->d - 1)) : 1;
-  if (p->eval_ws.bytes < 16 * half) CU(p->eval_ws.alloc(16 * half));
-  CU(p->pinned.ensure(16 * width + 64));
-  TRY(eval_enqueue(p, &cm, point, p->eval_ws.as<uint4>(), p->stream, p->pinned.b()));
+  CU(p->pinned.ensure(16 * width + 16 * (size_t)p->d + 64));
+  if (width > 1 && p->d <= bf::kEqTableMaxVars) {
+    TRY(eval_cols_enqueue(p, cm.data.as<uint4>(), width, point, p->pinned.b()));
+  } else {
+    if (p->eval_ws.bytes < 16 * half) CU(p->eval_ws.alloc(16 * half));
+    TRY(eval_enqueue(p, &cm, point, p->eval_ws.as<uint4>(), p->stream, p->pinned.b()));
+  }
   CU(cudaStreamSynchronize(p->stream));
   p->prof.drain();
   std::memcpy(values, p->pinned.b(), 16 * width);

@@ -100,6 +100,10 @@ struct FoldFixParams {
 cudaError_t launch_fold_fix(const FoldFixParams& p, uint4 r, cudaStream_t st);
 cudaError_t launch_combine_rows(const uint4* rows, size_t nrows, size_t width, const uint4* scalars, uint4* out,
                                 cudaStream_t st);
+// acc[4 c .. 4 c + 3] ^= sum_r eq[r] * data[r w + c] for every column c < w.
+cudaError_t launch_eval_cols(const uint4* eq, const uint4* data, size_t rows, size_t w, uint32_t* acc,
+                             cudaStream_t st);
+constexpr int kEqTableMaxVars = 28;  // launch_eq_table: up to 12 + 16 variables
 // The last `nvars` (<= kEvalTailMaxVars) fixes of MultiPoly::evaluate in one
 // block, in place on buf[0 .. 2^nvars): variable k is fixed with r[k] (or
 // rp[k] in device memory when rp is not null), top first; the value lands in

@@ -399,6 +399,59 @@ __device__ __forceinline__ void warp_hash_node(const WarpKeccak& wk, const uint4
   if (wk.lane < 4) reinterpret_cast<uint2*>(nxt + 2 * s)[wk.lane] = a;
 }
 
+// keccak256 of matrix rows of `words` 32-bit words, one lane per row, the
+// 32 rows [r0, r0 + 32) per warp.  The 136-byte rate is 34 words, so every
+// block of every row starts on a word: the warp stages the current block of
+// its rows in shared memory (`st`: 32 x kStagePitch words) with loads whose
+// 32 lanes read one 128-byte row run (8 in flight per lane), then each lane
+// absorbs its row.  word_at(row, i) returns word i of a row (rows < `rows`,
+// i < `words`); the 0x01 pad word follows the message and 0x80 ends the
+// last block.  Returns the interleaved digest (the trees' form).
+constexpr int kRateWords = 34;
+constexpr int kStagePitch = 35;  // odd pitch: lane r reads word r * 35 + i without bank conflicts
+template <class WordAt>
+__device__ __forceinline__ Digest keccak_rows_warp(uint32_t* st, size_t r0, size_t rows, uint32_t words,
+                                                   const WordAt& word_at) {
+  const uint32_t lane = threadIdx.x & 31u;
+  uint2 s[25];
+#pragma unroll
+  for (int i = 0; i < 25; ++i) s[i] = make_uint2(0, 0);
+  const uint32_t nblk = words / kRateWords + 1;
+  for (uint32_t blk = 0; blk < nblk; ++blk) {
+    auto pad = [&](uint32_t i, uint32_t v) {
+      const uint32_t col = blk * kRateWords + i;
+      uint32_t o = col < words ? v : (col == words ? 0x01u : 0u);
+      if (blk == nblk - 1 && i == kRateWords - 1) o |= 0x80000000u;
+      return o;
+    };
+    const uint32_t col = blk * kRateWords + lane;  // words 0..31 of the block: lane = word
+#pragma unroll 1
+    for (int h = 0; h < 32; h += 8) {
+      uint32_t raw[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) raw[k] = (col < words && r0 + h + k < rows) ? word_at(r0 + h + k, col) : 0u;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) st[(h + k) * kStagePitch + lane] = pad(lane, raw[k]);
+    }
+#pragma unroll
+    for (int i = 32; i < kRateWords; ++i) {  // words 32, 33: lane = row
+      const uint32_t c2 = blk * kRateWords + i;
+      const uint32_t v = (c2 < words && r0 + lane < rows) ? word_at(r0 + lane, c2) : 0u;
+      st[lane * kStagePitch + i] = pad(i, v);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < 17; ++k) {
+      const uint2 l = bi_from_lane(make_uint2(st[lane * kStagePitch + 2 * k], st[lane * kStagePitch + 2 * k + 1]));
+      s[k].x ^= l.x;
+      s[k].y ^= l.y;
+    }
+    __syncwarp();
+    keccak_f1600<true>(s);
+  }
+  return digest_from_state(s);
+}
+
 __device__ __forceinline__ Digest load_digest(const uint4* p, size_t i) {
   Digest d;
   d.lo = p[2 * i];

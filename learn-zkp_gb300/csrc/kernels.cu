@@ -671,28 +671,18 @@ __global__ void __launch_bounds__(256) tree_top_kernel(uint4* level, size_t n, u
 
 // Leaf of a row of `width` elements: keccak256 of its 16*width bytes
 // (GenericHasher over the row's bincode, p3/src/symmetric.rs:16-25), any
-// number of 136-byte blocks.
+// number of 136-byte blocks; a warp stages the blocks of 32 rows through
+// shared memory (keccak_rows_warp) so that its loads read whole row runs.
 __global__ void __launch_bounds__(128) leaves_rows_kernel(const uint4* __restrict__ cw, uint4* __restrict__ leaves,
                                                           size_t n, size_t width) {
-  const size_t lanes = 2 * width;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    uint2 s[25];
-#pragma unroll
-    for (int k = 0; k < 25; ++k) s[k] = make_uint2(0, 0);
-    const uint2* row = reinterpret_cast<const uint2*>(cw + i * width);
-    size_t k = 0;
-    for (; k + 17 <= lanes; k += 17) {  // full blocks
-      for (int q = 0; q < 17; ++q) s[q] = kx2(s[q], row[k + q]);
-      keccak_f1600(s);
-    }
-    const int rem = (int)(lanes - k);  // 0..16 lanes left
-    for (int q = 0; q < rem; ++q) s[q] = kx2(s[q], row[k + q]);
-    // pad10*1: 0x01 after the message, 0x80 in the last byte of the block
-    for (int q = 0; q < 17; ++q)
-      if (q == rem) s[q].x ^= 0x01u;
-    s[16].y ^= 0x80000000u;
-    keccak_f1600(s);
-    store_digest(leaves, i, digest_interleaved(digest_from_state(s)));  // trees hold interleaved digests
+  __shared__ uint32_t stage[4][32 * kStagePitch];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t* words = reinterpret_cast<const uint32_t*>(cw);
+  const size_t row_words = 4 * width;
+  auto word_at = [&](size_t row, uint32_t i) { return words[row * row_words + i]; };
+  for (size_t r0 = ((size_t)blockIdx.x * 4 + warp) * 32; r0 < n; r0 += (size_t)gridDim.x * 128) {
+    const Digest dg = keccak_rows_warp(stage[warp], r0, n, (uint32_t)row_words, word_at);
+    if (r0 + lane < n) store_digest(leaves, r0 + lane, dg);
   }
 }
 
@@ -1040,19 +1030,80 @@ cudaError_t launch_eval_tail(uint4* buf, const EvalTail& p, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-// out[row] = sum_c scalars[c] * rows[row * width + c]   (basefold.rs:166-183)
-__global__ void combine_rows_kernel(const uint4* __restrict__ rows, size_t nrows, size_t width,
-                                    const uint4* __restrict__ scalars, uint4* __restrict__ out) {
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < nrows; i += (size_t)gridDim.x * blockDim.x) {
+// out[row] = sum_c scalars[c] * rows[row * width + c]   (basefold.rs:166-183).
+// One thread per row: a block stages 128 rows x 8 columns (one 128-byte run
+// per row and column chunk; a warp's loads cover four whole runs) in shared
+// memory, pitch 9 elements so a warp's 16-byte reads of one column hit
+// distinct banks, and the chunk's scalars beside them.
+constexpr int kCombRowsB = 128, kCombColsB = 8;
+__global__ void __launch_bounds__(kCombRowsB) combine_rows_kernel(const uint4* __restrict__ rows, size_t nrows,
+                                                                 size_t width, const uint4* __restrict__ scalars,
+                                                                 uint4* __restrict__ out) {
+  __shared__ uint4 stage[kCombRowsB * (kCombColsB + 1)];
+  __shared__ uint4 sc[kCombColsB];
+  for (size_t r0 = (size_t)blockIdx.x * kCombRowsB; r0 < nrows; r0 += (size_t)gridDim.x * kCombRowsB) {
     uint4 acc = make_uint4(0, 0, 0, 0);
-    for (size_t c = 0; c < width; ++c) acc = gf_add(acc, gf_mul(scalars[c], rows[i * width + c]));
-    out[i] = acc;
+    for (size_t c0 = 0; c0 < width; c0 += kCombColsB) {
+      __syncthreads();  // the previous chunk's reads are done
+      if (threadIdx.x < kCombColsB) sc[threadIdx.x] = c0 + threadIdx.x < width ? scalars[c0 + threadIdx.x] : uint4{};
+      uint4 v[kCombColsB];
+#pragma unroll
+      for (int k = 0; k < kCombColsB; ++k) {  // element e = k 128 + t: row e / 8, column e % 8
+        const uint32_t e = k * kCombRowsB + threadIdx.x;
+        const size_t r = r0 + e / kCombColsB, c = c0 + e % kCombColsB;
+        v[k] = (r < nrows && c < width) ? rows[r * width + c] : make_uint4(0, 0, 0, 0);
+      }
+#pragma unroll
+      for (int k = 0; k < kCombColsB; ++k) {
+        const uint32_t e = k * kCombRowsB + threadIdx.x;
+        stage[(e / kCombColsB) * (kCombColsB + 1) + e % kCombColsB] = v[k];
+      }
+      __syncthreads();
+      const uint4* row = stage + threadIdx.x * (kCombColsB + 1);
+      const int nc = width - c0 < (size_t)kCombColsB ? (int)(width - c0) : kCombColsB;
+      for (int c = 0; c < nc; ++c) acc = gf_add(acc, gf_mul(sc[c], row[c]));
+    }
+    if (r0 + threadIdx.x < nrows) out[r0 + threadIdx.x] = acc;
   }
 }
 
 cudaError_t launch_combine_rows(const uint4* rows, size_t nrows, size_t width, const uint4* scalars, uint4* out,
                                 cudaStream_t st) {
-  combine_rows_kernel<<<grid_for(nrows, 256), 256, 0, st>>>(rows, nrows, width, scalars, out);
+  combine_rows_kernel<<<grid_for(nrows, kCombRowsB), kCombRowsB, 0, st>>>(rows, nrows, width, scalars, out);
+  COUNT_LAUNCH();
+  return cudaGetLastError();
+}
+
+// Column values of a row-major matrix at a point: acc[c] ^= sum_r eq[r] data[r w + c]
+// (basefold.rs:126-131: MultiPoly::evaluate of each column, here as the sum against the
+// point's eq table, the same field value).  Lane = column (32 per blockIdx.y), warps and
+// blocks over the rows, so a warp reads 32 consecutive elements of a row.
+__global__ void __launch_bounds__(256) eval_cols_kernel(const uint4* __restrict__ eq, const uint4* __restrict__ data,
+                                                       size_t rows, uint32_t w, uint32_t* acc) {
+  __shared__ uint4 part[8][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t c = blockIdx.y * 32 + lane;
+  uint4 s = make_uint4(0, 0, 0, 0);
+  if (c < w)
+    for (size_t r = (size_t)blockIdx.x * 8 + warp; r < rows; r += (size_t)gridDim.x * 8)
+      s = gf_add(s, gf_mul(eq[r], data[r * w + c]));
+  part[warp][lane] = s;
+  __syncthreads();
+  if (warp == 0 && c < w) {
+    uint4 v = part[0][lane];
+    for (int q = 1; q < 8; ++q) v = gf_add(v, part[q][lane]);
+    atomic_xor4(acc + 4 * (size_t)c, v);
+  }
+}
+
+cudaError_t launch_eval_cols(const uint4* eq, const uint4* data, size_t rows, size_t w, uint32_t* acc,
+                             cudaStream_t st) {
+  const size_t by = (w + 31) / 32;
+  size_t bx = (rows + 63) / 64;
+  const size_t cap = std::max<size_t>(1, (152 * 8 + by - 1) / by);
+  if (bx > cap) bx = cap;
+  eval_cols_kernel<<<dim3((unsigned)std::max<size_t>(bx, 1), (unsigned)by), 256, 0, st>>>(eq, data, rows,
+                                                                                          (uint32_t)w, acc);
   COUNT_LAUNCH();
   return cudaGetLastError();
 }

@@ -404,61 +404,17 @@ __global__ void __launch_bounds__(128) bb_leaves_one_kernel(const uint32_t* __re
 }
 
 // Any width: keccak256 of the row's 4w bytes (GenericHasher over the row's
-// bincode, p3/src/symmetric.rs:11-25), one lane per row.  The 136-byte rate
-// is 34 words, so the blocks of every row start on a word: a warp stages the
-// current block of its 32 rows in shared memory with coalesced loads (the
-// 0x01 padding word right after the message, 0x80 in the block's last byte),
-// then each lane absorbs its row.
-constexpr int kRateWords = 34;
-constexpr int kStagePitch = 35;  // odd pitch: lane r reads word r * 35 + i without bank conflicts
+// bincode, p3/src/symmetric.rs:11-25): canonical words staged by a warp per
+// 32 rows (keccak_rows_warp).
 __global__ void __launch_bounds__(128) bb_leaves_rows_kernel(const uint32_t* __restrict__ cw,
                                                             uint4* __restrict__ leaves, size_t rows, uint32_t w,
                                                             int bits) {
   __shared__ uint32_t stage[4][32 * kStagePitch];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  uint32_t* st = stage[warp];
-  const uint32_t nblk = w / kRateWords + 1;
+  auto word_at = [&](size_t row, uint32_t i) { return bb::from_mont(cw[row * w + i]); };
   for (size_t r0 = ((size_t)blockIdx.x * 4 + warp) * 32; r0 < rows; r0 += (size_t)gridDim.x * 128) {
-    uint2 s[25];
-#pragma unroll
-    for (int i = 0; i < 25; ++i) s[i] = make_uint2(0, 0);
-    for (uint32_t blk = 0; blk < nblk; ++blk) {
-      // word i of the block for row rr: the message word, the 0x01 pad
-      // word right after the message, and 0x80 in the block's last byte
-      auto word = [&](uint32_t rr, uint32_t i, uint32_t raw) {
-        const uint32_t col = blk * kRateWords + i;
-        uint32_t v = col < w ? bb::from_mont(raw) : (col == w ? 0x01u : 0u);
-        if (blk == nblk - 1 && i == kRateWords - 1) v |= 0x80000000u;
-        return v;
-      };
-      // words 0..31 of the 32 rows: a 128-byte run per row, 8 loads in flight
-      const uint32_t col = blk * kRateWords + lane;
-#pragma unroll 1
-      for (int h = 0; h < 32; h += 8) {
-        uint32_t raw[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) raw[k] = (col < w && r0 + h + k < rows) ? cw[(r0 + h + k) * w + col] : 0u;
-#pragma unroll
-        for (int k = 0; k < 8; ++k) st[(h + k) * kStagePitch + lane] = word(h + k, lane, raw[k]);
-      }
-      // words 32 and 33: lane = row
-#pragma unroll
-      for (int i = 32; i < kRateWords; ++i) {
-        const uint32_t c2 = blk * kRateWords + i;
-        const uint32_t v = (c2 < w && r0 + lane < rows) ? cw[(r0 + lane) * w + c2] : 0u;
-        st[lane * kStagePitch + i] = word(lane, i, v);
-      }
-      __syncwarp();
-#pragma unroll
-      for (int k = 0; k < 17; ++k) {
-        const uint2 l = bi_from_lane(make_uint2(st[lane * kStagePitch + 2 * k], st[lane * kStagePitch + 2 * k + 1]));
-        s[k].x ^= l.x;
-        s[k].y ^= l.y;
-      }
-      __syncwarp();
-      keccak_f1600<true>(s);
-    }
-    if (r0 + lane < rows) store_digest(leaves, brev_bits(r0 + lane, bits), digest_from_state(s));
+    const Digest dg = keccak_rows_warp(stage[warp], r0, rows, w, word_at);
+    if (r0 + lane < rows) store_digest(leaves, brev_bits(r0 + lane, bits), dg);
   }
 }
 
