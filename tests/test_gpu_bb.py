@@ -127,3 +127,72 @@ GENERIC = [(0, 0, 0, 1), (0, 2, 0, 2), (1, 1, 1, 1), (2, 0, 2, 1), (3, 1, 0, 1),
 @pytest.mark.parametrize("n,log2_c,log2_k0,w", GENERIC)
 def test_generic_code_matches_oracle(built_lib, n, log2_c, log2_k0, w):
     _check_generic(n, log2_c, log2_k0, w, 3000 + 17 * n + 5 * log2_c + log2_k0 + w)
+
+
+def test_caller_stream_and_two_threads(built_lib):
+    """Two pcs objects, each on its own caller-made CUDA stream, driven from
+    two host threads at once: the same bytes as one at a time."""
+    import threading
+
+    import torch
+    from basefold_gpu import BasefoldConfig, GenericChallenger, prime
+
+    cases = [(9, 1, 3, 31), (10, 2, 1, 32)]
+    want = {}
+    for n, log2_c, w, seed in cases:
+        data = rnd((1 << n, w) if w > 1 else 1 << n, seed)
+        point = rnd((n, 5), seed + 1)
+        root, values, blob = O.bb_harness_prepare(n, log2_c, data, point)
+        want[seed] = (data, point, root, values, blob, O.bb_open(n, log2_c, data, point, values, blob))
+    got, errors = {}, []
+
+    def run(n, log2_c, w, seed):
+        try:
+            stream = torch.cuda.Stream()
+            pcs = prime.BabyBearBasefold.setup(BasefoldConfig(prime.ReedSolomonCode(128, log2_c, n)), device=0,
+                                               stream=stream.cuda_stream)
+            data, point, root, values, blob, _ = want[seed]
+            for _ in range(3):
+                comm = pcs.commit(data)
+                vals = pcs.eval(comm, point)
+                proof = pcs.open(comm, [prime.PrimePolyEvals(vals, point)], GenericChallenger.from_state(blob))
+                got[seed] = (comm.root, vals, proof)
+                comm.free()
+        except Exception as e:  # reported by the main thread
+            errors.append(e)
+
+    ts = [threading.Thread(target=run, args=c) for c in cases]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    assert not errors, errors
+    for n, log2_c, w, seed in cases:
+        root, vals, proof = got[seed]
+        assert root == want[seed][2]
+        assert np.array_equal(vals, np.asarray(want[seed][3]).reshape(-1, 5))
+        assert proof == want[seed][5]
+
+
+def test_open_buffer_too_small_reports_size(built_lib):
+    import ctypes as C
+
+    from basefold_gpu import GenericChallenger, prime
+    from basefold_gpu._native import lib
+
+    n = 5
+    pcs = _pcs(n, 1)
+    data = rnd(1 << n, 41)
+    point = rnd((n, 5), 42)
+    comm = pcs.commit(data)
+    vals = pcs.eval(comm, point)
+    need = pcs.proof_size(1, 1)
+    small = np.zeros(16, np.uint8)
+    ln = C.c_size_t()
+    rc = lib().bf_bb_open(pcs._h, comm._h, C.c_void_p(point.ctypes.data), C.c_void_p(vals.ctypes.data), 1,
+                          GenericChallenger.keccak256()._h, C.c_void_p(small.ctypes.data), small.size, C.byref(ln))
+    assert rc == -4 and ln.value == need
+    # the full-size call still works and matches the oracle
+    _, values, blob = O.bb_harness_prepare(n, 1, data, point)
+    proof = pcs.open(comm, [prime.PrimePolyEvals(vals, point)], GenericChallenger.from_state(blob))
+    assert proof == O.bb_open(n, 1, data, point, values, blob)
