@@ -105,16 +105,10 @@ __device__ __forceinline__ void clmul64(uint64_t a, uint64_t b, uint64_t& lo, ui
   hi = p2 ^ (p1 >> 32);
 }
 
-// Montgomery reduction of the 256-bit carry-less product given as three
-// 128-bit Karatsuba parts: low = a0 b0, high = a1 b1, mid = (a0+a1)(b0+b1).
-__device__ __forceinline__ uint4 gf_karatsuba_reduce(uint64_t l0, uint64_t l1, uint64_t h0, uint64_t h1,
-                                                     uint64_t m0, uint64_t m1) {
-  m0 ^= l0 ^ h0;
-  m1 ^= l1 ^ h1;
-  const uint64_t c0 = l0;
-  uint64_t c1 = l1 ^ m0;
-  uint64_t c2 = h0 ^ m1;
-  uint64_t c3 = h1;
+// Montgomery reduction of a 256-bit carry-less product c0 (low) .. c3: the
+// field element c x^-128 mod P.  It is GF(2)-linear, so a sum of products
+// may be reduced once.
+__device__ __forceinline__ uint4 gf_reduce256(uint64_t c0, uint64_t c1, uint64_t c2, uint64_t c3) {
   // cancel bits 0..63:   + c0 * P
   c1 ^= (c0 << 63) ^ (c0 << 62) ^ (c0 << 57);
   c2 ^= c0 ^ (c0 >> 1) ^ (c0 >> 2) ^ (c0 >> 7);
@@ -122,6 +116,15 @@ __device__ __forceinline__ uint4 gf_karatsuba_reduce(uint64_t l0, uint64_t l1, u
   c2 ^= (c1 << 63) ^ (c1 << 62) ^ (c1 << 57);
   c3 ^= c1 ^ (c1 >> 1) ^ (c1 >> 2) ^ (c1 >> 7);
   return make_uint4((uint32_t)c2, (uint32_t)(c2 >> 32), (uint32_t)c3, (uint32_t)(c3 >> 32));
+}
+
+// Montgomery reduction of the 256-bit carry-less product given as three
+// 128-bit Karatsuba parts: low = a0 b0, high = a1 b1, mid = (a0+a1)(b0+b1).
+__device__ __forceinline__ uint4 gf_karatsuba_reduce(uint64_t l0, uint64_t l1, uint64_t h0, uint64_t h1,
+                                                     uint64_t m0, uint64_t m1) {
+  m0 ^= l0 ^ h0;
+  m1 ^= l1 ^ h1;
+  return gf_reduce256(l0, l1 ^ m0, h0 ^ m1, h1);
 }
 
 // Montgomery product a*b*x^-128 mod P.
@@ -133,6 +136,66 @@ __device__ __forceinline__ uint4 gf_mul(uint4 a, uint4 b) {
   clmul64(a1, b1, h0, h1);
   clmul64(a0 ^ a1, b0 ^ b1, m0, m1);
   return gf_karatsuba_reduce(l0, l1, h0, h1, m0, m1);
+}
+
+// One operand of many products, split once: the nine 32-bit words that
+// gf_mul's Karatsuba tree multiplies (low half, high half, their sum; in each
+// the two words and their sum), each already split into its four residue
+// classes mod 4 (the clmul32 masks), 36 words in all.
+struct GfPrep {
+  uint32_t m[36];
+};
+__device__ __forceinline__ void gf_prepare(uint4 b, uint32_t* m) {
+  const uint32_t w[9] = {b.x, b.y, b.x ^ b.y, b.z, b.w, b.z ^ b.w, b.x ^ b.z, b.y ^ b.w, b.x ^ b.z ^ b.y ^ b.w};
+#pragma unroll
+  for (int j = 0; j < 9; ++j) {
+    m[4 * j + 0] = w[j] & 0x11111111u;
+    m[4 * j + 1] = w[j] & 0x22222222u;
+    m[4 * j + 2] = w[j] & 0x44444444u;
+    m[4 * j + 3] = w[j] & 0x88888888u;
+  }
+}
+// clmul32(a, b) with b given split (gf_prepare's four words of one product).
+__device__ __forceinline__ uint64_t clmul32_prep(uint32_t a, uint32_t b0, uint32_t b1, uint32_t b2, uint32_t b3) {
+  const uint32_t a0 = a & 0x11111111u, a1 = a & 0x22222222u, a2 = a & 0x44444444u, a3 = a & 0x88888888u;
+  const uint64_t z0 = madw(a1, b3, mulw(a0, b0)) ^ mulw(a2, b2) ^ mulw(a3, b1);
+  const uint64_t z1 = madw(a2, b3, mulw(a0, b1)) ^ madw(a3, b2, mulw(a1, b0));
+  const uint64_t z2 = madw(a3, b3, mulw(a0, b2)) ^ mulw(a1, b1) ^ mulw(a2, b0);
+  const uint64_t z3 = mulw(a0, b3) ^ mulw(a1, b2) ^ mulw(a2, b1) ^ mulw(a3, b0);
+  return (z0 & 0x1111111111111111ull) | (z1 & 0x2222222222222222ull) | (z2 & 0x4444444444444444ull) |
+         (z3 & 0x8888888888888888ull);
+}
+// c ^= the unreduced 256-bit carry-less product a * b for a prepared b (its
+// 36 words at m, read as nine uint4); gf_reduce256(c) of a sum of these is
+// the sum of the gf_mul products.
+__device__ __forceinline__ void gf_clmul_acc(uint4 a, const uint4* m, uint64_t c[4]) {
+  const uint32_t x[9] = {a.x, a.y, a.x ^ a.y, a.z, a.w, a.z ^ a.w, a.x ^ a.z, a.y ^ a.w, a.x ^ a.z ^ a.y ^ a.w};
+  uint64_t q[9];
+#pragma unroll
+  for (int j = 0; j < 9; ++j) {
+    const uint4 b = m[j];
+    q[j] = clmul32_prep(x[j], b.x, b.y, b.z, b.w);
+  }
+  uint64_t lo[3], hi[3];
+#pragma unroll
+  for (int t = 0; t < 3; ++t) {  // 64 x 64 Karatsuba of each half
+    const uint64_t p0 = q[3 * t], p2 = q[3 * t + 1], p1 = q[3 * t + 2] ^ p0 ^ p2;
+    lo[t] = p0 ^ (p1 << 32);
+    hi[t] = p2 ^ (p1 >> 32);
+  }
+  // 128 x 128 Karatsuba: low = lo[0]:hi[0], high = lo[1]:hi[1], mid = lo[2]:hi[2]
+  const uint64_t m0 = lo[2] ^ lo[0] ^ lo[1], m1 = hi[2] ^ hi[0] ^ hi[1];
+  c[0] ^= lo[0];
+  c[1] ^= hi[0] ^ m0;
+  c[2] ^= lo[1] ^ m1;
+  c[3] ^= hi[1];
+}
+
+// c ^= the unreduced product a * b (both operands split here).
+__device__ __forceinline__ void gf_clmul_acc(uint4 a, uint4 b, uint64_t c[4]) {
+  uint32_t m[36];
+  gf_prepare(b, m);
+  gf_clmul_acc(a, reinterpret_cast<const uint4*>(m), c);
 }
 
 // gf_mul with H (0..9) of its nine 32 x 32 products from clmul32_h3: the

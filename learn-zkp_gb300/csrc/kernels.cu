@@ -841,9 +841,10 @@ cudaError_t launch_eq_table(const uint4* r, int nvars, uint4* out, uint4* tmp_lo
 __global__ void __launch_bounds__(256) dot_xor_kernel(const uint4* __restrict__ x, const uint4* __restrict__ y,
                                                       size_t n, uint32_t* acc) {
   __shared__ uint4 scratch[32];
-  uint4 s = make_uint4(0, 0, 0, 0);
+  uint64_t sum[4] = {0, 0, 0, 0};  // unreduced: one reduction per thread (GF(2)-linear)
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    s = gf_add(s, gf_mul(x[i], y[i]));
+    gf_clmul_acc(x[i], y[i], sum);
+  uint4 s = gf_reduce256(sum[0], sum[1], sum[2], sum[3]);
   s = block_xor(s, scratch);
   if (threadIdx.x == 0) atomic_xor4(acc, s);
 }
@@ -1034,18 +1035,22 @@ cudaError_t launch_eval_tail(uint4* buf, const EvalTail& p, cudaStream_t st) {
 // One thread per row: a block stages 128 rows x 8 columns (one 128-byte run
 // per row and column chunk; a warp's loads cover four whole runs) in shared
 // memory, pitch 9 elements so a warp's 16-byte reads of one column hit
-// distinct banks, and the chunk's scalars beside them.
+// distinct banks.  The chunk's scalars are split once (gf_prepare) for all
+// 128 rows, and a row sums its unreduced products and reduces once at the
+// end (the reduction is GF(2)-linear).
 constexpr int kCombRowsB = 128, kCombColsB = 8;
 __global__ void __launch_bounds__(kCombRowsB) combine_rows_kernel(const uint4* __restrict__ rows, size_t nrows,
                                                                  size_t width, const uint4* __restrict__ scalars,
                                                                  uint4* __restrict__ out) {
   __shared__ uint4 stage[kCombRowsB * (kCombColsB + 1)];
-  __shared__ uint4 sc[kCombColsB];
+  __shared__ uint4 prep[kCombColsB * 9];
   for (size_t r0 = (size_t)blockIdx.x * kCombRowsB; r0 < nrows; r0 += (size_t)gridDim.x * kCombRowsB) {
-    uint4 acc = make_uint4(0, 0, 0, 0);
+    uint64_t acc[4] = {0, 0, 0, 0};
     for (size_t c0 = 0; c0 < width; c0 += kCombColsB) {
       __syncthreads();  // the previous chunk's reads are done
-      if (threadIdx.x < kCombColsB) sc[threadIdx.x] = c0 + threadIdx.x < width ? scalars[c0 + threadIdx.x] : uint4{};
+      if (threadIdx.x < kCombColsB)
+        gf_prepare(c0 + threadIdx.x < width ? scalars[c0 + threadIdx.x] : make_uint4(0, 0, 0, 0),
+                   reinterpret_cast<uint32_t*>(prep + 9 * threadIdx.x));
       uint4 v[kCombColsB];
 #pragma unroll
       for (int k = 0; k < kCombColsB; ++k) {  // element e = k 128 + t: row e / 8, column e % 8
@@ -1061,9 +1066,9 @@ __global__ void __launch_bounds__(kCombRowsB) combine_rows_kernel(const uint4* _
       __syncthreads();
       const uint4* row = stage + threadIdx.x * (kCombColsB + 1);
       const int nc = width - c0 < (size_t)kCombColsB ? (int)(width - c0) : kCombColsB;
-      for (int c = 0; c < nc; ++c) acc = gf_add(acc, gf_mul(sc[c], row[c]));
+      for (int c = 0; c < nc; ++c) gf_clmul_acc(row[c], prep + 9 * c, acc);
     }
-    if (r0 + threadIdx.x < nrows) out[r0 + threadIdx.x] = acc;
+    if (r0 + threadIdx.x < nrows) out[r0 + threadIdx.x] = gf_reduce256(acc[0], acc[1], acc[2], acc[3]);
   }
 }
 
@@ -1083,11 +1088,11 @@ __global__ void __launch_bounds__(256) eval_cols_kernel(const uint4* __restrict_
   __shared__ uint4 part[8][32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t c = blockIdx.y * 32 + lane;
-  uint4 s = make_uint4(0, 0, 0, 0);
+  uint64_t sum[4] = {0, 0, 0, 0};  // unreduced: one reduction per thread (GF(2)-linear)
   if (c < w)
     for (size_t r = (size_t)blockIdx.x * 8 + warp; r < rows; r += (size_t)gridDim.x * 8)
-      s = gf_add(s, gf_mul(eq[r], data[r * w + c]));
-  part[warp][lane] = s;
+      gf_clmul_acc(data[r * w + c], eq[r], sum);
+  part[warp][lane] = gf_reduce256(sum[0], sum[1], sum[2], sum[3]);
   __syncthreads();
   if (warp == 0 && c < w) {
     uint4 v = part[0][lane];
