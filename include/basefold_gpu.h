@@ -390,6 +390,12 @@ void bf_bb_commitment_free(bf_bb_commitment* comm);
 /* PolyCommitScheme::eval (basefold.rs:126-131): `values` receives the
  * width column evaluations at the point (width x 20 bytes). */
 int bf_bb_eval(bf_bb_pcs* pcs, const bf_bb_commitment* comm, const uint8_t* point, uint8_t* values);
+/* PolyCommitScheme::eval(&self, data: &Data, point) for data that has no
+ * commitment: 2^num_vars rows of `width` canonical words in host memory
+ * (on_device 0: copied in) or device memory (on_device 1: 4-byte aligned,
+ * not modified); evaluated on the GPU into `values` (width x 20 bytes). */
+int bf_bb_eval_data(bf_bb_pcs* pcs, const void* evals, int on_device, size_t width, const uint8_t* point,
+                    uint8_t* values);
 /* PolyCommitScheme::open (basefold.rs:133-232) of n_evals points (0: the
  * default proof, as the reference returns for no evaluations; 1: `point`
  * and the commitment's width `values`); the transcript advances exactly as

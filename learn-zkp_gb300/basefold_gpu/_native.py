@@ -23,7 +23,7 @@ EXPORTS = [
     "bf_engine_autotune", "bf_engine_graphs", "bf_engine_stats", "bf_verify_batch", "bf_engine_set_tune", "bf_engine_cancel", "bf_engine_schedule",
     "bf_eval_data", "bf_tune_cache_load", "bf_tune_cache_save", "bf_tune_cache_clear",
     "bf_bb_pcs_setup", "bf_bb_pcs_setup_generic", "bf_bb_pcs_free", "bf_bb_pcs_num_queries", "bf_bb_pcs_proof_size", "bf_bb_commit",
-    "bf_bb_commit_device", "bf_bb_commitment_root", "bf_bb_commitment_free", "bf_bb_eval", "bf_bb_open",
+    "bf_bb_commit_device", "bf_bb_commitment_root", "bf_bb_commitment_free", "bf_bb_eval", "bf_bb_eval_data", "bf_bb_open",
     "bf_bb_verify", "bf_challenger_sample_bb_ext",
 ]
 
@@ -146,6 +146,7 @@ def lib():
         "bf_bb_commitment_root": ([vp, u8p], i),
         "bf_bb_commitment_free": ([vp], None),
         "bf_bb_eval": ([vp, vp, u8p, u8p], i),
+        "bf_bb_eval_data": ([vp, vp, i, sz, u8p, u8p], i),
         "bf_bb_open": ([vp, vp, u8p, u8p, i, vp, u8p, sz, C.POINTER(sz)], i),
         "bf_bb_verify": ([vp, u8p, u8p, u8p, sz, i, vp, u8p, sz], i),
         "bf_challenger_sample_bb_ext": ([vp, u8p], i),

@@ -183,10 +183,27 @@ class BabyBearBasefold:
         d = self.num_vars
         return _ext(point, d) if d else np.zeros((1, 5), np.uint32)
 
-    def eval(self, comm: PrimeCommitmentData, point) -> np.ndarray:
-        """eval (basefold.rs:126-131): the (width, 5) column values at the point."""
-        out = np.zeros((comm.width, 5), dtype=np.uint32)
-        check(lib().bf_bb_eval(self._h, comm._h, _p(self._point(point)), _p(out)))
+    def eval(self, data, point) -> np.ndarray:
+        """eval (basefold.rs:126-131): the (width, 5) column values at the
+        point, of a commitment's device-resident evaluations or of host rows
+        that have no commitment (copied in, evaluated on the GPU)."""
+        if isinstance(data, PrimeCommitmentData):
+            out = np.zeros((data.width, 5), dtype=np.uint32)
+            check(lib().bf_bb_eval(self._h, data._h, _p(self._point(point)), _p(out)))
+            return out
+        d = np.asarray(data)
+        d = np.ascontiguousarray(d.view(np.uint32) if d.dtype in (np.int32, np.uint32) else d.astype(np.uint32))
+        width = d.size // self._rows()
+        if width == 0 or width * self._rows() != d.size:
+            raise ValueError(f"{d.size} evaluations is not a multiple of 2^{self.num_vars} rows")
+        out = np.zeros((width, 5), dtype=np.uint32)
+        check(lib().bf_bb_eval_data(self._h, _p(d), 0, width, _p(self._point(point)), _p(out)))
+        return out
+
+    def eval_device(self, dev_ptr: int, point, width: int = 1) -> np.ndarray:
+        """eval of device-resident rows (2^num_vars x width canonical words) with no commitment."""
+        out = np.zeros((width, 5), dtype=np.uint32)
+        check(lib().bf_bb_eval_data(self._h, C.c_void_p(dev_ptr), 1, width, _p(self._point(point)), _p(out)))
         return out
 
     def open(self, comm: PrimeCommitmentData, evals, challenger: GenericChallenger) -> bytes:

@@ -319,13 +319,13 @@ void bf_bb_commitment_free(bf_bb_commitment* cm) {
   bb_release(p);
 }
 
-int bf_bb_eval(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, uint8_t* values) {
-  if (!p || !cm || !values || (p->num_vars > 0 && !point)) return fail(BF_ERR_ARG, "null argument");
-  if (cm->pcs != p) return fail(BF_ERR_ARG, "commitment made by another pcs");
+namespace {
+// The column values of 2^num_vars rows of w canonical words (device memory)
+// at a host point: the point's eq table against every column.
+int eval_device_rows(bf_bb_pcs* p, const uint32_t* data, size_t w, const uint8_t* point, uint8_t* values) {
   std::vector<E> x;
   TRY(load_points(point, (size_t)p->num_vars, x, "point coordinate"));
-  DeviceGuard g(p->device);
-  const size_t rows = (size_t)1 << p->num_vars, w = cm->w;
+  const size_t rows = (size_t)1 << p->num_vars;
   // the sums are 64-bit atomics: their slot starts on a 256-byte boundary
   const size_t eq_bytes = (20 * rows + 255) & ~(size_t)255, acc_bytes = 40 * w;
   if (p->ws.bytes < eq_bytes + acc_bytes) CU(p->ws.alloc(eq_bytes + acc_bytes));
@@ -337,14 +337,40 @@ int bf_bb_eval(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, u
   // evaluate = sum over the hypercube of eq(b, point) f(b): the same field
   // value as MultiPoly::evaluate's fix_last_var chain
   if (w == 1)
-    CU(bf::bb_launch_dot(eq, cm->data.as<uint32_t>(), 1, rows, acc, p->stream));
+    CU(bf::bb_launch_dot(eq, data, 1, rows, acc, p->stream));
   else
-    CU(bf::bb_launch_eval_cols(eq, cm->data.as<uint32_t>(), rows, w, acc, p->stream));
+    CU(bf::bb_launch_eval_cols(eq, data, rows, w, acc, p->stream));
   CU(cudaMemcpyAsync(p->pin.p, acc, acc_bytes, cudaMemcpyDeviceToHost, p->stream));
   CU(cudaStreamSynchronize(p->stream));
   const unsigned long long* s = reinterpret_cast<const unsigned long long*>(p->pin.p);
   for (size_t c = 0; c < w; ++c) bbh::store(values + 20 * c, bbh::from_canonical_sums(s + 5 * c));
   return BF_OK;
+}
+}  // namespace
+
+int bf_bb_eval(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, uint8_t* values) {
+  if (!p || !cm || !values || (p->num_vars > 0 && !point)) return fail(BF_ERR_ARG, "null argument");
+  if (cm->pcs != p) return fail(BF_ERR_ARG, "commitment made by another pcs");
+  DeviceGuard g(p->device);
+  return eval_device_rows(p, cm->data.as<uint32_t>(), cm->w, point, values);
+}
+
+int bf_bb_eval_data(bf_bb_pcs* p, const void* evals, int on_device, size_t width, const uint8_t* point,
+                    uint8_t* values) {
+  if (!p || !evals || !values || (p->num_vars > 0 && !point)) return fail(BF_ERR_ARG, "null argument");
+  if (p->device < 0) return fail(BF_ERR_ARG, "verifier-only pcs (device < 0)");
+  if (width == 0 || width > 65536) return fail(BF_ERR_ARG, "width %zu out of range (1..65536)", width);
+  if (on_device && (reinterpret_cast<uintptr_t>(evals) & 3))
+    return fail(BF_ERR_ARG, "device evaluations must be 4-byte aligned");
+  DeviceGuard g(p->device);
+  if (on_device) return eval_device_rows(p, static_cast<const uint32_t*>(evals), width, point, values);
+  DevBuf copy;  // host rows: copied in on the pcs's stream
+  const size_t bytes = 4 * width << p->num_vars;
+  CU(copy.alloc(bytes));
+  CU(cudaMemcpyAsync(copy.p, evals, bytes, cudaMemcpyHostToDevice, p->stream));
+  const int rc = eval_device_rows(p, copy.as<uint32_t>(), width, point, values);
+  cudaStreamSynchronize(p->stream);  // before the copy is freed (also on an error)
+  return rc;
 }
 
 int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, const uint8_t* values,

@@ -196,3 +196,18 @@ def test_open_buffer_too_small_reports_size(built_lib):
     _, values, blob = O.bb_harness_prepare(n, 1, data, point)
     proof = pcs.open(comm, [prime.PrimePolyEvals(vals, point)], GenericChallenger.from_state(blob))
     assert proof == O.bb_open(n, 1, data, point, values, blob)
+
+
+@pytest.mark.parametrize("n,w", [(0, 1), (1, 3), (7, 1), (9, 40), (12, 2)])
+def test_eval_of_uncommitted_data(built_lib, n, w):
+    """The trait's eval(&Data, point) for rows that have no commitment
+    (bf_bb_eval_data), from host and from device memory, against the oracle."""
+    import torch
+
+    pcs = _pcs(n, 1)
+    data = rnd((1 << n, w) if w > 1 else 1 << n, 500 + n + w)
+    point = rnd((n, 5), 600 + n)
+    want = np.asarray(O.bb_eval(n, data, point)).reshape(-1, 5)
+    assert np.array_equal(pcs.eval(data, point), want)
+    dev = torch.from_numpy(data.view(np.int32)).cuda()
+    assert np.array_equal(pcs.eval_device(dev.data_ptr(), point, w), want)
