@@ -140,3 +140,31 @@ class StdRng:
     def random_elems(self, n: int) -> np.ndarray:
         """Polyval::random_vec(n, rng): n elements, (n, 16) uint8."""
         return self._words(4 * n).astype("<u4").view(np.uint8).reshape(n, 16).copy()
+
+    # FromUniformBytes for BabyBear (p3/src/field/from_uniform_bytes.rs:37-45)
+    # and for BinomialExtensionField<BabyBear, 5> (:63-82): 4 bytes (one word)
+    # shifted right by one, redrawn while >= p; the extension draws 20 bytes
+    # (five words) at once and redraws all five while any is >= p.
+    BABYBEAR_P = 2013265921
+
+    def random_babybear(self, n: int) -> np.ndarray:
+        """BabyBear::random_vec(n, rng) as canonical uint32."""
+        out = np.zeros(n, dtype=np.uint32)
+        for i in range(n):
+            while True:
+                v = self.next_u32() >> 1
+                if v < self.BABYBEAR_P:
+                    out[i] = v
+                    break
+        return out
+
+    def random_babybear_ext(self, n: int) -> np.ndarray:
+        """BinomialExtensionField<BabyBear, 5>::random_vec(n, rng), (n, 5) uint32."""
+        out = np.zeros((n, 5), dtype=np.uint32)
+        for i in range(n):
+            while True:
+                v = self._words(5) >> np.uint32(1)
+                if bool((v < self.BABYBEAR_P).all()):
+                    out[i] = v
+                    break
+        return out

@@ -68,3 +68,71 @@ def test_seeded_harness_fixture():
             proof = O.open_proof(n, log2_c, evals, point, values, blob, w)
             assert root.hex() == c["root"] and values.tobytes().hex() == c["values"]
             assert hashlib.sha256(proof).hexdigest() == c["proof_sha256"]
+
+
+def _bb_fixture_rows(step):
+    import hashlib
+
+    sys.path.insert(0, GOLDEN)
+    import make_seeded_harness_bb as M
+
+    doc = json.load(open(os.path.join(GOLDEN, "seeded_harness_bb.json")))
+    rows = doc["cases"]
+    assert doc["cols"] == M.COLS and len(rows) == 3 * 90 + 9 * 90
+    k = 0
+    for log2_c in range(3):
+        for inp in M.harness_inputs(doc["seed"], log2_c):
+            yield rows[k], ("reed_solomon", log2_c, None), inp, k % step == 0
+            k += 1
+    for log2_c in range(3):
+        for log2_k0 in range(3):
+            for inp in M.harness_inputs(doc["seed"], log2_c, log2_k0):
+                yield rows[k], ("generic", log2_c, log2_k0), inp, k % step == 0
+                k += 1
+
+
+def test_seeded_harness_bb_fixture():
+    """The prime fixture's draws follow the harness (every case's shape and
+    order), and a sample of its cases is reproduced by the oracle."""
+    import hashlib
+
+    from oracle import oracle as O
+
+    checked = 0
+    for row, (code, log2_c, log2_k0), (n, w, lk, ts, evals, point), check in _bb_fixture_rows(11):
+        assert row[:5] == [code, log2_c, log2_k0, n, w]
+        if not check:
+            continue
+        kw = {} if ts is None else {"log2_k0": lk, "ts": ts}
+        root, values, blob = O.bb_harness_prepare(n, log2_c, evals, point, **kw)
+        proof = O.bb_open(n, log2_c, evals, point, values, blob, **kw)
+        assert root.hex() == row[5]
+        assert hashlib.sha256(values.tobytes()).hexdigest()[:16] == row[6]
+        assert [len(proof), hashlib.sha256(proof).hexdigest()[:32]] == row[7:]
+        checked += 1
+    assert checked >= 90
+
+
+def test_babybear_draws():
+    """BabyBear::random takes one word >> 1 and redraws while >= p; the
+    extension takes five words and redraws all five while any is >= p."""
+    rng = rand.StdRng.seed_from_u64(3)
+    words = rand.StdRng.seed_from_u64(3)._words(4000)
+    got = rng.random_babybear(200)
+    exp, i = [], 0
+    while len(exp) < 200:
+        v = int(words[i]) >> 1
+        i += 1
+        if v < 2013265921:
+            exp.append(v)
+    assert got.tolist() == exp
+    rng = rand.StdRng.seed_from_u64(4)
+    words = rand.StdRng.seed_from_u64(4)._words(4000)
+    got = rng.random_babybear_ext(100)
+    exp, i = [], 0
+    while len(exp) < 100:
+        v = [int(x) >> 1 for x in words[i:i + 5]]
+        i += 5
+        if all(x < 2013265921 for x in v):
+            exp.append(v)
+    assert got.tolist() == exp
