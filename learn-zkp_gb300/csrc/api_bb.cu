@@ -404,12 +404,12 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
   // and records.
   const size_t rows = (size_t)1 << nv, half = rows >> 1;
   const size_t n_fold = p->n0() * (((size_t)1 << d) - 1);  // sum over rounds of n_i
-  const size_t wsz[] = {w > 1 ? 20 * rows : 0,  w > 1 ? 20 * p->n_d() : 0, 20 * (half ? half : 1), 20 * half,
-                        20 * half,              20 * n_fold,             64 * n_fold,             8 * Q,
-                        Q * rec,                128};
-  size_t off[11] = {0};
-  for (int k = 0; k < 10; ++k) off[k + 1] = off[k] + ((wsz[k] + 255) & ~(size_t)255);
-  if (p->open_ws.bytes < off[10]) CU(p->open_ws.alloc(off[10]));
+  const size_t wsz[] = {w > 1 ? 20 * rows : 0, w > 1 ? 20 * p->n_d() : 0, 20 * (half ? half : 1), 20 * half,
+                        20 * half,             20 * n_fold,             64 * n_fold,             8 * Q,
+                        Q * rec,               128,                     w > 1 ? 20 * rows : 0};
+  size_t off[12] = {0};
+  for (int k = 0; k < 11; ++k) off[k + 1] = off[k] + ((wsz[k] + 255) & ~(size_t)255);
+  if (p->open_ws.bytes < off[11]) CU(p->open_ws.alloc(off[11]));
   uint8_t* base = p->open_ws.as<uint8_t>();
   uint32_t* polyE = reinterpret_cast<uint32_t*>(base + off[0]);
   uint32_t* piE = reinterpret_cast<uint32_t*>(base + off[1]);
@@ -421,6 +421,7 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
   uint8_t* recs = base + off[8];
   unsigned long long* acc = reinterpret_cast<unsigned long long*>(base + off[9]);
   uint4* root_dev = reinterpret_cast<uint4*>(base + off[9] + 64);  // after the five sums
+  uint32_t* poly_canon = reinterpret_cast<uint32_t*>(base + off[10]);  // width > 1: the combined poly, canonical
   CU(p->pin.ensure(8 * Q + 20 * k0 + 20 * 64 + 256));
 
   // The polynomial and codeword the folding sumcheck runs on (basefold.rs:154-177).
@@ -433,17 +434,22 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
   } else {
     const std::vector<E> s = bbh::scalars_by_eq(w, tr);
     for (size_t c = 0; c < w; ++c) claim = bbh::eadd(claim, bbh::emul(s[c], vals[c]));
-    // s R^2 against the canonical evaluations, s R against the Montgomery codeword
-    std::vector<bb::E5> sd(2 * w);
-    for (size_t c = 0; c < w; ++c) {
-      sd[c] = bbh::to_dev2(s[c]);
-      sd[w + c] = bbh::to_dev(s[c]);
-    }
+    // s R^2 against the canonical evaluations
+    std::vector<bb::E5> sd(w);
+    for (size_t c = 0; c < w; ++c) sd[c] = bbh::to_dev2(s[c]);
     DevBuf sdev;
-    CU(sdev.alloc(40 * w));
-    CU(cudaMemcpyAsync(sdev.p, sd.data(), 40 * w, cudaMemcpyHostToDevice, st));
+    CU(sdev.alloc(20 * w));
+    CU(cudaMemcpyAsync(sdev.p, sd.data(), 20 * w, cudaMemcpyHostToDevice, st));
     CU(bf::bb_launch_combine(cm->data.as<uint32_t>(), rows, w, sdev.as<uint32_t>(), polyE, st));
-    CU(bf::bb_launch_combine(cm->cw.as<uint32_t>(), p->n_d(), w, sdev.as<uint32_t>() + 5 * w, piE, st));
+    // The reference combines the codeword's rows the same way; both codes are
+    // linear over the base field, so that combination is the encoding of the
+    // combined polynomial, coefficient by coefficient: a 5-column encode of
+    // 2^num_vars rows instead of w products per codeword row, the same values.
+    CU(bf::bb_launch_from_mont(polyE, poly_canon, 5 * rows, st));
+    uint32_t* flag = p->small.as<uint32_t>();
+    CU(cudaMemsetAsync(flag, 0, 4, st));
+    CU(bf::bb_launch_encode(poly_canon, piE, p->d, p->log2_c, p->log2_k0, p->generic, 5, p->tw.as<uint32_t>(), flag,
+                            st));
     CU(cudaStreamSynchronize(st));  // sd and sdev go out of scope
     poly = polyE;
     pi = piE;

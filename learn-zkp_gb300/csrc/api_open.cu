@@ -554,9 +554,18 @@ int open_session_enqueue_start(bf_open_session* s) {
   cudaStream_t st = s->st;
   if (w > 1) {  // combine rows with the eq scalars (basefold.rs:166-183)
     CU(cudaMemcpyAsync(s->w_scalars, pin + 64, 16 * w, cudaMemcpyHostToDevice, st));
-    ProfScope ps(p->prof, st, P_FIX);
-    CU(bf::launch_combine_rows(cm->cw.as<uint4>(), p->n_d(), w, s->w_scalars, s->w_pi_first, st));
-    CU(bf::launch_combine_rows(cm->data.as<uint4>(), (size_t)1 << d, w, s->w_scalars, s->w_poly_first, st));
+    {
+      ProfScope ps(p->prof, st, P_FIX);
+      CU(bf::launch_combine_rows(cm->data.as<uint4>(), (size_t)1 << d, w, s->w_scalars, s->w_poly_first, st));
+    }
+    // The reference combines the codeword's rows the same way; the code is
+    // linear over the field, so that combination is the encoding of the
+    // combined polynomial: one width-1 encode of 2^d elements instead of
+    // w products per codeword row, the same values.
+    ProfScope ps(p->prof, st, P_ENCODE);
+    const cudaError_t e = bf::launch_encode(s->w_poly_first, s->w_pi_first, d, p->log2_c, 1,
+                                            p->tw_view.as<bf::TwiddleView>(), st, nullptr, nullptr, p->tune);
+    if (e != cudaSuccess) return fail(BF_ERR_CUDA, "encode of the combined polynomial: %s", cudaGetErrorString(e));
   }
   if (d == 0) {
     CU(cudaMemcpyAsync(pin, s->first_poly(), 16, cudaMemcpyDeviceToHost, st));

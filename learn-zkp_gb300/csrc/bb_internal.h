@@ -27,6 +27,8 @@ cudaError_t bb_launch_pow_table(uint32_t* out, size_t n, uint32_t g_mont, uint32
 // dense G_0.  A data word >= p sets *bad.
 cudaError_t bb_launch_encode(const uint32_t* m, uint32_t* cw, int d, int log2_c, int log2_k0, int generic, size_t w,
                              const uint32_t* tw, uint32_t* bad, cudaStream_t st);
+// out[k] = in[k] in canonical form (Montgomery in).
+cudaError_t bb_launch_from_mont(const uint32_t* in, uint32_t* out, size_t n, cudaStream_t st);
 // out[k] = in[k] in Montgomery form; *bad set for a word >= p.
 cudaError_t bb_launch_to_mont(const uint32_t* in, uint32_t* out, size_t n, uint32_t* bad, cudaStream_t st);
 // tinv[k] = (2 ts[k])^-1 (Montgomery); *bad set for a t that is 0 or >= p.

@@ -108,6 +108,12 @@ __global__ void bb_copy_mont_kernel(const uint32_t* in, uint32_t* out, size_t n,
   }
 }
 
+// Montgomery words back to canonical.
+__global__ void bb_from_mont_kernel(const uint32_t* in, uint32_t* out, size_t n) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+    out[k] = bb::from_mont(in[k]);
+}
+
 // The generic code's fold constants: (2 t)^-1 of every t (Montgomery out),
 // and a flag for a t that is zero or not canonical.
 __global__ void bb_tinv_kernel(const uint32_t* ts, uint32_t* tinv, size_t n, uint32_t* bad) {
@@ -688,6 +694,13 @@ static int ilog2_ceil(size_t v) {
   int r = 0;
   while (((size_t)1 << r) < v) ++r;
   return r;
+}
+
+cudaError_t bb_launch_from_mont(const uint32_t* in, uint32_t* out, size_t n, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  bb_from_mont_kernel<<<blocks_for(n, 256), 256, 0, st>>>(in, out, n);
+  count_launch();
+  return cudaGetLastError();
 }
 
 cudaError_t bb_launch_tinv(const uint32_t* ts, uint32_t* tinv, size_t n, uint32_t* bad, cudaStream_t st) {
