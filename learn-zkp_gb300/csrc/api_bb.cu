@@ -29,6 +29,12 @@ struct bf_bb_pcs {
   size_t Q = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
+  // bf_bb_commit copies host evaluations in slices on `aux`; the encode's
+  // first stage starts on each slice when its event completes
+  static constexpr int kH2DSlices = 8;
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ev_fork = nullptr;
+  cudaEvent_t slice_ev[kH2DSlices] = {};
   DevBuf tw;    // butterfly factors: layer s at 2^s - 1, 2^s of them (Montgomery)
   DevBuf tinv;  // fold constants: round i at n_0 (2^i - 1), (2 t_i[j])^-1 for j < n_i (Montgomery)
   DevBuf small;  // 4 KB: the canonical flag, sums, roots
@@ -72,12 +78,17 @@ struct bf_bb_pcs {
     if (device >= 0) {
       cudaSetDevice(device);
       if (stream) cudaStreamSynchronize(stream);
+      if (aux) cudaStreamSynchronize(aux);
       tw.release();
       tinv.release();
       small.release();
       ws.release();
       open_ws.release();
       if (own_stream && stream) cudaStreamDestroy(stream);
+      if (aux) cudaStreamDestroy(aux);
+      if (ev_fork) cudaEventDestroy(ev_fork);
+      for (cudaEvent_t e : slice_ev)
+        if (e) cudaEventDestroy(e);
     }
   }
 };
@@ -137,14 +148,15 @@ int eq_table_device(bf_bb_pcs* p, const std::vector<E>& x, uint32_t* ev) {
   return BF_OK;
 }
 
-int commit_device(bf_bb_pcs* p, bf_bb_commitment* cm, const uint32_t* data) {
+int commit_device(bf_bb_pcs* p, bf_bb_commitment* cm, const uint32_t* data, const cudaEvent_t* slice_ready = nullptr,
+                  int slices = 0) {
   const size_t w = cm->w, n = p->n_d();
   CU(cm->cw.alloc(4 * n * w));
   CU(cm->tree.alloc(64 * n));
   uint32_t* flag = p->small.as<uint32_t>();
   CU(cudaMemsetAsync(flag, 0, 4, p->stream));
   CU(bf::bb_launch_encode(data, cm->cw.as<uint32_t>(), p->d, p->log2_c, p->log2_k0, p->generic, w,
-                          p->tw.as<uint32_t>(), flag, p->stream));
+                          p->tw.as<uint32_t>(), flag, p->stream, slice_ready, slices));
   uint4* leaves = cm->tree.as<uint4>();
   CU(bf::bb_launch_leaves_rows(cm->cw.as<uint32_t>(), leaves, n, w, p->L, p->stream));
   uint4* root_dev = p->small.as<uint4>() + 2;
@@ -202,6 +214,9 @@ static int bb_setup(int device, int lambda, int log2_c, int log2_k0, int num_var
   }
   CU(p->pin.ensure(4096));
   CU(p->small.alloc(4096));
+  CU(cudaStreamCreateWithFlags(&p->aux, cudaStreamNonBlocking));
+  CU(cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming));
+  for (cudaEvent_t& e : p->slice_ev) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   CU(p->tw.alloc(4 * p->n_d()));
   CU(p->tinv.alloc(4 * p->n0() * (((size_t)1 << p->d) - 1) + 4));
   uint32_t* flag = p->small.as<uint32_t>();
@@ -277,8 +292,23 @@ int bf_bb_commit(bf_bb_pcs* p, const uint32_t* evals, size_t width, bf_bb_commit
   cm->w = width;
   const size_t bytes = 4 * width << p->num_vars;
   CU(cm->data.alloc(bytes));
-  CU(cudaMemcpyAsync(cm->data.p, evals, bytes, cudaMemcpyHostToDevice, p->stream));
-  TRY(commit_device(p, cm.get(), cm->data.as<uint32_t>()));
+  if (p->num_vars >= 16) {
+    // copy in slices on the second stream; the encode's first stage takes
+    // each slice as it lands (pinned `evals` overlap the copy with the encode)
+    const int S = bf_bb_pcs::kH2DSlices;
+    const size_t slice = bytes / S;
+    CU(cudaEventRecord(p->ev_fork, p->stream));
+    CU(cudaStreamWaitEvent(p->aux, p->ev_fork, 0));
+    for (int k = 0; k < S; ++k) {
+      CU(cudaMemcpyAsync(cm->data.as<uint8_t>() + k * slice, reinterpret_cast<const uint8_t*>(evals) + k * slice,
+                         slice, cudaMemcpyHostToDevice, p->aux));
+      CU(cudaEventRecord(p->slice_ev[k], p->aux));
+    }
+    TRY(commit_device(p, cm.get(), cm->data.as<uint32_t>(), p->slice_ev, S));
+  } else {
+    CU(cudaMemcpyAsync(cm->data.p, evals, bytes, cudaMemcpyHostToDevice, p->stream));
+    TRY(commit_device(p, cm.get(), cm->data.as<uint32_t>()));
+  }
   if (root) std::memcpy(root, cm->root, 32);
   bb_acquire(p);
   *out = cm.release();

@@ -25,8 +25,12 @@ cudaError_t bb_launch_pow_table(uint32_t* out, size_t n, uint32_t g_mont, uint32
 // layer s at tw[2^s - 1 + k]: g_s^k for the Reed–Solomon code (log2_k0 = 0),
 // ts[s - log2_n0][k] for the generic code (`generic`), whose stage 0 is the
 // dense G_0.  A data word >= p sets *bad.
+// With `slices` > 1, input slice k (data rows [k R / slices, (k+1) R / slices))
+// is ready when slice_ready[k] completes: the first stage waits for each slice
+// just before the part of its grid that reads it.
 cudaError_t bb_launch_encode(const uint32_t* m, uint32_t* cw, int d, int log2_c, int log2_k0, int generic, size_t w,
-                             const uint32_t* tw, uint32_t* bad, cudaStream_t st);
+                             const uint32_t* tw, uint32_t* bad, cudaStream_t st,
+                             const cudaEvent_t* slice_ready = nullptr, int slices = 0);
 // out[k] = in[k] in canonical form (Montgomery in).
 cudaError_t bb_launch_from_mont(const uint32_t* in, uint32_t* out, size_t n, cudaStream_t st);
 // out[k] = in[k] in Montgomery form; *bad set for a word >= p.

@@ -128,10 +128,11 @@ __global__ void bb_tinv_kernel(const uint32_t* ts, uint32_t* tinv, size_t n, uin
 // GenericRandomFoldableCode stage 0 (generic.rs:73-86, 120-125): every
 // chunk of k_0 message rows times G_0, g_0[i][j] = i^j, into n_0 codeword
 // rows: w[b n_0 + i] = sum_j i^j m[b k_0 + j], column by column.
-__global__ void bb_stage0_kernel(const uint32_t* __restrict__ m, uint32_t* __restrict__ cw, size_t rows_out,
-                                 uint32_t w, int log2_k0, int log2_n0, uint32_t* bad) {
-  const size_t total = rows_out * w;
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+__global__ void bb_stage0_kernel(const uint32_t* __restrict__ m, uint32_t* __restrict__ cw, size_t row0,
+                                 size_t rows_out, uint32_t w, int log2_k0, int log2_n0, uint32_t* bad) {
+  const size_t total = (row0 + rows_out) * w;
+  for (size_t e = row0 * w + (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (size_t)gridDim.x * blockDim.x) {
     const size_t x = e / w, c = e - x * w;
     const size_t b = x >> log2_n0;
     const uint32_t i = (uint32_t)(x & (((size_t)1 << log2_n0) - 1));
@@ -163,6 +164,7 @@ __global__ void bb_stage0_kernel(const uint32_t* __restrict__ m, uint32_t* __res
 struct BbPass {
   int s_lo, T, first, log2_c, lu, lc;
   uint32_t w, chunks;  // row width; column chunks of 2^lc
+  uint32_t block0;     // the launch runs blocks block0 + blockIdx.x (a first pass split by input slices)
 };
 
 // Tile coordinates of a block: the column chunk is the fastest-varying part
@@ -172,7 +174,8 @@ struct BbTile {
   uint32_t u_blk, c0;
   uint64_t hi;
   __device__ __forceinline__ BbTile(const BbPass& p) {
-    const uint32_t chunk = blockIdx.x % p.chunks, t = blockIdx.x / p.chunks;
+    const uint32_t b = blockIdx.x + p.block0;
+    const uint32_t chunk = b % p.chunks, t = b / p.chunks;
     const uint32_t nub_log = (uint32_t)(p.s_lo - p.lu);
     u_blk = t & ((1u << nub_log) - 1u);
     hi = t >> nub_log;
@@ -337,7 +340,7 @@ __global__ void __launch_bounds__(256) bb_dft_wide_kernel(const uint32_t* __rest
                                                          const uint32_t* __restrict__ tw, uint32_t* bad) {
   extern __shared__ uint32_t tile[];
   const int s_lo = p.s_lo, T = p.T;
-  const uint32_t chunk = blockIdx.x % p.chunks, t = blockIdx.x / p.chunks;
+  const uint32_t chunk = (blockIdx.x + p.block0) % p.chunks, t = (blockIdx.x + p.block0) / p.chunks;
   const uint32_t u = t & ((1u << s_lo) - 1u);
   const uint64_t x0 = ((uint64_t)(t >> s_lo) << (s_lo + T)) | u;
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
@@ -718,18 +721,32 @@ cudaError_t bb_launch_to_mont(const uint32_t* in, uint32_t* out, size_t n, uint3
 }
 
 cudaError_t bb_launch_encode(const uint32_t* m, uint32_t* cw, int d, int log2_c, int log2_k0, int generic, size_t w,
-                             const uint32_t* tw, uint32_t* bad, cudaStream_t st) {
+                             const uint32_t* tw, uint32_t* bad, cudaStream_t st, const cudaEvent_t* slice_ready,
+                             int slices) {
   const int L = d + log2_c + log2_k0;
   int lo = 0;  // the first DIT layer
+  if (slices < 1 || !slice_ready) slices = 1;
+  // input slice k (data rows [k 2^nv / slices, (k+1) 2^nv / slices)) feeds the
+  // first stage's k-th part: codeword rows [k 2^L / slices, (k+1) 2^L / slices)
+  auto wait_slice = [&](int k) { return slices > 1 ? cudaStreamWaitEvent(st, slice_ready[k], 0) : cudaSuccess; };
   if (generic) {
     const int log2_n0 = log2_c + log2_k0;
-    const size_t rows = (size_t)1 << L;
-    bb_stage0_kernel<<<blocks_for(rows * w, 256), 256, 0, st>>>(m, cw, rows, (uint32_t)w, log2_k0, log2_n0, bad);
-    count_launch();
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
+    const size_t rows = (size_t)1 << L, part = rows / (size_t)slices;
+    for (int k = 0; k < slices; ++k) {
+      cudaError_t e = wait_slice(k);
+      if (e != cudaSuccess) return e;
+      bb_stage0_kernel<<<blocks_for(part * w, 256), 256, 0, st>>>(m, cw, (size_t)k * part, part, (uint32_t)w, log2_k0,
+                                                                  log2_n0, bad);
+      count_launch();
+      e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+    }
     lo = log2_n0;  // the butterflies of ts[i-1] are layers log2_n0 + i - 1
   } else if (L == 0) {
+    for (int k = 0; k < slices; ++k) {
+      cudaError_t e = wait_slice(k);
+      if (e != cudaSuccess) return e;
+    }
     bb_copy_mont_kernel<<<blocks_for(w, 256), 256, 0, st>>>(m, cw, w, bad);
     count_launch();
     return cudaGetLastError();
@@ -777,15 +794,29 @@ cudaError_t bb_launch_encode(const uint32_t* m, uint32_t* cw, int d, int log2_c,
     if (threads > 256) threads = 256;
     if (threads < 32) threads = 32;
     const size_t blocks = ((size_t)1 << (L - T - lu)) * chunks;  // chunk fastest (BbTile)
-    if (lc == 5)  // wider than 16 columns: tiles of whole 32-column runs
-      bb_dft_wide_kernel<<<(unsigned)blocks, 256, words * sizeof(uint32_t), st>>>(m, cw, p, tw, bad);
-    else if (lu + lc == 5)  // a warp's lanes are one row run: registers take 4 layers per round trip
-      bb_dft_reg_kernel<<<(unsigned)blocks, 256, words * sizeof(uint32_t), st>>>(m, cw, p, tw, bad);
-    else
-      bb_dft_pass_kernel<<<(unsigned)blocks, threads, words * sizeof(uint32_t), st>>>(m, cw, p, tw, bad);
-    count_launch();
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
+    if (blocks > 0x7fffffffu) return cudaErrorInvalidValue;
+    // the first pass of a sliced input: its tiles, in order, read the slices in order
+    const int parts = (p.first && slices > 1 && (((size_t)1 << (L - T)) % slices) == 0) ? slices : 1;
+    if (p.first && parts == 1 && slices > 1)  // a first pass that cannot be split waits for every slice
+      for (int k = 0; k < slices; ++k) {
+        cudaError_t e = cudaStreamWaitEvent(st, slice_ready[k], 0);
+        if (e != cudaSuccess) return e;
+      }
+    for (int k = 0; k < parts; ++k) {
+      cudaError_t e = parts > 1 ? wait_slice(k) : cudaSuccess;
+      if (e != cudaSuccess) return e;
+      p.block0 = (uint32_t)(blocks / parts * k);
+      const unsigned grid = (unsigned)(blocks / parts);
+      if (lc == 5)  // wider than 16 columns: tiles of whole 32-column runs
+        bb_dft_wide_kernel<<<grid, 256, words * sizeof(uint32_t), st>>>(m, cw, p, tw, bad);
+      else if (lu + lc == 5)  // a warp's lanes are one row run: registers take 4 layers per round trip
+        bb_dft_reg_kernel<<<grid, 256, words * sizeof(uint32_t), st>>>(m, cw, p, tw, bad);
+      else
+        bb_dft_pass_kernel<<<grid, threads, words * sizeof(uint32_t), st>>>(m, cw, p, tw, bad);
+      count_launch();
+      e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+    }
     lo += T;
   }
   return cudaSuccess;
