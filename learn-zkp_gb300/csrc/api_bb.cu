@@ -434,12 +434,23 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
   // and records.
   const size_t rows = (size_t)1 << nv, half = rows >> 1;
   const size_t n_fold = p->n0() * (((size_t)1 << d) - 1);  // sum over rounds of n_i
-  const size_t wsz[] = {w > 1 ? 20 * rows : 0, w > 1 ? 20 * p->n_d() : 0, 20 * (half ? half : 1), 20 * half,
-                        20 * half,             20 * n_fold,             64 * n_fold,             8 * Q,
-                        Q * rec,               128,                     w > 1 ? 20 * rows : 0};
-  size_t off[12] = {0};
-  for (int k = 0; k < 11; ++k) off[k + 1] = off[k] + ((wsz[k] + 255) & ~(size_t)255);
-  if (p->open_ws.bytes < off[11]) CU(p->open_ws.alloc(off[11]));
+  const size_t wsz[] = {w > 1 ? 20 * rows : 0,
+                        w > 1 ? 20 * p->n_d() : 0,
+                        20 * (half ? half : 1),
+                        20 * half,
+                        20 * half,
+                        20 * n_fold,
+                        64 * n_fold,
+                        8 * Q,
+                        Q * rec,
+                        128,
+                        w > 1 ? 20 * rows : 0,
+                        sizeof(bf::BbTranscript) + sizeof(bf::BbRoundConsts),
+                        (20 + 72) * (size_t)(d > 0 ? d : 1)};
+  constexpr int kSlots = sizeof(wsz) / sizeof(wsz[0]);
+  size_t off[kSlots + 1] = {0};
+  for (int k = 0; k < kSlots; ++k) off[k + 1] = off[k] + ((wsz[k] + 255) & ~(size_t)255);
+  if (p->open_ws.bytes < off[kSlots]) CU(p->open_ws.alloc(off[kSlots]));
   uint8_t* base = p->open_ws.as<uint8_t>();
   uint32_t* polyE = reinterpret_cast<uint32_t*>(base + off[0]);
   uint32_t* piE = reinterpret_cast<uint32_t*>(base + off[1]);
@@ -452,7 +463,13 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
   unsigned long long* acc = reinterpret_cast<unsigned long long*>(base + off[9]);
   uint4* root_dev = reinterpret_cast<uint4*>(base + off[9] + 64);  // after the five sums
   uint32_t* poly_canon = reinterpret_cast<uint32_t*>(base + off[10]);  // width > 1: the combined poly, canonical
-  CU(p->pin.ensure(8 * Q + 20 * k0 + 20 * 64 + 256));
+  // the device transcript, the round constants, each round's challenge (20 bytes) and record (72)
+  bf::BbTranscript* tdev = reinterpret_cast<bf::BbTranscript*>(base + off[11]);
+  bf::BbRoundConsts* cdev = reinterpret_cast<bf::BbRoundConsts*>(base + off[11] + sizeof(bf::BbTranscript));
+  uint32_t* xs_dev = reinterpret_cast<uint32_t*>(base + off[12]);
+  uint8_t* rec_dev = base + off[12] + 20 * (size_t)(d > 0 ? d : 1);
+  CU(p->pin.ensure(8 * Q + 20 * k0 + 20 * 64 + 256 + sizeof(bf::BbTranscript) + sizeof(bf::BbRoundConsts) +
+                   72 * (size_t)d));
 
   // The polynomial and codeword the folding sumcheck runs on (basefold.rs:154-177).
   E claim;
@@ -488,14 +505,46 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
   // HalfEq over the point's first num_vars - 1 coordinates (eval_impr.rs)
   if (nv > 0) TRY(eq_table_device(p, std::vector<E>(r.begin(), r.end() - 1), heq));
 
-  bbh::Subclaim sc;
-  sc.value = claim;
+  // prove_interleaved_folding_sumcheck (basefold.rs:335-369) with the
+  // transcript on the device: every round is enqueued without waiting, the
+  // host reads the transcript back once at the end.
   std::vector<std::array<E, 2>> comp;
   std::vector<std::array<uint8_t, 32>> roots;
   bf::BbGather gp{};
   gp.pi0_base = w == 1;
+  const size_t tsz = sizeof(bf::BbTranscript) + sizeof(bf::BbRoundConsts);
+  if (d > 0) {
+    // the caller's transcript as a sponge: whole 136-byte blocks of its input
+    // absorbed here, the rest pending
+    bf::BbTranscript t{};
+    uint64_t A[25] = {0};
+    size_t pos = 0;
+    for (; pos + 136 <= tr.in.size(); pos += 136) {
+      for (int l = 0; l < 17; ++l) {
+        uint64_t v = 0;
+        std::memcpy(&v, tr.in.data() + pos + 8 * l, 8);
+        A[l] ^= v;
+      }
+      bfh::keccak_f(A);
+    }
+    for (int l = 0; l < 25; ++l) t.A[l] = make_uint2((uint32_t)A[l], (uint32_t)(A[l] >> 32));
+    t.pend_len = (uint32_t)(tr.in.size() - pos);
+    std::memcpy(t.pend, tr.in.data() + pos, t.pend_len);
+    t.out_len = (uint32_t)tr.out.size();
+    std::memcpy(t.out, tr.out.data(), t.out_len);
+    t.outer = bbh::to_dev(claim);
+    bf::BbRoundConsts c{};
+    for (int k = 0; k < nv; ++k) {
+      c.r[k] = bbh::to_dev(r[k]);
+      c.r_inv[k] = bbh::to_dev(es.r_inv[k]);
+      c.cf[k] = bbh::to_dev(es.correcting_factor((size_t)k));
+    }
+    std::memcpy(p->pin.p, &t, sizeof(t));
+    std::memcpy(p->pin.b() + sizeof(t), &c, sizeof(c));
+    CU(cudaMemcpyAsync(tdev, p->pin.p, tsz, cudaMemcpyHostToDevice, st));
+  }
   size_t fold_off = 0, tree_off = 0;
-  for (int k = 0; k < d; ++k) {  // prove_interleaved_folding_sumcheck (basefold.rs:335-369)
+  for (int k = 0; k < d; ++k) {
     const int i = d - 1 - k, li = p->log2_n0() + i;
     const int ri = i + lk;  // the sumcheck round (basefold.rs:356-361)
     const size_t ni = p->n_i(i);
@@ -507,24 +556,11 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
     CU(bf::launch_tree(tree, ni, st, root_dev, bf::Tune()));
     CU(cudaMemsetAsync(acc, 0, 40, st));
     CU(bf::bb_launch_dot(heq, poly, base_k, (size_t)1 << ri, acc, st));
-    CU(cudaMemcpyAsync(p->pin.p, acc, 96, cudaMemcpyDeviceToHost, st));
-    CU(cudaStreamSynchronize(st));
-    const unsigned long long* sums = reinterpret_cast<const unsigned long long*>(p->pin.p);
-    std::array<uint8_t, 32> root;
-    bfh::digest_from_interleaved(p->pin.b() + 64, root.data());
-    tr.observe(root.data(), 32);
-    E rp[3];
-    es.round_poly((size_t)ri, sc, base_k ? bbh::from_canonical_sums(sums) : bbh::from_dev_sums(sums), rp);
-    bbh::observe_e(tr, rp[0]);  // Eval::compress_round_poly keeps c0 and c2
-    bbh::observe_e(tr, rp[2]);
-    const E x = bbh::sample_e(tr);
-    es.fix_last(x);
-    sc.reduce(rp, 3, x);
-    comp.push_back({rp[0], rp[2]});
-    roots.push_back(root);
-    const bb::E5 xd = bbh::to_dev(x);
+    uint32_t* x_k = xs_dev + 5 * (size_t)k;
+    CU(bf::bb_launch_transcript_round(tdev, cdev, ri, nv, root_dev, acc, base_k, x_k, rec_dev + 72 * (size_t)k, st));
+    const bb::E5 unused{};
     uint32_t* fixed = fixbuf[k & 1];
-    CU(bf::bb_launch_fix(poly, base_k, fixed, (size_t)1 << ri, xd, st));
+    CU(bf::bb_launch_fix(poly, base_k, fixed, (size_t)1 << ri, unused, st, x_k));
     poly = fixed;
     bf::BbFold fp;
     fp.w = pi;
@@ -534,7 +570,8 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
     fp.n = ni;
     fp.leaves = i > 0 ? tree + 2 * (2 * ni) : nullptr;  // the next round's tree follows this one
     fp.leaf_bits = li - 1;
-    CU(bf::bb_launch_fold(fp, xd, st));
+    fp.xp = x_k;
+    CU(bf::bb_launch_fold(fp, unused, st));
     pi = fp.out;
     fold_off += ni;
     tree_off += 2 * ni;
@@ -545,10 +582,14 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
     const int fin_base = d == 0 && base_round;  // still the caller's base-field data
     CU(cudaMemcpyAsync(p->pin.p, poly, (fin_base ? 4 : 20) * k0, cudaMemcpyDeviceToHost, st));
     const size_t chk_off = 20 * k0 + 64;
+    const size_t t_off = chk_off + 20 * 64;  // then the transcript, then the round records
     size_t nchk = 0;
     if (d > 0) {  // debug_assert_eq!(encode0(final_poly), pi) (basefold.rs:189), up to 64 entries
       nchk = p->n0() < 64 ? p->n0() : 64;
       CU(cudaMemcpyAsync(p->pin.b() + chk_off, pi, 20 * nchk, cudaMemcpyDeviceToHost, st));
+      CU(cudaMemcpyAsync(p->pin.b() + t_off, tdev, sizeof(bf::BbTranscript), cudaMemcpyDeviceToHost, st));
+      CU(cudaMemcpyAsync(p->pin.b() + t_off + sizeof(bf::BbTranscript), rec_dev, 72 * (size_t)d,
+                         cudaMemcpyDeviceToHost, st));
     }
     CU(cudaStreamSynchronize(st));
     for (size_t t = 0; t < k0; ++t) {
@@ -569,6 +610,23 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
       for (int t = 0; t < 5; ++t) e.c[t] = bb::from_mont(m[t]);
       if (e != p->encode0_at(fin, q))
         return fail(BF_ERR_CHECK, "the last folded codeword is not the encoding of the final polynomial");
+    }
+    if (d > 0) {
+      // the caller's transcript continues from the device's: after a sample the
+      // sponge holds no absorbed block, only pending input bytes
+      bf::BbTranscript t;
+      std::memcpy(&t, p->pin.b() + t_off, sizeof(t));
+      for (int l = 0; l < 25; ++l)
+        if (t.A[l].x | t.A[l].y) return fail(BF_ERR_CHECK, "device transcript left an absorbed block");
+      tr.in.assign(t.pend, t.pend + t.pend_len);
+      tr.out.assign(t.out, t.out + t.out_len);
+      const uint8_t* rb = p->pin.b() + t_off + sizeof(bf::BbTranscript);
+      for (int k = 0; k < d; ++k) {
+        std::array<uint8_t, 32> root;
+        std::memcpy(root.data(), rb + 72 * k, 32);
+        roots.push_back(root);
+        comp.push_back({bbh::load(rb + 72 * k + 32), bbh::load(rb + 72 * k + 52)});
+      }
     }
   }
   for (const E& e : fin) bbh::observe_e(tr, e);

@@ -60,8 +60,9 @@ cudaError_t bb_launch_eq_expand(uint32_t* ev, size_t h, const bb::E5& x, cudaStr
 cudaError_t bb_launch_dot(const uint32_t* heq, const uint32_t* poly, int base, size_t n, unsigned long long* acc,
                           cudaStream_t st);
 // out[b] = in[b] + x (in[b + half] - in[b]); `base`: in is canonical data.
+// x is *xp (Montgomery, device memory) when xp is set.
 cudaError_t bb_launch_fix(const uint32_t* in, int base, uint32_t* out, size_t half, const bb::E5& x,
-                          cudaStream_t st);
+                          cudaStream_t st, const uint32_t* xp = nullptr);
 
 // Fold of round i (code.rs:66-84): out[j] = interpolate(tinv[j], w[j],
 // w[j + n], x), j < n = n_i, with the next round's leaves when `leaves` is set.
@@ -73,8 +74,39 @@ struct BbFold {
   size_t n;
   uint4* leaves;          // n/2 leaves of the next round, or null
   int leaf_bits;          // log2(n/2)
+  const uint32_t* xp;     // the challenge in device memory (Montgomery), or null: the x argument
 };
 cudaError_t bb_launch_fold(const BbFold& p, const bb::E5& x, cudaStream_t st);
+
+// The open's Fiat–Shamir transcript on the device: HashChallenger<u8,
+// Keccak256Hash, 32> (p3/src/challenger.rs) as a sponge — the lanes of the
+// input blocks absorbed so far plus the pending input bytes — and its output
+// buffer, with the EvalProver subclaims of the folding sumcheck.  Field
+// elements are Montgomery form.
+struct BbTranscript {
+  uint2 A[25];          // lanes (low word, high word) of the absorbed input blocks
+  uint8_t pend[256];    // input bytes not yet absorbed (fewer than 136 between rounds)
+  uint32_t pend_len;
+  uint8_t out[32];      // output buffer: bytes out[0 .. out_len), popped from the end
+  uint32_t out_len;
+  bb::E5 outer;         // the open's subclaim (sumcheck/src/lib.rs:18-48)
+  bb::E5 inner;         // EvalImprProver's inner subclaim value
+  bb::E5 xs[kBbMaxRounds];  // challenges in sampling order
+  uint32_t rounds;
+};
+// Per sumcheck round ri (< num_vars): the point coordinate, its inverse and
+// the correcting factor prod_{k >= ri} (1 - r_k)^-1 (eval_impr.rs:83-90).
+struct BbRoundConsts {
+  bb::E5 r[kBbMaxRounds], r_inv[kBbMaxRounds], cf[kBbMaxRounds];
+};
+// One folding-sumcheck round's transcript: observe the round's folded-codeword
+// root (interleaved digest at root_dev), compute the round polynomial from the
+// GPU sum (Montgomery sums, or canonical ones when `canonical`), observe its
+// compressed form, sample the challenge into x_out (Montgomery) and record
+// the root and the compressed polynomial (72 canonical bytes) at rec.
+cudaError_t bb_launch_transcript_round(BbTranscript* t, const BbRoundConsts* c, int ri, int num_vars,
+                                       const uint4* root_dev, const unsigned long long* sums, int canonical,
+                                       uint32_t* x_out, uint8_t* rec, cudaStream_t st);
 
 // Query openings in the proof's bincode layout, one record per query:
 // u64 w, w canonical words, u64 L, L digests, u64 d, then per round k:

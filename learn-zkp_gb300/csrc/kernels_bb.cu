@@ -575,7 +575,8 @@ __global__ void __launch_bounds__(256) bb_dot_kernel(const uint32_t* __restrict_
 }
 
 // fix_last_var (multilinear.rs:183-198): out[b] = lo + x (hi - lo).
-__global__ void bb_fix_kernel(const uint32_t* in, int base, uint32_t* out, size_t half, E5 x) {
+__global__ void bb_fix_kernel(const uint32_t* in, int base, uint32_t* out, size_t half, E5 x, const uint32_t* xp) {
+  if (xp) x = ld_e5(xp, 0);
   for (size_t b = (size_t)blockIdx.x * blockDim.x + threadIdx.x; b < half; b += (size_t)gridDim.x * blockDim.x) {
     if (base) {
       const uint32_t lo = bb::to_mont(in[b]), d = bb::sub(bb::to_mont(in[b + half]), lo);
@@ -599,6 +600,7 @@ __device__ __forceinline__ E5 bb_interp(const E5& lo, const E5& hi, uint32_t t, 
   return bb::e_add(l, bb::e_mul(bb::e_sub(h, l), x));
 }
 __global__ void __launch_bounds__(128) bb_fold_kernel(BbFold p, E5 x) {
+  if (p.xp) x = ld_e5(p.xp, 0);
   const size_t n = p.n, q = n >> 1;
   const size_t work = q ? q : 1;  // n = 1: the single output, no leaves
   for (size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x; s < work; s += (size_t)gridDim.x * blockDim.x) {
@@ -613,6 +615,221 @@ __global__ void __launch_bounds__(128) bb_fold_kernel(BbFold p, E5 x) {
     }
     if (p.leaves && q) store_digest(p.leaves, brev_bits(s, p.leaf_bits), hash_pair_e5(f[0], f[1]));
   }
+}
+
+// ---- the open's transcript on the device ---------------------------------------------
+// One warp per round: the sponge's lanes live in lanes 0..24 (WarpKeccak), the
+// pending input and the output bytes in shared memory, the scalar algebra on
+// lane 0 except the delta product, which is a warp product tree.
+namespace {
+struct TrCtx {
+  uint8_t pend[256];
+  uint8_t out[32];
+  int pend_len, out_len;
+};
+
+// XOR the 136-byte block blk (shared memory) into the sponge and permute.
+__device__ __forceinline__ uint2 tr_absorb(const WarpKeccak& wk, uint2 a, const uint8_t* blk) {
+  if (wk.lane < 17) {
+    uint32_t lo = 0, hi = 0;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      lo |= (uint32_t)blk[8 * wk.lane + b] << (8 * b);
+      hi |= (uint32_t)blk[8 * wk.lane + 4 + b] << (8 * b);
+    }
+    a.x ^= lo;
+    a.y ^= hi;
+  }
+  return wk.permute<false>(a);
+}
+
+// observe (challenger.rs:51-60): append n bytes (n <= 72) to the input and
+// clear the output; a full block is absorbed.  All lanes call.
+__device__ uint2 tr_observe(const WarpKeccak& wk, uint2 a, TrCtx& c, const uint8_t* src, int n) {
+  const int len = c.pend_len;
+  for (int i = wk.lane; i < n; i += 32) c.pend[len + i] = src[i];
+  __syncwarp();
+  int total = len + n;
+  if (total >= 136) {
+    a = tr_absorb(wk, a, c.pend);
+    __syncwarp();
+    uint8_t keep[3];  // the bytes past the block move to the front, 3 per lane at most
+    int m = 0;
+    for (int i = 136 + wk.lane; i < total; i += 32) keep[m++] = c.pend[i];
+    __syncwarp();
+    m = 0;
+    for (int i = 136 + wk.lane; i < total; i += 32) c.pend[i - 136] = keep[m++];
+    total -= 136;
+  }
+  __syncwarp();
+  if (wk.lane == 0) {
+    c.pend_len = total;
+    c.out_len = 0;
+  }
+  __syncwarp();
+  return a;
+}
+
+// One output byte, popped from the end; an empty output is refilled with
+// keccak256 of the input, which becomes the new input.  All lanes call and
+// get the byte.
+__device__ uint8_t tr_sample_byte(const WarpKeccak& wk, uint2& a, TrCtx& c) {
+  if (c.out_len == 0) {
+    const int len = c.pend_len;
+    uint8_t blk8[8];
+    if (wk.lane < 17)
+      for (int b = 0; b < 8; ++b) {
+        const int k = 8 * wk.lane + b;
+        uint8_t v = k < len ? c.pend[k] : 0;
+        if (k == len) v ^= 0x01u;
+        if (k == 135) v ^= 0x80u;
+        blk8[b] = v;
+      }
+    if (wk.lane < 17) {
+      uint32_t lo = 0, hi = 0;
+      for (int b = 0; b < 4; ++b) {
+        lo |= (uint32_t)blk8[b] << (8 * b);
+        hi |= (uint32_t)blk8[4 + b] << (8 * b);
+      }
+      a.x ^= lo;
+      a.y ^= hi;
+    }
+    a = wk.permute<false>(a);
+    __syncwarp();
+    if (wk.lane < 4)
+      for (int b = 0; b < 4; ++b) {
+        const uint8_t lo = (uint8_t)(a.x >> (8 * b)), hi = (uint8_t)(a.y >> (8 * b));
+        c.out[8 * wk.lane + b] = lo;
+        c.out[8 * wk.lane + 4 + b] = hi;
+        c.pend[8 * wk.lane + b] = lo;
+        c.pend[8 * wk.lane + 4 + b] = hi;
+      }
+    a = make_uint2(0, 0);  // the digest is the whole new input, still pending
+    __syncwarp();
+    if (wk.lane == 0) {
+      c.pend_len = 32;
+      c.out_len = 32;
+    }
+    __syncwarp();
+  }
+  const uint8_t b = c.out[c.out_len - 1];
+  __syncwarp();
+  if (wk.lane == 0) c.out_len -= 1;
+  __syncwarp();
+  return b;
+}
+
+// FromUniformBytes for BabyBear: 4 bytes LE shifted right by one, redrawn
+// while >= p; an extension element is five of them (challenger.rs:62-74).
+__device__ E5 tr_sample_e(const WarpKeccak& wk, uint2& a, TrCtx& c) {
+  E5 e;
+  for (int k = 0; k < 5; ++k) {
+    uint32_t v;
+    do {
+      v = 0;
+      for (int b = 0; b < 4; ++b) v |= (uint32_t)tr_sample_byte(wk, a, c) << (8 * b);
+      v >>= 1;
+    } while (v >= bb::P);
+    e.c[k] = bb::to_mont(v);
+  }
+  return e;
+}
+
+__device__ __forceinline__ void e5_bytes(const E5& e, uint8_t* b) {
+  for (int k = 0; k < 5; ++k) {
+    const uint32_t v = bb::from_mont(e.c[k]);
+    for (int q = 0; q < 4; ++q) b[4 * k + q] = (uint8_t)(v >> (8 * q));
+  }
+}
+__device__ __forceinline__ E5 shfl_e5(const E5& e, int src) {
+  E5 r;
+#pragma unroll
+  for (int k = 0; k < 5; ++k) r.c[k] = __shfl_sync(0xffffffffu, e.c[k], src);
+  return r;
+}
+}  // namespace
+
+// One folding-sumcheck round (basefold.rs:340-362 with sumcheck/src/lib.rs:81-103
+// and EvalImprProver's round polynomial, eval_impr.rs:41-58, 150-162), one warp.
+__global__ void __launch_bounds__(32) bb_transcript_round_kernel(BbTranscript* t, const BbRoundConsts* c, int ri,
+                                                                int num_vars, const uint4* root_dev,
+                                                                const unsigned long long* sums, int canonical,
+                                                                uint32_t* x_out, uint8_t* rec) {
+  __shared__ TrCtx ctx;
+  __shared__ uint8_t msg[72];  // the root, then the compressed round polynomial (canonical bytes)
+  const WarpKeccak wk;
+  const int lane = wk.lane;
+  for (int q = lane; q < 256; q += 32) ctx.pend[q] = t->pend[q];
+  ctx.out[lane] = t->out[lane];
+  if (lane == 0) {
+    ctx.pend_len = (int)t->pend_len;
+    ctx.out_len = (int)t->out_len;
+    const Digest dg = digest_bytes(load_digest(root_dev, 0));
+    const uint32_t words[8] = {dg.lo.x, dg.lo.y, dg.lo.z, dg.lo.w, dg.hi.x, dg.hi.y, dg.hi.z, dg.hi.w};
+    for (int i = 0; i < 8; ++i)
+      for (int b = 0; b < 4; ++b) msg[4 * i + b] = (uint8_t)(words[i] >> (8 * b));
+  }
+  uint2 a = lane < 25 ? t->A[lane] : make_uint2(0, 0);
+  __syncwarp();
+  a = tr_observe(wk, a, ctx, msg, 32);
+  // delta: eq_eval(r[ri+1..], inner.r()) (multilinear.rs:224-229) as a product
+  // tree over the warp, factor j = 2 x y + 1 - x - y with x = r[ri+1+j] and y
+  // the challenge sampled j+1 rounds ago
+  const bool last = ri + 1 == num_vars;
+  const E5 one = bb::e_from(bb::MONT_ONE);
+  const int k = (int)t->rounds;
+  const int nf = last ? 0 : min(k, num_vars - ri - 1);
+  E5 f = one;
+  if (lane < nf) {
+    const E5 x = c->r[ri + 1 + lane], y = t->xs[k - 1 - lane];
+    const E5 xy = bb::e_mul(x, y);
+    f = bb::e_sub(bb::e_sub(bb::e_add(bb::e_add(xy, xy), one), x), y);
+  }
+  for (int o = 16; o > 0; o >>= 1) f = bb::e_mul(f, shfl_e5(f, lane ^ o));  // every lane: the product
+  // the round polynomial from S = sum_b half_eq[b] poly[b] (lane 0)
+  E5 c0{}, c1{}, rp0{}, rp1{}, rp2{};
+  if (lane == 0) {
+    E5 S;
+    for (int q = 0; q < 5; ++q) {
+      const uint32_t v = (uint32_t)(sums[q] % bb::P);
+      S.c[q] = canonical ? bb::to_mont(v) : v;
+    }
+    const E5 sc = last ? t->outer : t->inner;
+    const E5 r = c->r[ri], omr = bb::e_sub(one, r);
+    c0 = bb::e_mul(c->cf[ri], S);
+    const E5 e1 = bb::e_mul(bb::e_sub(sc, bb::e_mul(omr, c0)), c->r_inv[ri]);
+    c1 = bb::e_sub(e1, c0);
+    const E5 d0 = bb::e_mul(f, omr), d1 = bb::e_mul(f, bb::e_sub(r, omr));
+    rp0 = bb::e_mul(c0, d0);
+    rp1 = bb::e_add(bb::e_mul(c0, d1), bb::e_mul(c1, d0));
+    rp2 = bb::e_mul(c1, d1);
+    e5_bytes(rp0, msg + 32);  // Eval::compress_round_poly keeps c0 and c2
+    e5_bytes(rp2, msg + 52);
+  }
+  __syncwarp();
+  for (int q = lane; q < 72; q += 32) rec[q] = msg[q];
+  a = tr_observe(wk, a, ctx, msg + 32, 40);
+  const E5 x = tr_sample_e(wk, a, ctx);
+  if (lane == 0) {
+    t->inner = bb::e_add(c0, bb::e_mul(c1, x));                            // fix_last_var (eval.rs:108-111)
+    t->outer = bb::e_add(rp0, bb::e_mul(x, bb::e_add(rp1, bb::e_mul(x, rp2))));  // horner (univariate.rs:5-12)
+    t->xs[k] = x;
+    t->rounds = (uint32_t)(k + 1);
+    st_e5(x_out, 0, x);
+    t->pend_len = (uint32_t)ctx.pend_len;
+    t->out_len = (uint32_t)ctx.out_len;
+  }
+  for (int q = lane; q < 256; q += 32) t->pend[q] = ctx.pend[q];
+  t->out[lane] = ctx.out[lane];
+  if (lane < 25) t->A[lane] = a;
+}
+
+cudaError_t bb_launch_transcript_round(BbTranscript* t, const BbRoundConsts* c, int ri, int num_vars,
+                                       const uint4* root_dev, const unsigned long long* sums, int canonical,
+                                       uint32_t* x_out, uint8_t* rec, cudaStream_t st) {
+  bb_transcript_round_kernel<<<1, 32, 0, st>>>(t, c, ri, num_vars, root_dev, sums, canonical, x_out, rec);
+  count_launch();
+  return cudaGetLastError();
 }
 
 // ---- query openings (basefold.rs:200-222) ---------------------------------------
@@ -874,8 +1091,9 @@ cudaError_t bb_launch_dot(const uint32_t* heq, const uint32_t* poly, int base, s
   return cudaGetLastError();
 }
 
-cudaError_t bb_launch_fix(const uint32_t* in, int base, uint32_t* out, size_t half, const E5& x, cudaStream_t st) {
-  bb_fix_kernel<<<blocks_for(half, 256), 256, 0, st>>>(in, base, out, half, x);
+cudaError_t bb_launch_fix(const uint32_t* in, int base, uint32_t* out, size_t half, const E5& x, cudaStream_t st,
+                          const uint32_t* xp) {
+  bb_fix_kernel<<<blocks_for(half, 256), 256, 0, st>>>(in, base, out, half, x, xp);
   count_launch();
   return cudaGetLastError();
 }
