@@ -1,7 +1,8 @@
 // Host-side scalars of the prime-field prover and verifier: BabyBear and its
 // quintic extension E = F[X] / (X^5 - 2) in canonical form, the transcript's
-// field sampling, and the per-round sumcheck algebra.  Only O(num_vars)
-// values pass through here; every array stays on the GPU.
+// field sampling, the verifier's sumcheck algebra and the prover's per-point
+// constants.  Only O(num_vars) values pass through here; every array stays
+// on the GPU.
 #pragma once
 #include <cstdint>
 #include <cstring>
@@ -203,13 +204,11 @@ struct Subclaim {
   }
 };
 
-// The scalar side of EvalProver over EvalImprProver with HalfEq (sumcheck/
-// src/function/eval.rs:27-116, eval_impr.rs:13-207): the GPU supplies the
-// sum over the hypercube half of half_eq * poly each round.
+// The constants of EvalProver over EvalImprProver with HalfEq (sumcheck/src/
+// function/eval.rs:27-116, eval_impr.rs:13-207) that the device transcript
+// needs: the point's coordinates, their inverses and the correcting factors.
 struct EvalScalars {
   std::vector<E> r, r_inv, one_minus_r_inv;
-  Subclaim inner;
-  E inner_rp[2];
   // false when a coordinate is 0, or 1 below the last (their inverses are taken)
   bool init(const std::vector<E>& point) {
     r = point;
@@ -226,34 +225,11 @@ struct EvalScalars {
     }
     return true;
   }
-  size_t num_vars() const { return r.size(); }
   E correcting_factor(size_t round) const {  // eval_impr.rs:83-90
     E p = E::one();
     for (size_t k = round; k < one_minus_r_inv.size(); ++k) p = emul(p, one_minus_r_inv[k]);
     return p;
   }
-  // compute_round_poly given S = sum_b half_eq[b] poly[b] (eval_impr.rs:
-  // 41-58, 150-162): three coefficients of the round polynomial.
-  void round_poly(size_t round, const Subclaim& outer, const E& S, E rp[3]) {
-    const Subclaim& sc = round + 1 == num_vars() ? outer : inner;
-    const E c0 = emul(correcting_factor(round), S);
-    const E e1 = emul(esub(sc.value, emul(esub(E::one(), r[round]), c0)), r_inv[round]);
-    const E c1 = esub(e1, c0);
-    inner_rp[0] = c0;
-    inner_rp[1] = c1;
-    E scalar = E::one();
-    if (round + 1 != num_vars()) {
-      const std::vector<E> rr = sc.r();
-      const size_t rest = r.size() - (round + 1);
-      scalar = eq_eval(r.data() + round + 1, rr.data(), rest < rr.size() ? rest : rr.size());
-    }
-    const E d0 = emul(scalar, esub(E::one(), r[round]));
-    const E d1 = emul(scalar, esub(r[round], esub(E::one(), r[round])));
-    rp[0] = emul(c0, d0);
-    rp[1] = eadd(emul(c0, d1), emul(c1, d0));
-    rp[2] = emul(c1, d1);
-  }
-  void fix_last(const E& x) { inner.reduce(inner_rp, 2, x); }  // eval.rs:108-111
 };
 
 }  // namespace bbh
