@@ -45,6 +45,9 @@ def parse():
                     help="one product sumcheck of K polys over 2^N points, nothing else (for ncu)")
     ap.add_argument("--profile-verify", type=int, nargs=2, metavar=("N", "COUNT"),
                     help="one batched verify of COUNT proofs of 2^N evaluations, nothing else (for ncu)")
+    ap.add_argument("--profile-wide", type=int, metavar="LOG_N",
+                    help="one commit + eval + open of a 2^LOG_N x 256 Polyval matrix (the reference's binary "
+                         "bench shape), nothing else (for ncu)")
     ap.add_argument("--profile-prime", type=int, nargs=3, metavar=("GENERIC", "LOG_N", "LOG_POLYS"),
                     help="one prime-field commit + open (GENERIC 0: Reed-Solomon, 1: generic code with "
                          "log2_k_0 = 3) of a 2^LOG_N x 2^LOG_POLYS BabyBear matrix, nothing else (for ncu)")
@@ -829,6 +832,16 @@ def main():
         sc_pcs = bg.Basefold.setup(bg.BasefoldConfig(bg.BinaryReedSolomonCode(128, 1, 0)), device=local)
         sc_pcs.prove_sumcheck_device(k, ns, polys.data_ptr(), bg.rand.random_elems(1, 77),
                                      bg.GenericChallenger(b"sumcheck"))
+        torch.cuda.synchronize()
+        return
+    if args.profile_wide:
+        wn, ww = args.profile_wide, 256
+        wpcs = bg.Basefold.setup(bg.BasefoldConfig(bg.BinaryReedSolomonCode(128, 1, wn)), device=local)
+        wdata = bg.rand.random_elems((ww << wn) + wn, 40 + wn)
+        wdev = torch.from_numpy(wdata[: ww << wn]).to(f"cuda:{local}")
+        wcomm = wpcs.commit_device(wdev.data_ptr(), width=ww, keep=wdev)
+        wvals = wpcs.eval(wpcs.data(wcomm), wdata[ww << wn:])
+        wpcs.open(wcomm, [bg.PolyEvals(wvals, wdata[ww << wn:])], bg.GenericChallenger.keccak256())
         torch.cuda.synchronize()
         return
     if args.profile_prime:
