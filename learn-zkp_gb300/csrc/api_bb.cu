@@ -8,6 +8,7 @@
 // the round's sum).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <memory>
 #include <vector>
@@ -40,6 +41,7 @@ struct bf_bb_pcs {
   DevBuf small;  // 4 KB: the canonical flag, sums, roots
   DevBuf ws;       // grow-only scratch of bf_bb_eval
   DevBuf open_ws;  // grow-only workspace of bf_bb_open
+  DevBuf data_ws;  // grow-only copy of host rows for bf_bb_eval_data
   PinnedBuf pin;
 
   size_t c() const { return (size_t)1 << log2_c; }
@@ -84,6 +86,7 @@ struct bf_bb_pcs {
       small.release();
       ws.release();
       open_ws.release();
+      data_ws.release();
       if (own_stream && stream) cudaStreamDestroy(stream);
       if (aux) cudaStreamDestroy(aux);
       if (ev_fork) cudaEventDestroy(ev_fork);
@@ -394,13 +397,11 @@ int bf_bb_eval_data(bf_bb_pcs* p, const void* evals, int on_device, size_t width
     return fail(BF_ERR_ARG, "device evaluations must be 4-byte aligned");
   DeviceGuard g(p->device);
   if (on_device) return eval_device_rows(p, static_cast<const uint32_t*>(evals), width, point, values);
-  DevBuf copy;  // host rows: copied in on the pcs's stream
+  // host rows: copied in on the pcs's stream into a grow-only buffer
   const size_t bytes = 4 * width << p->num_vars;
-  CU(copy.alloc(bytes));
-  CU(cudaMemcpyAsync(copy.p, evals, bytes, cudaMemcpyHostToDevice, p->stream));
-  const int rc = eval_device_rows(p, copy.as<uint32_t>(), width, point, values);
-  cudaStreamSynchronize(p->stream);  // before the copy is freed (also on an error)
-  return rc;
+  if (p->data_ws.bytes < bytes) CU(p->data_ws.alloc(bytes));
+  CU(cudaMemcpyAsync(p->data_ws.p, evals, bytes, cudaMemcpyHostToDevice, p->stream));
+  return eval_device_rows(p, p->data_ws.as<uint32_t>(), width, point, values);
 }
 
 int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, const uint8_t* values,
@@ -446,7 +447,8 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
                         128,
                         w > 1 ? 20 * rows : 0,
                         sizeof(bf::BbTranscript) + sizeof(bf::BbRoundConsts),
-                        (20 + 72) * (size_t)(d > 0 ? d : 1)};
+                        (20 + 72) * (size_t)(d > 0 ? d : 1),
+                        w > 1 ? 20 * w : 0};
   constexpr int kSlots = sizeof(wsz) / sizeof(wsz[0]);
   size_t off[kSlots + 1] = {0};
   for (int k = 0; k < kSlots; ++k) off[k + 1] = off[k] + ((wsz[k] + 255) & ~(size_t)255);
@@ -468,8 +470,10 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
   bf::BbRoundConsts* cdev = reinterpret_cast<bf::BbRoundConsts*>(base + off[11] + sizeof(bf::BbTranscript));
   uint32_t* xs_dev = reinterpret_cast<uint32_t*>(base + off[12]);
   uint8_t* rec_dev = base + off[12] + 20 * (size_t)(d > 0 ? d : 1);
-  CU(p->pin.ensure(8 * Q + 20 * k0 + 20 * 64 + 256 + sizeof(bf::BbTranscript) + sizeof(bf::BbRoundConsts) +
-                   72 * (size_t)d));
+  uint32_t* scal_dev = reinterpret_cast<uint32_t*>(base + off[13]);  // width > 1: the batching scalars
+  CU(p->pin.ensure(std::max<size_t>(8 * Q + 20 * k0 + 20 * 64 + 256 + sizeof(bf::BbTranscript) +
+                                         sizeof(bf::BbRoundConsts) + 72 * (size_t)d,
+                                     20 * w)));
 
   // The polynomial and codeword the folding sumcheck runs on (basefold.rs:154-177).
   E claim;
@@ -482,12 +486,10 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
     const std::vector<E> s = bbh::scalars_by_eq(w, tr);
     for (size_t c = 0; c < w; ++c) claim = bbh::eadd(claim, bbh::emul(s[c], vals[c]));
     // s R^2 against the canonical evaluations
-    std::vector<bb::E5> sd(w);
+    bb::E5* sd = reinterpret_cast<bb::E5*>(p->pin.p);
     for (size_t c = 0; c < w; ++c) sd[c] = bbh::to_dev2(s[c]);
-    DevBuf sdev;
-    CU(sdev.alloc(20 * w));
-    CU(cudaMemcpyAsync(sdev.p, sd.data(), 20 * w, cudaMemcpyHostToDevice, st));
-    CU(bf::bb_launch_combine(cm->data.as<uint32_t>(), rows, w, sdev.as<uint32_t>(), polyE, st));
+    CU(cudaMemcpyAsync(scal_dev, sd, 20 * w, cudaMemcpyHostToDevice, st));
+    CU(bf::bb_launch_combine(cm->data.as<uint32_t>(), rows, w, scal_dev, polyE, st));
     // The reference combines the codeword's rows the same way; both codes are
     // linear over the base field, so that combination is the encoding of the
     // combined polynomial, coefficient by coefficient: a 5-column encode of
@@ -497,7 +499,7 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
     CU(cudaMemsetAsync(flag, 0, 4, st));
     CU(bf::bb_launch_encode(poly_canon, piE, p->d, p->log2_c, p->log2_k0, p->generic, 5, p->tw.as<uint32_t>(), flag,
                             st));
-    CU(cudaStreamSynchronize(st));  // sd and sdev go out of scope
+    CU(cudaStreamSynchronize(st));  // the staging of the scalars is reused below
     poly = polyE;
     pi = piE;
     base_round = 0;
