@@ -164,6 +164,7 @@ __global__ void bb_stage0_kernel(const uint32_t* __restrict__ m, uint32_t* __res
 struct BbPass {
   int s_lo, T, first, log2_c, lu, lc;
   uint32_t w, chunks;  // row width; column chunks of 2^lc
+  int chunks_log;      // log2(chunks) when chunks is a power of two, else -1
   uint32_t block0;     // the launch runs blocks block0 + blockIdx.x (a first pass split by input slices)
 };
 
@@ -332,74 +333,137 @@ __global__ void __launch_bounds__(256) bb_dft_reg_kernel(const uint32_t* __restr
 }
 
 // The same pass for matrices wider than 16 columns (lc = 5, lu = 0): a tile is
-// 2^T rows x 32 columns, row a of the tile at matrix row x0 + a 2^s_lo, and
-// each thread walks its rows with one pointer increment per element instead
-// of recomputing the row index and a 64-bit product (the general loader's
-// per-element address arithmetic dominated the pass's instruction count).
+// 2^T rows x 32 columns, row a of the tile at matrix row x0 + a 2^s_lo, run by
+// eight warps.  The tile height is a template parameter, so the layer groups,
+// each warp's share of the rows and every shared-memory offset are compile-time
+// constants: the pass's instructions are the Montgomery butterflies, the
+// factor loads and one pointer step per global access.
+__host__ __device__ constexpr int bb_wide_group(int T, int l0) {  // layers of the register group starting at l0 (bb_group_layers)
+  const int r = T - l0 < 4 ? T - l0 : 4;
+  const int cap = T - 3 > 1 ? T - 3 : 1;
+  return r < cap ? r : cap;
+}
+
+// One register group: layers L0 .. L0 + R - 1 of the tile.  Warp q of the
+// 2^(T - R) groups takes rows a_base | j 2^L0 (j < 2^R) into registers.
+template <int T, int L0, int R>
+__device__ __forceinline__ void bb_wide_layers(uint32_t* tile, int s_lo, uint32_t u, uint32_t lane, uint32_t warp,
+                                               const uint32_t* __restrict__ tw) {
+  constexpr uint32_t kWork = 1u << (T - R);
+  constexpr uint32_t kIters = kWork >= 8 ? kWork / 8 : 1;
+#pragma unroll
+  for (uint32_t it = 0; it < kIters; ++it) {
+    const uint32_t q = warp + 8u * it;
+    if (kWork < 8 && q >= kWork) return;
+    const uint32_t qlo = q & ((1u << L0) - 1u);
+    uint32_t* rp = tile + ((((q >> L0) << (L0 + R)) | qlo) << 5) + lane;
+    uint32_t v[1 << R];
+#pragma unroll
+    for (int j = 0; j < (1 << R); ++j) v[j] = rp[j << (L0 + 5)];
+    // the rows of the pair (j0, j0 | 2^l) agree below bit L0 + l with a_base,
+    // whose bits L0 .. L0 + R - 1 are zero: the factor index is qlo 2^s_lo + u
+    // plus jj 2^(L0 + s_lo) for jj = j0 mod 2^l
+    const uint32_t* tq = tw + ((qlo << s_lo) | u);
+    const uint32_t step = 1u << (L0 + s_lo);
+#pragma unroll
+    for (int l = 0; l < R; ++l) {
+      const uint32_t* tl = tq + ((1u << (s_lo + L0 + l)) - 1u);
+      uint32_t tf[1 << (R - 1)];
+#pragma unroll
+      for (int jj = 0; jj < (1 << l); ++jj) tf[jj] = tl[jj * step];
+#pragma unroll
+      for (int j0 = 0; j0 < (1 << R); ++j0) {
+        if (j0 & (1 << l)) continue;
+        const int j1 = j0 | (1 << l);
+        const uint32_t x1 = bb::mul(v[j1], tf[j0 & ((1 << l) - 1)]), x0 = v[j0];
+        v[j0] = bb::add(x0, x1);
+        v[j1] = bb::sub(x0, x1);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < (1 << R); ++j) rp[j << (L0 + 5)] = v[j];
+  }
+}
+
+template <int T, int L0>
+struct BbWideGroups {
+  static __device__ __forceinline__ void run(uint32_t* tile, int s_lo, uint32_t u, uint32_t lane, uint32_t warp,
+                                             const uint32_t* __restrict__ tw) {
+    constexpr int R = bb_wide_group(T, L0);
+    bb_wide_layers<T, L0, R>(tile, s_lo, u, lane, warp, tw);
+    __syncthreads();
+    BbWideGroups<T, L0 + R>::run(tile, s_lo, u, lane, warp, tw);
+  }
+};
+template <int T>
+struct BbWideGroups<T, T> {
+  static __device__ __forceinline__ void run(uint32_t*, int, uint32_t, uint32_t, uint32_t, const uint32_t*) {}
+};
+
+template <int T>
 __global__ void __launch_bounds__(256) bb_dft_wide_kernel(const uint32_t* __restrict__ m, uint32_t* cw, BbPass p,
                                                          const uint32_t* __restrict__ tw, uint32_t* bad) {
   extern __shared__ uint32_t tile[];
-  const int s_lo = p.s_lo, T = p.T;
-  const uint32_t chunk = (blockIdx.x + p.block0) % p.chunks, t = (blockIdx.x + p.block0) / p.chunks;
+  constexpr uint32_t kRows = 1u << T;
+  constexpr uint32_t kPer = kRows >= 8 ? kRows / 8 : 1;  // tile rows per warp (rows warp, warp + 8, ..)
+  constexpr uint32_t kBatch = kPer < 8 ? kPer : 8;       // global loads in flight per thread
+  const int s_lo = p.s_lo;
+  const uint32_t b = blockIdx.x + p.block0;
+  const uint32_t chunk = p.chunks_log >= 0 ? b & (p.chunks - 1u) : b % p.chunks;
+  const uint32_t t = p.chunks_log >= 0 ? b >> p.chunks_log : b / p.chunks;
   const uint32_t u = t & ((1u << s_lo) - 1u);
   const uint64_t x0 = ((uint64_t)(t >> s_lo) << (s_lo + T)) | u;
-  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const uint32_t c = (chunk << 5) + lane;
   const bool col_ok = c < p.w;
-  const uint32_t rows = 1u << T;
   const size_t w = p.w;
+  const size_t step = ((size_t)8 << s_lo) * w;  // words between a thread's consecutive tile rows
   if (p.first) {  // spread rows: tile row a holds data row (x0 + a) >> log2_c when its low log2_c bits are 0
     const uint32_t cmask = (1u << p.log2_c) - 1u;
-    for (uint32_t a0 = warp; a0 < rows; a0 += 8 * nwarps) {
-      uint32_t v[8];
+#pragma unroll 1
+    for (uint32_t k0 = 0; k0 < kPer; k0 += kBatch) {
+      uint32_t v[kBatch];
 #pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        const uint32_t a = a0 + k * nwarps;
+      for (uint32_t k = 0; k < kBatch; ++k) {
+        const uint32_t a = warp + 8u * (k0 + k);
         const uint64_t x = x0 + a;
         v[k] = 0;
-        if (a < rows && col_ok && ((uint32_t)x & cmask) == 0) v[k] = m[(x >> p.log2_c) * w + c];
+        if ((kRows >= 8 || a < kRows) && col_ok && ((uint32_t)x & cmask) == 0) v[k] = m[(x >> p.log2_c) * w + c];
       }
 #pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        const uint32_t a = a0 + k * nwarps;
+      for (uint32_t k = 0; k < kBatch; ++k) {
+        const uint32_t a = warp + 8u * (k0 + k);
         if (v[k] >= bb::P) atomicOr(bad, 1u);
-        if (a < rows) tile[(a << 5) | lane] = bb::to_mont(v[k]);
+        if (kRows >= 8 || a < kRows) tile[(a << 5) | lane] = bb::to_mont(v[k]);
       }
     }
   } else {
-    const size_t stride = (size_t)nwarps << s_lo;  // rows between a thread's consecutive tile rows
     const uint32_t* src = cw + (x0 + ((size_t)warp << s_lo)) * w + c;
-    for (uint32_t a0 = warp; a0 < rows; a0 += 8 * nwarps) {
-      uint32_t v[8];
+#pragma unroll 1
+    for (uint32_t k0 = 0; k0 < kPer; k0 += kBatch) {
+      uint32_t v[kBatch];
 #pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        v[k] = (a0 + k * nwarps < rows && col_ok) ? src[0] : 0u;
-        src += stride * w;
+      for (uint32_t k = 0; k < kBatch; ++k) {
+        const uint32_t a = warp + 8u * (k0 + k);
+        v[k] = ((kRows >= 8 || a < kRows) && col_ok) ? src[0] : 0u;
+        src += step;
       }
 #pragma unroll
-      for (int k = 0; k < 8; ++k)
-        if (a0 + k * nwarps < rows) tile[((a0 + k * nwarps) << 5) | lane] = v[k];
+      for (uint32_t k = 0; k < kBatch; ++k) {
+        const uint32_t a = warp + 8u * (k0 + k);
+        if (kRows >= 8 || a < kRows) tile[(a << 5) | lane] = v[k];
+      }
     }
   }
   __syncthreads();
-  for (int l0 = 0, r; l0 < T; l0 += r) {
-    r = bb_group_layers(T, l0);
-    for (uint32_t q = warp; q < (1u << (T - r)); q += nwarps) {
-      switch (r) {
-        case 4: bb_reg_group<4>(tile, q, l0, s_lo, u, lane, tw); break;
-        case 3: bb_reg_group<3>(tile, q, l0, s_lo, u, lane, tw); break;
-        case 2: bb_reg_group<2>(tile, q, l0, s_lo, u, lane, tw); break;
-        default: bb_reg_group<1>(tile, q, l0, s_lo, u, lane, tw); break;
-      }
-    }
-    __syncthreads();
-  }
+  BbWideGroups<T, 0>::run(tile, s_lo, u, lane, warp, tw);
   if (col_ok) {
-    const size_t stride = ((size_t)nwarps << s_lo) * w;
     uint32_t* dst = cw + (x0 + ((size_t)warp << s_lo)) * w + c;
-    for (uint32_t a = warp; a < rows; a += nwarps) {
-      *dst = tile[(a << 5) | lane];
-      dst += stride;
+#pragma unroll 4
+    for (uint32_t k = 0; k < kPer; ++k) {
+      const uint32_t a = warp + 8u * k;
+      if (kRows >= 8 || a < kRows) *dst = tile[(a << 5) | lane];
+      dst += step;
     }
   }
 }
@@ -1006,6 +1070,7 @@ cudaError_t bb_launch_encode(const uint32_t* m, uint32_t* cw, int d, int log2_c,
     p.lc = lc;
     p.w = (uint32_t)w;
     p.chunks = chunks;
+    p.chunks_log = (chunks & (chunks - 1)) == 0 ? ilog2_ceil(chunks) : -1;
     const size_t words = (size_t)1 << (T + lu + lc);
     int threads = (int)(words / 2);
     if (threads > 256) threads = 256;
@@ -1024,9 +1089,20 @@ cudaError_t bb_launch_encode(const uint32_t* m, uint32_t* cw, int d, int log2_c,
       if (e != cudaSuccess) return e;
       p.block0 = (uint32_t)(blocks / parts * k);
       const unsigned grid = (unsigned)(blocks / parts);
-      if (lc == 5)  // wider than 16 columns: tiles of whole 32-column runs
-        bb_dft_wide_kernel<<<grid, 256, words * sizeof(uint32_t), st>>>(m, cw, p, tw, bad);
-      else if (lu + lc == 5)  // a warp's lanes are one row run: registers take 4 layers per round trip
+      if (lc == 5) {  // wider than 16 columns: tiles of whole 32-column runs (T <= 8)
+        const size_t sh = words * sizeof(uint32_t);
+        switch (T) {
+          case 1: bb_dft_wide_kernel<1><<<grid, 256, sh, st>>>(m, cw, p, tw, bad); break;
+          case 2: bb_dft_wide_kernel<2><<<grid, 256, sh, st>>>(m, cw, p, tw, bad); break;
+          case 3: bb_dft_wide_kernel<3><<<grid, 256, sh, st>>>(m, cw, p, tw, bad); break;
+          case 4: bb_dft_wide_kernel<4><<<grid, 256, sh, st>>>(m, cw, p, tw, bad); break;
+          case 5: bb_dft_wide_kernel<5><<<grid, 256, sh, st>>>(m, cw, p, tw, bad); break;
+          case 6: bb_dft_wide_kernel<6><<<grid, 256, sh, st>>>(m, cw, p, tw, bad); break;
+          case 7: bb_dft_wide_kernel<7><<<grid, 256, sh, st>>>(m, cw, p, tw, bad); break;
+          case 8: bb_dft_wide_kernel<8><<<grid, 256, sh, st>>>(m, cw, p, tw, bad); break;
+          default: return cudaErrorInvalidValue;
+        }
+      } else if (lu + lc == 5)  // a warp's lanes are one row run: registers take 4 layers per round trip
         bb_dft_reg_kernel<<<grid, 256, words * sizeof(uint32_t), st>>>(m, cw, p, tw, bad);
       else
         bb_dft_pass_kernel<<<grid, threads, words * sizeof(uint32_t), st>>>(m, cw, p, tw, bad);
