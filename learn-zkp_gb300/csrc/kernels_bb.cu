@@ -89,8 +89,6 @@ __device__ __forceinline__ void warp_sum5(unsigned long long s[5]) {
     for (int o = 16; o > 0; o >>= 1) s[k] += shfl_xor64(s[k], o);
 }
 
-__device__ __forceinline__ uint32_t mod_p(unsigned long long v) { return (uint32_t)(v % bb::P); }
-
 }  // namespace
 
 // ---- setup -------------------------------------------------------------------
@@ -145,6 +143,65 @@ __global__ void bb_stage0_kernel(const uint32_t* __restrict__ m, uint32_t* __res
       pw = bb::mul(pw, im);
     }
     cw[e] = acc;
+  }
+}
+
+// The same stage with G_0 as a kernel parameter, for k_0 <= 16 and
+// n_0 k_0 <= kBbG0Max: a thread takes one column of one chunk, holds its k_0
+// message values and writes the chunk's n_0 codeword rows.  The parameter holds
+// g_0[i][j] R^2 mod p, so the Montgomery reduction of a product with a
+// canonical message value is the product's Montgomery form; two products sum
+// below 2 p^2 < p 2^32 and share one reduction.
+constexpr int kBbG0Max = 1024;
+struct BbG0 {
+  uint32_t g[kBbG0Max];  // row i at g[i k_0]
+};
+
+__device__ __forceinline__ uint32_t bb_reduce(uint64_t t) {  // t R^-1 mod p for t < p 2^32
+  const uint32_t m = (uint32_t)t * bb::P_INV;
+  const uint32_t d = (uint32_t)(t >> 32) - __umulhi(m, bb::P);
+  return bb::umin(d, d + bb::P);
+}
+
+template <int K0>
+__global__ void __launch_bounds__(256) bb_stage0_fast_kernel(const uint32_t* __restrict__ m, uint32_t* __restrict__ cw,
+                                                            size_t chunk0, size_t chunks, uint32_t w, int n0,
+                                                            const __grid_constant__ BbG0 g0, uint32_t* bad) {
+  const size_t total = chunks * w;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    size_t b, c;
+    if (total >> 32) {
+      b = e / w;
+      c = e - b * w;
+    } else {  // 32-bit division where the index fits
+      const uint32_t q = (uint32_t)e / w;
+      b = q;
+      c = (uint32_t)e - q * w;
+    }
+    b += chunk0;
+    uint32_t v[K0];
+    bool ok = true;
+#pragma unroll
+    for (int j = 0; j < K0; ++j) {
+      v[j] = m[(b * K0 + j) * w + c];
+      ok = ok && v[j] < bb::P;
+    }
+    if (!ok) atomicOr(bad, 1u);
+    uint32_t* out = cw + b * (size_t)n0 * w + c;
+#pragma unroll 2
+    for (int i = 0; i < n0; ++i) {
+      const uint32_t* gi = g0.g + i * K0;
+      uint32_t acc;
+      if (K0 == 1) {
+        acc = bb_reduce((uint64_t)v[0] * gi[0]);
+      } else {
+        acc = bb_reduce((uint64_t)v[0] * gi[0] + (uint64_t)v[1] * gi[1]);
+#pragma unroll
+        for (int j = 2; j < K0; j += 2)
+          acc = bb::add(acc, bb_reduce((uint64_t)v[j] * gi[j] + (uint64_t)v[j + 1] * gi[j + 1]));
+      }
+      out[(size_t)i * w] = acc;
+    }
   }
 }
 
@@ -510,9 +567,11 @@ __global__ void __launch_bounds__(128) bb_leaves_pairs_kernel(const uint32_t* __
 // row's 32 words by the scalars (shared, broadcast reads).  A product
 // mul(s', v) is s' v R^-1: the caller passes s' = s R for a Montgomery source
 // (the codeword) and s' = s R^2 for canonical evaluations, so every product
-// is the Montgomery form of s v without converting the source.  Montgomery
-// form is linear, so the integer sums, reduced mod p, are the Montgomery
-// form of the dot product.
+// is the Montgomery form of s v without converting the source.  The products
+// s' v (source words below p) are summed unreduced in 64 bits, folded to
+// hi (2^32 mod p) + lo after every four columns so that four products never
+// overflow; the sum is congruent to R times the Montgomery form of the dot
+// product, and one Montgomery reduction of it mod p gives that form.
 constexpr int kCombRows = 128, kCombCols = 32;
 __global__ void __launch_bounds__(kCombRows, 6) bb_combine_kernel(const uint32_t* __restrict__ src, size_t rows,
                                                               uint32_t w, const uint32_t* __restrict__ scalars,
@@ -543,27 +602,37 @@ __global__ void __launch_bounds__(kCombRows, 6) bb_combine_kernel(const uint32_t
       }
       __syncthreads();
       const uint32_t* row = stage + threadIdx.x * (kCombCols + 1);
-#pragma unroll 8
-      for (int c = 0; c < kCombCols; ++c) {
-        const uint32_t x = row[c];
+#pragma unroll 2
+      for (int c4 = 0; c4 < kCombCols; c4 += 4) {
 #pragma unroll
-        for (int k = 0; k < 5; ++k) s[k] += bb::mul(sc[5 * c + k], x);
+        for (int c = c4; c < c4 + 4; ++c) {
+          const uint32_t x = row[c];
+#pragma unroll
+          for (int k = 0; k < 5; ++k) s[k] += (unsigned long long)sc[5 * c + k] * x;
+        }
+#pragma unroll
+        for (int k = 0; k < 5; ++k) s[k] = (s[k] >> 32) * (unsigned long long)bb::MONT_ONE + (uint32_t)s[k];
       }
     }
     const size_t r = r0 + threadIdx.x;
     if (r < rows) {
       E5 e;
 #pragma unroll
-      for (int k = 0; k < 5; ++k) e.c[k] = mod_p(s[k]);
+      for (int k = 0; k < 5; ++k) e.c[k] = bb_reduce(s[k] % bb::P);
       st_e5(out, r, e);
     }
   }
 }
 
 // ---- column evaluations (basefold.rs:126-131) ---------------------------------
-// Lane = column (32 per blockIdx.y), warps and blocks over the rows.  The
-// data stay canonical and the eq table is Montgomery, so each product and
-// the sums are canonical.
+// Lane = column (32 per blockIdx.y), warps and blocks over the rows; the data
+// stay canonical and the eq table is Montgomery.
+// Products are summed unreduced: a word v is first brought below 2^32 - p by
+// one conditional subtraction (v mod p for every 32-bit word), each product
+// eq R v (eq in Montgomery form) is then below 4.6e18, and a 64-bit sum is
+// folded to hi (2^32 mod p) + lo (below 1.2e18) after every two rows, so three
+// products never overflow it.  A thread's sum is congruent to R sum eq v;
+// one reduction mod p and one Montgomery reduction give its canonical part.
 __global__ void __launch_bounds__(256) bb_eval_cols_kernel(const uint32_t* __restrict__ eq,
                                                           const uint32_t* __restrict__ data, size_t rows, uint32_t w,
                                                           unsigned long long* acc) {
@@ -571,6 +640,10 @@ __global__ void __launch_bounds__(256) bb_eval_cols_kernel(const uint32_t* __res
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t c = blockIdx.y * 32 + lane;
   unsigned long long s[5] = {0, 0, 0, 0, 0};
+  auto fold = [&]() {
+#pragma unroll
+    for (int k = 0; k < 5; ++k) s[k] = (s[k] >> 32) * (unsigned long long)bb::MONT_ONE + (uint32_t)s[k];
+  };
   if (c < w) {
     const size_t step = (size_t)gridDim.x * 8;
     for (size_t r = (size_t)blockIdx.x * 8 + warp; r < rows; r += 4 * step) {
@@ -581,13 +654,16 @@ __global__ void __launch_bounds__(256) bb_eval_cols_kernel(const uint32_t* __res
       for (int q = 0; q < 4; ++q) {
         if (r + q * step >= rows) break;
         const size_t rr = r + q * step;
+        const uint32_t x = bb::umin(v[q], v[q] - bb::P);
 #pragma unroll
-        for (int k = 0; k < 5; ++k) s[k] += bb::mul(eq[5 * rr + k], v[q]);  // canonical: mul(eq R, v) = eq v
+        for (int k = 0; k < 5; ++k) s[k] += (unsigned long long)eq[5 * rr + k] * x;
+        if (q & 1) fold();
       }
+      fold();
     }
   }
 #pragma unroll
-  for (int k = 0; k < 5; ++k) part[warp][k][lane] = s[k];
+  for (int k = 0; k < 5; ++k) part[warp][k][lane] = bb_reduce(s[k] % bb::P);
   __syncthreads();
   if (warp == 0 && c < w) {
 #pragma unroll
@@ -1013,11 +1089,35 @@ cudaError_t bb_launch_encode(const uint32_t* m, uint32_t* cw, int d, int log2_c,
   if (generic) {
     const int log2_n0 = log2_c + log2_k0;
     const size_t rows = (size_t)1 << L, part = rows / (size_t)slices;
+    const size_t k0 = (size_t)1 << log2_k0, n0 = (size_t)1 << log2_n0;
+    const bool fast = log2_k0 <= 4 && n0 * k0 <= (size_t)kBbG0Max && part % n0 == 0;
+    BbG0 g0;
+    if (fast)  // g_0[i][j] = i^j (generic.rs:51-54), times R^2
+      for (size_t i = 0; i < n0; ++i) {
+        const uint32_t im = bb::to_mont((uint32_t)i);
+        uint32_t pw = bb::MONT_ONE;  // i^j R
+        for (size_t j = 0; j < k0; ++j) {
+          g0.g[i * k0 + j] = bb::to_mont(pw);
+          pw = bb::mul(pw, im);
+        }
+      }
     for (int k = 0; k < slices; ++k) {
       cudaError_t e = wait_slice(k);
       if (e != cudaSuccess) return e;
-      bb_stage0_kernel<<<blocks_for(part * w, 256), 256, 0, st>>>(m, cw, (size_t)k * part, part, (uint32_t)w, log2_k0,
-                                                                  log2_n0, bad);
+      if (fast) {
+        const size_t chunks = part / n0, c0 = (size_t)k * chunks;
+        const unsigned grid = blocks_for(chunks * w, 256);
+        switch (log2_k0) {
+          case 0: bb_stage0_fast_kernel<1><<<grid, 256, 0, st>>>(m, cw, c0, chunks, (uint32_t)w, (int)n0, g0, bad); break;
+          case 1: bb_stage0_fast_kernel<2><<<grid, 256, 0, st>>>(m, cw, c0, chunks, (uint32_t)w, (int)n0, g0, bad); break;
+          case 2: bb_stage0_fast_kernel<4><<<grid, 256, 0, st>>>(m, cw, c0, chunks, (uint32_t)w, (int)n0, g0, bad); break;
+          case 3: bb_stage0_fast_kernel<8><<<grid, 256, 0, st>>>(m, cw, c0, chunks, (uint32_t)w, (int)n0, g0, bad); break;
+          default: bb_stage0_fast_kernel<16><<<grid, 256, 0, st>>>(m, cw, c0, chunks, (uint32_t)w, (int)n0, g0, bad); break;
+        }
+      } else {
+        bb_stage0_kernel<<<blocks_for(part * w, 256), 256, 0, st>>>(m, cw, (size_t)k * part, part, (uint32_t)w,
+                                                                    log2_k0, log2_n0, bad);
+      }
       count_launch();
       e = cudaGetLastError();
       if (e != cudaSuccess) return e;
