@@ -406,7 +406,9 @@ __device__ __forceinline__ void warp_hash_node(const WarpKeccak& wk, const uint4
 // 32 lanes read one 128-byte row run (8 in flight per lane), then each lane
 // absorbs its row.  word_at(row, i) returns word i of a row (rows < `rows`,
 // i < `words`); the 0x01 pad word follows the message and 0x80 ends the
-// last block.  Returns the interleaved digest (the trees' form).
+// last block.  The row is absorbed and permuted on plain lanes (interleaving
+// 17 message lanes per block would cost more than the interleaved rounds
+// save); only the four digest lanes are interleaved, the trees' form.
 constexpr int kRateWords = 34;
 constexpr int kStagePitch = 35;  // odd pitch: lane r reads word r * 35 + i without bank conflicts
 template <class WordAt>
@@ -442,13 +444,17 @@ __device__ __forceinline__ Digest keccak_rows_warp(uint32_t* st, size_t r0, size
     __syncwarp();
 #pragma unroll
     for (int k = 0; k < 17; ++k) {
-      const uint2 l = bi_from_lane(make_uint2(st[lane * kStagePitch + 2 * k], st[lane * kStagePitch + 2 * k + 1]));
-      s[k].x ^= l.x;
-      s[k].y ^= l.y;
+      s[k].x ^= st[lane * kStagePitch + 2 * k];
+      s[k].y ^= st[lane * kStagePitch + 2 * k + 1];
     }
     __syncwarp();
-    keccak_f1600<true>(s);
+    if (blk + 1 < nblk)
+      keccak_f1600<false>(s);
+    else
+      keccak_f1600_digest<false>(s);
   }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) s[i] = bi_from_lane(s[i]);
   return digest_from_state(s);
 }
 

@@ -646,12 +646,12 @@ __global__ void __launch_bounds__(256) bb_eval_cols_kernel(const uint32_t* __res
   };
   if (c < w) {
     const size_t step = (size_t)gridDim.x * 8;
-    for (size_t r = (size_t)blockIdx.x * 8 + warp; r < rows; r += 4 * step) {
-      uint32_t v[4];  // four rows' loads in flight before they are used
+    for (size_t r = (size_t)blockIdx.x * 8 + warp; r < rows; r += 8 * step) {
+      uint32_t v[8];  // eight rows' loads in flight before they are used
 #pragma unroll
-      for (int q = 0; q < 4; ++q) v[q] = r + q * step < rows ? data[(r + q * step) * w + c] : 0u;
+      for (int q = 0; q < 8; ++q) v[q] = r + q * step < rows ? data[(r + q * step) * w + c] : 0u;
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
+      for (int q = 0; q < 8; ++q) {
         if (r + q * step >= rows) break;
         const size_t rr = r + q * step;
         const uint32_t x = bb::umin(v[q], v[q] - bb::P);
@@ -1243,7 +1243,15 @@ cudaError_t bb_launch_eval_cols(const uint32_t* eq, const uint32_t* data, size_t
                                 unsigned long long* acc, cudaStream_t st) {
   size_t bx = (rows + 63) / 64;  // at least 8 rows per warp
   const size_t by = (w + 31) / 32;
-  size_t cap = (152u * 8 + by - 1) / by;
+  // one wave: as many blocks as the SMs hold at once, spread over the column groups
+  static const size_t resident = [] {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bb_eval_cols_kernel, 256, 0);
+    return (size_t)(sms > 0 ? sms : 152) * (size_t)(per_sm > 0 ? per_sm : 4);
+  }();
+  size_t cap = resident / by;
   if (cap < 1) cap = 1;
   if (bx > cap) bx = cap;
   if (bx < 1) bx = 1;
