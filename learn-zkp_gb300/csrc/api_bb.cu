@@ -36,7 +36,7 @@ struct bf_bb_pcs {
   cudaStream_t aux = nullptr;
   cudaEvent_t ev_fork = nullptr;
   cudaEvent_t slice_ev[kH2DSlices] = {};
-  DevBuf tw;    // butterfly factors: layer s at 2^s - 1, 2^s of them (Montgomery)
+  DevBuf tw;    // butterfly factors: layer s at 2^s - 1, 2^s of them (Shoup pairs, uint2)
   DevBuf tinv;  // fold constants: round i at n_0 (2^i - 1), (2 t_i[j])^-1 for j < n_i (Montgomery)
   DevBuf small;  // 4 KB: the canonical flag, sums, roots
   DevBuf ws;       // grow-only scratch of bf_bb_eval
@@ -159,7 +159,7 @@ int commit_device(bf_bb_pcs* p, bf_bb_commitment* cm, const uint32_t* data, cons
   uint32_t* flag = p->small.as<uint32_t>();
   CU(cudaMemsetAsync(flag, 0, 4, p->stream));
   CU(bf::bb_launch_encode(data, cm->cw.as<uint32_t>(), p->d, p->log2_c, p->log2_k0, p->generic, w,
-                          p->tw.as<uint32_t>(), flag, p->stream, slice_ready, slices));
+                          p->tw.as<uint2>(), flag, p->stream, slice_ready, slices));
   uint4* leaves = cm->tree.as<uint4>();
   CU(bf::bb_launch_leaves_rows(cm->cw.as<uint32_t>(), leaves, n, w, p->L, p->stream));
   uint4* root_dev = p->small.as<uint4>() + 2;
@@ -220,15 +220,15 @@ static int bb_setup(int device, int lambda, int log2_c, int log2_k0, int num_var
   CU(cudaStreamCreateWithFlags(&p->aux, cudaStreamNonBlocking));
   CU(cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming));
   for (cudaEvent_t& e : p->slice_ev) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-  CU(p->tw.alloc(4 * p->n_d()));
+  CU(p->tw.alloc(8 * p->n_d()));
   CU(p->tinv.alloc(4 * p->n0() * (((size_t)1 << p->d) - 1) + 4));
   uint32_t* flag = p->small.as<uint32_t>();
   CU(cudaMemsetAsync(flag, 0, 4, p->stream));
   if (!p->generic) {
     // DIT twiddles: layer s (half-size 2^s) uses g_s = two_adic_generator(s + 1)
     for (int s = 0; s < p->L; ++s)
-      CU(bf::bb_launch_pow_table(p->tw.as<uint32_t>() + ((size_t)1 << s) - 1, (size_t)1 << s,
-                                 bb::to_mont(bbh::two_adic_generator(s + 1)), bb::MONT_ONE, p->stream));
+      CU(bf::bb_launch_pow_shoup(p->tw.as<uint2>() + ((size_t)1 << s) - 1, (size_t)1 << s,
+                                 bb::to_mont(bbh::two_adic_generator(s + 1)), p->stream));
     // ReedSolomonCode::new (reed_solomon.rs:20-38): t_i = two_adic_generator(
     // log2_c + i + 1), entry j = (2 t_i^j)^-1 = 2^-1 (t_i^-1)^j
     for (int i = 0; i < p->d; ++i) {
@@ -245,8 +245,8 @@ static int bb_setup(int device, int lambda, int log2_c, int log2_k0, int num_var
     CU(cudaMemcpyAsync(tdev.p, p->ts.data(), 4 * total, cudaMemcpyHostToDevice, p->stream));
     for (int i = 0; i < p->d; ++i) {
       const int s = p->log2_n0() + i;
-      CU(bf::bb_launch_to_mont(tdev.as<uint32_t>() + p->tinv_off(i), p->tw.as<uint32_t>() + ((size_t)1 << s) - 1,
-                               p->n_i(i), flag, p->stream));
+      CU(bf::bb_launch_shoup_from(tdev.as<uint32_t>() + p->tinv_off(i), p->tw.as<uint2>() + ((size_t)1 << s) - 1,
+                                  p->n_i(i), flag, p->stream));
     }
     CU(bf::bb_launch_tinv(tdev.as<uint32_t>(), p->tinv.as<uint32_t>(), total, flag, p->stream));
     CU(cudaStreamSynchronize(p->stream));  // tdev is released below
@@ -497,7 +497,7 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
     CU(bf::bb_launch_from_mont(polyE, poly_canon, 5 * rows, st));
     uint32_t* flag = p->small.as<uint32_t>();
     CU(cudaMemsetAsync(flag, 0, 4, st));
-    CU(bf::bb_launch_encode(poly_canon, piE, p->d, p->log2_c, p->log2_k0, p->generic, 5, p->tw.as<uint32_t>(), flag,
+    CU(bf::bb_launch_encode(poly_canon, piE, p->d, p->log2_c, p->log2_k0, p->generic, 5, p->tw.as<uint2>(), flag,
                             st));
     CU(cudaStreamSynchronize(st));  // the staging of the scalars is reused below
     poly = polyE;

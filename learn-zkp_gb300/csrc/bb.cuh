@@ -45,6 +45,18 @@ __host__ __device__ __forceinline__ uint32_t mul(uint32_t a, uint32_t b) {
   const uint32_t d = (uint32_t)(t >> 32) - mh;
   return umin(d, d + P);
 }
+// Shoup product a w mod p for any 32-bit a and a fixed w < p, given
+// ws = floor(w 2^32 / p): q = hi(a ws) is below a w / p by less than 2, so
+// a w - q p (mod 2^32) lies in [0, 2p).  One high multiply instead of the
+// Montgomery product's wide and high ones; with a in Montgomery form and w
+// canonical, the product stays in Montgomery form.
+__host__ __device__ __forceinline__ uint32_t shoup_quot(uint32_t w) { return (uint32_t)(((uint64_t)w << 32) / P); }
+#ifdef __CUDACC__
+__device__ __forceinline__ uint32_t mul_shoup(uint32_t a, uint2 f) {  // f = (w, shoup_quot(w))
+  const uint32_t r = a * f.x - __umulhi(a, f.y) * P;
+  return umin(r, r - P);
+}
+#endif
 __host__ __device__ __forceinline__ uint32_t to_mont(uint32_t a) { return mul(a, R2); }
 __host__ __device__ __forceinline__ uint32_t from_mont(uint32_t a) { return mul(a, 1u); }
 

@@ -20,21 +20,24 @@ constexpr int kBbMaxRounds = 27;  // num_vars + log2_c <= 27 (the two-adicity of
 
 // g^k * scale for k < n (Montgomery in, Montgomery out).
 cudaError_t bb_launch_pow_table(uint32_t* out, size_t n, uint32_t g_mont, uint32_t scale_mont, cudaStream_t st);
+// Butterfly factors as Shoup pairs (w canonical, floor(w 2^32 / p)): g^k for
+// k < n (g in Montgomery form), or the n canonical words at `in` (*bad set for
+// a word >= p).
+cudaError_t bb_launch_pow_shoup(uint2* out, size_t n, uint32_t g_mont, cudaStream_t st);
+cudaError_t bb_launch_shoup_from(const uint32_t* in, uint2* out, size_t n, uint32_t* bad, cudaStream_t st);
 // encode_batch of a 2^(d + log2_k0) x w matrix into its 2^(d + log2_k0 +
 // log2_c) x w codeword (Montgomery).  `tw` holds the butterfly factors of
-// layer s at tw[2^s - 1 + k]: g_s^k for the Reed–Solomon code (log2_k0 = 0),
-// ts[s - log2_n0][k] for the generic code (`generic`), whose stage 0 is the
-// dense G_0.  A data word >= p sets *bad.
+// layer s at tw[2^s - 1 + k] as Shoup pairs: g_s^k for the Reed–Solomon code
+// (log2_k0 = 0), ts[s - log2_n0][k] for the generic code (`generic`), whose
+// stage 0 is the dense G_0.  A data word >= p sets *bad.
 // With `slices` > 1, input slice k (data rows [k R / slices, (k+1) R / slices))
 // is ready when slice_ready[k] completes: the first stage waits for each slice
 // just before the part of its grid that reads it.
 cudaError_t bb_launch_encode(const uint32_t* m, uint32_t* cw, int d, int log2_c, int log2_k0, int generic, size_t w,
-                             const uint32_t* tw, uint32_t* bad, cudaStream_t st,
+                             const uint2* tw, uint32_t* bad, cudaStream_t st,
                              const cudaEvent_t* slice_ready = nullptr, int slices = 0);
 // out[k] = in[k] in canonical form (Montgomery in).
 cudaError_t bb_launch_from_mont(const uint32_t* in, uint32_t* out, size_t n, cudaStream_t st);
-// out[k] = in[k] in Montgomery form; *bad set for a word >= p.
-cudaError_t bb_launch_to_mont(const uint32_t* in, uint32_t* out, size_t n, uint32_t* bad, cudaStream_t st);
 // tinv[k] = (2 ts[k])^-1 (Montgomery); *bad set for a t that is 0 or >= p.
 cudaError_t bb_launch_tinv(const uint32_t* ts, uint32_t* tinv, size_t n, uint32_t* bad, cudaStream_t st);
 // Leaf of codeword row q (keccak256 of its w canonical words) at bitrev_bits(q).

@@ -97,6 +97,23 @@ __global__ void bb_pow_table_kernel(uint32_t* out, size_t n, uint32_t g, uint32_
     out[k] = bb::mul(scale, mont_pow(g, k));
 }
 
+// Butterfly factors as Shoup pairs (w canonical, floor(w 2^32 / p)): the
+// powers g^k, or the caller's canonical values (*bad set for one >= p).
+__global__ void bb_pow_shoup_kernel(uint2* out, size_t n, uint32_t g) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t w = bb::from_mont(mont_pow(g, k));
+    out[k] = make_uint2(w, bb::shoup_quot(w));
+  }
+}
+__global__ void bb_shoup_from_kernel(const uint32_t* in, uint2* out, size_t n, uint32_t* bad) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t v = in[k];
+    if (v >= bb::P) atomicOr(bad, 1u);
+    const uint32_t w = v % bb::P;
+    out[k] = make_uint2(w, bb::shoup_quot(w));
+  }
+}
+
 // Single-row codeword (num_vars = log2_c = 0): the data in Montgomery form.
 __global__ void bb_copy_mont_kernel(const uint32_t* in, uint32_t* out, size_t n, uint32_t* bad) {
   for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
@@ -292,7 +309,7 @@ __device__ __forceinline__ void bb_tile_store(const uint32_t* tile, uint32_t* cw
 }
 
 __global__ void __launch_bounds__(256) bb_dft_pass_kernel(const uint32_t* __restrict__ m, uint32_t* cw, BbPass p,
-                                                         const uint32_t* __restrict__ tw, uint32_t* bad) {
+                                                         const uint2* __restrict__ tw, uint32_t* bad) {
   extern __shared__ uint32_t tile[];
   const int s_lo = p.s_lo, T = p.T, lu = p.lu, lc = p.lc, ic = lu + lc;
   const BbTile tl(p);
@@ -302,7 +319,7 @@ __global__ void __launch_bounds__(256) bb_dft_pass_kernel(const uint32_t* __rest
   __syncthreads();
   for (int l = 0; l < T; ++l) {
     const int s = s_lo + l;
-    const uint32_t* __restrict__ tws = tw + ((size_t)1 << s) - 1;
+    const uint2* __restrict__ tws = tw + ((size_t)1 << s) - 1;
     const uint32_t lmask = (1u << l) - 1u;
     for (uint32_t e = threadIdx.x; e < (tsize >> 1); e += blockDim.x) {
       const uint32_t cu = e & ((1u << ic) - 1u), bi = e >> ic;
@@ -310,7 +327,7 @@ __global__ void __launch_bounds__(256) bb_dft_pass_kernel(const uint32_t* __rest
       const uint32_t u = (u_blk << lu) | (cu >> lc);
       const uint32_t k = ((a0 & lmask) << s_lo) | u;
       const uint32_t i0 = (a0 << ic) | cu, i1 = i0 | (1u << (l + ic));
-      const uint32_t v = bb::mul(tile[i1], tws[k]), x0 = tile[i0];
+      const uint32_t v = bb::mul_shoup(tile[i1], tws[k]), x0 = tile[i0];
       tile[i0] = bb::add(x0, v);
       tile[i1] = bb::sub(x0, v);
     }
@@ -326,7 +343,7 @@ __global__ void __launch_bounds__(256) bb_dft_pass_kernel(const uint32_t* __rest
 // Every shared-memory access of a warp is one 128-byte row run.
 template <int R>
 __device__ __forceinline__ void bb_reg_group(uint32_t* tile, uint32_t q, int l0, int s_lo, uint32_t u, uint32_t lane,
-                                             const uint32_t* __restrict__ tw) {
+                                             const uint2* __restrict__ tw) {
   const uint32_t a_base = ((q >> l0) << (l0 + R)) | (q & ((1u << l0) - 1u));
   uint32_t v[1 << R];
 #pragma unroll
@@ -340,14 +357,14 @@ __device__ __forceinline__ void bb_reg_group(uint32_t* tile, uint32_t q, int l0,
     const int s = s_lo + l0 + l;
     const uint32_t lmask = (1u << (l0 + l)) - 1u;
     const uint32_t base = (1u << s) - 1u + (((a_base & lmask) << s_lo) | u);  // 2^L - 1 words in all, L <= 27
-    uint32_t tf[1 << (R - 1)];
+    uint2 tf[1 << (R - 1)];
 #pragma unroll
     for (int jj = 0; jj < (1 << l); ++jj) tf[jj] = tw[base + ((uint32_t)jj << (l0 + s_lo))];
 #pragma unroll
     for (int j0 = 0; j0 < (1 << R); ++j0) {
       if (j0 & (1 << l)) continue;
       const int j1 = j0 | (1 << l);
-      const uint32_t x1 = bb::mul(v[j1], tf[j0 & ((1 << l) - 1)]), x0 = v[j0];
+      const uint32_t x1 = bb::mul_shoup(v[j1], tf[j0 & ((1 << l) - 1)]), x0 = v[j0];
       v[j0] = bb::add(x0, x1);
       v[j1] = bb::sub(x0, x1);
     }
@@ -366,7 +383,7 @@ __device__ __forceinline__ int bb_group_layers(int T, int l0) {
 }
 
 __global__ void __launch_bounds__(256) bb_dft_reg_kernel(const uint32_t* __restrict__ m, uint32_t* cw, BbPass p,
-                                                        const uint32_t* __restrict__ tw, uint32_t* bad) {
+                                                        const uint2* __restrict__ tw, uint32_t* bad) {
   extern __shared__ uint32_t tile[];
   const int s_lo = p.s_lo, T = p.T, lu = p.lu, lc = p.lc;  // lu + lc = 5
   const BbTile tl(p);
@@ -405,7 +422,7 @@ __host__ __device__ constexpr int bb_wide_group(int T, int l0) {  // layers of t
 // 2^(T - R) groups takes rows a_base | j 2^L0 (j < 2^R) into registers.
 template <int T, int L0, int R>
 __device__ __forceinline__ void bb_wide_layers(uint32_t* tile, int s_lo, uint32_t u, uint32_t lane, uint32_t warp,
-                                               const uint32_t* __restrict__ tw) {
+                                               const uint2* __restrict__ tw) {
   constexpr uint32_t kWork = 1u << (T - R);
   constexpr uint32_t kIters = kWork >= 8 ? kWork / 8 : 1;
 #pragma unroll
@@ -420,19 +437,19 @@ __device__ __forceinline__ void bb_wide_layers(uint32_t* tile, int s_lo, uint32_
     // the rows of the pair (j0, j0 | 2^l) agree below bit L0 + l with a_base,
     // whose bits L0 .. L0 + R - 1 are zero: the factor index is qlo 2^s_lo + u
     // plus jj 2^(L0 + s_lo) for jj = j0 mod 2^l
-    const uint32_t* tq = tw + ((qlo << s_lo) | u);
+    const uint2* tq = tw + ((qlo << s_lo) | u);
     const uint32_t step = 1u << (L0 + s_lo);
 #pragma unroll
     for (int l = 0; l < R; ++l) {
-      const uint32_t* tl = tq + ((1u << (s_lo + L0 + l)) - 1u);
-      uint32_t tf[1 << (R - 1)];
+      const uint2* tl = tq + ((1u << (s_lo + L0 + l)) - 1u);
+      uint2 tf[1 << (R - 1)];
 #pragma unroll
       for (int jj = 0; jj < (1 << l); ++jj) tf[jj] = tl[jj * step];
 #pragma unroll
       for (int j0 = 0; j0 < (1 << R); ++j0) {
         if (j0 & (1 << l)) continue;
         const int j1 = j0 | (1 << l);
-        const uint32_t x1 = bb::mul(v[j1], tf[j0 & ((1 << l) - 1)]), x0 = v[j0];
+        const uint32_t x1 = bb::mul_shoup(v[j1], tf[j0 & ((1 << l) - 1)]), x0 = v[j0];
         v[j0] = bb::add(x0, x1);
         v[j1] = bb::sub(x0, x1);
       }
@@ -445,7 +462,7 @@ __device__ __forceinline__ void bb_wide_layers(uint32_t* tile, int s_lo, uint32_
 template <int T, int L0>
 struct BbWideGroups {
   static __device__ __forceinline__ void run(uint32_t* tile, int s_lo, uint32_t u, uint32_t lane, uint32_t warp,
-                                             const uint32_t* __restrict__ tw) {
+                                             const uint2* __restrict__ tw) {
     constexpr int R = bb_wide_group(T, L0);
     bb_wide_layers<T, L0, R>(tile, s_lo, u, lane, warp, tw);
     __syncthreads();
@@ -454,12 +471,12 @@ struct BbWideGroups {
 };
 template <int T>
 struct BbWideGroups<T, T> {
-  static __device__ __forceinline__ void run(uint32_t*, int, uint32_t, uint32_t, uint32_t, const uint32_t*) {}
+  static __device__ __forceinline__ void run(uint32_t*, int, uint32_t, uint32_t, uint32_t, const uint2*) {}
 };
 
 template <int T>
 __global__ void __launch_bounds__(256) bb_dft_wide_kernel(const uint32_t* __restrict__ m, uint32_t* cw, BbPass p,
-                                                         const uint32_t* __restrict__ tw, uint32_t* bad) {
+                                                         const uint2* __restrict__ tw, uint32_t* bad) {
   extern __shared__ uint32_t tile[];
   constexpr uint32_t kRows = 1u << T;
   constexpr uint32_t kPer = kRows >= 8 ? kRows / 8 : 1;  // tile rows per warp (rows warp, warp + 8, ..)
@@ -1043,6 +1060,18 @@ static unsigned blocks_for(size_t n, int threads) {
   return b ? (unsigned)b : 1u;
 }
 
+cudaError_t bb_launch_pow_shoup(uint2* out, size_t n, uint32_t g_mont, cudaStream_t st) {
+  bb_pow_shoup_kernel<<<blocks_for(n, 256), 256, 0, st>>>(out, n, g_mont);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t bb_launch_shoup_from(const uint32_t* in, uint2* out, size_t n, uint32_t* bad, cudaStream_t st) {
+  bb_shoup_from_kernel<<<blocks_for(n, 256), 256, 0, st>>>(in, out, n, bad);
+  count_launch();
+  return cudaGetLastError();
+}
+
 cudaError_t bb_launch_pow_table(uint32_t* out, size_t n, uint32_t g_mont, uint32_t scale_mont, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   bb_pow_table_kernel<<<blocks_for(n, 256), 256, 0, st>>>(out, n, g_mont, scale_mont);
@@ -1070,15 +1099,8 @@ cudaError_t bb_launch_tinv(const uint32_t* ts, uint32_t* tinv, size_t n, uint32_
   return cudaGetLastError();
 }
 
-cudaError_t bb_launch_to_mont(const uint32_t* in, uint32_t* out, size_t n, uint32_t* bad, cudaStream_t st) {
-  if (n == 0) return cudaSuccess;
-  bb_copy_mont_kernel<<<blocks_for(n, 256), 256, 0, st>>>(in, out, n, bad);
-  count_launch();
-  return cudaGetLastError();
-}
-
 cudaError_t bb_launch_encode(const uint32_t* m, uint32_t* cw, int d, int log2_c, int log2_k0, int generic, size_t w,
-                             const uint32_t* tw, uint32_t* bad, cudaStream_t st, const cudaEvent_t* slice_ready,
+                             const uint2* tw, uint32_t* bad, cudaStream_t st, const cudaEvent_t* slice_ready,
                              int slices) {
   const int L = d + log2_c + log2_k0;
   int lo = 0;  // the first DIT layer
