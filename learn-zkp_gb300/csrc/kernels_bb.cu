@@ -163,15 +163,18 @@ __global__ void bb_stage0_kernel(const uint32_t* __restrict__ m, uint32_t* __res
   }
 }
 
-// The same stage with G_0 as a kernel parameter, for k_0 <= 16 and
-// n_0 k_0 <= kBbG0Max: a thread takes one column of one chunk, holds its k_0
-// message values and writes the chunk's n_0 codeword rows.  The parameter holds
-// g_0[i][j] R^2 mod p, so the Montgomery reduction of a product with a
-// canonical message value is the product's Montgomery form; two products sum
-// below 2 p^2 < p 2^32 and share one reduction.
-constexpr int kBbG0Max = 1024;
+// The same stage for k_0 <= 16: a thread takes one column of one chunk, holds
+// its k_0 message values and writes the chunk's n_0 codeword rows.  Row i is
+// V(i) for V(X) = sum_j m_j X^j, of degree below k_0 (g_0[i][j] = i^j), so only
+// rows i < k_0 are dot products; the rest follow from the backward differences
+// of V at k_0 - 1 (the (k_0 - 1)-th is constant), k_0 - 1 additions per row.
+// The kernel parameter holds g_0[i][j] R^2 mod p for i < k_0, so the Montgomery
+// reduction of a product with a canonical message value is the product's
+// Montgomery form; two products sum below 2 p^2 < p 2^32 and share one
+// reduction.
+constexpr int kBbG0Max = 256;
 struct BbG0 {
-  uint32_t g[kBbG0Max];  // row i at g[i k_0]
+  uint32_t g[kBbG0Max];  // row i < k_0 at g[i k_0]
 };
 
 __device__ __forceinline__ uint32_t bb_reduce(uint64_t t) {  // t R^-1 mod p for t < p 2^32
@@ -205,8 +208,9 @@ __global__ void __launch_bounds__(256) bb_stage0_fast_kernel(const uint32_t* __r
     }
     if (!ok) atomicOr(bad, 1u);
     uint32_t* out = cw + b * (size_t)n0 * w + c;
-#pragma unroll 2
-    for (int i = 0; i < n0; ++i) {
+    uint32_t y[K0];
+#pragma unroll
+    for (int i = 0; i < K0; ++i) {  // n_0 >= k_0
       const uint32_t* gi = g0.g + i * K0;
       uint32_t acc;
       if (K0 == 1) {
@@ -217,7 +221,24 @@ __global__ void __launch_bounds__(256) bb_stage0_fast_kernel(const uint32_t* __r
         for (int j = 2; j < K0; j += 2)
           acc = bb::add(acc, bb_reduce((uint64_t)v[j] * gi[j] + (uint64_t)v[j + 1] * gi[j + 1]));
       }
+      y[i] = acc;
       out[(size_t)i * w] = acc;
+    }
+    if (n0 > K0) {
+      uint32_t D[K0];  // D[k] = k-th backward difference of V at the last row written
+      D[0] = y[K0 - 1];
+#pragma unroll
+      for (int lev = 1; lev < K0; ++lev) {
+#pragma unroll
+        for (int i = K0 - 1; i >= lev; --i) y[i] = bb::sub(y[i], y[i - 1]);
+        D[lev] = y[K0 - 1];
+      }
+#pragma unroll 1
+      for (int i = K0; i < n0; ++i) {
+#pragma unroll
+        for (int k = K0 - 2; k >= 0; --k) D[k] = bb::add(D[k], D[k + 1]);
+        out[(size_t)i * w] = D[0];
+      }
     }
   }
 }
@@ -1112,10 +1133,10 @@ cudaError_t bb_launch_encode(const uint32_t* m, uint32_t* cw, int d, int log2_c,
     const int log2_n0 = log2_c + log2_k0;
     const size_t rows = (size_t)1 << L, part = rows / (size_t)slices;
     const size_t k0 = (size_t)1 << log2_k0, n0 = (size_t)1 << log2_n0;
-    const bool fast = log2_k0 <= 4 && n0 * k0 <= (size_t)kBbG0Max && part % n0 == 0;
+    const bool fast = log2_k0 <= 4 && part % n0 == 0;
     BbG0 g0;
-    if (fast)  // g_0[i][j] = i^j (generic.rs:51-54), times R^2
-      for (size_t i = 0; i < n0; ++i) {
+    if (fast)  // g_0[i][j] = i^j (generic.rs:51-54), times R^2, for the rows i < k_0
+      for (size_t i = 0; i < k0; ++i) {
         const uint32_t im = bb::to_mont((uint32_t)i);
         uint32_t pw = bb::MONT_ONE;  // i^j R
         for (size_t j = 0; j < k0; ++j) {

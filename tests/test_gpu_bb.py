@@ -129,12 +129,12 @@ def test_generic_code_matches_oracle(built_lib, n, log2_c, log2_k0, w):
     _check_generic(n, log2_c, log2_k0, w, 3000 + 17 * n + 5 * log2_c + log2_k0 + w)
 
 
-# Stage-0 shapes past the reference test's range: k_0 = 16 with n_0 k_0 = 512
-# and 1024 (G_0 passed to the kernel), n_0 k_0 = 2048 and k_0 = 32 (G_0
-# powers computed in the kernel), and a 2^17-row host commit whose stage 0
-# runs per input slice.
+# Stage-0 shapes past the reference test's range: k_0 = 16 with n_0 = 32, 64
+# and 128 (rows past k_0 from backward differences), k_0 = 32 with n_0 = 32 and
+# 128 (the general kernel), and a 2^17-row host commit whose stage 0 runs per
+# input slice.
 @pytest.mark.parametrize("n,log2_c,log2_k0,w", [(6, 1, 4, 3), (7, 2, 4, 2), (8, 3, 4, 1), (6, 0, 5, 2),
-                                                (17, 1, 3, 4)])
+                                                (9, 2, 5, 1), (17, 1, 3, 4)])
 def test_generic_code_stage0_shapes(built_lib, n, log2_c, log2_k0, w):
     _check_generic(n, log2_c, log2_k0, w, 3500 + 17 * n + 5 * log2_c + log2_k0 + w)
 
