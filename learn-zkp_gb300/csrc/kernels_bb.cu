@@ -431,8 +431,8 @@ __global__ void __launch_bounds__(256) bb_dft_reg_kernel(const uint32_t* __restr
 // 2^T rows x 32 columns, row a of the tile at matrix row x0 + a 2^s_lo, run by
 // eight warps.  The tile height is a template parameter, so the layer groups,
 // each warp's share of the rows and every shared-memory offset are compile-time
-// constants: the pass's instructions are the Montgomery butterflies, the
-// factor loads and one pointer step per global access.
+// constants: the pass's instructions are the butterflies (Shoup products by
+// the factor pairs), the factor loads and one pointer step per global access.
 __host__ __device__ constexpr int bb_wide_group(int T, int l0) {  // layers of the register group starting at l0 (bb_group_layers)
   const int r = T - l0 < 4 ? T - l0 : 4;
   const int cap = T - 3 > 1 ? T - 3 : 1;
