@@ -43,6 +43,10 @@ struct bf_bb_pcs {
   DevBuf open_ws;  // grow-only workspace of bf_bb_open
   DevBuf data_ws;  // grow-only copy of host rows for bf_bb_eval_data
   PinnedBuf pin;
+  // Commitment buffers (evaluation copy, codeword, tree) come from this
+  // stream-ordered pool, which keeps freed memory for the next commit: no
+  // cudaMalloc per commit, and no cudaFree (which waits for the whole device).
+  cudaMemPool_t pool = nullptr;
 
   size_t c() const { return (size_t)1 << log2_c; }
   size_t k0() const { return (size_t)1 << log2_k0; }
@@ -87,6 +91,8 @@ struct bf_bb_pcs {
       ws.release();
       open_ws.release();
       data_ws.release();
+      if (stream) cudaStreamSynchronize(stream);
+      if (pool) cudaMemPoolDestroy(pool);
       if (own_stream && stream) cudaStreamDestroy(stream);
       if (aux) cudaStreamDestroy(aux);
       if (ev_fork) cudaEventDestroy(ev_fork);
@@ -154,8 +160,8 @@ int eq_table_device(bf_bb_pcs* p, const std::vector<E>& x, uint32_t* ev) {
 int commit_device(bf_bb_pcs* p, bf_bb_commitment* cm, const uint32_t* data, const cudaEvent_t* slice_ready = nullptr,
                   int slices = 0) {
   const size_t w = cm->w, n = p->n_d();
-  CU(cm->cw.alloc(4 * n * w));
-  CU(cm->tree.alloc(64 * n));
+  CU(cm->cw.alloc_async(4 * n * w, p->pool, p->stream));
+  CU(cm->tree.alloc_async(64 * n, p->pool, p->stream));
   uint32_t* flag = p->small.as<uint32_t>();
   CU(cudaMemsetAsync(flag, 0, 4, p->stream));
   CU(bf::bb_launch_encode(data, cm->cw.as<uint32_t>(), p->d, p->log2_c, p->log2_k0, p->generic, w,
@@ -217,6 +223,16 @@ static int bb_setup(int device, int lambda, int log2_c, int log2_k0, int num_var
   }
   CU(p->pin.ensure(4096));
   CU(p->small.alloc(4096));
+  {
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    CU(cudaMemPoolCreate(&p->pool, &props));
+    uint64_t keep = ~(uint64_t)0;
+    CU(cudaMemPoolSetAttribute(p->pool, cudaMemPoolAttrReleaseThreshold, &keep));
+  }
   CU(cudaStreamCreateWithFlags(&p->aux, cudaStreamNonBlocking));
   CU(cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming));
   for (cudaEvent_t& e : p->slice_ev) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -294,7 +310,7 @@ int bf_bb_commit(bf_bb_pcs* p, const uint32_t* evals, size_t width, bf_bb_commit
   cm->pcs = p;
   cm->w = width;
   const size_t bytes = 4 * width << p->num_vars;
-  CU(cm->data.alloc(bytes));
+  CU(cm->data.alloc_async(bytes, p->pool, p->stream));  // before the fork: `aux` writes it after this point
   if (p->num_vars >= 16) {
     // copy in slices on the second stream; the encode's first stage takes
     // each slice as it lands (pinned `evals` overlap the copy with the encode)
@@ -346,8 +362,7 @@ void bf_bb_commitment_free(bf_bb_commitment* cm) {
   bf_bb_pcs* p = cm->pcs;
   {
     DeviceGuard g(p->device);
-    cudaStreamSynchronize(p->stream);
-    delete cm;
+    delete cm;  // owned buffers return to the pcs's pool in stream order
   }
   bb_release(p);
 }

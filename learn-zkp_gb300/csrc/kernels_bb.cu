@@ -1124,49 +1124,11 @@ cudaError_t bb_launch_encode(const uint32_t* m, uint32_t* cw, int d, int log2_c,
                              const uint2* tw, uint32_t* bad, cudaStream_t st, const cudaEvent_t* slice_ready,
                              int slices) {
   const int L = d + log2_c + log2_k0;
-  int lo = 0;  // the first DIT layer
   if (slices < 1 || !slice_ready) slices = 1;
-  // input slice k (data rows [k 2^nv / slices, (k+1) 2^nv / slices)) feeds the
-  // first stage's k-th part: codeword rows [k 2^L / slices, (k+1) 2^L / slices)
+  // input slice k (data rows [k 2^nv / slices, (k+1) 2^nv / slices)) feeds
+  // codeword rows [k 2^L / slices, (k+1) 2^L / slices)
   auto wait_slice = [&](int k) { return slices > 1 ? cudaStreamWaitEvent(st, slice_ready[k], 0) : cudaSuccess; };
-  if (generic) {
-    const int log2_n0 = log2_c + log2_k0;
-    const size_t rows = (size_t)1 << L, part = rows / (size_t)slices;
-    const size_t k0 = (size_t)1 << log2_k0, n0 = (size_t)1 << log2_n0;
-    const bool fast = log2_k0 <= 4 && part % n0 == 0;
-    BbG0 g0;
-    if (fast)  // g_0[i][j] = i^j (generic.rs:51-54), times R^2, for the rows i < k_0
-      for (size_t i = 0; i < k0; ++i) {
-        const uint32_t im = bb::to_mont((uint32_t)i);
-        uint32_t pw = bb::MONT_ONE;  // i^j R
-        for (size_t j = 0; j < k0; ++j) {
-          g0.g[i * k0 + j] = bb::to_mont(pw);
-          pw = bb::mul(pw, im);
-        }
-      }
-    for (int k = 0; k < slices; ++k) {
-      cudaError_t e = wait_slice(k);
-      if (e != cudaSuccess) return e;
-      if (fast) {
-        const size_t chunks = part / n0, c0 = (size_t)k * chunks;
-        const unsigned grid = blocks_for(chunks * w, 256);
-        switch (log2_k0) {
-          case 0: bb_stage0_fast_kernel<1><<<grid, 256, 0, st>>>(m, cw, c0, chunks, (uint32_t)w, (int)n0, g0, bad); break;
-          case 1: bb_stage0_fast_kernel<2><<<grid, 256, 0, st>>>(m, cw, c0, chunks, (uint32_t)w, (int)n0, g0, bad); break;
-          case 2: bb_stage0_fast_kernel<4><<<grid, 256, 0, st>>>(m, cw, c0, chunks, (uint32_t)w, (int)n0, g0, bad); break;
-          case 3: bb_stage0_fast_kernel<8><<<grid, 256, 0, st>>>(m, cw, c0, chunks, (uint32_t)w, (int)n0, g0, bad); break;
-          default: bb_stage0_fast_kernel<16><<<grid, 256, 0, st>>>(m, cw, c0, chunks, (uint32_t)w, (int)n0, g0, bad); break;
-        }
-      } else {
-        bb_stage0_kernel<<<blocks_for(part * w, 256), 256, 0, st>>>(m, cw, (size_t)k * part, part, (uint32_t)w,
-                                                                    log2_k0, log2_n0, bad);
-      }
-      count_launch();
-      e = cudaGetLastError();
-      if (e != cudaSuccess) return e;
-    }
-    lo = log2_n0;  // the butterflies of ts[i-1] are layers log2_n0 + i - 1
-  } else if (L == 0) {
+  if (!generic && L == 0) {
     for (int k = 0; k < slices; ++k) {
       cudaError_t e = wait_slice(k);
       if (e != cudaSuccess) return e;
@@ -1175,9 +1137,19 @@ cudaError_t bb_launch_encode(const uint32_t* m, uint32_t* cw, int d, int log2_c,
     count_launch();
     return cudaGetLastError();
   }
+  const int log2_n0 = log2_c + log2_k0;
+  const int first = generic ? log2_n0 : 0;  // the first DIT layer (the butterflies of ts[i-1] are layers log2_n0 + i - 1)
+
+  // The pass plan.
+  struct PassPlan {
+    BbPass p;
+    size_t blocks, words;
+    int threads;
+  };
+  PassPlan plan[kBbMaxRounds + 1];
+  int npass = 0;
   const int lc = ilog2_ceil(w < 32 ? w : 32);
   const unsigned chunks = (unsigned)((w + ((size_t)1 << lc) - 1) >> lc);
-  const int first = lo;
   // U C <= 32 consecutive words per row run; tiles of 2^(T + lu + lc) <= 8192 words
   auto lu_at = [&](int s_lo) {
     int lu = 0;
@@ -1189,8 +1161,8 @@ cudaError_t bb_launch_encode(const uint32_t* m, uint32_t* cw, int d, int log2_c,
   // the greedy split's pass count, then the layers spread evenly over that
   // many passes where the tiles allow (no short last pass of idle warps)
   int passes = 0;
-  for (int x = lo; x < L; x += tmax_at(x)) ++passes;
-  while (lo < L) {
+  for (int x = first; x < L; x += tmax_at(x)) ++passes;
+  for (int lo = first; lo < L;) {
     const int lu = lu_at(lo);
     int T = (L - lo + passes - 1) / passes;
     if (T > tmax_at(lo)) T = tmax_at(lo);
@@ -1204,7 +1176,8 @@ cudaError_t bb_launch_encode(const uint32_t* m, uint32_t* cw, int d, int log2_c,
       if (lo + T + reach < L) T = tmax_at(lo);
     }
     if (T > L - lo) T = L - lo;
-    BbPass p;
+    PassPlan& pp = plan[npass++];
+    BbPass& p = pp.p;
     p.s_lo = lo;
     p.T = T;
     p.first = !generic && lo == first;
@@ -1214,46 +1187,100 @@ cudaError_t bb_launch_encode(const uint32_t* m, uint32_t* cw, int d, int log2_c,
     p.w = (uint32_t)w;
     p.chunks = chunks;
     p.chunks_log = (chunks & (chunks - 1)) == 0 ? ilog2_ceil(chunks) : -1;
-    const size_t words = (size_t)1 << (T + lu + lc);
-    int threads = (int)(words / 2);
-    if (threads > 256) threads = 256;
-    if (threads < 32) threads = 32;
-    const size_t blocks = ((size_t)1 << (L - T - lu)) * chunks;  // chunk fastest (BbTile)
-    if (blocks > 0x7fffffffu) return cudaErrorInvalidValue;
-    // the first pass of a sliced input: its tiles, in order, read the slices in order
-    const int parts = (p.first && slices > 1 && (((size_t)1 << (L - T)) % slices) == 0) ? slices : 1;
-    if (p.first && parts == 1 && slices > 1)  // a first pass that cannot be split waits for every slice
-      for (int k = 0; k < slices; ++k) {
-        cudaError_t e = cudaStreamWaitEvent(st, slice_ready[k], 0);
-        if (e != cudaSuccess) return e;
+    p.block0 = 0;
+    pp.words = (size_t)1 << (T + lu + lc);
+    pp.threads = (int)(pp.words / 2);
+    if (pp.threads > 256) pp.threads = 256;
+    if (pp.threads < 32) pp.threads = 32;
+    pp.blocks = ((size_t)1 << (L - T - lu)) * chunks;  // chunk fastest (BbTile)
+    if (pp.blocks > 0x7fffffffu) return cudaErrorInvalidValue;
+    lo += T;
+  }
+  // Blocks [block0, block0 + grid) of a pass.
+  auto launch_pass = [&](const PassPlan& pp, size_t block0, size_t grid_blocks) -> cudaError_t {
+    BbPass p = pp.p;
+    p.block0 = (uint32_t)block0;
+    const unsigned grid = (unsigned)grid_blocks;
+    const size_t sh = pp.words * sizeof(uint32_t);
+    if (p.lc == 5) {  // wider than 16 columns: tiles of whole 32-column runs (T <= 8)
+      switch (p.T) {
+        case 1: bb_dft_wide_kernel<1><<<grid, 256, sh, st>>>(m, cw, p, tw, bad); break;
+        case 2: bb_dft_wide_kernel<2><<<grid, 256, sh, st>>>(m, cw, p, tw, bad); break;
+        case 3: bb_dft_wide_kernel<3><<<grid, 256, sh, st>>>(m, cw, p, tw, bad); break;
+        case 4: bb_dft_wide_kernel<4><<<grid, 256, sh, st>>>(m, cw, p, tw, bad); break;
+        case 5: bb_dft_wide_kernel<5><<<grid, 256, sh, st>>>(m, cw, p, tw, bad); break;
+        case 6: bb_dft_wide_kernel<6><<<grid, 256, sh, st>>>(m, cw, p, tw, bad); break;
+        case 7: bb_dft_wide_kernel<7><<<grid, 256, sh, st>>>(m, cw, p, tw, bad); break;
+        case 8: bb_dft_wide_kernel<8><<<grid, 256, sh, st>>>(m, cw, p, tw, bad); break;
+        default: return cudaErrorInvalidValue;
       }
-    for (int k = 0; k < parts; ++k) {
-      cudaError_t e = parts > 1 ? wait_slice(k) : cudaSuccess;
-      if (e != cudaSuccess) return e;
-      p.block0 = (uint32_t)(blocks / parts * k);
-      const unsigned grid = (unsigned)(blocks / parts);
-      if (lc == 5) {  // wider than 16 columns: tiles of whole 32-column runs (T <= 8)
-        const size_t sh = words * sizeof(uint32_t);
-        switch (T) {
-          case 1: bb_dft_wide_kernel<1><<<grid, 256, sh, st>>>(m, cw, p, tw, bad); break;
-          case 2: bb_dft_wide_kernel<2><<<grid, 256, sh, st>>>(m, cw, p, tw, bad); break;
-          case 3: bb_dft_wide_kernel<3><<<grid, 256, sh, st>>>(m, cw, p, tw, bad); break;
-          case 4: bb_dft_wide_kernel<4><<<grid, 256, sh, st>>>(m, cw, p, tw, bad); break;
-          case 5: bb_dft_wide_kernel<5><<<grid, 256, sh, st>>>(m, cw, p, tw, bad); break;
-          case 6: bb_dft_wide_kernel<6><<<grid, 256, sh, st>>>(m, cw, p, tw, bad); break;
-          case 7: bb_dft_wide_kernel<7><<<grid, 256, sh, st>>>(m, cw, p, tw, bad); break;
-          case 8: bb_dft_wide_kernel<8><<<grid, 256, sh, st>>>(m, cw, p, tw, bad); break;
-          default: return cudaErrorInvalidValue;
+    } else if (p.lu + p.lc == 5) {  // a warp's lanes are one row run: registers take 4 layers per round trip
+      bb_dft_reg_kernel<<<grid, 256, sh, st>>>(m, cw, p, tw, bad);
+    } else {
+      bb_dft_pass_kernel<<<grid, pp.threads, sh, st>>>(m, cw, p, tw, bad);
+    }
+    count_launch();
+    return cudaGetLastError();
+  };
+
+  // A pass whose tiles stay inside one input slice (rows 2^(s_lo + T) apart
+  // at most, and a whole number of tile rows per slice) runs slice by slice:
+  // its k-th part (blocks in order, chunk fastest) covers exactly slice k's
+  // codeword rows, so it starts as soon as that slice and the slice's earlier
+  // stages are done.  The leading passes that qualify, and the generic code's
+  // stage 0, run per slice; the others after the last slice.
+  int slog = 0;
+  while ((1 << slog) < slices) ++slog;
+  const bool pow2 = (1 << slog) == slices;
+  int npre = 0;
+  if (slices > 1 && pow2)
+    while (npre < npass && plan[npre].p.s_lo + plan[npre].p.T + slog <= L) ++npre;
+
+  // generic stage 0: g_0[i][j] = i^j (generic.rs:51-54), times R^2, for the rows i < k_0
+  const size_t rows = (size_t)1 << L, part = rows / (size_t)slices;
+  const size_t k0 = (size_t)1 << log2_k0, n0 = (size_t)1 << log2_n0;
+  const bool fast = generic && log2_k0 <= 4 && part % n0 == 0;
+  BbG0 g0;
+  if (fast)
+    for (size_t i = 0; i < k0; ++i) {
+      const uint32_t im = bb::to_mont((uint32_t)i);
+      uint32_t pw = bb::MONT_ONE;  // i^j R
+      for (size_t j = 0; j < k0; ++j) {
+        g0.g[i * k0 + j] = bb::to_mont(pw);
+        pw = bb::mul(pw, im);
+      }
+    }
+  for (int k = 0; k < slices; ++k) {
+    cudaError_t e = wait_slice(k);
+    if (e != cudaSuccess) return e;
+    if (generic) {
+      if (fast) {
+        const size_t nch = part / n0, c0 = (size_t)k * nch;
+        const unsigned grid = blocks_for(nch * w, 256);
+        switch (log2_k0) {
+          case 0: bb_stage0_fast_kernel<1><<<grid, 256, 0, st>>>(m, cw, c0, nch, (uint32_t)w, (int)n0, g0, bad); break;
+          case 1: bb_stage0_fast_kernel<2><<<grid, 256, 0, st>>>(m, cw, c0, nch, (uint32_t)w, (int)n0, g0, bad); break;
+          case 2: bb_stage0_fast_kernel<4><<<grid, 256, 0, st>>>(m, cw, c0, nch, (uint32_t)w, (int)n0, g0, bad); break;
+          case 3: bb_stage0_fast_kernel<8><<<grid, 256, 0, st>>>(m, cw, c0, nch, (uint32_t)w, (int)n0, g0, bad); break;
+          default: bb_stage0_fast_kernel<16><<<grid, 256, 0, st>>>(m, cw, c0, nch, (uint32_t)w, (int)n0, g0, bad); break;
         }
-      } else if (lu + lc == 5)  // a warp's lanes are one row run: registers take 4 layers per round trip
-        bb_dft_reg_kernel<<<grid, 256, words * sizeof(uint32_t), st>>>(m, cw, p, tw, bad);
-      else
-        bb_dft_pass_kernel<<<grid, threads, words * sizeof(uint32_t), st>>>(m, cw, p, tw, bad);
+      } else {
+        bb_stage0_kernel<<<blocks_for(part * w, 256), 256, 0, st>>>(m, cw, (size_t)k * part, part, (uint32_t)w,
+                                                                    log2_k0, log2_n0, bad);
+      }
       count_launch();
       e = cudaGetLastError();
       if (e != cudaSuccess) return e;
     }
-    lo += T;
+    for (int i = 0; i < npre; ++i) {
+      const size_t per = plan[i].blocks / (size_t)slices;
+      e = launch_pass(plan[i], per * (size_t)k, per);
+      if (e != cudaSuccess) return e;
+    }
+  }
+  for (int i = npre; i < npass; ++i) {
+    cudaError_t e = launch_pass(plan[i], 0, plan[i].blocks);
+    if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
 }
