@@ -786,8 +786,37 @@ def run_binary_wide(bg, torch, device, sizes=(16, 17, 18, 19), log_polys=8, reps
         rows.append([n, round(1e3 * tc, 2), round(1e3 * te, 2), round(1e3 * to, 2)])
         comm.free()
         release(pcs, dev)
+    # CPU: the oracle on all host threads at the smallest of these sizes, its proof
+    # compared with the GPU's, both timed on the same matrix
+    from oracle import oracle as O
+
+    n_cpu = sizes[0]
+    O.set_threads(os.cpu_count() or 1)
+    pcs = bg.Basefold.setup(bg.BasefoldConfig(bg.BinaryReedSolomonCode(128, 1, n_cpu)), device=device)
+    data = bg.rand.random_elems((w << n_cpu) + n_cpu, 40 + n_cpu)
+    evals, point = data[: w << n_cpu], data[w << n_cpu:]
+    t = time.perf_counter()
+    root = O.commit(n_cpu, 1, evals, width=w)
+    cpu_commit = time.perf_counter() - t
+    _, values, blob = O.harness_prepare(n_cpu, 1, evals, point, width=w)
+    t = time.perf_counter()
+    cpu_proof = O.open_proof(n_cpu, 1, evals, point, values, blob, width=w)
+    cpu_open = time.perf_counter() - t - cpu_commit  # the oracle's open recommits first
+    dev = torch.from_numpy(evals).to(f"cuda:{device}")
+    comm = pcs.commit_device(dev.data_ptr(), width=w, keep=dev)
+    assert comm.root == root
+    gpu_proof = pcs.open(comm, [bg.PolyEvals(values, point)], bg.GenericChallenger.from_state(blob))
+    assert gpu_proof == cpu_proof
+    comm.free()
+    release(pcs, dev)
+    gpu = rows[0]
     return {"workload": f"the reference's binary benches: a 2^log_n x {w} Polyval matrix, blowup 2",
-            "cols": ["log_n", "commit_ms", "eval_ms", "open_ms"], "rows": rows}
+            "cols": ["log_n", "commit_ms", "eval_ms", "open_ms"], "rows": rows,
+            "cpu_baseline": {"kind": "port", "cores": os.cpu_count() or 1,
+                             "sample": f"oracle (C++ restatement, all host threads) at 2^{n_cpu} x {w}; "
+                                       "proof byte-identical to the GPU's",
+                             "commit_ms": round(1e3 * cpu_commit, 1), "open_ms": round(1e3 * cpu_open, 1),
+                             "gpu_commit_ms": gpu[1], "gpu_open_ms": gpu[3]}}
 
 
 def served_cpu_reference(log2_c, size_range):
