@@ -151,9 +151,9 @@ int load_points(const uint8_t* bytes, size_t n, std::vector<E>& out, const char*
 
 // Device eq table of x (2^|x| extension entries) in `ev`.
 int eq_table_device(bf_bb_pcs* p, const std::vector<E>& x, uint32_t* ev) {
-  const bb::E5 one = bb::e_from(bb::MONT_ONE);
-  CU(cudaMemcpyAsync(ev, &one, sizeof(one), cudaMemcpyHostToDevice, p->stream));
-  for (size_t i = 0; i < x.size(); ++i) CU(bf::bb_launch_eq_expand(ev, (size_t)1 << i, bbh::to_dev(x[i]), p->stream));
+  std::vector<bb::E5> xd(x.size());
+  for (size_t i = 0; i < x.size(); ++i) xd[i] = bbh::to_dev(x[i]);
+  CU(bf::bb_launch_eq_table(ev, xd.data(), (int)xd.size(), p->stream));
   return BF_OK;
 }
 

@@ -56,8 +56,10 @@ cudaError_t bb_launch_combine(const uint32_t* src, size_t rows, size_t w, const 
 // canonical sums, reduced by the caller).
 cudaError_t bb_launch_eval_cols(const uint32_t* eq, const uint32_t* data, size_t rows, size_t w,
                                 unsigned long long* acc, cudaStream_t st);
-// ev[h + k] = ev[k] x; ev[k] -= ev[h + k] for k < h.
-cudaError_t bb_launch_eq_expand(uint32_t* ev, size_t h, const bb::E5& x, cudaStream_t st);
+// The eq table of the n coordinates x (Montgomery, n <= kBbMaxRounds): entry b
+// is the product of x_i (bit i of b set) or 1 - x_i, as MultiPoly::eq builds
+// it (p3/src/poly/multilinear.rs:41-64, 216-222).
+cudaError_t bb_launch_eq_table(uint32_t* ev, const bb::E5* x, int n, cudaStream_t st);
 // acc[k] += coefficient k of sum_{b < n} heq[b] * poly[b]; poly is canonical
 // base-field data when `base` (canonical sums), else extension (Montgomery sums).
 cudaError_t bb_launch_dot(const uint32_t* heq, const uint32_t* poly, int base, size_t n, unsigned long long* acc,

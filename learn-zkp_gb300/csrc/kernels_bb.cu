@@ -714,13 +714,41 @@ __global__ void __launch_bounds__(256) bb_eval_cols_kernel(const uint32_t* __res
 }
 
 // ---- multilinear evaluation and the sumcheck side -----------------------------
-// eq_expand (p3/src/poly/multilinear.rs:216-222): hi = lo x; lo -= hi.
-__global__ void bb_eq_expand_kernel(uint32_t* ev, size_t h, E5 x) {
-  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < h; k += (size_t)gridDim.x * blockDim.x) {
-    const E5 lo = ld_e5(ev, k);
-    const E5 hv = bb::e_mul(lo, x);
-    st_e5(ev, h + k, hv);
-    st_e5(ev, k, bb::e_sub(lo, hv));
+// MultiPoly::eq (p3/src/poly/multilinear.rs:41-64) expands the table level by
+// level with eq_expand (:216-222): hi = lo x_i; lo -= hi.  Here the whole table
+// is one launch: entry b is the product over i of x_i (bit i of b set) or
+// 1 - x_i, the same field value, since products do not depend on their
+// order.  A thread takes 2^kEqLow
+// consecutive entries: the product of their common high-bit factors, then the
+// expansion of the low bits in registers (one product and one subtraction
+// per new entry).
+constexpr int kEqLow = 3;
+struct BbEqFactors {
+  E5 x[kBbMaxRounds], omx[kBbMaxRounds];  // x_i and 1 - x_i (Montgomery)
+};
+__global__ void __launch_bounds__(256) bb_eq_table_kernel(uint32_t* ev, int n, const __grid_constant__ BbEqFactors f) {
+  const int k = n < kEqLow ? n : kEqLow;
+  const size_t groups = (size_t)1 << (n - k);
+  for (size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x; g < groups; g += (size_t)gridDim.x * blockDim.x) {
+    E5 v[1 << kEqLow];
+    E5 pre = bb::e_from(bb::MONT_ONE);
+    for (int i = k; i < n; ++i) pre = bb::e_mul(pre, ((g >> (i - k)) & 1) ? f.x[i] : f.omx[i]);
+    v[0] = pre;
+#pragma unroll
+    for (int i = 0; i < kEqLow; ++i) {
+      if (i >= k) break;
+#pragma unroll
+      for (int j = 0; j < (1 << i); ++j) {
+        const E5 hv = bb::e_mul(v[j], f.x[i]);
+        v[(1 << i) + j] = hv;
+        v[j] = bb::e_sub(v[j], hv);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < (1 << kEqLow); ++j) {
+      if (j >= (1 << k)) break;
+      st_e5(ev, (g << k) + j, v[j]);
+    }
   }
 }
 
@@ -1330,8 +1358,16 @@ cudaError_t bb_launch_eval_cols(const uint32_t* eq, const uint32_t* data, size_t
   return cudaGetLastError();
 }
 
-cudaError_t bb_launch_eq_expand(uint32_t* ev, size_t h, const E5& x, cudaStream_t st) {
-  bb_eq_expand_kernel<<<blocks_for(h, 256), 256, 0, st>>>(ev, h, x);
+cudaError_t bb_launch_eq_table(uint32_t* ev, const bb::E5* x, int n, cudaStream_t st) {
+  if (n < 0 || n > kBbMaxRounds) return cudaErrorInvalidValue;
+  BbEqFactors f;
+  const bb::E5 one = bb::e_from(bb::MONT_ONE);
+  for (int i = 0; i < n; ++i) {
+    f.x[i] = x[i];
+    f.omx[i] = bb::e_sub(one, x[i]);
+  }
+  const size_t groups = (size_t)1 << (n - (n < kEqLow ? n : kEqLow));
+  bb_eq_table_kernel<<<blocks_for(groups, 256), 256, 0, st>>>(ev, n, f);
   count_launch();
   return cudaGetLastError();
 }
