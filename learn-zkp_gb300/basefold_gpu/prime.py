@@ -211,7 +211,13 @@ class BabyBearBasefold:
         if len(evals) > 1:
             raise ValueError("one evaluation point only (basefold.rs:143-144)")
         n_evals = len(evals)
-        out = np.empty(max(self.proof_size(comm.width, n_evals), 1), dtype=np.uint8)
+        size = max(self.proof_size(comm.width, n_evals), 1)
+        # one output buffer per object, reused: its pages are already mapped
+        # (a fresh multi-MB array faults every page in while the proof is
+        # written); the proof is returned as a copy
+        out = getattr(self, "_proof_buf", None)
+        if out is None or out.size < size:
+            out = self._proof_buf = np.empty(size, dtype=np.uint8)
         ln = C.c_size_t()
         if n_evals:
             pt, vals = self._point(evals[0].point), _ext(evals[0].values, comm.width)

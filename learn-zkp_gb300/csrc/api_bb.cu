@@ -551,10 +551,11 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
     std::memcpy(t.out, tr.out.data(), t.out_len);
     t.outer = bbh::to_dev(claim);
     bf::BbRoundConsts c{};
+    const std::vector<E> cf = es.correcting_factors();
     for (int k = 0; k < nv; ++k) {
       c.r[k] = bbh::to_dev(r[k]);
       c.r_inv[k] = bbh::to_dev(es.r_inv[k]);
-      c.cf[k] = bbh::to_dev(es.correcting_factor((size_t)k));
+      c.cf[k] = bbh::to_dev(cf[k]);
     }
     std::memcpy(p->pin.p, &t, sizeof(t));
     std::memcpy(p->pin.b() + sizeof(t), &c, sizeof(c));

@@ -95,6 +95,26 @@ inline E einv(const E& a) {  // a != 0
   return escale(prod, finv(norm));
 }
 
+// Inverses of every v[k] with one field inversion (prefix products, then
+// back-substitution); false when some v[k] is 0.
+inline bool batch_einv(const std::vector<E>& v, std::vector<E>& out) {
+  out.assign(v.size(), E::one());
+  if (v.empty()) return true;
+  std::vector<E> pre(v.size());
+  E acc = E::one();
+  for (size_t k = 0; k < v.size(); ++k) {
+    if (v[k].is_zero()) return false;
+    pre[k] = acc;  // product of v[0 .. k)
+    acc = emul(acc, v[k]);
+  }
+  E inv = einv(acc);  // (v[0] .. v[k])^-1 as k runs down
+  for (size_t k = v.size(); k-- > 0;) {
+    out[k] = emul(inv, pre[k]);
+    inv = emul(inv, v[k]);
+  }
+  return true;
+}
+
 inline E load(const uint8_t* p) {
   E e;
   std::memcpy(e.c, p, 20);
@@ -212,23 +232,20 @@ struct EvalScalars {
   // false when a coordinate is 0, or 1 below the last (their inverses are taken)
   bool init(const std::vector<E>& point) {
     r = point;
-    r_inv.clear();
-    one_minus_r_inv.clear();
-    for (const E& x : r) {
-      if (x.is_zero()) return false;
-      r_inv.push_back(einv(x));
-    }
-    for (size_t k = 0; k + 1 < r.size(); ++k) {
-      const E d = esub(E::one(), r[k]);
-      if (d.is_zero()) return false;
-      one_minus_r_inv.push_back(einv(d));
-    }
+    std::vector<E> v = r, inv;  // r_k for every k, then 1 - r_k for k < n - 1
+    for (size_t k = 0; k + 1 < r.size(); ++k) v.push_back(esub(E::one(), r[k]));
+    if (!batch_einv(v, inv)) return false;
+    r_inv.assign(inv.begin(), inv.begin() + r.size());
+    one_minus_r_inv.assign(inv.begin() + r.size(), inv.end());
     return true;
   }
-  E correcting_factor(size_t round) const {  // eval_impr.rs:83-90
-    E p = E::one();
-    for (size_t k = round; k < one_minus_r_inv.size(); ++k) p = emul(p, one_minus_r_inv[k]);
-    return p;
+  // correcting factor of every round (eval_impr.rs:83-90): round k's is the
+  // product of (1 - r_j)^-1 over j >= k, so one backward pass of suffix
+  // products gives them all (1 past the last factor)
+  std::vector<E> correcting_factors() const {
+    std::vector<E> cf(r.size(), E::one());
+    for (size_t k = one_minus_r_inv.size(); k-- > 0;) cf[k] = emul(one_minus_r_inv[k], cf[k + 1]);
+    return cf;
   }
 };
 
