@@ -105,6 +105,9 @@ int bf_commit(bf_pcs* pcs, const uint8_t* evals, size_t width, bf_commitment** o
 /* Same, with `d_evals` already in device memory.  The commitment keeps a
  * reference to it (no copy): the buffer must outlive the commitment. */
 int bf_commit_device(bf_pcs* pcs, const void* d_evals, size_t width, bf_commitment** out, uint8_t root[32]);
+/* The commitment's device buffers return, in stream order, to a memory pool
+ * owned by its pcs, which keeps them for the next commitments until the pcs
+ * itself is freed (no cudaMalloc or cudaFree per commit). */
 void bf_commitment_free(bf_commitment* comm);
 /* AsRef<Commitment> of BasefoldCommitmentData (basefold.rs:37-47). */
 int bf_commitment_root(const bf_commitment* comm, uint8_t root[32]);
