@@ -160,6 +160,10 @@ def test_prime_bench_shape_2_19_x_256_matches_oracle(built_lib, generic):
     comm = pcs.commit_device(dev.data_ptr(), w, keep=dev)
     root, values, blob = O.bb_harness_prepare(n, log2_c, data, point, **kw)
     assert comm.root == root
+    # from host memory: copied in slices, the stages inside a slice run per slice
+    host_comm = pcs.commit(data)
+    assert host_comm.root == root
+    host_comm.free()
     got = pcs.eval(comm, point)
     assert np.array_equal(got, values)
     ev = [prime.PrimePolyEvals(got, point)]
