@@ -36,6 +36,10 @@ struct bf_bb_pcs {
   cudaStream_t aux = nullptr;
   cudaEvent_t ev_fork = nullptr;
   cudaEvent_t slice_ev[kH2DSlices] = {};
+  // bf_bb_open runs each round's sums and fix on `aux` beside the tree and the
+  // fold: ev_dot orders a round's sums before its transcript step, ev_x the
+  // challenge before the fix, ev_join `aux` back into the main stream
+  cudaEvent_t ev_dot = nullptr, ev_x = nullptr, ev_join = nullptr;
   DevBuf tw;    // butterfly factors: layer s at 2^s - 1, 2^s of them (Shoup pairs, uint2)
   DevBuf tinv;  // fold constants: round i at n_0 (2^i - 1), (2 t_i[j])^-1 for j < n_i (Montgomery)
   DevBuf small;  // 4 KB: the canonical flag, sums, roots
@@ -96,6 +100,8 @@ struct bf_bb_pcs {
       if (own_stream && stream) cudaStreamDestroy(stream);
       if (aux) cudaStreamDestroy(aux);
       if (ev_fork) cudaEventDestroy(ev_fork);
+      for (cudaEvent_t e : {ev_dot, ev_x, ev_join})
+        if (e) cudaEventDestroy(e);
       for (cudaEvent_t e : slice_ev)
         if (e) cudaEventDestroy(e);
     }
@@ -235,6 +241,7 @@ static int bb_setup(int device, int lambda, int log2_c, int log2_k0, int num_var
   }
   CU(cudaStreamCreateWithFlags(&p->aux, cudaStreamNonBlocking));
   CU(cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming));
+  for (cudaEvent_t* e : {&p->ev_dot, &p->ev_x, &p->ev_join}) CU(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
   for (cudaEvent_t& e : p->slice_ev) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   CU(p->tw.alloc(8 * p->n_d()));
   CU(p->tinv.alloc(4 * p->n0() * (((size_t)1 << p->d) - 1) + 4));
@@ -561,6 +568,21 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
     std::memcpy(p->pin.b() + sizeof(t), &c, sizeof(c));
     CU(cudaMemcpyAsync(tdev, p->pin.p, tsz, cudaMemcpyHostToDevice, st));
   }
+  // A round's sums need only the previous fix and its fix only the round's
+  // challenge, so both run on `aux` beside the round's tree and fold: the
+  // main stream's chain per round is tree, transcript step, fold.
+  struct AuxJoin {  // joins `aux` back into the main stream on every exit
+    bf_bb_pcs* p;
+    cudaStream_t st;
+    bool active = false;
+    ~AuxJoin() {
+      if (active && cudaEventRecord(p->ev_join, p->aux) == cudaSuccess) cudaStreamWaitEvent(st, p->ev_join, 0);
+    }
+  } join{p, st};
+  cudaStream_t sa = p->aux;
+  CU(cudaEventRecord(p->ev_fork, st));  // the eq table, the round-0 poly and the transcript state
+  CU(cudaStreamWaitEvent(sa, p->ev_fork, 0));
+  join.active = true;
   size_t fold_off = 0, tree_off = 0;
   for (int k = 0; k < d; ++k) {
     const int i = d - 1 - k, li = p->log2_n0() + i;
@@ -572,13 +594,17 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
     const int base_k = k == 0 && base_round;
     if (k == 0) CU(bf::bb_launch_leaves_pairs(pi, base_k, tree, ni, li, st));  // later rounds: made by the fold
     CU(bf::launch_tree(tree, ni, st, root_dev, bf::Tune()));
-    CU(cudaMemsetAsync(acc, 0, 40, st));
-    CU(bf::bb_launch_dot(heq, poly, base_k, (size_t)1 << ri, acc, st));
+    CU(cudaMemsetAsync(acc, 0, 40, sa));
+    CU(bf::bb_launch_dot(heq, poly, base_k, (size_t)1 << ri, acc, sa));
+    CU(cudaEventRecord(p->ev_dot, sa));
+    CU(cudaStreamWaitEvent(st, p->ev_dot, 0));
     uint32_t* x_k = xs_dev + 5 * (size_t)k;
     CU(bf::bb_launch_transcript_round(tdev, cdev, ri, nv, root_dev, acc, base_k, x_k, rec_dev + 72 * (size_t)k, st));
+    CU(cudaEventRecord(p->ev_x, st));
+    CU(cudaStreamWaitEvent(sa, p->ev_x, 0));
     const bb::E5 unused{};
-    uint32_t* fixed = fixbuf[k & 1];
-    CU(bf::bb_launch_fix(poly, base_k, fixed, (size_t)1 << ri, unused, st, x_k));
+    uint32_t* fixed = fixbuf[k & 1];  // the fix two rounds back and the sums since have read it (stream order)
+    CU(bf::bb_launch_fix(poly, base_k, fixed, (size_t)1 << ri, unused, sa, x_k));
     poly = fixed;
     bf::BbFold fp;
     fp.w = pi;
@@ -594,6 +620,9 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
     fold_off += ni;
     tree_off += 2 * ni;
   }
+  CU(cudaEventRecord(p->ev_join, sa));  // the last fix, before the final poly is read
+  CU(cudaStreamWaitEvent(st, p->ev_join, 0));
+  join.active = false;
   // final_poly (into_ext_poly): the k_0 evaluations left after d fixes, observed
   std::vector<E> fin(k0);
   {
