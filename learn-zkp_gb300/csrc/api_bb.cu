@@ -599,7 +599,8 @@ int bf_bb_open(bf_bb_pcs* p, const bf_bb_commitment* cm, const uint8_t* point, c
     CU(cudaEventRecord(p->ev_dot, sa));
     CU(cudaStreamWaitEvent(st, p->ev_dot, 0));
     uint32_t* x_k = xs_dev + 5 * (size_t)k;
-    CU(bf::bb_launch_transcript_round(tdev, cdev, ri, nv, root_dev, acc, base_k, x_k, rec_dev + 72 * (size_t)k, st));
+    CU(bf::bb_launch_transcript_round(tdev, cdev, k, ri, nv, root_dev, acc, base_k, x_k, rec_dev + 72 * (size_t)k,
+                                      st));
     CU(cudaEventRecord(p->ev_x, st));
     CU(cudaStreamWaitEvent(sa, p->ev_x, 0));
     const bb::E5 unused{};

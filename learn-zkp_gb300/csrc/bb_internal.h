@@ -104,12 +104,13 @@ struct BbTranscript {
 struct BbRoundConsts {
   bb::E5 r[kBbMaxRounds], r_inv[kBbMaxRounds], cf[kBbMaxRounds];
 };
-// One folding-sumcheck round's transcript: observe the round's folded-codeword
-// root (interleaved digest at root_dev), compute the round polynomial from the
-// GPU sum (Montgomery sums, or canonical ones when `canonical`), observe its
-// compressed form, sample the challenge into x_out (Montgomery) and record
-// the root and the compressed polynomial (72 canonical bytes) at rec.
-cudaError_t bb_launch_transcript_round(BbTranscript* t, const BbRoundConsts* c, int ri, int num_vars,
+// One folding-sumcheck round's transcript (k rounds done before it): observe
+// the round's folded-codeword root (interleaved digest at root_dev), compute
+// the round polynomial from the GPU sum (Montgomery sums, or canonical ones
+// when `canonical`), observe its compressed form, sample the challenge into
+// x_out (Montgomery) and record the root and the compressed polynomial (72
+// canonical bytes) at rec.
+cudaError_t bb_launch_transcript_round(BbTranscript* t, const BbRoundConsts* c, int k, int ri, int num_vars,
                                        const uint4* root_dev, const unsigned long long* sums, int canonical,
                                        uint32_t* x_out, uint8_t* rec, cudaStream_t st);
 

@@ -957,17 +957,35 @@ __device__ __forceinline__ E5 shfl_e5(const E5& e, int src) {
 
 // One folding-sumcheck round (basefold.rs:340-362 with sumcheck/src/lib.rs:81-103
 // and EvalImprProver's round polynomial, eval_impr.rs:41-58, 150-162), one warp.
-__global__ void __launch_bounds__(32) bb_transcript_round_kernel(BbTranscript* t, const BbRoundConsts* c, int ri,
-                                                                int num_vars, const uint4* root_dev,
+__global__ void __launch_bounds__(32) bb_transcript_round_kernel(BbTranscript* t, const BbRoundConsts* c, int k,
+                                                                int ri, int num_vars, const uint4* root_dev,
                                                                 const unsigned long long* sums, int canonical,
                                                                 uint32_t* x_out, uint8_t* rec) {
   __shared__ TrCtx ctx;
   __shared__ uint8_t msg[72];  // the root, then the compressed round polynomial (canonical bytes)
   const WarpKeccak wk;
   const int lane = wk.lane;
-  for (int q = lane; q < 256; q += 32) ctx.pend[q] = t->pend[q];
-  ctx.out[lane] = t->out[lane];
+  const bool last = ri + 1 == num_vars;
+  const int nf = last ? 0 : min(k, num_vars - ri - 1);  // k: rounds done
+  // Every global load first: none depends on another, so they are in flight
+  // together instead of one dependent round trip after another.
+  const uint32_t* pend_w = reinterpret_cast<const uint32_t*>(t->pend);
+  const uint32_t pw0 = pend_w[lane], pw1 = pend_w[lane + 32];
+  const uint8_t ob = t->out[lane];
+  uint2 a = lane < 25 ? t->A[lane] : make_uint2(0, 0);
+  E5 fx{}, fy{};  // the delta factor's x = r[ri+1+j] and y, the challenge sampled j+1 rounds ago
+  if (lane < nf) {
+    fx = c->r[ri + 1 + lane];
+    fy = t->xs[k - 1 - lane];
+  }
+  unsigned long long sv[5] = {0, 0, 0, 0, 0};
+  E5 sc{}, r{}, cf{}, rinv{};
   if (lane == 0) {
+    for (int q = 0; q < 5; ++q) sv[q] = sums[q];
+    sc = last ? t->outer : t->inner;
+    r = c->r[ri];
+    cf = c->cf[ri];
+    rinv = c->r_inv[ri];
     ctx.pend_len = (int)t->pend_len;
     ctx.out_len = (int)t->out_len;
     const Digest dg = digest_bytes(load_digest(root_dev, 0));
@@ -975,21 +993,18 @@ __global__ void __launch_bounds__(32) bb_transcript_round_kernel(BbTranscript* t
     for (int i = 0; i < 8; ++i)
       for (int b = 0; b < 4; ++b) msg[4 * i + b] = (uint8_t)(words[i] >> (8 * b));
   }
-  uint2 a = lane < 25 ? t->A[lane] : make_uint2(0, 0);
+  reinterpret_cast<uint32_t*>(ctx.pend)[lane] = pw0;
+  reinterpret_cast<uint32_t*>(ctx.pend)[lane + 32] = pw1;
+  ctx.out[lane] = ob;
   __syncwarp();
   a = tr_observe(wk, a, ctx, msg, 32);
   // delta: eq_eval(r[ri+1..], inner.r()) (multilinear.rs:224-229) as a product
-  // tree over the warp, factor j = 2 x y + 1 - x - y with x = r[ri+1+j] and y
-  // the challenge sampled j+1 rounds ago
-  const bool last = ri + 1 == num_vars;
+  // tree over the warp, factor j = 2 x y + 1 - x - y
   const E5 one = bb::e_from(bb::MONT_ONE);
-  const int k = (int)t->rounds;
-  const int nf = last ? 0 : min(k, num_vars - ri - 1);
   E5 f = one;
   if (lane < nf) {
-    const E5 x = c->r[ri + 1 + lane], y = t->xs[k - 1 - lane];
-    const E5 xy = bb::e_mul(x, y);
-    f = bb::e_sub(bb::e_sub(bb::e_add(bb::e_add(xy, xy), one), x), y);
+    const E5 xy = bb::e_mul(fx, fy);
+    f = bb::e_sub(bb::e_sub(bb::e_add(bb::e_add(xy, xy), one), fx), fy);
   }
   for (int o = 16; o > 0; o >>= 1) f = bb::e_mul(f, shfl_e5(f, lane ^ o));  // every lane: the product
   // the round polynomial from S = sum_b half_eq[b] poly[b] (lane 0)
@@ -997,13 +1012,12 @@ __global__ void __launch_bounds__(32) bb_transcript_round_kernel(BbTranscript* t
   if (lane == 0) {
     E5 S;
     for (int q = 0; q < 5; ++q) {
-      const uint32_t v = (uint32_t)(sums[q] % bb::P);
+      const uint32_t v = (uint32_t)(sv[q] % bb::P);
       S.c[q] = canonical ? bb::to_mont(v) : v;
     }
-    const E5 sc = last ? t->outer : t->inner;
-    const E5 r = c->r[ri], omr = bb::e_sub(one, r);
-    c0 = bb::e_mul(c->cf[ri], S);
-    const E5 e1 = bb::e_mul(bb::e_sub(sc, bb::e_mul(omr, c0)), c->r_inv[ri]);
+    const E5 omr = bb::e_sub(one, r);
+    c0 = bb::e_mul(cf, S);
+    const E5 e1 = bb::e_mul(bb::e_sub(sc, bb::e_mul(omr, c0)), rinv);
     c1 = bb::e_sub(e1, c0);
     const E5 d0 = bb::e_mul(f, omr), d1 = bb::e_mul(f, bb::e_sub(r, omr));
     rp0 = bb::e_mul(c0, d0);
@@ -1025,15 +1039,17 @@ __global__ void __launch_bounds__(32) bb_transcript_round_kernel(BbTranscript* t
     t->pend_len = (uint32_t)ctx.pend_len;
     t->out_len = (uint32_t)ctx.out_len;
   }
-  for (int q = lane; q < 256; q += 32) t->pend[q] = ctx.pend[q];
+  uint32_t* pend_out = reinterpret_cast<uint32_t*>(t->pend);
+  pend_out[lane] = reinterpret_cast<const uint32_t*>(ctx.pend)[lane];
+  pend_out[lane + 32] = reinterpret_cast<const uint32_t*>(ctx.pend)[lane + 32];
   t->out[lane] = ctx.out[lane];
   if (lane < 25) t->A[lane] = a;
 }
 
-cudaError_t bb_launch_transcript_round(BbTranscript* t, const BbRoundConsts* c, int ri, int num_vars,
+cudaError_t bb_launch_transcript_round(BbTranscript* t, const BbRoundConsts* c, int k, int ri, int num_vars,
                                        const uint4* root_dev, const unsigned long long* sums, int canonical,
                                        uint32_t* x_out, uint8_t* rec, cudaStream_t st) {
-  bb_transcript_round_kernel<<<1, 32, 0, st>>>(t, c, ri, num_vars, root_dev, sums, canonical, x_out, rec);
+  bb_transcript_round_kernel<<<1, 32, 0, st>>>(t, c, k, ri, num_vars, root_dev, sums, canonical, x_out, rec);
   count_launch();
   return cudaGetLastError();
 }
