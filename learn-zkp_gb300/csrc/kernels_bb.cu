@@ -573,8 +573,9 @@ __global__ void __launch_bounds__(128) bb_leaves_one_kernel(const uint32_t* __re
 
 // Any width: keccak256 of the row's 4w bytes (GenericHasher over the row's
 // bincode, p3/src/symmetric.rs:11-25): canonical words staged by a warp per
-// 32 rows (keccak_rows_warp).
-__global__ void __launch_bounds__(128) bb_leaves_rows_kernel(const uint32_t* __restrict__ cw,
+// 32 rows (keccak_rows_warp).  Five blocks per SM (96 registers, a few spilled
+// words) measured about 1% faster than four at 128 registers.
+__global__ void __launch_bounds__(128, 5) bb_leaves_rows_kernel(const uint32_t* __restrict__ cw,
                                                             uint4* __restrict__ leaves, size_t rows, uint32_t w,
                                                             int bits) {
   __shared__ uint32_t stage[4][32 * kStagePitch];
