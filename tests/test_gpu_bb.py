@@ -55,11 +55,14 @@ def test_commit_eval_open_match_oracle(built_lib, n, log2_c, w):
     _check(n, log2_c, w, 1000 + 31 * n + 7 * log2_c + w)
 
 
-@pytest.mark.parametrize("n,log2_c,w", [(14, 1, 1), (16, 2, 1), (20, 1, 1), (12, 1, 256), (14, 1, 256), (13, 2, 100)])
+@pytest.mark.parametrize("n,log2_c,w", [(14, 1, 1), (16, 2, 1), (20, 1, 1), (12, 1, 256), (14, 1, 256), (13, 2, 100),
+                                        (16, 1, 100)])
 def test_larger_sizes_match_oracle(built_lib, n, log2_c, w):
     """Sizes where the DFT runs several passes (tiles of up to 2^12 rows for
     one column, 2^8 rows x 32 columns otherwise) and the trees several
-    launch kinds."""
+    launch kinds; from 2^16 rows the host commit copies in slices and runs
+    the passes inside a slice per slice (width 100: four 32-column chunks,
+    the last one partial)."""
     _check(n, log2_c, w, 77 + n + w)
 
 
@@ -134,7 +137,7 @@ def test_generic_code_matches_oracle(built_lib, n, log2_c, log2_k0, w):
 # 128 (the general kernel), and a 2^17-row host commit whose stage 0 runs per
 # input slice.
 @pytest.mark.parametrize("n,log2_c,log2_k0,w", [(6, 1, 4, 3), (7, 2, 4, 2), (8, 3, 4, 1), (6, 0, 5, 2),
-                                                (9, 2, 5, 1), (17, 1, 3, 4)])
+                                                (9, 2, 5, 1), (17, 1, 3, 4), (16, 1, 3, 100)])
 def test_generic_code_stage0_shapes(built_lib, n, log2_c, log2_k0, w):
     _check_generic(n, log2_c, log2_k0, w, 3500 + 17 * n + 5 * log2_c + log2_k0 + w)
 
