@@ -1358,15 +1358,17 @@ cudaError_t bb_launch_eval_cols(const uint32_t* eq, const uint32_t* data, size_t
                                 unsigned long long* acc, cudaStream_t st) {
   size_t bx = (rows + 63) / 64;  // at least 8 rows per warp
   const size_t by = (w + 31) / 32;
-  // one wave: as many blocks as the SMs hold at once, spread over the column groups
-  static const size_t resident = [] {
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bb_eval_cols_kernel, 256, 0);
-    return (size_t)(sms > 0 ? sms : 152) * (size_t)(per_sm > 0 ? per_sm : 4);
+  // one wave: as many blocks as the SMs hold at once, spread over the column
+  // groups (blocks per SM depend on the kernel only; SMs on the current device)
+  static const int per_sm = [] {
+    int b = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, bb_eval_cols_kernel, 256, 0);
+    return b > 0 ? b : 4;
   }();
-  size_t cap = resident / by;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  size_t cap = (size_t)(sms > 0 ? sms : 152) * (size_t)per_sm / by;
   if (cap < 1) cap = 1;
   if (bx > cap) bx = cap;
   if (bx < 1) bx = 1;
